@@ -1,0 +1,408 @@
+"""Benchmark of the BUFF buff-simd hot path on GB300.
+
+Workload (single large column): 268,435,456 f64 values of a uniform-step random
+walk reflected into [-500, 500], rounded to 4 decimals (seeded, generated on the
+device), encoded at scale 10^4 -> 25-bit codes = 3 byte slices + 1 tail bit.
+
+One step = the query pair "range filter at 10% selectivity, then sum" over the
+resident column.  `value` = column rows answered per second by that pair (rows
+/ step time), max over ranks, times the number of ranks (replicas: each rank
+owns its own column; weak scaling).  Inputs (slice 0: 268 MB, full column:
+839 MB) are larger than the 129 MB L2, so no flush is needed between steps.
+
+`e2e` runs the same pair through the C ABI the way the reference is called
+(compress/buff_simd.rs:3361, split_double.rs:2127 take the encoded Vec<u8> by
+value): per step the host byte image is uploaded from pinned memory
+(buff_deserialize), filtered into a pinned host bitmap, summed into a host
+result.
+
+`--impl reference` times the CPU restatement of the reference algorithm (the
+oracle: progressive slice refinement + per-slice byte sums, the reference
+having no GPU path and no Rust toolchain here) on all host cores over a
+bounded sample of the same column.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+N_ROWS = 1 << 28
+SCALE = 10000
+SELECTIVITY = 0.10
+CPU_SAMPLE_ROWS = 1 << 25
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--rows", type=int, default=N_ROWS)
+    ap.add_argument("--no-ops", action="store_true", help="skip the per-op table")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def dist_init(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl"
+        try:
+            import torch
+
+            torch.cuda.set_device(local)
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary
+    (profiles/*.txt lines 'dram_bytes_per_launch <kernel> <bytes>')."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for fn in sorted(os.listdir(pdir)):
+        if not fn.endswith((".txt", ".md")):
+            continue
+        for line in open(os.path.join(pdir, fn)):
+            m = re.match(rf"\s*dram_bytes_per_launch\s+{kernel}\s+([0-9.eE+]+)", line)
+            if m:
+                return float(m.group(1))
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference_line(args, x_sample: np.ndarray, pred: float, threads: int, steps: int,
+                       warmup: int):
+    """Times the oracle's filter+sum (the reference algorithm) on host cores."""
+    from oracle import oracle as O
+
+    buf = O.encode(x_sample, SCALE)
+    for _ in range(warmup):
+        O.bench_filter_sum(buf, SCALE, pred, threads, 1)
+    t, cnt, s = O.bench_filter_sum(buf, SCALE, pred, threads, steps)
+    rows = x_sample.size
+    return t / steps, rows, cnt, s
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import torch
+
+    from buff_gb300.workloads import bounded_walk_torch
+
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    x = bounded_walk_torch(CPU_SAMPLE_ROWS, seed=2, device=dev).cpu().numpy()
+    pred = float(np.quantile(x[::64], 1.0 - SELECTIVITY))
+    threads = os.cpu_count() or 1
+    per_step, rows, cnt, s = cpu_reference_line(args, x, pred, threads, args.steps, args.warmup)
+    v = rows / per_step / 1e9
+    line = {
+        "impl": "reference", "metric": "filter+sum throughput (range filter 10% then sum)",
+        "value": v, "unit": "Gvalues/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": f"bounded_walk f64 scale 1e4, sample of {rows} rows of the "
+                               f"{N_ROWS}-row column", "rows": rows, "selectivity": SELECTIVITY},
+        "cpu_baseline": {"value": v, "unit": "Gvalues/s", "cores": threads, "kind": "port",
+                         "sample": f"{rows} rows, {args.steps} timed passes of filter+sum"},
+        "e2e": {"value": v, "unit": "Gvalues/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_op(fn, reps, stream):
+    import torch
+
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    fn()
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for _ in range(reps):
+        fn()
+    ev[1].record(stream)
+    ev[1].synchronize()
+    return ev[0].elapsed_time(ev[1]) / reps / 1e3
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+
+    from buff_gb300 import Column, capi
+    from buff_gb300.workloads import bounded_walk_torch
+
+    torch.cuda.set_device(local)
+    L = capi.lib()
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    n = args.rows
+    x = bounded_walk_torch(n, seed=2 + rank)
+    pred = float(torch.quantile(x[:: max(1, n >> 20)], 1.0 - SELECTIVITY).item())
+    torch.cuda.synchronize()
+    t0 = time.time()
+    col = Column.encode(x, SCALE, stream=stream)
+    torch.cuda.synchronize()
+    info = col.info
+    nw = (n + 31) // 32
+    words = torch.empty(nw, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+    parts = torch.zeros(9, dtype=torch.int64, device="cuda")
+    h = col.handle
+
+    def step():
+        capi.check(L.buff_range_filter(h, pred, words.data_ptr(), cnt.data_ptr(), sh))
+        capi.check(L.buff_sum_partials_async(h, parts.data_ptr(), sh))
+
+    # per-kernel events inside the timed region (on the launching stream)
+    ev_f0, ev_f1, ev_s1 = [], [], []
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = Clocks(local) if rank == 0 else None
+    launches0 = capi.kernel_launches()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(args.steps):
+        a, b, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        a.record(stream)
+        capi.check(L.buff_range_filter(h, pred, words.data_ptr(), cnt.data_ptr(), sh))
+        b.record(stream)
+        capi.check(L.buff_sum_partials_async(h, parts.data_ptr(), sh))
+        c2.record(stream)
+        ev_f0.append(a)
+        ev_f1.append(b)
+        ev_s1.append(c2)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    launches = capi.kernel_launches() - launches0
+    elapsed = start.elapsed_time(stop) / 1e3
+    clk = clocks.stop() if clocks else None
+    barrier(world)
+    elapsed = max_over_ranks(elapsed, world)
+    t_step = elapsed / args.steps
+    filt_s = statistics.median(a.elapsed_time(b) for a, b in zip(ev_f0, ev_f1)) / 1e3
+    sum_s = statistics.median(b.elapsed_time(c) for b, c in zip(ev_f1, ev_s1)) / 1e3
+    count = int(cnt.item())
+    host_parts = np.ascontiguousarray(parts.cpu().numpy().view(np.uint64))
+    res = capi.SumResult()
+    capi.check(L.buff_sum_finish(h, host_parts.ctypes.data, C.byref(res)))
+
+    peak, peak_kind = measured_peaks()
+    k, r = info.k, info.r
+    sum_bytes = k * n + (n * r + 7) // 8  # every slice + the packed tail
+    filt_bytes = n + 4 * nw  # slice 0 + bitmap (+ candidate sectors, counted by ncu)
+    roof_sum = sum_bytes / sum_s / 1e9
+    roof_filt = filt_bytes / filt_s / 1e9
+
+    # ---- e2e through the C ABI with host buffers --------------------------
+    img_len = info.serialized_bytes
+    img = torch.empty(img_len, dtype=torch.uint8, pin_memory=True)
+    col.serialize(out=img.numpy())
+    hwords = torch.empty(nw, dtype=torch.int32, pin_memory=True)
+    hcount = np.zeros(1, dtype=np.uint64)
+
+    def e2e_step():
+        hc = C.c_void_p()
+        capi.check(L.buff_deserialize(img.data_ptr(), img_len, SCALE, 0, sh, C.byref(hc)))
+        capi.check(L.buff_range_filter(hc, pred, hwords.data_ptr(), hcount.ctypes.data, sh))
+        sres = capi.SumResult()
+        capi.check(L.buff_sum(hc, C.byref(sres), sh))
+        capi.check(L.buff_col_free_async(hc, sh))
+        return sres
+
+    for _ in range(max(2, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_reps = max(3, min(args.steps, 10))
+    t1 = time.perf_counter()
+    for _ in range(e2e_reps):
+        sres = e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t1) / e2e_reps
+    assert int(hcount[0]) == count and sres.sum == res.sum
+
+    # ---- per-op table (the measured rows of the single-column config) -------
+    ops = {}
+    if not args.no_ops and rank == 0:
+        xs = x[:: max(1, n >> 20)]
+        for sel in (0.001, 0.01, 0.1, 0.5):
+            p = float(torch.quantile(xs, 1.0 - sel).item())
+            t = time_op(lambda: L.buff_range_filter(h, p, words.data_ptr(), cnt.data_ptr(), sh),
+                        10, stream)
+            ops[f"range_{sel:g}"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
+                                     "gb_s_alg": filt_bytes / t / 1e9}
+        peq = float(x[n // 3].item())
+        t = time_op(lambda: L.buff_equal_filter(h, peq, words.data_ptr(), cnt.data_ptr(), sh), 10,
+                    stream)
+        ops["equal"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "gb_s_alg": filt_bytes / t / 1e9}
+        t = time_op(lambda: L.buff_sum_partials_async(h, parts.data_ptr(), sh), 10, stream)
+        ops["sum"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "gb_s_alg": sum_bytes / t / 1e9}
+        mx = torch.zeros(1, dtype=torch.int64, device="cuda")
+        t = time_op(lambda: L.buff_max_async(h, mx.data_ptr(), sh), 10, stream)
+        ops["max"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "gb_s_alg": n / t / 1e9}
+        out = torch.empty(n, dtype=torch.float64, device="cuda")
+        t = time_op(lambda: L.buff_decode(h, out.data_ptr(), sh), 5, stream)
+        ops["decode_full"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
+                              "gb_s_alg": (sum_bytes + 8 * n) / t / 1e9}
+        for p in (1, 2, 4):
+            t = time_op(lambda: L.buff_decode_at_precision(h, p, out.data_ptr(), sh), 5, stream)
+            ops[f"decode_p{p}"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9}
+        del out
+
+        def enc():
+            c2 = Column.encode(x, SCALE, stream=stream)
+            c2.free()
+
+        t = time_op(enc, 3, stream)
+        ops["encode"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
+                         "gb_s_alg": (16 * n + sum_bytes) / t / 1e9}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        xs = x[:CPU_SAMPLE_ROWS].cpu().numpy()
+        per_step, rows, _, _ = cpu_reference_line(args, xs, pred, 1, 3, 1)
+        cpu = {"value": rows / per_step / 1e9, "unit": "Gvalues/s", "cores": 1, "kind": "port",
+               "sample": f"first {rows} rows of the column, 3 timed passes of filter+sum, "
+                         f"1 thread"}
+
+    if rank == 0:
+        tf = ncu_traffic("k_sum")
+        line = {
+            "metric": "filter+sum throughput (range filter 10% then sum)",
+            "value": world * n / t_step / 1e9, "unit": "Gvalues/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic",
+            "config": {"workload": "bounded_walk f64 [-500,500] 4 decimals, scale 1e4",
+                       "rows": n, "fixed_len": info.fixed_len, "slices": k, "tail_bits": r,
+                       "selectivity": SELECTIVITY, "count": count,
+                       "l2": "inputs larger than L2 (slice 0 268 MB, column 839 MB)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "kernel": "k_sum", "achieved": roof_sum, "peak": peak,
+                         "unit": "GB/s", "frac": roof_sum / peak, "peak_kind": peak_kind,
+                         "traffic": tf, "alg_bytes_per_launch": sum_bytes},
+            "roofline_filter": {"kernel": "k_filter", "achieved": roof_filt, "peak": peak,
+                                "unit": "GB/s", "frac": roof_filt / peak,
+                                "traffic": ncu_traffic("k_filter"),
+                                "alg_bytes_per_launch": filt_bytes},
+            "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Gvalues/s",
+                    "h2d_bytes_per_step": img_len, "d2h_bytes_per_step": 4 * nw + 8 + 72,
+                    "ms_per_step": e2e_s * 1e3},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+            "ops": ops,
+            "encode_once_s": time.time() - t0,
+        }
+        print(json.dumps(line), flush=True)
+    col.free()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

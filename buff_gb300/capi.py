@@ -1,0 +1,144 @@
+"""ctypes binding of the C ABI in ``include/buff_gpu.h``.
+
+The library is the in-tree ``buff_gb300/_build/libbuffgpu.so`` built by
+``buff_gb300.build``.  There is no fallback: if the library is missing or
+fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+OK, EINVAL, ENOMEM, ECUDA, EREFPANIC, ECORRUPT, ETIMEDOUT, ENOTSUP, EFULL = range(9)
+FLAG_INTENDED = 0x1
+
+EXPORTED = [
+    "buff_encode_f64", "buff_encode_f32", "buff_col_free", "buff_col_free_async",
+    "buff_col_get_info",
+    "buff_serialize", "buff_deserialize", "buff_decode", "buff_decode_at_precision",
+    "buff_range_filter", "buff_equal_filter", "buff_range_filter_with_slice",
+    "buff_equal_filter_with_slice", "buff_sum", "buff_sum_at_precision",
+    "buff_sum_partials_async", "buff_sum_finish", "buff_max", "buff_max_async",
+    "buff_status_string", "buff_last_cuda_error", "buff_kernel_launches",
+]
+
+
+class BuffError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = _status_string(status)
+        if status == ECUDA:
+            msg += f" (cudaError {lib().buff_last_cuda_error()})"
+        super().__init__(f"{what}: {msg}" if what else msg)
+
+
+class ReferencePanic(BuffError):
+    """The reference implementation panics on this input."""
+
+
+class ColInfo(C.Structure):
+    _fields_ = [("base", C.c_int64), ("n", C.c_uint32), ("ilen", C.c_uint32),
+                ("dlen", C.c_uint32), ("fixed_len", C.c_uint32), ("k", C.c_uint32),
+                ("r", C.c_uint32), ("scale", C.c_uint64), ("prec", C.c_int32),
+                ("precision_exp", C.c_int32), ("flags", C.c_uint32), ("reserved", C.c_uint32),
+                ("serialized_bytes", C.c_uint64), ("device_bytes", C.c_uint64)]
+
+
+class SumResult(C.Structure):
+    _fields_ = [("sum", C.c_double), ("exact", C.c_double), ("exact_num_lo", C.c_int64),
+                ("exact_num_hi", C.c_int64), ("partials", C.c_uint64 * 9),
+                ("n_partials", C.c_uint32), ("reserved", C.c_uint32)]
+
+    @property
+    def exact_num(self) -> int:
+        return (int(self.exact_num_hi) << 64) | (int(self.exact_num_lo) & ((1 << 64) - 1))
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = True):
+    """Loads libbuffgpu.so; builds it first when it is missing and nvcc exists."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing: run buff_gb300.build.build()")
+        _build.build()
+    L = C.CDLL(path)
+    P = C.c_void_p
+    pp = C.POINTER(C.c_void_p)
+    L.buff_encode_f64.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_encode_f32.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_col_free.argtypes = [P]
+    L.buff_col_free_async.argtypes = [P, P]
+    L.buff_col_get_info.argtypes = [P, C.POINTER(ColInfo)]
+    L.buff_serialize.argtypes = [P, P, C.c_uint64, C.POINTER(C.c_uint64), P]
+    L.buff_deserialize.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_decode.argtypes = [P, P, P]
+    L.buff_decode_at_precision.argtypes = [P, C.c_uint32, P, P]
+    for nm in ("buff_range_filter", "buff_equal_filter", "buff_range_filter_with_slice",
+               "buff_equal_filter_with_slice"):
+        getattr(L, nm).argtypes = [P, C.c_double, P, P, P]
+    L.buff_sum.argtypes = [P, C.POINTER(SumResult), P]
+    L.buff_sum_at_precision.argtypes = [P, C.c_uint32, P, P]
+    L.buff_sum_partials_async.argtypes = [P, P, P]
+    L.buff_sum_finish.argtypes = [P, P, C.POINTER(SumResult)]
+    L.buff_max.argtypes = [P, P, P, P, P, P]
+    L.buff_max_async.argtypes = [P, P, P]
+    L.buff_status_string.argtypes = [C.c_int]
+    L.buff_status_string.restype = C.c_char_p
+    L.buff_last_cuda_error.restype = C.c_int
+    L.buff_kernel_launches.restype = C.c_uint64
+    _lib = L
+    return L
+
+
+def _status_string(st: int) -> str:
+    try:
+        return lib().buff_status_string(st).decode()
+    except Exception:  # pragma: no cover - library unavailable
+        return f"status {st}"
+
+
+def check(st: int, what: str = ""):
+    if st == OK:
+        return
+    if st == EREFPANIC:
+        raise ReferencePanic(st, what)
+    raise BuffError(st, what)
+
+
+def ptr(x):
+    """Raw address of a numpy array, a torch tensor, an int or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+def stream_handle(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+def kernel_launches() -> int:
+    return int(lib().buff_kernel_launches())

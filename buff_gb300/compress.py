@@ -1,0 +1,251 @@
+"""Host-side mirror of the reference's ``SplitBDDoubleCompress`` buff-simd API.
+
+``SplitBDDoubleCompress(chunksize, batchsize, scale)`` keeps the reference's
+constructor (database/src/compress/split_double.rs:29-39) and method names
+(database/src/compress/buff_simd.rs); every method runs on the GPU through
+the C ABI of ``include/buff_gpu.h``.  Where the reference takes the encoded
+``Vec<u8>`` by value, these methods accept either a device-resident
+:class:`Column` or the reference byte image (``bytes``/``np.uint8``), which is
+uploaded once per call.  Where the reference only prints a result (filters,
+max), the methods return it.  Where the reference panics, they raise
+:class:`~buff_gb300.capi.ReferencePanic`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import capi
+from .capi import FLAG_INTENDED, check, lib, ptr, stream_handle
+
+
+@dataclass
+class FilterResult:
+    """A BitVec<u32>-shaped result: ceil(n/32) words, bit i%32 of word i/32."""
+
+    words: object  # np.ndarray[uint32] (host) or a device tensor
+    count: int
+    n: int
+
+    def rows(self) -> np.ndarray:
+        w = np.asarray(self.words if isinstance(self.words, np.ndarray) else self.words.cpu())
+        bits = np.unpackbits(w.astype("<u4").view(np.uint8), bitorder="little")
+        return np.nonzero(bits[: self.n])[0]
+
+
+@dataclass
+class MaxResult:
+    value: float
+    code: int
+    argmax_words: object
+    argmax_count: int
+
+
+class Column:
+    """A BUFF column resident in HBM (opaque ``buff_col*``)."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+
+    # -- lifetime -------------------------------------------------------
+    @classmethod
+    def encode(cls, values, scale: int, flags: int = 0, stream=None) -> "Column":
+        h = C.c_void_p()
+        if isinstance(values, np.ndarray):
+            arr = np.ascontiguousarray(values)
+            if arr.dtype == np.float32:
+                fn = lib().buff_encode_f32
+            else:
+                arr = np.ascontiguousarray(arr, dtype=np.float64)
+                fn = lib().buff_encode_f64
+            check(fn(ptr(arr), arr.size, scale, flags, stream_handle(stream), C.byref(h)), "encode")
+        else:  # torch tensor (host or device)
+            import torch
+
+            t = values.contiguous()
+            if t.dtype == torch.float32:
+                fn = lib().buff_encode_f32
+            elif t.dtype == torch.float64:
+                fn = lib().buff_encode_f64
+            else:
+                raise TypeError("values must be float32 or float64")
+            check(fn(ptr(t), t.numel(), scale, flags, stream_handle(stream), C.byref(h)), "encode")
+        return cls(h.value)
+
+    @classmethod
+    def deserialize(cls, data, scale: int, flags: int = 0, stream=None) -> "Column":
+        h = C.c_void_p()
+        if isinstance(data, (bytes, bytearray)):
+            arr = np.frombuffer(bytes(data), dtype=np.uint8)
+            n = arr.size
+        elif isinstance(data, np.ndarray):
+            arr = np.ascontiguousarray(data, dtype=np.uint8)
+            n = arr.size
+        else:
+            arr = data
+            n = data.numel()
+        check(lib().buff_deserialize(ptr(arr), n, scale, flags, stream_handle(stream),
+                                     C.byref(h)), "deserialize")
+        return cls(h.value)
+
+    def free(self):
+        if self._h and self._h.value:
+            lib().buff_col_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def info(self) -> capi.ColInfo:
+        inf = capi.ColInfo()
+        check(lib().buff_col_get_info(self._h, C.byref(inf)), "info")
+        return inf
+
+    @property
+    def n(self) -> int:
+        return self.info.n
+
+    # -- image ----------------------------------------------------------
+    def serialize(self, out=None, stream=None) -> bytes:
+        need = self.info.serialized_bytes
+        ln = C.c_uint64(0)
+        if out is None:
+            buf = np.empty(max(need, 1), dtype=np.uint8)
+            check(lib().buff_serialize(self._h, ptr(buf), need, C.byref(ln),
+                                       stream_handle(stream)), "serialize")
+            return buf[: ln.value].tobytes()
+        check(lib().buff_serialize(self._h, ptr(out), need, C.byref(ln), stream_handle(stream)),
+              "serialize")
+        return out
+
+    # -- queries --------------------------------------------------------
+    def decode(self, out=None, stream=None):
+        if out is None:
+            out = np.empty(max(self.n, 1), dtype=np.float64)
+            check(lib().buff_decode(self._h, ptr(out), stream_handle(stream)), "decode")
+            return out[: self.n]
+        check(lib().buff_decode(self._h, ptr(out), stream_handle(stream)), "decode")
+        return out
+
+    def decode_at_precision(self, precision: int, out=None, stream=None):
+        if out is None:
+            out = np.empty(max(self.n, 1), dtype=np.float64)
+            check(lib().buff_decode_at_precision(self._h, precision, ptr(out),
+                                                 stream_handle(stream)), "decode_at_precision")
+            return out[: self.n]
+        check(lib().buff_decode_at_precision(self._h, precision, ptr(out), stream_handle(stream)),
+              "decode_at_precision")
+        return out
+
+    def _filter(self, fn, pred: float, out=None, stream=None) -> FilterResult:
+        n = self.n
+        nw = (n + 31) // 32
+        cnt = np.zeros(1, dtype=np.uint64)
+        words = out if out is not None else np.zeros(max(nw, 1), dtype=np.uint32)
+        check(fn(self._h, float(pred), ptr(words), ptr(cnt), stream_handle(stream)), fn.__name__)
+        if out is None:
+            words = words[:nw]
+        return FilterResult(words, int(cnt[0]), n)
+
+    def range_filter(self, pred, out=None, stream=None):
+        return self._filter(lib().buff_range_filter, pred, out, stream)
+
+    def equal_filter(self, pred, out=None, stream=None):
+        return self._filter(lib().buff_equal_filter, pred, out, stream)
+
+    def range_filter_with_slice(self, pred, out=None, stream=None):
+        return self._filter(lib().buff_range_filter_with_slice, pred, out, stream)
+
+    def equal_filter_with_slice(self, pred, out=None, stream=None):
+        return self._filter(lib().buff_equal_filter_with_slice, pred, out, stream)
+
+    def sum(self, stream=None) -> capi.SumResult:
+        res = capi.SumResult()
+        check(lib().buff_sum(self._h, C.byref(res), stream_handle(stream)), "sum")
+        return res
+
+    def sum_at_precision(self, precision: int, stream=None) -> float:
+        v = C.c_double(0)
+        check(lib().buff_sum_at_precision(self._h, precision, C.byref(v), stream_handle(stream)),
+              "sum_at_precision")
+        return v.value
+
+    def max(self, argmax: bool = False, stream=None) -> MaxResult:
+        v = C.c_double(0)
+        code = C.c_uint64(0)
+        cnt = C.c_uint64(0)
+        words = np.zeros(max((self.n + 31) // 32, 1), dtype=np.uint32) if argmax else None
+        check(lib().buff_max(self._h, C.byref(v), C.byref(code), ptr(words),
+                             C.byref(cnt) if argmax else None, stream_handle(stream)), "max")
+        if words is not None:
+            words = words[: (self.n + 31) // 32]
+        return MaxResult(v.value, code.value, words, cnt.value)
+
+
+def _as_column(comp: "SplitBDDoubleCompress", data) -> Column:
+    if isinstance(data, Column):
+        return data
+    return Column.deserialize(data, comp.scale, comp.flags)
+
+
+class SplitBDDoubleCompress:
+    """GPU mirror of ``SplitBDDoubleCompress`` (compress/split_double.rs:29-39)."""
+
+    def __init__(self, chunksize: int, batchsize: int, scale: int, flags: int = 0):
+        self.chunksize = chunksize  # unused by the reference's buff-simd path
+        self.batchsize = batchsize  # unused by the reference's buff-simd path
+        self.scale = scale
+        self.flags = flags
+
+    # compress/buff_simd.rs:3116-3250
+    def buff_simd256_encode(self, values, stream=None) -> Column:
+        return Column.encode(values, self.scale, self.flags, stream)
+
+    # compress/buff_simd.rs:3252-3357
+    def buff_simd256_decode(self, data, stream=None):
+        return _as_column(self, data).decode(stream=stream)
+
+    # compress/buff_simd.rs:3361-3547 (the reference prints the count)
+    def buff_simd_range_filter(self, data, pred, stream=None) -> FilterResult:
+        return _as_column(self, data).range_filter(pred, stream=stream)
+
+    # compress/buff_simd.rs:3549-3733
+    def buff_simd_equal_filter(self, data, pred, stream=None) -> FilterResult:
+        return _as_column(self, data).equal_filter(pred, stream=stream)
+
+    # compress/buff_simd.rs:3736-3884
+    def buff_simd_range_filter_with_slice(self, data, pred, stream=None) -> FilterResult:
+        return _as_column(self, data).range_filter_with_slice(pred, stream=stream)
+
+    # compress/buff_simd.rs:3888-4025
+    def buff_simd_equal_filter_with_slice(self, data, pred, stream=None) -> FilterResult:
+        return _as_column(self, data).equal_filter_with_slice(pred, stream=stream)
+
+    # compress/split_double.rs:2127-2208 (on the unflipped slices)
+    def byte_fixed_sum(self, data, stream=None) -> float:
+        return _as_column(self, data).sum(stream=stream).sum
+
+    # compress/split_double.rs:3919-4105 (the reference prints the max)
+    def byte_fixed_max(self, data, stream=None) -> MaxResult:
+        return _as_column(self, data).max(argmax=True, stream=stream)
+
+    # compress/split_double.rs:1612-1893
+    def byte_residue_decode_with_precision(self, data, precision: int, stream=None):
+        return _as_column(self, data).decode_at_precision(precision, stream=stream)
+
+    # compress/split_double.rs:2409-2630
+    def byte_residue_sum_with_precision(self, data, precision: int, stream=None) -> float:
+        return _as_column(self, data).sum_at_precision(precision, stream=stream)
+
+
+__all__ = ["SplitBDDoubleCompress", "Column", "FilterResult", "MaxResult", "FLAG_INTENDED"]

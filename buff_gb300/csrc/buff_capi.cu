@@ -1,0 +1,783 @@
+// C ABI of the GB300 BUFF column codec (include/buff_gpu.h).
+//
+// Host side of every entry point: argument checks, the scalar steps the
+// reference runs once per column or query (precision, bit width, predicate
+// target, the f64 combine of the sum), staging of host buffers, and the
+// launch of the kernels in buff_kernels.cu.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
+
+#include "buff_internal.h"
+
+using buffk::EncStats;
+using buffk::FilterArgs;
+
+namespace {
+
+thread_local int g_last_cuda = 0;
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return BUFF_OK;
+  g_last_cuda = (int)e;
+  if (e == cudaErrorMemoryAllocation) return BUFF_ENOMEM;
+  return BUFF_ECUDA;
+}
+
+#define CK(expr)                              \
+  do {                                        \
+    cudaError_t _e = (expr);                  \
+    if (_e != cudaSuccess) {                  \
+      rc = cuda_status(_e);                   \
+      goto done;                              \
+    }                                         \
+  } while (0)
+
+inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// True when `p` can be dereferenced by the device (device or managed memory).
+bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// ---- scalar steps of the reference (host, once per column / query) ----
+
+// `(scale as f32).log10() as i32` (compress/buff_simd.rs:3127); scale 0 -> 0.
+int prec_of_scale(uint64_t scale) {
+  if (scale == 0) return 0;
+  float l = log10f((float)scale);
+  if (isnan(l)) return 0;
+  if (l >= 2147483647.0f) return 2147483647;
+  if (l <= -2147483648.0f) return -2147483647 - 1;
+  return (int)l;
+}
+
+// PRECISION_MAP (compress/mod.rs:29-46): decimals -> fractional bits.
+int dlen_of_prec(int prec) {
+  static const int kMap[16] = {-1, 5, 8, 11, 15, 18, 21, 25, 28, 31, 35, 38, 50, 10, 10, 10};
+  return (prec >= 1 && prec <= 15) ? kMap[prec] : -1;
+}
+
+// Exponent of get_precision_bound(prec) (methods/prec_double.rs:273-281,
+// PrecisionBound::new :28-33): the decimal string "0.<prec zeros>49".
+int precision_exp_of(int prec) {
+  char buf[64];
+  int p = 0;
+  buf[p++] = '0';
+  buf[p++] = '.';
+  for (int i = 0; i < prec && p < 60; ++i) buf[p++] = '0';
+  buf[p++] = '4';
+  buf[p++] = '9';
+  buf[p] = 0;
+  double d = strtod(buf, nullptr);
+  uint64_t u;
+  memcpy(&u, &d, 8);
+  return (int)((u >> 52) & 0x7FF) - 1023;
+}
+
+// PrecisionBound::fetch_fixed_aligned (methods/prec_double.rs:190-205).
+int64_t fetch_fixed_host(double v, int pexp, uint32_t dlen) {
+  uint64_t b;
+  memcpy(&b, &v, 8);
+  int exp = (int)((b >> 52) & 0x7FF) - 1023;
+  if (exp < pexp) return 0;
+  int sh = 63 - exp - (int)dlen;
+  uint64_t f = ((b << 11) | 0x8000000000000000ull) >> (sh & 63);
+  if (b >> 63) f = ~(f - 1);
+  return (int64_t)f;
+}
+
+void set_layout(buff_col *c, uint32_t fl) {
+  c->fixed_len = fl;
+  if (fl < 8) {
+    c->k = 0;
+    c->r = fl;
+  } else {
+    c->k = fl / 8;
+    c->r = fl % 8;
+  }
+}
+
+uint64_t serialized_size(const buff_col *c) {
+  return 20ull + (uint64_t)c->k * c->n + ((uint64_t)c->n * c->r + 7) / 8;
+}
+
+// Column storage comes from the device's stream-ordered pool, whose release
+// threshold is raised once per device so that freed columns stay cached for
+// the next encode/deserialize instead of going back to the driver.
+void init_pool(int device) {
+  static bool done[64] = {false};
+  if (device < 0 || device >= 64 || done[device]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  cudaGetLastError();
+  done[device] = true;
+}
+
+int alloc_col(buff_col *c, cudaStream_t s) {
+  init_pool(c->device);
+  const size_t rows = buffk::round_up(c->n ? c->n : 1, buffk::kRowChunk);
+  c->stride = rows;
+  c->tail_bytes = ((uint64_t)c->n * c->r + 7) / 8;
+  c->tail_alloc = rows / 8 * c->r + 64;
+  cudaError_t e = cudaSuccess;
+  if (c->k) e = cudaMallocAsync(reinterpret_cast<void **>(&c->slices), (size_t)c->k * c->stride, s);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaMallocAsync(reinterpret_cast<void **>(&c->tail), c->tail_alloc, s);
+  if (e != cudaSuccess) return cuda_status(e);
+  return BUFF_OK;
+}
+
+// Frees on `s` (stream-ordered after the work already queued there); with
+// s == nullptr the whole device is drained first, so any stream may still
+// have been reading the column.
+void free_col(buff_col *c, cudaStream_t s = nullptr, bool ordered = false) {
+  if (!c) return;
+  if (c->slices || c->tail) {
+    if (!ordered) cudaDeviceSynchronize();
+    if (c->slices) cudaFreeAsync(c->slices, s);
+    if (c->tail) cudaFreeAsync(c->tail, s);
+    if (!ordered) cudaStreamSynchronize(s);
+  }
+  delete c;
+}
+
+buff_col *new_col(uint64_t scale, uint32_t flags) {
+  buff_col *c = new (std::nothrow) buff_col;
+  if (!c) return nullptr;
+  memset(c, 0, sizeof(*c));
+  c->scale = scale;
+  c->flags = flags;
+  c->prec = prec_of_scale(scale);
+  c->precision_exp = precision_exp_of(c->prec);
+  cudaGetDevice(&c->device);
+  return c;
+}
+
+// Bits rebuilt by a precision-limited read (compress/split_double.rs:1642-1664).
+int precision_bits(const buff_col *c, uint32_t precision, uint32_t *total) {
+  const uint32_t ilen = c->ilen, dlen = c->dlen;
+  if (precision == 0) {
+    uint32_t rm = ilen;
+    if (ilen % 8 > 0) rm = (ilen / 8 + 1) * 8;
+    *total = rm;
+    return BUFF_OK;
+  }
+  const int bn = dlen_of_prec(precision > 15 ? -1 : (int)precision);
+  if (bn < 0) return BUFF_EREFPANIC;          // PRECISION_MAP.get(..).unwrap()
+  const uint32_t bits_needed = (uint32_t)bn;
+  if (!(dlen >= bits_needed)) return BUFF_EREFPANIC;  // assert!(dlen >= bits_needed)
+  uint32_t rm = ilen + bits_needed;
+  const uint32_t fixed_byte = (dlen + ilen) / 8;
+  uint32_t byte_needed = (ilen + bits_needed) / 8;
+  const uint32_t extra = (ilen + bits_needed) % 8;
+  if (byte_needed < fixed_byte && extra > 0) {
+    byte_needed += 1;
+    rm = byte_needed * 8;
+  }
+  *total = rm;
+  return BUFF_OK;
+}
+
+// The reference's f64 accumulation of byte_fixed_sum (split_double.rs:2141-2205)
+// over `total` leading bits, from the exact per-slice sums.
+double combine_sum(const buff_col *c, uint32_t total, const uint64_t *parts, bool intended) {
+  const int32_t ilen_i = (int32_t)c->ilen;
+  double sum_base = (double)c->n * (double)c->base;
+  sum_base = sum_base / ldexp(1.0, (int)c->dlen);
+  double sum = 0.0;
+  int32_t processed = 0;
+  uint32_t remain = total, slot = 0;
+  while (remain >= 8) {
+    remain -= 8;
+    processed += 8;
+    sum = sum + (double)parts[slot++] / ldexp(1.0, processed - ilen_i);
+    if (remain == 0 && !intended) return sum;  // no base term when nothing follows
+  }
+  if (remain > 0) {
+    processed += (int32_t)remain;
+    sum = sum + (double)parts[slot] / ldexp(1.0, processed - ilen_i);
+  }
+  sum += sum_base;
+  return sum;
+}
+
+// Device scratch for one call (stream-ordered pool allocation).
+template <typename T>
+cudaError_t scratch(T **p, size_t count, cudaStream_t s) {
+  return cudaMallocAsync(reinterpret_cast<void **>(p), count * sizeof(T) + 16, s);
+}
+
+// ---------------------------------------------------------------- encode
+
+template <typename T>
+int encode_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, cudaStream_t s,
+                buff_col **out) {
+  if (!out) return BUFF_EINVAL;
+  *out = nullptr;
+  if (n64 >= (1ull << 32)) return BUFF_EINVAL;  // the header stores n as u32
+  if (n64 > 0 && !values) return BUFF_EINVAL;
+  const uint32_t n = (uint32_t)n64;
+  const bool intended = flags & BUFF_FLAG_INTENDED;
+  const int prec = prec_of_scale(scale);
+  const int dl = dlen_of_prec(prec);
+  if (dl < 0) return BUFF_EREFPANIC;  // PRECISION_MAP has no entry (scale < 10 or > 10^15)
+  int rc = BUFF_OK;
+  buff_col *c = new_col(scale, flags);
+  if (!c) return BUFF_ENOMEM;
+  c->n = n;
+  c->dlen = (uint32_t)dl;
+  T *staged = nullptr;
+  EncStats *part = nullptr;
+  long long *sfx = nullptr;
+  const T *dx = values;
+  EncStats st;
+  memset(&st, 0, sizeof(st));
+  int64_t mn = INT64_MAX, mx = INT64_MIN;
+  const int nb = 4 * buffk::num_sms(c->device);
+  if (n > 0) {
+    if (!is_device_ptr(values) || (reinterpret_cast<uintptr_t>(values) & 15)) {
+      CK(scratch(&staged, n, s));
+      CK(cudaMemcpyAsync(staged, values, (size_t)n * sizeof(T), cudaMemcpyDefault, s));
+      dx = staged;
+    }
+    CK(scratch(&part, (size_t)nb + 1, s));
+    if (sizeof(T) == 8)
+      CK(buffk::launch_encode_reduce_f64(reinterpret_cast<const double *>(dx), n, c->precision_exp,
+                                         c->dlen, part, nb, part + nb, s));
+    else
+      CK(buffk::launch_encode_reduce_f32(reinterpret_cast<const float *>(dx), n, c->precision_exp,
+                                         c->dlen, part, nb, part + nb, s));
+    CK(cudaMemcpyAsync(&st, part + nb, sizeof(st), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    mn = st.mn;
+    if (intended) {
+      mx = st.mx0;
+    } else if (n >= 2) {
+      // Reference max (`else if`, compress/buff_simd.rs:3141-3146) = max of the
+      // rows after the leading strictly decreasing run x_0 > x_1 > ... .
+      const uint64_t brk = st.brk;
+      if (brk == 1 || st.mx1 > st.x1) {
+        mx = st.mx1;
+      } else if (brk >= n) {
+        mx = INT64_MIN;
+      } else {
+        CK(scratch(&sfx, 1, s));
+        if (sizeof(T) == 8)
+          CK(buffk::launch_suffix_max_f64(reinterpret_cast<const double *>(dx), n, (uint32_t)brk,
+                                          c->precision_exp, c->dlen, sfx, s));
+        else
+          CK(buffk::launch_suffix_max_f32(reinterpret_cast<const float *>(dx), n, (uint32_t)brk,
+                                          c->precision_exp, c->dlen, sfx, s));
+        long long v = 0;
+        CK(cudaMemcpyAsync(&v, sfx, sizeof(v), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        mx = v;
+      }
+    }
+  }
+  {
+    const int64_t delta = (int64_t)((uint64_t)mx - (uint64_t)mn);
+    uint32_t fl;
+    if (intended) {
+      fl = (n == 0 || delta == 0) ? 0u : (uint32_t)(64 - __builtin_clzll((uint64_t)delta));
+    } else if (delta == 0) {
+      fl = 0;
+    } else {
+      // `(delta as f64).log2().ceil() as usize` (buff_simd.rs:3156-3161)
+      const double cl = ceil(log2((double)delta));
+      fl = (isnan(cl) || cl <= 0.0) ? 0u : (uint32_t)cl;
+    }
+    if (!intended && fl == 0 && n > 0) {
+      // write_bits(_, 0) indexes one past the buffer (bit_packing.rs:117)
+      rc = BUFF_EREFPANIC;
+      goto done;
+    }
+    c->base = mn;
+    set_layout(c, fl);
+    c->ilen = (uint32_t)((uint64_t)fl - (uint64_t)c->dlen);
+    if ((rc = alloc_col(c, s))) goto done;
+    if (n > 0) {
+      if (sizeof(T) == 8)
+        CK(buffk::launch_encode_scatter_f64(reinterpret_cast<const double *>(dx), c, s));
+      else
+        CK(buffk::launch_encode_scatter_f32(reinterpret_cast<const float *>(dx), c, s));
+    }
+  }
+done:
+  if (staged) cudaFreeAsync(staged, s);
+  if (part) cudaFreeAsync(part, s);
+  if (sfx) cudaFreeAsync(sfx, s);
+  if (rc != BUFF_OK) {
+    cudaStreamSynchronize(s);
+    free_col(c);
+    return rc;
+  }
+  *out = c;
+  return BUFF_OK;
+}
+
+// ---------------------------------------------------------------- filters
+
+enum FilterKind { kRange = 0, kEqual = 1, kRangeSlice = 2, kEqualSlice = 3 };
+
+int filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t *count, cudaStream_t s,
+                FilterKind kind) {
+  if (!c || (!words && c->n > 0)) return BUFF_EINVAL;
+  const bool intended = c->flags & BUFF_FLAG_INTENDED;
+  const bool is_range = (kind == kRange || kind == kRangeSlice);
+  const bool with_slice = (kind == kRangeSlice || kind == kEqualSlice);
+  const uint32_t n = c->n, nw = (n + 31) / 32;
+  int rc = BUFF_OK;
+  uint32_t *dwords = words;
+  unsigned long long *dcount = nullptr;
+  const bool words_host = n > 0 && !is_device_ptr(words);
+  const bool count_host = count && !is_device_ptr(count);
+  bool need_sync = words_host || count_host;
+  // 0: fill zeros, 1: fill ones, 2: kernel
+  int action = 2;
+  FilterArgs a;
+  memset(&a, 0, sizeof(a));
+  const int64_t fixed_part = fetch_fixed_host(pred, c->precision_exp, c->dlen);
+  if (fixed_part < c->base) {
+    // early return (buff_simd.rs:3385-3388, 3573-3576, 3769-3772, 3919-3922):
+    // the printed count is n for range and both fused forms, 0 for equality.
+    action = (kind == kEqual) ? 0 : 1;
+  } else {
+    const uint64_t t = (uint64_t)(fixed_part - c->base);
+    const uint32_t fl = c->fixed_len;
+    if (with_slice && !intended && (c->k == 0 || n < 32)) return BUFF_EREFPANIC;
+    a.slices = c->slices;
+    a.stride = c->stride;
+    a.tail = c->tail;
+    a.n = n;
+    a.is_range = is_range ? 1u : 0u;
+    if (intended || c->k == 0) {
+      // full compare of every row against the untruncated target
+      // (fixed_len < 8: buff_simd.rs:3395-3402, 3583-3590)
+      const bool above = fl < 64 && (t >> fl) != 0;
+      if (above) {
+        action = 0;
+      } else {
+        a.full_rows = n;
+        a.k_used = c->k;
+        a.r = c->r;
+        for (uint32_t j = 0; j < c->k; ++j) a.tbyte[j] = (uint8_t)(t >> (fl - 8 * (j + 1)));
+        a.ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
+      }
+    } else {
+      // byte slices with truncated per-slice targets (buff_simd.rs:3407, 3425, 3448)
+      a.full_rows = n / 32 * 32;
+      a.k_used = with_slice ? (c->k < 4 ? c->k : 4u) : c->k;
+      a.r = c->r;
+      for (uint32_t j = 0; j < a.k_used; ++j) a.tbyte[j] = (uint8_t)(t >> (fl - 8 * (j + 1)));
+      a.ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
+      if (!is_range) {
+        a.tail_only_eq = 1;  // only the tail step writes `res` (buff_simd.rs:3684-3729)
+        if (c->r == 0) action = 0;
+      }
+    }
+  }
+  if (n == 0) {
+    if (count) {
+      if (count_host)
+        *count = 0;
+      else
+        return cuda_status(cudaMemsetAsync(count, 0, sizeof(uint64_t), S(s)));
+    }
+    return BUFF_OK;
+  }
+  if (words_host) CK(scratch(&dwords, nw, s));
+  if (count) {
+    if (count_host)
+      CK(scratch(&dcount, 1, s));
+    else
+      dcount = reinterpret_cast<unsigned long long *>(count);
+    CK(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s));
+  }
+  if (action == 2) {
+    a.words = dwords;
+    a.count = dcount;
+    CK(buffk::launch_filter(a, s));
+  } else {
+    CK(buffk::launch_fill_words(dwords, n, action ? 0xFFFFFFFFu : 0u, dcount, s));
+  }
+  if (words_host) CK(cudaMemcpyAsync(words, dwords, (size_t)nw * 4, cudaMemcpyDeviceToHost, s));
+  if (count_host) CK(cudaMemcpyAsync(count, dcount, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  if (need_sync) CK(cudaStreamSynchronize(s));
+done:
+  if (words_host && dwords) cudaFreeAsync(dwords, s);
+  if (count_host && dcount) cudaFreeAsync(dcount, s);
+  return rc;
+}
+
+// ---------------------------------------------------------------- sum
+
+int sum_partials(const buff_col *c, uint32_t total, unsigned long long *d, cudaStream_t s) {
+  // slices read: total/8 (<= k); packed bits per row after them: total % 8
+  // (for fixed_len < 8 and total < 8 the packed region itself).
+  uint32_t ks, ts;
+  if (total < 8) {
+    ks = 0;
+    ts = total;
+  } else {
+    ks = total / 8;
+    ts = total % 8;
+  }
+  if (ks > c->k) return BUFF_EREFPANIC;  // reads past the slices (slice index panic)
+  if (c->k && ks < c->k && ts) return BUFF_ENOTSUP;
+  if (c->k && total < 8 && total > 0) return BUFF_ENOTSUP;
+  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 9, s);
+  if (e != cudaSuccess) return cuda_status(e);
+  return cuda_status(buffk::launch_sum(c, ks, ts, d, s));
+}
+
+}  // namespace
+
+// ================================================================ C ABI
+
+extern "C" {
+
+int buff_encode_f64(const double *values, uint64_t n, uint64_t scale, uint32_t flags, void *stream,
+                    buff_col **out) {
+  return encode_impl<double>(values, n, scale, flags, S(stream), out);
+}
+
+int buff_encode_f32(const float *values, uint64_t n, uint64_t scale, uint32_t flags, void *stream,
+                    buff_col **out) {
+  return encode_impl<float>(values, n, scale, flags, S(stream), out);
+}
+
+int buff_col_free(buff_col *col) {
+  if (!col) return BUFF_EINVAL;
+  free_col(col);
+  return BUFF_OK;
+}
+
+int buff_col_free_async(buff_col *col, void *stream) {
+  if (!col) return BUFF_EINVAL;
+  free_col(col, S(stream), true);
+  return BUFF_OK;
+}
+
+int buff_col_get_info(const buff_col *c, buff_col_info *info) {
+  if (!c || !info) return BUFF_EINVAL;
+  memset(info, 0, sizeof(*info));
+  info->base = c->base;
+  info->n = c->n;
+  info->ilen = c->ilen;
+  info->dlen = c->dlen;
+  info->fixed_len = c->fixed_len;
+  info->k = c->k;
+  info->r = c->r;
+  info->scale = c->scale;
+  info->prec = c->prec;
+  info->precision_exp = c->precision_exp;
+  info->flags = c->flags;
+  info->serialized_bytes = serialized_size(c);
+  info->device_bytes = (uint64_t)c->k * c->stride + c->tail_alloc;
+  return BUFF_OK;
+}
+
+int buff_serialize(const buff_col *c, uint8_t *out, uint64_t cap, uint64_t *len, void *stream) {
+  if (!c || !len) return BUFF_EINVAL;
+  const uint64_t need = serialized_size(c);
+  *len = need;
+  if (!out || cap < need) return BUFF_EINVAL;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  const bool dev = is_device_ptr(out);
+  uint8_t hdr[20];
+  const uint64_t ub = (uint64_t)c->base;
+  const uint32_t words5[5] = {(uint32_t)ub, (uint32_t)(ub >> 32), c->n, c->ilen, c->dlen};
+  for (int i = 0; i < 5; ++i)
+    for (int b = 0; b < 4; ++b) hdr[4 * i + b] = (uint8_t)(words5[i] >> (8 * b));
+  if (dev)
+    CK(cudaMemcpyAsync(out, hdr, 20, cudaMemcpyHostToDevice, s));
+  else
+    memcpy(out, hdr, 20);
+  if (c->k && c->n)
+    CK(cudaMemcpy2DAsync(out + 20, c->n, c->slices, c->stride, c->n, c->k, cudaMemcpyDefault, s));
+  if (c->tail_bytes)
+    CK(cudaMemcpyAsync(out + 20 + (uint64_t)c->k * c->n, c->tail, c->tail_bytes, cudaMemcpyDefault,
+                       s));
+  if (dev) CK(cudaStreamSynchronize(s));  // hdr lives on this stack frame
+  else CK(cudaStreamSynchronize(s));
+done:
+  return rc;
+}
+
+int buff_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                     void *stream, buff_col **out) {
+  if (!out || !bytes) return BUFF_EINVAL;
+  *out = nullptr;
+  if (len < 20) return BUFF_ECORRUPT;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  const bool dev = is_device_ptr(bytes);
+  uint8_t hdr[20];
+  buff_col *c = nullptr;
+  uint32_t w[5];
+  if (dev) {
+    CK(cudaMemcpyAsync(hdr, bytes, 20, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  } else {
+    memcpy(hdr, bytes, 20);
+  }
+  for (int i = 0; i < 5; ++i)
+    w[i] = (uint32_t)hdr[4 * i] | ((uint32_t)hdr[4 * i + 1] << 8) |
+           ((uint32_t)hdr[4 * i + 2] << 16) | ((uint32_t)hdr[4 * i + 3] << 24);
+  c = new_col(scale, flags);
+  if (!c) return BUFF_ENOMEM;
+  c->base = (int64_t)((uint64_t)w[0] | ((uint64_t)w[1] << 32));
+  c->n = w[2];
+  c->ilen = w[3];
+  c->dlen = w[4];
+  {
+    const uint32_t fl = c->ilen + c->dlen;  // the decoders' `dlen + ilen` (u32)
+    if (fl > 64 || c->dlen > 1000) {
+      rc = BUFF_ECORRUPT;
+      goto done;
+    }
+    set_layout(c, fl);
+    if (serialized_size(c) > len) {
+      rc = BUFF_ECORRUPT;
+      goto done;
+    }
+    if ((rc = alloc_col(c, s))) goto done;
+    if (c->k && c->n)
+      CK(cudaMemcpy2DAsync(c->slices, c->stride, bytes + 20, c->n, c->n, c->k, cudaMemcpyDefault,
+                           s));
+    CK(cudaMemsetAsync(c->tail, 0, c->tail_alloc, s));
+    if (c->tail_bytes)
+      CK(cudaMemcpyAsync(c->tail, bytes + 20 + (uint64_t)c->k * c->n, c->tail_bytes,
+                         cudaMemcpyDefault, s));
+    if (!dev) CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (rc != BUFF_OK) {
+    free_col(c);
+    return rc;
+  }
+  *out = c;
+  return BUFF_OK;
+}
+
+int buff_decode(const buff_col *c, double *out, void *stream) {
+  if (!c || (!out && c->n)) return BUFF_EINVAL;
+  if (c->n == 0) return BUFF_OK;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  double *d = out;
+  const bool stage = !is_device_ptr(out) || (reinterpret_cast<uintptr_t>(out) & 15);
+  if (stage) CK(scratch(&d, c->n, s));
+  CK(buffk::launch_decode(c, c->fixed_len, 0, d, s));
+  if (stage) {
+    CK(cudaMemcpyAsync(out, d, (size_t)c->n * 8, cudaMemcpyDefault, s));
+    CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (stage && d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+int buff_decode_at_precision(const buff_col *c, uint32_t precision, double *out, void *stream) {
+  if (!c || (!out && c->n)) return BUFF_EINVAL;
+  uint32_t total = 0;
+  int rc = precision_bits(c, precision, &total);
+  if (rc) return rc;
+  const bool intended = c->flags & BUFF_FLAG_INTENDED;
+  if (intended) {
+    if (total > c->fixed_len) return BUFF_EREFPANIC;
+  } else {
+    if (total >= 8 && total / 8 > c->k) return BUFF_EREFPANIC;  // reads past the slices
+    if (total < 8 && c->k && total) return BUFF_ENOTSUP;
+  }
+  if (c->n == 0) return BUFF_OK;
+  cudaStream_t s = S(stream);
+  double *d = out;
+  const bool stage = !is_device_ptr(out) || (reinterpret_cast<uintptr_t>(out) & 15);
+  if (stage) CK(scratch(&d, c->n, s));
+  CK(buffk::launch_decode(c, total, intended ? 1 : 0, d, s));
+  if (stage) {
+    CK(cudaMemcpyAsync(out, d, (size_t)c->n * 8, cudaMemcpyDefault, s));
+    CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (stage && d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+int buff_range_filter(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                      void *stream) {
+  return filter_impl(c, pred, words, count, S(stream), kRange);
+}
+int buff_equal_filter(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                      void *stream) {
+  return filter_impl(c, pred, words, count, S(stream), kEqual);
+}
+int buff_range_filter_with_slice(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                                 void *stream) {
+  return filter_impl(c, pred, words, count, S(stream), kRangeSlice);
+}
+int buff_equal_filter_with_slice(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                                 void *stream) {
+  return filter_impl(c, pred, words, count, S(stream), kEqualSlice);
+}
+
+int buff_sum_partials_async(const buff_col *c, uint64_t *dev_partials, void *stream) {
+  if (!c || !dev_partials) return BUFF_EINVAL;
+  return sum_partials(c, c->fixed_len, reinterpret_cast<unsigned long long *>(dev_partials),
+                      S(stream));
+}
+
+int buff_sum_finish(const buff_col *c, const uint64_t *parts, buff_sum_result *out) {
+  if (!c || !parts || !out) return BUFF_EINVAL;
+  memset(out, 0, sizeof(*out));
+  const bool intended = c->flags & BUFF_FLAG_INTENDED;
+  out->sum = combine_sum(c, c->fixed_len, parts, intended);
+  __int128 acc = (__int128)c->n * (__int128)c->base;
+  for (uint32_t j = 0; j < c->k; ++j) acc += (__int128)parts[j] << (c->fixed_len - 8 * (j + 1));
+  if (c->r) acc += (__int128)parts[c->k];
+  out->exact_num_lo = (int64_t)(uint64_t)acc;
+  out->exact_num_hi = (int64_t)(acc >> 64);
+  // exact / 2^dlen, rounded once (int128 -> double is round-to-nearest-even)
+  out->exact = ldexp((double)acc, -(int)c->dlen);
+  out->n_partials = c->k + (c->r ? 1u : 0u);
+  for (uint32_t j = 0; j < out->n_partials && j < 9; ++j) out->partials[j] = parts[j];
+  return BUFF_OK;
+}
+
+int buff_sum(const buff_col *c, buff_sum_result *out, void *stream) {
+  if (!c || !out) return BUFF_EINVAL;
+  cudaStream_t s = S(stream);
+  uint64_t parts[9] = {0};
+  unsigned long long *d = nullptr;
+  int rc = BUFF_OK;
+  if (c->n) {
+    CK(scratch(&d, 9, s));
+    if ((rc = sum_partials(c, c->fixed_len, d, s))) goto done;
+    CK(cudaMemcpyAsync(parts, d, sizeof(parts), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  rc = buff_sum_finish(c, parts, out);
+done:
+  if (d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+int buff_sum_at_precision(const buff_col *c, uint32_t precision, double *out, void *stream) {
+  if (!c || !out) return BUFF_EINVAL;
+  uint32_t total = 0;
+  int rc = precision_bits(c, precision, &total);
+  if (rc) return rc;
+  cudaStream_t s = S(stream);
+  uint64_t parts[9] = {0};
+  unsigned long long *d = nullptr;
+  if (c->n) {
+    CK(scratch(&d, 9, s));
+    if ((rc = sum_partials(c, total, d, s))) goto done;
+    CK(cudaMemcpyAsync(parts, d, sizeof(parts), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  } else if (total >= 8 && total / 8 > c->k) {
+    rc = BUFF_EREFPANIC;
+    goto done;
+  }
+  *out = combine_sum(c, total, parts, c->flags & BUFF_FLAG_INTENDED);
+done:
+  if (d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+int buff_max_async(const buff_col *c, uint64_t *dev_max_code, void *stream) {
+  if (!c || !dev_max_code) return BUFF_EINVAL;
+  cudaStream_t s = S(stream);
+  cudaError_t e = cudaMemsetAsync(dev_max_code, 0, sizeof(uint64_t), s);
+  if (e != cudaSuccess) return cuda_status(e);
+  return cuda_status(
+      buffk::launch_max(c, reinterpret_cast<unsigned long long *>(dev_max_code), s));
+}
+
+int buff_max(const buff_col *c, double *max_value, uint64_t *max_code, uint32_t *argmax_words,
+             uint64_t *argmax_count, void *stream) {
+  if (!c) return BUFF_EINVAL;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  const uint32_t nw = (c->n + 31) / 32;
+  unsigned long long *d = nullptr;
+  uint32_t *dwords = nullptr;
+  uint64_t m = 0, cnt = 0;
+  const bool intended = c->flags & BUFF_FLAG_INTENDED;
+  const bool words_dev = argmax_words && is_device_ptr(argmax_words);
+  CK(scratch(&d, 2, s));
+  CK(cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), s));
+  if (c->n) CK(buffk::launch_max(c, d, s));
+  if (argmax_words || argmax_count) {
+    // byte_fixed_max fills `res` only in the tail step (or for fixed_len < 8).
+    const bool empty = !intended && c->k > 0 && c->r == 0;
+    if (c->n) {
+      if (argmax_words) {
+        if (words_dev)
+          dwords = argmax_words;
+        else
+          CK(scratch(&dwords, nw, s));
+      }
+      if (empty) {
+        if (dwords) CK(buffk::launch_fill_words(dwords, c->n, 0u, nullptr, s));
+      } else {
+        uint32_t *tmp = dwords;
+        if (!tmp) CK(scratch(&tmp, nw, s));
+        CK(buffk::launch_argmax(c, d, tmp, d + 1, s));
+        if (!dwords) cudaFreeAsync(tmp, s);
+      }
+      if (argmax_words && !words_dev)
+        CK(cudaMemcpyAsync(argmax_words, dwords, (size_t)nw * 4, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  CK(cudaMemcpyAsync(&m, d, sizeof(m), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&cnt, d + 1, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (max_code) *max_code = m;
+  if (max_value)
+    *max_value = (double)(int64_t)((uint64_t)c->base + m) / ldexp(1.0, (int)c->dlen);
+  if (argmax_count) *argmax_count = cnt;
+done:
+  if (d) cudaFreeAsync(d, s);
+  if (dwords && !words_dev) cudaFreeAsync(dwords, s);
+  return rc;
+}
+
+const char *buff_status_string(int st) {
+  switch (st) {
+    case BUFF_OK: return "ok";
+    case BUFF_EINVAL: return "invalid argument";
+    case BUFF_ENOMEM: return "out of memory";
+    case BUFF_ECUDA: return "CUDA runtime error";
+    case BUFF_EREFPANIC: return "input on which the reference implementation panics";
+    case BUFF_ECORRUPT: return "serialized column is inconsistent with its header";
+    case BUFF_ETIMEDOUT: return "bounded device wait expired";
+    case BUFF_ENOTSUP: return "not supported for this column layout";
+    case BUFF_EFULL: return "queue or memory budget exhausted";
+    default: return "unknown status";
+  }
+}
+
+int buff_last_cuda_error(void) { return g_last_cuda; }
+
+uint64_t buff_kernel_launches(void) { return buffk::launches(); }
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+// Internal declarations shared by the C ABI (buff_capi.cu) and the kernels
+// (buff_kernels.cu).  Not part of the public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+
+#include "../../include/buff_gpu.h"
+
+// Device image of one column.  `slices` holds k byte slices, each `stride`
+// bytes apart (stride >= n, a multiple of kRowChunk), bytes stored flipped
+// (x ^ 0x80) exactly as the reference writes them (compress/buff_simd.rs:3181-3225).
+// `tail` holds the r-bit packed remainder, LSB-first, byte-identical to
+// BitPack::write_bits (methods/bit_packing.rs:106-135); for fixed_len < 8 it
+// holds the whole packed code (k == 0, r == fixed_len).  Padding rows beyond
+// n are zero in the tail and arbitrary in the slices.
+struct buff_col {
+  int64_t base;
+  uint32_t n;
+  uint32_t ilen, dlen, fixed_len, k, r;
+  uint64_t scale;
+  int32_t prec, precision_exp;
+  uint32_t flags;
+  int device;
+  uint8_t *slices;
+  size_t stride;
+  uint8_t *tail;
+  size_t tail_bytes;  // bytes of the packed tail (ceil(n*r/8)), excluding padding
+  size_t tail_alloc;
+};
+
+namespace buffk {
+
+constexpr uint32_t kRowChunk = 512;  // rows one warp covers per step (32 lanes x 16 rows)
+
+inline size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+// Encode statistics gathered by the reduce pass.
+struct EncStats {
+  long long mn;     // min over all rows
+  long long mx1;    // max over rows >= 1
+  long long mx0;    // max over all rows
+  long long x0, x1; // first two quantized rows
+  unsigned long long brk;  // first i >= 1 with x_i >= x_{i-1} (n if none)
+};
+
+struct FilterArgs {
+  const uint8_t *slices;
+  size_t stride;
+  const uint8_t *tail;
+  uint32_t n;          // rows
+  uint32_t full_rows;  // rows that may be set (32*floor(n/32) for the reference's SIMD compare)
+  uint32_t k_used;     // slices compared
+  uint32_t r;          // packed tail bits compared (0 = no tail step)
+  uint32_t is_range;   // 1: value > pred, 0: value == pred
+  uint32_t tail_only_eq;  // equality result requires the tail step
+  uint8_t tbyte[8];    // target byte per slice (unflipped)
+  uint32_t ttail;      // target tail bits
+  uint32_t *words;
+  unsigned long long *count;  // may be null
+};
+
+// Per-stream launch helpers (buff_kernels.cu).  All return cudaError_t.
+cudaError_t launch_encode_reduce_f64(const double *x, uint32_t n, int32_t pexp, uint32_t dlen,
+                                     EncStats *d_part, int nblocks, EncStats *d_out,
+                                     cudaStream_t s);
+cudaError_t launch_encode_reduce_f32(const float *x, uint32_t n, int32_t pexp, uint32_t dlen,
+                                     EncStats *d_part, int nblocks, EncStats *d_out,
+                                     cudaStream_t s);
+cudaError_t launch_suffix_max_f64(const double *x, uint32_t n, uint32_t from, int32_t pexp,
+                                  uint32_t dlen, long long *d_out, cudaStream_t s);
+cudaError_t launch_suffix_max_f32(const float *x, uint32_t n, uint32_t from, int32_t pexp,
+                                  uint32_t dlen, long long *d_out, cudaStream_t s);
+cudaError_t launch_encode_scatter_f64(const double *x, const buff_col *c, cudaStream_t s);
+cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStream_t s);
+cudaError_t launch_filter(const FilterArgs &a, cudaStream_t s);
+cudaError_t launch_fill_words(uint32_t *words, uint32_t n, uint32_t value,
+                              unsigned long long *count, cudaStream_t s);
+cudaError_t launch_sum(const buff_col *c, uint32_t k_used, uint32_t tail_bits,
+                       unsigned long long *d_partials, cudaStream_t s);
+cudaError_t launch_max(const buff_col *c, unsigned long long *d_max, cudaStream_t s);
+cudaError_t launch_argmax(const buff_col *c, const unsigned long long *d_max, uint32_t *words,
+                          unsigned long long *count, cudaStream_t s);
+// Decode with `total` leading bits (REF) or masked to `total` bits (INTENDED).
+cudaError_t launch_decode(const buff_col *c, uint32_t total, int intended_mask, double *out,
+                          cudaStream_t s);
+
+int num_sms(int device);
+void count_launch(uint64_t n = 1);
+uint64_t launches();
+
+}  // namespace buffk

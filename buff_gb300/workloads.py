@@ -1,0 +1,63 @@
+"""Seeded synthetic columns with the shapes and value distributions of the
+benchmark configurations (none of them is a public dataset).
+
+- ``gaussian_walk``: x0 = 1.0, steps N(0, 0.01), rounded to 4 decimals
+  (1,000,000 values, scale 10^4).
+- ``bounded_walk``: steps U(-0.5, 0.5) reflected into [-500, 500], rounded to
+  4 decimals (268,435,456 values, scale 10^4 -> 25-bit codes, 3 slices + 1 bit).
+- ``outlier_column``: 99% N(100, 5) at 6 decimals, 1% U(-1e6, 1e6) at seeded
+  random positions (67,108,864 values, scale 10^6).
+
+The numpy forms are for host-sized cases; the torch forms build large columns
+directly in device memory.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def gaussian_walk(n: int, seed: int = 1) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    x = 1.0 + np.cumsum(rng.normal(0.0, 0.01, n))
+    return np.round(x, 4)
+
+
+def _fold(x, lo=-500.0, hi=500.0):
+    """Reflects a free walk into [lo, hi] (triangle-wave fold)."""
+    span = hi - lo
+    y = np.mod(x - lo, 2 * span)
+    return lo + np.where(y > span, 2 * span - y, y)
+
+
+def bounded_walk(n: int, seed: int = 2) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    x = np.cumsum(rng.uniform(-0.5, 0.5, n))
+    return np.round(_fold(x), 4)
+
+
+def outlier_column(n: int, seed: int = 3) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    x = np.round(rng.normal(100.0, 5.0, n), 6)
+    m = max(1, n // 100)
+    pos = rng.choice(n, size=m, replace=False)
+    x[pos] = np.round(rng.uniform(-1e6, 1e6, m), 6)
+    return x
+
+
+def bounded_walk_torch(n: int, seed: int = 2, device="cuda"):
+    """bounded_walk generated on the device (float64)."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    steps = torch.rand(n, generator=g, device=device, dtype=torch.float64) - 0.5
+    x = torch.cumsum(steps, 0)
+    lo, span = -500.0, 1000.0
+    y = torch.remainder(x - lo, 2 * span)
+    y = lo + torch.where(y > span, 2 * span - y, y)
+    return torch.round(y * 1e4) / 1e4
+
+
+def quantile_preds(x: np.ndarray, selectivities=(0.001, 0.01, 0.1, 0.5)):
+    """Predicates p with P(x > p) ~= selectivity."""
+    return [float(np.quantile(x, 1.0 - s)) for s in selectivities]

@@ -1,0 +1,177 @@
+/*
+ * buff_gpu.h — C ABI of the GB300 (sm_103a) BUFF column codec.
+ *
+ * BUFF ("decomposed bounded floats", Tranway1/buff) stores an f64/f32 column
+ * as bounded fixed-point codes split most-significant byte first into byte
+ * slices, plus a bit-packed tail, and answers queries directly on the slices.
+ * This library keeps the column resident in HBM behind an opaque handle and
+ * runs encode, filters, sum, max and (variable-precision) decode as CUDA
+ * kernels.  Every entry point mirrors one method of the reference's
+ * `SplitBDDoubleCompress` (database/src/compress/split_double.rs:29-39 and
+ * database/src/compress/buff_simd.rs); the comment on each one names the
+ * reference function it replaces.
+ *
+ * Conventions
+ *  - Every function returns an int status (BUFF_OK == 0).  Nothing aborts:
+ *    inputs on which the reference panics return BUFF_EREFPANIC.
+ *  - `stream` is a cudaStream_t (NULL = the legacy default stream).
+ *  - Pointers to values/outputs may be host (pageable or pinned) or device
+ *    memory; the library detects which.  A call that writes any host memory
+ *    synchronizes `stream` before returning; a call whose outputs are all
+ *    device memory only enqueues work.
+ *  - Handles are immutable after encode/deserialize: concurrent queries on
+ *    one handle from several streams or threads are safe.
+ *  - Bitmaps are BitVec<u32> words (bit-vec/src/lib.rs:213-218): row i is
+ *    bit (i % 32) of word (i / 32); ceil(n/32) words; bits past n are zero.
+ *  - By default every result is bit-identical to the reference, including
+ *    its documented quirks.  BUFF_FLAG_INTENDED (given at encode or
+ *    deserialize time) switches the column to the mathematically intended
+ *    semantics instead.
+ */
+#ifndef BUFF_GPU_H
+#define BUFF_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define BUFF_OK 0
+#define BUFF_EINVAL 1     /* bad argument (NULL handle, n >= 2^32, short buffer, ...) */
+#define BUFF_ENOMEM 2     /* device or host allocation failed */
+#define BUFF_ECUDA 3      /* a CUDA runtime call failed (see buff_last_cuda_error) */
+#define BUFF_EREFPANIC 4  /* the reference panics on this input */
+#define BUFF_ECORRUPT 5   /* serialized bytes are inconsistent with their header */
+#define BUFF_ETIMEDOUT 6  /* a bounded device-side wait expired */
+#define BUFF_ENOTSUP 7    /* not supported for this column layout */
+#define BUFF_EFULL 8      /* a queue or memory budget is exhausted */
+
+/* ---- flags ---- */
+/* Intended semantics instead of the reference's quirks: exact min/max and
+ * bit width at encode (constant columns allowed), filters cover the rows
+ * after the last full 32-row block, targets above the code range compare
+ * correctly, sum keeps the base term when the tail is empty, equality
+ * answers columns without tail bits, variable-precision decode keeps the
+ * retained bits in place. */
+#define BUFF_FLAG_INTENDED 0x1u
+
+typedef struct buff_col buff_col;
+
+/* Column metadata (the 20-byte reference header plus derived fields). */
+typedef struct buff_col_info {
+  int64_t base;          /* column minimum in fixed-point units */
+  uint32_t n;            /* rows */
+  uint32_t ilen;         /* integer bits as stored (wraps when fixed_len < dlen) */
+  uint32_t dlen;         /* fractional bits = PRECISION_MAP[prec] */
+  uint32_t fixed_len;    /* code width = ilen + dlen */
+  uint32_t k;            /* full byte slices (0 when fixed_len < 8) */
+  uint32_t r;            /* packed bits per row after the slices (fixed_len when < 8) */
+  uint64_t scale;        /* the SplitBDDoubleCompress scale the column was built with */
+  int32_t prec;          /* floor(log10(scale)) */
+  int32_t precision_exp; /* exponent of the reference's precision bound */
+  uint32_t flags;
+  uint32_t reserved;
+  uint64_t serialized_bytes; /* size of the reference byte image */
+  uint64_t device_bytes;     /* HBM held by the handle */
+} buff_col_info;
+
+/* Sum of a column. */
+typedef struct buff_sum_result {
+  double sum;            /* the reference's f64 accumulation, bit-exact */
+  double exact;          /* exact_num / 2^dlen, rounded once */
+  int64_t exact_num_lo;  /* exact numerator n*base + sum(code) as a 128-bit */
+  int64_t exact_num_hi;  /*   two's-complement integer (lo, hi) */
+  uint64_t partials[9];  /* per-slice byte sums (unflipped), then the tail sum */
+  uint32_t n_partials;
+  uint32_t reserved;
+} buff_sum_result;
+
+/* ---- encode / lifetime ---- */
+
+/* SplitBDDoubleCompress::buff_simd256_encode (compress/buff_simd.rs:3116-3250).
+ * Quantizes `n` values with scale `scale` (decimals = floor(log10(scale))),
+ * and builds the byte-sliced column in HBM.  n < 2^32. */
+int buff_encode_f64(const double *values, uint64_t n, uint64_t scale, uint32_t flags,
+                    void *stream, buff_col **out);
+/* The same for f32 input (T: Into<f64>, compress/buff_simd.rs:3117). */
+int buff_encode_f32(const float *values, uint64_t n, uint64_t scale, uint32_t flags,
+                    void *stream, buff_col **out);
+/* Releases the handle and its device memory (drains the device first, so
+ * queries still running on any stream are safe). */
+int buff_col_free(buff_col *col);
+/* Releases the handle; the memory returns to the pool in stream order on
+ * `stream`, after the work already queued there. */
+int buff_col_free_async(buff_col *col, void *stream);
+int buff_col_get_info(const buff_col *col, buff_col_info *info);
+
+/* The exact reference byte image (the Vec<u8> buff_simd256_encode returns):
+ * 20-byte header, k flipped byte slices of n bytes, packed tail. */
+int buff_serialize(const buff_col *col, uint8_t *out, uint64_t cap, uint64_t *len,
+                   void *stream);
+/* Rebuilds a handle from a reference byte image.  The image does not carry
+ * the scale, so the caller passes the SplitBDDoubleCompress scale. */
+int buff_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                     void *stream, buff_col **out);
+
+/* ---- queries ---- */
+
+/* SplitBDDoubleCompress::buff_simd256_decode (compress/buff_simd.rs:3252-3357):
+ * out[i] = (base + code_i) / 2^dlen for all n rows. */
+int buff_decode(const buff_col *col, double *out, void *stream);
+
+/* SplitBDDoubleCompress::byte_residue_decode_with_precision
+ * (compress/split_double.rs:1612-1893), applied to this layout: rebuilds only
+ * the leading bits that `precision` decimals need (precision 0 = integer
+ * part).  Unknown precision or one finer than the column: BUFF_EREFPANIC. */
+int buff_decode_at_precision(const buff_col *col, uint32_t precision, double *out,
+                             void *stream);
+
+/* SplitBDDoubleCompress::buff_simd_range_filter (compress/buff_simd.rs:3361-3547):
+ * rows with value > pred.  `words` receives ceil(n/32) bitmap words; `count`
+ * (may be NULL) the number of set bits. */
+int buff_range_filter(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
+                      void *stream);
+/* SplitBDDoubleCompress::buff_simd_equal_filter (compress/buff_simd.rs:3549-3733). */
+int buff_equal_filter(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
+                      void *stream);
+/* buff_simd_range_filter_with_slice (compress/buff_simd.rs:3736-3884): the
+ * fused form that compares at most 4 leading slices. */
+int buff_range_filter_with_slice(const buff_col *col, double pred, uint32_t *words,
+                                 uint64_t *count, void *stream);
+/* buff_simd_equal_filter_with_slice (compress/buff_simd.rs:3888-4025). */
+int buff_equal_filter_with_slice(const buff_col *col, double pred, uint32_t *words,
+                                 uint64_t *count, void *stream);
+
+/* SplitBDDoubleCompress::byte_fixed_sum (compress/split_double.rs:2127-2208) on
+ * the unflipped slice bytes; synchronizes. */
+int buff_sum(const buff_col *col, buff_sum_result *out, void *stream);
+/* byte_residue_sum_with_precision (compress/split_double.rs:2409-2630). */
+int buff_sum_at_precision(const buff_col *col, uint32_t precision, double *out, void *stream);
+/* Device-only half of buff_sum: enqueues the per-slice byte sums into
+ * `dev_partials` (k+1 u64, device memory).  buff_sum_finish turns host copies
+ * of those partials into the reference's f64 result. */
+int buff_sum_partials_async(const buff_col *col, uint64_t *dev_partials, void *stream);
+int buff_sum_finish(const buff_col *col, const uint64_t *host_partials, buff_sum_result *out);
+
+/* SplitBDDoubleCompress::byte_fixed_max (compress/split_double.rs:3919-4105):
+ * the column maximum, its code, and optionally the arg-max bitmap and its
+ * cardinality (argmax_words/argmax_count may be NULL). */
+int buff_max(const buff_col *col, double *max_value, uint64_t *max_code,
+             uint32_t *argmax_words, uint64_t *argmax_count, void *stream);
+/* Device-only max: enqueues the maximum code into *dev_max_code (device u64). */
+int buff_max_async(const buff_col *col, uint64_t *dev_max_code, void *stream);
+
+/* ---- diagnostics ---- */
+const char *buff_status_string(int status);
+/* The last CUDA error code seen by this thread (0 if none). */
+int buff_last_cuda_error(void);
+/* Number of this library's kernels launched by this process so far. */
+uint64_t buff_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BUFF_GPU_H */

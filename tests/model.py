@@ -1,0 +1,124 @@
+"""A second, independent statement of the buff-simd semantics in numpy/Python.
+
+The oracle (oracle/buff_oracle.c) follows the reference's control flow
+(BitPack cursor, progressive candidate refinement, SIMD threshold).  This model
+states the same results as whole-array formulas, so the two cross-check each
+other.  Small inputs only.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+PRECISION_MAP = {1: 5, 2: 8, 3: 11, 4: 15, 5: 18, 6: 21, 7: 25, 8: 28, 9: 31, 10: 35, 11: 38,
+                 12: 50, 13: 10, 14: 10, 15: 10}
+
+
+def prec_of_scale(scale: int) -> int:
+    if scale == 0:
+        return 0
+    return int(np.log10(np.float32(scale)))
+
+
+def precision_exp(prec: int) -> int:
+    v = float("0." + "0" * max(prec, 0) + "49")
+    return math.frexp(v)[1] - 1
+
+
+def fetch_fixed(x: np.ndarray, pexp: int, dlen: int) -> np.ndarray:
+    """fetch_fixed_aligned (methods/prec_double.rs:190-205), vectorized."""
+    b = np.ascontiguousarray(x, dtype=np.float64).view(np.uint64)
+    exp = ((b >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64) - 1023
+    sh = ((63 - exp - dlen) & 63).astype(np.uint64)
+    m = ((b << np.uint64(11)) | np.uint64(1 << 63)) >> sh
+    neg = (b >> np.uint64(63)) != 0
+    m = np.where(neg, (~(m - np.uint64(1))), m)
+    m = np.where(exp < pexp, np.uint64(0), m)
+    return m.view(np.int64)
+
+
+def ref_minmax(q: np.ndarray):
+    """The reference's `if x<min {..} else if x>max {..}` loop (buff_simd.rs:3139-3148)."""
+    mn, mx = (1 << 63) - 1, -(1 << 63)
+    for v in q.tolist():
+        if v < mn:
+            mn = v
+        elif v > mx:
+            mx = v
+    return mn, mx
+
+
+def wrap64(v: int) -> int:
+    v &= (1 << 64) - 1
+    return v - (1 << 64) if v >> 63 else v
+
+
+def layout(q: np.ndarray, scale: int, intended: bool):
+    prec = prec_of_scale(scale)
+    dlen = PRECISION_MAP[prec]
+    if intended:
+        mn, mx = int(q.min()), int(q.max())
+        delta = mx - mn
+        fl = 0 if delta == 0 else delta.bit_length()
+    else:
+        mn, mx = ref_minmax(q)
+        delta = wrap64(mx - mn)
+        if delta == 0:
+            fl = 0
+        else:
+            c = math.ceil(math.log2(float(delta))) if delta > 0 else float("nan")
+            fl = 0 if (c != c or c <= 0) else int(c)
+    k, r = (0, fl) if fl < 8 else (fl // 8, fl % 8)
+    codes = np.array([(int(v) - mn) & ((1 << fl) - 1) if fl else 0 for v in q.tolist()],
+                     dtype=np.uint64)
+    return dict(base=mn, fl=fl, k=k, r=r, dlen=dlen, codes=codes,
+                ilen=(fl - dlen) & 0xFFFFFFFF, pexp=precision_exp(prec))
+
+
+def bits_to_words(bits: np.ndarray) -> np.ndarray:
+    n = bits.size
+    nw = (n + 31) // 32
+    pad = np.zeros(nw * 32, dtype=np.uint8)
+    pad[:n] = bits
+    return np.packbits(pad, bitorder="little").view("<u4")[:nw].astype(np.uint32)
+
+
+def filter_words(L, pred: float, is_range: bool, intended: bool) -> np.ndarray:
+    n = L["codes"].size
+    fp = int(fetch_fixed(np.array([pred]), L["pexp"], L["dlen"])[0])
+    if fp < L["base"]:
+        return bits_to_words(np.full(n, 1 if is_range else 0, dtype=np.uint8))
+    t = fp - L["base"]
+    codes = [int(c) for c in L["codes"].tolist()]
+    fl, k, r = L["fl"], L["k"], L["r"]
+    if intended or k == 0:
+        hit = [(c > t) if is_range else (c == t) for c in codes]
+        return bits_to_words(np.array(hit, dtype=np.uint8))
+    tt = t & ((1 << fl) - 1)
+    full = n // 32 * 32
+    if (not is_range) and r == 0:
+        return bits_to_words(np.zeros(n, dtype=np.uint8))
+    hit = [((c > tt) if is_range else (c == tt)) and i < full for i, c in enumerate(codes)]
+    return bits_to_words(np.array(hit, dtype=np.uint8))
+
+
+def ref_sum(L, n: int, intended: bool = False) -> float:
+    codes = [int(c) for c in L["codes"].tolist()]
+    fl, k, r, dlen = L["fl"], L["k"], L["r"], L["dlen"]
+    ilen_i = L["ilen"] - (1 << 32) if L["ilen"] >> 31 else L["ilen"]
+    sum_base = float(n) * float(L["base"]) / 2.0 ** dlen
+    s = 0.0
+    processed = 0
+    for j in range(k):
+        sh = fl - 8 * (j + 1)
+        S = sum((c >> sh) & 0xFF for c in codes)
+        processed += 8
+        s = s + float(S) / 2.0 ** (processed - ilen_i)
+        if j == k - 1 and r == 0 and not intended:
+            return s
+    if r:
+        S = sum(c & ((1 << r) - 1) for c in codes)
+        processed += r
+        s = s + float(S) / 2.0 ** (processed - ilen_i)
+    return s + sum_base
