@@ -48,12 +48,15 @@ CPU_SAMPLE_ROWS = 1 << 25
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--rows", type=int, default=N_ROWS)
     ap.add_argument("--no-ops", action="store_true", help="skip the per-op table")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e leg")
+    ap.add_argument("--free-input", action="store_true",
+                    help="release the f64 input after encode (small-footprint profiling runs)")
     return ap.parse_args()
 
 
@@ -128,7 +131,7 @@ class Clocks:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={index}",
+                ["nvidia-smi", "-i", str(index),
                  "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
@@ -136,6 +139,11 @@ class Clocks:
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+        t0 = time.time()
+        while self.proc and time.time() - t0 < 5.0:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.05)
 
     def stop(self):
         if not self.proc:
@@ -189,6 +197,11 @@ def run_reference(args, rank, world):
     x = bounded_walk_torch(CPU_SAMPLE_ROWS, seed=2, device=dev).cpu().numpy()
     pred = float(np.quantile(x[::64], 1.0 - SELECTIVITY))
     threads = os.cpu_count() or 1
+    # size each step's sample so that the K timed steps take about a minute
+    t1, _, _ = cpu_reference_line(args, x, pred, threads, 1, 0)[:3]
+    frac = min(1.0, 60.0 / max(args.steps, 1) / max(t1, 1e-9))
+    rows_step = max(1 << 16, int(x.size * frac) // 32 * 32)
+    x = x[:rows_step]
     per_step, rows, cnt, s = cpu_reference_line(args, x, pred, threads, args.steps, args.warmup)
     v = rows / per_step / 1e9
     line = {
@@ -203,6 +216,39 @@ def run_reference(args, rank, world):
         "e2e": {"value": v, "unit": "Gvalues/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def run_e2e(L, col, img_len, nw, pred, sh, count, res, args):
+    """The reference-style call: upload the byte image, filter, sum, free."""
+    import torch
+
+    from buff_gb300 import capi
+
+    img = torch.empty(img_len, dtype=torch.uint8, pin_memory=True)
+    col.serialize(out=img.numpy())
+    hwords = torch.empty(nw, dtype=torch.int32, pin_memory=True)
+    hcount = np.zeros(1, dtype=np.uint64)
+
+    def e2e_step():
+        hc = C.c_void_p()
+        capi.check(L.buff_deserialize(img.data_ptr(), img_len, SCALE, 0, sh, C.byref(hc)))
+        capi.check(L.buff_range_filter(hc, pred, hwords.data_ptr(), hcount.ctypes.data, sh))
+        sres = capi.SumResult()
+        capi.check(L.buff_sum(hc, C.byref(sres), sh))
+        capi.check(L.buff_col_free_async(hc, sh))
+        return sres
+
+    for _ in range(3):
+        e2e_step()
+    torch.cuda.synchronize()
+    reps = max(3, min(args.steps, 20))
+    t1 = time.perf_counter()
+    for _ in range(reps):
+        sres = e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t1) / reps
+    assert int(hcount[0]) == count and sres.sum == res.sum
+    return e2e_s
 
 
 def time_op(fn, reps, stream):
@@ -241,6 +287,9 @@ def main():
     t0 = time.time()
     col = Column.encode(x, SCALE, stream=stream)
     torch.cuda.synchronize()
+    if args.free_input:
+        del x
+        torch.cuda.empty_cache()
     info = col.info
     nw = (n + 31) // 32
     words = torch.empty(nw, dtype=torch.int32, device="cuda")
@@ -254,11 +303,11 @@ def main():
 
     # per-kernel events inside the timed region (on the launching stream)
     ev_f0, ev_f1, ev_s1 = [], [], []
+    clocks = Clocks(local) if rank == 0 else None
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     barrier(world)
-    clocks = Clocks(local) if rank == 0 else None
     launches0 = capi.kernel_launches()
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
@@ -298,34 +347,18 @@ def main():
 
     # ---- e2e through the C ABI with host buffers --------------------------
     img_len = info.serialized_bytes
-    img = torch.empty(img_len, dtype=torch.uint8, pin_memory=True)
-    col.serialize(out=img.numpy())
-    hwords = torch.empty(nw, dtype=torch.int32, pin_memory=True)
-    hcount = np.zeros(1, dtype=np.uint64)
-
-    def e2e_step():
-        hc = C.c_void_p()
-        capi.check(L.buff_deserialize(img.data_ptr(), img_len, SCALE, 0, sh, C.byref(hc)))
-        capi.check(L.buff_range_filter(hc, pred, hwords.data_ptr(), hcount.ctypes.data, sh))
-        sres = capi.SumResult()
-        capi.check(L.buff_sum(hc, C.byref(sres), sh))
-        capi.check(L.buff_col_free_async(hc, sh))
-        return sres
-
-    for _ in range(max(2, args.warmup // 2)):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_reps = max(3, min(args.steps, 10))
-    t1 = time.perf_counter()
-    for _ in range(e2e_reps):
-        sres = e2e_step()
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t1) / e2e_reps
-    assert int(hcount[0]) == count and sres.sum == res.sum
+    e2e_s = None
+    if args.no_e2e:
+        e2e_line = None
+    else:
+        e2e_s = run_e2e(L, col, img_len, nw, pred, sh, count, res, args)
+        e2e_line = {"value": world * n / e2e_s / 1e9, "unit": "Gvalues/s",
+                    "h2d_bytes_per_step": img_len, "d2h_bytes_per_step": 4 * nw + 8 + 72,
+                    "ms_per_step": e2e_s * 1e3}
 
     # ---- per-op table (the measured rows of the single-column config) -------
     ops = {}
-    if not args.no_ops and rank == 0:
+    if not args.no_ops and rank == 0 and not args.free_input:
         xs = x[:: max(1, n >> 20)]
         for sel in (0.001, 0.01, 0.1, 0.5):
             p = float(torch.quantile(xs, 1.0 - sel).item())
@@ -360,7 +393,7 @@ def main():
                          "gb_s_alg": (16 * n + sum_bytes) / t / 1e9}
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu and not args.free_input:
         xs = x[:CPU_SAMPLE_ROWS].cpu().numpy()
         per_step, rows, _, _ = cpu_reference_line(args, xs, pred, 1, 3, 1)
         cpu = {"value": rows / per_step / 1e9, "unit": "Gvalues/s", "cores": 1, "kind": "port",
@@ -387,9 +420,7 @@ def main():
                                 "unit": "GB/s", "frac": roof_filt / peak,
                                 "traffic": ncu_traffic("k_filter"),
                                 "alg_bytes_per_launch": filt_bytes},
-            "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Gvalues/s",
-                    "h2d_bytes_per_step": img_len, "d2h_bytes_per_step": 4 * nw + 8 + 72,
-                    "ms_per_step": e2e_s * 1e3},
+            "e2e": e2e_line,
             "gpu_launches": launches,
             "clocks": clk,
             "cpu_baseline": cpu,

@@ -562,6 +562,9 @@ int buff_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_
     if (c->k && c->n)
       CK(cudaMemcpy2DAsync(c->slices, c->stride, bytes + 20, c->n, c->n, c->k, cudaMemcpyDefault,
                            s));
+    // padding rows of every slice hold the flipped zero byte (what encode writes)
+    if (c->k && c->stride > c->n)
+      CK(cudaMemset2DAsync(c->slices + c->n, c->stride, 0x80, c->stride - c->n, c->k, s));
     CK(cudaMemsetAsync(c->tail, 0, c->tail_alloc, s));
     if (c->tail_bytes)
       CK(cudaMemcpyAsync(c->tail, bytes + 20 + (uint64_t)c->k * c->n, c->tail_bytes,

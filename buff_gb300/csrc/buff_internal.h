@@ -15,7 +15,7 @@
 // `tail` holds the r-bit packed remainder, LSB-first, byte-identical to
 // BitPack::write_bits (methods/bit_packing.rs:106-135); for fixed_len < 8 it
 // holds the whole packed code (k == 0, r == fixed_len).  Padding rows beyond
-// n are zero in the tail and arbitrary in the slices.
+// n are zero in the tail and hold the flipped zero byte 0x80 in the slices.
 struct buff_col {
   int64_t base;
   uint32_t n;
@@ -78,6 +78,8 @@ cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStr
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t s);
 cudaError_t launch_fill_words(uint32_t *words, uint32_t n, uint32_t value,
                               unsigned long long *count, cudaStream_t s);
+// Sums of the first k_used slices and of the packed tail read as `tail_bits`-bit
+// fields (tail_bits == 0: no tail).  Slice padding must hold 0x80.
 cudaError_t launch_sum(const buff_col *c, uint32_t k_used, uint32_t tail_bits,
                        unsigned long long *d_partials, cudaStream_t s);
 cudaError_t launch_max(const buff_col *c, unsigned long long *d_max, cudaStream_t s);

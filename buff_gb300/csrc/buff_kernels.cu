@@ -24,6 +24,7 @@ std::atomic<uint64_t> g_launches{0};
 
 constexpr uint32_t H = 0x80808080u;
 constexpr int kThreads = 256;
+constexpr int kU = 4;  // independent 16-byte loads a lane keeps in flight in streaming loops
 
 __device__ __forceinline__ long long fetch_fixed(double v, int pexp, uint32_t dlen) {
   // PrecisionBound::fetch_fixed_aligned (methods/prec_double.rs:190-205):
@@ -75,7 +76,7 @@ __device__ __forceinline__ void cmp4(uint32_t w, const ByteTarget &t, uint32_t &
   uint32_t d0 = wh - t.lo0;  // MSB: a_lo >= t_lo
   // a_hi = ~w_hi.  t_hi = 1: a > t iff a_hi & (a_lo > t_lo); t_hi = 0: a_hi | (a_lo > t_lo).
   gt = ((t.th & ~w & d1) | (~t.th & (~w | d1))) & H;
-  eq = d0 & ~d1 & ~(w ^ t.th) & H;
+  eq = d0 & ~d1 & (w ^ t.th) & H;  // a_hi == t_hi  <=>  w_hi != t_hi
 }
 
 // Replaces the bytes of rows >= lim (0..16) in a 16-row vector by the flipped
@@ -213,21 +214,32 @@ __global__ void __launch_bounds__(kThreads) k_encode_reduce(const T *__restrict_
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t nth = gridDim.x * blockDim.x;
   const typename VO::V *xv = reinterpret_cast<const typename VO::V *>(x);
-  for (uint32_t v = tid; v < nv; v += nth) {
-    double e[E];
-    VO::get(__ldcs(xv + v), e);
-    uint32_t i0 = v * E;
-    long long prev = 0;
-    if (i0 > 0) prev = fetch_fixed((double)__ldg(x + i0 - 1), pexp, dlen);
+  for (uint32_t v0 = tid; v0 < nv; v0 += kU * nth) {
+    typename VO::V raw[kU];
 #pragma unroll
-    for (int j = 0; j < E; ++j) {
-      long long q = fetch_fixed(e[j], pexp, dlen);
-      uint32_t i = i0 + j;
-      mn = q < mn ? q : mn;
-      mx0 = q > mx0 ? q : mx0;
-      if (i >= from) mx1 = q > mx1 ? q : mx1;
-      if (i > 0 && q >= prev && (unsigned long long)i < brk) brk = i;
-      prev = q;
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t v = v0 + u * nth;
+      if (v < nv) raw[u] = __ldcs(xv + v);
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t v = v0 + u * nth;
+      if (v >= nv) break;
+      double e[E];
+      VO::get(raw[u], e);
+      const uint32_t i0 = v * E;
+      long long prev = 0;
+      if (i0 > 0) prev = fetch_fixed((double)__ldg(x + i0 - 1), pexp, dlen);
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        const long long q = fetch_fixed(e[j], pexp, dlen);
+        const uint32_t i = i0 + j;
+        mn = q < mn ? q : mn;
+        mx0 = q > mx0 ? q : mx0;
+        if (i >= from) mx1 = q > mx1 ? q : mx1;
+        if (i > 0 && q >= prev && (unsigned long long)i < brk) brk = i;
+        prev = q;
+      }
     }
   }
   for (uint32_t i = nv * E + tid; i < n; i += nth) {  // ragged end
@@ -395,11 +407,42 @@ __global__ void __launch_bounds__(kThreads) k_encode_scatter(
 // eq &= eq_j), then the packed tail.  Rows >= full_rows stay clear, which
 // reproduces the reference's 32-byte SIMD loop that never reaches the rows
 // after the last full 32-row block.
+// Candidate refinement of one 16-row vector (rows whose prefix equals the
+// target so far): the remaining slices, then the packed tail.  Kept out of
+// line: it runs for few vectors and would otherwise inflate the streaming
+// loop's registers.
+__device__ __noinline__ void refine_candidates(const uint8_t *__restrict__ slices, size_t stride,
+                                               uint32_t k_used, unsigned long long tb,
+                                               const uint8_t *__restrict__ tail, uint32_t r,
+                                               uint32_t ttail, uint32_t row0, uint32_t &gt,
+                                               uint32_t &eq) {
+  for (uint32_t j = 1; j < k_used && eq; ++j) {
+    uint32_t gj, ej;
+    cmp16(ld_cand(slices + j * stride + row0), make_target((uint32_t)(tb >> (8 * j)) & 0xFFu), gj,
+          ej);
+    gt |= eq & gj;
+    eq &= ej;
+  }
+  if (r && eq) {
+    unsigned long long lo, hi;
+    load_tail16(tail, row0 >> 4, r, lo, hi);
+    uint32_t gtt = 0, eqt = 0;
+    for (uint32_t i = 0; i < 16; ++i) {
+      const uint32_t f = field16(lo, hi, i, r);
+      gtt |= (uint32_t)(f > ttail) << i;
+      eqt |= (uint32_t)(f == ttail) << i;
+    }
+    gt |= eq & gtt;
+    eq &= eqt;
+  }
+}
+
+template <bool IS_RANGE>
 __global__ void __launch_bounds__(kThreads) k_filter(FilterArgs a) {
   const uint32_t lane = threadIdx.x & 31;
-  const uint32_t nvec = (a.n + 15) / 16;
-  const uint32_t nchunks = (nvec + 31) / 32;
   const uint32_t nwords = (a.n + 31) / 32;
+  const uint32_t step_rows = kU * kRowChunk;
+  const uint32_t nsteps = (a.n + step_rows - 1) / step_rows;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   unsigned long long tb = 0;
@@ -407,50 +450,51 @@ __global__ void __launch_bounds__(kThreads) k_filter(FilterArgs a) {
   for (int j = 0; j < 8; ++j) tb |= (unsigned long long)a.tbyte[j] << (8 * j);
   const ByteTarget tg0 = make_target((uint32_t)(tb & 0xFFu));
   unsigned long long cnt = 0;
-  for (uint32_t ch = warp; ch < nchunks; ch += nwarps) {
-    const uint32_t v = ch * 32 + lane;
-    const uint32_t row0 = v * 16;
-    uint32_t res = 0;
-    if (row0 < a.n) {
-      uint32_t gt, eq;
-      if (a.k_used) {
-        uint4 d = ld_stream(a.slices + row0);
-        cmp16(d, tg0, gt, eq);
-        for (uint32_t j = 1; j < a.k_used && eq; ++j) {
-          uint32_t gj, ej;
-          cmp16(ld_cand(a.slices + j * a.stride + row0), make_target((uint32_t)(tb >> (8 * j)) & 0xFFu), gj, ej);
-          gt |= eq & gj;
-          eq &= ej;
-        }
-      } else {
-        gt = 0;
-        eq = 0xFFFFu;
-      }
-      if (a.r && eq) {
-        unsigned long long lo, hi;
-        load_tail16(a.tail, v, a.r, lo, hi);
-        uint32_t gtt = 0, eqt = 0;
-        for (uint32_t i = 0; i < 16; ++i) {
-          const uint32_t f = field16(lo, hi, i, a.r);
-          gtt |= (uint32_t)(f > a.ttail) << i;
-          eqt |= (uint32_t)(f == a.ttail) << i;
-        }
-        gt |= eq & gtt;
-        eq &= eqt;
-      } else if (a.tail_only_eq) {
-        eq = 0;
-      }
-      res = a.is_range ? gt : eq;
-      const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
-      if (lim < 16) res &= (1u << lim) - 1u;
+  for (uint32_t st = warp; st < nsteps; st += nwarps) {
+    const uint32_t base = st * step_rows;
+    uint4 d[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t row0 = base + u * kRowChunk + lane * 16;
+      if (a.k_used && row0 < a.n)
+        d[u] = ld_stream(a.slices + row0);
+      else
+        d[u] = make_uint4(0, 0, 0, 0);
     }
-    const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
-    if (!(lane & 1)) {
-      const uint32_t word = v >> 1;
-      if (word < nwords) {
-        const uint32_t wv = (res & 0xFFFFu) | (hi16 << 16);
-        __stcs(a.words + word, wv);
-        cnt += __popc(wv);
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t row0 = base + u * kRowChunk + lane * 16;
+      uint32_t res = 0;
+      if (row0 < a.n) {
+        uint32_t gt = 0, eq;
+        if (a.k_used) {
+          uint32_t g0 = 0, e0, g1 = 0, e1, g2 = 0, e2, g3 = 0, e3;
+          cmp4(d[u].x, tg0, g0, e0);
+          cmp4(d[u].y, tg0, g1, e1);
+          cmp4(d[u].z, tg0, g2, e2);
+          cmp4(d[u].w, tg0, g3, e3);
+          if (IS_RANGE) gt = msb4(g0) | (msb4(g1) << 4) | (msb4(g2) << 8) | (msb4(g3) << 12);
+          eq = (e0 | e1 | e2 | e3) ? (msb4(e0) | (msb4(e1) << 4) | (msb4(e2) << 8) | (msb4(e3) << 12)) : 0u;
+        } else {
+          eq = 0xFFFFu;
+        }
+        if (eq && (a.k_used > 1 || a.r)) {
+          refine_candidates(a.slices, a.stride, a.k_used, tb, a.tail, a.r, a.ttail, row0, gt, eq);
+        } else if (a.tail_only_eq && !a.r) {
+          eq = 0;
+        }
+        res = IS_RANGE ? gt : eq;
+        const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
+        if (lim < 16) res &= (1u << lim) - 1u;
+      }
+      const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
+      if (!(lane & 1)) {
+        const uint32_t word = (base + u * kRowChunk) / 32 + (lane >> 1);
+        if (word < nwords) {
+          const uint32_t wv = (res & 0xFFFFu) | (hi16 << 16);
+          __stcs(a.words + word, wv);
+          cnt += __popc(wv);
+        }
       }
     }
   }
@@ -473,55 +517,85 @@ __global__ void k_fill_words(uint32_t *words, uint32_t n, uint32_t value,
 
 // ---------------------------------------------------------------- sum
 
-// byte_fixed_sum (compress/split_double.rs:2127-2208): per-slice sums of the
-// unflipped bytes and the sum of the r-bit tail fields, exact in u64.
-__global__ void __launch_bounds__(kThreads) k_sum(const uint8_t *__restrict__ slices,
-                                                  size_t stride, uint32_t k,
-                                                  const uint8_t *__restrict__ tail, uint32_t r,
-                                                  uint32_t n, unsigned long long *partials) {
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t nvec = (n + 15) / 16;
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t nth = gridDim.x * blockDim.x;
-  uint32_t acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (uint32_t v = tid; v < nvec; v += nth) {
-    const uint32_t row0 = v * 16;
-    const uint32_t lim = n - row0 < 16 ? n - row0 : 16u;
-#pragma unroll
-    for (uint32_t s = 0; s < 8; ++s) {
-      if (s < k) {
-        uint4 d = ld_stream(slices + s * stride + row0);
-        if (lim < 16) clear_padding(d, lim);
-        acc[s] = __dp4a(d.x ^ H, 0x01010101u, acc[s]);
-        acc[s] = __dp4a(d.y ^ H, 0x01010101u, acc[s]);
-        acc[s] = __dp4a(d.z ^ H, 0x01010101u, acc[s]);
-        acc[s] = __dp4a(d.w ^ H, 0x01010101u, acc[s]);
-      }
-    }
-    if (r) {
-      unsigned long long lo, hi;
-      load_tail16(tail, v, r, lo, hi);  // padding rows are zero in the tail
-      uint32_t t = 0;
-      for (uint32_t i = 0; i < lim; ++i) t += field16(lo, hi, i, r);
-      acc[8] += t;
-    }
+// Weighted popcount of one 32-bit word of a packed stream of `ts`-bit fields
+// whose first bit sits at stream bit `bit0`: sum over set bits b of
+// 2^((bit0 + b) mod ts).  (The sum of all fields of a stream only depends on
+// each bit's position mod ts, not on row boundaries.)
+__device__ __forceinline__ uint32_t wpopc(uint32_t w, uint32_t bit0, uint32_t ts) {
+  if (ts == 1) return __popc(w);
+  uint32_t pat = 0;  // bits 0, ts, 2ts, ...
+  for (uint32_t j = 0; j < 32; j += ts) pat |= 1u << j;
+  const uint32_t phase = bit0 % ts;
+  uint32_t acc = 0;
+  for (uint32_t p = 0; p < ts; ++p) {
+    const uint32_t sh = (p + ts - phase) % ts;  // bits j with (phase + j) % ts == p
+    acc += (uint32_t)__popc(w & (pat << sh)) << p;
   }
+  return acc;
+}
+
+// byte_fixed_sum (compress/split_double.rs:2127-2208): the per-slice sums of
+// the unflipped bytes and the sum of the packed tail fields, exact in u64.
+// Each slice is streamed as one flat array of `stride` bytes (padding rows
+// hold the flipped zero 0x80), and the tail as a flat bit stream of
+// n * ts bits, so every load is a coalesced 16-byte vector.
+__global__ void __launch_bounds__(kThreads) k_sum(const uint8_t *__restrict__ slices,
+                                                  size_t stride, uint32_t ks,
+                                                  const uint8_t *__restrict__ tail, uint32_t ts,
+                                                  unsigned long long tail_bits,
+                                                  unsigned long long *partials) {
   __shared__ unsigned long long s_acc[9];
   if (threadIdx.x < 9) s_acc[threadIdx.x] = 0;
   __syncthreads();
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nth = gridDim.x * blockDim.x;
+  const uint32_t nv = (uint32_t)(stride / 16);
+  for (uint32_t s = 0; s < ks; ++s) {
+    const uint8_t *sl = slices + (size_t)s * stride;
+    uint32_t acc = 0;
+    for (uint32_t v0 = tid; v0 < nv; v0 += kU * nth) {
+      uint4 d[kU];
 #pragma unroll
-  for (uint32_t s = 0; s < 9; ++s) {
-    if (s < k || (s == 8 && r)) {
-      unsigned long long v = warp_sum_ull(acc[s]);
-      if (lane == 0 && v) atomicAdd(&s_acc[s], v);
+      for (int u = 0; u < kU; ++u) {
+        const uint32_t v = v0 + u * nth;
+        d[u] = v < nv ? ld_stream(sl + (size_t)v * 16) : make_uint4(H, H, H, H);
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        acc = __dp4a(d[u].x ^ H, 0x01010101u, acc);
+        acc = __dp4a(d[u].y ^ H, 0x01010101u, acc);
+        acc = __dp4a(d[u].z ^ H, 0x01010101u, acc);
+        acc = __dp4a(d[u].w ^ H, 0x01010101u, acc);
+      }
     }
+    const unsigned long long w = warp_sum_ull(acc);
+    if (lane == 0 && w) atomicAdd(&s_acc[s], w);
+  }
+  if (ts) {
+    const unsigned long long nbytes = (tail_bits + 7) / 8;
+    const uint32_t ntv = (uint32_t)((nbytes + 15) / 16);
+    unsigned long long acc = 0;
+    for (uint32_t v = tid; v < ntv; v += nth) {
+      uint4 d = *reinterpret_cast<const uint4 *>(tail + (size_t)v * 16);
+      const uint32_t *w = reinterpret_cast<const uint32_t *>(&d);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const unsigned long long b0 = (unsigned long long)v * 128 + 32 * q;
+        uint32_t word = w[q];
+        if (b0 >= tail_bits)
+          word = 0;
+        else if (b0 + 32 > tail_bits)
+          word &= (1u << (uint32_t)(tail_bits - b0)) - 1u;
+        acc += wpopc(word, (uint32_t)(b0 % ts), ts);
+      }
+    }
+    acc = warp_sum_ull(acc);
+    if (lane == 0 && acc) atomicAdd(&s_acc[8], acc);
   }
   __syncthreads();
-  if (threadIdx.x < 9) {
-    const uint32_t s = threadIdx.x;
-    if (s < k && s_acc[s]) atomicAdd(&partials[s], s_acc[s]);
-    if (s == 8 && r && s_acc[8]) atomicAdd(&partials[k], s_acc[8]);
-  }
+  if (threadIdx.x < ks && s_acc[threadIdx.x]) atomicAdd(&partials[threadIdx.x], s_acc[threadIdx.x]);
+  if (threadIdx.x == 8 && ts && s_acc[8]) atomicAdd(&partials[ks], s_acc[8]);
 }
 
 // ---------------------------------------------------------------- max
@@ -548,66 +622,87 @@ __device__ __forceinline__ unsigned long long code_at(const uint8_t *slices, siz
   return c;
 }
 
+// Largest full code among the rows of one 16-row vector whose leading byte is
+// `top` (out of line for the same reason as refine_candidates).
+__device__ __noinline__ unsigned long long max_in_vector(const uint8_t *__restrict__ slices,
+                                                         size_t stride, uint32_t k,
+                                                         const uint8_t *__restrict__ tail,
+                                                         uint32_t r, uint32_t n, uint32_t row0,
+                                                         uint4 d, uint32_t top) {
+  const uint8_t *db = reinterpret_cast<const uint8_t *>(&d);
+  unsigned long long m = 0;
+  for (uint32_t i = 0; i < 16 && row0 + i < n; ++i)
+    if ((uint32_t)(db[i] ^ 0x80u) == top) {
+      const unsigned long long c = code_at(slices, stride, k, tail, r, row0 + i);
+      m = c > m ? c : m;
+    }
+  return m;
+}
+
 // byte_fixed_max (compress/split_double.rs:3919-4105): the maximum stored
 // code.  Each warp keeps the best code it has seen; only lanes holding the
-// warp's largest leading byte, when that byte can still beat the warp's best,
-// gather the remaining slices and the tail.
+// warp's largest leading byte, when that byte can still reach the warp's
+// best, gather the remaining slices and the tail.
 __global__ void __launch_bounds__(kThreads) k_max(const uint8_t *__restrict__ slices, size_t stride,
                                                   uint32_t k, const uint8_t *__restrict__ tail,
                                                   uint32_t r, uint32_t fl, uint32_t n,
                                                   unsigned long long *out) {
   const uint32_t lane = threadIdx.x & 31;
-  const uint32_t nvec = (n + 15) / 16;
-  const uint32_t nchunks = (nvec + 31) / 32;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   unsigned long long best = 0;
   bool have = false;
-  for (uint32_t ch = warp; ch < nchunks; ch += nwarps) {
-    const uint32_t v = ch * 32 + lane;
-    const uint32_t row0 = v * 16;
-    if (k == 0) {  // packed codes only
-      unsigned long long m = 0;
+  if (k == 0) {  // packed codes only (fixed_len < 8)
+    const uint32_t nvec = (n + 15) / 16;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += gridDim.x * blockDim.x) {
+      unsigned long long lo, hi;
+      load_tail16(tail, v, r, lo, hi);
+      for (uint32_t i = 0; i < 16 && v * 16 + i < n; ++i) {
+        unsigned long long f = field16(lo, hi, i, r);
+        best = f > best ? f : best;
+      }
+    }
+    best = warp_max_ull(best);
+    if (lane == 0 && n) atomicMax(out, best);
+    return;
+  }
+  const uint32_t step_rows = kU * kRowChunk;
+  const uint32_t nsteps = (n + step_rows - 1) / step_rows;
+  for (uint32_t st = warp; st < nsteps; st += nwarps) {
+    const uint32_t base = st * step_rows;
+    uint4 d[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t row0 = base + u * kRowChunk + lane * 16;
       if (row0 < n) {
-        unsigned long long lo, hi;
-        load_tail16(tail, v, r, lo, hi);
-        for (uint32_t i = 0; i < 16 && row0 + i < n; ++i) {
-          unsigned long long f = field16(lo, hi, i, r);
-          m = f > m ? f : m;
-        }
+        d[u] = ld_stream(slices + row0);
+        if (n - row0 < 16) clear_padding(d[u], n - row0);
+      } else {
+        d[u] = make_uint4(H, H, H, H);
       }
-      m = warp_max_ull(m);
-      best = m > best ? m : best;
-      have = true;
-      continue;
     }
-    uint32_t mb = 0;
-    uint4 d = make_uint4(0, 0, 0, 0);
-    if (row0 < n) {
-      d = ld_stream(slices + row0);
-      if (n - row0 < 16) clear_padding(d, n - row0);
-      mb = max_byte16(d);
+    uint32_t mb[kU];
+    uint32_t lm = 0;
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      mb[u] = max_byte16(d[u]);
+      lm = mb[u] > lm ? mb[u] : lm;
     }
-    uint32_t wmb = mb;
-    for (int o = 16; o; o >>= 1) {
-      uint32_t x = __shfl_xor_sync(0xFFFFFFFFu, wmb, o);
-      wmb = x > wmb ? x : wmb;
-    }
+    const uint32_t wmb = __reduce_max_sync(0xFFFFFFFFu, lm);
     const uint32_t best_top = have ? (uint32_t)(best >> (fl - 8)) : 0u;
-    if (!have || wmb >= best_top) {
-      unsigned long long m = 0;
-      if (row0 < n && mb == wmb) {
-        const uint8_t *db = reinterpret_cast<const uint8_t *>(&d);
-        for (uint32_t i = 0; i < 16 && row0 + i < n; ++i)
-          if ((uint32_t)(db[i] ^ 0x80u) == wmb) {
-            unsigned long long c = code_at(slices, stride, k, tail, r, row0 + i);
-            m = c > m ? c : m;
-          }
+    if (have && wmb < best_top) continue;
+    unsigned long long m = 0;
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t row0 = base + u * kRowChunk + lane * 16;
+      if (row0 < n && mb[u] == wmb) {
+        const unsigned long long c = max_in_vector(slices, stride, k, tail, r, n, row0, d[u], wmb);
+        m = c > m ? c : m;
       }
-      m = warp_max_ull(m);
-      if (!have || m > best) best = m;
-      have = true;
     }
+    m = warp_max_ull(m);
+    if (!have || m > best) best = m;
+    have = true;
   }
   if (lane == 0 && have) atomicMax(out, best);
 }
@@ -641,61 +736,45 @@ __global__ void __launch_bounds__(kThreads) k_argmax(const uint8_t *__restrict__
 // ---------------------------------------------------------------- decode
 
 // buff_simd256_decode (compress/buff_simd.rs:3252-3357) and the
-// precision-limited decode (compress/split_double.rs:1612-1893).  `total` is
-// the number of leading code bits rebuilt; the reference walks its slices as
-// if the code were `total` bits wide, so with the quirk kept (mask == 0) the
-// value is (base + X) / 2^dlen with X the top `total` bits *not* shifted back,
-// and when total % 8 != 0 the tail bits are read with a stride of total % 8.
-// mask != 0 keeps the top `total` bits in place instead.
+// precision-limited decode (compress/split_double.rs:1612-1893).  KS leading
+// slices and `ts` packed bits per row are rebuilt; the reference walks its
+// slices as if the code were 8*KS+ts bits wide, so with the quirk kept
+// (keep == ~0) the value is (base + X) / 2^dlen with X those bits *not*
+// shifted back, and when ts != r the packed bits are read with a stride of ts.
+// The INTENDED form passes all bits and a `keep` mask instead.
+template <int KS>
 __global__ void __launch_bounds__(kThreads) k_decode(const uint8_t *__restrict__ slices,
-                                                     size_t stride, uint32_t k,
+                                                     size_t stride,
                                                      const uint8_t *__restrict__ tail, uint32_t r,
-                                                     uint32_t fl, uint32_t n, long long base,
-                                                     double scl, uint32_t total, int mask,
+                                                     uint32_t ts, uint32_t n, long long base,
+                                                     double scl, unsigned long long keep,
                                                      double *__restrict__ out) {
   extern __shared__ double dsm[];
   const uint32_t lane = threadIdx.x & 31;
   double *ws = dsm + (size_t)(threadIdx.x >> 5) * kRowChunk;
-  const uint32_t nvec = (n + 15) / 16;
-  const uint32_t nchunks = (nvec + 31) / 32;
+  const uint32_t nchunks = (n + kRowChunk - 1) / kRowChunk;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  // Which bits the walk reads: `ks` whole slices and `ts` tail bits per row.
-  uint32_t ks, ts, shift_back;
-  unsigned long long keep = ~0ull;
-  if (mask) {
-    ks = k;
-    ts = r;
-    shift_back = 0;
-    const uint32_t drop = fl - total;
-    keep = drop >= 64 ? 0ull : (~0ull << drop);
-  } else if (total < 8) {
-    ks = 0;
-    ts = total;  // packed reads straight after the header
-    shift_back = 0;
-  } else {
-    ks = total / 8;
-    ts = total % 8;
-    shift_back = 0;
-  }
-  (void)shift_back;
   for (uint32_t ch = warp; ch < nchunks; ch += nwarps) {
-    const uint32_t v = ch * 32 + lane;
-    const uint32_t row0 = v * 16;
+    const uint32_t row0 = ch * kRowChunk + lane * 16;
     unsigned long long c[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) c[i] = 0;
     if (row0 < n) {
-      for (uint32_t s = 0; s < ks; ++s) {
-        uint4 d = ld_stream(slices + s * stride + row0);
-        const uint32_t *w = reinterpret_cast<const uint32_t *>(&d);
+      uint4 d[KS > 0 ? KS : 1];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) c[i] = (c[i] << 8) | (((w[i >> 2] >> (8 * (i & 3))) & 0xFFu) ^ 0x80u);
+      for (int s = 0; s < KS; ++s) d[s] = ld_stream(slices + s * stride + row0);
+      unsigned long long lo = 0, hi = 0;
+      if (ts && ts == r) load_tail16(tail, row0 >> 4, r, lo, hi);
+#pragma unroll
+      for (int s = 0; s < KS; ++s) {
+        const uint32_t *w = reinterpret_cast<const uint32_t *>(&d[s]);
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          c[i] = (c[i] << 8) | (((w[i >> 2] >> (8 * (i & 3))) & 0xFFu) ^ 0x80u);
       }
       if (ts) {
         if (ts == r) {
-          unsigned long long lo, hi;
-          load_tail16(tail, v, r, lo, hi);
 #pragma unroll
           for (int i = 0; i < 16; ++i) c[i] = (c[i] << r) | field16(lo, hi, i, r);
         } else {  // the reference's stride-ts reads of the packed region
@@ -729,8 +808,6 @@ __global__ void __launch_bounds__(kThreads) k_decode(const uint8_t *__restrict__
 }
 
 int grid_for(const void *fn, int threads, size_t smem, int device) {
-  static thread_local int cache_dev = -1;
-  (void)cache_dev;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
   if (per_sm < 1) per_sm = 1;
@@ -833,11 +910,15 @@ cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStr
 
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
-  const uint32_t nchunks = ((a.n + 15) / 16 + 31) / 32;
-  int grid = grid_for((const void *)k_filter, kThreads, 0, cur_device());
-  const int need = (int)((nchunks + (kThreads / 32) - 1) / (kThreads / 32));
+  const void *fn = a.is_range ? (const void *)k_filter<true> : (const void *)k_filter<false>;
+  const uint32_t nsteps = (a.n + kU * kRowChunk - 1) / (kU * kRowChunk);
+  int grid = grid_for(fn, kThreads, 0, cur_device());
+  const int need = (int)((nsteps + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
-  k_filter<<<grid, kThreads, 0, s>>>(a);
+  if (a.is_range)
+    k_filter<true><<<grid, kThreads, 0, s>>>(a);
+  else
+    k_filter<false><<<grid, kThreads, 0, s>>>(a);
   count_launch();
   return cudaGetLastError();
 }
@@ -857,11 +938,12 @@ cudaError_t launch_sum(const buff_col *c, uint32_t k_used, uint32_t tail_bits,
                        unsigned long long *d_partials, cudaStream_t s) {
   if (c->n == 0) return cudaSuccess;
   int grid = grid_for((const void *)k_sum, kThreads, 0, c->device);
-  const uint32_t nvec = (c->n + 15) / 16;
-  const int need = (int)((nvec + kThreads - 1) / kThreads);
+  const size_t nv = c->stride / 16;
+  const int need = (int)((nv + kThreads - 1) / kThreads);
   if (grid > need) grid = need;
-  k_sum<<<grid, kThreads, 0, s>>>(c->slices, c->stride, k_used, c->tail, tail_bits, c->n,
-                                  d_partials);
+  if (grid < 1) grid = 1;
+  k_sum<<<grid, kThreads, 0, s>>>(c->slices, c->stride, k_used, c->tail, tail_bits,
+                                  (unsigned long long)c->n * tail_bits, d_partials);
   count_launch();
   return cudaGetLastError();
 }
@@ -869,8 +951,8 @@ cudaError_t launch_sum(const buff_col *c, uint32_t k_used, uint32_t tail_bits,
 cudaError_t launch_max(const buff_col *c, unsigned long long *d_max, cudaStream_t s) {
   if (c->n == 0) return cudaSuccess;
   int grid = grid_for((const void *)k_max, kThreads, 0, c->device);
-  const uint32_t nchunks = ((c->n + 15) / 16 + 31) / 32;
-  const int need = (int)((nchunks + (kThreads / 32) - 1) / (kThreads / 32));
+  const uint32_t nsteps = (c->n + kU * kRowChunk - 1) / (kU * kRowChunk);
+  const int need = (int)((nsteps + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
   k_max<<<grid, kThreads, 0, s>>>(c->slices, c->stride, c->k, c->tail, c->r, c->fixed_len, c->n,
                                   d_max);
@@ -890,25 +972,53 @@ cudaError_t launch_argmax(const buff_col *c, const unsigned long long *d_max, ui
   return cudaGetLastError();
 }
 
-cudaError_t launch_decode(const buff_col *c, uint32_t total, int intended_mask, double *out,
-                          cudaStream_t s) {
-  if (c->n == 0) return cudaSuccess;
+template <int KS>
+static cudaError_t decode_ks(const buff_col *c, uint32_t ts, unsigned long long keep, double *out,
+                             cudaStream_t s) {
   const size_t smem = (size_t)(kThreads / 32) * kRowChunk * sizeof(double);
-  const void *fn = (const void *)k_decode;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const void *fn = (const void *)k_decode<KS>;
   int grid = grid_for(fn, kThreads, smem, c->device);
-  const uint32_t nchunks = ((c->n + 15) / 16 + 31) / 32;
+  const uint32_t nchunks = (c->n + kRowChunk - 1) / kRowChunk;
   const int need = (int)((nchunks + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
-  const double scl = 1.0 / (double)(1ull << 0);
-  (void)scl;
   // 2^-dlen is exact; (base + X) * 2^-dlen equals the reference's division.
   double inv = 1.0;
   for (uint32_t i = 0; i < c->dlen; ++i) inv *= 0.5;
-  k_decode<<<grid, kThreads, smem, s>>>(c->slices, c->stride, c->k, c->tail, c->r, c->fixed_len,
-                                        c->n, c->base, inv, total, intended_mask, out);
+  k_decode<KS><<<grid, kThreads, smem, s>>>(c->slices, c->stride, c->tail, c->r, ts, c->n, c->base,
+                                            inv, keep, out);
   count_launch();
   return cudaGetLastError();
+}
+
+cudaError_t launch_decode(const buff_col *c, uint32_t total, int intended_mask, double *out,
+                          cudaStream_t s) {
+  if (c->n == 0) return cudaSuccess;
+  uint32_t ks, ts;
+  unsigned long long keep = ~0ull;
+  if (intended_mask) {
+    ks = c->k;
+    ts = c->r;
+    const uint32_t drop = c->fixed_len - total;
+    keep = drop >= 64 ? 0ull : (~0ull << drop);
+  } else if (total < 8) {
+    ks = 0;
+    ts = total;  // packed reads straight after the header
+  } else {
+    ks = total / 8;
+    ts = total % 8;
+  }
+  switch (ks) {
+    case 0: return decode_ks<0>(c, ts, keep, out, s);
+    case 1: return decode_ks<1>(c, ts, keep, out, s);
+    case 2: return decode_ks<2>(c, ts, keep, out, s);
+    case 3: return decode_ks<3>(c, ts, keep, out, s);
+    case 4: return decode_ks<4>(c, ts, keep, out, s);
+    case 5: return decode_ks<5>(c, ts, keep, out, s);
+    case 6: return decode_ks<6>(c, ts, keep, out, s);
+    case 7: return decode_ks<7>(c, ts, keep, out, s);
+    case 8: return decode_ks<8>(c, ts, keep, out, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace buffk
