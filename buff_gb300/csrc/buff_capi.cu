@@ -224,6 +224,17 @@ cudaError_t scratch(T **p, size_t count, cudaStream_t s) {
 
 // ---------------------------------------------------------------- encode
 
+cudaError_t reduce(const double *x, uint32_t n, uint32_t from, const buff_col *c, int keys,
+                   int find_brk, EncStats *d, cudaStream_t s) {
+  return buffk::launch_encode_reduce_f64(x, n, from, c->precision_exp, c->dlen, keys, find_brk, d,
+                                         s);
+}
+cudaError_t reduce(const float *x, uint32_t n, uint32_t from, const buff_col *c, int keys,
+                   int find_brk, EncStats *d, cudaStream_t s) {
+  return buffk::launch_encode_reduce_f32(x, n, from, c->precision_exp, c->dlen, keys, find_brk, d,
+                                         s);
+}
+
 template <typename T>
 int encode_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, cudaStream_t s,
                 buff_col **out) {
@@ -242,28 +253,31 @@ int encode_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, c
   c->n = n;
   c->dlen = (uint32_t)dl;
   T *staged = nullptr;
-  EncStats *part = nullptr;
-  long long *sfx = nullptr;
+  EncStats *dst = nullptr;
   const T *dx = values;
   EncStats st;
   memset(&st, 0, sizeof(st));
   int64_t mn = INT64_MAX, mx = INT64_MIN;
-  const int nb = 4 * buffk::num_sms(c->device);
   if (n > 0) {
     if (!is_device_ptr(values) || (reinterpret_cast<uintptr_t>(values) & 15)) {
       CK(scratch(&staged, n, s));
       CK(cudaMemcpyAsync(staged, values, (size_t)n * sizeof(T), cudaMemcpyDefault, s));
       dx = staged;
     }
-    CK(scratch(&part, (size_t)nb + 1, s));
-    if (sizeof(T) == 8)
-      CK(buffk::launch_encode_reduce_f64(reinterpret_cast<const double *>(dx), n, c->precision_exp,
-                                         c->dlen, part, nb, part + nb, s));
-    else
-      CK(buffk::launch_encode_reduce_f32(reinterpret_cast<const float *>(dx), n, c->precision_exp,
-                                         c->dlen, part, nb, part + nb, s));
-    CK(cudaMemcpyAsync(&st, part + nb, sizeof(st), cudaMemcpyDeviceToHost, s));
+    CK(scratch(&dst, 1, s));
+    // Min/max on order keys of the raw values; quantize every row instead when
+    // an extreme is non-finite or too large for the shift, or when small
+    // magnitudes wrap the shift (precision bound below 2^-dlen: 13-15 decimals).
+    int keys = c->precision_exp >= -(int)c->dlen ? 1 : 0;
+    CK(reduce(dx, n, 1, c, keys, 1, dst, s));
+    CK(cudaMemcpyAsync(&st, dst, sizeof(st), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (!st.ok) {
+      keys = 0;
+      CK(reduce(dx, n, 1, c, keys, 1, dst, s));
+      CK(cudaMemcpyAsync(&st, dst, sizeof(st), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    }
     mn = st.mn;
     if (intended) {
       mx = st.mx0;
@@ -276,17 +290,11 @@ int encode_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, c
       } else if (brk >= n) {
         mx = INT64_MIN;
       } else {
-        CK(scratch(&sfx, 1, s));
-        if (sizeof(T) == 8)
-          CK(buffk::launch_suffix_max_f64(reinterpret_cast<const double *>(dx), n, (uint32_t)brk,
-                                          c->precision_exp, c->dlen, sfx, s));
-        else
-          CK(buffk::launch_suffix_max_f32(reinterpret_cast<const float *>(dx), n, (uint32_t)brk,
-                                          c->precision_exp, c->dlen, sfx, s));
-        long long v = 0;
-        CK(cudaMemcpyAsync(&v, sfx, sizeof(v), cudaMemcpyDeviceToHost, s));
+        EncStats s2;
+        CK(reduce(dx, n, (uint32_t)brk, c, keys, 0, dst, s));
+        CK(cudaMemcpyAsync(&s2, dst, sizeof(s2), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
-        mx = v;
+        mx = s2.mx1;
       }
     }
   }
@@ -320,8 +328,7 @@ int encode_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, c
   }
 done:
   if (staged) cudaFreeAsync(staged, s);
-  if (part) cudaFreeAsync(part, s);
-  if (sfx) cudaFreeAsync(sfx, s);
+  if (dst) cudaFreeAsync(dst, s);
   if (rc != BUFF_OK) {
     cudaStreamSynchronize(s);
     free_col(c);

@@ -39,11 +39,13 @@ inline size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 
 // Encode statistics gathered by the reduce pass.
 struct EncStats {
-  long long mn;     // min over all rows
-  long long mx1;    // max over rows >= 1
+  long long mn;     // min over all rows (quantized)
+  long long mx1;    // max over rows >= from (quantized)
   long long mx0;    // max over all rows
   long long x0, x1; // first two quantized rows
   unsigned long long brk;  // first i >= 1 with x_i >= x_{i-1} (n if none)
+  int ok;           // 0: a key-mode extreme was non-finite or out of range
+  int pad;
 };
 
 struct FilterArgs {
@@ -63,16 +65,16 @@ struct FilterArgs {
 };
 
 // Per-stream launch helpers (buff_kernels.cu).  All return cudaError_t.
-cudaError_t launch_encode_reduce_f64(const double *x, uint32_t n, int32_t pexp, uint32_t dlen,
-                                     EncStats *d_part, int nblocks, EncStats *d_out,
+// min over all rows and max over rows >= from, quantized; keys = 1 reduces
+// on order keys of the raw values (check EncStats::ok), keys = 0 on the
+// quantized values.  find_brk also locates the end of the leading strictly
+// decreasing run.
+cudaError_t launch_encode_reduce_f64(const double *x, uint32_t n, uint32_t from, int32_t pexp,
+                                     uint32_t dlen, int keys, int find_brk, EncStats *d_out,
                                      cudaStream_t s);
-cudaError_t launch_encode_reduce_f32(const float *x, uint32_t n, int32_t pexp, uint32_t dlen,
-                                     EncStats *d_part, int nblocks, EncStats *d_out,
+cudaError_t launch_encode_reduce_f32(const float *x, uint32_t n, uint32_t from, int32_t pexp,
+                                     uint32_t dlen, int keys, int find_brk, EncStats *d_out,
                                      cudaStream_t s);
-cudaError_t launch_suffix_max_f64(const double *x, uint32_t n, uint32_t from, int32_t pexp,
-                                  uint32_t dlen, long long *d_out, cudaStream_t s);
-cudaError_t launch_suffix_max_f32(const float *x, uint32_t n, uint32_t from, int32_t pexp,
-                                  uint32_t dlen, long long *d_out, cudaStream_t s);
 cudaError_t launch_encode_scatter_f64(const double *x, const buff_col *c, cudaStream_t s);
 cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStream_t s);
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t s);

@@ -26,19 +26,6 @@ constexpr uint32_t H = 0x80808080u;
 constexpr int kThreads = 256;
 constexpr int kU = 4;  // independent 16-byte loads a lane keeps in flight in streaming loops
 
-__device__ __forceinline__ long long fetch_fixed(double v, int pexp, uint32_t dlen) {
-  // PrecisionBound::fetch_fixed_aligned (methods/prec_double.rs:190-205):
-  // IEEE bit manipulation; the shift amount wraps mod 64 like the reference's
-  // release build.
-  unsigned long long bdu = (unsigned long long)__double_as_longlong(v);
-  int exp = (int)((bdu >> 52) & 0x7FFu) - 1023;
-  if (exp < pexp) return 0;
-  int sh = 63 - exp - (int)dlen;
-  unsigned long long f = ((bdu << 11) | 0x8000000000000000ull) >> (sh & 63);
-  if (bdu >> 63) f = ~(f - 1ull);
-  return (long long)f;
-}
-
 __device__ __forceinline__ uint4 ld_stream(const uint8_t *p) {
   uint4 v;
   asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
@@ -159,13 +146,6 @@ __device__ __forceinline__ unsigned long long warp_max_ull(unsigned long long v)
   }
   return v;
 }
-__device__ __forceinline__ unsigned long long warp_min_ull(unsigned long long v) {
-  for (int o = 16; o; o >>= 1) {
-    unsigned long long x = __shfl_xor_sync(0xFFFFFFFFu, v, o);
-    v = x < v ? x : v;
-  }
-  return v;
-}
 __device__ __forceinline__ unsigned long long warp_sum_ull(unsigned long long v) {
   for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
   return v;
@@ -173,49 +153,91 @@ __device__ __forceinline__ unsigned long long warp_sum_ull(unsigned long long v)
 
 // ---------------------------------------------------------------- encode
 
+// Exact f32 -> f64 widening on the integer pipes (the FP64 pipe of this part
+// is narrow): returns the IEEE-754 binary64 bits of the binary32 value `fb`.
+__device__ __forceinline__ unsigned long long f32_to_f64_bits(uint32_t fb) {
+  const unsigned long long sgn = (unsigned long long)(fb >> 31) << 63;
+  const uint32_t e = (fb >> 23) & 0xFFu;
+  const uint32_t m = fb & 0x7FFFFFu;
+  if (e == 0xFFu)  // inf / NaN (NaN quieted, as the host conversion does)
+    return sgn | (0x7FFull << 52) | ((unsigned long long)m << 29) | (m ? (1ull << 51) : 0ull);
+  if (e == 0) {
+    if (m == 0) return sgn;
+    const int p = 31 - __clz(m);  // subnormal: m * 2^-149, leading bit p
+    return sgn | ((unsigned long long)(p - 149 + 1023) << 52) |
+           (((unsigned long long)m << (52 - p)) & ((1ull << 52) - 1ull));
+  }
+  return sgn | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+}
+
+// Raw binary64 bits of the input elements, E per 16-byte vector.
 template <typename T>
-struct VecOf;
+struct Elem;
 template <>
-struct VecOf<double> {
-  using V = double2;
+struct Elem<double> {
+  using V = ulonglong2;
   static constexpr int E = 2;
-  __device__ static void get(const V &v, double *o) {
-    o[0] = v.x;
-    o[1] = v.y;
+  __device__ static unsigned long long bits(const V &v, int j) { return j ? v.y : v.x; }
+  __device__ static unsigned long long one(const double *x, uint32_t i) {
+    return (unsigned long long)__double_as_longlong(__ldg(x + i));
   }
 };
 template <>
-struct VecOf<float> {
-  using V = float4;
+struct Elem<float> {
+  using V = uint4;
   static constexpr int E = 4;
-  __device__ static void get(const V &v, double *o) {
-    o[0] = v.x;
-    o[1] = v.y;
-    o[2] = v.z;
-    o[3] = v.w;
+  __device__ static unsigned long long bits(const V &v, int j) {
+    return f32_to_f64_bits(j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w);
+  }
+  __device__ static unsigned long long one(const float *x, uint32_t i) {
+    return f32_to_f64_bits((uint32_t)__float_as_uint(__ldg(x + i)));
   }
 };
 
-// Pass 1 of buff_simd256_encode (compress/buff_simd.rs:3139-3148): min over all
-// rows, max over rows >= from, max over all rows, and the first row i >= 1
-// with x_i >= x_{i-1}.  The reference's `else if` makes its max equal to the
-// max over rows after the leading strictly decreasing run (each row of that
-// run is a new minimum; afterwards every new minimum is below the running
-// max), so the host finishes the reference max from these fields.
-template <typename T>
+// fetch_fixed_aligned on raw binary64 bits.
+__device__ __forceinline__ long long fetch_bits(unsigned long long bdu, int pexp, uint32_t dlen) {
+  const int exp = (int)((bdu >> 52) & 0x7FFu) - 1023;
+  if (exp < pexp) return 0;
+  const int sh = 63 - exp - (int)dlen;
+  unsigned long long f = ((bdu << 11) | 0x8000000000000000ull) >> (sh & 63);
+  if (bdu >> 63) f = ~(f - 1ull);
+  return (long long)f;
+}
+
+// Signed-integer key with the order of the binary64 values (-0 < +0; NaNs
+// are extremal).  fetch_fixed_aligned is non-decreasing on finite values
+// whose shift does not wrap, so min/max can be taken on keys and quantized
+// once.
+__device__ __forceinline__ long long order_key(unsigned long long b) {
+  return (long long)(b ^ ((unsigned long long)((long long)b >> 63) >> 1));
+}
+__device__ __forceinline__ unsigned long long key_bits(long long k) {
+  const unsigned long long u = (unsigned long long)k;
+  return u ^ ((unsigned long long)(k >> 63) >> 1);
+}
+
+struct MinMax {
+  long long lo, hi;
+};
+
+// Pass 1 of buff_simd256_encode (compress/buff_simd.rs:3139-3148): the
+// column min over all rows and the max over rows >= from.  KEYS: on order
+// keys of the raw values (pure bandwidth); otherwise on the quantized values
+// (exact for every input, used when the key pass reports a non-finite or
+// out-of-range extreme).
+template <typename T, bool KEYS>
 __global__ void __launch_bounds__(kThreads) k_encode_reduce(const T *__restrict__ x, uint32_t n,
                                                             uint32_t from, int pexp,
-                                                            uint32_t dlen, EncStats *part) {
-  using VO = VecOf<T>;
-  constexpr int E = VO::E;
-  long long mn = LLONG_MAX, mx1 = LLONG_MIN, mx0 = LLONG_MIN;
-  unsigned long long brk = n;
+                                                            uint32_t dlen, MinMax *part) {
+  using EL = Elem<T>;
+  constexpr int E = EL::E;
+  long long lo = LLONG_MAX, hi = LLONG_MIN;
   const uint32_t nv = n / E;
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t nth = gridDim.x * blockDim.x;
-  const typename VO::V *xv = reinterpret_cast<const typename VO::V *>(x);
+  const typename EL::V *xv = reinterpret_cast<const typename EL::V *>(x);
   for (uint32_t v0 = tid; v0 < nv; v0 += kU * nth) {
-    typename VO::V raw[kU];
+    typename EL::V raw[kU];
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
       const uint32_t v = v0 + u * nth;
@@ -225,105 +247,122 @@ __global__ void __launch_bounds__(kThreads) k_encode_reduce(const T *__restrict_
     for (int u = 0; u < kU; ++u) {
       const uint32_t v = v0 + u * nth;
       if (v >= nv) break;
-      double e[E];
-      VO::get(raw[u], e);
       const uint32_t i0 = v * E;
-      long long prev = 0;
-      if (i0 > 0) prev = fetch_fixed((double)__ldg(x + i0 - 1), pexp, dlen);
 #pragma unroll
       for (int j = 0; j < E; ++j) {
-        const long long q = fetch_fixed(e[j], pexp, dlen);
-        const uint32_t i = i0 + j;
-        mn = q < mn ? q : mn;
-        mx0 = q > mx0 ? q : mx0;
-        if (i >= from) mx1 = q > mx1 ? q : mx1;
-        if (i > 0 && q >= prev && (unsigned long long)i < brk) brk = i;
-        prev = q;
+        const unsigned long long b = EL::bits(raw[u], j);
+        const long long q = KEYS ? order_key(b) : fetch_bits(b, pexp, dlen);
+        lo = q < lo ? q : lo;
+        if (i0 + j >= from) hi = q > hi ? q : hi;
       }
     }
   }
   for (uint32_t i = nv * E + tid; i < n; i += nth) {  // ragged end
-    long long q = fetch_fixed((double)x[i], pexp, dlen);
-    mn = q < mn ? q : mn;
-    mx0 = q > mx0 ? q : mx0;
-    if (i >= from) mx1 = q > mx1 ? q : mx1;
-    if (i > 0) {
-      long long p = fetch_fixed((double)x[i - 1], pexp, dlen);
-      if (q >= p && (unsigned long long)i < brk) brk = i;
-    }
+    const unsigned long long b = EL::one(x, i);
+    const long long q = KEYS ? order_key(b) : fetch_bits(b, pexp, dlen);
+    lo = q < lo ? q : lo;
+    if (i >= from) hi = q > hi ? q : hi;
   }
-  __shared__ long long s_mn[kThreads / 32], s_mx1[kThreads / 32], s_mx0[kThreads / 32];
-  __shared__ unsigned long long s_brk[kThreads / 32];
-  mn = warp_min<long long>(mn);
-  mx1 = warp_max_ll(mx1);
-  mx0 = warp_max_ll(mx0);
-  brk = warp_min_ull(brk);
+  __shared__ long long s_lo[kThreads / 32], s_hi[kThreads / 32];
+  lo = warp_min<long long>(lo);
+  hi = warp_max_ll(hi);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (l == 0) {
-    s_mn[w] = mn;
-    s_mx1[w] = mx1;
-    s_mx0[w] = mx0;
-    s_brk[w] = brk;
+    s_lo[w] = lo;
+    s_hi[w] = hi;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int i = 1; i < kThreads / 32; ++i) {
-      mn = s_mn[i] < mn ? s_mn[i] : mn;
-      mx1 = s_mx1[i] > mx1 ? s_mx1[i] : mx1;
-      mx0 = s_mx0[i] > mx0 ? s_mx0[i] : mx0;
-      brk = s_brk[i] < brk ? s_brk[i] : brk;
+      lo = s_lo[i] < lo ? s_lo[i] : lo;
+      hi = s_hi[i] > hi ? s_hi[i] : hi;
     }
-    EncStats s;
-    s.mn = mn;
-    s.mx1 = mx1;
-    s.mx0 = mx0;
-    s.brk = brk;
-    s.x0 = 0;
-    s.x1 = 0;
-    part[blockIdx.x] = s;
+    part[blockIdx.x].lo = lo;
+    part[blockIdx.x].hi = hi;
   }
 }
 
+// Combines the per-block extremes, quantizes them (key mode: flags `ok`
+// when both extremes are finite and their shift does not wrap, so that
+// quantizing commutes with min/max), and finds brk = the first row i >= 1
+// with x_i >= x_{i-1} (quantized) -- the end of the leading strictly
+// decreasing run that the reference's `else if` max skips.
 template <typename T>
-__global__ void k_encode_finalize(const T *__restrict__ x, uint32_t n, int pexp, uint32_t dlen,
-                                  const EncStats *part, int nparts, EncStats *out) {
-  long long mn = LLONG_MAX, mx1 = LLONG_MIN, mx0 = LLONG_MIN;
-  unsigned long long brk = n;
-  for (int i = threadIdx.x; i < nparts; i += 32) {
-    EncStats s = part[i];
-    mn = s.mn < mn ? s.mn : mn;
-    mx1 = s.mx1 > mx1 ? s.mx1 : mx1;
-    mx0 = s.mx0 > mx0 ? s.mx0 : mx0;
-    brk = s.brk < brk ? s.brk : brk;
+__global__ void __launch_bounds__(kThreads) k_encode_finalize(const T *__restrict__ x, uint32_t n,
+                                                              int pexp, uint32_t dlen,
+                                                              const MinMax *part, int nparts,
+                                                              int keys, int find_brk,
+                                                              EncStats *out) {
+  using EL = Elem<T>;
+  __shared__ long long s_lo[kThreads / 32], s_hi[kThreads / 32];
+  __shared__ unsigned int s_brk;
+  long long lo = LLONG_MAX, hi = LLONG_MIN;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+    lo = part[i].lo < lo ? part[i].lo : lo;
+    hi = part[i].hi > hi ? part[i].hi : hi;
   }
-  mn = warp_min<long long>(mn);
-  mx1 = warp_max_ll(mx1);
-  mx0 = warp_max_ll(mx0);
-  brk = warp_min_ull(brk);
+  lo = warp_min<long long>(lo);
+  hi = warp_max_ll(hi);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    s_lo[w] = lo;
+    s_hi[w] = hi;
+  }
+  if (threadIdx.x == 0) s_brk = n;
+  __syncthreads();
+  // brk: scan the leading rows one block-width at a time
+  if (find_brk) {
+    for (uint32_t b0 = 1; b0 < n; b0 += blockDim.x) {
+      const uint32_t i = b0 + threadIdx.x;
+      if (i < n) {
+        const long long q = fetch_bits(EL::one(x, i), pexp, dlen);
+        const long long p = fetch_bits(EL::one(x, i - 1), pexp, dlen);
+        if (q >= p) atomicMin(&s_brk, i);
+      }
+      __syncthreads();
+      if (s_brk < n) break;
+    }
+  }
   if (threadIdx.x == 0) {
-    EncStats s;
-    s.mn = mn;
-    s.mx1 = mx1;
-    s.mx0 = mx0;
-    s.brk = brk;
-    s.x0 = n > 0 ? fetch_fixed((double)x[0], pexp, dlen) : 0;
-    s.x1 = n > 1 ? fetch_fixed((double)x[1], pexp, dlen) : 0;
-    *out = s;
+    for (int i = 1; i < kThreads / 32; ++i) {
+      lo = s_lo[i] < lo ? s_lo[i] : lo;
+      hi = s_hi[i] > hi ? s_hi[i] : hi;
+    }
+    EncStats st;
+    st.ok = 1;
+    if (keys) {
+      const unsigned long long bl = key_bits(lo), bh = key_bits(hi);
+      const int el = (int)((bl >> 52) & 0x7FFu) - 1023, eh = (int)((bh >> 52) & 0x7FFu) - 1023;
+      const int lim = 63 - (int)dlen;
+      st.ok = (el <= lim && eh <= lim) ? 1 : 0;  // finite (exp 1024 fails) and no wrap
+      st.mn = fetch_bits(bl, pexp, dlen);
+      st.mx1 = hi == LLONG_MIN ? LLONG_MIN : fetch_bits(bh, pexp, dlen);
+    } else {
+      st.mn = lo;
+      st.mx1 = hi;
+    }
+    st.x0 = n > 0 ? fetch_bits(EL::one(x, 0), pexp, dlen) : 0;
+    st.x1 = n > 1 ? fetch_bits(EL::one(x, 1), pexp, dlen) : 0;
+    st.mx0 = n > 1 ? (st.x0 > st.mx1 ? st.x0 : st.mx1) : st.x0;
+    st.brk = s_brk;
+    *out = st;
   }
 }
 
 // Pass 2 of buff_simd256_encode (compress/buff_simd.rs:3181-3232): quantize,
 // split each code MSB-first into k flipped bytes and an r-bit tail.  Lane L
-// loads its part of the warp's 512 rows coalesced, the bytes are transposed
-// through shared memory so that every lane stores one 16-byte vector per
-// slice, and the tail of 16 rows is packed into 2r bytes.
+// loads its part of the warp's 512 rows coalesced; the code is shifted to the
+// top of a 64-bit word so that slice s is byte 7-s, the bytes of neighbouring
+// rows are gathered with byte permutes into shared memory, and every lane
+// then stores one 16-byte vector per slice and packs the tail of its 16 rows
+// into 2r bytes.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_encode_scatter(
     const T *__restrict__ x, uint32_t n, int pexp, uint32_t dlen, long long base, uint32_t fl,
     uint32_t k, uint32_t r, uint8_t *__restrict__ slices, size_t stride,
     uint8_t *__restrict__ tail) {
-  using VO = VecOf<T>;
-  constexpr int E = VO::E;
+  using EL = Elem<T>;
+  constexpr int E = EL::E;
   constexpr int LOADS = 16 / E;
   extern __shared__ uint8_t smem[];
   const uint32_t planes = k + (r ? 1u : 0u);
@@ -333,32 +372,52 @@ __global__ void __launch_bounds__(kThreads) k_encode_scatter(
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const unsigned long long rmask = r ? ((1ull << r) - 1ull) : 0ull;
+  const uint32_t up = 64u - fl;  // left shift that puts slice s at byte 7-s
   for (uint32_t ch = warp; ch < nchunks; ch += nwarps) {
     const uint32_t r0 = ch * kRowChunk;
+    typename EL::V raw[LOADS];
+#pragma unroll
+    for (int m = 0; m < LOADS; ++m) {
+      const uint32_t i0 = r0 + m * 32 * E + lane * E;
+      if (i0 + E <= n) raw[m] = __ldcs(reinterpret_cast<const typename EL::V *>(x + i0));
+    }
 #pragma unroll
     for (int m = 0; m < LOADS; ++m) {
       const uint32_t off = m * 32 * E + lane * E;  // row offset within the chunk
       const uint32_t i0 = r0 + off;
-      double e[E];
-      if (i0 + E <= n && (i0 % E) == 0) {
-        VO::get(__ldcs(reinterpret_cast<const typename VO::V *>(x + i0)), e);
-      } else {
-#pragma unroll
-        for (int j = 0; j < E; ++j) e[j] = (i0 + j < n) ? (double)x[i0 + j] : 0.0;
-      }
       unsigned long long c[E];
 #pragma unroll
-      for (int j = 0; j < E; ++j)
-        c[j] = (i0 + j < n) ? (unsigned long long)(fetch_fixed(e[j], pexp, dlen) - base) : 0ull;
-      for (uint32_t s = 0; s < k; ++s) {
-        const uint32_t sh = fl - 8u * (s + 1u);
-        uint32_t packed = 0;
+      for (int j = 0; j < E; ++j) {
+        unsigned long long b = 0;
+        if (i0 + E <= n)
+          b = EL::bits(raw[m], j);
+        else if (i0 + j < n)
+          b = EL::one(x, i0 + j);
+        c[j] = (i0 + j < n) ? (unsigned long long)(fetch_bits(b, pexp, dlen) - base) : 0ull;
+      }
+      if (k) {
+        uint32_t hw[E], lw[E];
 #pragma unroll
-        for (int j = 0; j < E; ++j) packed |= (uint32_t)(((uint8_t)(c[j] >> sh)) ^ 0x80u) << (8 * j);
-        if (E == 2)
-          *reinterpret_cast<uint16_t *>(ws + s * kRowChunk + off) = (uint16_t)packed;
-        else
-          *reinterpret_cast<uint32_t *>(ws + s * kRowChunk + off) = packed;
+        for (int j = 0; j < E; ++j) {
+          const unsigned long long a = (c[j] << up) ^ 0x8080808080808080ull;
+          hw[j] = (uint32_t)(a >> 32);
+          lw[j] = (uint32_t)a;
+        }
+        for (uint32_t sl = 0; sl < k; ++sl) {
+          const bool in_hi = sl < 4;
+          const uint32_t b = in_hi ? 3u - sl : 7u - sl;  // byte within the 32-bit half
+          const uint32_t sel = b | ((4u + b) << 4);
+          if (E == 2) {
+            const uint32_t v = __byte_perm(in_hi ? hw[0] : lw[0], in_hi ? hw[1] : lw[1], sel);
+            *reinterpret_cast<uint16_t *>(ws + sl * kRowChunk + off) = (uint16_t)v;
+          } else {
+            const uint32_t v01 = __byte_perm(in_hi ? hw[0] : lw[0], in_hi ? hw[1] : lw[1], sel);
+            const uint32_t v23 = __byte_perm(in_hi ? hw[2 % E] : lw[2 % E],
+                                             in_hi ? hw[3 % E] : lw[3 % E], sel);
+            *reinterpret_cast<uint32_t *>(ws + sl * kRowChunk + off) =
+                __byte_perm(v01, v23, 0x5410);
+          }
+        }
       }
       if (r) {
         uint32_t packed = 0;
@@ -371,9 +430,9 @@ __global__ void __launch_bounds__(kThreads) k_encode_scatter(
       }
     }
     __syncwarp();
-    for (uint32_t s = 0; s < k; ++s) {
-      uint4 v = *reinterpret_cast<const uint4 *>(ws + s * kRowChunk + lane * 16);
-      __stcs(reinterpret_cast<uint4 *>(slices + s * stride + r0 + lane * 16), v);
+    for (uint32_t sl = 0; sl < k; ++sl) {
+      uint4 v = *reinterpret_cast<const uint4 *>(ws + sl * kRowChunk + lane * 16);
+      __stcs(reinterpret_cast<uint4 *>(slices + sl * stride + r0 + lane * 16), v);
     }
     if (r) {
       uint4 v = *reinterpret_cast<const uint4 *>(ws + k * kRowChunk + lane * 16);
@@ -437,70 +496,123 @@ __device__ __noinline__ void refine_candidates(const uint8_t *__restrict__ slice
   }
 }
 
+// One 16-row vector of slice 0 (4 words of flipped bytes) against the target:
+// the 16-bit gt mask (row order) and whether any row equals the target byte.
+__device__ __forceinline__ uint32_t gt16_eqany(const uint4 &d, const ByteTarget &t,
+                                               uint32_t &eqm0, uint32_t &eqm1, uint32_t &eqm2,
+                                               uint32_t &eqm3) {
+  uint32_t g0, g1, g2, g3;
+  cmp4(d.x, t, g0, eqm0);
+  cmp4(d.y, t, g1, eqm1);
+  cmp4(d.z, t, g2, eqm2);
+  cmp4(d.w, t, g3, eqm3);
+  return msb4(g0) | (msb4(g1) << 4) | (msb4(g2) << 8) | (msb4(g3) << 12);
+}
+
+__device__ __forceinline__ uint32_t gather16(uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3) {
+  return msb4(m0) | (msb4(m1) << 4) | (msb4(m2) << 8) | (msb4(m3) << 12);
+}
+
+// The result bits of one 16-row vector whose rows are all below full_rows.
 template <bool IS_RANGE>
-__global__ void __launch_bounds__(kThreads) k_filter(FilterArgs a) {
+__device__ __forceinline__ uint32_t filter_vec(const FilterArgs &a, const uint4 &d,
+                                               const ByteTarget &tg0, unsigned long long tb,
+                                               uint32_t row0) {
+  uint32_t e0, e1, e2, e3;
+  uint32_t gt = 0;
+  if (IS_RANGE)
+    gt = gt16_eqany(d, tg0, e0, e1, e2, e3);
+  else {
+    uint32_t g;
+    cmp4(d.x, tg0, g, e0);
+    cmp4(d.y, tg0, g, e1);
+    cmp4(d.z, tg0, g, e2);
+    cmp4(d.w, tg0, g, e3);
+  }
+  if (!(e0 | e1 | e2 | e3)) return IS_RANGE ? gt : 0u;
+  uint32_t eq = gather16(e0, e1, e2, e3);
+  if (a.k_used > 1 || a.r)
+    refine_candidates(a.slices, a.stride, a.k_used, tb, a.tail, a.r, a.ttail, row0, gt, eq);
+  else if (a.tail_only_eq)
+    eq = 0;
+  return IS_RANGE ? gt : eq;
+}
+
+// buff_simd_range_filter / buff_simd_equal_filter (compress/buff_simd.rs:
+// 3361-3733) and their fused `_with_slice` forms (:3736-4025).  For every
+// 16-row vector: compare slice 0 to the target byte; while some rows still
+// equal the target prefix, compare the next slice (gt |= eq & gt_j,
+// eq &= eq_j), then the packed tail.  Rows >= full_rows stay clear, which
+// reproduces the reference's 32-byte SIMD loop that never reaches the rows
+// after the last full 32-row block.  Warps stream 2048-row steps (4 loads of
+// 16 bytes in flight per lane); steps wholly below full_rows take the lean
+// path, the last partial step and fixed_len < 8 columns the general one.
+template <bool IS_RANGE>
+__global__ void __launch_bounds__(kThreads, 5) k_filter(FilterArgs a) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwords = (a.n + 31) / 32;
   const uint32_t step_rows = kU * kRowChunk;
   const uint32_t nsteps = (a.n + step_rows - 1) / step_rows;
+  const uint32_t nfast = a.k_used ? a.full_rows / step_rows : 0u;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   unsigned long long tb = 0;
 #pragma unroll
   for (int j = 0; j < 8; ++j) tb |= (unsigned long long)a.tbyte[j] << (8 * j);
   const ByteTarget tg0 = make_target((uint32_t)(tb & 0xFFu));
-  unsigned long long cnt = 0;
-  for (uint32_t st = warp; st < nsteps; st += nwarps) {
+  uint32_t cnt = 0;
+  const uint8_t *s0 = a.slices + lane * 16;
+  uint32_t *wout = a.words + (lane >> 1);
+  for (uint32_t st = warp; st < nfast; st += nwarps) {
     const uint32_t base = st * step_rows;
     uint4 d[kU];
 #pragma unroll
-    for (int u = 0; u < kU; ++u) {
-      const uint32_t row0 = base + u * kRowChunk + lane * 16;
-      if (a.k_used && row0 < a.n)
-        d[u] = ld_stream(a.slices + row0);
-      else
-        d[u] = make_uint4(0, 0, 0, 0);
-    }
+    for (int u = 0; u < kU; ++u) d[u] = ld_stream(s0 + base + u * kRowChunk);
 #pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t res = filter_vec<IS_RANGE>(a, d[u], tg0, tb, base + u * kRowChunk + lane * 16);
+      const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
+      const uint32_t wv = (res & 0xFFFFu) | (hi16 << 16);
+      if (!(lane & 1)) {
+        __stcs(wout + (base + u * kRowChunk) / 32, wv);
+        cnt += __popc(wv);
+      }
+    }
+  }
+  for (uint32_t st = nfast + warp; st < nsteps; st += nwarps) {
+    const uint32_t base = st * step_rows;
+#pragma unroll 1
     for (int u = 0; u < kU; ++u) {
       const uint32_t row0 = base + u * kRowChunk + lane * 16;
       uint32_t res = 0;
       if (row0 < a.n) {
-        uint32_t gt = 0, eq;
+        uint32_t gt = 0, eq = 0xFFFFu;
         if (a.k_used) {
-          uint32_t g0 = 0, e0, g1 = 0, e1, g2 = 0, e2, g3 = 0, e3;
-          cmp4(d[u].x, tg0, g0, e0);
-          cmp4(d[u].y, tg0, g1, e1);
-          cmp4(d[u].z, tg0, g2, e2);
-          cmp4(d[u].w, tg0, g3, e3);
-          if (IS_RANGE) gt = msb4(g0) | (msb4(g1) << 4) | (msb4(g2) << 8) | (msb4(g3) << 12);
-          eq = (e0 | e1 | e2 | e3) ? (msb4(e0) | (msb4(e1) << 4) | (msb4(e2) << 8) | (msb4(e3) << 12)) : 0u;
-        } else {
-          eq = 0xFFFFu;
+          const uint4 d = ld_stream(a.slices + row0);
+          uint32_t e0, e1, e2, e3;
+          gt = gt16_eqany(d, tg0, e0, e1, e2, e3);
+          eq = gather16(e0, e1, e2, e3);
         }
-        if (eq && (a.k_used > 1 || a.r)) {
+        if (eq && (a.k_used > 1 || a.r))
           refine_candidates(a.slices, a.stride, a.k_used, tb, a.tail, a.r, a.ttail, row0, gt, eq);
-        } else if (a.tail_only_eq && !a.r) {
+        else if (a.tail_only_eq && !a.r)
           eq = 0;
-        }
         res = IS_RANGE ? gt : eq;
         const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
         if (lim < 16) res &= (1u << lim) - 1u;
       }
       const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
-      if (!(lane & 1)) {
-        const uint32_t word = (base + u * kRowChunk) / 32 + (lane >> 1);
-        if (word < nwords) {
-          const uint32_t wv = (res & 0xFFFFu) | (hi16 << 16);
-          __stcs(a.words + word, wv);
-          cnt += __popc(wv);
-        }
+      const uint32_t word = (base + u * kRowChunk) / 32 + (lane >> 1);
+      if (!(lane & 1) && word < nwords) {
+        const uint32_t wv = (res & 0xFFFFu) | (hi16 << 16);
+        __stcs(a.words + word, wv);
+        cnt += __popc(wv);
       }
     }
   }
   if (a.count) {
-    cnt = warp_sum_ull(cnt);
-    if (lane == 0 && cnt) atomicAdd(a.count, cnt);
+    const unsigned long long c = warp_sum_ull(cnt);
+    if (lane == 0 && c) atomicAdd(a.count, c);
   }
 }
 
@@ -623,27 +735,47 @@ __device__ __forceinline__ unsigned long long code_at(const uint8_t *slices, siz
 }
 
 // Largest full code among the rows of one 16-row vector whose leading byte is
-// `top` (out of line for the same reason as refine_candidates).
+// `top`: the remaining slices are read as 16-byte vectors and the tail as
+// the 2r bytes of these rows (out of line for the same reason as
+// refine_candidates).
 __device__ __noinline__ unsigned long long max_in_vector(const uint8_t *__restrict__ slices,
                                                          size_t stride, uint32_t k,
                                                          const uint8_t *__restrict__ tail,
                                                          uint32_t r, uint32_t n, uint32_t row0,
                                                          uint4 d, uint32_t top) {
   const uint8_t *db = reinterpret_cast<const uint8_t *>(&d);
-  unsigned long long m = 0;
-  for (uint32_t i = 0; i < 16 && row0 + i < n; ++i)
-    if ((uint32_t)(db[i] ^ 0x80u) == top) {
-      const unsigned long long c = code_at(slices, stride, k, tail, r, row0 + i);
-      m = c > m ? c : m;
-    }
-  return m;
+  uint32_t cand = 0;
+  for (uint32_t i = 0; i < 16; ++i)
+    if (row0 + i < n && (uint32_t)(db[i] ^ 0x80u) == top) cand |= 1u << i;
+  // Every surviving candidate shares the prefix built so far, so one prefix
+  // and a candidate mask describe the state (MSB-first progressive max).
+  unsigned long long prefix = top;
+  for (uint32_t s = 1; s < k; ++s) {
+    uint4 v = ld_cand(slices + s * stride + row0);
+    const uint8_t *vb = reinterpret_cast<const uint8_t *>(&v);
+    uint32_t best = 0;
+    for (uint32_t i = 0; i < 16; ++i)
+      if (cand >> i & 1u) best = max(best, (uint32_t)(vb[i] ^ 0x80u));
+    uint32_t nc = 0;
+    for (uint32_t i = 0; i < 16; ++i)
+      if ((cand >> i & 1u) && (uint32_t)(vb[i] ^ 0x80u) == best) nc |= 1u << i;
+    cand = nc;
+    prefix = (prefix << 8) | best;
+  }
+  if (!r) return prefix;
+  unsigned long long lo, hi;
+  load_tail16(tail, row0 >> 4, r, lo, hi);
+  uint32_t bt = 0;
+  for (uint32_t i = 0; i < 16; ++i)
+    if (cand >> i & 1u) bt = max(bt, field16(lo, hi, i, r));
+  return (prefix << r) | bt;
 }
 
 // byte_fixed_max (compress/split_double.rs:3919-4105): the maximum stored
 // code.  Each warp keeps the best code it has seen; only lanes holding the
 // warp's largest leading byte, when that byte can still reach the warp's
 // best, gather the remaining slices and the tail.
-__global__ void __launch_bounds__(kThreads) k_max(const uint8_t *__restrict__ slices, size_t stride,
+__global__ void __launch_bounds__(kThreads, 4) k_max(const uint8_t *__restrict__ slices, size_t stride,
                                                   uint32_t k, const uint8_t *__restrict__ tail,
                                                   uint32_t r, uint32_t fl, uint32_t n,
                                                   unsigned long long *out) {
@@ -735,6 +867,38 @@ __global__ void __launch_bounds__(kThreads) k_argmax(const uint8_t *__restrict__
 
 // ---------------------------------------------------------------- decode
 
+// `(v as f64) / 2^dlen` with integer operations only: round-to-nearest-even
+// of the 64-bit integer to a 53-bit significand, then the exponent lowered by
+// dlen (exact: the result stays a normal double for |v| >= 1 and dlen <= 64).
+// The FP64 pipe of this part is narrow, so the conversion is done on the
+// integer pipes.
+__device__ __forceinline__ double i64_to_f64_scaled(long long v, int dlen) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = v < 0 ? 0x8000000000000000ull : 0ull;
+  const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  int e = 63 - __clzll(a);  // a in [2^e, 2^(e+1))
+  unsigned long long m;
+  if (e <= 52) {
+    m = a << (52 - e);
+  } else {
+    const int sh = e - 52;
+    const unsigned long long rem = a & ((1ull << sh) - 1ull);
+    const unsigned long long half = 1ull << (sh - 1);
+    m = a >> sh;
+    if (rem > half || (rem == half && (m & 1ull))) {
+      m += 1ull;
+      if (m >> 53) {
+        m >>= 1;
+        e += 1;
+      }
+    }
+  }
+  const unsigned long long bits =
+      sgn | ((unsigned long long)(e - dlen + 1023) << 52) | (m & ((1ull << 52) - 1ull));
+  return __longlong_as_double((long long)bits);
+}
+
+
 // buff_simd256_decode (compress/buff_simd.rs:3252-3357) and the
 // precision-limited decode (compress/split_double.rs:1612-1893).  KS leading
 // slices and `ts` packed bits per row are rebuilt; the reference walks its
@@ -747,7 +911,7 @@ __global__ void __launch_bounds__(kThreads) k_decode(const uint8_t *__restrict__
                                                      size_t stride,
                                                      const uint8_t *__restrict__ tail, uint32_t r,
                                                      uint32_t ts, uint32_t n, long long base,
-                                                     double scl, unsigned long long keep,
+                                                     int dlen, unsigned long long keep,
                                                      double *__restrict__ out) {
   extern __shared__ double dsm[];
   const uint32_t lane = threadIdx.x & 31;
@@ -790,7 +954,7 @@ __global__ void __launch_bounds__(kThreads) k_decode(const uint8_t *__restrict__
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
       const unsigned long long x = c[i] & keep;
-      ws[lane * 16 + i] = (double)((long long)((unsigned long long)base + x)) * scl;
+      ws[lane * 16 + i] = i64_to_f64_scaled((long long)((unsigned long long)base + x), dlen);
     }
     __syncwarp();
 #pragma unroll
@@ -837,51 +1001,32 @@ void count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxe
 uint64_t launches() { return g_launches.load(std::memory_order_relaxed); }
 
 template <typename T>
-static cudaError_t encode_reduce_impl(const T *x, uint32_t n, uint32_t from, int32_t pexp,
-                                      uint32_t dlen, EncStats *d_part, int nblocks,
-                                      EncStats *d_out, cudaStream_t s) {
-  k_encode_reduce<T><<<nblocks, kThreads, 0, s>>>(x, n, from, pexp, dlen, d_part);
-  k_encode_finalize<T><<<1, 32, 0, s>>>(x, n, pexp, dlen, d_part, nblocks, d_out);
-  count_launch(2);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_encode_reduce_f64(const double *x, uint32_t n, int32_t pexp, uint32_t dlen,
-                                     EncStats *d_part, int nblocks, EncStats *d_out,
-                                     cudaStream_t s) {
-  return encode_reduce_impl<double>(x, n, 1, pexp, dlen, d_part, nblocks, d_out, s);
-}
-cudaError_t launch_encode_reduce_f32(const float *x, uint32_t n, int32_t pexp, uint32_t dlen,
-                                     EncStats *d_part, int nblocks, EncStats *d_out,
-                                     cudaStream_t s) {
-  return encode_reduce_impl<float>(x, n, 1, pexp, dlen, d_part, nblocks, d_out, s);
-}
-
-int encode_reduce_blocks() { return 4 * num_sms(cur_device()); }
-
-template <typename T>
-static cudaError_t suffix_max_impl(const T *x, uint32_t n, uint32_t from, int32_t pexp,
-                                   uint32_t dlen, long long *d_out, cudaStream_t s) {
-  // Reuses the reduce with `from`: mx1 of the result is max over rows >= from.
+static cudaError_t reduce_impl(const T *x, uint32_t n, uint32_t from, int32_t pexp, uint32_t dlen,
+                               int keys, int find_brk, EncStats *d_out, cudaStream_t s) {
   const int nb = 4 * num_sms(cur_device());
-  EncStats *tmp = nullptr;
-  cudaError_t e = cudaMallocAsync(&tmp, sizeof(EncStats) * (nb + 1), s);
+  MinMax *part = nullptr;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&part), sizeof(MinMax) * nb, s);
   if (e != cudaSuccess) return e;
-  k_encode_reduce<T><<<nb, kThreads, 0, s>>>(x, n, from, pexp, dlen, tmp);
-  k_encode_finalize<T><<<1, 32, 0, s>>>(x, n, pexp, dlen, tmp, nb, tmp + nb);
+  if (keys)
+    k_encode_reduce<T, true><<<nb, kThreads, 0, s>>>(x, n, from, pexp, dlen, part);
+  else
+    k_encode_reduce<T, false><<<nb, kThreads, 0, s>>>(x, n, from, pexp, dlen, part);
+  k_encode_finalize<T><<<1, kThreads, 0, s>>>(x, n, pexp, dlen, part, nb, keys, find_brk, d_out);
   count_launch(2);
-  e = cudaMemcpyAsync(d_out, &tmp[nb].mx1, sizeof(long long), cudaMemcpyDeviceToDevice, s);
-  cudaFreeAsync(tmp, s);
-  if (e != cudaSuccess) return e;
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  cudaFreeAsync(part, s);
+  return e;
 }
-cudaError_t launch_suffix_max_f64(const double *x, uint32_t n, uint32_t from, int32_t pexp,
-                                  uint32_t dlen, long long *d_out, cudaStream_t s) {
-  return suffix_max_impl<double>(x, n, from, pexp, dlen, d_out, s);
+
+cudaError_t launch_encode_reduce_f64(const double *x, uint32_t n, uint32_t from, int32_t pexp,
+                                     uint32_t dlen, int keys, int find_brk, EncStats *d_out,
+                                     cudaStream_t s) {
+  return reduce_impl<double>(x, n, from, pexp, dlen, keys, find_brk, d_out, s);
 }
-cudaError_t launch_suffix_max_f32(const float *x, uint32_t n, uint32_t from, int32_t pexp,
-                                  uint32_t dlen, long long *d_out, cudaStream_t s) {
-  return suffix_max_impl<float>(x, n, from, pexp, dlen, d_out, s);
+cudaError_t launch_encode_reduce_f32(const float *x, uint32_t n, uint32_t from, int32_t pexp,
+                                     uint32_t dlen, int keys, int find_brk, EncStats *d_out,
+                                     cudaStream_t s) {
+  return reduce_impl<float>(x, n, from, pexp, dlen, keys, find_brk, d_out, s);
 }
 
 template <typename T>
@@ -981,11 +1126,8 @@ static cudaError_t decode_ks(const buff_col *c, uint32_t ts, unsigned long long 
   const uint32_t nchunks = (c->n + kRowChunk - 1) / kRowChunk;
   const int need = (int)((nchunks + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
-  // 2^-dlen is exact; (base + X) * 2^-dlen equals the reference's division.
-  double inv = 1.0;
-  for (uint32_t i = 0; i < c->dlen; ++i) inv *= 0.5;
   k_decode<KS><<<grid, kThreads, smem, s>>>(c->slices, c->stride, c->tail, c->r, ts, c->n, c->base,
-                                            inv, keep, out);
+                                            (int)c->dlen, keep, out);
   count_launch();
   return cudaGetLastError();
 }
