@@ -38,6 +38,8 @@ def gen(kind, n, seed):
         m = min(n, 700)
         x[:m] = np.round(1000.0 - np.arange(m) * 0.5, 3)
         return x
+    if kind == "tiny":  # magnitudes whose quantizer shift wraps at 13-15 decimals
+        return np.round(rng.normal(0, 1e-6, n), 14)
     if kind == "clustered":  # many equal prefixes -> deep refinement
         base = np.round(rng.uniform(0, 1, n // 64 + 1), 4)
         return np.repeat(base, 64)[:n] + np.round(rng.uniform(0, 1e-3, n), 6)
@@ -49,7 +51,8 @@ CASES = [
     ("walk", 1, 1000), ("walk", 2, 1000), ("walk", 33, 10), ("walk_neg", 50000, 1000),
     ("narrow", 20000, 100), ("narrow", 777, 10), ("wide", 65536, 1000000),
     ("wide", 12345, 100000000), ("huge", 30000, 1000000000), ("updown", 10000, 1000),
-    ("decreasing", 5000, 1000), ("clustered", 70000, 1000000),
+    ("decreasing", 5000, 1000), ("clustered", 70000, 1000000), ("walk", 5000, 10 ** 13),
+    ("walk", 3000, 10 ** 12), ("tiny", 4000, 10 ** 14),
 ]
 
 
@@ -183,6 +186,25 @@ def test_f32_input(gpu, oracle):
     ref = oracle.encode(x, 1000)
     col = Column.encode(x, 1000)
     assert col.serialize() == ref
+
+
+def test_nonfinite_and_special_values(gpu, oracle):
+    from buff_gb300 import Column
+
+    x = gen("walk", 20000, 6)
+    x[[5, 700, 19999]] = [np.inf, -np.inf, np.nan]
+    x[[9, 10]] = [0.0, -0.0]
+    for scale in (10000, 10 ** 14):
+        try:
+            ref = oracle.encode(x, scale)
+        except oracle.OraclePanic:
+            continue
+        assert Column.encode(x, scale).serialize() == ref
+    xf = gen("walk", 9000, 7).astype(np.float32)
+    xf[[3, 4, 5]] = [np.float32(1e-42), np.float32(-3e-45), np.float32(-0.0)]
+    xf[[6, 7]] = [np.float32(np.inf), np.float32(-2.5e38)]
+    ref = oracle.encode(xf, 1000)
+    assert Column.encode(xf, 1000).serialize() == ref
 
 
 def test_empty_column(gpu, oracle):
