@@ -34,10 +34,6 @@ __device__ __forceinline__ uint4 ld_stream(const uint8_t *p) {
   return v;
 }
 
-__device__ __forceinline__ uint4 ld_cand(const uint8_t *p) {
-  return __ldg(reinterpret_cast<const uint4 *>(p));
-}
-
 // Per-slice compare constants for an unflipped target byte t.
 struct ByteTarget {
   uint32_t lo1;  // (t & 0x7f) + 1 in every byte
@@ -66,32 +62,6 @@ __device__ __forceinline__ void cmp4(uint32_t w, const ByteTarget &t, uint32_t &
   eq = d0 & ~d1 & (w ^ t.th) & H;  // a_hi == t_hi  <=>  w_hi != t_hi
 }
 
-// Replaces the bytes of rows >= lim (0..16) in a 16-row vector by the flipped
-// zero byte 0x80, so padding rows add nothing to sums or maxima.
-__device__ __forceinline__ void clear_padding(uint4 &d, uint32_t lim) {
-  uint32_t *w = reinterpret_cast<uint32_t *>(&d);
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const uint32_t lo = 4u * q;
-    const uint32_t keep = lim >= lo + 4 ? 0xFFFFFFFFu : (lim <= lo ? 0u : ((1u << (8 * (lim - lo))) - 1u));
-    w[q] = (w[q] & keep) | (H & ~keep);
-  }
-}
-
-__device__ __forceinline__ uint32_t msb4(uint32_t m) {  // MSBs of 4 bytes -> 4 bits
-  return (m * 0x00204081u) >> 28;
-}
-
-__device__ __forceinline__ void cmp16(const uint4 &d, const ByteTarget &t, uint32_t &gt,
-                                      uint32_t &eq) {
-  uint32_t g0, e0, g1, e1, g2, e2, g3, e3;
-  cmp4(d.x, t, g0, e0);
-  cmp4(d.y, t, g1, e1);
-  cmp4(d.z, t, g2, e2);
-  cmp4(d.w, t, g3, e3);
-  gt = msb4(g0) | (msb4(g1) << 4) | (msb4(g2) << 8) | (msb4(g3) << 12);
-  eq = msb4(e0) | (msb4(e1) << 4) | (msb4(e2) << 8) | (msb4(e3) << 12);
-}
 
 // The 16 r-bit tail fields of rows [16v, 16v+16): 2r bytes at byte 2r*v.
 __device__ __forceinline__ void load_tail16(const uint8_t *tail, uint32_t v, uint32_t r,
@@ -356,11 +326,11 @@ __global__ void __launch_bounds__(kThreads) k_encode_finalize(const T *__restric
 // rows are gathered with byte permutes into shared memory, and every lane
 // then stores one 16-byte vector per slice and packs the tail of its 16 rows
 // into 2r bytes.
-template <typename T>
+template <typename T, int K>
 __global__ void __launch_bounds__(kThreads) k_encode_scatter(
     const T *__restrict__ x, uint32_t n, int pexp, uint32_t dlen, long long base, uint32_t fl,
-    uint32_t k, uint32_t r, uint8_t *__restrict__ slices, size_t stride,
-    uint8_t *__restrict__ tail) {
+    uint32_t r, uint8_t *__restrict__ slices, size_t stride, uint8_t *__restrict__ tail) {
+  constexpr uint32_t k = K;
   using EL = Elem<T>;
   constexpr int E = EL::E;
   constexpr int LOADS = 16 / E;
@@ -395,7 +365,7 @@ __global__ void __launch_bounds__(kThreads) k_encode_scatter(
           b = EL::one(x, i0 + j);
         c[j] = (i0 + j < n) ? (unsigned long long)(fetch_bits(b, pexp, dlen) - base) : 0ull;
       }
-      if (k) {
+      if constexpr (K > 0) {
         uint32_t hw[E], lw[E];
 #pragma unroll
         for (int j = 0; j < E; ++j) {
@@ -403,6 +373,7 @@ __global__ void __launch_bounds__(kThreads) k_encode_scatter(
           hw[j] = (uint32_t)(a >> 32);
           lw[j] = (uint32_t)a;
         }
+#pragma unroll
         for (uint32_t sl = 0; sl < k; ++sl) {
           const bool in_hi = sl < 4;
           const uint32_t b = in_hi ? 3u - sl : 7u - sl;  // byte within the 32-bit half
@@ -430,11 +401,18 @@ __global__ void __launch_bounds__(kThreads) k_encode_scatter(
       }
     }
     __syncwarp();
-    for (uint32_t sl = 0; sl < k; ++sl) {
+#pragma unroll
+    for (int sl = 0; sl < K; ++sl) {
       uint4 v = *reinterpret_cast<const uint4 *>(ws + sl * kRowChunk + lane * 16);
       __stcs(reinterpret_cast<uint4 *>(slices + sl * stride + r0 + lane * 16), v);
     }
-    if (r) {
+    if (r == 1) {  // one bit per row: gather bit 0 of 8 bytes with one multiply
+      const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(ws + k * kRowChunk + lane * 16);
+      const uint32_t lo8 = (uint32_t)((v.x * 0x0102040810204080ull) >> 56);
+      const uint32_t hi8 = (uint32_t)((v.y * 0x0102040810204080ull) >> 56);
+      *reinterpret_cast<uint16_t *>(tail + (size_t)2 * ((r0 >> 4) + lane)) =
+          (uint16_t)(lo8 | (hi8 << 8));
+    } else if (r) {
       uint4 v = *reinterpret_cast<const uint4 *>(ws + k * kRowChunk + lane * 16);
       const uint8_t *b = reinterpret_cast<const uint8_t *>(&v);
       unsigned long long lo = 0, hi = 0;
@@ -466,28 +444,91 @@ __global__ void __launch_bounds__(kThreads) k_encode_scatter(
 // eq &= eq_j), then the packed tail.  Rows >= full_rows stay clear, which
 // reproduces the reference's 32-byte SIMD loop that never reaches the rows
 // after the last full 32-row block.
-// Candidate refinement of one 16-row vector (rows whose prefix equals the
+// 32 flipped slice bytes (rows row0..row0+31) in eight 32-bit words.
+struct Bytes32 {
+  uint32_t w[8];
+};
+
+// 256-bit non-allocating load (sm_100+; the address is 32-byte aligned).
+__device__ __forceinline__ Bytes32 ld_stream32(const uint8_t *p) {
+  Bytes32 b;
+  asm volatile("ld.global.nc.L1::no_allocate.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(b.w[0]), "=r"(b.w[1]), "=r"(b.w[2]), "=r"(b.w[3]), "=r"(b.w[4]),
+                 "=r"(b.w[5]), "=r"(b.w[6]), "=r"(b.w[7])
+               : "l"(p));
+  return b;
+}
+__device__ __forceinline__ Bytes32 ld_cand32(const uint8_t *p) {
+  const uint4 lo = __ldg(reinterpret_cast<const uint4 *>(p));
+  const uint4 hi = __ldg(reinterpret_cast<const uint4 *>(p + 16));
+  Bytes32 b;
+  b.w[0] = lo.x;
+  b.w[1] = lo.y;
+  b.w[2] = lo.z;
+  b.w[3] = lo.w;
+  b.w[4] = hi.x;
+  b.w[5] = hi.y;
+  b.w[6] = hi.z;
+  b.w[7] = hi.w;
+  return b;
+}
+
+// Byte MSBs of two words (4 rows each) -> 8 row-ordered bits in the low byte:
+// with c = (m0 >> 4) | m1 the MSBs sit at bits 8b+3 (row b) and 8b+7 (row
+// 4+b); multiplying by 2^29 + 2^22 + 2^15 + 2^8 moves exactly those eight bits,
+// without collisions, to bits 32..39 of the 64-bit product.
+__device__ __forceinline__ uint32_t msb8(uint32_t m0, uint32_t m1) {
+  return __umulhi((m0 >> 4) | m1, 0x20408100u);
+}
+// MSBs of eight words -> the 32-bit bitmap word (bit i = byte i).
+__device__ __forceinline__ uint32_t gather32(const uint32_t *m) {
+  const uint32_t a = __byte_perm(msb8(m[0], m[1]), msb8(m[2], m[3]), 0x0040);
+  const uint32_t b = __byte_perm(msb8(m[4], m[5]), msb8(m[6], m[7]), 0x0040);
+  return __byte_perm(a, b, 0x5410);
+}
+
+// Per-byte compares of flipped bytes w against an unflipped target whose top
+// bit is TH: MSB of each byte of the result.  (a = w ^ 0x80; a_lo = w_lo.)
+template <bool TH>
+__device__ __forceinline__ uint32_t gt4t(uint32_t w, uint32_t lo1) {
+  const uint32_t d1 = (w | H) - lo1;  // MSB: a_lo > t_lo
+  return TH ? (~w & d1 & H) : ((~w | d1) & H);
+}
+template <bool TH>
+__device__ __forceinline__ uint32_t eq4t(uint32_t w, uint32_t lo0, uint32_t lo1) {
+  const uint32_t wh = w | H;
+  return (wh - lo0) & ~(wh - lo1) & (TH ? ~w : w) & H;
+}
+
+// Candidate refinement of one 32-row block (rows whose prefix equals the
 // target so far): the remaining slices, then the packed tail.  Kept out of
-// line: it runs for few vectors and would otherwise inflate the streaming
+// line: it runs for few blocks and would otherwise inflate the streaming
 // loop's registers.
-__device__ __noinline__ void refine_candidates(const uint8_t *__restrict__ slices, size_t stride,
-                                               uint32_t k_used, unsigned long long tb,
-                                               const uint8_t *__restrict__ tail, uint32_t r,
-                                               uint32_t ttail, uint32_t row0, uint32_t &gt,
-                                               uint32_t &eq) {
+__device__ __noinline__ void refine32(const uint8_t *__restrict__ slices, size_t stride,
+                                      uint32_t k_used, unsigned long long tb,
+                                      const uint8_t *__restrict__ tail, uint32_t r, uint32_t ttail,
+                                      uint32_t row0, uint32_t &gt, uint32_t &eq) {
   for (uint32_t j = 1; j < k_used && eq; ++j) {
-    uint32_t gj, ej;
-    cmp16(ld_cand(slices + j * stride + row0), make_target((uint32_t)(tb >> (8 * j)) & 0xFFu), gj,
-          ej);
-    gt |= eq & gj;
-    eq &= ej;
+    const Bytes32 b = ld_cand32(slices + j * stride + row0);
+    const ByteTarget t = make_target((uint32_t)(tb >> (8 * j)) & 0xFFu);
+    uint32_t g[8], e[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) cmp4(b.w[q], t, g[q], e[q]);
+    gt |= eq & gather32(g);
+    eq &= gather32(e);
   }
   if (r && eq) {
-    unsigned long long lo, hi;
-    load_tail16(tail, row0 >> 4, r, lo, hi);
+    // 32 rows of r bits = 4r bytes at byte (row0 / 32) * 4r (4-byte aligned)
+    const uint32_t *tp = reinterpret_cast<const uint32_t *>(tail + (size_t)(row0 >> 5) * 4 * r);
+    uint32_t tw[8];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) tw[i] = (uint32_t)i < r ? __ldg(tp + i) : 0u;
+    tw[7] = 0;
     uint32_t gtt = 0, eqt = 0;
-    for (uint32_t i = 0; i < 16; ++i) {
-      const uint32_t f = field16(lo, hi, i, r);
+    for (uint32_t i = 0; i < 32; ++i) {
+      if (!(eq >> i & 1u)) continue;
+      const uint32_t bit = i * r, wi = bit >> 5, sh = bit & 31;
+      const uint32_t f = __funnelshift_r(tw[wi], tw[wi + 1], sh) & ((1u << r) - 1u);
       gtt |= (uint32_t)(f > ttail) << i;
       eqt |= (uint32_t)(f == ttail) << i;
     }
@@ -496,118 +537,97 @@ __device__ __noinline__ void refine_candidates(const uint8_t *__restrict__ slice
   }
 }
 
-// One 16-row vector of slice 0 (4 words of flipped bytes) against the target:
-// the 16-bit gt mask (row order) and whether any row equals the target byte.
-__device__ __forceinline__ uint32_t gt16_eqany(const uint4 &d, const ByteTarget &t,
-                                               uint32_t &eqm0, uint32_t &eqm1, uint32_t &eqm2,
-                                               uint32_t &eqm3) {
-  uint32_t g0, g1, g2, g3;
-  cmp4(d.x, t, g0, eqm0);
-  cmp4(d.y, t, g1, eqm1);
-  cmp4(d.z, t, g2, eqm2);
-  cmp4(d.w, t, g3, eqm3);
-  return msb4(g0) | (msb4(g1) << 4) | (msb4(g2) << 8) | (msb4(g3) << 12);
-}
-
-__device__ __forceinline__ uint32_t gather16(uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3) {
-  return msb4(m0) | (msb4(m1) << 4) | (msb4(m2) << 8) | (msb4(m3) << 12);
-}
-
-// The result bits of one 16-row vector whose rows are all below full_rows.
-template <bool IS_RANGE>
-__device__ __forceinline__ uint32_t filter_vec(const FilterArgs &a, const uint4 &d,
-                                               const ByteTarget &tg0, unsigned long long tb,
-                                               uint32_t row0) {
-  uint32_t e0, e1, e2, e3;
-  uint32_t gt = 0;
-  if (IS_RANGE)
-    gt = gt16_eqany(d, tg0, e0, e1, e2, e3);
-  else {
-    uint32_t g;
-    cmp4(d.x, tg0, g, e0);
-    cmp4(d.y, tg0, g, e1);
-    cmp4(d.z, tg0, g, e2);
-    cmp4(d.w, tg0, g, e3);
-  }
-  if (!(e0 | e1 | e2 | e3)) return IS_RANGE ? gt : 0u;
-  uint32_t eq = gather16(e0, e1, e2, e3);
-  if (a.k_used > 1 || a.r)
-    refine_candidates(a.slices, a.stride, a.k_used, tb, a.tail, a.r, a.ttail, row0, gt, eq);
-  else if (a.tail_only_eq)
-    eq = 0;
-  return IS_RANGE ? gt : eq;
-}
-
 // buff_simd_range_filter / buff_simd_equal_filter (compress/buff_simd.rs:
-// 3361-3733) and their fused `_with_slice` forms (:3736-4025).  For every
-// 16-row vector: compare slice 0 to the target byte; while some rows still
-// equal the target prefix, compare the next slice (gt |= eq & gt_j,
-// eq &= eq_j), then the packed tail.  Rows >= full_rows stay clear, which
-// reproduces the reference's 32-byte SIMD loop that never reaches the rows
-// after the last full 32-row block.  Warps stream 2048-row steps (4 loads of
-// 16 bytes in flight per lane); steps wholly below full_rows take the lean
-// path, the last partial step and fixed_len < 8 columns the general one.
-template <bool IS_RANGE>
-__global__ void __launch_bounds__(kThreads, 5) k_filter(FilterArgs a) {
+// 3361-3733) and their fused `_with_slice` forms (:3736-4025).  Lane L owns
+// 32 consecutive rows -- one bitmap word -- per load: 32 bytes of slice 0 are
+// compared to the target byte (per-byte SWAR on 32-bit words, MSB gather with
+// one multiply per 8 rows); while some rows still equal the target prefix the
+// next slice refines them (gt |= eq & gt_j, eq &= eq_j), then the packed tail.
+// Rows >= full_rows stay clear, which reproduces the reference's 32-byte SIMD
+// loop that never reaches the rows after the last full 32-row block.  TH is
+// the top bit of the slice-0 target byte.
+template <bool IS_RANGE, bool TH>
+__global__ void __launch_bounds__(kThreads) k_filter(FilterArgs a) {
+  constexpr int U = 2;  // 32-byte loads in flight per lane
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwords = (a.n + 31) / 32;
-  const uint32_t step_rows = kU * kRowChunk;
-  const uint32_t nsteps = (a.n + step_rows - 1) / step_rows;
-  const uint32_t nfast = a.k_used ? a.full_rows / step_rows : 0u;
+  const uint32_t nblk = a.k_used ? (a.n + 31) / 32 : 0u;  // 32-row blocks with a slice byte
+  const uint32_t nsteps = (nblk + U * 32 - 1) / (U * 32);
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   unsigned long long tb = 0;
 #pragma unroll
   for (int j = 0; j < 8; ++j) tb |= (unsigned long long)a.tbyte[j] << (8 * j);
-  const ByteTarget tg0 = make_target((uint32_t)(tb & 0xFFu));
+  const uint32_t t0 = (uint32_t)(tb & 0xFFu);
+  const uint32_t lo0 = (t0 & 0x7Fu) * 0x01010101u, lo1 = ((t0 & 0x7Fu) + 1u) * 0x01010101u;
+  const bool deep = a.k_used > 1 || a.r;
   uint32_t cnt = 0;
-  const uint8_t *s0 = a.slices + lane * 16;
-  uint32_t *wout = a.words + (lane >> 1);
-  for (uint32_t st = warp; st < nfast; st += nwarps) {
-    const uint32_t base = st * step_rows;
-    uint4 d[kU];
+  for (uint32_t st = warp; st < nsteps; st += nwarps) {
+    const uint32_t blk0 = st * (U * 32) + lane;
+    Bytes32 d[U];
 #pragma unroll
-    for (int u = 0; u < kU; ++u) d[u] = ld_stream(s0 + base + u * kRowChunk);
+    for (int u = 0; u < U; ++u) {
+      const uint32_t blk = blk0 + u * 32;
+      if (blk < nblk) d[u] = ld_stream32(a.slices + (size_t)blk * 32);
+    }
 #pragma unroll
-    for (int u = 0; u < kU; ++u) {
-      const uint32_t res = filter_vec<IS_RANGE>(a, d[u], tg0, tb, base + u * kRowChunk + lane * 16);
-      const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
-      const uint32_t wv = (res & 0xFFFFu) | (hi16 << 16);
-      if (!(lane & 1)) {
-        __stcs(wout + (base + u * kRowChunk) / 32, wv);
-        cnt += __popc(wv);
+    for (int u = 0; u < U; ++u) {
+      const uint32_t blk = blk0 + u * 32;
+      if (blk >= nblk) continue;
+      const uint32_t row0 = blk * 32;
+      uint32_t m[8];
+      uint32_t eor = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        m[q] = eq4t<TH>(d[u].w[q], lo0, lo1);
+        eor |= m[q];
       }
+      uint32_t eq = eor ? gather32(m) : 0u;
+      uint32_t gt = 0;
+      if (IS_RANGE) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) m[q] = gt4t<TH>(d[u].w[q], lo1);
+        gt = gather32(m);
+      }
+      if (eq) {
+        if (deep)
+          refine32(a.slices, a.stride, a.k_used, tb, a.tail, a.r, a.ttail, row0, gt, eq);
+        else if (a.tail_only_eq)
+          eq = 0;
+      }
+      uint32_t res = IS_RANGE ? gt : eq;
+      if (row0 + 32 > a.full_rows) {
+        const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
+        res &= lim >= 32 ? 0xFFFFFFFFu : ((1u << lim) - 1u);
+      }
+      __stcs(a.words + blk, res);
+      cnt += __popc(res);
     }
   }
-  for (uint32_t st = nfast + warp; st < nsteps; st += nwarps) {
-    const uint32_t base = st * step_rows;
-#pragma unroll 1
-    for (int u = 0; u < kU; ++u) {
-      const uint32_t row0 = base + u * kRowChunk + lane * 16;
-      uint32_t res = 0;
-      if (row0 < a.n) {
-        uint32_t gt = 0, eq = 0xFFFFu;
-        if (a.k_used) {
-          const uint4 d = ld_stream(a.slices + row0);
-          uint32_t e0, e1, e2, e3;
-          gt = gt16_eqany(d, tg0, e0, e1, e2, e3);
-          eq = gather16(e0, e1, e2, e3);
+  // fixed_len < 8: no slices, every row compared in full on its packed code
+  if (!a.k_used) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint32_t wd = tid; wd < nwords; wd += gridDim.x * blockDim.x) {
+      uint32_t gt = 0, eq = 0xFFFFFFFFu;
+      if (a.r) {
+        eq = 0;
+        for (uint32_t i = 0; i < 32; ++i) {
+          const unsigned long long bit = (unsigned long long)(wd * 32 + i) * a.r;
+          const uint32_t b0 = __ldg(a.tail + (bit >> 3));
+          const uint32_t b1 = ((bit & 7) + a.r > 8) ? __ldg(a.tail + (bit >> 3) + 1) : 0u;
+          const uint32_t f = ((b0 | (b1 << 8)) >> (bit & 7)) & ((1u << a.r) - 1u);
+          gt |= (uint32_t)(f > a.ttail) << i;
+          eq |= (uint32_t)(f == a.ttail) << i;
         }
-        if (eq && (a.k_used > 1 || a.r))
-          refine_candidates(a.slices, a.stride, a.k_used, tb, a.tail, a.r, a.ttail, row0, gt, eq);
-        else if (a.tail_only_eq && !a.r)
-          eq = 0;
-        res = IS_RANGE ? gt : eq;
+      }
+      uint32_t res = IS_RANGE ? gt : eq;
+      const uint32_t row0 = wd * 32;
+      if (row0 + 32 > a.full_rows) {
         const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
-        if (lim < 16) res &= (1u << lim) - 1u;
+        res &= lim >= 32 ? 0xFFFFFFFFu : ((1u << lim) - 1u);
       }
-      const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
-      const uint32_t word = (base + u * kRowChunk) / 32 + (lane >> 1);
-      if (!(lane & 1) && word < nwords) {
-        const uint32_t wv = (res & 0xFFFFu) | (hi16 << 16);
-        __stcs(a.words + word, wv);
-        cnt += __popc(wv);
-      }
+      a.words[wd] = res;
+      cnt += __popc(res);
     }
   }
   if (a.count) {
@@ -712,12 +732,6 @@ __global__ void __launch_bounds__(kThreads) k_sum(const uint8_t *__restrict__ sl
 
 // ---------------------------------------------------------------- max
 
-__device__ __forceinline__ uint32_t max_byte16(const uint4 &d) {
-  uint32_t m = __vmaxu4(__vmaxu4(d.x ^ H, d.y ^ H), __vmaxu4(d.z ^ H, d.w ^ H));
-  m = __vmaxu4(m, m >> 16);
-  m = __vmaxu4(m, m >> 8);
-  return m & 0xFFu;
-}
 
 // The full stored code of row i (slices MSB-first, then the tail field).
 __device__ __forceinline__ unsigned long long code_at(const uint8_t *slices, size_t stride,
@@ -734,58 +748,56 @@ __device__ __forceinline__ unsigned long long code_at(const uint8_t *slices, siz
   return c;
 }
 
-// Largest full code among the rows of one 16-row vector whose leading byte is
-// `top`: the remaining slices are read as 16-byte vectors and the tail as
-// the 2r bytes of these rows (out of line for the same reason as
-// refine_candidates).
-__device__ __noinline__ unsigned long long max_in_vector(const uint8_t *__restrict__ slices,
-                                                         size_t stride, uint32_t k,
-                                                         const uint8_t *__restrict__ tail,
-                                                         uint32_t r, uint32_t n, uint32_t row0,
-                                                         uint4 d, uint32_t top) {
-  const uint8_t *db = reinterpret_cast<const uint8_t *>(&d);
-  uint32_t cand = 0;
-  for (uint32_t i = 0; i < 16; ++i)
-    if (row0 + i < n && (uint32_t)(db[i] ^ 0x80u) == top) cand |= 1u << i;
-  // Every surviving candidate shares the prefix built so far, so one prefix
-  // and a candidate mask describe the state (MSB-first progressive max).
+// Largest full code among rows row0..row0+31 whose leading byte is `top`
+// (bit i of `cand`): every surviving candidate shares the prefix built so
+// far, so one prefix and a candidate mask describe the MSB-first progressive
+// max.  Out of line: it runs for few blocks.
+__device__ __noinline__ unsigned long long max_in_block(const uint8_t *__restrict__ slices,
+                                                        size_t stride, uint32_t k,
+                                                        const uint8_t *__restrict__ tail,
+                                                        uint32_t r, uint32_t row0, uint32_t cand,
+                                                        uint32_t top) {
   unsigned long long prefix = top;
   for (uint32_t s = 1; s < k; ++s) {
-    uint4 v = ld_cand(slices + s * stride + row0);
-    const uint8_t *vb = reinterpret_cast<const uint8_t *>(&v);
+    const uint8_t *p = slices + s * stride + row0;
     uint32_t best = 0;
-    for (uint32_t i = 0; i < 16; ++i)
-      if (cand >> i & 1u) best = max(best, (uint32_t)(vb[i] ^ 0x80u));
+    for (uint32_t c = cand; c; c &= c - 1) best = max(best, (uint32_t)(__ldg(p + __ffs(c) - 1) ^ 0x80u));
     uint32_t nc = 0;
-    for (uint32_t i = 0; i < 16; ++i)
-      if ((cand >> i & 1u) && (uint32_t)(vb[i] ^ 0x80u) == best) nc |= 1u << i;
+    for (uint32_t c = cand; c; c &= c - 1) {
+      const uint32_t i = __ffs(c) - 1;
+      if ((uint32_t)(__ldg(p + i) ^ 0x80u) == best) nc |= 1u << i;
+    }
     cand = nc;
     prefix = (prefix << 8) | best;
   }
   if (!r) return prefix;
-  unsigned long long lo, hi;
-  load_tail16(tail, row0 >> 4, r, lo, hi);
   uint32_t bt = 0;
-  for (uint32_t i = 0; i < 16; ++i)
-    if (cand >> i & 1u) bt = max(bt, field16(lo, hi, i, r));
+  for (uint32_t c = cand; c; c &= c - 1) {
+    const uint32_t i = __ffs(c) - 1;
+    const unsigned long long bit = (unsigned long long)(row0 + i) * r;
+    const uint32_t b0 = __ldg(tail + (bit >> 3));
+    const uint32_t b1 = ((bit & 7) + r > 8) ? __ldg(tail + (bit >> 3) + 1) : 0u;
+    bt = max(bt, ((b0 | (b1 << 8)) >> (bit & 7)) & ((1u << r) - 1u));
+  }
   return (prefix << r) | bt;
 }
 
 // byte_fixed_max (compress/split_double.rs:3919-4105): the maximum stored
-// code.  Each warp keeps the best code it has seen; only lanes holding the
-// warp's largest leading byte, when that byte can still reach the warp's
-// best, gather the remaining slices and the tail.
-__global__ void __launch_bounds__(kThreads, 4) k_max(const uint8_t *__restrict__ slices, size_t stride,
+// code.  Lanes own 32 rows per 256-bit load.  Each warp keeps the best code it
+// has seen and, per step, first tests with per-byte SWAR whether any leading
+// byte reaches the best's leading byte; only then does it find the step's
+// largest leading byte and gather the remaining slices of those rows.
+__global__ void __launch_bounds__(kThreads) k_max(const uint8_t *__restrict__ slices, size_t stride,
                                                   uint32_t k, const uint8_t *__restrict__ tail,
                                                   uint32_t r, uint32_t fl, uint32_t n,
                                                   unsigned long long *out) {
+  constexpr int U = 2;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  unsigned long long best = 0;
-  bool have = false;
   if (k == 0) {  // packed codes only (fixed_len < 8)
     const uint32_t nvec = (n + 15) / 16;
+    unsigned long long best = 0;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += gridDim.x * blockDim.x) {
       unsigned long long lo, hi;
       load_tail16(tail, v, r, lo, hi);
@@ -798,43 +810,79 @@ __global__ void __launch_bounds__(kThreads, 4) k_max(const uint8_t *__restrict__
     if (lane == 0 && n) atomicMax(out, best);
     return;
   }
-  const uint32_t step_rows = kU * kRowChunk;
-  const uint32_t nsteps = (n + step_rows - 1) / step_rows;
+  const uint32_t nblk = (n + 31) / 32;
+  const uint32_t nsteps = (nblk + U * 32 - 1) / (U * 32);
+  unsigned long long best = 0;
+  bool have = false;
+  uint32_t top = 0;  // leading byte of best
   for (uint32_t st = warp; st < nsteps; st += nwarps) {
-    const uint32_t base = st * step_rows;
-    uint4 d[kU];
+    const uint32_t blk0 = st * (U * 32) + lane;
+    Bytes32 d[U];
 #pragma unroll
-    for (int u = 0; u < kU; ++u) {
-      const uint32_t row0 = base + u * kRowChunk + lane * 16;
-      if (row0 < n) {
-        d[u] = ld_stream(slices + row0);
-        if (n - row0 < 16) clear_padding(d[u], n - row0);
+    for (int u = 0; u < U; ++u) {
+      const uint32_t blk = blk0 + u * 32;
+      if (blk < nblk) {
+        d[u] = ld_stream32(slices + (size_t)blk * 32);
+        const uint32_t row0 = blk * 32;
+        if (row0 + 32 > n) {  // padding rows -> flipped zero
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const uint32_t lo = row0 + 4u * q;
+            const uint32_t keep = n >= lo + 4 ? 0xFFFFFFFFu : (n <= lo ? 0u : ((1u << (8 * (n - lo))) - 1u));
+            d[u].w[q] = (d[u].w[q] & keep) | (H & ~keep);
+          }
+        }
       } else {
-        d[u] = make_uint4(H, H, H, H);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) d[u].w[q] = H;
       }
     }
-    uint32_t mb[kU];
+    // any leading byte >= top?  (a >= t: t_hi ? a_hi & a_lo>=t_lo : a_hi | a_lo>=t_lo)
+    const uint32_t lo0 = (top & 0x7Fu) * 0x01010101u;
+    const uint32_t th = (top & 0x80u) ? 0xFFFFFFFFu : 0u;
+    uint32_t any = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const uint32_t w = d[u].w[q];
+        const uint32_t d0 = (w | H) - lo0;
+        any |= ((th & ~w & d0) | (~th & (~w | d0))) & H;
+      }
+    if (have && !__any_sync(0xFFFFFFFFu, any != 0)) continue;
+    uint32_t mb[U];
     uint32_t lm = 0;
 #pragma unroll
-    for (int u = 0; u < kU; ++u) {
-      mb[u] = max_byte16(d[u]);
+    for (int u = 0; u < U; ++u) {
+      uint32_t m = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) m = __vmaxu4(m, d[u].w[q] ^ H);
+      m = __vmaxu4(m, m >> 16);
+      m = __vmaxu4(m, m >> 8);
+      mb[u] = m & 0xFFu;
       lm = mb[u] > lm ? mb[u] : lm;
     }
     const uint32_t wmb = __reduce_max_sync(0xFFFFFFFFu, lm);
-    const uint32_t best_top = have ? (uint32_t)(best >> (fl - 8)) : 0u;
-    if (have && wmb < best_top) continue;
+    if (have && wmb < top) continue;
     unsigned long long m = 0;
 #pragma unroll
-    for (int u = 0; u < kU; ++u) {
-      const uint32_t row0 = base + u * kRowChunk + lane * 16;
-      if (row0 < n && mb[u] == wmb) {
-        const unsigned long long c = max_in_vector(slices, stride, k, tail, r, n, row0, d[u], wmb);
+    for (int u = 0; u < U; ++u) {
+      const uint32_t blk = blk0 + u * 32;
+      if (blk < nblk && mb[u] == wmb) {
+        uint32_t cand = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+          for (int b = 0; b < 4; ++b)
+            if (((d[u].w[q] >> (8 * b)) & 0xFFu) == (wmb ^ 0x80u)) cand |= 1u << (4 * q + b);
+        const unsigned long long c = max_in_block(slices, stride, k, tail, r, blk * 32, cand, wmb);
         m = c > m ? c : m;
       }
     }
     m = warp_max_ull(m);
     if (!have || m > best) best = m;
     have = true;
+    top = (uint32_t)(best >> (fl - 8)) & 0xFFu;
   }
   if (lane == 0 && have) atomicMax(out, best);
 }
@@ -906,68 +954,65 @@ __device__ __forceinline__ double i64_to_f64_scaled(long long v, int dlen) {
 // (keep == ~0) the value is (base + X) / 2^dlen with X those bits *not*
 // shifted back, and when ts != r the packed bits are read with a stride of ts.
 // The INTENDED form passes all bits and a `keep` mask instead.
+//
+// Lane L produces rows 64m + 2L and 64m + 2L + 1 of each 512-row chunk, so the
+// f64 results leave as coalesced 16-byte stores; the two slice bytes per row
+// pair are 2-byte loads (64 contiguous bytes per warp), and the packed bits of
+// a 64-row group (8*ts bytes) are loaded by the first 2*ts lanes and handed out
+// with shuffles.
 template <int KS>
 __global__ void __launch_bounds__(kThreads) k_decode(const uint8_t *__restrict__ slices,
                                                      size_t stride,
-                                                     const uint8_t *__restrict__ tail, uint32_t r,
+                                                     const uint8_t *__restrict__ tail,
                                                      uint32_t ts, uint32_t n, long long base,
                                                      int dlen, unsigned long long keep,
                                                      double *__restrict__ out) {
-  extern __shared__ double dsm[];
   const uint32_t lane = threadIdx.x & 31;
-  double *ws = dsm + (size_t)(threadIdx.x >> 5) * kRowChunk;
   const uint32_t nchunks = (n + kRowChunk - 1) / kRowChunk;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const unsigned long long tmask = ts ? ((1ull << ts) - 1ull) : 0ull;
   for (uint32_t ch = warp; ch < nchunks; ch += nwarps) {
-    const uint32_t row0 = ch * kRowChunk + lane * 16;
-    unsigned long long c[16];
+    const uint32_t r0 = ch * kRowChunk;
+    uint32_t sb[8][KS > 0 ? KS : 1];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) c[i] = 0;
-    if (row0 < n) {
-      uint4 d[KS > 0 ? KS : 1];
+    for (int m = 0; m < 8; ++m)
 #pragma unroll
-      for (int s = 0; s < KS; ++s) d[s] = ld_stream(slices + s * stride + row0);
-      unsigned long long lo = 0, hi = 0;
-      if (ts && ts == r) load_tail16(tail, row0 >> 4, r, lo, hi);
-#pragma unroll
-      for (int s = 0; s < KS; ++s) {
-        const uint32_t *w = reinterpret_cast<const uint32_t *>(&d[s]);
-#pragma unroll
-        for (int i = 0; i < 16; ++i)
-          c[i] = (c[i] << 8) | (((w[i >> 2] >> (8 * (i & 3))) & 0xFFu) ^ 0x80u);
-      }
-      if (ts) {
-        if (ts == r) {
-#pragma unroll
-          for (int i = 0; i < 16; ++i) c[i] = (c[i] << r) | field16(lo, hi, i, r);
-        } else {  // the reference's stride-ts reads of the packed region
-          for (int i = 0; i < 16; ++i) {
-            const unsigned long long bit = (unsigned long long)(row0 + i) * ts;
-            const uint32_t b0 = __ldg(tail + (bit >> 3));
-            const uint32_t b1 = ((bit & 7) + ts > 8) ? __ldg(tail + (bit >> 3) + 1) : 0u;
-            c[i] = (c[i] << ts) | (((b0 | (b1 << 8)) >> (bit & 7)) & ((1u << ts) - 1u));
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const unsigned long long x = c[i] & keep;
-      ws[lane * 16 + i] = i64_to_f64_scaled((long long)((unsigned long long)base + x), dlen);
-    }
-    __syncwarp();
+      for (int s = 0; s < KS; ++s)
+        sb[m][s] = __ldg(reinterpret_cast<const uint16_t *>(slices + s * stride + r0 + m * 64 +
+                                                            2 * lane));
+    uint32_t tw[8];
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
-      const uint32_t off = m * 64 + lane * 2;
-      const uint32_t i0 = ch * kRowChunk + off;
-      double2 p = *reinterpret_cast<const double2 *>(ws + off);
-      if (i0 + 2 <= n)
-        __stcs(reinterpret_cast<double2 *>(out + i0), p);
-      else if (i0 < n)
-        out[i0] = p.x;
+      tw[m] = 0;
+      if (ts && lane < 2 * ts)
+        tw[m] = __ldg(reinterpret_cast<const uint32_t *>(
+                          tail + (size_t)8 * ts * (r0 / 64 + m)) + lane);
     }
-    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      unsigned long long c0 = 0, c1 = 0;
+#pragma unroll
+      for (int s = 0; s < KS; ++s) {
+        c0 = (c0 << 8) | ((sb[m][s] & 0xFFu) ^ 0x80u);
+        c1 = (c1 << 8) | (((sb[m][s] >> 8) & 0xFFu) ^ 0x80u);
+      }
+      if (ts) {
+        const uint32_t bit = 2 * lane * ts, wi = bit >> 5;
+        const uint32_t w0 = __shfl_sync(0xFFFFFFFFu, tw[m], wi);
+        const uint32_t w1 = __shfl_sync(0xFFFFFFFFu, tw[m], (wi + 1) & 31);
+        const uint32_t f = __funnelshift_r(w0, w1, bit & 31);
+        c0 = (c0 << ts) | (f & tmask);
+        c1 = (c1 << ts) | ((f >> ts) & tmask);
+      }
+      const uint32_t i0 = r0 + m * 64 + 2 * lane;
+      const double v0 = i64_to_f64_scaled((long long)((unsigned long long)base + (c0 & keep)), dlen);
+      const double v1 = i64_to_f64_scaled((long long)((unsigned long long)base + (c1 & keep)), dlen);
+      if (i0 + 2 <= n)
+        __stcs(reinterpret_cast<double2 *>(out + i0), make_double2(v0, v1));
+      else if (i0 < n)
+        out[i0] = v0;
+    }
   }
 }
 
@@ -1029,23 +1074,41 @@ cudaError_t launch_encode_reduce_f32(const float *x, uint32_t n, uint32_t from, 
   return reduce_impl<float>(x, n, from, pexp, dlen, keys, find_brk, d_out, s);
 }
 
-template <typename T>
-static cudaError_t scatter_impl(const T *x, const buff_col *c, cudaStream_t s) {
-  if (c->n == 0 || (c->k == 0 && c->r == 0)) return cudaSuccess;
-  const uint32_t planes = c->k + (c->r ? 1u : 0u);
+template <typename T, int K>
+static cudaError_t scatter_k(const T *x, const buff_col *c, cudaStream_t s) {
+  const uint32_t planes = K + (c->r ? 1u : 0u);
   const size_t smem = (size_t)(kThreads / 32) * planes * kRowChunk;
-  const void *fn = (const void *)k_encode_scatter<T>;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const void *fn = (const void *)k_encode_scatter<T, K>;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const uint32_t nchunks = (c->n + kRowChunk - 1) / kRowChunk;
   int grid = grid_for(fn, kThreads, smem, c->device);
   const int need = (int)((nchunks + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
-  k_encode_scatter<T><<<grid, kThreads, smem, s>>>(x, c->n, c->precision_exp, c->dlen, c->base,
-                                                   c->fixed_len, c->k, c->r, c->slices, c->stride,
-                                                   c->tail);
+  k_encode_scatter<T, K><<<grid, kThreads, smem, s>>>(x, c->n, c->precision_exp, c->dlen, c->base,
+                                                      c->fixed_len, c->r, c->slices, c->stride,
+                                                      c->tail);
   count_launch();
   return cudaGetLastError();
 }
+
+template <typename T>
+static cudaError_t scatter_impl(const T *x, const buff_col *c, cudaStream_t s) {
+  if (c->n == 0 || (c->k == 0 && c->r == 0)) return cudaSuccess;
+  switch (c->k) {
+    case 0: return scatter_k<T, 0>(x, c, s);
+    case 1: return scatter_k<T, 1>(x, c, s);
+    case 2: return scatter_k<T, 2>(x, c, s);
+    case 3: return scatter_k<T, 3>(x, c, s);
+    case 4: return scatter_k<T, 4>(x, c, s);
+    case 5: return scatter_k<T, 5>(x, c, s);
+    case 6: return scatter_k<T, 6>(x, c, s);
+    case 7: return scatter_k<T, 7>(x, c, s);
+    case 8: return scatter_k<T, 8>(x, c, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_encode_scatter_f64(const double *x, const buff_col *c, cudaStream_t s) {
   return scatter_impl<double>(x, c, s);
 }
@@ -1055,15 +1118,15 @@ cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStr
 
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
-  const void *fn = a.is_range ? (const void *)k_filter<true> : (const void *)k_filter<false>;
-  const uint32_t nsteps = (a.n + kU * kRowChunk - 1) / (kU * kRowChunk);
-  int grid = grid_for(fn, kThreads, 0, cur_device());
+  const bool th = a.tbyte[0] & 0x80u;
+  void (*fn)(FilterArgs) = a.is_range ? (th ? k_filter<true, true> : k_filter<true, false>)
+                                      : (th ? k_filter<false, true> : k_filter<false, false>);
+  const uint32_t nsteps = ((a.n + 31) / 32 + 63) / 64;
+  int grid = grid_for((const void *)fn, kThreads, 0, cur_device());
   const int need = (int)((nsteps + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
-  if (a.is_range)
-    k_filter<true><<<grid, kThreads, 0, s>>>(a);
-  else
-    k_filter<false><<<grid, kThreads, 0, s>>>(a);
+  if (grid < 1) grid = 1;
+  fn<<<grid, kThreads, 0, s>>>(a);
   count_launch();
   return cudaGetLastError();
 }
@@ -1096,7 +1159,7 @@ cudaError_t launch_sum(const buff_col *c, uint32_t k_used, uint32_t tail_bits,
 cudaError_t launch_max(const buff_col *c, unsigned long long *d_max, cudaStream_t s) {
   if (c->n == 0) return cudaSuccess;
   int grid = grid_for((const void *)k_max, kThreads, 0, c->device);
-  const uint32_t nsteps = (c->n + kU * kRowChunk - 1) / (kU * kRowChunk);
+  const uint32_t nsteps = ((c->n + 31) / 32 + 63) / 64;
   const int need = (int)((nsteps + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
   k_max<<<grid, kThreads, 0, s>>>(c->slices, c->stride, c->k, c->tail, c->r, c->fixed_len, c->n,
@@ -1120,14 +1183,13 @@ cudaError_t launch_argmax(const buff_col *c, const unsigned long long *d_max, ui
 template <int KS>
 static cudaError_t decode_ks(const buff_col *c, uint32_t ts, unsigned long long keep, double *out,
                              cudaStream_t s) {
-  const size_t smem = (size_t)(kThreads / 32) * kRowChunk * sizeof(double);
   const void *fn = (const void *)k_decode<KS>;
-  int grid = grid_for(fn, kThreads, smem, c->device);
+  int grid = grid_for(fn, kThreads, 0, c->device);
   const uint32_t nchunks = (c->n + kRowChunk - 1) / kRowChunk;
   const int need = (int)((nchunks + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
-  k_decode<KS><<<grid, kThreads, smem, s>>>(c->slices, c->stride, c->tail, c->r, ts, c->n, c->base,
-                                            (int)c->dlen, keep, out);
+  k_decode<KS><<<grid, kThreads, 0, s>>>(c->slices, c->stride, c->tail, ts, c->n, c->base,
+                                         (int)c->dlen, keep, out);
   count_launch();
   return cudaGetLastError();
 }
