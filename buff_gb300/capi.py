@@ -13,7 +13,8 @@ import numpy as np
 
 from . import build as _build
 
-OK, EINVAL, ENOMEM, ECUDA, EREFPANIC, ECORRUPT, ETIMEDOUT, ENOTSUP, EFULL = range(9)
+OK, EINVAL, ENOMEM, ECUDA, EREFPANIC, ECORRUPT, ETIMEDOUT, ENOTSUP, EFULL, ESCRATCH = range(10)
+NOALLOC_MAX_ROWS = 1 << 26
 FLAG_INTENDED = 0x1
 
 EXPORTED = [
@@ -24,6 +25,7 @@ EXPORTED = [
     "buff_equal_filter_with_slice", "buff_sum", "buff_sum_at_precision",
     "buff_sum_partials_async", "buff_sum_finish", "buff_max", "buff_max_async",
     "buff_status_string", "buff_last_cuda_error", "buff_kernel_launches",
+    "buff_range_filter_noalloc",
 ]
 
 
@@ -90,6 +92,7 @@ def lib(build_if_missing: bool = True):
     for nm in ("buff_range_filter", "buff_equal_filter", "buff_range_filter_with_slice",
                "buff_equal_filter_with_slice"):
         getattr(L, nm).argtypes = [P, C.c_double, P, P, P]
+    L.buff_range_filter_noalloc.argtypes = [P, C.c_double, P, P, P]
     L.buff_sum.argtypes = [P, C.POINTER(SumResult), P]
     L.buff_sum_at_precision.argtypes = [P, C.c_uint32, P, P]
     L.buff_sum_partials_async.argtypes = [P, P, P]

@@ -782,6 +782,7 @@ const char *buff_status_string(int st) {
     case BUFF_ETIMEDOUT: return "bounded device wait expired";
     case BUFF_ENOTSUP: return "not supported for this column layout";
     case BUFF_EFULL: return "queue or memory budget exhausted";
+    case BUFF_ESCRATCH: return "column larger than the fixed scratch of the allocation-free entry point";
     default: return "unknown status";
   }
 }

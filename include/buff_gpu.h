@@ -48,6 +48,7 @@ extern "C" {
 #define BUFF_ETIMEDOUT 6  /* a bounded device-side wait expired */
 #define BUFF_ENOTSUP 7    /* not supported for this column layout */
 #define BUFF_EFULL 8      /* a queue or memory budget is exhausted */
+#define BUFF_ESCRATCH 9   /* larger than the fixed scratch of an allocation-free entry point */
 
 /* ---- flags ---- */
 /* Intended semantics instead of the reference's quirks: exact min/max and
@@ -163,6 +164,28 @@ int buff_max(const buff_col *col, double *max_value, uint64_t *max_code,
              uint32_t *argmax_words, uint64_t *argmax_count, void *stream);
 /* Device-only max: enqueues the maximum code into *dev_max_code (device u64). */
 int buff_max_async(const buff_col *col, uint64_t *dev_max_code, void *stream);
+
+/* ---- allocation-free query ---- */
+
+/* Largest column (rows) that buff_range_filter_noalloc accepts. */
+#define BUFF_NOALLOC_MAX_ROWS (1u << 26)
+
+/* buff_range_filter for callers that cannot allocate device memory while
+ * answering a query -- for example a server that has already reserved the
+ * whole HBM budget for its resident columns, or a process whose device memory
+ * belongs to another allocator.  No counterpart in the reference: it exists
+ * only for this GPU library.  Same results as buff_range_filter; `words`
+ * (ceil(n/32) u32) and `count` (may be NULL) may be host or device memory.
+ * It calls no cudaMalloc/cudaFree or other allocating routine: the bitmap and
+ * count are staged in a fixed scratch array of about 8 MiB that belongs to the
+ * library's device image, so every GPU that loads the library holds it until
+ * the process exits.  Columns with more than BUFF_NOALLOC_MAX_ROWS rows return
+ * BUFF_ESCRATCH.  The first call on a device looks up the scratch address for
+ * that device (make it before any stream capture); all calls share the array,
+ * so calls whose work overlaps on the GPU race and must be ordered by the
+ * caller.  The call synchronizes `stream`. */
+int buff_range_filter_noalloc(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
+                              void *stream);
 
 /* ---- diagnostics ---- */
 const char *buff_status_string(int status);
