@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libbuffgpu.so")
-SOURCES = ["buff_kernels.cu", "buff_capi.cu", "buff_noalloc.cu"]
+SOURCES = ["buff_kernels.cu", "buff_capi.cu", "buff_noalloc.cu", "buff_major.cu", "buff_snappy.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
               "--expt-relaxed-constexpr"]
@@ -46,7 +46,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     procs = []
     objs = []
     for src in SOURCES:
-        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         cmd = [cc, *ARCH, *flags, "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)

@@ -16,6 +16,7 @@ from . import build as _build
 OK, EINVAL, ENOMEM, ECUDA, EREFPANIC, ECORRUPT, ETIMEDOUT, ENOTSUP, EFULL, ESCRATCH = range(10)
 NOALLOC_MAX_ROWS = 1 << 26
 FLAG_INTENDED = 0x1
+FLAG_RAW_BITMAPS = 0x2
 
 EXPORTED = [
     "buff_encode_f64", "buff_encode_f32", "buff_col_free", "buff_col_free_async",
@@ -26,6 +27,9 @@ EXPORTED = [
     "buff_sum_partials_async", "buff_sum_finish", "buff_max", "buff_max_async",
     "buff_status_string", "buff_last_cuda_error", "buff_kernel_launches",
     "buff_range_filter_noalloc",
+    "buff_encode_majority_f64", "buff_encode_majority_f32", "buff_deserialize_majority",
+    "buff_decode_majority", "buff_range_filter_majority", "buff_equal_filter_majority",
+    "buff_sum_majority", "buff_max_majority",
 ]
 
 
@@ -46,7 +50,7 @@ class ColInfo(C.Structure):
     _fields_ = [("base", C.c_int64), ("n", C.c_uint32), ("ilen", C.c_uint32),
                 ("dlen", C.c_uint32), ("fixed_len", C.c_uint32), ("k", C.c_uint32),
                 ("r", C.c_uint32), ("scale", C.c_uint64), ("prec", C.c_int32),
-                ("precision_exp", C.c_int32), ("flags", C.c_uint32), ("reserved", C.c_uint32),
+                ("precision_exp", C.c_int32), ("flags", C.c_uint32), ("outlier_cols", C.c_uint32),
                 ("serialized_bytes", C.c_uint64), ("device_bytes", C.c_uint64)]
 
 
@@ -99,6 +103,14 @@ def lib(build_if_missing: bool = True):
     L.buff_sum_finish.argtypes = [P, P, C.POINTER(SumResult)]
     L.buff_max.argtypes = [P, P, P, P, P, P]
     L.buff_max_async.argtypes = [P, P, P]
+    L.buff_encode_majority_f64.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_encode_majority_f32.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_deserialize_majority.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_decode_majority.argtypes = [P, P, P]
+    L.buff_range_filter_majority.argtypes = [P, C.c_double, P, P, P]
+    L.buff_equal_filter_majority.argtypes = [P, C.c_double, P, P, P]
+    L.buff_sum_majority.argtypes = [P, C.POINTER(SumResult), P]
+    L.buff_max_majority.argtypes = [P, P, P, P, P, P]
     L.buff_status_string.argtypes = [C.c_int]
     L.buff_status_string.restype = C.c_char_p
     L.buff_last_cuda_error.restype = C.c_int

@@ -18,7 +18,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import capi
-from .capi import FLAG_INTENDED, check, lib, ptr, stream_handle
+from .capi import FLAG_INTENDED, FLAG_RAW_BITMAPS, check, lib, ptr, stream_handle
 
 
 @dataclass
@@ -50,25 +50,29 @@ class Column:
         self._h = C.c_void_p(handle)
 
     # -- lifetime -------------------------------------------------------
+    _ENCODE = ("buff_encode_f32", "buff_encode_f64")
+    _DESERIALIZE = "buff_deserialize"
+
     @classmethod
     def encode(cls, values, scale: int, flags: int = 0, stream=None) -> "Column":
         h = C.c_void_p()
+        f32, f64 = (getattr(lib(), nm) for nm in cls._ENCODE)
         if isinstance(values, np.ndarray):
             arr = np.ascontiguousarray(values)
             if arr.dtype == np.float32:
-                fn = lib().buff_encode_f32
+                fn = f32
             else:
                 arr = np.ascontiguousarray(arr, dtype=np.float64)
-                fn = lib().buff_encode_f64
+                fn = f64
             check(fn(ptr(arr), arr.size, scale, flags, stream_handle(stream), C.byref(h)), "encode")
         else:  # torch tensor (host or device)
             import torch
 
             t = values.contiguous()
             if t.dtype == torch.float32:
-                fn = lib().buff_encode_f32
+                fn = f32
             elif t.dtype == torch.float64:
-                fn = lib().buff_encode_f64
+                fn = f64
             else:
                 raise TypeError("values must be float32 or float64")
             check(fn(ptr(t), t.numel(), scale, flags, stream_handle(stream), C.byref(h)), "encode")
@@ -86,8 +90,8 @@ class Column:
         else:
             arr = data
             n = data.numel()
-        check(lib().buff_deserialize(ptr(arr), n, scale, flags, stream_handle(stream),
-                                     C.byref(h)), "deserialize")
+        check(getattr(lib(), cls._DESERIALIZE)(ptr(arr), n, scale, flags, stream_handle(stream),
+                                               C.byref(h)), "deserialize")
         return cls(h.value)
 
     def free(self):
@@ -119,6 +123,9 @@ class Column:
     def serialize(self, out=None, stream=None) -> bytes:
         need = self.info.serialized_bytes
         ln = C.c_uint64(0)
+        if need == 0:  # buff-major: the size is known after compressing the bitmaps
+            lib().buff_serialize(self._h, None, 0, C.byref(ln), stream_handle(stream))
+            need = ln.value
         if out is None:
             buf = np.empty(max(need, 1), dtype=np.uint8)
             check(lib().buff_serialize(self._h, ptr(buf), need, C.byref(ln),
@@ -192,6 +199,58 @@ class Column:
         return MaxResult(v.value, code.value, words, cnt.value)
 
 
+class MajorColumn(Column):
+    """A buff-major (outlier) column resident in HBM: sparse leading byte
+    columns kept as (major byte, outlier bitmap, outlier bytes), the rest as
+    slices (compress/buff_simd.rs:317-630)."""
+
+    _ENCODE = ("buff_encode_majority_f32", "buff_encode_majority_f64")
+    _DESERIALIZE = "buff_deserialize_majority"
+
+    def decode(self, out=None, stream=None):
+        if out is None:
+            out = np.empty(max(self.n, 1), dtype=np.float64)
+            check(lib().buff_decode_majority(self._h, ptr(out), stream_handle(stream)), "decode")
+            return out[: self.n]
+        check(lib().buff_decode_majority(self._h, ptr(out), stream_handle(stream)), "decode")
+        return out
+
+    def range_filter(self, pred, out=None, stream=None):
+        return self._filter(lib().buff_range_filter_majority, pred, out, stream)
+
+    def equal_filter(self, pred, out=None, stream=None):
+        return self._filter(lib().buff_equal_filter_majority, pred, out, stream)
+
+    def sum(self, stream=None) -> capi.SumResult:
+        res = capi.SumResult()
+        check(lib().buff_sum_majority(self._h, C.byref(res), stream_handle(stream)), "sum")
+        return res
+
+    def max(self, argmax: bool = False, stream=None) -> MaxResult:
+        v = C.c_double(0)
+        code = C.c_uint64(0)
+        cnt = C.c_uint64(0)
+        words = np.zeros(max((self.n + 31) // 32, 1), dtype=np.uint32) if argmax else None
+        check(lib().buff_max_majority(self._h, C.byref(v), C.byref(code), ptr(words),
+                                      C.byref(cnt) if argmax else None, stream_handle(stream)),
+              "max")
+        if words is not None:
+            words = words[: (self.n + 31) // 32]
+        return MaxResult(v.value, code.value, words, cnt.value)
+
+    def _unsupported(self, *a, **k):
+        raise capi.BuffError(capi.ENOTSUP, "not defined on buff-major columns")
+
+    decode_at_precision = sum_at_precision = _unsupported
+    range_filter_with_slice = equal_filter_with_slice = _unsupported
+
+
+def _as_major(comp: "SplitBDDoubleCompress", data) -> MajorColumn:
+    if isinstance(data, MajorColumn):
+        return data
+    return MajorColumn.deserialize(data, comp.scale, comp.flags)
+
+
 def _as_column(comp: "SplitBDDoubleCompress", data) -> Column:
     if isinstance(data, Column):
         return data
@@ -247,5 +306,31 @@ class SplitBDDoubleCompress:
     def byte_residue_sum_with_precision(self, data, precision: int, stream=None) -> float:
         return _as_column(self, data).sum_at_precision(precision, stream=stream)
 
+    # ---- buff-major (outlier) format --------------------------------
+    # compress/buff_simd.rs:317-630
+    def buff_encode_majority(self, values, stream=None) -> MajorColumn:
+        return MajorColumn.encode(values, self.scale, self.flags, stream)
 
-__all__ = ["SplitBDDoubleCompress", "Column", "FilterResult", "MaxResult", "FLAG_INTENDED"]
+    # compress/buff_simd.rs:633-861
+    def buff_decode_majority(self, data, stream=None):
+        return _as_major(self, data).decode(stream=stream)
+
+    # compress/buff_simd.rs:863-1277 (the reference prints the count)
+    def buff_range_filter_majority(self, data, pred, stream=None) -> FilterResult:
+        return _as_major(self, data).range_filter(pred, stream=stream)
+
+    # compress/buff_simd.rs:1916-2292
+    def buff_equal_filter_majority(self, data, pred, stream=None) -> FilterResult:
+        return _as_major(self, data).equal_filter(pred, stream=stream)
+
+    # compress/buff_simd.rs:2294-2442
+    def buff_sum_majority(self, data, stream=None) -> float:
+        return _as_major(self, data).sum(stream=stream).sum
+
+    # compress/buff_simd.rs:2444-2861 (the reference prints the max)
+    def buff_max_majority(self, data, stream=None) -> MaxResult:
+        return _as_major(self, data).max(argmax=True, stream=stream)
+
+
+__all__ = ["SplitBDDoubleCompress", "Column", "MajorColumn", "FilterResult", "MaxResult",
+           "FLAG_INTENDED", "FLAG_RAW_BITMAPS"]

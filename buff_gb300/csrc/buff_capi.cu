@@ -13,6 +13,8 @@
 #include <new>
 
 #include "buff_internal.h"
+#include "buff_snappy.h"
+#include <vector>
 
 using buffk::EncStats;
 using buffk::FilterArgs;
@@ -147,10 +149,13 @@ int alloc_col(buff_col *c, cudaStream_t s) {
 // have been reading the column.
 void free_col(buff_col *c, cudaStream_t s = nullptr, bool ordered = false) {
   if (!c) return;
-  if (c->slices || c->tail) {
+  void *bufs[5] = {c->slices, c->tail, c->obits, c->orank, c->obytes};
+  bool any = false;
+  for (void *b : bufs) any |= b != nullptr;
+  if (any) {
     if (!ordered) cudaDeviceSynchronize();
-    if (c->slices) cudaFreeAsync(c->slices, s);
-    if (c->tail) cudaFreeAsync(c->tail, s);
+    for (void *b : bufs)
+      if (b) cudaFreeAsync(b, s);
     if (!ordered) cudaStreamSynchronize(s);
   }
   delete c;
@@ -345,6 +350,7 @@ enum FilterKind { kRange = 0, kEqual = 1, kRangeSlice = 2, kEqualSlice = 3 };
 int filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t *count, cudaStream_t s,
                 FilterKind kind) {
   if (!c || (!words && c->n > 0)) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns: the *_majority calls
   const bool intended = c->flags & BUFF_FLAG_INTENDED;
   const bool is_range = (kind == kRange || kind == kRangeSlice);
   const bool with_slice = (kind == kRangeSlice || kind == kEqualSlice);
@@ -453,6 +459,230 @@ int sum_partials(const buff_col *c, uint32_t total, unsigned long long *d, cudaS
   return cuda_status(buffk::launch_sum(c, ks, ts, d, s));
 }
 
+// ---------------------------------------------------------------- buff-major
+
+// Boyer-Moore majority vote of one byte over the sample (buff_simd.rs:382-446).
+static void bm_vote(const uint64_t *codes, uint32_t cnt, uint32_t sh, uint8_t *major, int32_t *freq) {
+  int32_t f = 0;
+  uint8_t m = 0;
+  for (uint32_t i = 0; i < cnt; ++i) {
+    const uint8_t b = (uint8_t)(codes[i] >> sh);
+    if (f == 0) {
+      m = b;
+      f = 1;
+    } else if (m == b) {
+      ++f;
+    } else {
+      --f;
+    }
+  }
+  *major = m;
+  *freq = f;
+}
+
+template <typename T>
+int encode_major_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, cudaStream_t s,
+                      buff_col **out) {
+  if (!out) return BUFF_EINVAL;
+  *out = nullptr;
+  if (flags & BUFF_FLAG_INTENDED) return BUFF_ENOTSUP;
+  if (n64 >= (1ull << 32)) return BUFF_EINVAL;
+  if (n64 > 0 && !values) return BUFF_EINVAL;
+  const uint32_t n = (uint32_t)n64;
+  const int prec = prec_of_scale(scale);
+  const int dl = dlen_of_prec(prec);
+  if (dl < 0) return BUFF_EREFPANIC;
+  if (n < 2000) return BUFF_EREFPANIC;  // fixed_vec[0..SAMPLE] (buff_simd.rs:382)
+  int rc = BUFF_OK;
+  buff_col *c = new_col(scale, flags);
+  if (!c) return BUFF_ENOMEM;
+  c->layout = 1;
+  c->n = n;
+  c->dlen = (uint32_t)dl;
+  T *staged = nullptr;
+  EncStats *dst = nullptr;
+  uint8_t *lead = nullptr;
+  const T *dx = values;
+  EncStats st;
+  memset(&st, 0, sizeof(st));
+  T head[2000];
+  uint64_t codes[2000];
+  uint32_t fl = 0, m = 0;
+  if (!is_device_ptr(values) || (reinterpret_cast<uintptr_t>(values) & 15)) {
+    CK(scratch(&staged, n, s));
+    CK(cudaMemcpyAsync(staged, values, (size_t)n * sizeof(T), cudaMemcpyDefault, s));
+    dx = staged;
+  }
+  CK(scratch(&dst, 1, s));
+  {
+    int keys = c->precision_exp >= -(int)c->dlen ? 1 : 0;
+    CK(reduce(dx, n, 1, c, keys, 0, dst, s));
+    CK(cudaMemcpyAsync(&st, dst, sizeof(st), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(head, dx, sizeof(head), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (!st.ok) {
+      CK(reduce(dx, n, 1, c, 0, 0, dst, s));
+      CK(cudaMemcpyAsync(&st, dst, sizeof(st), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    }
+  }
+  {
+    // exact min/max here (two ifs, buff_simd.rs:340-347)
+    const int64_t mn = st.mn, mx = st.mx0;
+    const int64_t delta = (int64_t)((uint64_t)mx - (uint64_t)mn);
+    if (delta != 0) {
+      const double cl = ceil(log2((double)delta));
+      fl = (isnan(cl) || cl <= 0.0) ? 0u : (uint32_t)cl;
+    }
+    for (uint32_t i = 0; i < 2000; ++i)
+      codes[i] = (uint64_t)(fetch_fixed_host((double)head[i], c->precision_exp, c->dlen) - mn);
+    uint32_t rsf = fl >= 8 ? fl - 8 : 0;
+    const int32_t limit = (int32_t)(2000.0f * 0.6f);
+    uint8_t major;
+    int32_t freq;
+    bm_vote(codes, 2000, rsf, &major, &freq);
+    if (freq > limit) {
+      c->majors[m++] = major;
+      while (rsf > 7 && m < 8) {
+        rsf -= 8;
+        bm_vote(codes, 2000, rsf, &major, &freq);
+        if (freq > limit)
+          c->majors[m++] = major;
+        else
+          break;
+      }
+    }
+    if (fl < 8) {
+      // with a sparse column `remain -= 8` underflows; without one the packed
+      // codes overwrite the column-count byte, so neither image is decodable
+      rc = m ? BUFF_EREFPANIC : BUFF_ENOTSUP;
+      goto done;
+    }
+    c->base = mn;
+    set_layout(c, fl);
+    c->m = m;
+    c->ilen = (uint32_t)((uint64_t)fl - (uint64_t)c->dlen);
+    const uint32_t k = c->k;
+    c->k = k - m;  // allocate the dense slices only
+    rc = alloc_col(c, s);
+    c->k = k;
+    if (rc) goto done;
+    c->nwp = c->stride / 32;
+    if (m) CK(scratch(&lead, (size_t)m * c->stride, s));
+    if (sizeof(T) == 8)
+      CK(buffk::launch_encode_scatter_f64(reinterpret_cast<const double *>(dx), c, s, lead, m));
+    else
+      CK(buffk::launch_encode_scatter_f32(reinterpret_cast<const float *>(dx), c, s, lead, m));
+    if (m) CK(buffk::major_build_sparse(c, lead, s));
+  }
+done:
+  if (staged) cudaFreeAsync(staged, s);
+  if (dst) cudaFreeAsync(dst, s);
+  if (lead) cudaFreeAsync(lead, s);
+  if (rc != BUFF_OK) {
+    cudaStreamSynchronize(s);
+    free_col(c);
+    return rc;
+  }
+  *out = c;
+  return BUFF_OK;
+}
+
+// The byte image of a buff-major column (buff_simd.rs:449-528): header,
+// column count, per sparse column (major, bitmap size, bitmap, outlier
+// count, outlier bytes), a pad byte, the unflipped dense slices, the tail.
+int major_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s) {
+  int rc = BUFF_OK;
+  const uint32_t n = c->n, kd = c->k - c->m;
+  const size_t nw = ((size_t)n + 31) / 32;
+  std::vector<uint32_t> bits((size_t)c->m * nw);
+  std::vector<uint8_t> ob(c->oofs[c->m]);
+  std::vector<uint8_t> dense((size_t)kd * n), tail(c->tail_bytes);
+  for (uint32_t col = 0; col < c->m; ++col)
+    CK(cudaMemcpyAsync(bits.data() + col * nw, c->obits + col * c->nwp, nw * 4,
+                       cudaMemcpyDeviceToHost, s));
+  if (!ob.empty()) CK(cudaMemcpyAsync(ob.data(), c->obytes, ob.size(), cudaMemcpyDeviceToHost, s));
+  if (kd && n)
+    CK(cudaMemcpy2DAsync(dense.data(), n, c->slices, c->stride, n, kd, cudaMemcpyDeviceToHost, s));
+  if (!tail.empty())
+    CK(cudaMemcpyAsync(tail.data(), c->tail, tail.size(), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  {
+    img.clear();
+    auto put32 = [&](uint32_t v) {
+      for (int b = 0; b < 4; ++b) img.push_back((uint8_t)(v >> (8 * b)));
+    };
+    const uint64_t ub = (uint64_t)c->base;
+    put32((uint32_t)ub);
+    put32((uint32_t)(ub >> 32));
+    put32(n);
+    put32(c->ilen);
+    put32(c->dlen);
+    img.push_back((uint8_t)c->m);
+    std::vector<uint8_t> bin(8 + 4 * nw);
+    for (uint32_t col = 0; col < c->m; ++col) {
+      // BitVec::to_binary: u64 nbits, then the words (bit-vec lib.rs:399-406)
+      for (int b = 0; b < 8; ++b) bin[b] = (uint8_t)((uint64_t)n >> (8 * b));
+      for (size_t w = 0; w < nw; ++w)
+        for (int b = 0; b < 4; ++b) bin[8 + 4 * w + b] = (uint8_t)(bits[col * nw + w] >> (8 * b));
+      std::vector<uint8_t> bm = (c->flags & BUFF_FLAG_RAW_BITMAPS)
+                                    ? bin
+                                    : buffsnappy::compress(bin.data(), bin.size());
+      img.push_back(c->majors[col]);
+      put32((uint32_t)bm.size());
+      img.insert(img.end(), bm.begin(), bm.end());
+      put32(c->nout[col]);
+      img.insert(img.end(), ob.begin() + c->oofs[col], ob.begin() + c->oofs[col] + c->nout[col]);
+    }
+    if (c->m) img.push_back(0);  // finish_write_byte before the dense region
+    for (uint8_t &b : dense) b ^= 0x80;  // the dense slices are stored unflipped
+    img.insert(img.end(), dense.begin(), dense.end());
+    img.insert(img.end(), tail.begin(), tail.end());
+  }
+done:
+  return rc;
+}
+
+int filter_major_impl(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                      cudaStream_t s, bool is_range) {
+  if (!c || (!words && c->n > 0)) return BUFF_EINVAL;
+  if (c->layout != 1) return BUFF_ENOTSUP;
+  const uint32_t n = c->n, nw = (n + 31) / 32;
+  int rc = BUFF_OK;
+  uint32_t *dwords = words;
+  unsigned long long *dcount = nullptr;
+  const bool words_host = n > 0 && !is_device_ptr(words);
+  const bool count_host = count && !is_device_ptr(count);
+  const int64_t fp = fetch_fixed_host(pred, c->precision_exp, c->dlen);
+  const bool early = fp < c->base;  // (buff_simd.rs:886-889, 1939-1942)
+  uint8_t tb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  uint32_t ttail = 0;
+  if (!early) {
+    const uint64_t t = (uint64_t)(fp - c->base);
+    for (uint32_t j = 0; j < c->k; ++j) tb[j] = (uint8_t)(t >> (c->fixed_len - 8 * (j + 1)));
+    ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
+  }
+  if (words_host) CK(scratch(&dwords, nw, s));
+  if (count) {
+    if (count_host)
+      CK(scratch(&dcount, 1, s));
+    else
+      dcount = reinterpret_cast<unsigned long long *>(count);
+    CK(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s));
+  }
+  if (early)
+    CK(buffk::launch_fill_words(dwords, n, is_range ? 0xFFFFFFFFu : 0u, dcount, s));
+  else
+    CK(buffk::major_filter(c, is_range ? 1 : 0, tb, ttail, dwords, dcount, s));
+  if (words_host) CK(cudaMemcpyAsync(words, dwords, (size_t)nw * 4, cudaMemcpyDeviceToHost, s));
+  if (count_host) CK(cudaMemcpyAsync(count, dcount, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  if (words_host || count_host) CK(cudaStreamSynchronize(s));
+done:
+  if (words_host && dwords) cudaFreeAsync(dwords, s);
+  if (count_host && dcount) cudaFreeAsync(dcount, s);
+  return rc;
+}
+
 }  // namespace
 
 // ================================================================ C ABI
@@ -495,13 +725,32 @@ int buff_col_get_info(const buff_col *c, buff_col_info *info) {
   info->prec = c->prec;
   info->precision_exp = c->precision_exp;
   info->flags = c->flags;
+  info->outlier_cols = c->m;
   info->serialized_bytes = serialized_size(c);
   info->device_bytes = (uint64_t)c->k * c->stride + c->tail_alloc;
+  if (c->layout == 1) {
+    info->device_bytes = (uint64_t)(c->k - c->m) * c->stride + c->tail_alloc +
+                         (uint64_t)c->m * c->nwp * 8 + c->oofs[c->m];
+    info->serialized_bytes = 0;  // known after compressing the bitmaps (buff_serialize)
+  }
   return BUFF_OK;
 }
 
 int buff_serialize(const buff_col *c, uint8_t *out, uint64_t cap, uint64_t *len, void *stream) {
   if (!c || !len) return BUFF_EINVAL;
+  if (c->layout == 1) {
+    std::vector<uint8_t> img;
+    const int st = major_image(c, img, S(stream));
+    if (st) return st;
+    *len = img.size();
+    if (!out || cap < img.size()) return BUFF_EINVAL;
+    if (is_device_ptr(out)) {
+      const cudaError_t e = cudaMemcpy(out, img.data(), img.size(), cudaMemcpyHostToDevice);
+      return cuda_status(e);
+    }
+    memcpy(out, img.data(), img.size());
+    return BUFF_OK;
+  }
   const uint64_t need = serialized_size(c);
   *len = need;
   if (!out || cap < need) return BUFF_EINVAL;
@@ -589,6 +838,7 @@ done:
 
 int buff_decode(const buff_col *c, double *out, void *stream) {
   if (!c || (!out && c->n)) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns: the *_majority calls
   if (c->n == 0) return BUFF_OK;
   cudaStream_t s = S(stream);
   int rc = BUFF_OK;
@@ -607,6 +857,7 @@ done:
 
 int buff_decode_at_precision(const buff_col *c, uint32_t precision, double *out, void *stream) {
   if (!c || (!out && c->n)) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns: the *_majority calls
   uint32_t total = 0;
   int rc = precision_bits(c, precision, &total);
   if (rc) return rc;
@@ -651,6 +902,7 @@ int buff_equal_filter_with_slice(const buff_col *c, double pred, uint32_t *words
 
 int buff_sum_partials_async(const buff_col *c, uint64_t *dev_partials, void *stream) {
   if (!c || !dev_partials) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns: the *_majority calls
   return sum_partials(c, c->fixed_len, reinterpret_cast<unsigned long long *>(dev_partials),
                       S(stream));
 }
@@ -674,6 +926,7 @@ int buff_sum_finish(const buff_col *c, const uint64_t *parts, buff_sum_result *o
 
 int buff_sum(const buff_col *c, buff_sum_result *out, void *stream) {
   if (!c || !out) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns: the *_majority calls
   cudaStream_t s = S(stream);
   uint64_t parts[9] = {0};
   unsigned long long *d = nullptr;
@@ -692,6 +945,7 @@ done:
 
 int buff_sum_at_precision(const buff_col *c, uint32_t precision, double *out, void *stream) {
   if (!c || !out) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns: the *_majority calls
   uint32_t total = 0;
   int rc = precision_bits(c, precision, &total);
   if (rc) return rc;
@@ -715,6 +969,7 @@ done:
 
 int buff_max_async(const buff_col *c, uint64_t *dev_max_code, void *stream) {
   if (!c || !dev_max_code) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns: the *_majority calls
   cudaStream_t s = S(stream);
   cudaError_t e = cudaMemsetAsync(dev_max_code, 0, sizeof(uint64_t), s);
   if (e != cudaSuccess) return cuda_status(e);
@@ -725,6 +980,7 @@ int buff_max_async(const buff_col *c, uint64_t *dev_max_code, void *stream) {
 int buff_max(const buff_col *c, double *max_value, uint64_t *max_code, uint32_t *argmax_words,
              uint64_t *argmax_count, void *stream) {
   if (!c) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns: the *_majority calls
   cudaStream_t s = S(stream);
   int rc = BUFF_OK;
   const uint32_t nw = (c->n + 31) / 32;
@@ -768,6 +1024,328 @@ int buff_max(const buff_col *c, double *max_value, uint64_t *max_code, uint32_t 
 done:
   if (d) cudaFreeAsync(d, s);
   if (dwords && !words_dev) cudaFreeAsync(dwords, s);
+  return rc;
+}
+
+// ---------------------------------------------------------------- buff-major ABI
+
+int buff_encode_majority_f64(const double *values, uint64_t n, uint64_t scale, uint32_t flags,
+                             void *stream, buff_col **out) {
+  return encode_major_impl<double>(values, n, scale, flags, S(stream), out);
+}
+
+int buff_encode_majority_f32(const float *values, uint64_t n, uint64_t scale, uint32_t flags,
+                             void *stream, buff_col **out) {
+  return encode_major_impl<float>(values, n, scale, flags, S(stream), out);
+}
+
+int buff_deserialize_majority(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                              void *stream, buff_col **out) {
+  if (!out || !bytes) return BUFF_EINVAL;
+  *out = nullptr;
+  if (flags & BUFF_FLAG_INTENDED) return BUFF_ENOTSUP;
+  if (len < 21) return BUFF_ECORRUPT;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  std::vector<uint8_t> host;
+  const uint8_t *b = bytes;
+  buff_col *c = nullptr;
+  std::vector<std::vector<uint32_t>> bms;
+  std::vector<const uint8_t *> outl;
+  size_t pos = 21, dense_at = 21;
+  uint32_t w5[5], m;
+  if (is_device_ptr(bytes)) {
+    host.resize(len);
+    CK(cudaMemcpyAsync(host.data(), bytes, len, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    b = host.data();
+  }
+  for (int i = 0; i < 5; ++i)
+    w5[i] = (uint32_t)b[4 * i] | ((uint32_t)b[4 * i + 1] << 8) | ((uint32_t)b[4 * i + 2] << 16) |
+            ((uint32_t)b[4 * i + 3] << 24);
+  m = b[20];
+  c = new_col(scale, flags);
+  if (!c) return BUFF_ENOMEM;
+  c->layout = 1;
+  c->base = (int64_t)((uint64_t)w5[0] | ((uint64_t)w5[1] << 32));
+  c->n = w5[2];
+  c->ilen = w5[3];
+  c->dlen = w5[4];
+  {
+    const uint32_t fl = c->ilen + c->dlen;
+    if (fl > 64 || c->dlen > 1000 || fl < 8 || m > fl / 8) {
+      rc = fl < 8 ? BUFF_ENOTSUP : BUFF_ECORRUPT;
+      goto done;
+    }
+    set_layout(c, fl);
+    c->m = m;
+    const size_t nw = ((size_t)c->n + 31) / 32;
+    auto rd32 = [&](size_t at) -> uint32_t {
+      return (uint32_t)b[at] | ((uint32_t)b[at + 1] << 8) | ((uint32_t)b[at + 2] << 16) |
+             ((uint32_t)b[at + 3] << 24);
+    };
+    uint64_t off = 0;
+    for (uint32_t col = 0; col < m; ++col) {
+      if (pos + 5 > len) {
+        rc = BUFF_ECORRUPT;
+        goto done;
+      }
+      c->majors[col] = b[pos];
+      const uint32_t bml = rd32(pos + 1);
+      if (pos + 5 + (uint64_t)bml + 4 > len) {
+        rc = BUFF_ECORRUPT;
+        goto done;
+      }
+      std::vector<uint8_t> bin;
+      if (flags & BUFF_FLAG_RAW_BITMAPS) {
+        bin.assign(b + pos + 5, b + pos + 5 + bml);
+      } else if (!buffsnappy::decompress(b + pos + 5, bml, bin)) {
+        rc = BUFF_ECORRUPT;
+        goto done;
+      }
+      // BitVec::from_binary (bit-vec lib.rs:409-428)
+      std::vector<uint32_t> words(nw, 0);
+      for (size_t at = 8, w = 0; at + 4 <= bin.size() && w < nw; at += 4, ++w)
+        words[w] = (uint32_t)bin[at] | ((uint32_t)bin[at + 1] << 8) |
+                   ((uint32_t)bin[at + 2] << 16) | ((uint32_t)bin[at + 3] << 24);
+      if (nw && (c->n & 31)) words[nw - 1] &= (1u << (c->n & 31)) - 1u;
+      bms.push_back(std::move(words));
+      const size_t np = pos + 5 + bml;
+      const uint32_t nout = rd32(np);
+      if (np + 4 + (uint64_t)nout > len) {
+        rc = BUFF_ECORRUPT;
+        goto done;
+      }
+      c->nout[col] = nout;
+      c->oofs[col] = off;
+      off += nout;
+      outl.push_back(b + np + 4);
+      pos = np + 4 + nout;  // the pad written after the outliers holds the next major
+    }
+    c->oofs[m] = off;
+    dense_at = m ? pos + 1 : 21;
+    const uint32_t kd = c->k - m;
+    const uint64_t need = dense_at + (uint64_t)kd * c->n + ((uint64_t)c->n * c->r + 7) / 8;
+    if (need > len) {
+      rc = BUFF_ECORRUPT;
+      goto done;
+    }
+    const uint32_t k = c->k;
+    c->k = kd;
+    rc = alloc_col(c, s);
+    c->k = k;
+    if (rc) goto done;
+    c->nwp = c->stride / 32;
+    if (kd && c->n) {
+      CK(cudaMemcpy2DAsync(c->slices, c->stride, b + dense_at, c->n, c->n, kd,
+                           cudaMemcpyHostToDevice, s));
+      CK(buffk::flip_bytes(c->slices, (size_t)kd * c->stride, s));
+      if (c->stride > c->n)
+        CK(cudaMemset2DAsync(c->slices + c->n, c->stride, 0x80, c->stride - c->n, kd, s));
+    }
+    CK(cudaMemsetAsync(c->tail, 0, c->tail_alloc, s));
+    if (c->tail_bytes)
+      CK(cudaMemcpyAsync(c->tail, b + dense_at + (uint64_t)kd * c->n, c->tail_bytes,
+                         cudaMemcpyHostToDevice, s));
+    if (m) {
+      CK(scratch(&c->obits, (size_t)m * c->nwp, s));
+      CK(scratch(&c->orank, (size_t)m * (c->nwp + 16), s));
+      CK(scratch(&c->obytes, off + 16, s));
+      CK(cudaMemsetAsync(c->obits, 0, sizeof(uint32_t) * m * c->nwp, s));
+      for (uint32_t col = 0; col < m; ++col) {
+        CK(cudaMemcpyAsync(c->obits + col * c->nwp, bms[col].data(), nw * 4,
+                           cudaMemcpyHostToDevice, s));
+        if (c->nout[col])
+          CK(cudaMemcpyAsync(c->obytes + c->oofs[col], outl[col], c->nout[col],
+                             cudaMemcpyHostToDevice, s));
+      }
+      CK(buffk::major_index(c, s));
+    }
+    CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (rc != BUFF_OK) {
+    free_col(c);
+    return rc;
+  }
+  *out = c;
+  return BUFF_OK;
+}
+
+int buff_range_filter_majority(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                               void *stream) {
+  return filter_major_impl(c, pred, words, count, S(stream), true);
+}
+
+int buff_equal_filter_majority(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                               void *stream) {
+  return filter_major_impl(c, pred, words, count, S(stream), false);
+}
+
+int buff_decode_majority(const buff_col *c, double *out, void *stream) {
+  if (!c || (!out && c->n)) return BUFF_EINVAL;
+  if (c->layout != 1) return BUFF_ENOTSUP;
+  for (uint32_t col = 0; col < c->m; ++col)
+    if (c->nout[col] == 0) return BUFF_EREFPANIC;  // outlier_iter.next().unwrap() (:680)
+  if (c->n == 0) return BUFF_OK;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  double *d = out;
+  const bool stage = !is_device_ptr(out) || (reinterpret_cast<uintptr_t>(out) & 15);
+  if (stage) CK(scratch(&d, c->n, s));
+  if (c->m)
+    CK(buffk::major_decode(c, d, s));
+  else
+    CK(buffk::launch_decode(c, c->fixed_len, 0, d, s));
+  if (stage) {
+    CK(cudaMemcpyAsync(out, d, (size_t)c->n * 8, cudaMemcpyDefault, s));
+    CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (stage && d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+int buff_sum_majority(const buff_col *c, buff_sum_result *out, void *stream) {
+  if (!c || !out) return BUFF_EINVAL;
+  if (c->layout != 1) return BUFF_ENOTSUP;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  unsigned long long *d = nullptr;
+  uint64_t h[24] = {0};
+  const uint32_t kd = c->k - c->m;
+  CK(scratch(&d, 24, s));
+  CK(cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 24, s));
+  for (uint32_t col = 0; col < c->m; ++col)
+    if (c->nout[col]) CK(buffk::major_bytesum(c->obytes + c->oofs[col], c->nout[col], d + col, s));
+  if (c->n) CK(buffk::launch_sum(c, kd, c->r, d + 8, s));
+  CK(cudaMemcpyAsync(h, d, sizeof(uint64_t) * 24, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  {
+    // buff_sum_majority (buff_simd.rs:2294-2442)
+    memset(out, 0, sizeof(*out));
+    uint64_t parts[9] = {0};
+    uint32_t np = 0;
+    for (uint32_t col = 0; col < c->m; ++col)
+      parts[np++] = h[col] + (uint64_t)c->majors[col] * ((uint64_t)c->n - c->nout[col]);
+    for (uint32_t j = 0; j < kd; ++j) parts[np++] = h[8 + j];
+    if (c->r) parts[np++] = h[8 + kd];
+    const int32_t ilen_i = (int32_t)c->ilen;
+    double sum_base = (double)c->n * (double)c->base;
+    sum_base = sum_base / ldexp(1.0, (int)c->dlen);
+    double sum = 0.0;
+    int32_t processed = 0;
+    uint32_t remain = c->fixed_len;
+    bool no_base = false;
+    for (uint32_t i = 0; i < c->k; ++i) {
+      remain -= 8;
+      processed += 8;
+      sum = sum + (double)parts[i] / ldexp(1.0, processed - ilen_i);
+      if (i >= c->m && remain == 0) no_base = true;  // a dense slice ends the code
+    }
+    if (!no_base) {
+      if (remain > 0) {
+        processed += (int32_t)remain;
+        sum = sum + (double)parts[c->k] / ldexp(1.0, processed - ilen_i);
+      }
+      sum += sum_base;
+    }
+    out->sum = sum;
+    __int128 acc = (__int128)c->n * (__int128)c->base;
+    for (uint32_t j = 0; j < c->k; ++j) acc += (__int128)parts[j] << (c->fixed_len - 8 * (j + 1));
+    if (c->r) acc += (__int128)parts[c->k];
+    out->exact_num_lo = (int64_t)(uint64_t)acc;
+    out->exact_num_hi = (int64_t)(acc >> 64);
+    out->exact = ldexp((double)acc, -(int)c->dlen);
+    out->n_partials = np;
+    for (uint32_t j = 0; j < np; ++j) out->partials[j] = parts[j];
+  }
+done:
+  if (d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+int buff_max_majority(const buff_col *c, double *max_value, uint64_t *max_code,
+                      uint32_t *argmax_words, uint64_t *argmax_count, void *stream) {
+  if (!c) return BUFF_EINVAL;
+  if (c->layout != 1) return BUFF_ENOTSUP;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  uint32_t *cand = nullptr, *buf = nullptr;
+  unsigned long long *cnt = nullptr;
+  uint64_t mx = 0, amc = 0;
+  const size_t nw = ((size_t)c->n + 31) / 32;
+  const uint32_t kd = c->k - c->m;
+  uint32_t hb[2];
+  auto fetch = [&](uint32_t *hv) -> cudaError_t {
+    cudaError_t e = cudaMemcpyAsync(hv, buf, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
+  };
+  CK(scratch(&cand, c->nwp, s));
+  CK(scratch(&buf, 2, s));
+  CK(scratch(&cnt, 1, s));
+  CK(cudaMemsetAsync(cand, 0, sizeof(uint32_t) * c->nwp, s));
+  CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+  if (c->n) {
+    CK(buffk::launch_fill_words(cand, c->n, 0xFFFFFFFFu, nullptr, s));
+    for (uint32_t col = 0; col < c->m; ++col) {  // buff_simd.rs:2466-2557
+      const uint32_t sh = c->fixed_len - 8 * (col + 1), M = c->majors[col];
+      CK(cudaMemsetAsync(buf, 0, 8, s));
+      CK(buffk::major_candmax(c, col, col == 0 ? nullptr : cand, buf, s));
+      CK(fetch(hb));
+      if (col == 0) {
+        if (hb[1] && hb[0] > M) {
+          CK(buffk::major_select(c, 0, cand, 1, hb[0], s));
+          mx |= (uint64_t)hb[0] << sh;
+        } else {
+          CK(buffk::major_select(c, 0, cand, 0, 0, s));
+          mx |= (uint64_t)M << sh;
+        }
+        continue;
+      }
+      if (!hb[1]) {  // no candidate is an outlier: the major byte is not added
+        CK(buffk::major_select(c, col, cand, 2, 0, s));
+        continue;
+      }
+      if (hb[0] > M) {
+        CK(buffk::major_select(c, col, cand, 1, hb[0], s));
+        mx |= (uint64_t)hb[0] << sh;
+      } else {
+        CK(buffk::major_select(c, col, cand, 2, 0, s));
+        mx |= (uint64_t)M << sh;
+      }
+    }
+    for (uint32_t j = 0; j < kd; ++j) {  // dense slices (:2560-2612)
+      const uint32_t sh = c->fixed_len - 8 * (c->m + j + 1);
+      const uint8_t *sl = c->slices + (size_t)j * c->stride;
+      CK(cudaMemsetAsync(buf, 0, 8, s));
+      CK(buffk::cand_max(sl, nullptr, 0, cand, nw, buf, s));
+      CK(fetch(hb));
+      CK(buffk::cand_select(sl, nullptr, 0, cand, nw, hb[0], nullptr, s));
+      mx |= (uint64_t)hb[0] << sh;
+    }
+    if (c->r) {  // tail (:2613-2651): its candidates are the arg-max rows
+      CK(cudaMemsetAsync(buf, 0, 8, s));
+      CK(buffk::cand_max(nullptr, c->tail, c->r, cand, nw, buf, s));
+      CK(fetch(hb));
+      CK(buffk::cand_select(nullptr, c->tail, c->r, cand, nw, hb[0], cnt, s));
+      mx |= hb[0];
+    } else {
+      CK(cudaMemsetAsync(cand, 0, sizeof(uint32_t) * c->nwp, s));
+    }
+  }
+  if (argmax_words && c->n)
+    CK(cudaMemcpyAsync(argmax_words, cand, nw * 4, cudaMemcpyDefault, s));
+  CK(cudaMemcpyAsync(&amc, cnt, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (max_code) *max_code = mx;
+  if (max_value) *max_value = (double)(int64_t)((uint64_t)c->base + mx) / ldexp(1.0, (int)c->dlen);
+  if (argmax_count) *argmax_count = amc;
+done:
+  if (cand) cudaFreeAsync(cand, s);
+  if (buf) cudaFreeAsync(buf, s);
+  if (cnt) cudaFreeAsync(cnt, s);
   return rc;
 }
 

@@ -29,6 +29,19 @@ struct buff_col {
   uint8_t *tail;
   size_t tail_bytes;  // bytes of the packed tail (ceil(n*r/8)), excluding padding
   size_t tail_alloc;
+  // buff-major layout (compress/buff_simd.rs:317-630): the first m full bytes
+  // are sparse columns (major byte + outlier rows + outlier bytes); `slices`
+  // then holds only the k - m dense slices (still flipped on the device).
+  uint32_t layout;      // 0: buff-simd, 1: buff-major
+  uint32_t m;           // sparse columns
+  uint8_t majors[8];
+  uint32_t nout[8];     // outliers per sparse column
+  uint32_t olast[8];    // row of the last outlier per sparse column
+  size_t nwp;           // bitmap words per sparse column (stride / 32)
+  uint32_t *obits;      // m x nwp outlier bitmaps (BitVec<u32> words)
+  uint32_t *orank;      // m x (nwp + 1) outliers before each word
+  uint8_t *obytes;      // outlier bytes of all sparse columns, row order
+  uint64_t oofs[9];     // start of each column's outlier bytes
 };
 
 namespace buffk {
@@ -75,8 +88,12 @@ cudaError_t launch_encode_reduce_f64(const double *x, uint32_t n, uint32_t from,
 cudaError_t launch_encode_reduce_f32(const float *x, uint32_t n, uint32_t from, int32_t pexp,
                                      uint32_t dlen, int keys, int find_brk, EncStats *d_out,
                                      cudaStream_t s);
-cudaError_t launch_encode_scatter_f64(const double *x, const buff_col *c, cudaStream_t s);
-cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStream_t s);
+// Quantize and slice; the first `nlead` slices are written to `lead` (stride
+// apart) instead of the column's slices (the sparse columns of buff-major).
+cudaError_t launch_encode_scatter_f64(const double *x, const buff_col *c, cudaStream_t s,
+                                      uint8_t *lead = nullptr, uint32_t nlead = 0);
+cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStream_t s,
+                                      uint8_t *lead = nullptr, uint32_t nlead = 0);
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t s);
 cudaError_t launch_fill_words(uint32_t *words, uint32_t n, uint32_t value,
                               unsigned long long *count, cudaStream_t s);
@@ -90,6 +107,25 @@ cudaError_t launch_argmax(const buff_col *c, const unsigned long long *d_max, ui
 // Decode with `total` leading bits (REF) or masked to `total` bits (INTENDED).
 cudaError_t launch_decode(const buff_col *c, uint32_t total, int intended_mask, double *out,
                           cudaStream_t s);
+
+// buff-major layout (buff_major.cu)
+cudaError_t major_build_sparse(buff_col *c, const uint8_t *lead, cudaStream_t s);
+cudaError_t major_index(buff_col *c, cudaStream_t s);
+cudaError_t flip_bytes(uint8_t *p, size_t nbytes, cudaStream_t s);
+cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, uint32_t ttail,
+                         uint32_t *words, unsigned long long *count, cudaStream_t s);
+cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out,
+                          cudaStream_t s);
+cudaError_t major_candmax(const buff_col *c, uint32_t col, const uint32_t *cand, uint32_t *out,
+                          cudaStream_t s);
+cudaError_t major_select(const buff_col *c, uint32_t col, uint32_t *cand, int mode,
+                         uint32_t value, cudaStream_t s);
+cudaError_t cand_max(const uint8_t *slice, const uint8_t *tail, uint32_t r, const uint32_t *cand,
+                     size_t nw, uint32_t *out, cudaStream_t s);
+cudaError_t cand_select(const uint8_t *slice, const uint8_t *tail, uint32_t r, uint32_t *cand,
+                        size_t nw, uint32_t value, unsigned long long *count, cudaStream_t s);
+cudaError_t popcount_words(const uint32_t *w, size_t nw, unsigned long long *out, cudaStream_t s);
+cudaError_t major_decode(const buff_col *c, double *out, cudaStream_t s);
 
 int num_sms(int device);
 void count_launch(uint64_t n = 1);

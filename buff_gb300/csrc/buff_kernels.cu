@@ -14,177 +14,18 @@
 
 #include <atomic>
 
+#include "buff_device.cuh"
 #include "buff_internal.h"
 
 namespace buffk {
 
 namespace {
 
+using namespace dev;
+
 std::atomic<uint64_t> g_launches{0};
 
-constexpr uint32_t H = 0x80808080u;
-constexpr int kThreads = 256;
-constexpr int kU = 4;  // independent 16-byte loads a lane keeps in flight in streaming loops
-
-__device__ __forceinline__ uint4 ld_stream(const uint8_t *p) {
-  uint4 v;
-  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
-               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-               : "l"(p));
-  return v;
-}
-
-// Per-slice compare constants for an unflipped target byte t.
-struct ByteTarget {
-  uint32_t lo1;  // (t & 0x7f) + 1 in every byte
-  uint32_t lo0;  // (t & 0x7f) in every byte
-  uint32_t th;   // all ones when t >= 0x80
-};
-
-__host__ __device__ __forceinline__ ByteTarget make_target(uint32_t t) {
-  ByteTarget b;
-  b.lo0 = (t & 0x7Fu) * 0x01010101u;
-  b.lo1 = ((t & 0x7Fu) + 1u) * 0x01010101u;
-  b.th = (t & 0x80u) ? 0xFFFFFFFFu : 0u;
-  return b;
-}
-
-// SWAR compare of 4 flipped bytes w (a = w ^ 0x80 unflipped) against t.
-// MSB of each byte of *gt is a > t, of *eq is a == t.  No borrow crosses a
-// byte: (w|H) - lo1 and (w|H) - lo0 stay within [0, 255] per byte.
-__device__ __forceinline__ void cmp4(uint32_t w, const ByteTarget &t, uint32_t &gt,
-                                     uint32_t &eq) {
-  uint32_t wh = w | H;
-  uint32_t d1 = wh - t.lo1;  // MSB: a_lo > t_lo
-  uint32_t d0 = wh - t.lo0;  // MSB: a_lo >= t_lo
-  // a_hi = ~w_hi.  t_hi = 1: a > t iff a_hi & (a_lo > t_lo); t_hi = 0: a_hi | (a_lo > t_lo).
-  gt = ((t.th & ~w & d1) | (~t.th & (~w | d1))) & H;
-  eq = d0 & ~d1 & (w ^ t.th) & H;  // a_hi == t_hi  <=>  w_hi != t_hi
-}
-
-
-// The 16 r-bit tail fields of rows [16v, 16v+16): 2r bytes at byte 2r*v.
-__device__ __forceinline__ void load_tail16(const uint8_t *tail, uint32_t v, uint32_t r,
-                                            unsigned long long &lo, unsigned long long &hi) {
-  const uint16_t *p = reinterpret_cast<const uint16_t *>(tail + (size_t)2 * r * v);
-  lo = 0;
-  hi = 0;
-#pragma unroll
-  for (uint32_t i = 0; i < 7; ++i) {
-    if (i < r) {
-      unsigned long long h = __ldg(p + i);
-      if (i < 4)
-        lo |= h << (16 * i);
-      else
-        hi |= h << (16 * (i - 4));
-    }
-  }
-}
-
-__device__ __forceinline__ uint32_t field16(unsigned long long lo, unsigned long long hi,
-                                            uint32_t i, uint32_t r) {
-  uint32_t p = i * r;
-  unsigned long long v;
-  if (p >= 64)
-    v = hi >> (p - 64);
-  else if (p + r > 64)
-    v = (lo >> p) | (hi << (64 - p));
-  else
-    v = lo >> p;
-  return (uint32_t)v & ((1u << r) - 1u);
-}
-
-template <typename T>
-__device__ __forceinline__ long long warp_min(long long v) {
-  for (int o = 16; o; o >>= 1) {
-    long long x = __shfl_xor_sync(0xFFFFFFFFu, v, o);
-    v = x < v ? x : v;
-  }
-  return v;
-}
-__device__ __forceinline__ long long warp_max_ll(long long v) {
-  for (int o = 16; o; o >>= 1) {
-    long long x = __shfl_xor_sync(0xFFFFFFFFu, v, o);
-    v = x > v ? x : v;
-  }
-  return v;
-}
-__device__ __forceinline__ unsigned long long warp_max_ull(unsigned long long v) {
-  for (int o = 16; o; o >>= 1) {
-    unsigned long long x = __shfl_xor_sync(0xFFFFFFFFu, v, o);
-    v = x > v ? x : v;
-  }
-  return v;
-}
-__device__ __forceinline__ unsigned long long warp_sum_ull(unsigned long long v) {
-  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
-  return v;
-}
-
 // ---------------------------------------------------------------- encode
-
-// Exact f32 -> f64 widening on the integer pipes (the FP64 pipe of this part
-// is narrow): returns the IEEE-754 binary64 bits of the binary32 value `fb`.
-__device__ __forceinline__ unsigned long long f32_to_f64_bits(uint32_t fb) {
-  const unsigned long long sgn = (unsigned long long)(fb >> 31) << 63;
-  const uint32_t e = (fb >> 23) & 0xFFu;
-  const uint32_t m = fb & 0x7FFFFFu;
-  if (e == 0xFFu)  // inf / NaN (NaN quieted, as the host conversion does)
-    return sgn | (0x7FFull << 52) | ((unsigned long long)m << 29) | (m ? (1ull << 51) : 0ull);
-  if (e == 0) {
-    if (m == 0) return sgn;
-    const int p = 31 - __clz(m);  // subnormal: m * 2^-149, leading bit p
-    return sgn | ((unsigned long long)(p - 149 + 1023) << 52) |
-           (((unsigned long long)m << (52 - p)) & ((1ull << 52) - 1ull));
-  }
-  return sgn | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
-}
-
-// Raw binary64 bits of the input elements, E per 16-byte vector.
-template <typename T>
-struct Elem;
-template <>
-struct Elem<double> {
-  using V = ulonglong2;
-  static constexpr int E = 2;
-  __device__ static unsigned long long bits(const V &v, int j) { return j ? v.y : v.x; }
-  __device__ static unsigned long long one(const double *x, uint32_t i) {
-    return (unsigned long long)__double_as_longlong(__ldg(x + i));
-  }
-};
-template <>
-struct Elem<float> {
-  using V = uint4;
-  static constexpr int E = 4;
-  __device__ static unsigned long long bits(const V &v, int j) {
-    return f32_to_f64_bits(j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w);
-  }
-  __device__ static unsigned long long one(const float *x, uint32_t i) {
-    return f32_to_f64_bits((uint32_t)__float_as_uint(__ldg(x + i)));
-  }
-};
-
-// fetch_fixed_aligned on raw binary64 bits.
-__device__ __forceinline__ long long fetch_bits(unsigned long long bdu, int pexp, uint32_t dlen) {
-  const int exp = (int)((bdu >> 52) & 0x7FFu) - 1023;
-  if (exp < pexp) return 0;
-  const int sh = 63 - exp - (int)dlen;
-  unsigned long long f = ((bdu << 11) | 0x8000000000000000ull) >> (sh & 63);
-  if (bdu >> 63) f = ~(f - 1ull);
-  return (long long)f;
-}
-
-// Signed-integer key with the order of the binary64 values (-0 < +0; NaNs
-// are extremal).  fetch_fixed_aligned is non-decreasing on finite values
-// whose shift does not wrap, so min/max can be taken on keys and quantized
-// once.
-__device__ __forceinline__ long long order_key(unsigned long long b) {
-  return (long long)(b ^ ((unsigned long long)((long long)b >> 63) >> 1));
-}
-__device__ __forceinline__ unsigned long long key_bits(long long k) {
-  const unsigned long long u = (unsigned long long)k;
-  return u ^ ((unsigned long long)(k >> 63) >> 1);
-}
 
 struct MinMax {
   long long lo, hi;
@@ -329,7 +170,8 @@ __global__ void __launch_bounds__(kThreads) k_encode_finalize(const T *__restric
 template <typename T, int K>
 __global__ void __launch_bounds__(kThreads) k_encode_scatter(
     const T *__restrict__ x, uint32_t n, int pexp, uint32_t dlen, long long base, uint32_t fl,
-    uint32_t r, uint8_t *__restrict__ slices, size_t stride, uint8_t *__restrict__ tail) {
+    uint32_t r, uint8_t *__restrict__ slices, size_t stride, uint8_t *__restrict__ tail,
+    uint8_t *__restrict__ lead, uint32_t nlead) {
   constexpr uint32_t k = K;
   using EL = Elem<T>;
   constexpr int E = EL::E;
@@ -404,7 +246,9 @@ __global__ void __launch_bounds__(kThreads) k_encode_scatter(
 #pragma unroll
     for (int sl = 0; sl < K; ++sl) {
       uint4 v = *reinterpret_cast<const uint4 *>(ws + sl * kRowChunk + lane * 16);
-      __stcs(reinterpret_cast<uint4 *>(slices + sl * stride + r0 + lane * 16), v);
+      // the first `nlead` slices go to `lead` (buff-major sparse columns)
+      uint8_t *dst = (uint32_t)sl < nlead ? lead + sl * stride : slices + (sl - nlead) * stride;
+      __stcs(reinterpret_cast<uint4 *>(dst + r0 + lane * 16), v);
     }
     if (r == 1) {  // one bit per row: gather bit 0 of 8 bytes with one multiply
       const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(ws + k * kRowChunk + lane * 16);
@@ -444,62 +288,6 @@ __global__ void __launch_bounds__(kThreads) k_encode_scatter(
 // eq &= eq_j), then the packed tail.  Rows >= full_rows stay clear, which
 // reproduces the reference's 32-byte SIMD loop that never reaches the rows
 // after the last full 32-row block.
-// 32 flipped slice bytes (rows row0..row0+31) in eight 32-bit words.
-struct Bytes32 {
-  uint32_t w[8];
-};
-
-// 256-bit non-allocating load (sm_100+; the address is 32-byte aligned).
-__device__ __forceinline__ Bytes32 ld_stream32(const uint8_t *p) {
-  Bytes32 b;
-  asm volatile("ld.global.nc.L1::no_allocate.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(b.w[0]), "=r"(b.w[1]), "=r"(b.w[2]), "=r"(b.w[3]), "=r"(b.w[4]),
-                 "=r"(b.w[5]), "=r"(b.w[6]), "=r"(b.w[7])
-               : "l"(p));
-  return b;
-}
-__device__ __forceinline__ Bytes32 ld_cand32(const uint8_t *p) {
-  const uint4 lo = __ldg(reinterpret_cast<const uint4 *>(p));
-  const uint4 hi = __ldg(reinterpret_cast<const uint4 *>(p + 16));
-  Bytes32 b;
-  b.w[0] = lo.x;
-  b.w[1] = lo.y;
-  b.w[2] = lo.z;
-  b.w[3] = lo.w;
-  b.w[4] = hi.x;
-  b.w[5] = hi.y;
-  b.w[6] = hi.z;
-  b.w[7] = hi.w;
-  return b;
-}
-
-// Byte MSBs of two words (4 rows each) -> 8 row-ordered bits in the low byte:
-// with c = (m0 >> 4) | m1 the MSBs sit at bits 8b+3 (row b) and 8b+7 (row
-// 4+b); multiplying by 2^29 + 2^22 + 2^15 + 2^8 moves exactly those eight bits,
-// without collisions, to bits 32..39 of the 64-bit product.
-__device__ __forceinline__ uint32_t msb8(uint32_t m0, uint32_t m1) {
-  return __umulhi((m0 >> 4) | m1, 0x20408100u);
-}
-// MSBs of eight words -> the 32-bit bitmap word (bit i = byte i).
-__device__ __forceinline__ uint32_t gather32(const uint32_t *m) {
-  const uint32_t a = __byte_perm(msb8(m[0], m[1]), msb8(m[2], m[3]), 0x0040);
-  const uint32_t b = __byte_perm(msb8(m[4], m[5]), msb8(m[6], m[7]), 0x0040);
-  return __byte_perm(a, b, 0x5410);
-}
-
-// Per-byte compares of flipped bytes w against an unflipped target whose top
-// bit is TH: MSB of each byte of the result.  (a = w ^ 0x80; a_lo = w_lo.)
-template <bool TH>
-__device__ __forceinline__ uint32_t gt4t(uint32_t w, uint32_t lo1) {
-  const uint32_t d1 = (w | H) - lo1;  // MSB: a_lo > t_lo
-  return TH ? (~w & d1 & H) : ((~w | d1) & H);
-}
-template <bool TH>
-__device__ __forceinline__ uint32_t eq4t(uint32_t w, uint32_t lo0, uint32_t lo1) {
-  const uint32_t wh = w | H;
-  return (wh - lo0) & ~(wh - lo1) & (TH ? ~w : w) & H;
-}
-
 // Candidate refinement of one 32-row block (rows whose prefix equals the
 // target so far): the remaining slices, then the packed tail.  Kept out of
 // line: it runs for few blocks and would otherwise inflate the streaming
@@ -648,23 +436,6 @@ __global__ void k_fill_words(uint32_t *words, uint32_t n, uint32_t value,
 }
 
 // ---------------------------------------------------------------- sum
-
-// Weighted popcount of one 32-bit word of a packed stream of `ts`-bit fields
-// whose first bit sits at stream bit `bit0`: sum over set bits b of
-// 2^((bit0 + b) mod ts).  (The sum of all fields of a stream only depends on
-// each bit's position mod ts, not on row boundaries.)
-__device__ __forceinline__ uint32_t wpopc(uint32_t w, uint32_t bit0, uint32_t ts) {
-  if (ts == 1) return __popc(w);
-  uint32_t pat = 0;  // bits 0, ts, 2ts, ...
-  for (uint32_t j = 0; j < 32; j += ts) pat |= 1u << j;
-  const uint32_t phase = bit0 % ts;
-  uint32_t acc = 0;
-  for (uint32_t p = 0; p < ts; ++p) {
-    const uint32_t sh = (p + ts - phase) % ts;  // bits j with (phase + j) % ts == p
-    acc += (uint32_t)__popc(w & (pat << sh)) << p;
-  }
-  return acc;
-}
 
 // byte_fixed_sum (compress/split_double.rs:2127-2208): the per-slice sums of
 // the unflipped bytes and the sum of the packed tail fields, exact in u64.
@@ -915,38 +686,6 @@ __global__ void __launch_bounds__(kThreads) k_argmax(const uint8_t *__restrict__
 
 // ---------------------------------------------------------------- decode
 
-// `(v as f64) / 2^dlen` with integer operations only: round-to-nearest-even
-// of the 64-bit integer to a 53-bit significand, then the exponent lowered by
-// dlen (exact: the result stays a normal double for |v| >= 1 and dlen <= 64).
-// The FP64 pipe of this part is narrow, so the conversion is done on the
-// integer pipes.
-__device__ __forceinline__ double i64_to_f64_scaled(long long v, int dlen) {
-  if (v == 0) return 0.0;
-  const unsigned long long sgn = v < 0 ? 0x8000000000000000ull : 0ull;
-  const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
-  int e = 63 - __clzll(a);  // a in [2^e, 2^(e+1))
-  unsigned long long m;
-  if (e <= 52) {
-    m = a << (52 - e);
-  } else {
-    const int sh = e - 52;
-    const unsigned long long rem = a & ((1ull << sh) - 1ull);
-    const unsigned long long half = 1ull << (sh - 1);
-    m = a >> sh;
-    if (rem > half || (rem == half && (m & 1ull))) {
-      m += 1ull;
-      if (m >> 53) {
-        m >>= 1;
-        e += 1;
-      }
-    }
-  }
-  const unsigned long long bits =
-      sgn | ((unsigned long long)(e - dlen + 1023) << 52) | (m & ((1ull << 52) - 1ull));
-  return __longlong_as_double((long long)bits);
-}
-
-
 // buff_simd256_decode (compress/buff_simd.rs:3252-3357) and the
 // precision-limited decode (compress/split_double.rs:1612-1893).  KS leading
 // slices and `ts` packed bits per row are rebuilt; the reference walks its
@@ -1075,7 +814,8 @@ cudaError_t launch_encode_reduce_f32(const float *x, uint32_t n, uint32_t from, 
 }
 
 template <typename T, int K>
-static cudaError_t scatter_k(const T *x, const buff_col *c, cudaStream_t s) {
+static cudaError_t scatter_k(const T *x, const buff_col *c, uint8_t *lead, uint32_t nlead,
+                             cudaStream_t s) {
   const uint32_t planes = K + (c->r ? 1u : 0u);
   const size_t smem = (size_t)(kThreads / 32) * planes * kRowChunk;
   const void *fn = (const void *)k_encode_scatter<T, K>;
@@ -1087,33 +827,36 @@ static cudaError_t scatter_k(const T *x, const buff_col *c, cudaStream_t s) {
   if (grid > need) grid = need;
   k_encode_scatter<T, K><<<grid, kThreads, smem, s>>>(x, c->n, c->precision_exp, c->dlen, c->base,
                                                       c->fixed_len, c->r, c->slices, c->stride,
-                                                      c->tail);
+                                                      c->tail, lead, nlead);
   count_launch();
   return cudaGetLastError();
 }
 
 template <typename T>
-static cudaError_t scatter_impl(const T *x, const buff_col *c, cudaStream_t s) {
+static cudaError_t scatter_impl(const T *x, const buff_col *c, uint8_t *lead, uint32_t nlead,
+                                cudaStream_t s) {
   if (c->n == 0 || (c->k == 0 && c->r == 0)) return cudaSuccess;
   switch (c->k) {
-    case 0: return scatter_k<T, 0>(x, c, s);
-    case 1: return scatter_k<T, 1>(x, c, s);
-    case 2: return scatter_k<T, 2>(x, c, s);
-    case 3: return scatter_k<T, 3>(x, c, s);
-    case 4: return scatter_k<T, 4>(x, c, s);
-    case 5: return scatter_k<T, 5>(x, c, s);
-    case 6: return scatter_k<T, 6>(x, c, s);
-    case 7: return scatter_k<T, 7>(x, c, s);
-    case 8: return scatter_k<T, 8>(x, c, s);
+    case 0: return scatter_k<T, 0>(x, c, lead, nlead, s);
+    case 1: return scatter_k<T, 1>(x, c, lead, nlead, s);
+    case 2: return scatter_k<T, 2>(x, c, lead, nlead, s);
+    case 3: return scatter_k<T, 3>(x, c, lead, nlead, s);
+    case 4: return scatter_k<T, 4>(x, c, lead, nlead, s);
+    case 5: return scatter_k<T, 5>(x, c, lead, nlead, s);
+    case 6: return scatter_k<T, 6>(x, c, lead, nlead, s);
+    case 7: return scatter_k<T, 7>(x, c, lead, nlead, s);
+    case 8: return scatter_k<T, 8>(x, c, lead, nlead, s);
     default: return cudaErrorInvalidValue;
   }
 }
 
-cudaError_t launch_encode_scatter_f64(const double *x, const buff_col *c, cudaStream_t s) {
-  return scatter_impl<double>(x, c, s);
+cudaError_t launch_encode_scatter_f64(const double *x, const buff_col *c, cudaStream_t s,
+                                      uint8_t *lead, uint32_t nlead) {
+  return scatter_impl<double>(x, c, lead, nlead, s);
 }
-cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStream_t s) {
-  return scatter_impl<float>(x, c, s);
+cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStream_t s,
+                                      uint8_t *lead, uint32_t nlead) {
+  return scatter_impl<float>(x, c, lead, nlead, s);
 }
 
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t s) {

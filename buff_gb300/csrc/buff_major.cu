@@ -1,0 +1,663 @@
+// The buff-major (outlier) layout on the GPU: encode, serialize/deserialize,
+// filters, sum, max and decode (compress/buff_simd.rs:317-2861).
+//
+// Device form of a buff-major column: per sparse column c a major byte, the
+// outlier-row bitmap (BitVec<u32> words), the number of outliers before every
+// word (exclusive prefix) and the outlier bytes in row order; the dense
+// slices are kept flipped like buff-simd slices so the shared compare code
+// applies; the tail is the same packed r-bit stream.  Queries read one bitmap
+// word per 32 rows for each sparse column (n/8 bytes instead of n), look up
+// outlier bytes by rank, and touch dense slices only for 32-row blocks that
+// still hold candidates.
+//
+// Results follow the reference bit for bit, including its behaviour on the
+// second and later sparse columns: the range filter sets outliers above the
+// target byte whether or not the row is still a candidate and drops the
+// candidates when target and major byte are both 0; the max skips a column's
+// major byte when no candidate is an outlier there and keeps the major byte
+// when every candidate outlier is below it; the decode ORs the major byte
+// shifted twice, and only into rows before the column's last outlier.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <new>
+#include <vector>
+
+#include "buff_device.cuh"
+#include "buff_internal.h"
+#include "buff_snappy.h"
+
+namespace buffk {
+namespace {
+
+using namespace dev;
+
+constexpr uint32_t kSample = 2000;  // split_double.rs:25 SAMPLE
+
+inline size_t rank_stride(const buff_col *c) { return c->nwp + 16; }
+
+// ---------------------------------------------------------------- encode
+
+// Outlier rows of one sparse column: bytes (flipped) that differ from the
+// major byte; the bitmap word and its population per 32 rows.
+__global__ void k_major_bits(const uint8_t *__restrict__ lead, uint32_t n, uint32_t major,
+                             size_t nwp, uint32_t *__restrict__ bits, uint32_t *__restrict__ cnt) {
+  const ByteTarget t = make_target(major);
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nwp;
+       w += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t row0 = (uint32_t)(w * 32);
+    uint32_t out = 0;
+    if (row0 < n) {
+      const uint4 a = __ldg(reinterpret_cast<const uint4 *>(lead + row0));
+      const uint4 b = __ldg(reinterpret_cast<const uint4 *>(lead + row0 + 16));
+      const uint32_t wv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+      uint32_t e[8], g;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) cmp4(wv[q], t, g, e[q]);
+      out = ~gather32(e);
+      if (n - row0 < 32) out &= (1u << (n - row0)) - 1u;
+    }
+    bits[w] = out;
+    cnt[w] = __popc(out);
+  }
+}
+
+// Exclusive prefix sums of `count` u32 values in place, the total at
+// data[count]: per-block scan of 4096 values, a single-block scan of the
+// block totals, then the block offsets added back.
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4 * kScanThreads;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_local(uint32_t *data, size_t count,
+                                                              uint32_t *totals) {
+  __shared__ uint32_t s_warp[32];
+  const size_t base = (size_t)blockIdx.x * kScanItems + threadIdx.x * 4;
+  uint32_t v[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] = base + i < count ? data[base + i] : 0u;
+  const uint32_t sum = v[0] + v[1] + v[2] + v[3];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t inc = sum;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) s_warp[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t t = s_warp[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, t, o);
+      if (lane >= o) t += y;
+    }
+    s_warp[lane] = t;
+  }
+  __syncthreads();
+  uint32_t run = inc - sum + (wid ? s_warp[wid - 1] : 0u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (base + i < count) data[base + i] = run;
+    run += v[i];
+  }
+  if (threadIdx.x == kScanThreads - 1) totals[blockIdx.x] = run;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_totals(uint32_t *totals, uint32_t nb,
+                                                               uint32_t *grand) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (uint32_t b0 = 0; b0 < nb; b0 += kScanThreads) {
+    const uint32_t i = b0 + threadIdx.x;
+    const uint32_t v = i < nb ? totals[i] : 0u;
+    uint32_t inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (lane == 31) s_warp[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+      uint32_t t = s_warp[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, t, o);
+        if (lane >= o) t += y;
+      }
+      s_warp[lane] = t;
+    }
+    __syncthreads();
+    const uint32_t excl = s_carry + inc - v + (wid ? s_warp[wid - 1] : 0u);
+    if (i < nb) totals[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == kScanThreads - 1) s_carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *grand = s_carry;
+}
+
+__global__ void k_scan_add(uint32_t *data, size_t count, const uint32_t *totals) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) data[i] += totals[i / kScanItems];
+}
+
+cudaError_t scan_exclusive(uint32_t *data, size_t count, uint32_t *tmp, cudaStream_t s) {
+  const uint32_t nb = (uint32_t)((count + kScanItems - 1) / kScanItems);
+  k_scan_local<<<nb, kScanThreads, 0, s>>>(data, count, tmp);
+  k_scan_totals<<<1, kScanThreads, 0, s>>>(tmp, nb, data + count);
+  k_scan_add<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(data, count, tmp);
+  count_launch(3);
+  return cudaGetLastError();
+}
+
+// Outlier bytes (unflipped) of one sparse column, compacted in row order.
+__global__ void k_major_compact(const uint8_t *__restrict__ lead, const uint32_t *__restrict__ bits,
+                                const uint32_t *__restrict__ rank, size_t nwp,
+                                uint8_t *__restrict__ out) {
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nwp;
+       w += (size_t)gridDim.x * blockDim.x) {
+    uint32_t b = bits[w];
+    uint32_t at = rank[w];
+    while (b) {
+      const uint32_t j = __ffs(b) - 1;
+      b &= b - 1;
+      out[at++] = lead[w * 32 + j] ^ 0x80u;
+    }
+  }
+}
+
+// 1 + the last outlier row of a sparse column (0 when it has none).
+__global__ void k_major_last(const uint32_t *__restrict__ bits, size_t nwp, uint32_t *last) {
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nwp;
+       w += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t b = bits[w];
+    if (b) atomicMax(last, (uint32_t)(w * 32) + (31 - __clz(b)) + 1);
+  }
+}
+
+// ---------------------------------------------------------------- filters
+
+struct MajorArgs {
+  uint32_t n, m, kd, r;
+  size_t nwp, rs, stride;
+  const uint32_t *obits, *orank;
+  const uint8_t *obytes;
+  unsigned long long oofs[8];
+  uint8_t majors[8];
+  uint8_t tbyte[8];  // target byte per full byte (sparse columns, then dense slices)
+  uint32_t ttail;
+  const uint8_t *slices, *tail;
+  uint32_t *words;
+  unsigned long long *count;
+};
+
+// buff_range_filter_majority (compress/buff_simd.rs:863-1277) and
+// buff_equal_filter_majority (:1916-2292), one thread per 32 rows.
+template <bool IS_RANGE>
+__global__ void __launch_bounds__(kThreads) k_filter_major(MajorArgs a) {
+  const size_t nwords = (a.n + 31) / 32;
+  uint32_t cnt = 0;
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nwords;
+       w += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t row0 = (uint32_t)(w * 32);
+    const uint32_t valid = a.n - row0 >= 32 ? 0xFFFFFFFFu : ((1u << (a.n - row0)) - 1u);
+    uint32_t gt = 0, eq = valid;
+    for (uint32_t c = 0; c < a.m; ++c) {
+      const uint32_t B = a.obits[c * a.nwp + w];
+      const uint32_t M = a.majors[c], T = a.tbyte[c];
+      uint32_t ogt = 0, oeq = 0;
+      if (B) {
+        const uint8_t *ob = a.obytes + a.oofs[c] + a.orank[c * a.rs + w];
+        uint32_t b = B;
+        for (uint32_t k = 0; b; ++k) {
+          const uint32_t j = __ffs(b) - 1;
+          b &= b - 1;
+          const uint32_t val = __ldg(ob + k);
+          ogt |= (uint32_t)(val > T) << j;
+          oeq |= (uint32_t)(val == T) << j;
+        }
+      }
+      const uint32_t non = ~B & valid;
+      if (!IS_RANGE) {
+        eq &= oeq | (M == T ? non : 0u);
+      } else if (c == 0) {
+        gt = ogt | (M > T ? non : 0u);
+        eq = oeq | (M == T ? non : 0u);
+      } else if (T == 0 && M == 0) {
+        gt |= eq & B;  // candidates that are outliers; the others are dropped
+        eq = 0;
+      } else {
+        gt |= ogt;  // every outlier above the target byte, candidate or not
+        if (T < M) gt |= eq & non;
+        eq &= oeq | (T == M ? non : 0u);
+      }
+    }
+    for (uint32_t j = 0; j < a.kd && eq; ++j) {  // dense slices, progressive
+      const uint8_t *p = a.slices + j * a.stride + row0;
+      const uint4 lo = __ldg(reinterpret_cast<const uint4 *>(p));
+      const uint4 hi = __ldg(reinterpret_cast<const uint4 *>(p + 16));
+      const uint32_t wv[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+      const ByteTarget t = make_target(a.tbyte[a.m + j]);
+      uint32_t g[8], e[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) cmp4(wv[q], t, g[q], e[q]);
+      gt |= eq & gather32(g);
+      eq &= gather32(e);
+    }
+    uint32_t res;
+    if (a.r && eq) {
+      const uint32_t *tp = reinterpret_cast<const uint32_t *>(a.tail + (size_t)(row0 >> 5) * 4 * a.r);
+      uint32_t tw[8];
+#pragma unroll
+      for (int i = 0; i < 7; ++i) tw[i] = (uint32_t)i < a.r ? __ldg(tp + i) : 0u;
+      tw[7] = 0;
+      uint32_t gtt = 0, eqt = 0;
+      for (uint32_t i = 0; i < 32; ++i) {
+        if (!(eq >> i & 1u)) continue;
+        const uint32_t bit = i * a.r, wi = bit >> 5;
+        const uint32_t f = __funnelshift_r(tw[wi], tw[wi + 1], bit & 31) & ((1u << a.r) - 1u);
+        gtt |= (uint32_t)(f > a.ttail) << i;
+        eqt |= (uint32_t)(f == a.ttail) << i;
+      }
+      gt |= eq & gtt;
+      eq &= eqt;
+      res = IS_RANGE ? gt : eq;
+    } else {
+      // equality only sets rows in the tail step (:2235-2287)
+      res = IS_RANGE ? gt : 0u;
+    }
+    a.words[w] = res;
+    cnt += __popc(res);
+  }
+  if (a.count) {
+    const unsigned long long c = warp_sum_ull(cnt);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(a.count, c);
+  }
+}
+
+// ---------------------------------------------------------------- sum / max helpers
+
+__global__ void k_bytesum(const uint8_t *__restrict__ p, size_t nbytes, unsigned long long *out) {
+  unsigned long long acc = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nbytes;
+       i += (size_t)gridDim.x * blockDim.x)
+    acc += p[i];
+  acc = warp_sum_ull(acc);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
+
+// Largest outlier byte among rows set in `cand` (all outlier rows when cand is
+// null) of sparse column c; any[0] |= 1 when there is such a row.
+__global__ void k_major_candmax(const uint32_t *__restrict__ bits, const uint32_t *__restrict__ rank,
+                                const uint8_t *__restrict__ ob, const uint32_t *__restrict__ cand,
+                                size_t nw, uint32_t *out) {
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
+       w += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t B = bits[w];
+    const uint32_t sel = cand ? B & cand[w] : B;
+    if (!sel) continue;
+    uint32_t b = B, best = 0;
+    for (uint32_t k = rank[w]; b; ++k) {
+      const uint32_t j = __ffs(b) - 1;
+      b &= b - 1;
+      if (sel >> j & 1u) best = max(best, (uint32_t)ob[k]);
+    }
+    atomicMax(out, best);
+    atomicOr(out + 1, 1u);
+  }
+}
+
+// New candidate words for a sparse column: mode 0: ~B (valid rows); mode 1:
+// rows of (B & cand) whose outlier byte equals `value`; mode 2: cand & ~B.
+__global__ void k_major_select(const uint32_t *__restrict__ bits, const uint32_t *__restrict__ rank,
+                               const uint8_t *__restrict__ ob, uint32_t *cand, size_t nw,
+                               uint32_t n, int mode, uint32_t value) {
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
+       w += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t row0 = (uint32_t)(w * 32);
+    const uint32_t valid = n - row0 >= 32 ? 0xFFFFFFFFu : ((1u << (n - row0)) - 1u);
+    const uint32_t B = bits[w];
+    uint32_t out;
+    if (mode == 0) {
+      out = ~B & valid;
+    } else if (mode == 2) {
+      out = cand[w] & ~B;
+    } else {
+      const uint32_t sel = B & cand[w];
+      out = 0;
+      uint32_t b = B;
+      for (uint32_t k = rank[w]; b; ++k) {
+        const uint32_t j = __ffs(b) - 1;
+        b &= b - 1;
+        if ((sel >> j & 1u) && ob[k] == value) out |= 1u << j;
+      }
+    }
+    cand[w] = out;
+  }
+}
+
+// Progressive max step over a dense slice (flipped bytes; r == 0) or the
+// packed tail (r bits): the largest value among candidate rows.
+__device__ __forceinline__ uint32_t field_at(const uint8_t *slice, const uint8_t *tail, uint32_t r,
+                                             uint32_t row) {
+  if (!r) return (uint32_t)(slice[row] ^ 0x80u);
+  const unsigned long long bit = (unsigned long long)row * r;
+  const uint32_t b0 = tail[bit >> 3];
+  const uint32_t b1 = ((bit & 7) + r > 8) ? tail[(bit >> 3) + 1] : 0u;
+  return ((b0 | (b1 << 8)) >> (bit & 7)) & ((1u << r) - 1u);
+}
+
+__global__ void k_cand_max(const uint8_t *__restrict__ slice, const uint8_t *__restrict__ tail,
+                           uint32_t r, const uint32_t *__restrict__ cand, size_t nw, uint32_t *out) {
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
+       w += (size_t)gridDim.x * blockDim.x) {
+    uint32_t b = cand[w];
+    if (!b) continue;
+    uint32_t best = 0;
+    while (b) {
+      const uint32_t j = __ffs(b) - 1;
+      b &= b - 1;
+      best = max(best, field_at(slice, tail, r, (uint32_t)(w * 32 + j)));
+    }
+    atomicMax(out, best);
+  }
+}
+
+__global__ void k_cand_select(const uint8_t *__restrict__ slice, const uint8_t *__restrict__ tail,
+                              uint32_t r, uint32_t *cand, size_t nw, uint32_t value,
+                              unsigned long long *count) {
+  unsigned long long c = 0;
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
+       w += (size_t)gridDim.x * blockDim.x) {
+    uint32_t b = cand[w], out = 0;
+    while (b) {
+      const uint32_t j = __ffs(b) - 1;
+      b &= b - 1;
+      if (field_at(slice, tail, r, (uint32_t)(w * 32 + j)) == value) out |= 1u << j;
+    }
+    cand[w] = out;
+    c += __popc(out);
+  }
+  if (count) {
+    c = warp_sum_ull(c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+  }
+}
+
+__global__ void k_popc(const uint32_t *__restrict__ w, size_t nw, unsigned long long *out) {
+  unsigned long long c = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nw;
+       i += (size_t)gridDim.x * blockDim.x)
+    c += __popc(w[i]);
+  c = warp_sum_ull(c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// ---------------------------------------------------------------- decode
+
+struct DecodeMajorArgs {
+  uint32_t n, m, kd, r, fl;
+  size_t nwp, rs, stride;
+  const uint32_t *obits, *orank;
+  const uint8_t *obytes;
+  unsigned long long oofs[8];
+  uint8_t majors[8];
+  uint32_t olast[8];
+  const uint8_t *slices, *tail;
+  long long base;
+  int dlen;
+  double *out;
+};
+
+// buff_decode_majority (compress/buff_simd.rs:633-861), one thread per row.
+__global__ void __launch_bounds__(kThreads) k_decode_major(DecodeMajorArgs a) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t w = i >> 5;
+    const uint32_t j = (uint32_t)(i & 31);
+    unsigned long long v = 0;
+    for (uint32_t c = 0; c < a.m; ++c) {
+      const uint32_t sh = a.fl - 8 * (c + 1);
+      const uint32_t B = a.obits[c * a.nwp + w];
+      if (B >> j & 1u) {
+        const uint32_t k = a.orank[c * a.rs + w] + __popc(B & ((1u << j) - 1u));
+        const unsigned long long b = a.obytes[a.oofs[c] + k];
+        v = c == 0 ? (b << sh) : (v | (b << sh));
+      } else if (c == 0) {
+        v = (unsigned long long)a.majors[0] << sh;
+      } else if (i + 1 < a.olast[c]) {
+        v |= (((unsigned long long)a.majors[c] << sh) << sh);
+      }
+    }
+    for (uint32_t d = 0; d < a.kd; ++d) {
+      const uint32_t sh = a.fl - 8 * (a.m + d + 1);
+      v |= (unsigned long long)(a.slices[d * a.stride + i] ^ 0x80u) << sh;
+    }
+    if (a.r) v |= field_at(nullptr, a.tail, a.r, (uint32_t)i);
+    a.out[i] = i64_to_f64_scaled((long long)((unsigned long long)a.base + v), a.dlen);
+  }
+}
+
+__global__ void k_xor80(uint8_t *p, size_t nbytes) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nbytes;
+       i += (size_t)gridDim.x * blockDim.x)
+    p[i] ^= 0x80u;
+}
+
+__global__ void k_word_popc(const uint32_t *__restrict__ bits, size_t nw, uint32_t *cnt) {
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
+       w += (size_t)gridDim.x * blockDim.x)
+    cnt[w] = __popc(bits[w]);
+}
+
+int grid_of(size_t items, int threads) {
+  size_t g = (items + threads - 1) / threads;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const size_t cap = (size_t)8 * num_sms(dev);
+  if (g > cap) g = cap;
+  return g < 1 ? 1 : (int)g;
+}
+
+}  // namespace
+
+// ================================================================ host side
+
+cudaError_t flip_bytes(uint8_t *p, size_t nbytes, cudaStream_t s) {
+  if (!nbytes) return cudaSuccess;
+  k_xor80<<<grid_of(nbytes, 256), 256, 0, s>>>(p, nbytes);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// Ranks and last-outlier rows of already loaded bitmaps (deserialize).
+cudaError_t major_index(buff_col *c, cudaStream_t s) {
+  cudaError_t e;
+  const size_t rs = rank_stride(c);
+  uint32_t *tmp = nullptr, *dlast = nullptr;
+  const size_t nb = (c->nwp + kScanItems - 1) / kScanItems + 1;
+  e = cudaMallocAsync(reinterpret_cast<void **>(&tmp), sizeof(uint32_t) * nb, s);
+  if (e != cudaSuccess) return e;
+  e = cudaMallocAsync(reinterpret_cast<void **>(&dlast), sizeof(uint32_t) * 8, s);
+  if (e != cudaSuccess) return e;
+  cudaMemsetAsync(dlast, 0, sizeof(uint32_t) * 8, s);
+  for (uint32_t col = 0; col < c->m; ++col) {
+    const uint32_t *bits = c->obits + col * c->nwp;
+    uint32_t *rank = c->orank + col * rs;
+    k_word_popc<<<grid_of(c->nwp, 256), 256, 0, s>>>(bits, c->nwp, rank);
+    k_major_last<<<grid_of(c->nwp, 256), 256, 0, s>>>(bits, c->nwp, dlast + col);
+    count_launch(2);
+    if ((e = scan_exclusive(rank, c->nwp, tmp, s)) != cudaSuccess) return e;
+  }
+  uint32_t last[8];
+  cudaMemcpyAsync(last, dlast, sizeof(uint32_t) * 8, cudaMemcpyDeviceToHost, s);
+  e = cudaStreamSynchronize(s);
+  for (uint32_t col = 0; col < c->m; ++col) c->olast[col] = last[col];
+  cudaFreeAsync(tmp, s);
+  cudaFreeAsync(dlast, s);
+  return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t major_build_sparse(buff_col *c, const uint8_t *lead, cudaStream_t s) {
+  // bitmaps, ranks and compacted outlier bytes from the `m` leading slices
+  cudaError_t e;
+  const size_t rs = rank_stride(c);
+  e = cudaMallocAsync(reinterpret_cast<void **>(&c->obits), sizeof(uint32_t) * c->m * c->nwp, s);
+  if (e != cudaSuccess) return e;
+  e = cudaMallocAsync(reinterpret_cast<void **>(&c->orank), sizeof(uint32_t) * c->m * rs, s);
+  if (e != cudaSuccess) return e;
+  uint32_t *tmp = nullptr, *dlast = nullptr;
+  const size_t nb = (c->nwp + kScanItems - 1) / kScanItems + 1;
+  e = cudaMallocAsync(reinterpret_cast<void **>(&tmp), sizeof(uint32_t) * nb, s);
+  if (e != cudaSuccess) return e;
+  e = cudaMallocAsync(reinterpret_cast<void **>(&dlast), sizeof(uint32_t) * 8, s);
+  if (e != cudaSuccess) return e;
+  cudaMemsetAsync(dlast, 0, sizeof(uint32_t) * 8, s);
+  for (uint32_t col = 0; col < c->m; ++col) {
+    uint32_t *bits = c->obits + col * c->nwp, *rank = c->orank + col * rs;
+    k_major_bits<<<grid_of(c->nwp, 256), 256, 0, s>>>(lead + col * c->stride, c->n, c->majors[col],
+                                                      c->nwp, bits, rank);
+    k_major_last<<<grid_of(c->nwp, 256), 256, 0, s>>>(bits, c->nwp, dlast + col);
+    count_launch(2);
+    if ((e = scan_exclusive(rank, c->nwp, tmp, s)) != cudaSuccess) return e;
+  }
+  uint32_t totals[8], last[8];
+  for (uint32_t col = 0; col < c->m; ++col)
+    cudaMemcpyAsync(&totals[col], c->orank + col * rs + c->nwp, 4, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(last, dlast, sizeof(uint32_t) * 8, cudaMemcpyDeviceToHost, s);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  uint64_t off = 0;
+  for (uint32_t col = 0; col < c->m; ++col) {
+    c->nout[col] = totals[col];
+    c->olast[col] = last[col];
+    c->oofs[col] = off;
+    off += totals[col];
+  }
+  c->oofs[c->m] = off;
+  e = cudaMallocAsync(reinterpret_cast<void **>(&c->obytes), off + 16, s);
+  if (e != cudaSuccess) return e;
+  for (uint32_t col = 0; col < c->m; ++col) {
+    k_major_compact<<<grid_of(c->nwp, 256), 256, 0, s>>>(lead + col * c->stride,
+                                                         c->obits + col * c->nwp,
+                                                         c->orank + col * rs, c->nwp,
+                                                         c->obytes + c->oofs[col]);
+    count_launch();
+  }
+  cudaFreeAsync(tmp, s);
+  cudaFreeAsync(dlast, s);
+  return cudaGetLastError();
+}
+
+cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, uint32_t ttail,
+                         uint32_t *words, unsigned long long *count, cudaStream_t s) {
+  MajorArgs a;
+  memset(&a, 0, sizeof(a));
+  a.n = c->n;
+  a.m = c->m;
+  a.kd = c->k - c->m;
+  a.r = c->r;
+  a.nwp = c->nwp;
+  a.rs = rank_stride(c);
+  a.stride = c->stride;
+  a.obits = c->obits;
+  a.orank = c->orank;
+  a.obytes = c->obytes;
+  for (uint32_t i = 0; i < 8; ++i) {
+    a.oofs[i] = c->oofs[i];
+    a.majors[i] = c->majors[i];
+    a.tbyte[i] = tbyte[i];
+  }
+  a.ttail = ttail;
+  a.slices = c->slices;
+  a.tail = c->tail;
+  a.words = words;
+  a.count = count;
+  const size_t nw = (c->n + 31) / 32;
+  const int grid = grid_of(nw, kThreads);
+  if (is_range)
+    k_filter_major<true><<<grid, kThreads, 0, s>>>(a);
+  else
+    k_filter_major<false><<<grid, kThreads, 0, s>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out, cudaStream_t s) {
+  k_bytesum<<<grid_of(nbytes, 256), 256, 0, s>>>(p, nbytes, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t major_candmax(const buff_col *c, uint32_t col, const uint32_t *cand, uint32_t *out,
+                          cudaStream_t s) {
+  k_major_candmax<<<grid_of(c->nwp, 256), 256, 0, s>>>(c->obits + col * c->nwp,
+                                                        c->orank + col * rank_stride(c),
+                                                        c->obytes + c->oofs[col], cand, c->nwp,
+                                                        out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t major_select(const buff_col *c, uint32_t col, uint32_t *cand, int mode, uint32_t value,
+                         cudaStream_t s) {
+  k_major_select<<<grid_of(c->nwp, 256), 256, 0, s>>>(c->obits + col * c->nwp,
+                                                       c->orank + col * rank_stride(c),
+                                                       c->obytes + c->oofs[col], cand, c->nwp,
+                                                       c->n, mode, value);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t cand_max(const uint8_t *slice, const uint8_t *tail, uint32_t r, const uint32_t *cand,
+                     size_t nw, uint32_t *out, cudaStream_t s) {
+  k_cand_max<<<grid_of(nw, 256), 256, 0, s>>>(slice, tail, r, cand, nw, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t cand_select(const uint8_t *slice, const uint8_t *tail, uint32_t r, uint32_t *cand,
+                        size_t nw, uint32_t value, unsigned long long *count, cudaStream_t s) {
+  k_cand_select<<<grid_of(nw, 256), 256, 0, s>>>(slice, tail, r, cand, nw, value, count);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t popcount_words(const uint32_t *w, size_t nw, unsigned long long *out, cudaStream_t s) {
+  k_popc<<<grid_of(nw, 256), 256, 0, s>>>(w, nw, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t major_decode(const buff_col *c, double *out, cudaStream_t s) {
+  DecodeMajorArgs a;
+  memset(&a, 0, sizeof(a));
+  a.n = c->n;
+  a.m = c->m;
+  a.kd = c->k - c->m;
+  a.r = c->r;
+  a.fl = c->fixed_len;
+  a.nwp = c->nwp;
+  a.rs = rank_stride(c);
+  a.stride = c->stride;
+  a.obits = c->obits;
+  a.orank = c->orank;
+  a.obytes = c->obytes;
+  for (uint32_t i = 0; i < 8; ++i) {
+    a.oofs[i] = c->oofs[i];
+    a.majors[i] = c->majors[i];
+    a.olast[i] = c->olast[i];
+  }
+  a.slices = c->slices;
+  a.tail = c->tail;
+  a.base = c->base;
+  a.dlen = (int)c->dlen;
+  a.out = out;
+  k_decode_major<<<grid_of(c->n, kThreads), kThreads, 0, s>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace buffk

@@ -63,6 +63,7 @@ int64_t fetch_fixed(double v, int pexp, uint32_t dlen) {
 extern "C" int buff_range_filter_noalloc(const buff_col *c, double pred, uint32_t *words,
                                          uint64_t *count, void *stream) {
   if (!c || (!words && c->n > 0)) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns are not supported here
   if (c->n > BUFF_NOALLOC_MAX_ROWS) return BUFF_ESCRATCH;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   int dev = 0;

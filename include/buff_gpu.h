@@ -58,6 +58,9 @@ extern "C" {
  * answers columns without tail bits, variable-precision decode keeps the
  * retained bits in place. */
 #define BUFF_FLAG_INTENDED 0x1u
+/* buff-major columns: store (and expect) the outlier bitmaps as raw
+ * BitVec::to_binary bytes instead of snappy-compressed ones. */
+#define BUFF_FLAG_RAW_BITMAPS 0x2u
 
 typedef struct buff_col buff_col;
 
@@ -74,8 +77,9 @@ typedef struct buff_col_info {
   int32_t prec;          /* floor(log10(scale)) */
   int32_t precision_exp; /* exponent of the reference's precision bound */
   uint32_t flags;
-  uint32_t reserved;
-  uint64_t serialized_bytes; /* size of the reference byte image */
+  uint32_t outlier_cols;     /* sparse (majority) byte columns of a buff-major column */
+  uint64_t serialized_bytes; /* size of the reference byte image (0 for buff-major: call
+                                buff_serialize with out = NULL) */
   uint64_t device_bytes;     /* HBM held by the handle */
 } buff_col_info;
 
@@ -164,6 +168,35 @@ int buff_max(const buff_col *col, double *max_value, uint64_t *max_code,
              uint32_t *argmax_words, uint64_t *argmax_count, void *stream);
 /* Device-only max: enqueues the maximum code into *dev_max_code (device u64). */
 int buff_max_async(const buff_col *col, uint64_t *dev_max_code, void *stream);
+
+/* ---- buff-major (outlier) columns ---- */
+
+/* SplitBDDoubleCompress::buff_encode_majority (compress/buff_simd.rs:317-630):
+ * leading byte columns whose Boyer-Moore majority over the first 2000 rows
+ * reaches 1200 are stored as (major byte, outlier-row bitmap, outlier bytes);
+ * the remaining bytes as slices and the packed tail.  Needs n >= 2000 and
+ * codes of at least 8 bits. */
+int buff_encode_majority_f64(const double *values, uint64_t n, uint64_t scale, uint32_t flags,
+                             void *stream, buff_col **out);
+int buff_encode_majority_f32(const float *values, uint64_t n, uint64_t scale, uint32_t flags,
+                             void *stream, buff_col **out);
+/* Rebuilds a buff-major column from its reference byte image. */
+int buff_deserialize_majority(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                              void *stream, buff_col **out);
+/* buff_decode_majority (compress/buff_simd.rs:633-861). */
+int buff_decode_majority(const buff_col *col, double *out, void *stream);
+/* buff_range_filter_majority (compress/buff_simd.rs:863-1277). */
+int buff_range_filter_majority(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
+                               void *stream);
+/* buff_equal_filter_majority (compress/buff_simd.rs:1916-2292). */
+int buff_equal_filter_majority(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
+                               void *stream);
+/* buff_sum_majority (compress/buff_simd.rs:2294-2442); synchronizes. */
+int buff_sum_majority(const buff_col *col, buff_sum_result *out, void *stream);
+/* buff_max_majority (compress/buff_simd.rs:2444-2861): max, its code and the
+ * arg-max rows of the tail step (argmax_words/argmax_count may be NULL). */
+int buff_max_majority(const buff_col *col, double *max_value, uint64_t *max_code,
+                      uint32_t *argmax_words, uint64_t *argmax_count, void *stream);
 
 /* ---- allocation-free query ---- */
 

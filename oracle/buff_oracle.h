@@ -137,6 +137,26 @@ int or_sum_at_precision(const uint8_t *bytes, size_t len, uint64_t scale, int fl
 double or_bench_filter_sum(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
                            int nthreads, int reps, uint64_t *count, double *sum);
 
+/* --- buff-major (outlier) format: oracle/buff_oracle_major.c --- */
+#define OR_BM_SNAPPY 0 /* outlier bitmaps snappy-compressed (the reference) */
+#define OR_BM_RAW 1    /* outlier bitmaps stored as raw BitVec::to_binary bytes */
+size_t or_snappy_max_compressed(size_t n);
+int or_snappy_compress(const uint8_t *in, size_t n, uint8_t *out, size_t cap, size_t *outlen);
+int or_snappy_decompress(const uint8_t *in, size_t n, uint8_t *out, size_t cap, size_t *outlen);
+int or_encode_majority(const double *x, uint32_t n, uint64_t scale, int bm_mode, uint8_t **out,
+                       size_t *out_len);
+int or_majority_layout(const uint8_t *bytes, size_t len, int bm_mode, uint32_t *ncols,
+                       uint8_t *majors, uint32_t *nouts, size_t *dense_off);
+int or_decode_majority(const uint8_t *bytes, size_t len, uint64_t scale, int bm_mode, double *out);
+int or_range_filter_majority(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                             int bm_mode, uint32_t *words, uint64_t *count, int *early);
+int or_equal_filter_majority(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                             int bm_mode, uint32_t *words, uint64_t *count, int *early);
+int or_sum_majority(const uint8_t *bytes, size_t len, uint64_t scale, int bm_mode, double *sum,
+                    uint64_t *partials);
+int or_max_majority(const uint8_t *bytes, size_t len, uint64_t scale, int bm_mode, double *maxv,
+                    uint64_t *max_code, uint32_t *argmax_words, uint64_t *argmax_count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,8 +25,9 @@ class OraclePanic(RuntimeError):
 
 
 def build() -> str:
-    src = os.path.join(_HERE, "buff_oracle.c")
-    if (not os.path.exists(_LIB_PATH)) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("buff_oracle.c", "buff_oracle_major.c", "buff_oracle.h")]
+    if (not os.path.exists(_LIB_PATH)) or any(os.path.getmtime(_LIB_PATH) < os.path.getmtime(s)
+                                               for s in srcs):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -77,6 +78,18 @@ def lib():
                                              C.c_uint, P]
         L.or_sum_at_precision.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, C.c_uint32,
                                           C.c_uint, P]
+        L.or_snappy_max_compressed.argtypes = [C.c_size_t]
+        L.or_snappy_max_compressed.restype = C.c_size_t
+        L.or_snappy_compress.argtypes = [P, C.c_size_t, P, C.c_size_t, P]
+        L.or_snappy_decompress.argtypes = [P, C.c_size_t, P, C.c_size_t, P]
+        L.or_encode_majority.argtypes = [P, C.c_uint32, C.c_uint64, C.c_int, C.POINTER(u8p),
+                                         C.POINTER(C.c_size_t)]
+        L.or_majority_layout.argtypes = [P, C.c_size_t, C.c_int, P, P, P, P]
+        L.or_decode_majority.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P]
+        for nm in ("or_range_filter_majority", "or_equal_filter_majority"):
+            getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, C.c_int, P, P, P]
+        L.or_sum_majority.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P, P]
+        L.or_max_majority.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P, P, P, P]
         L.or_bench_filter_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, C.c_int,
                                           C.c_int, P, P]
         L.or_bench_filter_sum.restype = C.c_double
@@ -265,3 +278,95 @@ def bench_filter_sum(buf, scale, pred, nthreads=1, reps=1):
     s = np.zeros(1, dtype=np.float64)
     t = lib().or_bench_filter_sum(_ptr(b), b.size, scale, pred, nthreads, reps, _ptr(cnt), _ptr(s))
     return t, int(cnt[0]), float(s[0])
+
+
+# --- buff-major (outlier) format -------------------------------------------
+BM_SNAPPY, BM_RAW = 0, 1
+
+
+def snappy_compress(data: bytes) -> bytes:
+    b = np.frombuffer(data, dtype=np.uint8).copy() if data else np.zeros(1, dtype=np.uint8)
+    cap = lib().or_snappy_max_compressed(len(data))
+    out = np.zeros(cap, dtype=np.uint8)
+    ln = C.c_size_t(0)
+    _check(lib().or_snappy_compress(_ptr(b), len(data), _ptr(out), cap, C.byref(ln)))
+    return out[: ln.value].tobytes()
+
+
+def snappy_decompress(data: bytes) -> bytes:
+    b = np.frombuffer(data, dtype=np.uint8).copy()
+    ln = C.c_size_t(0)
+    _check(lib().or_snappy_decompress(_ptr(b), b.size, None, 0, C.byref(ln)))
+    out = np.zeros(max(ln.value, 1), dtype=np.uint8)
+    _check(lib().or_snappy_decompress(_ptr(b), b.size, _ptr(out), out.size, C.byref(ln)))
+    return out[: ln.value].tobytes()
+
+
+def encode_majority(x, scale: int, bm_mode: int = BM_SNAPPY) -> bytes:
+    arr = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    out = C.POINTER(C.c_uint8)()
+    ln = C.c_size_t(0)
+    _check(lib().or_encode_majority(_ptr(arr), arr.size, scale, bm_mode, C.byref(out),
+                                    C.byref(ln)))
+    try:
+        return C.string_at(out, ln.value)
+    finally:
+        lib().or_free(out)
+
+
+def majority_layout(buf: bytes, bm_mode: int = BM_SNAPPY):
+    b = _buf(buf)
+    nc = np.zeros(1, dtype=np.uint32)
+    maj = np.zeros(8, dtype=np.uint8)
+    nout = np.zeros(8, dtype=np.uint32)
+    off = np.zeros(1, dtype=np.uint64)
+    _check(lib().or_majority_layout(_ptr(b), b.size, bm_mode, _ptr(nc), _ptr(maj), _ptr(nout),
+                                    _ptr(off)))
+    k = int(nc[0])
+    return k, [int(v) for v in maj[:k]], [int(v) for v in nout[:k]], int(off[0])
+
+
+def decode_majority(buf, scale, bm_mode=BM_SNAPPY):
+    b = _buf(buf)
+    n = header(buf).n
+    out = np.zeros(max(n, 1), dtype=np.float64)
+    _check(lib().or_decode_majority(_ptr(b), b.size, scale, bm_mode, _ptr(out)))
+    return out[:n]
+
+
+def _filter_major(fn, buf, scale, pred, bm_mode):
+    b = _buf(buf)
+    n = header(buf).n
+    words = np.zeros(max((n + 31) // 32, 1), dtype=np.uint32)
+    cnt = np.zeros(1, dtype=np.uint64)
+    early = np.zeros(1, dtype=np.int32)
+    _check(fn(_ptr(b), b.size, scale, pred, bm_mode, _ptr(words), _ptr(cnt), _ptr(early)))
+    return words[: (n + 31) // 32], int(cnt[0]), bool(early[0])
+
+
+def range_filter_majority(buf, scale, pred, bm_mode=BM_SNAPPY):
+    return _filter_major(lib().or_range_filter_majority, buf, scale, pred, bm_mode)
+
+
+def equal_filter_majority(buf, scale, pred, bm_mode=BM_SNAPPY):
+    return _filter_major(lib().or_equal_filter_majority, buf, scale, pred, bm_mode)
+
+
+def sum_majority(buf, scale, bm_mode=BM_SNAPPY):
+    b = _buf(buf)
+    s = np.zeros(1, dtype=np.float64)
+    parts = np.zeros(16, dtype=np.uint64)
+    _check(lib().or_sum_majority(_ptr(b), b.size, scale, bm_mode, _ptr(s), _ptr(parts)))
+    return float(s[0]), [int(p) for p in parts]
+
+
+def max_majority(buf, scale, bm_mode=BM_SNAPPY):
+    b = _buf(buf)
+    n = header(buf).n
+    mv = np.zeros(1, dtype=np.float64)
+    mc = np.zeros(1, dtype=np.uint64)
+    words = np.zeros(max((n + 31) // 32, 1), dtype=np.uint32)
+    cnt = np.zeros(1, dtype=np.uint64)
+    _check(lib().or_max_majority(_ptr(b), b.size, scale, bm_mode, _ptr(mv), _ptr(mc),
+                                 _ptr(words), _ptr(cnt)))
+    return float(mv[0]), int(mc[0]), words[: (n + 31) // 32], int(cnt[0])

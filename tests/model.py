@@ -122,3 +122,183 @@ def ref_sum(L, n: int, intended: bool = False) -> float:
         processed += r
         s = s + float(S) / 2.0 ** (processed - ilen_i)
     return s + sum_base
+
+
+# --- buff-major (outlier) format: whole-array statement of the reference ----
+
+def _bm_vote(vals):
+    freq, major = 0, 0
+    for b in vals:
+        if freq == 0:
+            major, freq = b, 1
+        elif major == b:
+            freq += 1
+        else:
+            freq -= 1
+    return major, freq
+
+
+def major_layout(x: np.ndarray, scale: int):
+    """Columns, majors and outlier masks of buff_encode_majority (buff_simd.rs:317-630)."""
+    prec = prec_of_scale(scale)
+    dlen = PRECISION_MAP[prec]
+    pexp = precision_exp(prec)
+    q = fetch_fixed(x, pexp, dlen)
+    mn, mx = int(q.min()), int(q.max())
+    delta = mx - mn
+    fl = 0 if delta == 0 else int(math.ceil(math.log2(float(delta))))
+    codes = [(int(v) - mn) & ((1 << 64) - 1) for v in q.tolist()]
+    rsf = fl - 8 if fl >= 8 else 0
+    majors = []
+    maj, freq = _bm_vote([(c >> rsf) & 0xFF for c in codes[:2000]])
+    if freq > 1200:
+        majors.append(maj)
+        while rsf > 7:
+            rsf -= 8
+            maj, freq = _bm_vote([(c >> rsf) & 0xFF for c in codes[:2000]])
+            if freq > 1200:
+                majors.append(maj)
+            else:
+                break
+    return dict(base=mn, fl=fl, dlen=dlen, pexp=pexp, codes=codes, majors=majors,
+                ilen=(fl - dlen) & 0xFFFFFFFF)
+
+
+def _byte(c, fl, j):
+    return (c >> (fl - 8 * (j + 1))) & 0xFF
+
+
+def major_decode_codes(L):
+    """buff_decode_majority's codes (buff_simd.rs:633-861): the 2nd+ sparse
+    column ORs its major shifted twice, and only before its last outlier."""
+    fl, codes, majors = L["fl"], L["codes"], L["majors"]
+    n = len(codes)
+    out = []
+    m = len(majors)
+    last = []
+    for c in range(m):
+        rows = [i for i in range(n) if _byte(codes[i], fl, c) != majors[c]]
+        last.append(rows[-1] if rows else -1)
+    mask64 = (1 << 64) - 1
+    for i, code in enumerate(codes):
+        v = 0
+        for c in range(m):
+            sh = fl - 8 * (c + 1)
+            b = _byte(code, fl, c)
+            if c == 0:
+                v = (b << sh) if b != majors[0] else (majors[0] << sh)
+            else:
+                if b != majors[c]:
+                    v |= b << sh
+                elif i < last[c]:
+                    v |= ((majors[c] << sh) << sh) & mask64
+        low = fl - 8 * m
+        v |= code & ((1 << low) - 1)
+        out.append(v & mask64)
+    return out
+
+
+def major_filter(L, pred: float, is_range: bool):
+    fl, codes, majors, base = L["fl"], L["codes"], L["majors"], L["base"]
+    n = len(codes)
+    fp = int(fetch_fixed(np.array([pred]), L["pexp"], L["dlen"])[0])
+    if fp < base:
+        return bits_to_words(np.full(n, 1 if is_range else 0, dtype=np.uint8))
+    t = fp - base
+    m = len(majors)
+    gt = [False] * n
+    eq = [True] * n
+    for c in range(m):
+        T = (t >> (fl - 8 * (c + 1))) & 0xFF
+        M = majors[c]
+        for i in range(n):
+            b = _byte(codes[i], fl, c)
+            out = b != M
+            if not is_range:
+                eq[i] = eq[i] and b == T
+                continue
+            if c == 0:
+                gt[i] = b > T
+                eq[i] = b == T
+            elif T == 0 and M == 0:
+                if eq[i] and out:
+                    gt[i] = True
+                eq[i] = False                      # the candidates are dropped
+            else:
+                if out and b > T:
+                    gt[i] = True                   # not restricted to candidates
+                if not out and T < M and eq[i]:
+                    gt[i] = True
+                eq[i] = eq[i] and ((out and b == T) or (not out and T == M))
+    low = fl - 8 * m
+    if low > 0:
+        r = low % 8
+        for i in range(n):
+            if not eq[i]:
+                continue
+            lowv = codes[i] & ((1 << low) - 1)
+            tlow = t & ((1 << low) - 1)
+            if (low >= 8) or r:
+                if is_range:
+                    gt[i] = gt[i] or lowv > tlow
+            eq[i] = lowv == tlow
+    res = gt if is_range else ([e and (fl - 8 * m) % 8 != 0 for e in eq] if fl - 8 * m > 0 else [False] * n)
+    return bits_to_words(np.array(res, dtype=np.uint8))
+
+
+def major_sum(L) -> float:
+    fl, codes, majors, base, dlen = L["fl"], L["codes"], L["majors"], L["base"], L["dlen"]
+    n = len(codes)
+    ilen_i = L["ilen"] - (1 << 32) if L["ilen"] >> 31 else L["ilen"]
+    sum_base = float(n) * float(base) / 2.0 ** dlen
+    s, processed = 0.0, 0
+    k = fl // 8
+    for j in range(k):
+        S = sum(_byte(c, fl, j) for c in codes)
+        processed += 8
+        s = s + float(S) / 2.0 ** (processed - ilen_i)
+        if j >= len(majors) and j == k - 1 and fl % 8 == 0:
+            return s
+    r = fl % 8
+    if r:
+        processed += r
+        s = s + float(sum(c & ((1 << r) - 1) for c in codes)) / 2.0 ** (processed - ilen_i)
+    return s + sum_base
+
+
+def major_max_code(L) -> int:
+    fl, codes, majors = L["fl"], L["codes"], L["majors"]
+    n = len(codes)
+    m = len(majors)
+    cand = list(range(n))
+    mx = 0
+    for c in range(m):
+        sh = fl - 8 * (c + 1)
+        M = majors[c]
+        bytes_ = {i: _byte(codes[i], fl, c) for i in cand}
+        outs = [i for i in cand if bytes_[i] != M]
+        if c == 0:
+            best = max(bytes_.values())
+            cand = [i for i in cand if bytes_[i] == best]
+            mx |= best << sh
+            continue
+        if not outs:
+            continue                               # the major never reaches max
+        best = max(bytes_[i] for i in outs)
+        if best > M:
+            cand = [i for i in outs if bytes_[i] == best]
+            mx |= best << sh
+        else:
+            cand = [i for i in cand if bytes_[i] == M]
+            mx |= M << sh
+    for j in range(m, fl // 8):
+        sh = fl - 8 * (j + 1)
+        if not cand:
+            continue
+        best = max(_byte(codes[i], fl, j) for i in cand)
+        cand = [i for i in cand if _byte(codes[i], fl, j) == best]
+        mx |= best << sh
+    r = fl % 8
+    if r and cand:
+        mx |= max(codes[i] & ((1 << r) - 1) for i in cand)
+    return mx

@@ -1,0 +1,147 @@
+"""GPU parity of the buff-major (outlier) format against the oracle.
+
+Columns with 0-3 sparse leading byte columns are encoded on the GPU and by the
+oracle; with raw outlier bitmaps the byte images must be identical, with
+snappy bitmaps both images must decode to the same column.  Every query
+(decode, range/equal filter, sum, max) on the GPU column must equal the
+oracle's answer on the reference image.
+"""
+import numpy as np
+import pytest
+
+from tests.test_oracle_major import major_case
+
+pytestmark = pytest.mark.gpu
+
+RAW = 1
+SNAPPY = 0
+
+
+def _preds(x):
+    xs = np.sort(x)
+    return [float(x[100]), float(np.quantile(x, 0.3)), float(np.quantile(x, 0.99)),
+            float(xs[-2]), float(x.max()), float(x.max()) + 1, float(x.min()) - 1,
+            float(x.min()), float(np.median(x)), float(x[7]) + 1e-9]
+
+
+def _check_queries(oracle, col, ref, scale, mode, x):
+    from buff_gb300 import capi
+
+    n = x.size
+    ncols, majors, nouts, _ = oracle.majority_layout(ref, mode)
+    assert col.info.outlier_cols == ncols
+    if all(nouts):
+        assert np.array_equal(col.decode(), oracle.decode_majority(ref, scale, mode))
+    else:
+        with pytest.raises(capi.ReferencePanic):
+            col.decode()
+    for p in _preds(x):
+        w, c, _ = oracle.range_filter_majority(ref, scale, p, mode)
+        r = col.range_filter(p)
+        assert np.array_equal(r.words, w), ("range", p)
+        assert r.count == c
+        w, c, _ = oracle.equal_filter_majority(ref, scale, p, mode)
+        r = col.equal_filter(p)
+        assert np.array_equal(r.words, w), ("equal", p)
+        assert r.count == c
+    s, parts = oracle.sum_majority(ref, scale, mode)
+    res = col.sum()
+    assert res.sum == s
+    assert list(res.partials[: res.n_partials]) == parts[: res.n_partials]
+    mv, mc, aw, ac = oracle.max_majority(ref, scale, mode)
+    m = col.max(argmax=True)
+    assert m.code == mc and m.value == mv
+    assert np.array_equal(m.argmax_words, aw) and m.argmax_count == ac
+    assert n == col.n
+
+
+@pytest.mark.parametrize("kind", ["one", "two", "three", "none"])
+@pytest.mark.parametrize("n", [4099, 300_001])
+def test_major_raw_bitmaps_bit_exact(oracle, gpu, kind, n):
+    from buff_gb300.compress import FLAG_RAW_BITMAPS, MajorColumn
+
+    x, scale = major_case(kind, n, 11)
+    ref = oracle.encode_majority(x, scale, RAW)
+    col = MajorColumn.encode(x, scale, FLAG_RAW_BITMAPS)
+    assert col.serialize() == ref
+    _check_queries(oracle, col, ref, scale, RAW, x)
+    back = MajorColumn.deserialize(ref, scale, FLAG_RAW_BITMAPS)
+    assert back.serialize() == ref
+    _check_queries(oracle, back, ref, scale, RAW, x)
+
+
+@pytest.mark.parametrize("kind", ["one", "two", "three", "none"])
+def test_major_snappy_bitmaps(oracle, gpu, kind):
+    from buff_gb300.compress import MajorColumn
+
+    x, scale = major_case(kind, 200_003, 12)
+    ref = oracle.encode_majority(x, scale, SNAPPY)
+    col = MajorColumn.encode(x, scale)
+    img = col.serialize()
+    # both snappy streams hold the same bitmaps: the decoded layouts agree
+    assert oracle.majority_layout(img, SNAPPY) == oracle.majority_layout(ref, SNAPPY)
+    nouts = oracle.majority_layout(ref, SNAPPY)[2]
+    if all(nouts):
+        assert np.array_equal(oracle.decode_majority(img, scale, SNAPPY),
+                              oracle.decode_majority(ref, scale, SNAPPY))
+    _check_queries(oracle, col, ref, scale, SNAPPY, x)
+    back = MajorColumn.deserialize(ref, scale)
+    _check_queries(oracle, back, ref, scale, SNAPPY, x)
+
+
+def test_major_outlier_workload(oracle, gpu):
+    """A 1% outlier column with 6 decimals: one sparse byte column."""
+    from buff_gb300 import workloads
+    from buff_gb300.compress import FLAG_RAW_BITMAPS, MajorColumn
+
+    x = workloads.outlier_column(1_000_003, seed=4)
+    ref = oracle.encode_majority(x, 1000000, RAW)
+    col = MajorColumn.encode(x, 1000000, FLAG_RAW_BITMAPS)
+    assert col.serialize() == ref
+    _check_queries(oracle, col, ref, 1000000, RAW, x)
+
+
+def test_major_f32_and_device_input(oracle, gpu):
+    import torch
+
+    from buff_gb300.compress import FLAG_RAW_BITMAPS, MajorColumn
+
+    x, scale = major_case("two", 50_001, 13)
+    x32 = x.astype(np.float32)
+    ref = oracle.encode_majority(x32.astype(np.float64), scale, RAW)
+    assert MajorColumn.encode(x32, scale, FLAG_RAW_BITMAPS).serialize() == ref
+    dev = torch.from_numpy(x).cuda()
+    ref64 = oracle.encode_majority(x, scale, RAW)
+    col = MajorColumn.encode(dev, scale, FLAG_RAW_BITMAPS)
+    assert col.serialize() == ref64
+    out = torch.empty(x.size, dtype=torch.float64, device="cuda")
+    nouts = oracle.majority_layout(ref64, RAW)[2]
+    if all(nouts):
+        col.decode(out=out)
+        assert np.array_equal(out.cpu().numpy(), oracle.decode_majority(ref64, scale, RAW))
+
+
+def test_major_errors(gpu):
+    from buff_gb300 import capi
+    from buff_gb300.compress import FLAG_INTENDED, Column, MajorColumn
+
+    with pytest.raises(capi.ReferencePanic):  # fewer rows than the 2000-row sample
+        MajorColumn.encode(np.arange(1999.0), 100)
+    with pytest.raises(capi.BuffError) as e:
+        MajorColumn.encode(np.arange(5000.0), 100, FLAG_INTENDED)
+    assert e.value.status == capi.ENOTSUP
+    x, scale = major_case("one", 5000, 3)
+    col = MajorColumn.encode(x, scale)
+    for fn in (lambda: Column.decode(col), lambda: Column.range_filter(col, 1.0),
+               lambda: Column.sum(col), lambda: Column.max(col)):
+        with pytest.raises(capi.BuffError) as e:
+            fn()
+        assert e.value.status == capi.ENOTSUP
+    plain = Column.encode(x, scale)
+    with pytest.raises(capi.BuffError) as e:
+        MajorColumn.sum(plain)
+    assert e.value.status == capi.ENOTSUP
+    ref = col.serialize()
+    with pytest.raises(capi.BuffError) as e:  # truncated image
+        MajorColumn.deserialize(ref[: len(ref) // 2], scale)
+    assert e.value.status == capi.ECORRUPT
