@@ -17,6 +17,7 @@ OK, EINVAL, ENOMEM, ECUDA, EREFPANIC, ECORRUPT, ETIMEDOUT, ENOTSUP, EFULL, ESCRA
 NOALLOC_MAX_ROWS = 1 << 26
 FLAG_INTENDED = 0x1
 FLAG_RAW_BITMAPS = 0x2
+FLAG_BUFF_LAYOUT = 0x4
 
 EXPORTED = [
     "buff_encode_f64", "buff_encode_f32", "buff_col_free", "buff_col_free_async",
@@ -30,6 +31,9 @@ EXPORTED = [
     "buff_encode_majority_f64", "buff_encode_majority_f32", "buff_deserialize_majority",
     "buff_decode_majority", "buff_range_filter_majority", "buff_equal_filter_majority",
     "buff_sum_majority", "buff_max_majority",
+    "buff_decode_condition", "buff_major_decode_condition", "buff_decode_selected",
+    "buff_range_filter_condition", "buff_range_filter_majority_condition",
+    "buff_range_filter_decode",
 ]
 
 
@@ -111,6 +115,12 @@ def lib(build_if_missing: bool = True):
     L.buff_equal_filter_majority.argtypes = [P, C.c_double, P, P, P]
     L.buff_sum_majority.argtypes = [P, C.POINTER(SumResult), P]
     L.buff_max_majority.argtypes = [P, P, P, P, P, P]
+    L.buff_decode_condition.argtypes = [P, P, C.c_uint64, P, P]
+    L.buff_major_decode_condition.argtypes = [P, P, C.c_uint64, P, P, P]
+    L.buff_decode_selected.argtypes = [P, P, P, P, P]
+    L.buff_range_filter_condition.argtypes = [P, C.c_double, P, P, P, P]
+    L.buff_range_filter_majority_condition.argtypes = [P, C.c_double, P, P, P, P]
+    L.buff_range_filter_decode.argtypes = [P, C.c_double, P, P, P, P]
     L.buff_status_string.argtypes = [C.c_int]
     L.buff_status_string.restype = C.c_char_p
     L.buff_last_cuda_error.restype = C.c_int

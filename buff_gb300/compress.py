@@ -18,7 +18,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import capi
-from .capi import FLAG_INTENDED, FLAG_RAW_BITMAPS, check, lib, ptr, stream_handle
+from .capi import (FLAG_BUFF_LAYOUT, FLAG_INTENDED, FLAG_RAW_BITMAPS, check, lib, ptr,
+                   stream_handle)
 
 
 @dataclass
@@ -33,6 +34,20 @@ class FilterResult:
         w = np.asarray(self.words if isinstance(self.words, np.ndarray) else self.words.cpu())
         bits = np.unpackbits(w.astype("<u4").view(np.uint8), bitorder="little")
         return np.nonzero(bits[: self.n])[0]
+
+
+def rows_to_words(rows, n: int) -> np.ndarray:
+    """A BitVec<u32> bitmap with the listed rows set."""
+    bits = np.zeros(((n + 31) // 32) * 32, dtype=np.uint8)
+    bits[np.asarray(rows, dtype=np.int64)] = 1
+    return np.packbits(bits, bitorder="little").view("<u4").astype(np.uint32)
+
+
+def _row_list(rows):
+    if hasattr(rows, "data_ptr"):  # torch tensor (uint32 / int32), host or device
+        return rows.contiguous(), rows.numel()
+    arr = np.ascontiguousarray(np.asarray(rows, dtype=np.uint32).reshape(-1))
+    return arr, arr.size
 
 
 @dataclass
@@ -181,6 +196,62 @@ class Column:
         check(lib().buff_sum(self._h, C.byref(res), stream_handle(stream)), "sum")
         return res
 
+    # -- row-conditioned reads -------------------------------------------
+    _DECODE_CONDITION = "buff_decode_condition"
+    _FILTER_CONDITION = "buff_range_filter_condition"
+
+    def decode_condition(self, rows, out=None, stream=None):
+        """Values of the listed rows (strictly ascending ids)."""
+        r, m = _row_list(rows)
+        dst = out if out is not None else np.empty(max(m, 1), dtype=np.float64)
+        if self._DECODE_CONDITION == "buff_decode_condition":
+            check(lib().buff_decode_condition(self._h, ptr(r), m, ptr(dst), stream_handle(stream)),
+                  "decode_condition")
+            return dst if out is not None else dst[:m]
+        nout = C.c_uint64(0)
+        check(lib().buff_major_decode_condition(self._h, ptr(r), m, ptr(dst), C.byref(nout),
+                                                stream_handle(stream)), "decode_condition")
+        return dst[: nout.value] if out is None else dst
+
+    def decode_selected(self, words, out=None, stream=None):
+        """Values of the rows set in a bitmap (e.g. a FilterResult's words)."""
+        if isinstance(words, FilterResult):
+            words = words.words
+        cnt = C.c_uint64(0)
+        dst = out if out is not None else np.empty(max(self.n, 1), dtype=np.float64)
+        check(lib().buff_decode_selected(self._h, ptr(words), ptr(dst), C.byref(cnt),
+                                         stream_handle(stream)), "decode_selected")
+        return dst[: cnt.value] if out is None else (dst, cnt.value)
+
+    def range_filter_condition(self, pred, cand, out=None, stream=None) -> FilterResult:
+        """Range predicate on candidate rows (a bitmap or a row list)."""
+        n = self.n
+        nw = (n + 31) // 32
+        if isinstance(cand, FilterResult):
+            cand = cand.words
+        elif not (hasattr(cand, "data_ptr") or
+                  (isinstance(cand, np.ndarray) and cand.dtype == np.uint32 and cand.size == nw)):
+            cand = rows_to_words(cand, n)
+        cnt = np.zeros(1, dtype=np.uint64)
+        words = out if out is not None else np.zeros(max(nw, 1), dtype=np.uint32)
+        fn = getattr(lib(), self._FILTER_CONDITION)
+        check(fn(self._h, float(pred), ptr(cand), ptr(words), ptr(cnt), stream_handle(stream)),
+              self._FILTER_CONDITION)
+        if out is None:
+            words = words[:nw]
+        return FilterResult(words, int(cnt[0]), n)
+
+    def range_filter_decode(self, pred, stream=None):
+        """Range filter, then the selected rows' values (one call)."""
+        n = self.n
+        words = np.zeros(max((n + 31) // 32, 1), dtype=np.uint32)
+        vals = np.empty(max(n, 1), dtype=np.float64)
+        cnt = C.c_uint64(0)
+        check(lib().buff_range_filter_decode(self._h, float(pred), ptr(words), ptr(vals),
+                                             C.byref(cnt), stream_handle(stream)),
+              "range_filter_decode")
+        return FilterResult(words[: (n + 31) // 32], cnt.value, n), vals[: cnt.value]
+
     def sum_at_precision(self, precision: int, stream=None) -> float:
         v = C.c_double(0)
         check(lib().buff_sum_at_precision(self._h, precision, C.byref(v), stream_handle(stream)),
@@ -206,6 +277,8 @@ class MajorColumn(Column):
 
     _ENCODE = ("buff_encode_majority_f32", "buff_encode_majority_f64")
     _DESERIALIZE = "buff_deserialize_majority"
+    _DECODE_CONDITION = "buff_major_decode_condition"
+    _FILTER_CONDITION = "buff_range_filter_majority_condition"
 
     def decode(self, out=None, stream=None):
         if out is None:
@@ -243,6 +316,7 @@ class MajorColumn(Column):
 
     decode_at_precision = sum_at_precision = _unsupported
     range_filter_with_slice = equal_filter_with_slice = _unsupported
+    decode_selected = range_filter_decode = _unsupported
 
 
 def _as_major(comp: "SplitBDDoubleCompress", data) -> MajorColumn:
@@ -306,6 +380,14 @@ class SplitBDDoubleCompress:
     def byte_residue_sum_with_precision(self, data, precision: int, stream=None) -> float:
         return _as_column(self, data).sum_at_precision(precision, stream=stream)
 
+    # compress/buff_simd.rs:1528-1712 (buff layout; rows strictly ascending)
+    def buff_decode_condition(self, data, rows, stream=None):
+        return _as_column(self, data).decode_condition(rows, stream=stream)
+
+    # compress/buff_simd.rs:4683-4921 (returns the BitVec<u32>)
+    def buff_range_filter_condition(self, data, pred, rows, stream=None) -> FilterResult:
+        return _as_column(self, data).range_filter_condition(pred, rows, stream=stream)
+
     # ---- buff-major (outlier) format --------------------------------
     # compress/buff_simd.rs:317-630
     def buff_encode_majority(self, values, stream=None) -> MajorColumn:
@@ -331,6 +413,14 @@ class SplitBDDoubleCompress:
     def buff_max_majority(self, data, stream=None) -> MaxResult:
         return _as_major(self, data).max(argmax=True, stream=stream)
 
+    # compress/buff_simd.rs:1714-1914
+    def buff_major_decode_condition(self, data, rows, stream=None):
+        return _as_major(self, data).decode_condition(rows, stream=stream)
+
+    # compress/buff_simd.rs:1279-1526
+    def buff_range_filter_majority_condition(self, data, pred, rows, stream=None) -> FilterResult:
+        return _as_major(self, data).range_filter_condition(pred, rows, stream=stream)
+
 
 __all__ = ["SplitBDDoubleCompress", "Column", "MajorColumn", "FilterResult", "MaxResult",
-           "FLAG_INTENDED", "FLAG_RAW_BITMAPS"]
+           "FLAG_INTENDED", "FLAG_RAW_BITMAPS", "FLAG_BUFF_LAYOUT", "rows_to_words"]

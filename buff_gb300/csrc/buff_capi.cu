@@ -433,7 +433,7 @@ int filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t *count
   if (count_host) CK(cudaMemcpyAsync(count, dcount, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
   if (need_sync) CK(cudaStreamSynchronize(s));
 done:
-  if (words_host && dwords) cudaFreeAsync(dwords, s);
+  if (words_host && dwords && dwords != words) cudaFreeAsync(dwords, s);
   if (count_host && dcount) cudaFreeAsync(dcount, s);
   return rc;
 }
@@ -678,8 +678,162 @@ int filter_major_impl(const buff_col *c, double pred, uint32_t *words, uint64_t 
   if (count_host) CK(cudaMemcpyAsync(count, dcount, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
   if (words_host || count_host) CK(cudaStreamSynchronize(s));
 done:
-  if (words_host && dwords) cudaFreeAsync(dwords, s);
+  if (words_host && dwords && dwords != words) cudaFreeAsync(dwords, s);
   if (count_host && dcount) cudaFreeAsync(dcount, s);
+  return rc;
+}
+
+
+// ---------------------------------------------------------------- row-conditioned reads
+
+// Device copy of a row list (host lists are checked here, device lists by a
+// kernel); BUFF_EINVAL unless strictly ascending and below n, as the
+// reference's `entry - pre` walk requires.
+int stage_rows(const buff_col *c, const uint32_t *rows, uint64_t nrows, const uint32_t **drows,
+               uint32_t **owned, cudaStream_t s) {
+  int rc = BUFF_OK;
+  *owned = nullptr;
+  *drows = rows;
+  if (is_device_ptr(rows)) {
+    uint32_t *bad = nullptr, hbad = 0;
+    CK(scratch(&bad, 1, s));
+    CK(cudaMemsetAsync(bad, 0, 4, s));
+    CK(buffk::check_rows(rows, nrows, c->n, bad, s));
+    CK(cudaMemcpyAsync(&hbad, bad, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    cudaFreeAsync(bad, s);
+    if (hbad) return BUFF_EINVAL;
+    return BUFF_OK;
+  }
+  for (uint64_t i = 0; i < nrows; ++i)
+    if (rows[i] >= c->n || (i && rows[i] <= rows[i - 1])) return BUFF_EINVAL;
+  CK(scratch(owned, nrows, s));
+  CK(cudaMemcpyAsync(*owned, rows, nrows * 4, cudaMemcpyHostToDevice, s));
+  *drows = *owned;
+done:
+  return rc;
+}
+
+int decode_list_impl(const buff_col *c, const uint32_t *rows, uint64_t nrows, double *out,
+                     int tail_shift, cudaStream_t s) {
+  int rc = BUFF_OK;
+  const uint32_t *drows = nullptr;
+  uint32_t *owned = nullptr;
+  const bool stage = !is_device_ptr(out);
+  double *d = stage ? nullptr : out;
+  if ((rc = stage_rows(c, rows, nrows, &drows, &owned, s))) goto done;
+  if (stage) CK(scratch(&d, nrows, s));
+  CK(buffk::decode_rows(c, drows, nrows, nullptr, nullptr, tail_shift, d, s));
+  if (stage) {
+    CK(cudaMemcpyAsync(out, d, nrows * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (owned) cudaFreeAsync(owned, s);
+  if (stage && d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+// Rows set in device words `dwords` (bits at or past n ignored): their
+// ranks, the count, and the decoded values into `out` (host or device).
+int decode_words_impl(const buff_col *c, const uint32_t *dwords, double *out, uint64_t *count,
+                      int tail_shift, cudaStream_t s) {
+  int rc = BUFF_OK;
+  const uint32_t n = c->n;
+  const size_t nw = ((size_t)n + 31) / 32;
+  uint32_t *rank = nullptr;
+  uint32_t tailw[2] = {0, 0};
+  uint64_t cnt = 0;
+  const bool stage = out && !is_device_ptr(out);
+  double *d = stage ? nullptr : out;
+  if (n == 0) {
+    if (count) *count = 0;
+    return BUFF_OK;
+  }
+  CK(scratch(&rank, nw + 1, s));
+  CK(buffk::word_ranks(dwords, nw, rank, s));
+  CK(cudaMemcpyAsync(&tailw[0], rank + nw - 1, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&tailw[1], dwords + nw - 1, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  {
+    const uint32_t valid = (n & 31) ? ((1u << (n & 31)) - 1u) : 0xFFFFFFFFu;
+    cnt = (uint64_t)tailw[0] + (uint64_t)__builtin_popcount(tailw[1] & valid);
+  }
+  if (count) *count = cnt;
+  if (out && cnt) {
+    if (stage) CK(scratch(&d, cnt, s));
+    CK(buffk::decode_rows(c, nullptr, 0, dwords, rank, tail_shift, d, s));
+    if (stage) {
+      CK(cudaMemcpyAsync(out, d, cnt * 8, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    }
+  }
+done:
+  if (rank) cudaFreeAsync(rank, s);
+  if (stage && d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+// buff_range_filter_condition (buff_simd.rs:4683-4921): candidate rows only,
+// no early "all rows" (the reference returns its empty res), truncated
+// target bytes, no 32-row restriction.
+int filter_cond_impl(const buff_col *c, double pred, const uint32_t *cand, uint32_t *words,
+                     uint64_t *count, cudaStream_t s) {
+  const uint32_t n = c->n, nw = (n + 31) / 32;
+  int rc = BUFF_OK;
+  uint32_t *dwords = words, *dcand = const_cast<uint32_t *>(cand);
+  unsigned long long *dcount = nullptr;
+  const bool words_host = n > 0 && !is_device_ptr(words);
+  const bool count_host = count && !is_device_ptr(count);
+  const bool cand_host = n > 0 && !is_device_ptr(cand);
+  const int64_t fp = fetch_fixed_host(pred, c->precision_exp, c->dlen);
+  bool none = fp < c->base;
+  uint8_t tb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  uint32_t ttail = 0;
+  if (!none) {
+    const uint64_t t = (uint64_t)(fp - c->base);
+    if (c->k == 0) {  // fixed_len < 8: `dec > fixed_target as u8` (:4713-4748)
+      const uint32_t tt = (uint32_t)(t & 0xFF);
+      if (c->r < 8 && tt >= (1u << c->r)) none = true;
+      ttail = tt;
+    } else {
+      for (uint32_t j = 0; j < c->k; ++j) tb[j] = (uint8_t)(t >> (c->fixed_len - 8 * (j + 1)));
+      ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
+    }
+  }
+  if (n == 0) {
+    if (count) {
+      if (count_host)
+        *count = 0;
+      else
+        return cuda_status(cudaMemsetAsync(count, 0, sizeof(uint64_t), s));
+    }
+    return BUFF_OK;
+  }
+  if (words_host) CK(scratch(&dwords, nw, s));
+  if (count) {
+    if (count_host)
+      CK(scratch(&dcount, 1, s));
+    else
+      dcount = reinterpret_cast<unsigned long long *>(count);
+    CK(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s));
+  }
+  if (none) {
+    CK(buffk::launch_fill_words(dwords, n, 0u, dcount, s));
+  } else {
+    if (cand_host) {
+      CK(scratch(&dcand, nw, s));
+      CK(cudaMemcpyAsync(dcand, cand, (size_t)nw * 4, cudaMemcpyHostToDevice, s));
+    }
+    CK(buffk::major_filter(c, 1, tb, ttail, dwords, dcount, s, dcand));
+  }
+  if (words_host) CK(cudaMemcpyAsync(words, dwords, (size_t)nw * 4, cudaMemcpyDeviceToHost, s));
+  if (count_host) CK(cudaMemcpyAsync(count, dcount, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  if (words_host || count_host || cand_host) CK(cudaStreamSynchronize(s));
+done:
+  if (words_host && dwords && dwords != words) cudaFreeAsync(dwords, s);
+  if (count_host && dcount) cudaFreeAsync(dcount, s);
+  if (cand_host && dcand && dcand != cand) cudaFreeAsync(dcand, s);
   return rc;
 }
 
@@ -768,11 +922,15 @@ int buff_serialize(const buff_col *c, uint8_t *out, uint64_t cap, uint64_t *len,
     memcpy(out, hdr, 20);
   if (c->k && c->n)
     CK(cudaMemcpy2DAsync(out + 20, c->n, c->slices, c->stride, c->n, c->k, cudaMemcpyDefault, s));
+  // the buff layout (byte_fixed_encode) stores the slice bytes unflipped
+  if (dev && (c->flags & BUFF_FLAG_BUFF_LAYOUT))
+    CK(buffk::flip_bytes(out + 20, (size_t)c->k * c->n, s));
   if (c->tail_bytes)
     CK(cudaMemcpyAsync(out + 20 + (uint64_t)c->k * c->n, c->tail, c->tail_bytes, cudaMemcpyDefault,
                        s));
-  if (dev) CK(cudaStreamSynchronize(s));  // hdr lives on this stack frame
-  else CK(cudaStreamSynchronize(s));
+  CK(cudaStreamSynchronize(s));  // hdr lives on this stack frame
+  if (!dev && (c->flags & BUFF_FLAG_BUFF_LAYOUT))
+    for (uint64_t i = 0; i < (uint64_t)c->k * c->n; ++i) out[20 + i] ^= 0x80u;
 done:
   return rc;
 }
@@ -818,6 +976,8 @@ int buff_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_
     if (c->k && c->n)
       CK(cudaMemcpy2DAsync(c->slices, c->stride, bytes + 20, c->n, c->n, c->k, cudaMemcpyDefault,
                            s));
+    if (c->k && c->n && (flags & BUFF_FLAG_BUFF_LAYOUT))
+      CK(buffk::flip_bytes(c->slices, (size_t)c->k * c->stride, s));
     // padding rows of every slice hold the flipped zero byte (what encode writes)
     if (c->k && c->stride > c->n)
       CK(cudaMemset2DAsync(c->slices + c->n, c->stride, 0x80, c->stride - c->n, c->k, s));
@@ -842,8 +1002,8 @@ int buff_decode(const buff_col *c, double *out, void *stream) {
   if (c->n == 0) return BUFF_OK;
   cudaStream_t s = S(stream);
   int rc = BUFF_OK;
-  double *d = out;
   const bool stage = !is_device_ptr(out) || (reinterpret_cast<uintptr_t>(out) & 15);
+  double *d = stage ? nullptr : out;
   if (stage) CK(scratch(&d, c->n, s));
   CK(buffk::launch_decode(c, c->fixed_len, 0, d, s));
   if (stage) {
@@ -870,8 +1030,8 @@ int buff_decode_at_precision(const buff_col *c, uint32_t precision, double *out,
   }
   if (c->n == 0) return BUFF_OK;
   cudaStream_t s = S(stream);
-  double *d = out;
   const bool stage = !is_device_ptr(out) || (reinterpret_cast<uintptr_t>(out) & 15);
+  double *d = stage ? nullptr : out;
   if (stage) CK(scratch(&d, c->n, s));
   CK(buffk::launch_decode(c, total, intended ? 1 : 0, d, s));
   if (stage) {
@@ -1190,8 +1350,8 @@ int buff_decode_majority(const buff_col *c, double *out, void *stream) {
   if (c->n == 0) return BUFF_OK;
   cudaStream_t s = S(stream);
   int rc = BUFF_OK;
-  double *d = out;
   const bool stage = !is_device_ptr(out) || (reinterpret_cast<uintptr_t>(out) & 15);
+  double *d = stage ? nullptr : out;
   if (stage) CK(scratch(&d, c->n, s));
   if (c->m)
     CK(buffk::major_decode(c, d, s));
@@ -1346,6 +1506,97 @@ done:
   if (cand) cudaFreeAsync(cand, s);
   if (buf) cudaFreeAsync(buf, s);
   if (cnt) cudaFreeAsync(cnt, s);
+  return rc;
+}
+
+// ---------------------------------------------------------------- row-conditioned ABI
+
+int buff_decode_condition(const buff_col *c, const uint32_t *rows, uint64_t nrows, double *out,
+                          void *stream) {
+  if (!c || (nrows && (!rows || !out))) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;
+  const bool intended = c->flags & BUFF_FLAG_INTENDED;
+  if (nrows == 0) return intended ? BUFF_OK : BUFF_EREFPANIC;  // iter.next().unwrap() (:1559)
+  return decode_list_impl(c, rows, nrows, out, intended ? 0 : 1, S(stream));
+}
+
+int buff_major_decode_condition(const buff_col *c, const uint32_t *rows, uint64_t nrows,
+                                double *out, uint64_t *nout, void *stream) {
+  if (!c || !nout || (nrows && (!rows || !out))) return BUFF_EINVAL;
+  if (c->layout != 1) return BUFF_ENOTSUP;
+  *nout = 0;
+  if (c->m > 0 || nrows == 0) return BUFF_OK;  // "not implemented yet": empty (:1741-1743)
+  const int rc = decode_list_impl(c, rows, nrows, out, 0, S(stream));
+  if (rc == BUFF_OK) *nout = nrows;
+  return rc;
+}
+
+int buff_decode_selected(const buff_col *c, const uint32_t *words, double *out, uint64_t *count,
+                         void *stream) {
+  if (!c || !count || (c->n && !words)) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  const size_t nw = ((size_t)c->n + 31) / 32;
+  uint32_t *dw = const_cast<uint32_t *>(words);
+  const bool host = c->n && !is_device_ptr(words);
+  if (host) {
+    CK(scratch(&dw, nw, s));
+    CK(cudaMemcpyAsync(dw, words, nw * 4, cudaMemcpyHostToDevice, s));
+  }
+  rc = decode_words_impl(c, dw, out, count, (c->flags & BUFF_FLAG_INTENDED) ? 0 : 1, s);
+done:
+  if (host && dw && dw != words) cudaFreeAsync(dw, s);
+  return rc;
+}
+
+int buff_range_filter_condition(const buff_col *c, double pred, const uint32_t *cand_words,
+                                uint32_t *words, uint64_t *count, void *stream) {
+  if (!c || (c->n && (!cand_words || !words))) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;
+  return filter_cond_impl(c, pred, cand_words, words, count, S(stream));
+}
+
+int buff_range_filter_majority_condition(const buff_col *c, double pred,
+                                         const uint32_t *cand_words, uint32_t *words,
+                                         uint64_t *count, void *stream) {
+  if (!c || (c->n && (!cand_words || !words))) return BUFF_EINVAL;
+  if (c->layout != 1) return BUFF_ENOTSUP;
+  if (c->m > 0) {  // "not implemented yet": the empty res (:1313-1315)
+    cudaStream_t s = S(stream);
+    int rc = BUFF_OK;
+    const size_t nw = ((size_t)c->n + 31) / 32;
+    if (nw) CK(cudaMemsetAsync(words, 0, nw * 4, s));
+    if (count) CK(cudaMemsetAsync(count, 0, sizeof(uint64_t), s));
+    CK(cudaStreamSynchronize(s));
+  done:
+    return rc;
+  }
+  return filter_cond_impl(c, pred, cand_words, words, count, S(stream));
+}
+
+int buff_range_filter_decode(const buff_col *c, double pred, uint32_t *words, double *out,
+                             uint64_t *count, void *stream) {
+  if (!c || !count || (c->n && !out)) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  const size_t nw = ((size_t)c->n + 31) / 32;
+  const bool own = !words || !is_device_ptr(words);
+  uint32_t *dw = own ? nullptr : words;
+  if (c->n == 0) {
+    *count = 0;
+    return BUFF_OK;
+  }
+  if (own) CK(scratch(&dw, nw, s));
+  if ((rc = filter_impl(c, pred, dw, nullptr, s, kRange))) goto done;
+  rc = decode_words_impl(c, dw, out, count, (c->flags & BUFF_FLAG_INTENDED) ? 0 : 1, s);
+  if (rc == BUFF_OK && words && own) {
+    CK(cudaMemcpyAsync(words, dw, nw * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (own && dw) cudaFreeAsync(dw, s);
   return rc;
 }
 

@@ -112,8 +112,12 @@ cudaError_t launch_decode(const buff_col *c, uint32_t total, int intended_mask, 
 cudaError_t major_build_sparse(buff_col *c, const uint8_t *lead, cudaStream_t s);
 cudaError_t major_index(buff_col *c, cudaStream_t s);
 cudaError_t flip_bytes(uint8_t *p, size_t nbytes, cudaStream_t s);
+// Filters of the buff-major layout; with m == 0 the same compare runs over a
+// plain column's slices and tail.  cand (may be null) restricts the rows.
 cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, uint32_t ttail,
-                         uint32_t *words, unsigned long long *count, cudaStream_t s);
+                         uint32_t *words, unsigned long long *count, cudaStream_t s,
+                         const uint32_t *cand = nullptr);
+cudaError_t word_ranks(const uint32_t *words, size_t nw, uint32_t *rank, cudaStream_t s);
 cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out,
                           cudaStream_t s);
 cudaError_t major_candmax(const buff_col *c, uint32_t col, const uint32_t *cand, uint32_t *out,
@@ -126,6 +130,16 @@ cudaError_t cand_select(const uint8_t *slice, const uint8_t *tail, uint32_t r, u
                         size_t nw, uint32_t value, unsigned long long *count, cudaStream_t s);
 cudaError_t popcount_words(const uint32_t *w, size_t nw, unsigned long long *out, cudaStream_t s);
 cudaError_t major_decode(const buff_col *c, double *out, cudaStream_t s);
+
+// Row-conditioned decode (buff_cond.cu): rows from a list (rows != null,
+// nrows entries) or from a bitmap with its word ranks (word_ranks).
+// tail_shift: 1 ORs the packed tail shifted by r (buff_decode_condition).
+cudaError_t decode_rows(const buff_col *c, const uint32_t *rows, uint64_t nrows,
+                        const uint32_t *words, const uint32_t *rank, int tail_shift, double *out,
+                        cudaStream_t s);
+// Sets *bad (device) to 1 unless rows[] is strictly ascending and below n.
+cudaError_t check_rows(const uint32_t *rows, uint64_t nrows, uint32_t n, uint32_t *bad,
+                       cudaStream_t s);
 
 int num_sms(int device);
 void count_launch(uint64_t n = 1);

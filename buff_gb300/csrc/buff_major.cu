@@ -34,8 +34,6 @@ namespace {
 
 using namespace dev;
 
-constexpr uint32_t kSample = 2000;  // split_double.rs:25 SAMPLE
-
 inline size_t rank_stride(const buff_col *c) { return c->nwp + 16; }
 
 // ---------------------------------------------------------------- encode
@@ -190,6 +188,7 @@ struct MajorArgs {
   uint8_t tbyte[8];  // target byte per full byte (sparse columns, then dense slices)
   uint32_t ttail;
   const uint8_t *slices, *tail;
+  const uint32_t *cand;  // candidate rows (null: all rows)
   uint32_t *words;
   unsigned long long *count;
 };
@@ -205,6 +204,7 @@ __global__ void __launch_bounds__(kThreads) k_filter_major(MajorArgs a) {
     const uint32_t row0 = (uint32_t)(w * 32);
     const uint32_t valid = a.n - row0 >= 32 ? 0xFFFFFFFFu : ((1u << (a.n - row0)) - 1u);
     uint32_t gt = 0, eq = valid;
+    if (a.cand) eq &= a.cand[w];
     for (uint32_t c = 0; c < a.m; ++c) {
       const uint32_t B = a.obits[c * a.nwp + w];
       const uint32_t M = a.majors[c], T = a.tbyte[c];
@@ -552,9 +552,11 @@ cudaError_t major_build_sparse(buff_col *c, const uint8_t *lead, cudaStream_t s)
 }
 
 cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, uint32_t ttail,
-                         uint32_t *words, unsigned long long *count, cudaStream_t s) {
+                         uint32_t *words, unsigned long long *count, cudaStream_t s,
+                         const uint32_t *cand) {
   MajorArgs a;
   memset(&a, 0, sizeof(a));
+  a.cand = cand;
   a.n = c->n;
   a.m = c->m;
   a.kd = c->k - c->m;
@@ -583,6 +585,24 @@ cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, 
     k_filter_major<false><<<grid, kThreads, 0, s>>>(a);
   count_launch();
   return cudaGetLastError();
+}
+
+// Exclusive prefix counts of set bits per word (rank[0..nw), total at
+// rank[nw]); rank needs nw + 1 entries.
+cudaError_t word_ranks(const uint32_t *words, size_t nw, uint32_t *rank, cudaStream_t s) {
+  uint32_t *tmp = nullptr;
+  const size_t nb = (nw + kScanItems - 1) / kScanItems + 1;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&tmp), sizeof(uint32_t) * nb, s);
+  if (e != cudaSuccess) return e;
+  if (nw) {
+    k_word_popc<<<grid_of(nw, 256), 256, 0, s>>>(words, nw, rank);
+    count_launch();
+    e = scan_exclusive(rank, nw, tmp, s);
+  } else {
+    e = cudaMemsetAsync(rank, 0, sizeof(uint32_t), s);
+  }
+  cudaFreeAsync(tmp, s);
+  return e;
 }
 
 cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out, cudaStream_t s) {

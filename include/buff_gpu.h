@@ -61,6 +61,11 @@ extern "C" {
 /* buff-major columns: store (and expect) the outlier bitmaps as raw
  * BitVec::to_binary bytes instead of snappy-compressed ones. */
 #define BUFF_FLAG_RAW_BITMAPS 0x2u
+/* Plain columns: the byte image is the buff layout of byte_fixed_encode
+ * (compress/split_double.rs:298-432), whose slice bytes are stored without
+ * the ^0x80 flip of buff_simd256_encode.  Affects buff_serialize and
+ * buff_deserialize only; every query returns the same results. */
+#define BUFF_FLAG_BUFF_LAYOUT 0x4u
 
 typedef struct buff_col buff_col;
 
@@ -197,6 +202,45 @@ int buff_sum_majority(const buff_col *col, buff_sum_result *out, void *stream);
  * arg-max rows of the tail step (argmax_words/argmax_count may be NULL). */
 int buff_max_majority(const buff_col *col, double *max_value, uint64_t *max_code,
                       uint32_t *argmax_words, uint64_t *argmax_count, void *stream);
+
+/* ---- row-conditioned reads ---- */
+
+/* buff_decode_condition (compress/buff_simd.rs:1528-1712): the values of the
+ * listed rows, in list order.  rows: strictly ascending row ids below n (host
+ * or device), else BUFF_EINVAL.  As in the reference, a code with a packed
+ * tail (fixed_len > 8, r > 0) gets its tail field ORed r bits too high, and an
+ * empty list panics (BUFF_EREFPANIC); BUFF_FLAG_INTENDED decodes exactly. */
+int buff_decode_condition(const buff_col *col, const uint32_t *rows, uint64_t nrows, double *out,
+                          void *stream);
+/* buff_major_decode_condition (compress/buff_simd.rs:1714-1914): exact values
+ * of the listed rows of a buff-major column without sparse columns; with
+ * sparse columns the reference returns an empty Vec (*nout = 0). */
+int buff_major_decode_condition(const buff_col *col, const uint32_t *rows, uint64_t nrows,
+                                double *out, uint64_t *nout, void *stream);
+/* buff_decode_condition over the rows set in a BitVec<u32> bitmap (the order
+ * BVIter yields them; bits at or past n are ignored).  *count = rows decoded;
+ * out needs room for that many values.  An empty bitmap gives *count = 0. */
+int buff_decode_selected(const buff_col *col, const uint32_t *words, double *out, uint64_t *count,
+                         void *stream);
+/* buff_range_filter_condition (compress/buff_simd.rs:4683-4921): the range
+ * predicate on the candidate rows set in cand_words (the reference walks them
+ * as a row iterator).  A target below the column's base gives no rows (the
+ * reference returns its empty result); target bytes are truncated as in the
+ * plain filter; every row may be set (no 32-row restriction). */
+int buff_range_filter_condition(const buff_col *col, double pred, const uint32_t *cand_words,
+                                uint32_t *words, uint64_t *count, void *stream);
+/* buff_range_filter_majority_condition (compress/buff_simd.rs:1279-1526):
+ * as above on a buff-major column without sparse columns; with sparse columns
+ * the reference returns an empty result. */
+int buff_range_filter_majority_condition(const buff_col *col, double pred,
+                                         const uint32_t *cand_words, uint32_t *words,
+                                         uint64_t *count, void *stream);
+/* No counterpart in the reference (it has no caller chaining the two): the
+ * bitmap of buff_range_filter, then buff_decode_selected on it, with the
+ * selected values left on the device when out is device memory.  words may be
+ * NULL; *count = rows selected. */
+int buff_range_filter_decode(const buff_col *col, double pred, uint32_t *words, double *out,
+                             uint64_t *count, void *stream);
 
 /* ---- allocation-free query ---- */
 

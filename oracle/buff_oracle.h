@@ -157,6 +157,19 @@ int or_sum_majority(const uint8_t *bytes, size_t len, uint64_t scale, int bm_mod
 int or_max_majority(const uint8_t *bytes, size_t len, uint64_t scale, int bm_mode, double *maxv,
                     uint64_t *max_code, uint32_t *argmax_words, uint64_t *argmax_count);
 
+/* --- row-conditioned reads of the buff layout: oracle/buff_oracle_cond.c ---
+ * rows: strictly ascending row ids below n (OR_EINVAL otherwise). */
+int or_decode_condition(const uint8_t *bytes, size_t len, uint64_t scale, const uint64_t *rows,
+                        size_t nrows, double *out);
+int or_major_decode_condition(const uint8_t *bytes, size_t len, uint64_t scale,
+                              const uint64_t *rows, size_t nrows, double *out, size_t *nout);
+int or_range_filter_condition(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                              const uint64_t *rows, size_t nrows, uint32_t *words,
+                              uint64_t *count);
+int or_range_filter_majority_condition(const uint8_t *bytes, size_t len, uint64_t scale,
+                                       double pred, const uint64_t *rows, size_t nrows,
+                                       uint32_t *words, uint64_t *count);
+
 #ifdef __cplusplus
 }
 #endif

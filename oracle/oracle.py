@@ -25,7 +25,8 @@ class OraclePanic(RuntimeError):
 
 
 def build() -> str:
-    srcs = [os.path.join(_HERE, f) for f in ("buff_oracle.c", "buff_oracle_major.c", "buff_oracle.h")]
+    srcs = [os.path.join(_HERE, f) for f in ("buff_oracle.c", "buff_oracle_major.c",
+                                             "buff_oracle_cond.c", "buff_oracle.h", "Makefile")]
     if (not os.path.exists(_LIB_PATH)) or any(os.path.getmtime(_LIB_PATH) < os.path.getmtime(s)
                                                for s in srcs):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -90,6 +91,10 @@ def lib():
             getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, C.c_int, P, P, P]
         L.or_sum_majority.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P, P]
         L.or_max_majority.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P, P, P, P]
+        L.or_decode_condition.argtypes = [P, C.c_size_t, C.c_uint64, P, C.c_size_t, P]
+        L.or_major_decode_condition.argtypes = [P, C.c_size_t, C.c_uint64, P, C.c_size_t, P, P]
+        for nm in ("or_range_filter_condition", "or_range_filter_majority_condition"):
+            getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, P, C.c_size_t, P, P]
         L.or_bench_filter_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, C.c_int,
                                           C.c_int, P, P]
         L.or_bench_filter_sum.restype = C.c_double
@@ -370,3 +375,49 @@ def max_majority(buf, scale, bm_mode=BM_SNAPPY):
     _check(lib().or_max_majority(_ptr(b), b.size, scale, bm_mode, _ptr(mv), _ptr(mc),
                                  _ptr(words), _ptr(cnt)))
     return float(mv[0]), int(mc[0]), words[: (n + 31) // 32], int(cnt[0])
+
+
+# --- row-conditioned reads of the buff layout (buff_oracle_cond.c) ---------
+
+def _rows(rows):
+    return np.ascontiguousarray(np.asarray(rows, dtype=np.uint64).reshape(-1))
+
+
+def decode_condition(buf, scale, rows):
+    """buff_decode_condition (buff_simd.rs:1528-1712) on a buff-layout image."""
+    b = _buf(buf)
+    r = _rows(rows)
+    out = np.zeros(max(r.size, 1), dtype=np.float64)
+    _check(lib().or_decode_condition(_ptr(b), b.size, scale, _ptr(r), r.size, _ptr(out)))
+    return out[: r.size]
+
+
+def major_decode_condition(buf, scale, rows):
+    """buff_major_decode_condition (buff_simd.rs:1714-1914)."""
+    b = _buf(buf)
+    r = _rows(rows)
+    out = np.zeros(max(r.size, 1), dtype=np.float64)
+    nout = C.c_size_t(0)
+    _check(lib().or_major_decode_condition(_ptr(b), b.size, scale, _ptr(r), r.size, _ptr(out),
+                                           C.byref(nout)))
+    return out[: nout.value]
+
+
+def _filter_cond(fn, buf, scale, pred, rows):
+    b = _buf(buf)
+    r = _rows(rows)
+    n = header(buf).n
+    words = np.zeros(max((n + 31) // 32, 1), dtype=np.uint32)
+    cnt = np.zeros(1, dtype=np.uint64)
+    _check(fn(_ptr(b), b.size, scale, pred, _ptr(r), r.size, _ptr(words), _ptr(cnt)))
+    return words[: (n + 31) // 32], int(cnt[0])
+
+
+def range_filter_condition(buf, scale, pred, rows):
+    """buff_range_filter_condition (buff_simd.rs:4683-4921)."""
+    return _filter_cond(lib().or_range_filter_condition, buf, scale, pred, rows)
+
+
+def range_filter_majority_condition(buf, scale, pred, rows):
+    """buff_range_filter_majority_condition (buff_simd.rs:1279-1526)."""
+    return _filter_cond(lib().or_range_filter_majority_condition, buf, scale, pred, rows)

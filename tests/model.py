@@ -302,3 +302,44 @@ def major_max_code(L) -> int:
     if r and cand:
         mx |= max(codes[i] & ((1 << r) - 1) for i in cand)
     return mx
+
+
+# --- row-conditioned reads (buff layout) ------------------------------------
+
+def cond_decode(L, rows, tail_shift: bool):
+    """buff_decode_condition (tail_shift, Q8) / buff_major_decode_condition."""
+    fl, r, base, dlen = L["fl"], L["r"], L["base"], L["dlen"]
+    out = []
+    for i in rows:
+        c = int(L["codes"][i])
+        if fl >= 8 and r and tail_shift:
+            c = (c >> r << r) | ((c & ((1 << r) - 1)) << r)
+        out.append(float(wrap64(base + c)) / 2.0 ** dlen)
+    return np.array(out, dtype=np.float64)
+
+
+def cond_range(L, pred: float, rows):
+    """buff_range_filter_condition: lexicographic compare of the (bytes, tail)
+    tuple with the truncated target tuple, on the listed rows only."""
+    n = L["codes"].size
+    fp = int(fetch_fixed(np.array([pred]), L["pexp"], L["dlen"])[0])
+    hit = np.zeros(n, dtype=np.uint8)
+    if fp < L["base"]:
+        return bits_to_words(hit)
+    t = fp - L["base"]
+    fl, k, r = L["fl"], L["k"], L["r"]
+
+    def tup(v):
+        if fl < 8:
+            return (v & ((1 << fl) - 1),)
+        return tuple((v >> (fl - 8 * (j + 1))) & 0xFF for j in range(k)) + \
+            ((v & ((1 << r) - 1),) if r else ())
+
+    if fl < 8:
+        tt = (t & 0xFF,)
+    else:
+        tt = tup(t)
+    for i in rows:
+        if tup(int(L["codes"][i])) > tt:
+            hit[i] = 1
+    return bits_to_words(hit)
