@@ -34,7 +34,12 @@ EXPORTED = [
     "buff_decode_condition", "buff_major_decode_condition", "buff_decode_selected",
     "buff_range_filter_condition", "buff_range_filter_majority_condition",
     "buff_range_filter_decode",
+    "buff_batch_encode_f64", "buff_plan_create", "buff_plan_set_preds", "buff_plan_launch",
+    "buff_plan_capture", "buff_plan_replay", "buff_plan_results", "buff_plan_free",
+    "buff_batch_autotune",
 ]
+
+Q_RANGE, Q_EQUAL, Q_SUM, Q_MAX, Q_DECODE = 0x1, 0x2, 0x4, 0x8, 0x10
 
 
 class BuffError(RuntimeError):
@@ -66,6 +71,26 @@ class SumResult(C.Structure):
     @property
     def exact_num(self) -> int:
         return (int(self.exact_num_hi) << 64) | (int(self.exact_num_lo) & ((1 << 64) - 1))
+
+
+class BatchTune(C.Structure):
+    _fields_ = [("tile_rows", C.c_uint32), ("blocks_per_sm", C.c_uint32),
+                ("stage", C.c_uint32), ("reserved", C.c_uint32)]
+
+    def __repr__(self):
+        return (f"BatchTune(tile_rows={self.tile_rows}, blocks_per_sm={self.blocks_per_sm}, "
+                f"stage={self.stage})")
+
+
+class Query(C.Structure):
+    _fields_ = [("col", C.c_void_p), ("ops", C.c_uint32), ("precision", C.c_uint32),
+                ("pred", C.c_double), ("words", C.c_void_p), ("values", C.c_void_p)]
+
+
+class QueryResult(C.Structure):
+    _fields_ = [("count", C.c_uint64), ("sum", C.c_double), ("max_value", C.c_double),
+                ("max_code", C.c_uint64), ("partials", C.c_uint64 * 9),
+                ("n_partials", C.c_uint32), ("status", C.c_int32)]
 
 
 _lib = None
@@ -121,6 +146,15 @@ def lib(build_if_missing: bool = True):
     L.buff_range_filter_condition.argtypes = [P, C.c_double, P, P, P, P]
     L.buff_range_filter_majority_condition.argtypes = [P, C.c_double, P, P, P, P]
     L.buff_range_filter_decode.argtypes = [P, C.c_double, P, P, P, P]
+    L.buff_batch_encode_f64.argtypes = [P, P, P, C.c_uint32, C.c_uint32, P, P, P]
+    L.buff_plan_create.argtypes = [P, C.c_uint32, P, P, pp]
+    L.buff_plan_set_preds.argtypes = [P, P]
+    L.buff_plan_launch.argtypes = [P, P]
+    L.buff_plan_capture.argtypes = [P, P]
+    L.buff_plan_replay.argtypes = [P, P]
+    L.buff_plan_results.argtypes = [P, P, P]
+    L.buff_plan_free.argtypes = [P]
+    L.buff_batch_autotune.argtypes = [P, C.c_uint32, P, P, P]
     L.buff_status_string.argtypes = [C.c_int]
     L.buff_status_string.restype = C.c_char_p
     L.buff_last_cuda_error.restype = C.c_int

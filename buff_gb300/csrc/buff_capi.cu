@@ -149,6 +149,16 @@ int alloc_col(buff_col *c, cudaStream_t s) {
 // have been reading the column.
 void free_col(buff_col *c, cudaStream_t s = nullptr, bool ordered = false) {
   if (!c) return;
+  if (c->arena) {  // slices and tail belong to the arena of a batched encode
+    if (c->arena->refs.fetch_sub(1) == 1) {
+      if (!ordered) cudaDeviceSynchronize();
+      cudaFreeAsync(c->arena->base, s);
+      if (!ordered) cudaStreamSynchronize(s);
+      delete c->arena;
+    }
+    c->slices = nullptr;
+    c->tail = nullptr;
+  }
   void *bufs[5] = {c->slices, c->tail, c->obits, c->orank, c->obytes};
   bool any = false;
   for (void *b : bufs) any |= b != nullptr;
@@ -1621,3 +1631,19 @@ int buff_last_cuda_error(void) { return g_last_cuda; }
 uint64_t buff_kernel_launches(void) { return buffk::launches(); }
 
 }  // extern "C"
+
+namespace buffh {
+int cuda_status(cudaError_t e) { return ::cuda_status(e); }
+bool is_device_ptr(const void *p) { return ::is_device_ptr(p); }
+int64_t fetch_fixed(double v, int pexp, uint32_t dlen) { return fetch_fixed_host(v, pexp, dlen); }
+void set_layout(buff_col *c, uint32_t fl) { ::set_layout(c, fl); }
+buff_col *new_col(uint64_t scale, uint32_t flags) { return ::new_col(scale, flags); }
+void free_col(buff_col *c) { ::free_col(c); }
+int precision_bits(const buff_col *c, uint32_t precision, uint32_t *total) {
+  return ::precision_bits(c, precision, total);
+}
+double combine_sum(const buff_col *c, uint32_t total, const uint64_t *parts, bool intended) {
+  return ::combine_sum(c, total, parts, intended);
+}
+int dlen_of_scale(uint64_t scale) { return dlen_of_prec(prec_of_scale(scale)); }
+}  // namespace buffh

@@ -16,6 +16,13 @@
 // BitPack::write_bits (methods/bit_packing.rs:106-135); for fixed_len < 8 it
 // holds the whole packed code (k == 0, r == fixed_len).  Padding rows beyond
 // n are zero in the tail and hold the flipped zero byte 0x80 in the slices.
+// One device allocation shared by the columns of a batched encode; freed
+// when the last of them is freed.
+struct buff_arena {
+  void *base;
+  std::atomic<int> refs;
+};
+
 struct buff_col {
   int64_t base;
   uint32_t n;
@@ -42,7 +49,22 @@ struct buff_col {
   uint32_t *orank;      // m x (nwp + 1) outliers before each word
   uint8_t *obytes;      // outlier bytes of all sparse columns, row order
   uint64_t oofs[9];     // start of each column's outlier bytes
+  buff_arena *arena;    // non-null: slices and tail live in a shared arena
 };
+
+// Host helpers of the C ABI (buff_capi.cu) shared with the batched and
+// serving code.
+namespace buffh {
+int cuda_status(cudaError_t e);
+bool is_device_ptr(const void *p);
+int64_t fetch_fixed(double v, int pexp, uint32_t dlen);
+void set_layout(buff_col *c, uint32_t fl);
+buff_col *new_col(uint64_t scale, uint32_t flags);
+void free_col(buff_col *c);
+int precision_bits(const buff_col *c, uint32_t precision, uint32_t *total);
+double combine_sum(const buff_col *c, uint32_t total, const uint64_t *parts, bool intended);
+int dlen_of_scale(uint64_t scale);  // -1: PRECISION_MAP has no entry
+}  // namespace buffh
 
 namespace buffk {
 

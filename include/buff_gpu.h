@@ -242,6 +242,74 @@ int buff_range_filter_majority_condition(const buff_col *col, double pred,
 int buff_range_filter_decode(const buff_col *col, double pred, uint32_t *words, double *out,
                              uint64_t *count, void *stream);
 
+/* ---- batched form (no counterpart in the reference: it runs one column per
+ *      call) ---- */
+
+/* Work-queue parameters of the persistent batched kernels. */
+typedef struct buff_batch_tune {
+  uint32_t tile_rows;     /* rows per work item: a multiple of 1024 (encode uses 4x) */
+  uint32_t blocks_per_sm; /* persistent 256-thread CTAs per SM, 1..8 */
+  uint32_t stage;         /* 1024-row steps whose first-slice loads are issued together: 1 or 2 */
+  uint32_t reserved;
+} buff_batch_tune;
+
+/* Encodes ncols f64 columns as buff_simd256_encode does, each with its own
+ * scale: one persistent launch takes every column's min/max, one more
+ * quantizes and scatters every column into a shared device arena (freed with
+ * its last column).  Columns given as host or unaligned pointers, with
+ * non-finite extremes, or whose `else if` max needs a second scan go through
+ * buff_encode_f64.  tune may be NULL.  out receives ncols handles. */
+int buff_batch_encode_f64(const double *const *values, const uint64_t *lens,
+                          const uint64_t *scales, uint32_t ncols, uint32_t flags,
+                          const buff_batch_tune *tune, void *stream, buff_col **out);
+
+#define BUFF_Q_RANGE 0x1u  /* buff_simd_range_filter bitmap */
+#define BUFF_Q_EQUAL 0x2u  /* buff_simd_equal_filter bitmap */
+#define BUFF_Q_SUM 0x4u    /* byte_fixed_sum */
+#define BUFF_Q_MAX 0x8u    /* byte_fixed_max value (no arg-max bitmap) */
+#define BUFF_Q_DECODE 0x10u /* buff_simd256_decode / byte_residue_decode_with_precision */
+
+/* One query of a batch: ops is one of RANGE or EQUAL (optionally with SUM),
+ * or any of SUM, MAX, DECODE.  Outputs are device memory. */
+typedef struct buff_query {
+  const buff_col *col; /* a plain (buff-simd) column */
+  uint32_t ops;
+  uint32_t precision;  /* DECODE: 0 = full precision, else decimals */
+  double pred;         /* RANGE / EQUAL */
+  uint32_t *words;     /* RANGE / EQUAL: ceil(n/32) words */
+  double *values;      /* DECODE: n values */
+} buff_query;
+
+typedef struct buff_query_result {
+  uint64_t count;       /* rows set by the filter */
+  double sum;           /* the reference's f64 sum */
+  double max_value;
+  uint64_t max_code;
+  uint64_t partials[9]; /* per-slice byte sums, then the tail sum */
+  uint32_t n_partials;
+  int32_t status;
+} buff_query_result;
+
+/* A batch of queries as one persistent launch over (query, row tile) items. */
+typedef struct buff_plan buff_plan;
+int buff_plan_create(const buff_query *queries, uint32_t nq, const buff_batch_tune *tune,
+                     void *stream, buff_plan **out);
+/* New predicates for the same queries (takes effect at the next launch or
+ * replay; the caller orders it after the previous one finished). */
+int buff_plan_set_preds(buff_plan *plan, const double *preds);
+int buff_plan_launch(buff_plan *plan, void *stream);
+/* Records the launch sequence of the plan into a CUDA graph (stream must
+ * not be the legacy default stream); buff_plan_replay launches it. */
+int buff_plan_capture(buff_plan *plan, void *stream);
+int buff_plan_replay(buff_plan *plan, void *stream);
+/* Waits for the stream and fills one result per query. */
+int buff_plan_results(buff_plan *plan, buff_query_result *out, void *stream);
+int buff_plan_free(buff_plan *plan);
+/* Times the plan over a grid of tile sizes, CTAs per SM and stage depths
+ * and returns the fastest (and its launch time in ms). */
+int buff_batch_autotune(const buff_query *queries, uint32_t nq, void *stream,
+                        buff_batch_tune *best, float *best_ms);
+
 /* ---- allocation-free query ---- */
 
 /* Largest column (rows) that buff_range_filter_noalloc accepts. */
