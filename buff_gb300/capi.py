@@ -37,6 +37,9 @@ EXPORTED = [
     "buff_batch_encode_f64", "buff_plan_create", "buff_plan_set_preds", "buff_plan_launch",
     "buff_plan_capture", "buff_plan_replay", "buff_plan_results", "buff_plan_free",
     "buff_batch_autotune",
+    "buff_server_create", "buff_server_add_column", "buff_server_start", "buff_server_submit",
+    "buff_server_poll", "buff_server_release", "buff_server_stop", "buff_server_free",
+    "buff_server_stats", "buff_server_replay", "buff_copy",
 ]
 
 Q_RANGE, Q_EQUAL, Q_SUM, Q_MAX, Q_DECODE = 0x1, 0x2, 0x4, 0x8, 0x10
@@ -91,6 +94,24 @@ class QueryResult(C.Structure):
     _fields_ = [("count", C.c_uint64), ("sum", C.c_double), ("max_value", C.c_double),
                 ("max_code", C.c_uint64), ("partials", C.c_uint64 * 9),
                 ("n_partials", C.c_uint32), ("status", C.c_int32)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("output_budget_bytes", C.c_uint64), ("store_budget_bytes", C.c_uint64),
+                ("max_batch", C.c_uint32), ("max_inflight", C.c_uint32),
+                ("batched", C.c_uint32), ("auto_release", C.c_uint32), ("tune", BatchTune)]
+
+
+class Request(C.Structure):
+    _fields_ = [("column", C.c_uint32), ("ops", C.c_uint32), ("precision", C.c_uint32),
+                ("reserved", C.c_uint32), ("pred", C.c_double), ("tag", C.c_uint64)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("status", C.c_int32), ("reserved", C.c_uint32),
+                ("result", QueryResult), ("words", C.c_void_p), ("values", C.c_void_p),
+                ("submit_ns", C.c_uint64), ("done_ns", C.c_uint64),
+                ("out_off", C.c_uint64 * 2), ("out_cls", C.c_int32 * 2)]
 
 
 _lib = None
@@ -155,6 +176,17 @@ def lib(build_if_missing: bool = True):
     L.buff_plan_results.argtypes = [P, P, P]
     L.buff_plan_free.argtypes = [P]
     L.buff_batch_autotune.argtypes = [P, C.c_uint32, P, P, P]
+    L.buff_server_create.argtypes = [C.POINTER(ServerConfig), pp]
+    L.buff_server_add_column.argtypes = [P, P, C.POINTER(C.c_uint32)]
+    L.buff_server_start.argtypes = [P]
+    L.buff_server_submit.argtypes = [P, P, C.c_uint32]
+    L.buff_server_poll.argtypes = [P, P, C.c_uint32, C.POINTER(C.c_uint32)]
+    L.buff_server_release.argtypes = [P, P]
+    L.buff_server_stop.argtypes = [P]
+    L.buff_server_free.argtypes = [P]
+    L.buff_server_stats.argtypes = [P, P, P, P]
+    L.buff_server_replay.argtypes = [P, P, P, C.c_uint32, P, P, P]
+    L.buff_copy.argtypes = [P, P, C.c_uint64, P]
     L.buff_status_string.argtypes = [C.c_int]
     L.buff_status_string.restype = C.c_char_p
     L.buff_last_cuda_error.restype = C.c_int
@@ -197,6 +229,13 @@ def stream_handle(stream):
     if isinstance(stream, int):
         return stream
     return stream.cuda_stream  # torch.cuda.Stream
+
+
+def copy_bytes(src: int, nbytes: int) -> bytes:
+    """Bytes at a device (or host) address, copied to the host."""
+    buf = np.empty(max(nbytes, 1), dtype=np.uint8)
+    check(lib().buff_copy(buf.ctypes.data, src, nbytes, None), "copy")
+    return buf[:nbytes].tobytes()
 
 
 def kernel_launches() -> int:

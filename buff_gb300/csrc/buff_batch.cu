@@ -318,7 +318,7 @@ struct BQ {
 
 constexpr uint32_t kOpRange = BUFF_Q_RANGE, kOpEqual = BUFF_Q_EQUAL, kOpSum = BUFF_Q_SUM,
                    kOpMax = BUFF_Q_MAX, kOpDecode = BUFF_Q_DECODE;
-constexpr int kAcc = 12;
+constexpr int kAcc = kBatchAcc;
 
 // tw[i] for a runtime i without indexing a register array (which would
 // place it in local memory).
@@ -510,13 +510,108 @@ __global__ void __launch_bounds__(kBT) k_batch(const BQ *__restrict__ qs,
   }
 }
 
+// The same work with items numbered per query: query q owns items
+// [prefix[q], prefix[q+1]) (its row tiles), found by binary search, so a
+// batch needs no item list.
+template <int STAGE>
+__global__ void __launch_bounds__(kBT) k_batch_pfx(const BQ *__restrict__ qs,
+                                                   const uint32_t *__restrict__ prefix,
+                                                   uint32_t nq, uint32_t nitems, uint32_t tile,
+                                                   unsigned int *counter) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1u);
+    it = __shfl_sync(0xFFFFFFFFu, it, 0);
+    if (it >= nitems) return;
+    uint32_t lo = 0, hi = nq;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (__ldg(prefix + mid) <= it)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    const BQ q = qs[lo];
+    const uint32_t r0 = (it - __ldg(prefix + lo)) * tile;
+    const uint32_t r1 = min(q.n, r0 + tile);
+    if (q.ops & (kOpRange | kOpEqual | kOpSum)) tile_filter_sum<STAGE>(q, r0, r1, lane);
+    if (q.ops & (kOpMax | kOpDecode)) tile_max_decode(q, r0, r1, lane);
+  }
+}
+
 int dev_sms() {
   int d = 0;
   cudaGetDevice(&d);
   return num_sms(d);
 }
 
+int plan_query(const buff_query &uq, unsigned long long *acc, BQ *q);
+
 }  // namespace
+
+// Entry points for the serving loop (buff_server.cu).
+size_t batch_desc_size() { return sizeof(BQ); }
+
+int batch_plan_query(const buff_query &q, unsigned long long *acc, void *desc) {
+  return plan_query(q, acc, static_cast<BQ *>(desc));
+}
+
+uint32_t batch_tiles(const void *desc, uint32_t tile) {
+  const BQ *q = static_cast<const BQ *>(desc);
+  return (q->n + tile - 1) / tile;
+}
+
+int batch_grid(const buff_batch_tune &t, uint32_t nitems) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, t.stage == 2 ? (const void *)k_batch_pfx<2> : (const void *)k_batch_pfx<1>, kBT, 0);
+  if (per_sm < 1) per_sm = 1;
+  const int bps = (int)t.blocks_per_sm < per_sm ? (int)t.blocks_per_sm : per_sm;
+  int grid = bps * dev_sms();
+  const uint32_t need = (nitems + kWarps - 1) / kWarps;
+  if ((uint32_t)grid > need) grid = need ? (int)need : 1;
+  return grid;
+}
+
+cudaError_t batch_launch_prefix(const void *d_desc, const uint32_t *d_prefix, uint32_t nq,
+                                uint32_t nitems, const buff_batch_tune &t, unsigned int *counter,
+                                cudaStream_t s) {
+  if (!nitems) return cudaSuccess;
+  const int grid = batch_grid(t, nitems);
+  const BQ *qs = static_cast<const BQ *>(d_desc);
+  if (t.stage == 2)
+    k_batch_pfx<2><<<grid, kBT, 0, s>>>(qs, d_prefix, nq, nitems, t.tile_rows, counter);
+  else
+    k_batch_pfx<1><<<grid, kBT, 0, s>>>(qs, d_prefix, nq, nitems, t.tile_rows, counter);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// Result of one query from its accumulators ([0] count, [1..8] slice sums,
+// [9] tail sum, [10] max code).
+void batch_result(const buff_query &q, const unsigned long long *a, buff_query_result *out) {
+  const buff_col *c = q.col;
+  buff_query_result &r = *out;
+  memset(&r, 0, sizeof(r));
+  const uint32_t ops = q.ops;
+  r.count = (ops & (kOpRange | kOpEqual)) ? a[0] : 0;
+  if (ops & kOpSum) {
+    // byte_fixed_sum over the whole code (split_double.rs:2127-2208)
+    uint64_t parts[9] = {0};
+    uint32_t np = 0;
+    for (uint32_t j = 0; j < c->k; ++j) parts[np++] = a[1 + j];
+    if (c->r) parts[np++] = a[9];
+    r.n_partials = np;
+    for (uint32_t j = 0; j < np; ++j) r.partials[j] = parts[j];
+    r.sum = buffh::combine_sum(c, c->fixed_len, parts, c->flags & BUFF_FLAG_INTENDED);
+  }
+  if ((ops & kOpMax) && c->n) {
+    r.max_code = a[10];
+    r.max_value = (double)(int64_t)((uint64_t)c->base + a[10]) / ldexp(1.0, (int)c->dlen);
+  }
+}
+
 }  // namespace buffk
 
 // ================================================================ host side
@@ -542,16 +637,8 @@ struct buff_plan {
   cudaGraphExec_t exec;
 };
 
+namespace buffk {
 namespace {
-
-#define BCK(expr)                              \
-  do {                                         \
-    cudaError_t _e = (expr);                   \
-    if (_e != cudaSuccess) {                   \
-      rc = buffh::cuda_status(_e);             \
-      goto done;                               \
-    }                                          \
-  } while (0)
 
 buff_batch_tune default_tune() {
   buff_batch_tune t;
@@ -637,6 +724,20 @@ int plan_query(const buff_query &uq, unsigned long long *acc, BQ *q) {
   }
   return BUFF_OK;
 }
+
+}  // namespace
+}  // namespace buffk
+
+namespace {
+
+#define BCK(expr)                              \
+  do {                                         \
+    cudaError_t _e = (expr);                   \
+    if (_e != cudaSuccess) {                   \
+      rc = buffh::cuda_status(_e);             \
+      goto done;                               \
+    }                                          \
+  } while (0)
 
 void release_plan(buff_plan *p) {
   if (!p) return;
@@ -781,27 +882,8 @@ int buff_plan_results(buff_plan *p, buff_query_result *out, void *stream) {
   const cudaError_t e = cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return buffh::cuda_status(e);
   for (uint32_t i = 0; i < p->nq; ++i) {
-    const buff_col *c = p->queries[i].col;
-    const unsigned long long *a = p->h_acc + (size_t)kAcc * i;
-    buff_query_result &r = out[i];
-    memset(&r, 0, sizeof(r));
-    const uint32_t ops = p->queries[i].ops;
-    r.count = (ops & (kOpRange | kOpEqual)) ? a[0] : 0;
-    if (ops & kOpSum) {
-      // byte_fixed_sum over the whole code (split_double.rs:2127-2208)
-      uint64_t parts[9] = {0};
-      uint32_t np = 0;
-      for (uint32_t j = 0; j < c->k; ++j) parts[np++] = a[1 + j];
-      if (c->r) parts[np++] = a[9];
-      r.n_partials = np;
-      for (uint32_t j = 0; j < np; ++j) r.partials[j] = parts[j];
-      r.sum = buffh::combine_sum(c, c->fixed_len, parts, c->flags & BUFF_FLAG_INTENDED);
-    }
-    if ((ops & kOpMax) && c->n) {
-      r.max_code = a[10];
-      r.max_value = (double)(int64_t)((uint64_t)c->base + a[10]) / ldexp(1.0, (int)c->dlen);
-    }
-    r.status = p->status[i];
+    batch_result(p->queries[i], p->h_acc + (size_t)kAcc * i, &out[i]);
+    out[i].status = p->status[i];
   }
   return BUFF_OK;
 }

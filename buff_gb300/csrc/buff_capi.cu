@@ -1628,6 +1628,15 @@ const char *buff_status_string(int st) {
 
 int buff_last_cuda_error(void) { return g_last_cuda; }
 
+int buff_copy(void *dst, const void *src, uint64_t nbytes, void *stream) {
+  if (nbytes && (!dst || !src)) return BUFF_EINVAL;
+  if (!nbytes) return BUFF_OK;
+  cudaStream_t s = S(stream);
+  cudaError_t e = cudaMemcpyAsync(dst, src, nbytes, cudaMemcpyDefault, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return cuda_status(e);
+}
+
 uint64_t buff_kernel_launches(void) { return buffk::launches(); }
 
 }  // extern "C"

@@ -163,6 +163,17 @@ cudaError_t decode_rows(const buff_col *c, const uint32_t *rows, uint64_t nrows,
 cudaError_t check_rows(const uint32_t *rows, uint64_t nrows, uint32_t n, uint32_t *bad,
                        cudaStream_t s);
 
+// Batched queries (buff_batch.cu) for the serving loop: per-query device
+// descriptors of batch_desc_size() bytes, accumulators of kBatchAcc u64.
+constexpr int kBatchAcc = 12;
+size_t batch_desc_size();
+int batch_plan_query(const buff_query &q, unsigned long long *acc, void *desc);
+uint32_t batch_tiles(const void *desc, uint32_t tile);
+cudaError_t batch_launch_prefix(const void *d_desc, const uint32_t *d_prefix, uint32_t nq,
+                                uint32_t nitems, const buff_batch_tune &t, unsigned int *counter,
+                                cudaStream_t s);
+void batch_result(const buff_query &q, const unsigned long long *acc, buff_query_result *out);
+
 int num_sms(int device);
 void count_launch(uint64_t n = 1);
 uint64_t launches();

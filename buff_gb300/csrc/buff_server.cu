@@ -1,0 +1,629 @@
+// Serving loop: a store of resident columns and a request loop with
+// continuous batching (buff_server_* in buff_gpu.h; the reference has no
+// serving layer).
+//
+// One host thread owns the GPU side.  Each pass it (1) retires every batch
+// whose event has fired, turning its accumulators into results and freeing
+// its outputs, then (2) admits waiting requests in arrival order while a
+// batch slot is free and the output budget allows, and launches them as one
+// persistent batched query kernel (buff_batch.cu) on that slot's stream.
+// Requests that arrive while earlier batches run are admitted into the next
+// free slot at once, so up to `max_inflight` batches overlap on the device.
+// With `batched = 0` the same loop runs one query per launch through the
+// single-column entry points (the baseline the batched form is compared to).
+//
+// Output memory (bitmaps, decoded values) comes from one device arena of
+// `output_budget_bytes`, handed out in power-of-two size classes; a request
+// whose outputs do not fit waits (and blocks later ones, keeping arrival
+// order) until completions return memory.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <atomic>
+#include <chrono>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "buff_internal.h"
+
+namespace {
+
+uint64_t now_ns() {
+  return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+int ceil_log2(uint64_t v) {
+  int c = 0;
+  while ((1ull << c) < v) ++c;
+  return c;
+}
+
+// Power-of-two size classes carved from one arena; freed blocks are reused
+// by their class.  reset() returns everything (only with nothing in flight).
+struct OutAlloc {
+  uint8_t *base = nullptr;
+  uint64_t cap = 0, bump = 0, used = 0;
+  std::vector<uint64_t> free_[48];
+
+  bool alloc(uint64_t bytes, uint64_t *off, int *cls) {
+    const int c = ceil_log2(bytes < 4096 ? 4096 : bytes);
+    if (c >= 48) return false;
+    const uint64_t sz = 1ull << c;
+    if (!free_[c].empty()) {
+      *off = free_[c].back();
+      free_[c].pop_back();
+    } else if (bump + sz <= cap) {
+      *off = bump;
+      bump += sz;
+    } else {
+      return false;
+    }
+    *cls = c;
+    used += sz;
+    return true;
+  }
+  void release(uint64_t off, int cls) {
+    free_[cls].push_back(off);
+    used -= 1ull << cls;
+  }
+  void reset() {
+    for (auto &f : free_) f.clear();
+    bump = 0;
+    used = 0;
+  }
+};
+
+struct Req {
+  buff_request r;
+  uint64_t submit_ns;
+  const buff_col *col;
+  uint32_t *words;
+  double *values;
+  uint64_t off[2];
+  int cls[2];  // -1: no allocation
+  int32_t status;
+};
+
+// Result area of one plain-mode request (pinned): count, 9 partials, max.
+struct PlainRes {
+  unsigned long long count;
+  unsigned long long parts[9];
+  unsigned long long max;
+};
+
+struct Slot {
+  cudaStream_t s = nullptr;
+  cudaEvent_t ev = nullptr;
+  void *h_desc = nullptr, *d_desc = nullptr;
+  uint32_t *h_pfx = nullptr, *d_pfx = nullptr;
+  unsigned long long *h_acc = nullptr, *d_acc = nullptr;
+  unsigned int *d_counter = nullptr;
+  PlainRes *h_plain = nullptr, *d_plain = nullptr;
+  std::vector<Req> reqs;
+  bool busy = false;
+  uint64_t seq = 0;
+};
+
+}  // namespace
+
+struct buff_server {
+  buff_server_config cfg;
+  int device = 0;
+  std::vector<buff_col *> store;
+  uint64_t store_bytes = 0;
+  OutAlloc out;
+  std::vector<Slot> slots;
+  uint64_t seq = 0;
+
+  std::mutex mu;  // pending and done
+  std::deque<Req> pending;
+  std::vector<buff_completion> done;
+  std::atomic<uint64_t> n_done{0};
+
+  std::thread th;
+  std::atomic<bool> running{false};
+  std::atomic<bool> stop{false};
+  std::atomic<int> loop_status{BUFF_OK};
+  std::deque<Req> waiting;  // loop thread only
+  uint64_t batches = 0, launched_reqs = 0;
+};
+
+namespace {
+
+uint64_t col_bytes(const buff_col *c) {
+  return (uint64_t)(c->k - c->m) * c->stride + c->tail_alloc;
+}
+
+void free_outputs(buff_server *S, Req &q) {
+  for (int i = 0; i < 2; ++i)
+    if (q.cls[i] >= 0) {
+      S->out.release(q.off[i], q.cls[i]);
+      q.cls[i] = -1;
+    }
+}
+
+uint64_t class_bytes(uint64_t b) { return 1ull << ceil_log2(b < 4096 ? 4096 : b); }
+
+// Output bytes a request needs, rounded to its size classes.
+uint64_t out_need(const Req &q) {
+  const uint64_t n = q.col->n;
+  uint64_t need = 0;
+  if (q.r.ops & (BUFF_Q_RANGE | BUFF_Q_EQUAL)) need += class_bytes(((n + 31) / 32) * 4);
+  if (q.r.ops & BUFF_Q_DECODE) need += class_bytes(8 * n);
+  return need;
+}
+
+// Output allocations of one request; false when the budget is full now.
+bool alloc_outputs(buff_server *S, Req &q) {
+  q.cls[0] = q.cls[1] = -1;
+  q.words = nullptr;
+  q.values = nullptr;
+  const uint32_t ops = q.r.ops;
+  const uint64_t n = q.col->n;
+  if (ops & (BUFF_Q_RANGE | BUFF_Q_EQUAL)) {
+    const uint64_t nb = ((n + 31) / 32) * 4;
+    if (!S->out.alloc(nb ? nb : 4, &q.off[0], &q.cls[0])) return false;
+    q.words = reinterpret_cast<uint32_t *>(S->out.base + q.off[0]);
+  }
+  if (ops & BUFF_Q_DECODE) {
+    if (!S->out.alloc(n ? 8 * n : 8, &q.off[1], &q.cls[1])) {
+      free_outputs(S, q);
+      return false;
+    }
+    q.values = reinterpret_cast<double *>(S->out.base + q.off[1]);
+  }
+  return true;
+}
+
+void finish(buff_server *S, Req &q, const buff_query_result &res) {
+  buff_completion c;
+  memset(&c, 0, sizeof(c));
+  c.tag = q.r.tag;
+  c.status = q.status;
+  c.result = res;
+  c.result.status = q.status;
+  c.submit_ns = q.submit_ns;
+  c.done_ns = now_ns();
+  if (S->cfg.auto_release) {
+    free_outputs(S, q);
+  } else {
+    c.words = q.words;
+    c.values = q.values;
+    c.out_off[0] = q.cls[0] >= 0 ? q.off[0] : ~0ull;
+    c.out_off[1] = q.cls[1] >= 0 ? q.off[1] : ~0ull;
+    c.out_cls[0] = q.cls[0];
+    c.out_cls[1] = q.cls[1];
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->done.push_back(c);
+  S->n_done.fetch_add(1, std::memory_order_release);
+}
+
+void retire(buff_server *S, Slot &sl) {
+  for (size_t i = 0; i < sl.reqs.size(); ++i) {
+    Req &q = sl.reqs[i];
+    buff_query_result res;
+    memset(&res, 0, sizeof(res));
+    if (q.status == BUFF_OK) {
+      buff_query uq;
+      memset(&uq, 0, sizeof(uq));
+      uq.col = q.col;
+      uq.ops = q.r.ops;
+      if (S->cfg.batched) {
+        buffk::batch_result(uq, sl.h_acc + (size_t)buffk::kBatchAcc * i, &res);
+      } else {
+        const PlainRes &p = sl.h_plain[i];
+        const buff_col *c = q.col;
+        if (uq.ops & (BUFF_Q_RANGE | BUFF_Q_EQUAL)) res.count = p.count;
+        if (uq.ops & BUFF_Q_SUM) {
+          buff_sum_result sr;
+          buff_sum_finish(c, reinterpret_cast<const uint64_t *>(p.parts), &sr);
+          res.sum = sr.sum;
+          res.n_partials = sr.n_partials;
+          for (uint32_t j = 0; j < sr.n_partials && j < 9; ++j) res.partials[j] = sr.partials[j];
+        }
+        if ((uq.ops & BUFF_Q_MAX) && c->n) {
+          res.max_code = p.max;
+          res.max_value = (double)(int64_t)((uint64_t)c->base + p.max) / ldexp(1.0, (int)c->dlen);
+        }
+      }
+    }
+    finish(S, q, res);
+  }
+  sl.reqs.clear();
+  sl.busy = false;
+}
+
+// One batch of admitted requests as one persistent launch.
+int launch_batched(buff_server *S, Slot &sl) {
+  const size_t dsz = buffk::batch_desc_size();
+  const uint32_t nq = (uint32_t)sl.reqs.size();
+  uint32_t items = 0;
+  for (uint32_t i = 0; i < nq; ++i) {
+    Req &q = sl.reqs[i];
+    buff_query uq;
+    memset(&uq, 0, sizeof(uq));
+    uq.col = q.col;
+    uq.ops = q.r.ops;
+    uq.precision = q.r.precision;
+    uq.pred = q.r.pred;
+    uq.words = q.words;
+    uq.values = q.values;
+    void *d = static_cast<uint8_t *>(sl.h_desc) + dsz * i;
+    q.status = buffk::batch_plan_query(uq, sl.d_acc + (size_t)buffk::kBatchAcc * i, d);
+    sl.h_pfx[i] = items;
+    if (q.status == BUFF_OK)
+      items += buffk::batch_tiles(d, S->cfg.tune.tile_rows);
+    else
+      memset(d, 0, dsz);  // an invalid request: zero rows, no work items
+  }
+  sl.h_pfx[nq] = items;
+  cudaStream_t s = sl.s;
+  cudaError_t e = cudaMemcpyAsync(sl.d_desc, sl.h_desc, dsz * nq, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(sl.d_pfx, sl.h_pfx, sizeof(uint32_t) * (nq + 1), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(sl.d_acc, 0, sizeof(unsigned long long) * buffk::kBatchAcc * nq, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_counter, 0, sizeof(unsigned int), s);
+  if (e == cudaSuccess)
+    e = buffk::batch_launch_prefix(sl.d_desc, sl.d_pfx, nq, items, S->cfg.tune, sl.d_counter, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(sl.h_acc, sl.d_acc, sizeof(unsigned long long) * buffk::kBatchAcc * nq,
+                        cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaEventRecord(sl.ev, s);
+  return buffh::cuda_status(e);
+}
+
+// One request through the single-column entry points (one query per launch).
+int launch_plain(Slot &sl) {
+  Req &q = sl.reqs[0];
+  const buff_col *c = q.col;
+  cudaStream_t s = sl.s;
+  void *sv = s;
+  PlainRes *d = sl.d_plain;
+  int st = BUFF_OK;
+  const uint32_t ops = q.r.ops;
+  if (ops & BUFF_Q_RANGE)
+    st = buff_range_filter(c, q.r.pred, q.words, reinterpret_cast<uint64_t *>(&d->count), sv);
+  else if (ops & BUFF_Q_EQUAL)
+    st = buff_equal_filter(c, q.r.pred, q.words, reinterpret_cast<uint64_t *>(&d->count), sv);
+  if (!st && (ops & BUFF_Q_SUM))
+    st = buff_sum_partials_async(c, reinterpret_cast<uint64_t *>(d->parts), sv);
+  if (!st && (ops & BUFF_Q_MAX)) st = buff_max_async(c, reinterpret_cast<uint64_t *>(&d->max), sv);
+  if (!st && (ops & BUFF_Q_DECODE))
+    st = q.r.precision ? buff_decode_at_precision(c, q.r.precision, q.values, sv)
+                       : buff_decode(c, q.values, sv);
+  q.status = st;
+  cudaError_t e = cudaMemcpyAsync(sl.h_plain, d, sizeof(PlainRes), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaEventRecord(sl.ev, s);
+  return buffh::cuda_status(e);
+}
+
+void loop(buff_server *S) {
+  cudaSetDevice(S->device);
+  const uint32_t maxb = S->cfg.batched ? S->cfg.max_batch : 1;
+  for (;;) {
+    bool worked = false;
+    // retire finished batches
+    for (Slot &sl : S->slots) {
+      if (!sl.busy) continue;
+      const cudaError_t q = cudaEventQuery(sl.ev);
+      if (q == cudaSuccess) {
+        retire(S, sl);
+        worked = true;
+      } else if (q != cudaErrorNotReady) {
+        S->loop_status.store(buffh::cuda_status(q));
+        for (Req &r : sl.reqs) r.status = BUFF_ECUDA;
+        retire(S, sl);
+      }
+    }
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      while (!S->pending.empty()) {
+        Req &q = S->pending.front();
+        if (!q.col)
+          free_outputs(S, q);  // buff_server_release of a completed request's outputs
+        else
+          S->waiting.push_back(q);
+        S->pending.pop_front();
+        worked = true;
+      }
+    }
+    // admit in arrival order into free slots
+    for (Slot &sl : S->slots) {
+      if (sl.busy || S->waiting.empty()) continue;
+      while (!S->waiting.empty() && sl.reqs.size() < maxb) {
+        Req &q = S->waiting.front();
+        if (out_need(q) > S->out.cap) {  // larger than the whole budget
+          q.status = BUFF_EFULL;
+          buff_query_result res;
+          memset(&res, 0, sizeof(res));
+          finish(S, q, res);
+          S->waiting.pop_front();
+          continue;
+        }
+        if (!alloc_outputs(S, q)) {
+          bool any = false;
+          for (Slot &o : S->slots) any |= o.busy;
+          // wait for completions (or the caller's releases) to return memory;
+          // with nothing in flight and nothing held by callers, the size
+          // classes are rebuilt from scratch
+          if (any || !sl.reqs.empty() || !S->cfg.auto_release) break;
+          S->out.reset();
+          if (!alloc_outputs(S, q)) break;
+        }
+        sl.reqs.push_back(q);
+        S->waiting.pop_front();
+      }
+      if (sl.reqs.empty()) break;
+      const int st = S->cfg.batched ? launch_batched(S, sl) : launch_plain(sl);
+      if (st) {
+        S->loop_status.store(st);
+        for (Req &r : sl.reqs) r.status = st;
+        retire(S, sl);
+        continue;
+      }
+      sl.busy = true;
+      sl.seq = ++S->seq;
+      S->batches++;
+      S->launched_reqs += sl.reqs.size();
+      worked = true;
+    }
+    if (!worked) {
+      bool idle = S->waiting.empty();
+      for (Slot &sl : S->slots) idle &= !sl.busy;
+      if (idle && S->stop.load()) {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (S->pending.empty()) break;
+      }
+      std::this_thread::yield();
+    }
+  }
+}
+
+void destroy_slots(buff_server *S) {
+  for (Slot &sl : S->slots) {
+    if (sl.ev) cudaEventDestroy(sl.ev);
+    if (sl.s) cudaStreamDestroy(sl.s);
+    if (sl.h_desc) cudaFreeHost(sl.h_desc);
+    if (sl.h_pfx) cudaFreeHost(sl.h_pfx);
+    if (sl.h_acc) cudaFreeHost(sl.h_acc);
+    if (sl.h_plain) cudaFreeHost(sl.h_plain);
+    if (sl.d_desc) cudaFree(sl.d_desc);
+    if (sl.d_pfx) cudaFree(sl.d_pfx);
+    if (sl.d_acc) cudaFree(sl.d_acc);
+    if (sl.d_counter) cudaFree(sl.d_counter);
+    if (sl.d_plain) cudaFree(sl.d_plain);
+  }
+  S->slots.clear();
+}
+
+}  // namespace
+
+extern "C" {
+
+int buff_server_create(const buff_server_config *cfg, buff_server **out) {
+  if (!cfg || !out) return BUFF_EINVAL;
+  *out = nullptr;
+  buff_server_config c = *cfg;
+  if (!c.max_inflight || c.max_inflight > 64 || !c.max_batch || c.max_batch > 65536 ||
+      !c.output_budget_bytes)
+    return BUFF_EINVAL;
+  if (c.tune.tile_rows == 0) {
+    c.tune.tile_rows = 32768;
+    c.tune.blocks_per_sm = 4;
+    c.tune.stage = 2;
+  }
+  if (c.tune.tile_rows % 1024 || c.tune.blocks_per_sm < 1 || c.tune.blocks_per_sm > 8 ||
+      (c.tune.stage != 1 && c.tune.stage != 2))
+    return BUFF_EINVAL;
+  buff_server *S = new (std::nothrow) buff_server();
+  if (!S) return BUFF_ENOMEM;
+  S->cfg = c;
+  cudaGetDevice(&S->device);
+  int rc = BUFF_OK;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&S->out.base), c.output_budget_bytes);
+  if (e != cudaSuccess) {
+    rc = buffh::cuda_status(e);
+    delete S;
+    return rc;
+  }
+  S->out.cap = c.output_budget_bytes;
+  S->slots.resize(c.max_inflight);
+  const uint32_t mb = c.batched ? c.max_batch : 1;
+  const size_t dsz = buffk::batch_desc_size();
+  for (Slot &sl : S->slots) {
+    if ((e = cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking)) != cudaSuccess) break;
+    if ((e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming)) != cudaSuccess) break;
+    if ((e = cudaMallocHost(&sl.h_desc, dsz * mb)) != cudaSuccess) break;
+    if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_pfx), 4 * (mb + 1))) != cudaSuccess) break;
+    if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_acc),
+                            8 * buffk::kBatchAcc * mb)) != cudaSuccess)
+      break;
+    if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_plain), sizeof(PlainRes))) != cudaSuccess)
+      break;
+    if ((e = cudaMalloc(&sl.d_desc, dsz * mb)) != cudaSuccess) break;
+    if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_pfx), 4 * (mb + 1))) != cudaSuccess) break;
+    if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_acc), 8 * buffk::kBatchAcc * mb)) !=
+        cudaSuccess)
+      break;
+    if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_counter), 4)) != cudaSuccess) break;
+    if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_plain), sizeof(PlainRes))) != cudaSuccess)
+      break;
+    sl.reqs.reserve(mb);
+  }
+  if (e != cudaSuccess) {
+    rc = buffh::cuda_status(e);
+    destroy_slots(S);
+    cudaFree(S->out.base);
+    delete S;
+    return rc;
+  }
+  *out = S;
+  return BUFF_OK;
+}
+
+int buff_server_add_column(buff_server *S, buff_col *col, uint32_t *id) {
+  if (!S || !col || !id) return BUFF_EINVAL;
+  if (col->layout != 0) return BUFF_ENOTSUP;
+  if (S->running.load()) return BUFF_EINVAL;  // the store is fixed while serving
+  const uint64_t b = col_bytes(col);
+  if (S->cfg.store_budget_bytes && S->store_bytes + b > S->cfg.store_budget_bytes)
+    return BUFF_EFULL;
+  S->store.push_back(col);
+  S->store_bytes += b;
+  *id = (uint32_t)(S->store.size() - 1);
+  return BUFF_OK;
+}
+
+int buff_server_start(buff_server *S) {
+  if (!S || S->running.load()) return BUFF_EINVAL;
+  S->stop.store(false);
+  S->running.store(true);
+  S->th = std::thread(loop, S);
+  return BUFF_OK;
+}
+
+int buff_server_submit(buff_server *S, const buff_request *reqs, uint32_t n) {
+  if (!S || (n && !reqs)) return BUFF_EINVAL;
+  const uint64_t t = now_ns();
+  std::lock_guard<std::mutex> lk(S->mu);
+  for (uint32_t i = 0; i < n; ++i) {
+    Req q;
+    memset(&q, 0, sizeof(q));
+    q.r = reqs[i];
+    q.submit_ns = t;
+    q.cls[0] = q.cls[1] = -1;
+    if (reqs[i].column >= S->store.size()) {
+      buff_completion c;
+      memset(&c, 0, sizeof(c));
+      c.tag = reqs[i].tag;
+      c.status = BUFF_EINVAL;
+      c.result.status = BUFF_EINVAL;
+      c.submit_ns = c.done_ns = t;
+      S->done.push_back(c);
+      S->n_done.fetch_add(1, std::memory_order_release);
+      continue;
+    }
+    q.col = S->store[reqs[i].column];
+    S->pending.push_back(q);
+  }
+  return BUFF_OK;
+}
+
+int buff_server_poll(buff_server *S, buff_completion *out, uint32_t cap, uint32_t *n) {
+  if (!S || !n || (cap && !out)) return BUFF_EINVAL;
+  std::lock_guard<std::mutex> lk(S->mu);
+  const uint32_t m = (uint32_t)(S->done.size() < cap ? S->done.size() : cap);
+  for (uint32_t i = 0; i < m; ++i) out[i] = S->done[i];
+  S->done.erase(S->done.begin(), S->done.begin() + m);
+  *n = m;
+  return BUFF_OK;
+}
+
+int buff_server_release(buff_server *S, const buff_completion *c) {
+  if (!S || !c) return BUFF_EINVAL;
+  // The loop thread owns the output allocator: the release travels to it as
+  // a request without a column, taken before any waiting request.
+  Req q;
+  memset(&q, 0, sizeof(q));
+  q.cls[0] = c->out_cls[0];
+  q.cls[1] = c->out_cls[1];
+  q.off[0] = c->out_off[0];
+  q.off[1] = c->out_off[1];
+  q.col = nullptr;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->pending.push_front(q);
+  return BUFF_OK;
+}
+
+int buff_server_stop(buff_server *S) {
+  if (!S) return BUFF_EINVAL;
+  if (S->running.load()) {
+    S->stop.store(true);
+    if (S->th.joinable()) S->th.join();
+    S->running.store(false);
+  }
+  return S->loop_status.load();
+}
+
+int buff_server_free(buff_server *S) {
+  if (!S) return BUFF_EINVAL;
+  buff_server_stop(S);
+  cudaDeviceSynchronize();
+  destroy_slots(S);
+  cudaFree(S->out.base);
+  delete S;
+  return BUFF_OK;
+}
+
+int buff_server_stats(buff_server *S, uint64_t *batches, uint64_t *requests,
+                      uint64_t *output_bytes_in_use) {
+  if (!S) return BUFF_EINVAL;
+  if (batches) *batches = S->batches;
+  if (requests) *requests = S->launched_reqs;
+  if (output_bytes_in_use) *output_bytes_in_use = S->out.used;
+  return BUFF_OK;
+}
+
+int buff_server_replay(buff_server *S, const buff_request *reqs, const uint64_t *arrival_ns,
+                       uint32_t n, uint64_t *latency_ns, buff_query_result *results,
+                       double *wall_s) {
+  if (!S || (n && (!reqs || !arrival_ns || !latency_ns))) return BUFF_EINVAL;
+  if (!S->running.load()) return BUFF_EINVAL;
+  std::vector<uint64_t> due(n);
+  const uint64_t t0 = now_ns() + 1000000;  // 1 ms to let the feeder start
+  for (uint32_t i = 0; i < n; ++i) due[i] = t0 + arrival_ns[i];
+  std::vector<buff_request> tagged(reqs, reqs + n);
+  for (uint32_t i = 0; i < n; ++i) tagged[i].tag = i;
+  std::thread feeder([&]() {
+    uint32_t i = 0;
+    while (i < n) {
+      const uint64_t t = now_ns();
+      uint32_t j = i;
+      while (j < n && due[j] <= t) ++j;
+      if (j > i) {
+        buff_server_submit(S, tagged.data() + i, j - i);
+        i = j;
+      } else {
+        std::this_thread::yield();
+      }
+    }
+  });
+  std::vector<buff_completion> buf(4096);
+  uint32_t got = 0;
+  uint64_t last = t0;
+  int rc = BUFF_OK;
+  while (got < n) {
+    uint32_t m = 0;
+    buff_server_poll(S, buf.data(), (uint32_t)buf.size(), &m);
+    for (uint32_t k = 0; k < m; ++k) {
+      const buff_completion &c = buf[k];
+      const uint64_t i = c.tag;
+      if (i >= n) continue;
+      latency_ns[i] = c.done_ns > due[i] ? c.done_ns - due[i] : 0;
+      if (results) results[i] = c.result;
+      if (c.status && !rc) rc = c.status;
+      if (c.done_ns > last) last = c.done_ns;
+      if (!S->cfg.auto_release) buff_server_release(S, &c);
+      ++got;
+    }
+    if (!m) std::this_thread::yield();
+    const int ls = S->loop_status.load();
+    if (ls != BUFF_OK) {
+      rc = ls;
+      break;
+    }
+  }
+  feeder.join();
+  if (wall_s) *wall_s = (double)(last - t0) / 1e9;
+  return rc;
+}
+
+}  // extern "C"

@@ -310,6 +310,71 @@ int buff_plan_free(buff_plan *plan);
 int buff_batch_autotune(const buff_query *queries, uint32_t nq, void *stream,
                         buff_batch_tune *best, float *best_ms);
 
+/* ---- serving (no counterpart in the reference) ---- */
+
+/* A store of resident columns and a request loop on one host thread.  With
+ * batched = 1 it batches the requests that are waiting whenever a batch slot
+ * is free (continuous batching: up to max_inflight batches run at once, each
+ * one persistent launch of up to max_batch queries); with batched = 0 every
+ * request runs alone through the single-column calls (one query per launch).
+ * Outputs (bitmaps, decoded values) come from a device arena of
+ * output_budget_bytes; a request waits until its outputs fit. */
+typedef struct buff_server_config {
+  uint64_t output_budget_bytes;
+  uint64_t store_budget_bytes; /* 0: no limit on resident columns */
+  uint32_t max_batch;
+  uint32_t max_inflight;
+  uint32_t batched;
+  uint32_t auto_release; /* 1: outputs are freed when the request completes */
+  buff_batch_tune tune;  /* tile_rows = 0: defaults */
+} buff_server_config;
+
+typedef struct buff_request {
+  uint32_t column;    /* store id from buff_server_add_column */
+  uint32_t ops;       /* BUFF_Q_* as in buff_query */
+  uint32_t precision; /* DECODE: 0 = full precision */
+  uint32_t reserved;
+  double pred;
+  uint64_t tag;       /* returned in the completion */
+} buff_request;
+
+typedef struct buff_completion {
+  uint64_t tag;
+  int32_t status;
+  uint32_t reserved;
+  buff_query_result result;
+  const uint32_t *words; /* device bitmap (auto_release = 0; NULL otherwise) */
+  const double *values;  /* device values (auto_release = 0; NULL otherwise) */
+  uint64_t submit_ns, done_ns; /* steady-clock times */
+  uint64_t out_off[2];         /* opaque: for buff_server_release */
+  int32_t out_cls[2];
+} buff_completion;
+
+typedef struct buff_server buff_server;
+int buff_server_create(const buff_server_config *cfg, buff_server **out);
+/* Adds a resident column (borrowed: it must outlive the server); BUFF_EFULL
+ * beyond store_budget_bytes.  Only before buff_server_start. */
+int buff_server_add_column(buff_server *srv, buff_col *col, uint32_t *id);
+int buff_server_start(buff_server *srv);
+/* Thread-safe. */
+int buff_server_submit(buff_server *srv, const buff_request *reqs, uint32_t n);
+/* Completed requests, oldest first. */
+int buff_server_poll(buff_server *srv, buff_completion *out, uint32_t cap, uint32_t *n);
+/* Returns a completion's outputs to the arena (auto_release = 0). */
+int buff_server_release(buff_server *srv, const buff_completion *c);
+int buff_server_stop(buff_server *srv);
+int buff_server_free(buff_server *srv);
+int buff_server_stats(buff_server *srv, uint64_t *batches, uint64_t *requests,
+                      uint64_t *output_bytes_in_use);
+/* Load replay for measurement: submits reqs[i] at arrival_ns[i] after the
+ * start (a feeder thread), waits for every completion and returns each
+ * request's latency from its arrival time to its completion, its result
+ * (results may be NULL) and the wall time from the first arrival to the last
+ * completion. */
+int buff_server_replay(buff_server *srv, const buff_request *reqs, const uint64_t *arrival_ns,
+                       uint32_t n, uint64_t *latency_ns, buff_query_result *results,
+                       double *wall_s);
+
 /* ---- allocation-free query ---- */
 
 /* Largest column (rows) that buff_range_filter_noalloc accepts. */
@@ -334,6 +399,10 @@ int buff_range_filter_noalloc(const buff_col *col, double pred, uint32_t *words,
 
 /* ---- diagnostics ---- */
 const char *buff_status_string(int status);
+/* Copies nbytes between any host and device addresses and waits for the
+ * stream: lets a caller that does not link the CUDA runtime read device
+ * outputs (bitmaps and values left on the device). */
+int buff_copy(void *dst, const void *src, uint64_t nbytes, void *stream);
 /* The last CUDA error code seen by this thread (0 if none). */
 int buff_last_cuda_error(void);
 /* Number of this library's kernels launched by this process so far. */

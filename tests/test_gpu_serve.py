@@ -1,0 +1,173 @@
+"""Serving loop on the GPU: every request's result is the same alone and in a
+mixed, overlapping stream, in batched and one-query-per-launch mode, and
+under an output budget that forces requests to wait."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _store(seed=11, ncols=24):
+    from buff_gb300.compress import Column
+
+    rng = np.random.default_rng(seed)
+    cols, data = [], []
+    for i in range(ncols):
+        n = int(np.exp(rng.uniform(np.log(1000), np.log(400_000))))
+        dec = int(rng.integers(2, 7))
+        x = np.round(np.cumsum(rng.normal(0, 0.3, n)) + rng.uniform(-50, 50), dec)
+        cols.append(Column.encode(x, 10 ** dec))
+        data.append(x)
+    return cols, data
+
+
+def _mix(data, nreq, seed):
+    from buff_gb300.capi import Q_DECODE, Q_EQUAL, Q_MAX, Q_RANGE, Q_SUM
+    from buff_gb300.serve import request
+
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for t in range(nreq):
+        c = int(rng.integers(0, len(data)))
+        x = data[c]
+        u = rng.uniform()
+        if u < 0.5:
+            ops, pred, prec = Q_RANGE, float(x[rng.integers(0, x.size)]), 0
+        elif u < 0.7:
+            ops, pred, prec = Q_EQUAL, float(x[rng.integers(0, x.size)]), 0
+        elif u < 0.9:
+            ops, pred, prec = (Q_SUM if rng.uniform() < 0.5 else Q_MAX), 0.0, 0
+        else:
+            ops, pred, prec = Q_DECODE, 0.0, int(rng.integers(0, 2))
+        reqs.append(request(c, ops, pred, prec, tag=t))
+    return reqs
+
+
+def _snapshot(c, req, n):
+    """Result and device outputs of one completion, copied to the host."""
+    from buff_gb300.capi import Q_DECODE, Q_EQUAL, Q_RANGE, copy_bytes
+
+    out = {"status": c.status, "count": c.result.count, "sum": c.result.sum,
+           "max": (c.result.max_code, c.result.max_value),
+           "parts": tuple(c.result.partials[: c.result.n_partials])}
+    if req.ops & (Q_RANGE | Q_EQUAL) and c.words:
+        out["words"] = copy_bytes(c.words, 4 * ((n + 31) // 32))
+    if req.ops & Q_DECODE and c.values:
+        out["values"] = copy_bytes(c.values, 8 * n)
+    return out
+
+
+def _run(server, reqs, data, one_at_a_time):
+    snaps = {}
+    if one_at_a_time:
+        for r in reqs:
+            server.submit([r])
+            (c,) = server.wait(1)
+            snaps[c.tag] = _snapshot(c, r, data[r.column].size)
+            server.release(c)
+    else:
+        server.submit(reqs)
+        done = server.wait(len(reqs))
+        for c in done:
+            r = reqs[c.tag]
+            snaps[c.tag] = _snapshot(c, r, data[r.column].size)
+            server.release(c)
+    return snaps
+
+
+@pytest.mark.parametrize("batched", [True, False])
+def test_alone_equals_mixed(gpu, batched):
+    from buff_gb300.serve import Server
+
+    cols, data = _store()
+    reqs = _mix(data, 300, 5)
+    s = Server(1 << 30, max_batch=64, max_inflight=3, batched=batched, auto_release=False)
+    for c in cols:
+        s.add_column(c)
+    s.start()
+    alone = _run(s, reqs, data, True)
+    mixed = _run(s, reqs, data, False)
+    s.stop()
+    s.free()
+    assert alone.keys() == mixed.keys() == set(range(len(reqs)))
+    for t in range(len(reqs)):
+        assert alone[t] == mixed[t], t
+
+
+def test_results_match_single_column(gpu):
+    from buff_gb300.capi import Q_DECODE, Q_EQUAL, Q_MAX, Q_RANGE, Q_SUM
+    from buff_gb300.serve import Server
+
+    cols, data = _store(seed=12, ncols=10)
+    reqs = _mix(data, 120, 6)
+    s = Server(1 << 30, max_batch=32, max_inflight=2, batched=True, auto_release=False)
+    for c in cols:
+        s.add_column(c)
+    s.start()
+    got = _run(s, reqs, data, False)
+    s.stop()
+    s.free()
+    for t, r in enumerate(reqs):
+        col, n, g = cols[r.column], data[r.column].size, got[t]
+        assert g["status"] == 0
+        if r.ops & (Q_RANGE | Q_EQUAL):
+            ref = col.range_filter(r.pred) if r.ops & Q_RANGE else col.equal_filter(r.pred)
+            assert g["count"] == ref.count
+            assert g["words"] == ref.words.astype("<u4").tobytes()
+        if r.ops & Q_SUM:
+            assert g["sum"] == col.sum().sum
+        if r.ops & Q_MAX:
+            m = col.max()
+            assert g["max"] == (m.code, m.value)
+        if r.ops & Q_DECODE:
+            ref = col.decode_at_precision(r.precision) if r.precision else col.decode()
+            assert g["values"] == np.ascontiguousarray(ref).tobytes()
+
+
+def test_budget_forces_waits_and_efull(gpu):
+    from buff_gb300.capi import Q_DECODE, Q_SUM
+    from buff_gb300.compress import Column
+    from buff_gb300.serve import Server, request
+
+    rng = np.random.default_rng(2)
+    x = np.round(np.cumsum(rng.normal(0, 1, 200_000)), 2)
+    col = Column.encode(x, 100)
+    # budget for two decodes at a time: 24 decodes must queue for memory
+    s = Server(2 * (1 << 21), max_batch=8, max_inflight=4, batched=True, auto_release=True)
+    cid = s.add_column(col)
+    s.start()
+    reqs = [request(cid, Q_DECODE, tag=i) for i in range(24)] + \
+        [request(cid, Q_SUM, tag=24)]
+    s.submit(reqs)
+    done = s.wait(len(reqs))
+    assert sorted(c.tag for c in done) == list(range(25))
+    assert all(c.status == 0 for c in done)
+    assert s.stats()["output_bytes_in_use"] == 0
+    s.stop()
+    s.free()
+    tiny = Server(1 << 20, batched=True)
+    cid = tiny.add_column(col)
+    tiny.start()
+    tiny.submit([request(cid, Q_DECODE, tag=7)])
+    (c,) = tiny.wait(1)
+    assert c.status == 8  # BUFF_EFULL: the outputs exceed the whole budget
+    tiny.stop()
+    tiny.free()
+
+
+def test_replay_reports_latency(gpu):
+    from buff_gb300.serve import Server
+
+    cols, data = _store(seed=13, ncols=8)
+    reqs = _mix(data, 2000, 9)
+    arrivals = np.cumsum(np.random.default_rng(1).exponential(20_000, len(reqs))).astype(np.uint64)
+    for batched in (True, False):
+        s = Server(1 << 30, max_batch=256, max_inflight=4, batched=batched)
+        for c in cols:
+            s.add_column(c)
+        s.start()
+        lat, res, wall = s.replay(reqs, arrivals)
+        s.stop()
+        s.free()
+        assert lat.size == len(reqs) and (lat > 0).all() and wall > 0
+        assert all(r.status == 0 for r in res)
