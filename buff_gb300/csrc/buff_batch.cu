@@ -329,6 +329,7 @@ __device__ __forceinline__ uint32_t pick8(const uint32_t (&tw)[8], uint32_t i) {
   return v;
 }
 
+// 32 slice bytes (rows row0..row0+31) with streaming loads.
 __device__ __forceinline__ Bytes32 ld32(const uint8_t *p) {
   const uint4 a = __ldcs(reinterpret_cast<const uint4 *>(p));
   const uint4 b = __ldcs(reinterpret_cast<const uint4 *>(p + 16));
@@ -344,88 +345,127 @@ __device__ __forceinline__ Bytes32 ld32(const uint8_t *p) {
   return v;
 }
 
-// Filters and sums over rows [r0, r1) of one query; lane L owns rows
-// row0 = step + 32L .. +31 of each 1024-row step.
-template <int STAGE>
+// Bits at multiples of r in a 64-bit word (r = 1..7).
+__device__ __forceinline__ unsigned long long every_r(uint32_t r) {
+  unsigned long long m = 0;
+  for (uint32_t j = 0; j < 64; j += r) m |= 1ull << j;
+  return m;
+}
+
+// Sum of the 16 r-bit fields packed LSB-first in (lo, hi): every set bit b
+// of the 16r-bit stream adds 2^(b mod r).  pat = every_r(r); the phase of
+// the hi word's bit 0 is 64 mod r.
+__device__ __forceinline__ uint32_t fields16_sum(unsigned long long lo, unsigned long long hi,
+                                                 uint32_t r, unsigned long long pat) {
+  if (r == 1) return __popcll(lo) + __popcll(hi);
+  const uint32_t ph = 64 % r;
+  uint32_t acc = 0;
+  for (uint32_t p = 0; p < r; ++p) {
+    const uint32_t q = (p + r - ph) % r;  // hi bit j has stream bit 64 + j == p (mod r)
+    acc += (uint32_t)(__popcll(lo & (pat << p)) + __popcll(hi & (pat << q))) << p;
+  }
+  return acc;
+}
+
+// MSBs of the bytes of four words -> 16 row-ordered bits.
+__device__ __forceinline__ uint32_t gather16(const uint32_t *m) {
+  return __byte_perm(msb8(m[0], m[1]), msb8(m[2], m[3]), 0x0040);
+}
+
+__device__ __forceinline__ uint32_t w4(const uint4 &v, int i) {
+  return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+
+// Filters and sums over rows [r0, r1) of one query.  Lane L owns the 16
+// rows row0 = step + 16L .. +15 of each 512-row step; STAGE steps are
+// loaded together (every slice when summing, slice 0 otherwise).  Lane
+// pairs combine their 16-row results into one bitmap word.
+template <int STAGE, bool DO_F, bool DO_S>
 __device__ __forceinline__ void tile_filter_sum(const BQ &q, uint32_t r0, uint32_t r1,
                                                 uint32_t lane) {
-  const bool do_f = q.ops & (kOpRange | kOpEqual);
-  const bool do_s = q.ops & kOpSum;
+  constexpr bool do_f = DO_F;
+  constexpr bool do_s = DO_S;
   const bool is_range = q.ops & kOpRange;
+  const bool cmp = do_f && q.fill == 0;
+  const uint32_t nload = do_s ? (q.k < 4 ? q.k : 4u) : (q.k ? 1u : 0u);
+  const unsigned long long pat = q.r > 1 ? every_r(q.r) : 0ull;
   uint32_t sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  unsigned long long tacc = 0;
+  uint32_t tacc = 0;
   uint32_t cnt = 0;
-  const uint32_t rmask = q.r ? ((1u << q.r) - 1u) : 0u;
-  for (uint32_t sb = r0; sb < r1; sb += 1024 * STAGE) {
-    Bytes32 first[STAGE];
+  for (uint32_t sb = r0; sb < r1; sb += 512 * STAGE) {
+    uint4 v[STAGE][4];
 #pragma unroll
-    for (int u = 0; u < STAGE; ++u) {  // slice 0 of STAGE steps in flight
-      const uint32_t row0 = sb + u * 1024 + lane * 32;
-      if (q.k && row0 < r1) first[u] = ld32(q.slices + row0);
+    for (int u = 0; u < STAGE; ++u) {
+      const uint32_t row0 = sb + u * 512 + lane * 16;
+#pragma unroll
+      for (uint32_t j = 0; j < 4; ++j)
+        if (j < nload && row0 < r1) v[u][j] = __ldcs(reinterpret_cast<const uint4 *>(
+                                          q.slices + j * q.stride + row0));
     }
 #pragma unroll
     for (int u = 0; u < STAGE; ++u) {
-      const uint32_t row0 = sb + u * 1024 + lane * 32;
-      if (row0 >= r1) continue;
-      const uint32_t left = q.n - row0;
-      const uint32_t valid = left >= 32 ? 0xFFFFFFFFu : ((1u << left) - 1u);
-      uint32_t eq = valid, gt = 0;
-      if (row0 + 32 > q.full_rows)
-        eq &= row0 >= q.full_rows ? 0u : ((1u << (q.full_rows - row0)) - 1u);
-      const bool cmp = do_f && q.fill == 0;
+      const uint32_t row0 = sb + u * 512 + lane * 16;
+      const bool act = row0 < r1;
+      uint32_t valid = 0, eq = 0, gt = 0;
+      if (act) {
+        const uint32_t left = q.n - row0;
+        valid = left >= 16 ? 0xFFFFu : ((1u << left) - 1u);
+        eq = valid;
+        if (row0 + 16 > q.full_rows)
+          eq &= row0 >= q.full_rows ? 0u : ((1u << (q.full_rows - row0)) - 1u);
 #pragma unroll
-      for (uint32_t j = 0; j < 8; ++j) {
-        if (j >= q.k) break;
-        const bool need_f = cmp && j < q.k_used && eq;
-        if (!do_s && !need_f) break;
-        const Bytes32 b = j == 0 ? first[u] : ld32(q.slices + j * q.stride + row0);
-        if (do_s) {
-#pragma unroll
-          for (int w = 0; w < 8; ++w) sacc[j] = __dp4a(b.w[w] ^ H, 0x01010101u, sacc[j]);
-        }
-        if (need_f) {
-          const ByteTarget t = make_target(q.tbyte[j]);
-          uint32_t g[8], e[8];
-#pragma unroll
-          for (int w = 0; w < 8; ++w) cmp4(b.w[w], t, g[w], e[w]);
-          gt |= eq & gather32(g);
-          eq &= gather32(e);
-        }
-      }
-      if (q.r) {
-        const bool need_tf = cmp && q.r_used && eq;
-        if (do_s || need_tf) {
-          const uint32_t *tp =
-              reinterpret_cast<const uint32_t *>(q.tail + (size_t)(row0 >> 5) * 4 * q.r);
-          uint32_t tw[8];
-#pragma unroll
-          for (uint32_t i = 0; i < 7; ++i) tw[i] = i < q.r ? __ldcs(tp + i) : 0u;
-          tw[7] = 0;
+        for (uint32_t j = 0; j < 8; ++j) {
+          if (j >= q.k) break;
+          const bool need_f = cmp && j < q.k_used && eq;
+          if (!do_s && !need_f) break;
+          const uint4 w = j < nload ? v[u][j & 3]
+                                    : __ldcs(reinterpret_cast<const uint4 *>(
+                                          q.slices + j * q.stride + row0));
           if (do_s) {
-            // rows past n hold zero tail bits
-#pragma unroll
-            for (uint32_t i = 0; i < 7; ++i)
-              if (i < q.r) tacc += wpopc(tw[i], 32 * i, q.r);
+            sacc[j] = __dp4a(w.x ^ H, 0x01010101u, sacc[j]);
+            sacc[j] = __dp4a(w.y ^ H, 0x01010101u, sacc[j]);
+            sacc[j] = __dp4a(w.z ^ H, 0x01010101u, sacc[j]);
+            sacc[j] = __dp4a(w.w ^ H, 0x01010101u, sacc[j]);
           }
-          if (need_tf) {
-            uint32_t gtt = 0, eqt = 0, b = eq;
-            while (b) {
-              const uint32_t i = __ffs(b) - 1;
-              b &= b - 1;
-              const uint32_t bit = i * q.r, wi = bit >> 5;
-              const uint32_t f = __funnelshift_r(pick8(tw, wi), pick8(tw, wi + 1), bit & 31) & rmask;
-              gtt |= (uint32_t)(f > q.ttail) << i;
-              eqt |= (uint32_t)(f == q.ttail) << i;
+          if (need_f) {
+            const ByteTarget t = make_target(q.tbyte[j]);
+            uint32_t g[4], e[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) cmp4(w4(w, i), t, g[i], e[i]);
+            gt |= eq & gather16(g);
+            eq &= gather16(e);
+          }
+        }
+        if (q.r) {
+          const bool need_tf = cmp && q.r_used && eq;
+          if (do_s || need_tf) {
+            unsigned long long lo, hi;
+            load_tail16(q.tail, row0 >> 4, q.r, lo, hi);
+            if (do_s) tacc += fields16_sum(lo, hi, q.r, pat);  // rows past n hold zeros
+            if (need_tf) {
+              uint32_t gtt = 0, eqt = 0, b = eq;
+              while (b) {
+                const uint32_t i = __ffs(b) - 1;
+                b &= b - 1;
+                const uint32_t f = field16(lo, hi, i, q.r);
+                gtt |= (uint32_t)(f > q.ttail) << i;
+                eqt |= (uint32_t)(f == q.ttail) << i;
+              }
+              gt |= eq & gtt;
+              eq &= eqt;
             }
-            gt |= eq & gtt;
-            eq &= eqt;
           }
         }
       }
       if (do_f) {
-        const uint32_t res = q.fill == 1 ? valid : q.fill == 2 ? 0u : (is_range ? gt : eq);
-        q.words[row0 >> 5] = res;
-        cnt += __popc(res);
+        const uint32_t res = !act ? 0u : q.fill == 1 ? valid : q.fill == 2 ? 0u
+                                                      : (is_range ? gt : eq);
+        const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
+        if (act && !(lane & 1)) {
+          const uint32_t word = res | (hi16 << 16);
+          q.words[row0 >> 5] = word;
+          cnt += __popc(word);
+        }
       }
     }
   }
@@ -447,77 +487,246 @@ __device__ __forceinline__ void tile_filter_sum(const BQ &q, uint32_t r0, uint32
   }
 }
 
-__device__ __forceinline__ uint32_t tail_field(const uint8_t *tail, uint32_t row, uint32_t bits) {
-  const unsigned long long bit = (unsigned long long)row * bits;
-  const uint32_t b0 = __ldg(tail + (bit >> 3));
-  const uint32_t b1 = ((bit & 7) + bits > 8) ? __ldg(tail + (bit >> 3) + 1) : 0u;
-  return ((b0 | (b1 << 8)) >> (bit & 7)) & ((1u << bits) - 1u);
+// Largest byte of a word.
+__device__ __forceinline__ uint32_t max4(uint32_t w) {
+  const uint32_t a = __vmaxu4(w, w >> 16);
+  return max(a & 0xFFu, (a >> 8) & 0xFFu);
 }
 
-// Max and decode over rows [r0, r1): lane L owns rows r0 + 32m + L.
-__device__ __forceinline__ void tile_max_decode(const BQ &q, uint32_t r0, uint32_t r1,
-                                                uint32_t lane) {
-  const bool do_m = q.ops & kOpMax;
-  const bool do_d = q.ops & kOpDecode;
-  unsigned long long mx = 0;
-  for (uint32_t b0 = r0; b0 < r1; b0 += 32) {
-    const uint32_t row = b0 + lane;
-    if (row >= r1) break;
-    uint32_t by[8];
+// Bytes equal to b (b replicated in every byte) -> their MSBs.
+__device__ __forceinline__ uint32_t eqb4(uint32_t w, uint32_t bb) {
+  const uint32_t x = w ^ bb;  // zero bytes where equal
+  return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
+}
+
+// byte_fixed_max over rows [r0, r1) (split_double.rs:3919-4105 computes the
+// same maximum slice by slice).  One pass over slice 0, 512 rows per warp
+// step: the step's largest top byte M is compared with the tile's best code
+// so far, and only a step that can reach it refines its candidate rows
+// (top byte == M) through the later slices and the tail, each level taking
+// the warp-wide largest byte among the remaining candidates.
+template <int STAGE>
+__device__ __forceinline__ void tile_max(const BQ &q, uint32_t r0, uint32_t r1, uint32_t lane) {
+  const uint32_t fl = q.k ? 8 * q.k + q.r : q.r;
+  unsigned long long best = 0;
+  bool have = false;
+  for (uint32_t sb = r0; sb < r1; sb += 512 * STAGE) {
+    uint4 v[STAGE];
 #pragma unroll
-    for (uint32_t j = 0; j < 8; ++j)
-      by[j] = j < q.k ? (uint32_t)(__ldcs(q.slices + j * q.stride + row) ^ 0x80u) : 0u;
-    if (do_m) {
-      unsigned long long c = 0;
+    for (int u = 0; u < STAGE; ++u) {
+      const uint32_t row0 = sb + u * 512 + lane * 16;
+      if (q.k && row0 < r1)
+        v[u] = __ldcs(reinterpret_cast<const uint4 *>(q.slices + row0));
+      else
+        v[u] = make_uint4(H, H, H, H);  // flipped zero bytes
+    }
+#pragma unroll
+    for (int u = 0; u < STAGE; ++u) {
+      const uint32_t step = sb + u * 512;
+      if (step >= r1) break;  // warp-uniform
+      const uint32_t row0 = step + lane * 16;
+      const bool act = row0 < r1;
+      unsigned long long code;
+      uint32_t cand;
+      if (q.k) {
+        const uint32_t w0 = v[u].x ^ H, w1 = v[u].y ^ H, w2 = v[u].z ^ H, w3 = v[u].w ^ H;
+        const uint32_t m = max4(__vmaxu4(__vmaxu4(w0, w1), __vmaxu4(w2, w3)));
+        const uint32_t M = __reduce_max_sync(0xFFFFFFFFu, m);
+        if (have && M < (uint32_t)(best >> (fl - 8))) continue;  // cannot reach the best
+        const uint32_t bb = M * 0x01010101u;
+        uint32_t e[4] = {eqb4(w0, bb), eqb4(w1, bb), eqb4(w2, bb), eqb4(w3, bb)};
+        cand = act ? gather16(e) : 0u;
+        code = M;
+        for (uint32_t j = 1; j < q.k; ++j) {
+          uint32_t mj = 0;
+          uint4 b = make_uint4(0, 0, 0, 0);
+          if (cand) {
+            b = __ldcs(reinterpret_cast<const uint4 *>(q.slices + j * q.stride + row0));
+            const uint32_t bw[4] = {b.x ^ H, b.y ^ H, b.z ^ H, b.w ^ H};
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              if (cand >> i & 1u) mj = max(mj, (bw[i >> 2] >> (8 * (i & 3))) & 0xFFu);
+          }
+          const uint32_t Mj = __reduce_max_sync(0xFFFFFFFFu, mj);
+          if (cand) {
+            const uint32_t bbj = Mj * 0x01010101u;
+            uint32_t ej[4] = {eqb4(b.x ^ H, bbj), eqb4(b.y ^ H, bbj), eqb4(b.z ^ H, bbj),
+                              eqb4(b.w ^ H, bbj)};
+            cand &= gather16(ej);
+          }
+          code = (code << 8) | Mj;
+        }
+      } else {
+        cand = act ? ((q.n - row0 >= 16) ? 0xFFFFu : ((1u << (q.n - row0)) - 1u)) : 0u;
+        code = 0;
+      }
+      if (q.r) {
+        uint32_t mt = 0;
+        if (cand) {
+          unsigned long long lo, hi;
+          load_tail16(q.tail, row0 >> 4, q.r, lo, hi);
+          uint32_t b = cand;
+          while (b) {
+            const uint32_t i = __ffs(b) - 1;
+            b &= b - 1;
+            mt = max(mt, field16(lo, hi, i, q.r));
+          }
+        }
+        code = (code << q.r) | __reduce_max_sync(0xFFFFFFFFu, mt);
+      }
+      if (!have || code > best) best = code;
+      have = true;
+    }
+  }
+  if (lane == 0 && have) atomicMax(q.acc + 10, best);
+}
+
+// Decode over rows [r0, r1), 128-row groups: lane L owns rows 4L..4L+3 of
+// each group, so slice bytes come in 4-byte loads covering 128 contiguous
+// bytes per warp and values leave as two 16-byte stores per lane; the
+// group's dts-bit tail fields (16 dts bytes) are loaded by the first 4 dts
+// lanes and handed out with shuffles.  STAGE groups are loaded together.
+template <int STAGE>
+__device__ __forceinline__ void tile_decode(const BQ &q, uint32_t r0, uint32_t r1,
+                                            uint32_t lane) {
+  const uint32_t db = q.dts;
+  const uint32_t dmask = db ? ((1u << db) - 1u) : 0u;
+  for (uint32_t g = r0; g < r1; g += 128 * STAGE) {
+    uint32_t sw[STAGE][8];
+    uint32_t dw[STAGE];
+#pragma unroll
+    for (int u = 0; u < STAGE; ++u) {
+      const uint32_t base = g + 128 * u;
+      dw[u] = 0;
+      if (base >= r1) continue;
+      const uint32_t row = base + 4 * lane;
 #pragma unroll
       for (uint32_t j = 0; j < 8; ++j)
-        if (j < q.k) c = (c << 8) | by[j];
-      if (q.r) c = (c << q.r) | tail_field(q.tail, row, q.r);
-      mx = c > mx ? c : mx;
+        if (j < q.dks)
+          sw[u][j] = __ldcs(reinterpret_cast<const uint32_t *>(q.slices + j * q.stride + row));
+      if (db && lane < 4 * db)
+        dw[u] = __ldcs(reinterpret_cast<const uint32_t *>(q.tail + (size_t)(base >> 7) * 16 * db) +
+                       lane);
     }
-    if (do_d) {
-      unsigned long long c = 0;
 #pragma unroll
-      for (uint32_t j = 0; j < 8; ++j)
-        if (j < q.dks) c = (c << 8) | by[j];
-      if (q.dts) c = (c << q.dts) | tail_field(q.tail, row, q.dts);
-      __stcs(q.values + row,
-             i64_to_f64_scaled((long long)((unsigned long long)q.base + (c & q.keep)), q.dlen));
+    for (int u = 0; u < STAGE; ++u) {
+      const uint32_t base = g + 128 * u;
+      if (base >= r1) break;  // warp-uniform
+      const uint32_t row = base + 4 * lane;
+      uint32_t f = 0;
+      if (db) {
+        const uint32_t bit = 4 * lane * db, wi = bit >> 5;
+        const uint32_t w0 = __shfl_sync(0xFFFFFFFFu, dw[u], wi);
+        const uint32_t w1 = __shfl_sync(0xFFFFFFFFu, dw[u], (wi + 1) & 31);
+        f = __funnelshift_r(w0, w1, bit & 31);
+      }
+      double val[4];
+#pragma unroll
+      for (uint32_t i = 0; i < 4; ++i) {
+        unsigned long long d = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < 8; ++j) {
+          if (j >= q.dks) break;
+          d = (d << 8) | (((sw[u][j] >> (8 * i)) & 0xFFu) ^ 0x80u);
+        }
+        if (db) d = (d << db) | ((f >> (i * db)) & dmask);
+        val[i] = i64_to_f64_scaled((long long)((unsigned long long)q.base + (d & q.keep)), q.dlen);
+      }
+      if (row + 4 <= r1) {
+        __stcs(reinterpret_cast<double2 *>(q.values + row), make_double2(val[0], val[1]));
+        __stcs(reinterpret_cast<double2 *>(q.values + row + 2), make_double2(val[2], val[3]));
+      } else {
+#pragma unroll
+        for (uint32_t i = 0; i < 4; ++i)
+          if (row + i < r1) q.values[row + i] = val[i];
+      }
     }
   }
-  if (do_m) {
-    mx = warp_max_ull(mx);
-    if (lane == 0) atomicMax(q.acc + 10, mx);
-  }
 }
 
+// Filter only: lane L owns the 32 rows row0 = step + 32L .. +31 (one bitmap
+// word) of each 1024-row step; STAGE steps of slice 0 are loaded together,
+// later slices and the tail only for words that still hold candidates.
 template <int STAGE>
-__global__ void __launch_bounds__(kBT) k_batch(const BQ *__restrict__ qs,
-                                               const uint2 *__restrict__ items, uint32_t nitems,
-                                               uint32_t tile, unsigned int *counter) {
-  const uint32_t lane = threadIdx.x & 31;
-  for (;;) {
-    uint32_t it = 0;
-    if (lane == 0) it = atomicAdd(counter, 1u);
-    it = __shfl_sync(0xFFFFFFFFu, it, 0);
-    if (it >= nitems) return;
-    const uint2 item = items[it];
-    const BQ q = qs[item.x];
-    const uint32_t r0 = item.y * tile;
-    const uint32_t r1 = min(q.n, r0 + tile);
-    if (q.ops & (kOpRange | kOpEqual | kOpSum)) tile_filter_sum<STAGE>(q, r0, r1, lane);
-    if (q.ops & (kOpMax | kOpDecode)) tile_max_decode(q, r0, r1, lane);
+__device__ __forceinline__ void tile_filter32(const BQ &q, uint32_t r0, uint32_t r1,
+                                              uint32_t lane) {
+  const bool is_range = q.ops & kOpRange;
+  const bool cmp = q.fill == 0;
+  const uint32_t rmask = q.r ? ((1u << q.r) - 1u) : 0u;
+  uint32_t cnt = 0;
+  for (uint32_t sb = r0; sb < r1; sb += 1024 * STAGE) {
+    Bytes32 v[STAGE];
+#pragma unroll
+    for (int u = 0; u < STAGE; ++u) {
+      const uint32_t row0 = sb + u * 1024 + lane * 32;
+      if (cmp && q.k_used && row0 < r1) v[u] = ld32(q.slices + row0);
+    }
+#pragma unroll
+    for (int u = 0; u < STAGE; ++u) {
+      const uint32_t row0 = sb + u * 1024 + lane * 32;
+      if (row0 >= r1) continue;
+      const uint32_t left = q.n - row0;
+      const uint32_t valid = left >= 32 ? 0xFFFFFFFFu : ((1u << left) - 1u);
+      uint32_t res;
+      if (!cmp) {
+        res = q.fill == 1 ? valid : 0u;
+      } else {
+        uint32_t eq = valid, gt = 0;
+        if (row0 + 32 > q.full_rows)
+          eq &= row0 >= q.full_rows ? 0u : ((1u << (q.full_rows - row0)) - 1u);
+        for (uint32_t j = 0; j < q.k_used && eq; ++j) {
+          const Bytes32 b = j == 0 ? v[u] : ld32(q.slices + j * q.stride + row0);
+          const ByteTarget t = make_target(q.tbyte[j]);
+          uint32_t g[8], e[8];
+#pragma unroll
+          for (int w = 0; w < 8; ++w) cmp4(b.w[w], t, g[w], e[w]);
+          gt |= eq & gather32(g);
+          eq &= gather32(e);
+        }
+        if (q.r_used && eq) {
+          const uint32_t *tp =
+              reinterpret_cast<const uint32_t *>(q.tail + (size_t)(row0 >> 5) * 4 * q.r);
+          uint32_t tw[8];
+#pragma unroll
+          for (uint32_t i = 0; i < 7; ++i) tw[i] = i < q.r ? __ldcs(tp + i) : 0u;
+          tw[7] = 0;
+          uint32_t gtt = 0, eqt = 0, bb = eq;
+          while (bb) {
+            const uint32_t i = __ffs(bb) - 1;
+            bb &= bb - 1;
+            const uint32_t bit = i * q.r, wi = bit >> 5;
+            const uint32_t f =
+                __funnelshift_r(pick8(tw, wi), pick8(tw, wi + 1), bit & 31) & rmask;
+            gtt |= (uint32_t)(f > q.ttail) << i;
+            eqt |= (uint32_t)(f == q.ttail) << i;
+          }
+          gt |= eq & gtt;
+          eq &= eqt;
+        }
+        res = is_range ? gt : eq;
+      }
+      q.words[row0 >> 5] = res;
+      cnt += __popc(res);
+    }
   }
+  const unsigned long long sc = warp_sum_ull(cnt);
+  if (lane == 0 && sc) atomicAdd(q.acc, sc);
 }
 
-// The same work with items numbered per query: query q owns items
-// [prefix[q], prefix[q+1]) (its row tiles), found by binary search, so a
-// batch needs no item list.
-template <int STAGE>
-__global__ void __launch_bounds__(kBT) k_batch_pfx(const BQ *__restrict__ qs,
-                                                   const uint32_t *__restrict__ prefix,
-                                                   uint32_t nq, uint32_t nitems, uint32_t tile,
-                                                   unsigned int *counter) {
+// Query classes: each runs in its own persistent launch, compiled for its
+// ops only.  A query with a filter and a sum is one FS item; a query with a
+// sum (without a filter) and a max or decode is an S item and an MD item.
+enum { kClsF = 0, kClsFS = 1, kClsS = 2, kClsMD = 3, kClasses = 4 };
+
+// Persistent worker of one class: warp-granular items; the batch's class
+// list holds query indices qidx[] and the exclusive prefix of their tile
+// counts, so item i belongs to the query found by binary search.
+template <int CLS, int STAGE>
+__global__ void __launch_bounds__(kBT) k_bq(const BQ *__restrict__ qs,
+                                            const uint32_t *__restrict__ qidx,
+                                            const uint32_t *__restrict__ prefix, uint32_t nq,
+                                            uint32_t nitems, uint32_t tile,
+                                            unsigned int *counter) {
   const uint32_t lane = threadIdx.x & 31;
   for (;;) {
     uint32_t it = 0;
@@ -532,11 +741,31 @@ __global__ void __launch_bounds__(kBT) k_batch_pfx(const BQ *__restrict__ qs,
       else
         hi = mid;
     }
-    const BQ q = qs[lo];
+    const BQ &q = qs[__ldg(qidx + lo)];
     const uint32_t r0 = (it - __ldg(prefix + lo)) * tile;
     const uint32_t r1 = min(q.n, r0 + tile);
-    if (q.ops & (kOpRange | kOpEqual | kOpSum)) tile_filter_sum<STAGE>(q, r0, r1, lane);
-    if (q.ops & (kOpMax | kOpDecode)) tile_max_decode(q, r0, r1, lane);
+    if (CLS == kClsF) tile_filter32<STAGE>(q, r0, r1, lane);
+    if (CLS == kClsFS) tile_filter_sum<STAGE, true, true>(q, r0, r1, lane);
+    if (CLS == kClsS) tile_filter_sum<STAGE, false, true>(q, r0, r1, lane);
+    if (CLS == kClsMD) {
+      if (q.ops & kOpMax) tile_max<STAGE>(q, r0, r1, lane);
+      if (q.ops & kOpDecode) tile_decode<STAGE>(q, r0, r1, lane);
+    }
+  }
+}
+
+template <int CLS>
+const void *bq_fn(int stage) {
+  return stage == 4 ? (const void *)k_bq<CLS, 4>
+                    : stage == 2 ? (const void *)k_bq<CLS, 2> : (const void *)k_bq<CLS, 1>;
+}
+
+const void *class_fn(int cls, int stage) {
+  switch (cls) {
+    case kClsF: return bq_fn<kClsF>(stage);
+    case kClsFS: return bq_fn<kClsFS>(stage);
+    case kClsS: return bq_fn<kClsS>(stage);
+    default: return bq_fn<kClsMD>(stage);
   }
 }
 
@@ -557,15 +786,57 @@ int batch_plan_query(const buff_query &q, unsigned long long *acc, void *desc) {
   return plan_query(q, acc, static_cast<BQ *>(desc));
 }
 
-uint32_t batch_tiles(const void *desc, uint32_t tile) {
-  const BQ *q = static_cast<const BQ *>(desc);
-  return (q->n + tile - 1) / tile;
+size_t batch_sched_words(uint32_t nq) { return 4 * (size_t)nq + 2 * kClasses; }
+
+// Class lists of a batch: for class c, qidx (query indices) then the
+// exclusive prefix of their tile counts, packed in `buf`.
+void batch_schedule(const void *h_desc, uint32_t nq, uint32_t tile, uint32_t *buf,
+                    BatchSched *sc) {
+  const BQ *qs = static_cast<const BQ *>(h_desc);
+  uint32_t nc[kClasses] = {0, 0, 0, 0};
+  auto classes = [](const BQ &q, int *out) {
+    int m = 0;
+    if (q.n == 0) return 0;
+    if (q.ops & (kOpRange | kOpEqual))
+      out[m++] = (q.ops & kOpSum) ? kClsFS : kClsF;
+    else if (q.ops & kOpSum)
+      out[m++] = kClsS;
+    if (q.ops & (kOpMax | kOpDecode)) out[m++] = kClsMD;
+    return m;
+  };
+  for (uint32_t i = 0; i < nq; ++i) {
+    int cl[2];
+    const int m = classes(qs[i], cl);
+    for (int j = 0; j < m; ++j) nc[cl[j]]++;
+  }
+  uint32_t off = 0;
+  for (int c = 0; c < kClasses; ++c) {
+    sc->n[c] = nc[c];
+    sc->qidx_off[c] = off;
+    sc->prefix_off[c] = off + nc[c];
+    sc->items[c] = 0;
+    off += 2 * nc[c] + 1;
+  }
+  uint32_t fill[kClasses] = {0, 0, 0, 0};
+  for (uint32_t i = 0; i < nq; ++i) {
+    int cl[2];
+    const int m = classes(qs[i], cl);
+    const uint32_t t = (qs[i].n + tile - 1) / tile;
+    for (int j = 0; j < m; ++j) {
+      const int c = cl[j];
+      buf[sc->qidx_off[c] + fill[c]] = i;
+      buf[sc->prefix_off[c] + fill[c]] = sc->items[c];
+      fill[c]++;
+      sc->items[c] += t;
+    }
+  }
+  for (int c = 0; c < kClasses; ++c) buf[sc->prefix_off[c] + nc[c]] = sc->items[c];
+  sc->words = off;
 }
 
-int batch_grid(const buff_batch_tune &t, uint32_t nitems) {
+int class_grid(int cls, const buff_batch_tune &t, uint32_t nitems) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, t.stage == 2 ? (const void *)k_batch_pfx<2> : (const void *)k_batch_pfx<1>, kBT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, class_fn(cls, t.stage), kBT, 0);
   if (per_sm < 1) per_sm = 1;
   const int bps = (int)t.blocks_per_sm < per_sm ? (int)t.blocks_per_sm : per_sm;
   int grid = bps * dev_sms();
@@ -574,18 +845,41 @@ int batch_grid(const buff_batch_tune &t, uint32_t nitems) {
   return grid;
 }
 
-cudaError_t batch_launch_prefix(const void *d_desc, const uint32_t *d_prefix, uint32_t nq,
-                                uint32_t nitems, const buff_batch_tune &t, unsigned int *counter,
-                                cudaStream_t s) {
-  if (!nitems) return cudaSuccess;
-  const int grid = batch_grid(t, nitems);
+// One persistent launch per non-empty class, in order on `s`; counters
+// holds kClasses zeroed work counters.
+cudaError_t batch_launch(const void *d_desc, const uint32_t *d_buf, const BatchSched &sc,
+                         const buff_batch_tune &t, unsigned int *counters, cudaStream_t s) {
   const BQ *qs = static_cast<const BQ *>(d_desc);
-  if (t.stage == 2)
-    k_batch_pfx<2><<<grid, kBT, 0, s>>>(qs, d_prefix, nq, nitems, t.tile_rows, counter);
-  else
-    k_batch_pfx<1><<<grid, kBT, 0, s>>>(qs, d_prefix, nq, nitems, t.tile_rows, counter);
-  count_launch();
-  return cudaGetLastError();
+  const int order[kClasses] = {kClsMD, kClsFS, kClsS, kClsF};
+  for (int oi = 0; oi < kClasses; ++oi) {
+    const int c = order[oi];
+    if (!sc.items[c]) continue;
+    const int grid = class_grid(c, t, sc.items[c]);
+    const uint32_t *qi = d_buf + sc.qidx_off[c], *pf = d_buf + sc.prefix_off[c];
+#define BQ_LAUNCH(CLS)                                                                          \
+  do {                                                                                         \
+    if (t.stage == 4)                                                                          \
+      k_bq<CLS, 4><<<grid, kBT, 0, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,         \
+                                        counters + c);                                         \
+    else if (t.stage == 2)                                                                     \
+      k_bq<CLS, 2><<<grid, kBT, 0, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,         \
+                                        counters + c);                                         \
+    else                                                                                       \
+      k_bq<CLS, 1><<<grid, kBT, 0, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,         \
+                                        counters + c);                                         \
+  } while (0)
+    switch (c) {
+      case kClsF: BQ_LAUNCH(kClsF); break;
+      case kClsFS: BQ_LAUNCH(kClsFS); break;
+      case kClsS: BQ_LAUNCH(kClsS); break;
+      default: BQ_LAUNCH(kClsMD); break;
+    }
+#undef BQ_LAUNCH
+    count_launch();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 // Result of one query from its accumulators ([0] count, [1..8] slice sums,
@@ -627,12 +921,12 @@ struct buff_plan {
   std::vector<int32_t> status;
   BQ *h_q;                   // pinned
   BQ *d_q;
-  uint2 *d_items;
-  uint32_t nitems;
+  uint32_t *h_sched;         // pinned class lists
+  uint32_t *d_sched;
+  BatchSched sc;
   unsigned long long *d_acc;
   unsigned long long *h_acc;  // pinned
-  unsigned int *d_counter;
-  int grid;
+  unsigned int *d_counter;    // one per class
   cudaGraph_t graph;
   cudaGraphExec_t exec;
 };
@@ -651,7 +945,8 @@ buff_batch_tune default_tune() {
 
 bool tune_ok(const buff_batch_tune &t) {
   return t.tile_rows >= 1024 && t.tile_rows % 1024 == 0 && t.tile_rows <= (1u << 24) &&
-         t.blocks_per_sm >= 1 && t.blocks_per_sm <= 8 && (t.stage == 1 || t.stage == 2);
+         t.blocks_per_sm >= 1 && t.blocks_per_sm <= 8 &&
+         (t.stage == 1 || t.stage == 2 || t.stage == 4);
 }
 
 // Host side of one query: validates it and fills the device descriptor
@@ -745,8 +1040,9 @@ void release_plan(buff_plan *p) {
   if (p->graph) cudaGraphDestroy(p->graph);
   if (p->h_q) cudaFreeHost(p->h_q);
   if (p->h_acc) cudaFreeHost(p->h_acc);
+  if (p->h_sched) cudaFreeHost(p->h_sched);
   if (p->d_q) cudaFree(p->d_q);
-  if (p->d_items) cudaFree(p->d_items);
+  if (p->d_sched) cudaFree(p->d_sched);
   if (p->d_acc) cudaFree(p->d_acc);
   if (p->d_counter) cudaFree(p->d_counter);
   delete p;
@@ -755,18 +1051,12 @@ void release_plan(buff_plan *p) {
 cudaError_t enqueue(buff_plan *p, cudaStream_t s) {
   cudaError_t e = cudaMemcpyAsync(p->d_q, p->h_q, sizeof(BQ) * p->nq, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)
+    e = cudaMemcpyAsync(p->d_sched, p->h_sched, sizeof(uint32_t) * p->sc.words,
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
     e = cudaMemsetAsync(p->d_acc, 0, sizeof(unsigned long long) * kAcc * p->nq, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned int), s);
-  if (e == cudaSuccess && p->nitems) {
-    if (p->tune.stage == 2)
-      k_batch<2><<<p->grid, kBT, 0, s>>>(p->d_q, p->d_items, p->nitems, p->tune.tile_rows,
-                                          p->d_counter);
-    else
-      k_batch<1><<<p->grid, kBT, 0, s>>>(p->d_q, p->d_items, p->nitems, p->tune.tile_rows,
-                                          p->d_counter);
-    count_launch();
-    e = cudaGetLastError();
-  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned int) * 4, s);
+  if (e == cudaSuccess) e = batch_launch(p->d_q, p->d_sched, p->sc, p->tune, p->d_counter, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(p->h_acc, p->d_acc, sizeof(unsigned long long) * kAcc * p->nq,
                         cudaMemcpyDeviceToHost, s);
@@ -792,37 +1082,25 @@ int buff_plan_create(const buff_query *queries, uint32_t nq, const buff_batch_tu
   p->tune = t;
   p->queries.assign(queries, queries + nq);
   p->status.assign(nq, BUFF_OK);
-  std::vector<uint2> items;
   {
     const size_t qb = sizeof(BQ) * (nq ? nq : 1);
     const size_t ab = sizeof(unsigned long long) * kAcc * (nq ? nq : 1);
+    const size_t sb = sizeof(uint32_t) * batch_sched_words(nq);
     BCK(cudaMallocHost(reinterpret_cast<void **>(&p->h_q), qb));
     BCK(cudaMallocHost(reinterpret_cast<void **>(&p->h_acc), ab));
+    BCK(cudaMallocHost(reinterpret_cast<void **>(&p->h_sched), sb));
     BCK(cudaMalloc(reinterpret_cast<void **>(&p->d_q), qb));
     BCK(cudaMalloc(reinterpret_cast<void **>(&p->d_acc), ab));
-    BCK(cudaMalloc(reinterpret_cast<void **>(&p->d_counter), sizeof(unsigned int)));
+    BCK(cudaMalloc(reinterpret_cast<void **>(&p->d_sched), sb));
+    BCK(cudaMalloc(reinterpret_cast<void **>(&p->d_counter), sizeof(unsigned int) * 4));
     for (uint32_t i = 0; i < nq; ++i) {
       const int st = plan_query(queries[i], p->d_acc + (size_t)kAcc * i, &p->h_q[i]);
       if (st) {
         rc = st;
         goto done;
       }
-      const uint32_t n = p->h_q[i].n;
-      for (uint32_t tt = 0; (uint64_t)tt * t.tile_rows < n; ++tt) items.push_back(make_uint2(i, tt));
     }
-    p->nitems = (uint32_t)items.size();
-    BCK(cudaMalloc(reinterpret_cast<void **>(&p->d_items), sizeof(uint2) * (items.size() + 1)));
-    if (!items.empty())
-      BCK(cudaMemcpy(p->d_items, items.data(), sizeof(uint2) * items.size(),
-                     cudaMemcpyHostToDevice));
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, t.stage == 2 ? (const void *)k_batch<2> : (const void *)k_batch<1>, kBT, 0);
-    if (per_sm < 1) per_sm = 1;
-    const int bps = (int)t.blocks_per_sm < per_sm ? (int)t.blocks_per_sm : per_sm;
-    p->grid = bps * dev_sms();
-    const uint32_t need = (p->nitems + kWarps - 1) / kWarps;
-    if ((uint32_t)p->grid > need) p->grid = need ? (int)need : 1;
+    batch_schedule(p->h_q, nq, t.tile_rows, p->h_sched, &p->sc);
   }
 done:
   if (rc != BUFF_OK) {
@@ -842,6 +1120,7 @@ int buff_plan_set_preds(buff_plan *p, const double *preds) {
     if (st) return st;
     p->queries[i] = q;
   }
+  batch_schedule(p->h_q, p->nq, p->tune.tile_rows, p->h_sched, &p->sc);
   return BUFF_OK;
 }
 
@@ -899,9 +1178,9 @@ int buff_batch_autotune(const buff_query *queries, uint32_t nq, void *stream,
                         buff_batch_tune *best, float *best_ms) {
   if (!best || (nq && !queries)) return BUFF_EINVAL;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  const uint32_t tiles[] = {8192, 16384, 32768, 65536, 131072};
-  const uint32_t bps[] = {2, 4, 8};
-  const uint32_t stages[] = {1, 2};
+  const uint32_t tiles[] = {8192, 16384, 32768, 65536};
+  const uint32_t bps[] = {3, 4, 6, 8};
+  const uint32_t stages[] = {1, 2, 4};
   float bms = 1e30f;
   buff_batch_tune bt = default_tune();
   cudaEvent_t e0, e1;

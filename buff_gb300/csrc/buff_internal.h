@@ -168,10 +168,18 @@ cudaError_t check_rows(const uint32_t *rows, uint64_t nrows, uint32_t n, uint32_
 constexpr int kBatchAcc = 12;
 size_t batch_desc_size();
 int batch_plan_query(const buff_query &q, unsigned long long *acc, void *desc);
-uint32_t batch_tiles(const void *desc, uint32_t tile);
-cudaError_t batch_launch_prefix(const void *d_desc, const uint32_t *d_prefix, uint32_t nq,
-                                uint32_t nitems, const buff_batch_tune &t, unsigned int *counter,
-                                cudaStream_t s);
+// Per-class work lists of one batch (query indices and tile prefixes packed
+// into one u32 buffer of batch_sched_words(nq) words).
+struct BatchSched {
+  uint32_t n[4], items[4], qidx_off[4], prefix_off[4];
+  uint32_t words;  // used length of the buffer
+};
+size_t batch_sched_words(uint32_t nq);
+void batch_schedule(const void *h_desc, uint32_t nq, uint32_t tile, uint32_t *buf,
+                    BatchSched *sc);
+// Launches every class of a scheduled batch on s; counters: 4 zeroed u32.
+cudaError_t batch_launch(const void *d_desc, const uint32_t *d_buf, const BatchSched &sc,
+                         const buff_batch_tune &t, unsigned int *counters, cudaStream_t s);
 void batch_result(const buff_query &q, const unsigned long long *acc, buff_query_result *out);
 
 int num_sms(int device);

@@ -101,7 +101,6 @@ struct Slot {
   cudaStream_t s = nullptr;
   cudaEvent_t ev = nullptr;
   void *h_desc = nullptr, *d_desc = nullptr;
-  uint32_t *h_pfx = nullptr, *d_pfx = nullptr;
   unsigned long long *h_acc = nullptr, *d_acc = nullptr;
   unsigned int *d_counter = nullptr;
   PlainRes *h_plain = nullptr, *d_plain = nullptr;
@@ -132,6 +131,7 @@ struct buff_server {
   std::atomic<int> loop_status{BUFF_OK};
   std::deque<Req> waiting;  // loop thread only
   uint64_t batches = 0, launched_reqs = 0;
+  uint32_t warp_slots = 0;  // resident warps of the device (SMs x 64)
 };
 
 namespace {
@@ -244,7 +244,6 @@ void retire(buff_server *S, Slot &sl) {
 int launch_batched(buff_server *S, Slot &sl) {
   const size_t dsz = buffk::batch_desc_size();
   const uint32_t nq = (uint32_t)sl.reqs.size();
-  uint32_t items = 0;
   for (uint32_t i = 0; i < nq; ++i) {
     Req &q = sl.reqs[i];
     buff_query uq;
@@ -257,22 +256,33 @@ int launch_batched(buff_server *S, Slot &sl) {
     uq.values = q.values;
     void *d = static_cast<uint8_t *>(sl.h_desc) + dsz * i;
     q.status = buffk::batch_plan_query(uq, sl.d_acc + (size_t)buffk::kBatchAcc * i, d);
-    sl.h_pfx[i] = items;
-    if (q.status == BUFF_OK)
-      items += buffk::batch_tiles(d, S->cfg.tune.tile_rows);
-    else
-      memset(d, 0, dsz);  // an invalid request: zero rows, no work items
+    if (q.status != BUFF_OK) memset(d, 0, dsz);  // an invalid request: zero rows, no work
   }
-  sl.h_pfx[nq] = items;
+  // one upload: the descriptors, then the class lists right after them
+  const size_t soff = (dsz * nq + 15) / 16 * 16;
+  uint32_t *h_sched = reinterpret_cast<uint32_t *>(static_cast<uint8_t *>(sl.h_desc) + soff);
+  const uint32_t *d_sched =
+      reinterpret_cast<const uint32_t *>(static_cast<uint8_t *>(sl.d_desc) + soff);
+  // tile per batch: small batches split each query over many warps (latency),
+  // large ones use the configured tile (fewer, longer items)
+  uint64_t rows = 0;
+  for (uint32_t i = 0; i < nq; ++i) rows += sl.reqs[i].col->n;
+  const uint64_t slots = (uint64_t)S->warp_slots * 4;
+  uint64_t tile = rows / (slots ? slots : 1);
+  tile = (tile + 1023) / 1024 * 1024;
+  if (tile < 1024) tile = 1024;
+  if (tile > S->cfg.tune.tile_rows) tile = S->cfg.tune.tile_rows;
+  buff_batch_tune t = S->cfg.tune;
+  t.tile_rows = (uint32_t)tile;
+  buffk::BatchSched sc;
+  buffk::batch_schedule(sl.h_desc, nq, t.tile_rows, h_sched, &sc);
   cudaStream_t s = sl.s;
-  cudaError_t e = cudaMemcpyAsync(sl.d_desc, sl.h_desc, dsz * nq, cudaMemcpyHostToDevice, s);
+  cudaError_t e = cudaMemcpyAsync(sl.d_desc, sl.h_desc, soff + 4 * (size_t)sc.words,
+                                  cudaMemcpyHostToDevice, s);
+  // counters (16 bytes, padded to 64) precede the accumulators
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(sl.d_pfx, sl.h_pfx, sizeof(uint32_t) * (nq + 1), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess)
-    e = cudaMemsetAsync(sl.d_acc, 0, sizeof(unsigned long long) * buffk::kBatchAcc * nq, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_counter, 0, sizeof(unsigned int), s);
-  if (e == cudaSuccess)
-    e = buffk::batch_launch_prefix(sl.d_desc, sl.d_pfx, nq, items, S->cfg.tune, sl.d_counter, s);
+    e = cudaMemsetAsync(sl.d_counter, 0, 64 + sizeof(unsigned long long) * buffk::kBatchAcc * nq, s);
+  if (e == cudaSuccess) e = buffk::batch_launch(sl.d_desc, d_sched, sc, t, sl.d_counter, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(sl.h_acc, sl.d_acc, sizeof(unsigned long long) * buffk::kBatchAcc * nq,
                         cudaMemcpyDeviceToHost, s);
@@ -392,12 +402,9 @@ void destroy_slots(buff_server *S) {
     if (sl.ev) cudaEventDestroy(sl.ev);
     if (sl.s) cudaStreamDestroy(sl.s);
     if (sl.h_desc) cudaFreeHost(sl.h_desc);
-    if (sl.h_pfx) cudaFreeHost(sl.h_pfx);
     if (sl.h_acc) cudaFreeHost(sl.h_acc);
     if (sl.h_plain) cudaFreeHost(sl.h_plain);
     if (sl.d_desc) cudaFree(sl.d_desc);
-    if (sl.d_pfx) cudaFree(sl.d_pfx);
-    if (sl.d_acc) cudaFree(sl.d_acc);
     if (sl.d_counter) cudaFree(sl.d_counter);
     if (sl.d_plain) cudaFree(sl.d_plain);
   }
@@ -421,7 +428,7 @@ int buff_server_create(const buff_server_config *cfg, buff_server **out) {
     c.tune.stage = 2;
   }
   if (c.tune.tile_rows % 1024 || c.tune.blocks_per_sm < 1 || c.tune.blocks_per_sm > 8 ||
-      (c.tune.stage != 1 && c.tune.stage != 2))
+      (c.tune.stage != 1 && c.tune.stage != 2 && c.tune.stage != 4))
     return BUFF_EINVAL;
   buff_server *S = new (std::nothrow) buff_server();
   if (!S) return BUFF_ENOMEM;
@@ -435,25 +442,26 @@ int buff_server_create(const buff_server_config *cfg, buff_server **out) {
     return rc;
   }
   S->out.cap = c.output_budget_bytes;
+  S->warp_slots = (uint32_t)buffk::num_sms(S->device) * 64u;
   S->slots.resize(c.max_inflight);
   const uint32_t mb = c.batched ? c.max_batch : 1;
   const size_t dsz = buffk::batch_desc_size();
   for (Slot &sl : S->slots) {
     if ((e = cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking)) != cudaSuccess) break;
     if ((e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming)) != cudaSuccess) break;
-    if ((e = cudaMallocHost(&sl.h_desc, dsz * mb)) != cudaSuccess) break;
-    if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_pfx), 4 * (mb + 1))) != cudaSuccess) break;
+    const size_t sw = 4 * buffk::batch_sched_words(mb);
+    const size_t stage = (dsz * mb + 15) / 16 * 16 + sw;
+    if ((e = cudaMallocHost(&sl.h_desc, stage)) != cudaSuccess) break;
     if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_acc),
                             8 * buffk::kBatchAcc * mb)) != cudaSuccess)
       break;
     if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_plain), sizeof(PlainRes))) != cudaSuccess)
       break;
-    if ((e = cudaMalloc(&sl.d_desc, dsz * mb)) != cudaSuccess) break;
-    if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_pfx), 4 * (mb + 1))) != cudaSuccess) break;
-    if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_acc), 8 * buffk::kBatchAcc * mb)) !=
+    if ((e = cudaMalloc(&sl.d_desc, stage)) != cudaSuccess) break;
+    if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_counter), 64 + 8 * buffk::kBatchAcc * mb)) !=
         cudaSuccess)
       break;
-    if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_counter), 4)) != cudaSuccess) break;
+    sl.d_acc = reinterpret_cast<unsigned long long *>(reinterpret_cast<uint8_t *>(sl.d_counter) + 64);
     if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_plain), sizeof(PlainRes))) != cudaSuccess)
       break;
     sl.reqs.reserve(mb);

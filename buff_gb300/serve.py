@@ -63,18 +63,22 @@ class Server:
         check(lib().buff_server_stats(self._h, C.byref(b), C.byref(r), C.byref(u)), "stats")
         return {"batches": b.value, "requests": r.value, "output_bytes_in_use": u.value}
 
-    def replay(self, reqs, arrival_ns: np.ndarray):
-        """Plays requests at their arrival times; returns (latencies ns,
-        results, wall seconds)."""
+    def replay(self, reqs, arrival_ns: np.ndarray, results: bool = True):
+        """Plays requests (a list of Request or an array of REQ_DTYPE) at
+        their arrival times; returns (latencies ns, results, wall seconds)."""
         n = len(reqs)
-        arr = (Request * max(n, 1))(*reqs)
+        if isinstance(reqs, np.ndarray):
+            assert reqs.dtype == REQ_DTYPE
+            arr = np.ascontiguousarray(reqs).ctypes.data
+        else:
+            arr = (Request * max(n, 1))(*reqs)
         arrival = np.ascontiguousarray(arrival_ns, dtype=np.uint64)
         lat = np.zeros(max(n, 1), dtype=np.uint64)
-        res = (QueryResult * max(n, 1))()
+        res = (QueryResult * max(n, 1))() if results else None
         wall = C.c_double(0)
         check(lib().buff_server_replay(self._h, arr, arrival.ctypes.data, n, lat.ctypes.data,
                                        res, C.byref(wall)), "server_replay")
-        return lat[:n], list(res[:n]), wall.value
+        return lat[:n], (list(res[:n]) if results else None), wall.value
 
     def stop(self):
         if self._h and self._h.value:
@@ -92,8 +96,14 @@ class Server:
             pass
 
 
+# numpy layout of buff_request (for request streams built as arrays)
+REQ_DTYPE = np.dtype([("column", "<u4"), ("ops", "<u4"), ("precision", "<u4"),
+                      ("reserved", "<u4"), ("pred", "<f8"), ("tag", "<u8")])
+assert REQ_DTYPE.itemsize == C.sizeof(Request)
+
+
 def request(column: int, ops: int, pred: float = 0.0, precision: int = 0, tag: int = 0):
     return Request(column, ops, precision, 0, float(pred), tag)
 
 
-__all__ = ["Server", "request"]
+__all__ = ["Server", "request", "REQ_DTYPE"]

@@ -8,6 +8,10 @@ benchmark configurations (none of them is a public dataset).
 - ``outlier_column``: 99% N(100, 5) at 6 decimals, 1% U(-1e6, 1e6) at seeded
   random positions (67,108,864 values, scale 10^6).
 
+- ``column_set``: many random-walk columns with log-uniform lengths, each with
+  its own decimals (2-6), step size and start (the batched and serving
+  configurations: 4,096 columns of 1K-4M rows, 2,048 columns of 64K-16M rows).
+
 The numpy forms are for host-sized cases; the torch forms build large columns
 directly in device memory.
 """
@@ -61,3 +65,30 @@ def bounded_walk_torch(n: int, seed: int = 2, device="cuda"):
 def quantile_preds(x: np.ndarray, selectivities=(0.001, 0.01, 0.1, 0.5)):
     """Predicates p with P(x > p) ~= selectivity."""
     return [float(np.quantile(x, 1.0 - s)) for s in selectivities]
+
+
+def column_set(ncols: int, lo: int, hi: int, seed: int):
+    """Lengths (log-uniform in [lo, hi]), decimals U{2..6}, step sizes and
+    starts of a seeded set of random-walk columns."""
+    rng = np.random.default_rng(seed)
+    lens = np.exp(rng.uniform(np.log(lo), np.log(hi), ncols)).astype(np.int64)
+    dec = rng.integers(2, 7, ncols)
+    sigma = 10.0 ** rng.uniform(-2, 1, ncols)
+    start = rng.uniform(-1e3, 1e3, ncols)
+    return lens, dec, sigma, start
+
+
+def fill_walk_torch(out, n: int, dec: int, sigma: float, start: float, seed: int):
+    """Writes a random walk of n rows rounded to `dec` decimals into `out[:n]`."""
+    import torch
+
+    g = torch.Generator(device=out.device)
+    g.manual_seed(seed)
+    v = out[:n]
+    torch.randn(n, generator=g, device=out.device, dtype=torch.float64, out=v)
+    v.mul_(sigma)
+    v.cumsum_(0)
+    v.add_(start)
+    s = 10.0 ** dec
+    v.mul_(s).round_().div_(s)
+    return v

@@ -249,7 +249,7 @@ int buff_range_filter_decode(const buff_col *col, double pred, uint32_t *words, 
 typedef struct buff_batch_tune {
   uint32_t tile_rows;     /* rows per work item: a multiple of 1024 (encode uses 4x) */
   uint32_t blocks_per_sm; /* persistent 256-thread CTAs per SM, 1..8 */
-  uint32_t stage;         /* 1024-row steps whose first-slice loads are issued together: 1 or 2 */
+  uint32_t stage;         /* row steps whose slice loads are issued together: 1, 2 or 4 */
   uint32_t reserved;
 } buff_batch_tune;
 
