@@ -59,7 +59,11 @@ def parse_args():
                     help="release the f64 input after encode (small-footprint profiling runs)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched form")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving form")
+    ap.add_argument("--no-outlier", action="store_true", help="skip the outlier-column form")
+    ap.add_argument("--outlier-rows", type=int, default=1 << 26)
     ap.add_argument("--batched-cols", type=int, default=4096)
+    ap.add_argument("--batched-tune", default=None,
+                    help="tile_rows,blocks_per_sm,stage for the batched plan (default: autotune)")
     ap.add_argument("--serve-cols", type=int, default=2048)
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="length of each offered-load run of the serving sweep")
@@ -97,7 +101,8 @@ def max_over_ranks(v, world):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -257,6 +262,68 @@ def run_e2e(L, col, img_len, nw, pred, sh, count, res, args):
     return e2e_s
 
 
+# ---------------------------------------------------------------- outlier column
+
+def run_outlier_form(args, stream, peak):
+    """67,108,864 rows: 99% N(100, 5) and 1% U(-1e6, 1e6) at seeded random
+    positions, 6 decimals (scale 10^6).  The buff-major encode keeps the
+    leading byte columns whose first-2000-row majority is strong as (major
+    byte, outlier bitmap, outlier bytes); filters merge the outlier hits."""
+    import torch
+
+    from buff_gb300 import capi
+    from buff_gb300.compress import Column, MajorColumn
+    from buff_gb300.workloads import outlier_column_torch
+
+    L = capi.lib()
+    sh = stream.cuda_stream
+    n = args.outlier_rows
+    x = outlier_column_torch(n, seed=3)
+    torch.cuda.synchronize()
+    samp = x[:: max(1, n >> 20)]
+    preds = {f"range_{q:g}": float(torch.quantile(samp, 1.0 - q).item()) for q in (0.01, 0.1, 0.5)}
+    peq = float(x[n // 7].item())
+
+    def enc():
+        c = MajorColumn.encode(x, 1000000, stream=stream)
+        c.free()
+
+    t_enc = time_op(enc, 3, stream)
+    col = MajorColumn.encode(x, 1000000, stream=stream)
+    plain = Column.encode(x, 1000000, stream=stream)
+    info, pinfo = col.info, plain.info
+    nw = (n + 31) // 32
+    words = torch.empty(nw, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+    ops = {"encode": {"ms": t_enc * 1e3, "gvalues_s": n / t_enc / 1e9,
+                      "gb_s_input": 8 * n / t_enc / 1e9}}
+    h, ph = col.handle, plain.handle
+    for name, p in list(preds.items()) + [("equal", peq)]:
+        fn = L.buff_equal_filter_majority if name == "equal" else L.buff_range_filter_majority
+        pfn = L.buff_equal_filter if name == "equal" else L.buff_range_filter
+        t = time_op(lambda: fn(h, p, words.data_ptr(), cnt.data_ptr(), sh), 10, stream)
+        tp = time_op(lambda: pfn(ph, p, words.data_ptr(), cnt.data_ptr(), sh), 10, stream)
+        ops[name] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "plain_layout_ms": tp * 1e3}
+    res = capi.SumResult()
+    t = time_op(lambda: L.buff_sum_majority(h, C.byref(res), sh), 5, stream)
+    ops["sum"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "note": "includes the host combine"}
+    mv = C.c_double(0)
+    mc = C.c_uint64(0)
+    t = time_op(lambda: L.buff_max_majority(h, C.byref(mv), C.byref(mc), None, None, sh), 5,
+                stream)
+    ops["max"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "note": "per-column host loop"}
+    out = {"workload": f"{n} rows: 99% N(100,5), 1% U(-1e6,1e6) at seeded random positions, "
+                       f"6 decimals, scale 1e6 (seed 3)", "rows": n,
+           "fixed_len": info.fixed_len, "outlier_cols": info.outlier_cols,
+           "device_bytes": info.device_bytes, "plain_layout_device_bytes": pinfo.device_bytes,
+           "ops": ops}
+    col.free()
+    plain.free()
+    del x
+    torch.cuda.empty_cache()
+    return out
+
+
 # ---------------------------------------------------------------- batched form
 
 def run_batched_form(args, stream, peak):
@@ -323,7 +390,11 @@ def run_batched_form(args, stream, peak):
     wb = torch.zeros(int(woff[-1]), dtype=torch.int32, device="cuda")
     wp = torch.zeros(int(woff[-1]), dtype=torch.int32, device="cuda")
     qs = [batch.query(cols[i], Q_RANGE | Q_SUM, preds[i], wb[int(woff[i]):]) for i in range(ncols)]
-    best, tune_ms = batch.autotune(qs, stream)
+    if args.batched_tune:
+        tr, bp, st = (int(v) for v in args.batched_tune.split(","))
+        best, tune_ms = batch.tune(tr, bp, st), None
+    else:
+        best, tune_ms = batch.autotune(qs, stream)
     plan = batch.Plan(qs, best, stream)
     gs = torch.cuda.Stream()
     plan.capture(gs)
@@ -708,13 +779,15 @@ def main():
                "sample": f"first {rows} rows of the column, 3 timed passes of filter+sum, "
                          f"1 thread"}
 
-    batched_form = serving_form = None
+    batched_form = serving_form = outlier_form = None
     if rank == 0 and world == 1:
         col.free()
         col = None
         if not args.free_input:
             del x
         torch.cuda.empty_cache()
+        if not args.no_outlier:
+            outlier_form = run_outlier_form(args, stream, peak)
         if not args.no_batched:
             batched_form = run_batched_form(args, stream, peak)
         if not args.no_serve:
@@ -746,6 +819,7 @@ def main():
             "cpu_baseline": cpu,
             "ops": ops,
             "encode_once_s": time.time() - t0,
+            "outlier": outlier_form,
             "batched": batched_form,
             "serving": serving_form,
         }

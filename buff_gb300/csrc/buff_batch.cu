@@ -190,8 +190,10 @@ struct ScatCol {
 // a 64-bit word, bytes of neighbouring rows gathered with byte permutes into
 // shared memory, then one 16-byte store per lane per slice and the packed
 // tail of the lane's 16 rows.
+template <int K>
 __device__ __forceinline__ void scatter_chunk(const ScatCol &c, uint32_t r0, uint32_t lane,
                                               uint8_t *ws) {
+  constexpr uint32_t k = K;
   ulonglong2 raw[8];
 #pragma unroll
   for (int m = 0; m < 8; ++m) {
@@ -214,14 +216,14 @@ __device__ __forceinline__ void scatter_chunk(const ScatCol &c, uint32_t r0, uin
         b = (unsigned long long)__double_as_longlong(c.x[i0 + j]);
       cc[j] = (i0 + j < c.n) ? (unsigned long long)(fetch_bits(b, c.pexp, c.dlen) - c.base) : 0ull;
     }
-    if (c.k) {
+    if (k) {
       const unsigned long long a0 = (cc[0] << (up & 63)) ^ 0x8080808080808080ull;
       const unsigned long long a1 = (cc[1] << (up & 63)) ^ 0x8080808080808080ull;
       const uint32_t hw0 = (uint32_t)(a0 >> 32), lw0 = (uint32_t)a0;
       const uint32_t hw1 = (uint32_t)(a1 >> 32), lw1 = (uint32_t)a1;
 #pragma unroll
       for (uint32_t sl = 0; sl < 8; ++sl) {
-        if (sl < c.k) {
+        if ((int)sl < K) {
           const bool in_hi = sl < 4;
           const uint32_t b = in_hi ? 3u - sl : 7u - sl;
           const uint32_t sel = b | ((4u + b) << 4);
@@ -232,25 +234,25 @@ __device__ __forceinline__ void scatter_chunk(const ScatCol &c, uint32_t r0, uin
     }
     if (c.r) {
       const uint32_t packed = (uint32_t)(cc[0] & rmask) | ((uint32_t)(cc[1] & rmask) << 8);
-      *reinterpret_cast<uint16_t *>(ws + c.k * kRowChunk + off) = (uint16_t)packed;
+      *reinterpret_cast<uint16_t *>(ws + k * kRowChunk + off) = (uint16_t)packed;
     }
   }
   __syncwarp();
 #pragma unroll
   for (uint32_t sl = 0; sl < 8; ++sl) {
-    if (sl < c.k) {
+    if ((int)sl < K) {
       const uint4 v = *reinterpret_cast<const uint4 *>(ws + sl * kRowChunk + lane * 16);
       __stcs(reinterpret_cast<uint4 *>(c.slices + sl * c.stride + r0 + lane * 16), v);
     }
   }
   if (c.r == 1) {
-    const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(ws + c.k * kRowChunk + lane * 16);
+    const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(ws + k * kRowChunk + lane * 16);
     const uint32_t lo8 = (uint32_t)((v.x * 0x0102040810204080ull) >> 56);
     const uint32_t hi8 = (uint32_t)((v.y * 0x0102040810204080ull) >> 56);
     *reinterpret_cast<uint16_t *>(c.tail + (size_t)2 * ((r0 >> 4) + lane)) =
         (uint16_t)(lo8 | (hi8 << 8));
   } else if (c.r) {
-    const uint4 v = *reinterpret_cast<const uint4 *>(ws + c.k * kRowChunk + lane * 16);
+    const uint4 v = *reinterpret_cast<const uint4 *>(ws + k * kRowChunk + lane * 16);
     const uint8_t *b = reinterpret_cast<const uint8_t *>(&v);
     unsigned long long lo = 0, hi = 0;
 #pragma unroll
@@ -271,9 +273,10 @@ __device__ __forceinline__ void scatter_chunk(const ScatCol &c, uint32_t r0, uin
   __syncwarp();
 }
 
-// Persistent scatter: every warp takes (column, tile) items; a tile is a
-// multiple of 512 rows, and the last tile of a column also writes the
-// padding rows up to the slice stride (code 0).
+// Persistent scatter for the columns with K slices: every warp takes
+// (column, tile) items; a tile is a multiple of 512 rows, and the last tile
+// of a column also writes the padding rows up to the slice stride (code 0).
+template <int K>
 __global__ void __launch_bounds__(kBT) k_benc_scatter(const ScatCol *__restrict__ cols,
                                                       const uint2 *__restrict__ items,
                                                       uint32_t nitems, uint32_t tile,
@@ -290,8 +293,21 @@ __global__ void __launch_bounds__(kBT) k_benc_scatter(const ScatCol *__restrict_
     const ScatCol c = cols[item.x];
     const uint32_t rows = (uint32_t)c.stride;  // n rounded up to 512
     const uint32_t r0 = item.y * tile, r1 = min(rows, r0 + tile);
-    for (uint32_t ch = r0; ch < r1; ch += kRowChunk) scatter_chunk(c, ch, lane, ws);
+    for (uint32_t ch = r0; ch < r1; ch += kRowChunk) scatter_chunk<K>(c, ch, lane, ws);
   }
+}
+
+cudaError_t launch_benc_scatter(int k, int grid, const ScatCol *cols, const uint2 *items,
+                                uint32_t nitems, uint32_t tile, unsigned int *counter,
+                                cudaStream_t s) {
+  switch (k) {
+#define BS(K) \
+  case K: k_benc_scatter<K><<<grid, kBT, 0, s>>>(cols, items, nitems, tile, counter); break;
+    BS(0) BS(1) BS(2) BS(3) BS(4) BS(5) BS(6) BS(7) BS(8)
+#undef BS
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------- queries
@@ -353,16 +369,17 @@ __device__ __forceinline__ unsigned long long every_r(uint32_t r) {
 }
 
 // Sum of the 16 r-bit fields packed LSB-first in (lo, hi): every set bit b
-// of the 16r-bit stream adds 2^(b mod r).  pat = every_r(r); the phase of
-// the hi word's bit 0 is 64 mod r.
+// of the 16r-bit stream adds 2^(b mod r).  pat = every_r(r); bit j of hi is
+// stream bit 64 + j, whose residue class starts at qh0 = (r - 64 mod r) mod r
+// (computed once per tile).
 __device__ __forceinline__ uint32_t fields16_sum(unsigned long long lo, unsigned long long hi,
-                                                 uint32_t r, unsigned long long pat) {
+                                                 uint32_t r, unsigned long long pat,
+                                                 uint32_t qh0) {
   if (r == 1) return __popcll(lo) + __popcll(hi);
-  const uint32_t ph = 64 % r;
-  uint32_t acc = 0;
+  uint32_t acc = 0, qh = qh0;
   for (uint32_t p = 0; p < r; ++p) {
-    const uint32_t q = (p + r - ph) % r;  // hi bit j has stream bit 64 + j == p (mod r)
-    acc += (uint32_t)(__popcll(lo & (pat << p)) + __popcll(hi & (pat << q))) << p;
+    acc += (uint32_t)(__popcll(lo & (pat << p)) + __popcll(hi & (pat << qh))) << p;
+    qh = qh + 1 == r ? 0u : qh + 1;
   }
   return acc;
 }
@@ -389,6 +406,7 @@ __device__ __forceinline__ void tile_filter_sum(const BQ &q, uint32_t r0, uint32
   const bool cmp = do_f && q.fill == 0;
   const uint32_t nload = do_s ? (q.k < 4 ? q.k : 4u) : (q.k ? 1u : 0u);
   const unsigned long long pat = q.r > 1 ? every_r(q.r) : 0ull;
+  const uint32_t qh0 = q.r > 1 ? (q.r - 64 % q.r) % q.r : 0u;
   uint32_t sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   uint32_t tacc = 0;
   uint32_t cnt = 0;
@@ -441,7 +459,7 @@ __device__ __forceinline__ void tile_filter_sum(const BQ &q, uint32_t r0, uint32
           if (do_s || need_tf) {
             unsigned long long lo, hi;
             load_tail16(q.tail, row0 >> 4, q.r, lo, hi);
-            if (do_s) tacc += fields16_sum(lo, hi, q.r, pat);  // rows past n hold zeros
+            if (do_s) tacc += fields16_sum(lo, hi, q.r, pat, qh0);  // rows past n hold zeros
             if (need_tf) {
               uint32_t gtt = 0, eqt = 0, b = eq;
               while (b) {
@@ -713,6 +731,146 @@ __device__ __forceinline__ void tile_filter32(const BQ &q, uint32_t r0, uint32_t
   if (lane == 0 && sc) atomicAdd(q.acc, sc);
 }
 
+// ---- filter + sum with the slices staged through shared memory
+//
+// Each lane copies its own 16-byte pieces (16 rows of up to 4 slices) and the
+// first 4r lanes the step's 64r tail bytes into a per-warp ring of kDepth
+// 512-row steps with cp.async, so kDepth steps of every slice are in flight
+// without holding registers; a lane reads back only what it copied (the
+// tail group excepted, hence the warp barrier around each step).
+constexpr int kDepth = 4;
+constexpr uint32_t kSlotBytes = 4 * 512 + 512;  // 4 slices + up to 448 tail bytes
+constexpr uint32_t kRingBytes = kDepth * kSlotBytes;
+
+__device__ __forceinline__ void cp16(uint8_t *dst, const uint8_t *src) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void fs_issue(const BQ &q, uint32_t sb, uint32_t r1, uint32_t lane,
+                                         uint32_t nst, uint8_t *slot) {
+  if (sb < r1) {
+    const uint32_t row0 = sb + lane * 16;
+    if (row0 < r1)
+      for (uint32_t j = 0; j < nst; ++j)
+        cp16(slot + j * 512 + lane * 16, q.slices + j * q.stride + row0);
+    if (q.r && lane < 4 * q.r)
+      cp16(slot + 4 * 512 + lane * 16, q.tail + (size_t)(sb >> 9) * 64 * q.r + lane * 16);
+  }
+  cp_commit();  // every lane commits one group per step, even an empty one
+}
+
+template <bool DO_F>
+__device__ __forceinline__ void tile_fs_async(const BQ &q, uint32_t r0, uint32_t r1,
+                                              uint32_t lane, uint8_t *ring) {
+  const bool is_range = q.ops & kOpRange;
+  const bool cmp = DO_F && q.fill == 0;
+  const uint32_t nst = q.k < 4 ? q.k : 4u;  // slices staged; later ones load directly
+  const unsigned long long pat = q.r > 1 ? every_r(q.r) : 0ull;
+  const uint32_t qh0 = q.r > 1 ? (q.r - 64 % q.r) % q.r : 0u;
+  uint32_t sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  uint32_t tacc = 0, cnt = 0;
+  __syncwarp();  // the ring may still be read by the previous item
+#pragma unroll
+  for (int d = 0; d < kDepth - 1; ++d) fs_issue(q, r0 + d * 512, r1, lane, nst, ring + d * kSlotBytes);
+  uint32_t t = 0;
+  for (uint32_t sb = r0; sb < r1; sb += 512, ++t) {
+    fs_issue(q, sb + (kDepth - 1) * 512, r1, lane, nst,
+             ring + ((t + kDepth - 1) % kDepth) * kSlotBytes);
+    cp_wait<kDepth - 1>();
+    __syncwarp();
+    const uint8_t *slot = ring + (t % kDepth) * kSlotBytes;
+    const uint32_t row0 = sb + lane * 16;
+    const bool act = row0 < r1;
+    uint32_t valid = 0, eq = 0, gt = 0;
+    if (act) {
+      const uint32_t left = q.n - row0;
+      valid = left >= 16 ? 0xFFFFu : ((1u << left) - 1u);
+      eq = valid;
+      if (row0 + 16 > q.full_rows)
+        eq &= row0 >= q.full_rows ? 0u : ((1u << (q.full_rows - row0)) - 1u);
+#pragma unroll
+      for (uint32_t j = 0; j < 8; ++j) {
+        if (j >= q.k) break;
+        const bool need_f = cmp && j < q.k_used && eq;
+        const uint4 w = j < 4 ? *reinterpret_cast<const uint4 *>(slot + j * 512 + lane * 16)
+                              : __ldcs(reinterpret_cast<const uint4 *>(q.slices + j * q.stride + row0));
+        sacc[j] = __dp4a(w.x ^ H, 0x01010101u, sacc[j]);
+        sacc[j] = __dp4a(w.y ^ H, 0x01010101u, sacc[j]);
+        sacc[j] = __dp4a(w.z ^ H, 0x01010101u, sacc[j]);
+        sacc[j] = __dp4a(w.w ^ H, 0x01010101u, sacc[j]);
+        if (need_f) {
+          const ByteTarget tg = make_target(q.tbyte[j]);
+          uint32_t g[4], e[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) cmp4(w4(w, i), tg, g[i], e[i]);
+          gt |= eq & gather16(g);
+          eq &= gather16(e);
+        }
+      }
+      if (q.r) {
+        const unsigned short *tp =
+            reinterpret_cast<const unsigned short *>(slot + 4 * 512 + lane * 2 * q.r);
+        unsigned long long lo = 0, hi = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < 7; ++i) {
+          if (i < q.r) {
+            const unsigned long long h = tp[i];
+            if (i < 4)
+              lo |= h << (16 * i);
+            else
+              hi |= h << (16 * (i - 4));
+          }
+        }
+        tacc += fields16_sum(lo, hi, q.r, pat, qh0);
+        if (cmp && q.r_used && eq) {
+          uint32_t gtt = 0, eqt = 0, b = eq;
+          while (b) {
+            const uint32_t i = __ffs(b) - 1;
+            b &= b - 1;
+            const uint32_t f = field16(lo, hi, i, q.r);
+            gtt |= (uint32_t)(f > q.ttail) << i;
+            eqt |= (uint32_t)(f == q.ttail) << i;
+          }
+          gt |= eq & gtt;
+          eq &= eqt;
+        }
+      }
+    }
+    if (DO_F) {
+      const uint32_t res = !act ? 0u : q.fill == 1 ? valid : q.fill == 2 ? 0u
+                                                    : (is_range ? gt : eq);
+      const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
+      if (act && !(lane & 1)) {
+        const uint32_t word = res | (hi16 << 16);
+        q.words[row0 >> 5] = word;
+        cnt += __popc(word);
+      }
+    }
+    __syncwarp();  // the slot is refilled by the next step's copies
+  }
+  cp_wait<0>();
+#pragma unroll
+  for (uint32_t j = 0; j < 8; ++j) {
+    if (j >= q.k) break;
+    const unsigned long long sj = warp_sum_ull(sacc[j]);
+    if (lane == 0 && sj) atomicAdd(q.acc + 1 + j, sj);
+  }
+  if (q.r) {
+    const unsigned long long st = warp_sum_ull(tacc);
+    if (lane == 0 && st) atomicAdd(q.acc + 9, st);
+  }
+  if (DO_F) {
+    const unsigned long long sc = warp_sum_ull(cnt);
+    if (lane == 0 && sc) atomicAdd(q.acc, sc);
+  }
+}
+
 // Query classes: each runs in its own persistent launch, compiled for its
 // ops only.  A query with a filter and a sum is one FS item; a query with a
 // sum (without a filter) and a max or decode is an S item and an MD item.
@@ -727,7 +885,9 @@ __global__ void __launch_bounds__(kBT) k_bq(const BQ *__restrict__ qs,
                                             const uint32_t *__restrict__ prefix, uint32_t nq,
                                             uint32_t nitems, uint32_t tile,
                                             unsigned int *counter) {
+  extern __shared__ __align__(16) uint8_t dyn_smem[];
   const uint32_t lane = threadIdx.x & 31;
+  uint8_t *ring = dyn_smem + (threadIdx.x >> 5) * kRingBytes;  // FS / S classes only
   for (;;) {
     uint32_t it = 0;
     if (lane == 0) it = atomicAdd(counter, 1u);
@@ -745,8 +905,8 @@ __global__ void __launch_bounds__(kBT) k_bq(const BQ *__restrict__ qs,
     const uint32_t r0 = (it - __ldg(prefix + lo)) * tile;
     const uint32_t r1 = min(q.n, r0 + tile);
     if (CLS == kClsF) tile_filter32<STAGE>(q, r0, r1, lane);
-    if (CLS == kClsFS) tile_filter_sum<STAGE, true, true>(q, r0, r1, lane);
-    if (CLS == kClsS) tile_filter_sum<STAGE, false, true>(q, r0, r1, lane);
+    if (CLS == kClsFS) tile_fs_async<true>(q, r0, r1, lane, ring);
+    if (CLS == kClsS) tile_fs_async<false>(q, r0, r1, lane, ring);
     if (CLS == kClsMD) {
       if (q.ops & kOpMax) tile_max<STAGE>(q, r0, r1, lane);
       if (q.ops & kOpDecode) tile_decode<STAGE>(q, r0, r1, lane);
@@ -834,9 +994,25 @@ void batch_schedule(const void *h_desc, uint32_t nq, uint32_t tile, uint32_t *bu
   sc->words = off;
 }
 
+size_t class_smem(int cls) {
+  return (cls == kClsFS || cls == kClsS) ? (size_t)kWarps * kRingBytes : 0;
+}
+
+// Allows the ring's dynamic shared memory once per kernel instance.
+void class_prepare(int cls, int stage) {
+  static bool done[4][5] = {};
+  if (done[cls][stage]) return;
+  const size_t sm = class_smem(cls);
+  if (sm) cudaFuncSetAttribute(class_fn(cls, stage), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)sm);
+  done[cls][stage] = true;
+}
+
 int class_grid(int cls, const buff_batch_tune &t, uint32_t nitems) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, class_fn(cls, t.stage), kBT, 0);
+  class_prepare(cls, (int)t.stage);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, class_fn(cls, t.stage), kBT,
+                                                class_smem(cls));
   if (per_sm < 1) per_sm = 1;
   const int bps = (int)t.blocks_per_sm < per_sm ? (int)t.blocks_per_sm : per_sm;
   int grid = bps * dev_sms();
@@ -856,16 +1032,17 @@ cudaError_t batch_launch(const void *d_desc, const uint32_t *d_buf, const BatchS
     if (!sc.items[c]) continue;
     const int grid = class_grid(c, t, sc.items[c]);
     const uint32_t *qi = d_buf + sc.qidx_off[c], *pf = d_buf + sc.prefix_off[c];
+    const size_t sm = class_smem(c);
 #define BQ_LAUNCH(CLS)                                                                          \
   do {                                                                                         \
     if (t.stage == 4)                                                                          \
-      k_bq<CLS, 4><<<grid, kBT, 0, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,         \
+      k_bq<CLS, 4><<<grid, kBT, sm, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,        \
                                         counters + c);                                         \
     else if (t.stage == 2)                                                                     \
-      k_bq<CLS, 2><<<grid, kBT, 0, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,         \
+      k_bq<CLS, 2><<<grid, kBT, sm, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,        \
                                         counters + c);                                         \
     else                                                                                       \
-      k_bq<CLS, 1><<<grid, kBT, 0, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,         \
+      k_bq<CLS, 1><<<grid, kBT, sm, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,        \
                                         counters + c);                                         \
   } while (0)
     switch (c) {
@@ -1410,28 +1587,52 @@ int buff_batch_encode_f64(const double *const *values, const uint64_t *lens,
       d.fl = c->fixed_len;
       d.k = c->k;
       d.r = c->r;
-      const uint32_t ci = (uint32_t)sc.size();
       sc.push_back(d);
       scol.push_back(i);
-      for (uint32_t tt = 0; (uint64_t)tt * sc_tile < c->stride; ++tt) items.push_back(make_uint2(ci, tt));
       // tail padding past the last full 512-row chunk is never written by the scatter
       BCK(cudaMemsetAsync(c->tail + c->stride / 8 * c->r, 0, 64, s));
+    }
+    // items grouped by slice count: one launch per count, compiled for it
+    std::vector<uint32_t> kstart(10, 0);
+    {
+      std::vector<std::vector<uint2>> byk(9);
+      for (uint32_t ci = 0; ci < sc.size(); ++ci)
+        for (uint32_t tt = 0; (uint64_t)tt * sc_tile < sc[ci].stride; ++tt)
+          byk[sc[ci].k].push_back(make_uint2(ci, tt));
+      for (int k = 0; k <= 8; ++k) {
+        kstart[k] = (uint32_t)items.size();
+        items.insert(items.end(), byk[k].begin(), byk[k].end());
+      }
+      kstart[9] = (uint32_t)items.size();
     }
     for (uint32_t i = 0; i < ncols; ++i)
       if (cols[i]) buffh::free_col(cols[i]);
     if (!sc.empty()) {
+      unsigned int *d_cnt9 = nullptr;
       BCK(cudaMallocAsync(reinterpret_cast<void **>(&d_sc), sizeof(ScatCol) * sc.size(), s));
       if (d_items) BCK(cudaFreeAsync(d_items, s));
       d_items = nullptr;
       BCK(cudaMallocAsync(reinterpret_cast<void **>(&d_items), sizeof(uint2) * items.size(), s));
+      BCK(cudaMallocAsync(reinterpret_cast<void **>(&d_cnt9), sizeof(unsigned int) * 9, s));
       BCK(cudaMemcpyAsync(d_sc, sc.data(), sizeof(ScatCol) * sc.size(), cudaMemcpyHostToDevice, s));
       BCK(cudaMemcpyAsync(d_items, items.data(), sizeof(uint2) * items.size(),
                           cudaMemcpyHostToDevice, s));
-      BCK(cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), s));
-      k_benc_scatter<<<grid, kBT, 0, s>>>(d_sc, d_items, (uint32_t)items.size(), sc_tile,
-                                          d_counter);
-      count_launch();
-      BCK(cudaGetLastError());
+      BCK(cudaMemsetAsync(d_cnt9, 0, sizeof(unsigned int) * 9, s));
+      for (int k = 0; k <= 8; ++k) {
+        const uint32_t ni = kstart[k + 1] - kstart[k];
+        if (!ni) continue;
+        int g = grid;
+        if ((uint32_t)g > (ni + kWarps - 1) / kWarps) g = (int)((ni + kWarps - 1) / kWarps);
+        const cudaError_t e =
+            launch_benc_scatter(k, g, d_sc, d_items + kstart[k], ni, sc_tile, d_cnt9 + k, s);
+        count_launch();
+        if (e != cudaSuccess) {
+          cudaFreeAsync(d_cnt9, s);
+          rc = buffh::cuda_status(e);
+          goto done;
+        }
+      }
+      cudaFreeAsync(d_cnt9, s);
       BCK(cudaStreamSynchronize(s));  // the descriptors above live on this stack frame
     }
   }

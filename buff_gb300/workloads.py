@@ -48,6 +48,19 @@ def outlier_column(n: int, seed: int = 3) -> np.ndarray:
     return x
 
 
+def outlier_column_torch(n: int, seed: int = 3, device="cuda"):
+    """outlier_column generated on the device (float64)."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    x = torch.randn(n, generator=g, device=device, dtype=torch.float64) * 5.0 + 100.0
+    m = max(1, n // 100)
+    pos = torch.randperm(n, generator=g, device=device)[:m]
+    x[pos] = (torch.rand(m, generator=g, device=device, dtype=torch.float64) * 2 - 1) * 1e6
+    return torch.round(x * 1e6) / 1e6
+
+
 def bounded_walk_torch(n: int, seed: int = 2, device="cuda"):
     """bounded_walk generated on the device (float64)."""
     import torch
