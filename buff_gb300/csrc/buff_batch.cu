@@ -30,6 +30,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <new>
 #include <vector>
 
@@ -1000,12 +1001,12 @@ size_t class_smem(int cls) {
 
 // Allows the ring's dynamic shared memory once per kernel instance.
 void class_prepare(int cls, int stage) {
-  static bool done[4][5] = {};
-  if (done[cls][stage]) return;
+  static std::atomic<bool> done[4][5];
+  if (done[cls][stage].load(std::memory_order_acquire)) return;
   const size_t sm = class_smem(cls);
   if (sm) cudaFuncSetAttribute(class_fn(cls, stage), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sm);
-  done[cls][stage] = true;
+  done[cls][stage].store(true, std::memory_order_release);  // setting it twice is harmless
 }
 
 int class_grid(int cls, const buff_batch_tune &t, uint32_t nitems) {

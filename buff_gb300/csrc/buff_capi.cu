@@ -10,11 +10,12 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <new>
+#include <vector>
 
 #include "buff_internal.h"
 #include "buff_snappy.h"
-#include <vector>
 
 using buffk::EncStats;
 using buffk::FilterArgs;
@@ -119,15 +120,15 @@ uint64_t serialized_size(const buff_col *c) {
 // threshold is raised once per device so that freed columns stay cached for
 // the next encode/deserialize instead of going back to the driver.
 void init_pool(int device) {
-  static bool done[64] = {false};
-  if (device < 0 || device >= 64 || done[device]) return;
+  static std::atomic<bool> done[64];
+  if (device < 0 || device >= 64 || done[device].load(std::memory_order_acquire)) return;
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
     uint64_t thr = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
   cudaGetLastError();
-  done[device] = true;
+  done[device].store(true, std::memory_order_release);  // setting it twice is harmless
 }
 
 int alloc_col(buff_col *c, cudaStream_t s) {

@@ -771,14 +771,16 @@ int cur_device() {
 }  // namespace
 
 int num_sms(int device) {
-  static int cached[64] = {0};
+  static std::atomic<int> cached[64];
   if (device < 0 || device >= 64) return 1;
-  if (!cached[device]) {
+  int c = cached[device].load(std::memory_order_relaxed);
+  if (!c) {
     int v = 0;
     cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device);
-    cached[device] = v > 0 ? v : 1;
+    c = v > 0 ? v : 1;
+    cached[device].store(c, std::memory_order_relaxed);
   }
-  return cached[device];
+  return c;
 }
 
 void count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
