@@ -39,7 +39,7 @@ EXPORTED = [
     "buff_batch_autotune",
     "buff_server_create", "buff_server_add_column", "buff_server_start", "buff_server_submit",
     "buff_server_poll", "buff_server_release", "buff_server_stop", "buff_server_free",
-    "buff_server_stats", "buff_server_replay", "buff_copy",
+    "buff_server_stats", "buff_server_replay", "buff_copy", "buff_max_range",
 ]
 
 Q_RANGE, Q_EQUAL, Q_SUM, Q_MAX, Q_DECODE = 0x1, 0x2, 0x4, 0x8, 0x10
@@ -187,6 +187,7 @@ def lib(build_if_missing: bool = True):
     L.buff_server_stats.argtypes = [P, P, P, P]
     L.buff_server_replay.argtypes = [P, P, P, C.c_uint32, P, P, P]
     L.buff_copy.argtypes = [P, P, C.c_uint64, P]
+    L.buff_max_range.argtypes = [P, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P]
     L.buff_status_string.argtypes = [C.c_int]
     L.buff_status_string.restype = C.c_char_p
     L.buff_last_cuda_error.restype = C.c_int

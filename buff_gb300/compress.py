@@ -241,6 +241,15 @@ class Column:
             words = words[:nw]
         return FilterResult(words, int(cnt[0]), n)
 
+    def max_range(self, start: int, end: int, window: int, out=None, stream=None):
+        """Maximum of every window of `window` rows in [start, end)."""
+        nwin = (end - start) // window + 1 if window and end >= start else 1
+        dst = out if out is not None else np.empty(max(nwin, 1), dtype=np.float64)
+        cnt = C.c_uint64(0)
+        check(lib().buff_max_range(self._h, start, end, window, ptr(dst), C.byref(cnt),
+                                   stream_handle(stream)), "max_range")
+        return dst[: cnt.value] if out is None else (dst, cnt.value)
+
     def range_filter_decode(self, pred, stream=None):
         """Range filter, then the selected rows' values (one call)."""
         n = self.n
@@ -387,6 +396,10 @@ class SplitBDDoubleCompress:
     # compress/buff_simd.rs:4683-4921 (returns the BitVec<u32>)
     def buff_range_filter_condition(self, data, pred, rows, stream=None) -> FilterResult:
         return _as_column(self, data).range_filter_condition(pred, rows, stream=stream)
+
+    # compress/buff_simd.rs:5096-5334 (the reference prints the count)
+    def buff_max_range(self, data, s: int, e: int, window: int, stream=None):
+        return _as_column(self, data).max_range(s, e, window, stream=stream)
 
     # ---- buff-major (outlier) format --------------------------------
     # compress/buff_simd.rs:317-630

@@ -1611,6 +1611,46 @@ done:
   return rc;
 }
 
+// ---------------------------------------------------------------- windowed max
+
+int buff_max_range(const buff_col *c, uint32_t start, uint32_t end, uint32_t window, double *out,
+                   uint64_t *nout, void *stream) {
+  if (!c || !nout) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;
+  *nout = 0;
+  const bool intended = c->flags & BUFF_FLAG_INTENDED;
+  // the reference divides by the window, reads rows [start, end) and, for
+  // codes wider than a byte, asserts that the windows cover the range exactly
+  if (window == 0 || end < start || end > c->n) return intended ? BUFF_EINVAL : BUFF_EREFPANIC;
+  const uint32_t full = (end - start) / window;
+  const bool ragged = (end - start) % window != 0;
+  if (!intended && c->fixed_len > 8 && (ragged || full == 0)) return BUFF_EREFPANIC;
+  const uint32_t nwin = full + (intended && ragged ? 1u : 0u);
+  if (nwin && !out) return BUFF_EINVAL;
+  const uint32_t hi = intended ? end : start + full * window;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  unsigned long long *codes = nullptr;
+  double *d = nullptr;
+  const bool stage = nwin && !is_device_ptr(out);
+  if (!nwin) return BUFF_OK;
+  CK(scratch(&codes, nwin, s));
+  if (stage)
+    CK(scratch(&d, nwin, s));
+  else
+    d = out;
+  CK(buffk::max_range(c, start, hi, start, window, nwin, codes, d, s));
+  if (stage) {
+    CK(cudaMemcpyAsync(out, d, sizeof(double) * nwin, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  *nout = nwin;
+done:
+  if (codes) cudaFreeAsync(codes, s);
+  if (stage && d) cudaFreeAsync(d, s);
+  return rc;
+}
+
 const char *buff_status_string(int st) {
   switch (st) {
     case BUFF_OK: return "ok";

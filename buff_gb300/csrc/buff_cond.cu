@@ -82,6 +82,102 @@ __global__ void k_check_rows(const uint32_t *__restrict__ rows, uint64_t nrows, 
   }
 }
 
+// ---------------------------------------------------------------- windowed max
+
+struct WinArgs {
+  const uint8_t *slices, *tail;
+  size_t stride;
+  uint32_t k, r, lo, hi, s, w;
+  unsigned long long *codes;  // one per window, zeroed
+};
+
+// The full codes of rows row0..row0+3 (row0 a multiple of 4): 4-byte slice
+// loads and one 4r-bit field group of the tail.
+__device__ __forceinline__ void codes4(const WinArgs &a, uint32_t row0, unsigned long long *c) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) c[i] = 0;
+  for (uint32_t j = 0; j < a.k; ++j) {
+    const uint32_t w = __ldg(reinterpret_cast<const uint32_t *>(a.slices + j * a.stride + row0));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) c[i] = (c[i] << 8) | (((w >> (8 * i)) & 0xFFu) ^ 0x80u);
+  }
+  if (a.r) {
+    const unsigned long long bit = (unsigned long long)row0 * a.r;
+    const uint32_t *tp = reinterpret_cast<const uint32_t *>(a.tail) + (bit >> 5);
+    const uint32_t f = __funnelshift_r(__ldg(tp), __ldg(tp + 1), (uint32_t)(bit & 31));
+    const uint32_t m = (1u << a.r) - 1u;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) c[i] = (c[i] << a.r) | ((f >> (i * a.r)) & m);
+  }
+}
+
+// Per-window maxima of the codes of rows [lo, hi), windows of w rows from s.
+// A warp covers 128 rows per step (lane: 4 rows).  With w >= 128 a step
+// touches at most two windows, reduced across the warp; narrower windows
+// flush each lane's running maximum at every window change.
+template <bool WIDE>
+__global__ void __launch_bounds__(kThreads) k_max_range(WinArgs a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t first = a.lo & ~127u;
+  const uint32_t nsteps = (a.hi - first + 127) / 128;
+  for (uint32_t st = warp; st < nsteps; st += nwarps) {
+    const uint32_t c0 = first + st * 128;
+    const uint32_t row0 = c0 + lane * 4;
+    unsigned long long c[4] = {0, 0, 0, 0};
+    const bool any = row0 < a.hi && row0 + 4 > a.lo;
+    if (any) codes4(a, row0, c);
+    if (WIDE) {
+      const uint32_t wa = ((c0 > a.lo ? c0 : a.lo) - a.s) / a.w;
+      const uint32_t split = a.s + (wa + 1) * a.w;  // first row of window wa + 1
+      unsigned long long ma = 0, mb = 0;
+      bool ha = false, hb = false;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t row = row0 + i;
+        if (!any || row < a.lo || row >= a.hi) continue;
+        if (row < split) {
+          ma = c[i] > ma ? c[i] : ma;
+          ha = true;
+        } else {
+          mb = c[i] > mb ? c[i] : mb;
+          hb = true;
+        }
+      }
+      ma = warp_max_ull(ma);
+      const bool anya = __any_sync(0xFFFFFFFFu, ha);
+      if (lane == 0 && anya) atomicMax(a.codes + wa, ma);
+      if (__any_sync(0xFFFFFFFFu, hb)) {
+        mb = warp_max_ull(mb);
+        if (lane == 0) atomicMax(a.codes + wa + 1, mb);
+      }
+    } else if (any) {
+      uint32_t cur = 0xFFFFFFFFu;
+      unsigned long long m = 0;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t row = row0 + i;
+        if (row < a.lo || row >= a.hi) continue;
+        const uint32_t win = (row - a.s) / a.w;
+        if (win != cur) {
+          if (cur != 0xFFFFFFFFu) atomicMax(a.codes + cur, m);
+          cur = win;
+          m = 0;
+        }
+        m = c[i] > m ? c[i] : m;
+      }
+      if (cur != 0xFFFFFFFFu) atomicMax(a.codes + cur, m);
+    }
+  }
+}
+
+__global__ void k_codes_to_values(const unsigned long long *codes, uint32_t n, long long base,
+                                  int dlen, double *out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = i64_to_f64_scaled((long long)((unsigned long long)base + codes[i]), dlen);
+}
+
 int grid_for_items(uint64_t items) {
   uint64_t g = (items + kThreads - 1) / kThreads;
   int dev = 0;
@@ -115,6 +211,32 @@ cudaError_t decode_rows(const buff_col *c, const uint32_t *rows, uint64_t nrows,
     k_decode_words<<<grid_for_items(c->n), kThreads, 0, s>>>(a, words, rank);
   }
   count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t max_range(const buff_col *c, uint32_t lo, uint32_t hi, uint32_t s, uint32_t w,
+                      uint32_t nwin, unsigned long long *codes, double *out, cudaStream_t st) {
+  WinArgs a;
+  a.slices = c->slices;
+  a.tail = c->tail;
+  a.stride = c->stride;
+  a.k = c->k;
+  a.r = c->r;
+  a.lo = lo;
+  a.hi = hi;
+  a.s = s;
+  a.w = w;
+  a.codes = codes;
+  cudaError_t e = cudaMemsetAsync(codes, 0, sizeof(unsigned long long) * nwin, st);
+  if (e != cudaSuccess || !nwin) return e;
+  const uint64_t steps = (hi - (lo & ~127u) + 127) / 128;
+  const int grid = grid_for_items(steps * 32);
+  if (w >= 128)
+    k_max_range<true><<<grid, kThreads, 0, st>>>(a);
+  else
+    k_max_range<false><<<grid, kThreads, 0, st>>>(a);
+  k_codes_to_values<<<(nwin + 255) / 256, 256, 0, st>>>(codes, nwin, c->base, (int)c->dlen, out);
+  count_launch(2);
   return cudaGetLastError();
 }
 

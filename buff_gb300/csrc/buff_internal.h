@@ -159,6 +159,10 @@ cudaError_t major_decode(const buff_col *c, double *out, cudaStream_t s);
 cudaError_t decode_rows(const buff_col *c, const uint32_t *rows, uint64_t nrows,
                         const uint32_t *words, const uint32_t *rank, int tail_shift, double *out,
                         cudaStream_t s);
+// Maxima of the codes of rows [lo, hi) per window of w rows from s (nwin
+// windows) into codes[] and, as values, out[] (device).
+cudaError_t max_range(const buff_col *c, uint32_t lo, uint32_t hi, uint32_t s, uint32_t w,
+                      uint32_t nwin, unsigned long long *codes, double *out, cudaStream_t st);
 // Sets *bad (device) to 1 unless rows[] is strictly ascending and below n.
 cudaError_t check_rows(const uint32_t *rows, uint64_t nrows, uint32_t n, uint32_t *bad,
                        cudaStream_t s);

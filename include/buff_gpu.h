@@ -242,6 +242,17 @@ int buff_range_filter_majority_condition(const buff_col *col, double pred,
 int buff_range_filter_decode(const buff_col *col, double pred, uint32_t *words, double *out,
                              uint64_t *count, void *stream);
 
+/* buff_max_range (compress/buff_simd.rs:5096-5334): the maximum of every
+ * window of `window` rows in [start, end), as values, into out (host or
+ * device; room for (end - start) / window values); *nout = windows written.
+ * As in the reference a ragged last window is dropped when the code fits one
+ * byte and panics otherwise (BUFF_EREFPANIC), as do window = 0, end < start,
+ * end > n and, for wider codes, a range shorter than one window.  With
+ * BUFF_FLAG_INTENDED the ragged last window is kept and bad ranges return
+ * BUFF_EINVAL. */
+int buff_max_range(const buff_col *col, uint32_t start, uint32_t end, uint32_t window,
+                   double *out, uint64_t *nout, void *stream);
+
 /* ---- batched form (no counterpart in the reference: it runs one column per
  *      call) ---- */
 

@@ -169,6 +169,9 @@ int or_range_filter_condition(const uint8_t *bytes, size_t len, uint64_t scale, 
 int or_range_filter_majority_condition(const uint8_t *bytes, size_t len, uint64_t scale,
                                        double pred, const uint64_t *rows, size_t nrows,
                                        uint32_t *words, uint64_t *count);
+/* buff_max_range: the maxima of the full windows of `window` rows in [s, e). */
+int or_max_range(const uint8_t *bytes, size_t len, uint64_t scale, uint32_t s, uint32_t e,
+                 uint32_t window, double *out, size_t *nout);
 
 #ifdef __cplusplus
 }

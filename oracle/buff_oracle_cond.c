@@ -6,6 +6,7 @@
  *   buff_major_decode_condition        compress/buff_simd.rs:1714-1914
  *   buff_range_filter_condition        compress/buff_simd.rs:4683-4921
  *   buff_range_filter_majority_condition  compress/buff_simd.rs:1279-1526
+ *   buff_max_range                     compress/buff_simd.rs:5096-5334
  *
  * Each walks the byte image with the BitPack reader in the reference's order:
  * per slice, skip to the next listed row, read its byte, skip to the end of
@@ -278,5 +279,198 @@ int or_range_filter_majority_condition(const uint8_t *bytes, size_t len, uint64_
   if (cols > 0) return OR_OK; /* "not implemented yet": the empty res (:1313-1315) */
   int rc = cond_range(&br, &h, scale, pred, rows, nrows, words);
   if (count) *count = count_words(words, nw);
+  return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* buff_max_range (compress/buff_simd.rs:5096-5334): per-window maxima  */
+/* of rows [s, e) in windows of `window` rows, on the buff layout.       */
+/* ------------------------------------------------------------------ */
+
+/* Candidate list with the roaring-style operations the reference uses
+ * (add, remove_range, ascending iteration). */
+typedef struct rows_t {
+  uint32_t *v;
+  size_t n, cap;
+} rows_t;
+
+static int rows_add(rows_t *r, uint32_t x) {
+  if (r->n && r->v[r->n - 1] == x) return OR_OK;
+  if (r->n == r->cap) {
+    size_t nc = r->cap ? 2 * r->cap : 1024;
+    uint32_t *nv = (uint32_t *)realloc(r->v, nc * 4);
+    if (!nv) return OR_ENOMEM;
+    r->v = nv;
+    r->cap = nc;
+  }
+  r->v[r->n++] = x; /* callers add in ascending order */
+  return OR_OK;
+}
+
+/* remove_range(lo .. hi): drops trailing entries in [lo, hi) (entries are
+ * ascending and every later entry is >= hi when this is called). */
+static void rows_remove_tail(rows_t *r, uint32_t lo, uint32_t hi) {
+  while (r->n && r->v[r->n - 1] >= lo && r->v[r->n - 1] < hi) r->n--;
+}
+
+int or_max_range(const uint8_t *bytes, size_t len, uint64_t scale, uint32_t s, uint32_t e,
+                 uint32_t window, double *out, size_t *nout) {
+  (void)scale;
+  or_br br;
+  or_br_init(&br, bytes, len);
+  cond_hdr h;
+  *nout = 0;
+  if (cond_header(&br, &h)) return OR_PANIC;
+  if (window == 0) return OR_PANIC; /* (cur_s - s) / window */
+  uint32_t remain = (uint32_t)h.remain;
+  const double scl = ldexp(1.0, (int)h.dlen);
+  const uint32_t nwin = e >= s ? (e - s) / window : 0;
+  uint64_t *maxv = (uint64_t *)calloc(nwin + 1, 8);
+  size_t nmax = 0;
+  rows_t rb1 = {0, 0, 0}, cur = {0, 0, 0};
+  int rc = OR_OK;
+  if (!maxv) return OR_ENOMEM;
+  if (e < s || e > h.n) { /* read_n_byte / read_bits past the data */
+    rc = OR_PANIC;
+    goto done;
+  }
+  if (remain < 8) {
+    uint64_t mx = 0;
+    uint32_t cur_s = s;
+    if (or_br_skip(&br, (size_t)s * remain)) {
+      rc = OR_PANIC;
+      goto done;
+    }
+    for (uint32_t i = s; i < e; i++) {
+      if (i == cur_s + window) {
+        cur_s = i;
+        maxv[nmax++] = mx;
+        mx = 0;
+      }
+      uint8_t c;
+      if (or_br_read_bits(&br, remain, &c)) {
+        rc = OR_PANIC;
+        goto done;
+      }
+      if (c > mx) mx = c;
+    }
+    if (e == cur_s + window) maxv[nmax++] = mx;
+    goto emit;
+  }
+  remain -= 8;
+  {
+    uint8_t byte_max = 0;
+    uint32_t cur_s = s, i = s;
+    const uint8_t *chunk;
+    or_br_skip_n_byte(&br, s);
+    if (e > s) {
+      if (or_br_read_n_byte(&br, e - s, &chunk)) {
+        rc = OR_PANIC;
+        goto done;
+      }
+    } else {
+      chunk = NULL;
+    }
+    for (; i < e; i++) {
+      uint8_t c = chunk[i - s];
+      if (i == cur_s + window) {
+        cur_s = i;
+        maxv[nmax++] = (uint64_t)byte_max << remain;
+        byte_max = 0;
+      }
+      if (c > byte_max) {
+        byte_max = c;
+        rows_remove_tail(&rb1, cur_s, i);
+        if ((rc = rows_add(&rb1, i))) goto done;
+      } else if (c == byte_max) {
+        if ((rc = rows_add(&rb1, i))) goto done;
+      }
+    }
+    if (i == cur_s + window) maxv[nmax++] = (uint64_t)byte_max << remain;
+    or_br_skip_n_byte(&br, h.n - e);
+  }
+  while (remain > 0) {
+    uint8_t byte_max = 0;
+    uint32_t cur_s = s;
+    const int bytewise = remain >= 8;
+    uint32_t bits;
+    if (bytewise) {
+      remain -= 8;
+      bits = 8;
+    } else {
+      or_br_finish_read_byte(&br);
+      bits = remain;
+    }
+    cur.n = 0;
+    uint32_t pre = 0;
+    for (size_t t = 0; t < rb1.n; t++) {
+      uint32_t dc = rb1.v[t];
+      if (t > 0 && dc >= cur_s + window) {
+        size_t wi = (cur_s - s) / window;
+        if (wi >= nmax) {
+          rc = OR_PANIC; /* max_vec.get_mut(..).unwrap() */
+          goto done;
+        }
+        maxv[wi] |= (uint64_t)byte_max << (bytewise ? remain : 0);
+        byte_max = 0;
+        cur_s += window;
+      }
+      uint8_t d;
+      if (bytewise) {
+        if (t == 0) {
+          if (dc) or_br_skip_n_byte(&br, dc);
+        } else if (dc - pre != 1) {
+          or_br_skip_n_byte(&br, dc - pre - 1);
+        }
+        if (or_br_read_byte(&br, &d)) {
+          rc = OR_PANIC;
+          goto done;
+        }
+      } else {
+        if (t == 0) {
+          if (dc && or_br_skip(&br, (size_t)dc * bits)) {
+            rc = OR_PANIC;
+            goto done;
+          }
+        } else if (dc - pre != 1 && or_br_skip(&br, (size_t)(dc - pre - 1) * bits)) {
+          rc = OR_PANIC;
+          goto done;
+        }
+        if (or_br_read_bits(&br, bits, &d)) {
+          rc = OR_PANIC;
+          goto done;
+        }
+      }
+      if (d > byte_max) {
+        byte_max = d;
+        if (t > 0) rows_remove_tail(&cur, cur_s, dc);
+        if ((rc = rows_add(&cur, dc))) goto done;
+      } else if (d == byte_max) {
+        if ((rc = rows_add(&cur, dc))) goto done;
+      }
+      pre = dc;
+    }
+    /* assert_eq!((cur_s-s)/window+1, (e-s)/window) */
+    if ((cur_s - s) / window + 1 != nwin) {
+      rc = OR_PANIC;
+      goto done;
+    }
+    maxv[(cur_s - s) / window] |= (uint64_t)byte_max << (bytewise ? remain : 0);
+    if (bytewise) {
+      if (rb1.n && h.n - pre > 1) or_br_skip_n_byte(&br, h.n - pre - 1);
+      rows_t tmp = rb1;
+      rb1 = cur;
+      cur = tmp;
+    } else {
+      remain = 0;
+    }
+  }
+emit:
+  for (size_t i = 0; i < nmax; i++) out[i] = (double)(int64_t)((uint64_t)h.base + maxv[i]) / scl;
+  *nout = nmax;
+done:
+  free(maxv);
+  free(rb1.v);
+  free(cur.v);
   return rc;
 }

@@ -95,6 +95,8 @@ def lib():
         L.or_major_decode_condition.argtypes = [P, C.c_size_t, C.c_uint64, P, C.c_size_t, P, P]
         for nm in ("or_range_filter_condition", "or_range_filter_majority_condition"):
             getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, P, C.c_size_t, P, P]
+        L.or_max_range.argtypes = [P, C.c_size_t, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
+                                   P, P]
         L.or_bench_filter_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, C.c_int,
                                           C.c_int, P, P]
         L.or_bench_filter_sum.restype = C.c_double
@@ -421,3 +423,13 @@ def range_filter_condition(buf, scale, pred, rows):
 def range_filter_majority_condition(buf, scale, pred, rows):
     """buff_range_filter_majority_condition (buff_simd.rs:1279-1526)."""
     return _filter_cond(lib().or_range_filter_majority_condition, buf, scale, pred, rows)
+
+
+def max_range(buf, scale, s, e, window):
+    """buff_max_range (buff_simd.rs:5096-5334) on a buff-layout image."""
+    b = _buf(buf)
+    nw = (e - s) // window if (window and e >= s) else 0
+    out = np.zeros(max(nw, 1), dtype=np.float64)
+    n = C.c_size_t(0)
+    _check(lib().or_max_range(_ptr(b), b.size, scale, s, e, window, _ptr(out), C.byref(n)))
+    return out[: n.value]

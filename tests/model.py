@@ -343,3 +343,13 @@ def cond_range(L, pred: float, rows):
         if tup(int(L["codes"][i])) > tt:
             hit[i] = 1
     return bits_to_words(hit)
+
+
+def max_range(L, s, e, w):
+    """Per full window of w rows in [s, e): the largest code, as a value."""
+    codes = [int(c) for c in L["codes"].tolist()]
+    out = []
+    for a in range(s, e - w + 1, w):
+        m = max(codes[a:a + w])
+        out.append(float(wrap64(L["base"] + m)) / 2.0 ** L["dlen"])
+    return np.array(out)

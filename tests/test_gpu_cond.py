@@ -140,3 +140,35 @@ def test_major_condition(oracle, gpu, kind):
         w, c = oracle.range_filter_majority_condition(img, scale, p, rows.astype(np.uint64))
         r = col.range_filter_condition(p, rows)
         assert np.array_equal(r.words, w) and r.count == c
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_max_range(oracle, gpu, case):
+    from buff_gb300 import capi
+    from buff_gb300.compress import FLAG_INTENDED, Column
+
+    name, x, scale = CASES[case]
+    img = oracle.encode(x, scale, flipped=False)
+    col = Column.encode(x, scale)
+    n = x.size
+    fl = oracle.header(img).fixed_len
+    for s, w in ((0, 1000), (13, 128), (5, 3), (0, 1), (100, 4096), (0, n // 3), (31, 200)):
+        if w == 0 or s + w > n:
+            continue
+        e = s + (n - s) // w * w
+        exp = oracle.max_range(img, scale, s, e, w)
+        got = col.max_range(s, e, w)
+        assert np.array_equal(got, exp), (name, s, e, w)
+    e = min(n, 1000 + 37)
+    if fl > 8:
+        with pytest.raises(capi.ReferencePanic):
+            col.max_range(0, e, 100)
+    else:
+        assert np.array_equal(col.max_range(0, e, 100), oracle.max_range(img, scale, 0, e, 100))
+    with pytest.raises(capi.ReferencePanic):
+        col.max_range(0, n + 1, 10)
+    ci = Column.encode(x, scale, FLAG_INTENDED)
+    full = ci.decode()
+    got = ci.max_range(3, e, 100)
+    exp = np.array([full[a:min(a + 100, e)].max() for a in range(3, e, 100)])
+    assert np.array_equal(got, exp)

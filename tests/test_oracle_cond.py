@@ -79,3 +79,24 @@ def test_condition_rejects_unsorted_rows(oracle):
         oracle.decode_condition(buf, 10, [5, 3])
     with pytest.raises(RuntimeError):
         oracle.decode_condition(buf, 10, [5, 100])
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_max_range_vs_model(oracle, case):
+    name, x, scale = cond_cases()[case]
+    buf = oracle.encode(x, scale, flipped=False)
+    L = M.layout(M.fetch_fixed(x, M.precision_exp(M.prec_of_scale(scale)),
+                               M.PRECISION_MAP[M.prec_of_scale(scale)]), scale, False)
+    n = x.size
+    for s, e, w in ((0, n // 100 * 100, 100), (7, 7 + 3 * min(1000, (n - 7) // 3), 3),
+                    (0, n - n % 64, 64), (5, 5 + 512, 512)):
+        got = oracle.max_range(buf, scale, s, e, w)
+        assert np.array_equal(got, M.max_range(L, s, e, w)), (name, s, e, w)
+    # a ragged last window: dropped when the code fits one byte, a panic otherwise
+    if L["fl"] <= 8:
+        assert oracle.max_range(buf, scale, 0, 105, 10).size == 10
+    else:
+        with pytest.raises(oracle.OraclePanic):
+            oracle.max_range(buf, scale, 0, 105, 10)
+    with pytest.raises(oracle.OraclePanic):
+        oracle.max_range(buf, scale, 0, n + 1, 10)
