@@ -762,6 +762,33 @@ def main():
             ops[f"decode_p{p}"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9}
         del out
 
+        # the buff-slice layout of the same column (compress/buff_slice.rs)
+        if not args.free_input:
+            from buff_gb300.compress import SliceColumn
+
+            scol = SliceColumn.encode(x, SCALE, stream=stream)
+            sh_ = scol.handle
+            sbytes = scol.info.k * n
+            p10 = float(torch.quantile(xs, 0.9).item())
+            t = time_op(lambda: L.buff_slice_range_filter(sh_, p10, words.data_ptr(),
+                                                          cnt.data_ptr(), sh), 10, stream)
+            ops["slice_range_0.1"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9}
+            t = time_op(lambda: L.buff_slice_equal_filter(sh_, peq, words.data_ptr(),
+                                                          cnt.data_ptr(), sh), 10, stream)
+            ops["slice_equal"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9}
+            sv = C.c_double(0)
+            t = time_op(lambda: L.buff_slice_sum(sh_, C.byref(sv), sh), 10, stream)
+            ops["slice_sum"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
+                                "gb_s_alg": sbytes / t / 1e9, "note": "synchronizes"}
+            t = time_op(lambda: L.buff_slice_max(sh_, C.byref(sv), None, None, sh), 10, stream)
+            ops["slice_max"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "note": "synchronizes"}
+            out = torch.empty(n, dtype=torch.float64, device="cuda")
+            t = time_op(lambda: L.buff_slice_decode(sh_, out.data_ptr(), sh), 5, stream)
+            ops["slice_decode"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
+                                   "gb_s_alg": (sbytes + 8 * n) / t / 1e9}
+            del out
+            scol.free()
+
         if not args.free_input:
             def enc():
                 c2 = Column.encode(x, SCALE, stream=stream)

@@ -328,6 +328,85 @@ class MajorColumn(Column):
     decode_selected = range_filter_decode = _unsupported
 
 
+class SliceColumn(Column):
+    """A buff-slice column resident in HBM (compress/buff_slice.rs:298-437):
+    ceil(fixed_len/8) byte slices, the last holding the low code bits
+    left-aligned."""
+
+    _ENCODE = ("buff_slice_encode_f32", "buff_slice_encode_f64")
+    _DESERIALIZE = "buff_slice_deserialize"
+
+    def decode(self, out=None, stream=None):
+        dst = out if out is not None else np.empty(max(self.n, 1), dtype=np.float64)
+        check(lib().buff_slice_decode(self._h, ptr(dst), stream_handle(stream)), "decode")
+        return dst[: self.n] if out is None else dst
+
+    def range_filter(self, pred, out=None, stream=None):
+        return self._filter(lib().buff_slice_range_filter, pred, out, stream)
+
+    def equal_filter(self, pred, out=None, stream=None):
+        return self._filter(lib().buff_slice_equal_filter, pred, out, stream)
+
+    def slice_sum(self, any_width: bool = False, stream=None) -> float:
+        v = C.c_double(0)
+        fn = lib().buff_slice_buffsum if any_width else lib().buff_slice_sum
+        check(fn(self._h, C.byref(v), stream_handle(stream)), "slice_sum")
+        return v.value
+
+    def slice_max(self, any_width: bool = False, stream=None):
+        v = C.c_double(0)
+        cnt = C.c_uint64(0)
+        words = np.zeros(max((self.n + 31) // 32, 1), dtype=np.uint32)
+        fn = lib().buff_slice_buffmax if any_width else lib().buff_slice_max
+        check(fn(self._h, C.byref(v), ptr(words), C.byref(cnt), stream_handle(stream)),
+              "slice_max")
+        return MaxResult(v.value, 0, words[: (self.n + 31) // 32], cnt.value)
+
+    def _unsupported(self, *a, **k):
+        raise capi.BuffError(capi.ENOTSUP, "not defined on buff-slice columns")
+
+    sum = max = decode_at_precision = sum_at_precision = _unsupported
+    range_filter_with_slice = equal_filter_with_slice = _unsupported
+    decode_condition = decode_selected = range_filter_condition = _unsupported
+    range_filter_decode = max_range = _unsupported
+
+
+class BuffSliceCompress:
+    """GPU mirror of ``BuffSliceCompress`` (compress/buff_slice.rs:222-296)."""
+
+    def __init__(self, chunksize: int, batchsize: int, scale: int):
+        self.chunksize = chunksize
+        self.batchsize = batchsize
+        self.scale = scale
+
+    def _col(self, data) -> SliceColumn:
+        return data if isinstance(data, SliceColumn) else SliceColumn.deserialize(data, self.scale)
+
+    def buff_slice_encode(self, values, stream=None) -> SliceColumn:
+        return SliceColumn.encode(values, self.scale, 0, stream)
+
+    def buff_slice_decode(self, data, stream=None):
+        return self._col(data).decode(stream=stream)
+
+    def buff_slice_range_filter(self, data, pred, stream=None) -> FilterResult:
+        return self._col(data).range_filter(pred, stream=stream)
+
+    def buff_slice_equal_filter(self, data, pred, stream=None) -> FilterResult:
+        return self._col(data).equal_filter(pred, stream=stream)
+
+    def buff_slice_sum(self, data, stream=None) -> float:
+        return self._col(data).slice_sum(False, stream=stream)
+
+    def buff_slice_buffsum(self, data, stream=None) -> float:
+        return self._col(data).slice_sum(True, stream=stream)
+
+    def buff_slice_max(self, data, stream=None) -> MaxResult:
+        return self._col(data).slice_max(False, stream=stream)
+
+    def buff_slice_buffmax(self, data, stream=None) -> MaxResult:
+        return self._col(data).slice_max(True, stream=stream)
+
+
 def _as_major(comp: "SplitBDDoubleCompress", data) -> MajorColumn:
     if isinstance(data, MajorColumn):
         return data
@@ -435,5 +514,6 @@ class SplitBDDoubleCompress:
         return _as_major(self, data).range_filter_condition(pred, rows, stream=stream)
 
 
-__all__ = ["SplitBDDoubleCompress", "Column", "MajorColumn", "FilterResult", "MaxResult",
+__all__ = ["SplitBDDoubleCompress", "BuffSliceCompress", "Column", "MajorColumn", "SliceColumn",
+           "FilterResult", "MaxResult",
            "FLAG_INTENDED", "FLAG_RAW_BITMAPS", "FLAG_BUFF_LAYOUT", "rows_to_words"]

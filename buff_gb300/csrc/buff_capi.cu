@@ -251,11 +251,22 @@ cudaError_t reduce(const float *x, uint32_t n, uint32_t from, const buff_col *c,
                                          s);
 }
 
+// Slice layout (buff_slice_encode, compress/buff_slice.rs:298-437): every
+// slice byte aligned, the last holding the low code bits left-aligned.
+void set_slice_layout(buff_col *c, uint32_t fl) {
+  c->layout = 2;
+  c->k = fl < 8 ? 1u : (fl + 7) / 8;
+  c->r = 0;
+  c->fixed_len = 8 * c->k;
+  c->pad = c->fixed_len - fl;
+}
+
 template <typename T>
 int encode_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, cudaStream_t s,
-                buff_col **out) {
+                buff_col **out, bool slice = false) {
   if (!out) return BUFF_EINVAL;
   *out = nullptr;
+  if (slice && (flags & BUFF_FLAG_INTENDED)) return BUFF_ENOTSUP;
   if (n64 >= (1ull << 32)) return BUFF_EINVAL;  // the header stores n as u32
   if (n64 > 0 && !values) return BUFF_EINVAL;
   const uint32_t n = (uint32_t)n64;
@@ -326,13 +337,16 @@ int encode_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, c
       const double cl = ceil(log2((double)delta));
       fl = (isnan(cl) || cl <= 0.0) ? 0u : (uint32_t)cl;
     }
-    if (!intended && fl == 0 && n > 0) {
+    if (!intended && !slice && fl == 0 && n > 0) {
       // write_bits(_, 0) indexes one past the buffer (bit_packing.rs:117)
       rc = BUFF_EREFPANIC;
       goto done;
     }
     c->base = mn;
-    set_layout(c, fl);
+    if (slice)
+      set_slice_layout(c, fl);
+    else
+      set_layout(c, fl);
     c->ilen = (uint32_t)((uint64_t)fl - (uint64_t)c->dlen);
     if ((rc = alloc_col(c, s))) goto done;
     if (n > 0) {
@@ -1649,6 +1663,276 @@ done:
   if (codes) cudaFreeAsync(codes, s);
   if (stage && d) cudaFreeAsync(d, s);
   return rc;
+}
+
+// ---------------------------------------------------------------- buff-slice ABI
+
+int buff_slice_encode_f64(const double *values, uint64_t n, uint64_t scale, uint32_t flags,
+                          void *stream, buff_col **out) {
+  return encode_impl<double>(values, n, scale, flags, S(stream), out, true);
+}
+
+int buff_slice_encode_f32(const float *values, uint64_t n, uint64_t scale, uint32_t flags,
+                          void *stream, buff_col **out) {
+  return encode_impl<float>(values, n, scale, flags, S(stream), out, true);
+}
+
+int buff_slice_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                           void *stream, buff_col **out) {
+  if (!out || !bytes) return BUFF_EINVAL;
+  *out = nullptr;
+  if (len < 20) return BUFF_ECORRUPT;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  const bool dev = is_device_ptr(bytes);
+  uint8_t hdr[20];
+  uint32_t w[5];
+  buff_col *c = nullptr;
+  if (dev) {
+    CK(cudaMemcpyAsync(hdr, bytes, 20, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  } else {
+    memcpy(hdr, bytes, 20);
+  }
+  for (int i = 0; i < 5; ++i)
+    w[i] = (uint32_t)hdr[4 * i] | ((uint32_t)hdr[4 * i + 1] << 8) |
+           ((uint32_t)hdr[4 * i + 2] << 16) | ((uint32_t)hdr[4 * i + 3] << 24);
+  c = new_col(scale, flags);
+  if (!c) return BUFF_ENOMEM;
+  c->base = (int64_t)((uint64_t)w[0] | ((uint64_t)w[1] << 32));
+  c->n = w[2];
+  c->ilen = w[3];
+  c->dlen = w[4];
+  {
+    const uint32_t fl = c->ilen + c->dlen;
+    if (fl > 64 || c->dlen > 1000) {
+      rc = BUFF_ECORRUPT;
+      goto done;
+    }
+    set_slice_layout(c, fl);
+    if (20 + (uint64_t)c->k * c->n > len) {
+      rc = BUFF_ECORRUPT;
+      goto done;
+    }
+    if ((rc = alloc_col(c, s))) goto done;
+    if (c->n)
+      CK(cudaMemcpy2DAsync(c->slices, c->stride, bytes + 20, c->n, c->n, c->k, cudaMemcpyDefault,
+                           s));
+    if (c->stride > c->n)
+      CK(cudaMemset2DAsync(c->slices + c->n, c->stride, 0x80, c->stride - c->n, c->k, s));
+    CK(cudaMemsetAsync(c->tail, 0, c->tail_alloc, s));
+    if (!dev) CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (rc != BUFF_OK) {
+    free_col(c);
+    return rc;
+  }
+  *out = c;
+  return BUFF_OK;
+}
+
+int buff_slice_decode(const buff_col *c, double *out, void *stream) {
+  if (!c || (!out && c->n)) return BUFF_EINVAL;
+  if (c->layout != 2) return BUFF_ENOTSUP;
+  if (c->n == 0) return BUFF_OK;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  const bool stage = !is_device_ptr(out) || (reinterpret_cast<uintptr_t>(out) & 15);
+  double *d = stage ? nullptr : out;
+  if (stage) CK(scratch(&d, c->n, s));
+  CK(buffk::launch_decode(c, c->fixed_len, 0, d, s));
+  if (stage) {
+    CK(cudaMemcpyAsync(out, d, (size_t)c->n * 8, cudaMemcpyDefault, s));
+    CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (stage && d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+namespace {
+
+// buff_slice_range_filter / buff_slice_equal_filter (buff_slice.rs:1348-1751):
+// target byte per slice (`t >> (fl - 8(j+1))`, or `t << pad` for the padded
+// last slice), at most 4 slices, rows of full 32-row blocks only; a target
+// below the base prints n for both.
+int slice_filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                      cudaStream_t s, bool is_range) {
+  if (!c || (!words && c->n > 0)) return BUFF_EINVAL;
+  if (c->layout != 2) return BUFF_ENOTSUP;
+  const uint32_t n = c->n, nw = (n + 31) / 32;
+  const uint32_t fl = c->fixed_len - c->pad;
+  int rc = BUFF_OK;
+  uint32_t *dwords = words;
+  unsigned long long *dcount = nullptr;
+  const bool words_host = n > 0 && !is_device_ptr(words);
+  const bool count_host = count && !is_device_ptr(count);
+  const int64_t fp = fetch_fixed_host(pred, c->precision_exp, c->dlen);
+  const bool early = fp < c->base;
+  buffk::FilterArgs a;
+  memset(&a, 0, sizeof(a));
+  if (!early) {
+    if (fl == 0 || n < 32) return BUFF_EREFPANIC;  // ceil(0, 8) / `len - 32` underflow
+    const uint64_t t = (uint64_t)(fp - c->base);
+    a.slices = c->slices;
+    a.stride = c->stride;
+    a.tail = c->tail;
+    a.n = n;
+    a.is_range = is_range ? 1u : 0u;
+    a.k_used = c->k < 4 ? c->k : 4u;
+    a.r = 0;
+    a.full_rows = n / 32 * 32;
+    for (uint32_t j = 0; j < a.k_used; ++j)
+      a.tbyte[j] = (fl >= 8 * (j + 1)) ? (uint8_t)(t >> (fl - 8 * (j + 1)))
+                                       : (uint8_t)(t << ((8 * (j + 1) - fl) & 63));
+  }
+  if (n == 0) {
+    if (count) {
+      if (count_host)
+        *count = 0;
+      else
+        return cuda_status(cudaMemsetAsync(count, 0, sizeof(uint64_t), s));
+    }
+    return BUFF_OK;
+  }
+  if (words_host) CK(scratch(&dwords, nw, s));
+  if (count) {
+    if (count_host)
+      CK(scratch(&dcount, 1, s));
+    else
+      dcount = reinterpret_cast<unsigned long long *>(count);
+    CK(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s));
+  }
+  if (early) {
+    CK(buffk::launch_fill_words(dwords, n, 0xFFFFFFFFu, dcount, s));
+  } else {
+    a.words = dwords;
+    a.count = dcount;
+    CK(buffk::launch_filter(a, s));
+  }
+  if (words_host) CK(cudaMemcpyAsync(words, dwords, (size_t)nw * 4, cudaMemcpyDeviceToHost, s));
+  if (count_host) CK(cudaMemcpyAsync(count, dcount, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  if (words_host || count_host) CK(cudaStreamSynchronize(s));
+done:
+  if (words_host && dwords && dwords != words) cudaFreeAsync(dwords, s);
+  if (count_host && dcount) cudaFreeAsync(dcount, s);
+  return rc;
+}
+
+// True when every partial sum of the values and every value is an exact
+// multiple of 2^-dlen below 2^53 of them: then the reference's sequential
+// f64 sum and its f64 compares are exact, and so is ours.
+bool slice_exact(const buff_col *c) {
+  const uint32_t fl = c->fixed_len - c->pad;
+  const long double top = (long double)c->base + ldexpl(1.0L, (int)fl);
+  const long double lo = (long double)c->base;
+  const long double m = fabsl(top) > fabsl(lo) ? fabsl(top) : fabsl(lo);
+  return m * (long double)(c->n ? c->n : 1) < ldexpl(1.0L, 53);
+}
+
+int slice_sum_impl(const buff_col *c, double *sum, cudaStream_t s, bool any_width) {
+  if (!c || !sum) return BUFF_EINVAL;
+  if (c->layout != 2) return BUFF_ENOTSUP;
+  const uint32_t fl = c->fixed_len - c->pad;
+  if (!any_width && (fl == 0 || c->k > 4)) return BUFF_EREFPANIC;  // buff_slice.rs:1178
+  if (!slice_exact(c)) return BUFF_ENOTSUP;  // the sequential f64 sum would round
+  if (c->n == 0) {
+    *sum = 0.0;
+    return BUFF_OK;
+  }
+  int rc = BUFF_OK;
+  unsigned long long *d = nullptr;
+  uint64_t parts[9] = {0};
+  CK(scratch(&d, 9, s));
+  CK(cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 9, s));
+  CK(buffk::launch_sum(c, c->k, 0, d, s));
+  CK(cudaMemcpyAsync(parts, d, sizeof(parts), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  {
+    // sum of padded codes, the padding shifted out (every padded code is a
+    // multiple of 2^pad, so the division is exact)
+    __int128 acc = 0;
+    for (uint32_t j = 0; j < c->k; ++j) acc += (__int128)parts[j] << (8 * (c->k - 1 - j));
+    acc >>= c->pad;
+    acc += (__int128)c->n * (__int128)c->base;
+    *sum = ldexp((double)(int64_t)acc, -(int)c->dlen);
+  }
+done:
+  if (d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+int slice_max_impl(const buff_col *c, double *max_value, uint32_t *argmax_words,
+                   uint64_t *argmax_count, cudaStream_t s, bool any_width) {
+  if (!c) return BUFF_EINVAL;
+  if (c->layout != 2) return BUFF_ENOTSUP;
+  const uint32_t fl = c->fixed_len - c->pad;
+  if (!any_width && (fl == 0 || c->k > 4)) return BUFF_EREFPANIC;
+  if (!slice_exact(c)) return BUFF_ENOTSUP;  // f64 compares of rounded values
+  const uint32_t nw = (c->n + 31) / 32;
+  int rc = BUFF_OK;
+  unsigned long long *d = nullptr;
+  uint32_t *dwords = nullptr;
+  uint64_t m = 0, cnt = 0;
+  const bool words_dev = argmax_words && is_device_ptr(argmax_words);
+  if (c->n == 0) {  // f64::min_value() and no rows
+    if (max_value) *max_value = -1.7976931348623157e308;
+    if (argmax_count) *argmax_count = 0;
+    return BUFF_OK;
+  }
+  CK(scratch(&d, 2, s));
+  CK(cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), s));
+  CK(buffk::launch_max(c, d, s));
+  if (argmax_words || argmax_count) {
+    if (argmax_words && words_dev)
+      dwords = argmax_words;
+    else
+      CK(scratch(&dwords, nw, s));
+    CK(buffk::launch_argmax(c, d, dwords, d + 1, s));
+    if (argmax_words && !words_dev)
+      CK(cudaMemcpyAsync(argmax_words, dwords, (size_t)nw * 4, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaMemcpyAsync(&m, d, sizeof(m), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&cnt, d + 1, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (max_value)
+    *max_value = (double)(int64_t)((uint64_t)c->base + (m >> c->pad)) / ldexp(1.0, (int)c->dlen);
+  if (argmax_count) *argmax_count = cnt;
+done:
+  if (d) cudaFreeAsync(d, s);
+  if (dwords && !words_dev) cudaFreeAsync(dwords, s);
+  return rc;
+}
+
+}  // namespace
+
+int buff_slice_range_filter(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                            void *stream) {
+  return slice_filter_impl(c, pred, words, count, S(stream), true);
+}
+
+int buff_slice_equal_filter(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                            void *stream) {
+  return slice_filter_impl(c, pred, words, count, S(stream), false);
+}
+
+int buff_slice_sum(const buff_col *c, double *sum, void *stream) {
+  return slice_sum_impl(c, sum, S(stream), false);
+}
+
+int buff_slice_buffsum(const buff_col *c, double *sum, void *stream) {
+  return slice_sum_impl(c, sum, S(stream), true);
+}
+
+int buff_slice_max(const buff_col *c, double *max_value, uint32_t *argmax_words,
+                   uint64_t *argmax_count, void *stream) {
+  return slice_max_impl(c, max_value, argmax_words, argmax_count, S(stream), false);
+}
+
+int buff_slice_buffmax(const buff_col *c, double *max_value, uint32_t *argmax_words,
+                       uint64_t *argmax_count, void *stream) {
+  return slice_max_impl(c, max_value, argmax_words, argmax_count, S(stream), true);
 }
 
 const char *buff_status_string(int st) {

@@ -39,7 +39,8 @@ struct buff_col {
   // buff-major layout (compress/buff_simd.rs:317-630): the first m full bytes
   // are sparse columns (major byte + outlier rows + outlier bytes); `slices`
   // then holds only the k - m dense slices (still flipped on the device).
-  uint32_t layout;      // 0: buff-simd, 1: buff-major
+  uint32_t layout;      // 0: buff-simd, 1: buff-major, 2: buff-slice
+  uint32_t pad;         // buff-slice: zero bits below the code in the last slice
   uint32_t m;           // sparse columns
   uint8_t majors[8];
   uint32_t nout[8];     // outliers per sparse column
@@ -126,7 +127,8 @@ cudaError_t launch_sum(const buff_col *c, uint32_t k_used, uint32_t tail_bits,
 cudaError_t launch_max(const buff_col *c, unsigned long long *d_max, cudaStream_t s);
 cudaError_t launch_argmax(const buff_col *c, const unsigned long long *d_max, uint32_t *words,
                           unsigned long long *count, cudaStream_t s);
-// Decode with `total` leading bits (REF) or masked to `total` bits (INTENDED).
+// Decode with `total` leading bits (REF) or masked to `total` bits (INTENDED);
+// buff-slice columns shift their padding out (c->pad).
 cudaError_t launch_decode(const buff_col *c, uint32_t total, int intended_mask, double *out,
                           cudaStream_t s);
 

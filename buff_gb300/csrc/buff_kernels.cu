@@ -211,7 +211,8 @@ __global__ void __launch_bounds__(kThreads) k_encode_scatter(
         uint32_t hw[E], lw[E];
 #pragma unroll
         for (int j = 0; j < E; ++j) {
-          const unsigned long long a = (c[j] << up) ^ 0x8080808080808080ull;
+          // up == 64 only for an all-zero buff-slice code width: every byte is 0
+          const unsigned long long a = (up >= 64 ? 0ull : (c[j] << up)) ^ 0x8080808080808080ull;
           hw[j] = (uint32_t)(a >> 32);
           lw[j] = (uint32_t)a;
         }
@@ -733,7 +734,7 @@ __global__ void __launch_bounds__(kThreads) k_decode(const uint8_t *__restrict__
                                                      const uint8_t *__restrict__ tail,
                                                      uint32_t ts, uint32_t n, long long base,
                                                      int dlen, unsigned long long keep,
-                                                     double *__restrict__ out) {
+                                                     uint32_t rshift, double *__restrict__ out) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nchunks = (n + kRowChunk - 1) / kRowChunk;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -773,6 +774,8 @@ __global__ void __launch_bounds__(kThreads) k_decode(const uint8_t *__restrict__
         c1 = (c1 << ts) | ((f >> ts) & tmask);
       }
       const uint32_t i0 = r0 + m * 64 + 2 * lane;
+      c0 >>= rshift;
+      c1 >>= rshift;
       const double v0 = i64_to_f64_scaled((long long)((unsigned long long)base + (c0 & keep)), dlen);
       const double v1 = i64_to_f64_scaled((long long)((unsigned long long)base + (c1 & keep)), dlen);
       if (i0 + 2 <= n)
@@ -855,9 +858,11 @@ static cudaError_t scatter_k(const T *x, const buff_col *c, uint8_t *lead, uint3
   int grid = grid_for(fn, kThreads, smem, c->device);
   const int need = (int)((nchunks + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
+  // a buff-slice column's last slice holds the low code bits left-aligned:
+  // shifting by the unpadded width puts them at the top of that byte
   k_encode_scatter<T, K><<<grid, kThreads, smem, s>>>(x, c->n, c->precision_exp, c->dlen, c->base,
-                                                      c->fixed_len, c->r, c->slices, c->stride,
-                                                      c->tail, lead, nlead);
+                                                      c->fixed_len - c->pad, c->r, c->slices,
+                                                      c->stride, c->tail, lead, nlead);
   count_launch();
   return cudaGetLastError();
 }
@@ -962,7 +967,7 @@ static cudaError_t decode_ks(const buff_col *c, uint32_t ts, unsigned long long 
   const int need = (int)((nchunks + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
   k_decode<KS><<<grid, kThreads, 0, s>>>(c->slices, c->stride, c->tail, ts, c->n, c->base,
-                                         (int)c->dlen, keep, out);
+                                         (int)c->dlen, keep, c->pad, out);
   count_launch();
   return cudaGetLastError();
 }

@@ -253,6 +253,40 @@ int buff_range_filter_decode(const buff_col *col, double pred, uint32_t *words, 
 int buff_max_range(const buff_col *col, uint32_t start, uint32_t end, uint32_t window,
                    double *out, uint64_t *nout, void *stream);
 
+/* ---- buff-slice layout (compress/buff_slice.rs) ----
+ * ceil(fixed_len/8) flipped byte slices, the last one holding the low code
+ * bits left-aligned (`code << padding`); no packed tail.  Handles made by
+ * these calls answer only the buff_slice_* queries (and buff_serialize). */
+
+/* buff_slice_encode (buff_slice.rs:298-437); a constant column is allowed. */
+int buff_slice_encode_f64(const double *values, uint64_t n, uint64_t scale, uint32_t flags,
+                          void *stream, buff_col **out);
+int buff_slice_encode_f32(const float *values, uint64_t n, uint64_t scale, uint32_t flags,
+                          void *stream, buff_col **out);
+int buff_slice_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                           void *stream, buff_col **out);
+/* buff_slice_decode (:439-546). */
+int buff_slice_decode(const buff_col *col, double *out, void *stream);
+/* buff_slice_range_filter / buff_slice_equal_filter (:1348-1439, :1665-1751):
+ * at most 4 slices compared, rows of full 32-row blocks only; a target below
+ * the base prints n for both (every row set); fewer than 32 rows panic. */
+int buff_slice_range_filter(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
+                            void *stream);
+int buff_slice_equal_filter(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
+                            void *stream);
+/* buff_slice_sum (:1101-1182, at most 4 slices) and buff_slice_buffsum
+ * (:702-814): the reference adds the decoded values in row order in f64;
+ * the result here is that sum whenever it is exact (every value and partial
+ * sum below 2^53 units of 2^-dlen), else BUFF_ENOTSUP. */
+int buff_slice_sum(const buff_col *col, double *sum, void *stream);
+int buff_slice_buffsum(const buff_col *col, double *sum, void *stream);
+/* buff_slice_max (:816-928, at most 4 slices) and buff_slice_buffmax
+ * (:548-700): the largest value and the rows that reach it. */
+int buff_slice_max(const buff_col *col, double *max_value, uint32_t *argmax_words,
+                   uint64_t *argmax_count, void *stream);
+int buff_slice_buffmax(const buff_col *col, double *max_value, uint32_t *argmax_words,
+                       uint64_t *argmax_count, void *stream);
+
 /* ---- batched form (no counterpart in the reference: it runs one column per
  *      call) ---- */
 

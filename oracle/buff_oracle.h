@@ -173,6 +173,17 @@ int or_range_filter_majority_condition(const uint8_t *bytes, size_t len, uint64_
 int or_max_range(const uint8_t *bytes, size_t len, uint64_t scale, uint32_t s, uint32_t e,
                  uint32_t window, double *out, size_t *nout);
 
+/* --- buff-slice layout: oracle/buff_oracle_slice.c --- */
+int or_slice_encode(const double *x, uint32_t n, uint64_t scale, uint8_t **out, size_t *out_len);
+int or_slice_decode(const uint8_t *bytes, size_t len, uint64_t scale, double *out);
+int or_slice_range_filter(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                          uint32_t *words, uint64_t *count, int *early);
+int or_slice_equal_filter(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                          uint32_t *words, uint64_t *count, int *early);
+int or_slice_sum(const uint8_t *bytes, size_t len, uint64_t scale, int any_width, double *sum);
+int or_slice_max(const uint8_t *bytes, size_t len, uint64_t scale, int any_width, double *maxv,
+                 uint32_t *words, uint64_t *count);
+
 #ifdef __cplusplus
 }
 #endif

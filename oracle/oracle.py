@@ -26,7 +26,8 @@ class OraclePanic(RuntimeError):
 
 def build() -> str:
     srcs = [os.path.join(_HERE, f) for f in ("buff_oracle.c", "buff_oracle_major.c",
-                                             "buff_oracle_cond.c", "buff_oracle.h", "Makefile")]
+                                             "buff_oracle_cond.c", "buff_oracle_slice.c", "buff_oracle.h",
+                                             "Makefile")]
     if (not os.path.exists(_LIB_PATH)) or any(os.path.getmtime(_LIB_PATH) < os.path.getmtime(s)
                                                for s in srcs):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -95,6 +96,13 @@ def lib():
         L.or_major_decode_condition.argtypes = [P, C.c_size_t, C.c_uint64, P, C.c_size_t, P, P]
         for nm in ("or_range_filter_condition", "or_range_filter_majority_condition"):
             getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, P, C.c_size_t, P, P]
+        L.or_slice_encode.argtypes = [P, C.c_uint32, C.c_uint64, C.POINTER(u8p),
+                                      C.POINTER(C.c_size_t)]
+        L.or_slice_decode.argtypes = [P, C.c_size_t, C.c_uint64, P]
+        for nm in ("or_slice_range_filter", "or_slice_equal_filter"):
+            getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, P, P, P]
+        L.or_slice_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P]
+        L.or_slice_max.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P, P, P]
         L.or_max_range.argtypes = [P, C.c_size_t, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                    P, P]
         L.or_bench_filter_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, C.c_int,
@@ -433,3 +441,61 @@ def max_range(buf, scale, s, e, window):
     n = C.c_size_t(0)
     _check(lib().or_max_range(_ptr(b), b.size, scale, s, e, window, _ptr(out), C.byref(n)))
     return out[: n.value]
+
+
+# --- buff-slice layout (buff_oracle_slice.c) --------------------------------
+
+def slice_encode(x, scale: int) -> bytes:
+    """buff_slice_encode (buff_slice.rs:298-437)."""
+    arr = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    out = C.POINTER(C.c_uint8)()
+    ln = C.c_size_t(0)
+    _check(lib().or_slice_encode(_ptr(arr), arr.size, scale, C.byref(out), C.byref(ln)))
+    try:
+        return C.string_at(out, ln.value)
+    finally:
+        lib().or_free(out)
+
+
+def slice_decode(buf, scale):
+    b = _buf(buf)
+    n = header(buf).n
+    out = np.zeros(max(n, 1), dtype=np.float64)
+    _check(lib().or_slice_decode(_ptr(b), b.size, scale, _ptr(out)))
+    return out[:n]
+
+
+def _slice_filter(fn, buf, scale, pred):
+    b = _buf(buf)
+    n = header(buf).n
+    words = np.zeros(max((n + 31) // 32, 1), dtype=np.uint32)
+    cnt = np.zeros(1, dtype=np.uint64)
+    early = np.zeros(1, dtype=np.int32)
+    _check(fn(_ptr(b), b.size, scale, pred, _ptr(words), _ptr(cnt), _ptr(early)))
+    return words[: (n + 31) // 32], int(cnt[0]), bool(early[0])
+
+
+def slice_range_filter(buf, scale, pred):
+    return _slice_filter(lib().or_slice_range_filter, buf, scale, pred)
+
+
+def slice_equal_filter(buf, scale, pred):
+    return _slice_filter(lib().or_slice_equal_filter, buf, scale, pred)
+
+
+def slice_sum(buf, scale, any_width=False):
+    b = _buf(buf)
+    s = np.zeros(1, dtype=np.float64)
+    _check(lib().or_slice_sum(_ptr(b), b.size, scale, 1 if any_width else 0, _ptr(s)))
+    return float(s[0])
+
+
+def slice_max(buf, scale, any_width=False):
+    b = _buf(buf)
+    n = header(buf).n
+    mv = np.zeros(1, dtype=np.float64)
+    words = np.zeros(max((n + 31) // 32, 1), dtype=np.uint32)
+    cnt = np.zeros(1, dtype=np.uint64)
+    _check(lib().or_slice_max(_ptr(b), b.size, scale, 1 if any_width else 0, _ptr(mv),
+                              _ptr(words), _ptr(cnt)))
+    return float(mv[0]), words[: (n + 31) // 32], int(cnt[0])
