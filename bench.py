@@ -750,6 +750,12 @@ def main():
         ops["equal"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "gb_s_alg": filt_bytes / t / 1e9}
         t = time_op(lambda: L.buff_sum_partials_async(h, parts.data_ptr(), sh), 10, stream)
         ops["sum"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "gb_s_alg": sum_bytes / t / 1e9}
+        t = time_op(lambda: L.buff_range_filter_sum(h, pred, words.data_ptr(), cnt.data_ptr(),
+                                                    parts.data_ptr(), sh), 10, stream)
+        ops["range_0.1_and_sum_one_pass"] = {
+            "ms": t * 1e3, "gvalues_s": n / t / 1e9,
+            "gb_s_alg": (sum_bytes + 4 * nw) / t / 1e9,
+            "note": "buff_range_filter_sum: the step's two results from one pass"}
         mx = torch.zeros(1, dtype=torch.int64, device="cuda")
         t = time_op(lambda: L.buff_max_async(h, mx.data_ptr(), sh), 10, stream)
         ops["max"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "gb_s_alg": n / t / 1e9}

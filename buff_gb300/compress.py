@@ -196,6 +196,19 @@ class Column:
         check(lib().buff_sum(self._h, C.byref(res), stream_handle(stream)), "sum")
         return res
 
+    def range_filter_sum(self, pred, stream=None):
+        """Range filter and sum in one pass: (FilterResult, SumResult)."""
+        n = self.n
+        nw = (n + 31) // 32
+        words = np.zeros(max(nw, 1), dtype=np.uint32)
+        cnt = np.zeros(1, dtype=np.uint64)
+        parts = np.zeros(9, dtype=np.uint64)
+        check(lib().buff_range_filter_sum(self._h, float(pred), ptr(words), ptr(cnt), ptr(parts),
+                                          stream_handle(stream)), "range_filter_sum")
+        res = capi.SumResult()
+        check(lib().buff_sum_finish(self._h, parts.ctypes.data, C.byref(res)), "sum_finish")
+        return FilterResult(words[:nw], int(cnt[0]), n), res
+
     # -- row-conditioned reads -------------------------------------------
     _DECODE_CONDITION = "buff_decode_condition"
     _FILTER_CONDITION = "buff_range_filter_condition"

@@ -1092,6 +1092,74 @@ int buff_sum_partials_async(const buff_col *c, uint64_t *dev_partials, void *str
                       S(stream));
 }
 
+int buff_range_filter_sum(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                          uint64_t *partials, void *stream) {
+  if (!c || !partials || (!words && c->n > 0)) return BUFF_EINVAL;
+  if (c->layout != 0) return BUFF_ENOTSUP;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  const uint32_t n = c->n, nw = (n + 31) / 32;
+  const bool intended = c->flags & BUFF_FLAG_INTENDED;
+  const int64_t fp = fetch_fixed_host(pred, c->precision_exp, c->dlen);
+  uint32_t *dwords = words;
+  unsigned long long *dcount = nullptr, *dparts = nullptr;
+  const bool words_host = n > 0 && !is_device_ptr(words);
+  const bool count_host = count && !is_device_ptr(count);
+  const bool parts_host = !is_device_ptr(partials);
+  if (intended || c->k == 0 || fp < c->base || n == 0) {
+    // plans without a single pass: the two calls
+    if ((rc = filter_impl(c, pred, words, count, s, kRange))) return rc;
+    if (parts_host) {
+      buff_sum_result r;
+      if ((rc = buff_sum(c, &r, stream))) return rc;
+      for (uint32_t j = 0; j < 9; ++j) partials[j] = j < r.n_partials ? r.partials[j] : 0;
+      return BUFF_OK;
+    }
+    return sum_partials(c, c->fixed_len, reinterpret_cast<unsigned long long *>(partials), s);
+  }
+  {
+    buffk::FilterArgs a;
+    memset(&a, 0, sizeof(a));
+    const uint64_t t = (uint64_t)(fp - c->base);
+    const uint32_t fl = c->fixed_len;
+    a.slices = c->slices;
+    a.stride = c->stride;
+    a.tail = c->tail;
+    a.n = n;
+    a.is_range = 1;
+    a.full_rows = n / 32 * 32;
+    a.k_used = c->k;
+    a.r = c->r;
+    for (uint32_t j = 0; j < c->k; ++j) a.tbyte[j] = (uint8_t)(t >> (fl - 8 * (j + 1)));
+    a.ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
+    if (words_host) CK(scratch(&dwords, nw, s));
+    if (count) {
+      if (count_host)
+        CK(scratch(&dcount, 1, s));
+      else
+        dcount = reinterpret_cast<unsigned long long *>(count);
+      CK(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s));
+    }
+    if (parts_host)
+      CK(scratch(&dparts, 9, s));
+    else
+      dparts = reinterpret_cast<unsigned long long *>(partials);
+    CK(cudaMemsetAsync(dparts, 0, sizeof(unsigned long long) * 9, s));
+    a.words = dwords;
+    a.count = dcount;
+    CK(buffk::launch_filter_sum(a, c, dparts, s));
+    if (words_host) CK(cudaMemcpyAsync(words, dwords, (size_t)nw * 4, cudaMemcpyDeviceToHost, s));
+    if (count_host) CK(cudaMemcpyAsync(count, dcount, 8, cudaMemcpyDeviceToHost, s));
+    if (parts_host) CK(cudaMemcpyAsync(partials, dparts, 72, cudaMemcpyDeviceToHost, s));
+    if (words_host || count_host || parts_host) CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (words_host && dwords && dwords != words) cudaFreeAsync(dwords, s);
+  if (count_host && dcount) cudaFreeAsync(dcount, s);
+  if (parts_host && dparts) cudaFreeAsync(dparts, s);
+  return rc;
+}
+
 int buff_sum_finish(const buff_col *c, const uint64_t *parts, buff_sum_result *out) {
   if (!c || !parts || !out) return BUFF_EINVAL;
   memset(out, 0, sizeof(*out));

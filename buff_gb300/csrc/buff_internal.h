@@ -124,6 +124,9 @@ cudaError_t launch_fill_words(uint32_t *words, uint32_t n, uint32_t value,
 // fields (tail_bits == 0: no tail).  Slice padding must hold 0x80.
 cudaError_t launch_sum(const buff_col *c, uint32_t k_used, uint32_t tail_bits,
                        unsigned long long *d_partials, cudaStream_t s);
+// Range filter (REF plan in `a`, k >= 1) and the full-width sums in one pass.
+cudaError_t launch_filter_sum(const FilterArgs &a, const buff_col *c,
+                              unsigned long long *d_partials, cudaStream_t s);
 cudaError_t launch_max(const buff_col *c, unsigned long long *d_max, cudaStream_t s);
 cudaError_t launch_argmax(const buff_col *c, const unsigned long long *d_max, uint32_t *words,
                           unsigned long long *count, cudaStream_t s);

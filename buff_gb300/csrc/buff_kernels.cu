@@ -502,6 +502,126 @@ __global__ void __launch_bounds__(kThreads) k_sum(const uint8_t *__restrict__ sl
   if (threadIdx.x == 8 && ts && s_acc[8]) atomicAdd(&partials[ks], s_acc[8]);
 }
 
+// The query pair "range filter, then sum" in one pass (buff_range_filter_sum):
+// k_sum's flat streaming of every slice, with slice 0 read as one 256-bit
+// load per 32-row block -- the block's bitmap word -- so the byte sums and
+// the per-byte SWAR compare with the target share the load.  Candidate
+// blocks are refined through the later slices and the tail (refine32).
+// Rows >= full_rows stay clear (the reference's 32-row SIMD loop).
+template <bool TH>
+__global__ void __launch_bounds__(kThreads) k_filter_sum(FilterArgs a, uint32_t ks, uint32_t ts,
+                                                         unsigned long long tail_bits,
+                                                         unsigned long long *partials) {
+  constexpr int U = 2;  // 32-byte blocks in flight per thread
+  __shared__ unsigned long long s_acc[9];
+  if (threadIdx.x < 9) s_acc[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nth = gridDim.x * blockDim.x;
+  const uint32_t nv = (uint32_t)(a.stride / 16);
+  const uint32_t nblk = (uint32_t)(a.stride / 32);
+  const uint32_t nwords = (a.n + 31) / 32;
+  unsigned long long tb = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) tb |= (unsigned long long)a.tbyte[j] << (8 * j);
+  const uint32_t t0 = (uint32_t)(tb & 0xFFu);
+  const uint32_t lo0 = (t0 & 0x7Fu) * 0x01010101u, lo1 = ((t0 & 0x7Fu) + 1u) * 0x01010101u;
+  const bool deep = a.k_used > 1 || a.r;
+  uint32_t cnt = 0;
+  {
+    uint32_t acc = 0;
+    for (uint32_t b0 = tid; b0 < nblk; b0 += U * nth) {
+      Bytes32 d[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t blk = b0 + u * nth;
+        if (blk < nblk) {
+          d[u] = ld_stream32(a.slices + (size_t)blk * 32);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) d[u].w[q] = H;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t blk = b0 + u * nth;
+        uint32_t me[8], mg[8], eor = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          acc = __dp4a(d[u].w[q] ^ H, 0x01010101u, acc);
+          me[q] = eq4t<TH>(d[u].w[q], lo0, lo1);
+          mg[q] = gt4t<TH>(d[u].w[q], lo1);
+          eor |= me[q];
+        }
+        if (blk >= nwords) continue;  // padding blocks: summed (zero bytes), never filtered
+        uint32_t eq = eor ? gather32(me) : 0u;
+        uint32_t gt = gather32(mg);
+        const uint32_t row0 = blk * 32;
+        if (eq && deep)
+          refine32(a.slices, a.stride, a.k_used, tb, a.tail, a.r, a.ttail, row0, gt, eq);
+        if (row0 + 32 > a.full_rows) {
+          const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
+          gt &= lim >= 32 ? 0xFFFFFFFFu : ((1u << lim) - 1u);
+        }
+        __stcs(a.words + blk, gt);
+        cnt += __popc(gt);
+      }
+    }
+    const unsigned long long w = warp_sum_ull(acc);
+    if (lane == 0 && w) atomicAdd(&s_acc[0], w);
+  }
+  for (uint32_t s = 1; s < ks; ++s) {
+    const uint8_t *sl = a.slices + (size_t)s * a.stride;
+    uint32_t acc = 0;
+    for (uint32_t v0 = tid; v0 < nv; v0 += kU * nth) {
+      uint4 d[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const uint32_t v = v0 + u * nth;
+        d[u] = v < nv ? ld_stream(sl + (size_t)v * 16) : make_uint4(H, H, H, H);
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        acc = __dp4a(d[u].x ^ H, 0x01010101u, acc);
+        acc = __dp4a(d[u].y ^ H, 0x01010101u, acc);
+        acc = __dp4a(d[u].z ^ H, 0x01010101u, acc);
+        acc = __dp4a(d[u].w ^ H, 0x01010101u, acc);
+      }
+    }
+    const unsigned long long w = warp_sum_ull(acc);
+    if (lane == 0 && w) atomicAdd(&s_acc[s], w);
+  }
+  if (ts) {
+    const unsigned long long nbytes = (tail_bits + 7) / 8;
+    const uint32_t ntv = (uint32_t)((nbytes + 15) / 16);
+    unsigned long long acc = 0;
+    for (uint32_t v = tid; v < ntv; v += nth) {
+      uint4 d = *reinterpret_cast<const uint4 *>(a.tail + (size_t)v * 16);
+      const uint32_t *w = reinterpret_cast<const uint32_t *>(&d);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const unsigned long long b0 = (unsigned long long)v * 128 + 32 * q;
+        uint32_t word = w[q];
+        if (b0 >= tail_bits)
+          word = 0;
+        else if (b0 + 32 > tail_bits)
+          word &= (1u << (uint32_t)(tail_bits - b0)) - 1u;
+        acc += wpopc(word, (uint32_t)(b0 % ts), ts);
+      }
+    }
+    acc = warp_sum_ull(acc);
+    if (lane == 0 && acc) atomicAdd(&s_acc[8], acc);
+  }
+  if (a.count) {
+    const unsigned long long c = warp_sum_ull(cnt);
+    if (lane == 0 && c) atomicAdd(a.count, c);
+  }
+  __syncthreads();
+  if (threadIdx.x < ks && s_acc[threadIdx.x]) atomicAdd(&partials[threadIdx.x], s_acc[threadIdx.x]);
+  if (threadIdx.x == 8 && ts && s_acc[8]) atomicAdd(&partials[ks], s_acc[8]);
+}
+
 // ---------------------------------------------------------------- max
 
 
@@ -930,6 +1050,25 @@ cudaError_t launch_sum(const buff_col *c, uint32_t k_used, uint32_t tail_bits,
   if (grid < 1) grid = 1;
   k_sum<<<grid, kThreads, 0, s>>>(c->slices, c->stride, k_used, c->tail, tail_bits,
                                   (unsigned long long)c->n * tail_bits, d_partials);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_filter_sum(const FilterArgs &a, const buff_col *c,
+                              unsigned long long *d_partials, cudaStream_t s) {
+  if (c->n == 0) return cudaSuccess;
+  const bool th = a.tbyte[0] & 0x80u;
+  const void *fn = th ? (const void *)k_filter_sum<true> : (const void *)k_filter_sum<false>;
+  int grid = grid_for(fn, kThreads, 0, c->device);
+  const size_t nv = c->stride / 16;
+  const int need = (int)((nv + kThreads - 1) / kThreads);
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  const unsigned long long tb = (unsigned long long)c->n * c->r;
+  if (th)
+    k_filter_sum<true><<<grid, kThreads, 0, s>>>(a, c->k, c->r, tb, d_partials);
+  else
+    k_filter_sum<false><<<grid, kThreads, 0, s>>>(a, c->k, c->r, tb, d_partials);
   count_launch();
   return cudaGetLastError();
 }

@@ -165,6 +165,12 @@ int buff_sum_at_precision(const buff_col *col, uint32_t precision, double *out, 
  * of those partials into the reference's f64 result. */
 int buff_sum_partials_async(const buff_col *col, uint64_t *dev_partials, void *stream);
 int buff_sum_finish(const buff_col *col, const uint64_t *host_partials, buff_sum_result *out);
+/* No counterpart in the reference (it reads the column once per call): the
+ * bitmap and count of buff_range_filter and the partial sums of
+ * buff_sum_partials_async, from one pass over the slices.  partials: 9
+ * u64 (device or host); buff_sum_finish turns them into the sum. */
+int buff_range_filter_sum(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
+                          uint64_t *partials, void *stream);
 
 /* SplitBDDoubleCompress::byte_fixed_max (compress/split_double.rs:3919-4105):
  * the column maximum, its code, and optionally the arg-max bitmap and its

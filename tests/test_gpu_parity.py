@@ -113,6 +113,13 @@ def test_column_parity(gpu, oracle, kind, n, scale, intended):
     s, parts, exact = oracle.buff_sum(ref, scale, True, intended)
     r = col.sum()
     assert r.sum == s or (np.isnan(r.sum) and np.isnan(s))
+    # the range filter and the sum from one pass
+    for p in _pred_list(x):
+        w, c, _ = oracle.range_filter(ref, scale, p, intended)
+        fr, fs = col.range_filter_sum(p)
+        assert words_equal(fr.words, w) and fr.count == c, ("one pass", p)
+        assert fs.sum == s or (np.isnan(fs.sum) and np.isnan(s))
+        assert fs.exact_num == exact
     assert list(r.partials[: r.n_partials]) == parts
     assert r.exact_num == exact
     # max (+ arg-max bitmap)
@@ -304,4 +311,7 @@ def test_full_size_properties(gpu):
         assert e.count == int(((q - base) == t).sum().item())
     s = col.sum()
     assert s.exact_num == int(q.sum().item())
+    fr, fs = col.range_filter_sum(p)
+    assert fr.count == g.count and np.array_equal(fr.words, g.words)
+    assert fs.exact_num == s.exact_num and fs.sum == s.sum
     assert col.max().code == int(q.max().item()) - base
