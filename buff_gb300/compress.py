@@ -375,13 +375,24 @@ class SliceColumn(Column):
               "slice_max")
         return MaxResult(v.value, 0, words[: (self.n + 31) // 32], cnt.value)
 
+    def max_range(self, start: int, end: int, window: int, out=None, stream=None):
+        """Maximum of every window of `window` rows in [start, end)
+        (buff_slice_max_range)."""
+        hi = min(end, self.n)
+        nwin = (hi - start + window - 1) // window + 1 if window and hi > start else 1
+        dst = out if out is not None else np.empty(nwin, dtype=np.float64)
+        cnt = C.c_uint64(0)
+        check(lib().buff_slice_max_range(self._h, start, end, window, ptr(dst), C.byref(cnt),
+                                         stream_handle(stream)), "slice_max_range")
+        return dst[: cnt.value] if out is None else (dst, cnt.value)
+
     def _unsupported(self, *a, **k):
         raise capi.BuffError(capi.ENOTSUP, "not defined on buff-slice columns")
 
     sum = max = decode_at_precision = sum_at_precision = _unsupported
     range_filter_with_slice = equal_filter_with_slice = _unsupported
     decode_condition = decode_selected = range_filter_condition = _unsupported
-    range_filter_decode = max_range = _unsupported
+    range_filter_decode = _unsupported
 
 
 class BuffSliceCompress:
@@ -418,6 +429,9 @@ class BuffSliceCompress:
 
     def buff_slice_buffmax(self, data, stream=None) -> MaxResult:
         return self._col(data).slice_max(True, stream=stream)
+
+    def buff_slice_max_range(self, data, s: int, e: int, window: int, stream=None):
+        return self._col(data).max_range(s, e, window, stream=stream)
 
 
 def _as_major(comp: "SplitBDDoubleCompress", data) -> MajorColumn:

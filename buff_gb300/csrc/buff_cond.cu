@@ -172,10 +172,15 @@ __global__ void __launch_bounds__(kThreads) k_max_range(WinArgs a) {
   }
 }
 
+// Window maxima as values.  `shift` drops the right padding of a buff-slice
+// code; `empty` marks windows that read no row (f64::min_value()).
 __global__ void k_codes_to_values(const unsigned long long *codes, uint32_t n, long long base,
-                                  int dlen, double *out) {
+                                  int dlen, uint32_t shift, uint32_t empty_from, double *out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = i64_to_f64_scaled((long long)((unsigned long long)base + codes[i]), dlen);
+  if (i >= n) return;
+  out[i] = i >= empty_from
+               ? -1.7976931348623157e308
+               : i64_to_f64_scaled((long long)((unsigned long long)base + (codes[i] >> shift)), dlen);
 }
 
 int grid_for_items(uint64_t items) {
@@ -215,7 +220,8 @@ cudaError_t decode_rows(const buff_col *c, const uint32_t *rows, uint64_t nrows,
 }
 
 cudaError_t max_range(const buff_col *c, uint32_t lo, uint32_t hi, uint32_t s, uint32_t w,
-                      uint32_t nwin, unsigned long long *codes, double *out, cudaStream_t st) {
+                      uint32_t nwin, unsigned long long *codes, double *out, cudaStream_t st,
+                      uint32_t shift, uint32_t empty_from) {
   WinArgs a;
   a.slices = c->slices;
   a.tail = c->tail;
@@ -229,14 +235,18 @@ cudaError_t max_range(const buff_col *c, uint32_t lo, uint32_t hi, uint32_t s, u
   a.codes = codes;
   cudaError_t e = cudaMemsetAsync(codes, 0, sizeof(unsigned long long) * nwin, st);
   if (e != cudaSuccess || !nwin) return e;
-  const uint64_t steps = (hi - (lo & ~127u) + 127) / 128;
-  const int grid = grid_for_items(steps * 32);
-  if (w >= 128)
-    k_max_range<true><<<grid, kThreads, 0, st>>>(a);
-  else
-    k_max_range<false><<<grid, kThreads, 0, st>>>(a);
-  k_codes_to_values<<<(nwin + 255) / 256, 256, 0, st>>>(codes, nwin, c->base, (int)c->dlen, out);
-  count_launch(2);
+  if (hi > lo) {
+    const uint64_t steps = (hi - (lo & ~127u) + 127) / 128;
+    const int grid = grid_for_items(steps * 32);
+    if (w >= 128)
+      k_max_range<true><<<grid, kThreads, 0, st>>>(a);
+    else
+      k_max_range<false><<<grid, kThreads, 0, st>>>(a);
+    count_launch();
+  }
+  k_codes_to_values<<<(nwin + 255) / 256, 256, 0, st>>>(codes, nwin, c->base, (int)c->dlen, shift,
+                                                         empty_from, out);
+  count_launch();
   return cudaGetLastError();
 }
 

@@ -167,7 +167,8 @@ cudaError_t decode_rows(const buff_col *c, const uint32_t *rows, uint64_t nrows,
 // Maxima of the codes of rows [lo, hi) per window of w rows from s (nwin
 // windows) into codes[] and, as values, out[] (device).
 cudaError_t max_range(const buff_col *c, uint32_t lo, uint32_t hi, uint32_t s, uint32_t w,
-                      uint32_t nwin, unsigned long long *codes, double *out, cudaStream_t st);
+                      uint32_t nwin, unsigned long long *codes, double *out, cudaStream_t st,
+                      uint32_t shift = 0, uint32_t empty_from = 0xFFFFFFFFu);
 // Sets *bad (device) to 1 unless rows[] is strictly ascending and below n.
 cudaError_t check_rows(const uint32_t *rows, uint64_t nrows, uint32_t n, uint32_t *bad,
                        cudaStream_t s);

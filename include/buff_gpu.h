@@ -292,6 +292,18 @@ int buff_slice_max(const buff_col *col, double *max_value, uint32_t *argmax_word
                    uint64_t *argmax_count, void *stream);
 int buff_slice_buffmax(const buff_col *col, double *max_value, uint32_t *argmax_words,
                        uint64_t *argmax_count, void *stream);
+/* buff_slice_max_range (:930-1099): the maximum of every window of `window`
+ * rows in [start, end), as values, into out (host or device; room for
+ * ceil((min(end, n) - start) / window) values, at least 1); *nout = windows
+ * written.  As in the reference, rows past n are not read, and the call
+ * panics (BUFF_EREFPANIC) unless the windows it started number
+ * (end - start) / window (u32): a ragged last window panics unless end runs
+ * past the rows; widths above 32 bits and window = 0 panic too.  When no row
+ * is read the one window holds f64::min_value().  With BUFF_FLAG_INTENDED any
+ * width is accepted, the ragged last window is kept and bad ranges return
+ * BUFF_EINVAL. */
+int buff_slice_max_range(const buff_col *col, uint32_t start, uint32_t end, uint32_t window,
+                         double *out, uint64_t *nout, void *stream);
 
 /* ---- batched form (no counterpart in the reference: it runs one column per
  *      call) ---- */

@@ -183,6 +183,9 @@ int or_slice_equal_filter(const uint8_t *bytes, size_t len, uint64_t scale, doub
 int or_slice_sum(const uint8_t *bytes, size_t len, uint64_t scale, int any_width, double *sum);
 int or_slice_max(const uint8_t *bytes, size_t len, uint64_t scale, int any_width, double *maxv,
                  uint32_t *words, uint64_t *count);
+/* buff_slice_max_range: per-window maxima of rows [s, e); out has room for cap values. */
+int or_slice_max_range(const uint8_t *b, size_t len, uint64_t scale, uint32_t s, uint32_t e,
+                       uint32_t window, double *out, size_t cap, size_t *nout);
 
 #ifdef __cplusplus
 }

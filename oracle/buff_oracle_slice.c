@@ -14,6 +14,7 @@
  *   buff_slice_buffsum         :702-814     (sequential f64 sum, any width)
  *   buff_slice_max             :816-928     (f64 max + arg-max rows, at most 4 slices)
  *   buff_slice_buffmax         :548-700     (f64 max + arg-max rows, any width)
+ *   buff_slice_max_range       :930-1099    (per-window f64 maxima, at most 4 slices)
  */
 #include <float.h>
 #include <math.h>
@@ -224,4 +225,42 @@ int or_slice_max(const uint8_t *b, size_t len, uint64_t scale, int any_width, do
   *maxv = m;
   *count = c;
   return OR_OK;
+}
+
+/* Per-window maxima of the decoded values of rows [s, e), windows of
+ * `window` rows starting at s (buff_slice.rs:930-1099).  The row loop runs
+ * over all n rows and stops at e, so rows past n are never read; a window
+ * closes when the row index reaches cur_s + window; the last window's
+ * maximum is pushed after the loop (f64::min_value() if no row was read).
+ * Then `assert_eq!((cur_s - s) / window + 1, (e - s) / window)` in u32:
+ * a ragged last window panics unless e runs past the rows.  The arg-max
+ * bitmap the reference keeps is never read, so it is not built here. */
+int or_slice_max_range(const uint8_t *b, size_t len, uint64_t scale, uint32_t s, uint32_t e,
+                       uint32_t window, double *out, size_t cap, size_t *nout) {
+  (void)scale;
+  slice_hdr h;
+  *nout = 0;
+  if (slice_header(b, len, &h)) return OR_PANIC;
+  if (h.fl == 0 || h.num > 4) return OR_PANIC; /* `_ => panic!("bit length greater than 32 ...")` */
+  if (window == 0) return OR_PANIC;             /* the final assert divides by the window */
+  double m = -DBL_MAX;
+  uint32_t cur_s = s;
+  size_t k = 0;
+  for (uint32_t i = 0; i < h.n; i++) {
+    if (i < s) continue;
+    if (i >= e) break;
+    if ((uint64_t)i == (uint64_t)cur_s + window) {
+      if (k < cap) out[k] = m;
+      k++;
+      m = -DBL_MAX;
+      cur_s = i;
+    }
+    double f = slice_value(&h, slice_code(b, &h, i));
+    if (f > m) m = f;
+  }
+  if ((cur_s - s) / window + 1 != (uint32_t)(e - s) / window) return OR_PANIC;
+  if (k < cap) out[k] = m;
+  k++;
+  *nout = k;
+  return k <= cap ? OR_OK : OR_EINVAL;
 }

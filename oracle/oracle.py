@@ -103,6 +103,8 @@ def lib():
             getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, P, P, P]
         L.or_slice_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P]
         L.or_slice_max.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P, P, P]
+        L.or_slice_max_range.argtypes = [P, C.c_size_t, C.c_uint64, C.c_uint32, C.c_uint32,
+                                         C.c_uint32, P, C.c_size_t, P]
         L.or_max_range.argtypes = [P, C.c_size_t, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                    P, P]
         L.or_bench_filter_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, C.c_int,
@@ -499,3 +501,15 @@ def slice_max(buf, scale, any_width=False):
     _check(lib().or_slice_max(_ptr(b), b.size, scale, 1 if any_width else 0, _ptr(mv),
                               _ptr(words), _ptr(cnt)))
     return float(mv[0]), words[: (n + 31) // 32], int(cnt[0])
+
+
+def slice_max_range(buf, scale, s, e, window):
+    """buff_slice_max_range (buff_slice.rs:930-1099): per-window maxima."""
+    b = _buf(buf)
+    n = header(buf).n
+    cap = (min(e, n) - s + window - 1) // window + 1 if (window and min(e, n) > s) else 1
+    out = np.zeros(cap, dtype=np.float64)
+    k = C.c_size_t(0)
+    _check(lib().or_slice_max_range(_ptr(b), b.size, scale, s, e, window, _ptr(out), cap,
+                                    C.byref(k)))
+    return out[: k.value]

@@ -83,3 +83,37 @@ def test_slice_rejects_other_calls(gpu):
     plain = Column.encode(x, 100)
     with pytest.raises(capi.BuffError):
         SliceColumn.decode(plain)
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_slice_max_range(oracle, gpu, case):
+    from buff_gb300 import capi
+    from buff_gb300.compress import FLAG_INTENDED, SliceColumn
+
+    name, x, scale = CASES[case]
+    xd = x.astype(np.float64)
+    img = oracle.slice_encode(xd, scale)
+    col = SliceColumn.encode(x, scale)
+    n = xd.size
+    windows = [(0, 1000, 100), (13, 13 + 128 * 7, 128), (5, 8, 3), (0, n, 1), (31, 231, 200),
+               (0, n // 3, 7), (0, n // 1000 * 1000, 1000), (n - 50, n + 50, 100),
+               (n - 50, n + 150, 100), (n + 5, n + 105, 100), (10, 5, 3), (0, 100, 0),
+               (7, 7 + 3 * 64 + 1, 64), (12345, 12345 + 97 * 333, 333)]
+    for s, e, w in windows:
+        if s > n and e <= n:
+            continue
+        try:
+            exp = oracle.slice_max_range(img, scale, s, e, w)
+        except oracle.OraclePanic:
+            with pytest.raises(capi.ReferencePanic):
+                col.max_range(s, e, w)
+            continue
+        assert np.array_equal(col.max_range(s, e, w), exp), (name, s, e, w)
+    ci = SliceColumn.encode(x, scale, FLAG_INTENDED)
+    vals = ci.decode()
+    e = min(n, 1037)
+    got = ci.max_range(3, e, 100)
+    assert np.array_equal(got, np.array([vals[a:min(a + 100, e)].max() for a in range(3, e, 100)]))
+    with pytest.raises(capi.BuffError) as err:
+        ci.max_range(0, n + 1, 10)
+    assert err.value.status == capi.EINVAL

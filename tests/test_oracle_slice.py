@@ -62,3 +62,41 @@ def test_slice_layout_vs_model(oracle, case):
         eq = np.array([key(c) == tk and i < full for i, c in enumerate(codes)], dtype=np.uint8)
         assert np.array_equal(wr, M.bits_to_words(gt)), (name, p)
         assert np.array_equal(we, M.bits_to_words(eq)), (name, p)
+
+
+def _model_max_range(vals, n, fl, num, s, e, w):
+    """Window maxima as buff_slice.rs:930-1099 states them; None = panic."""
+    if fl == 0 or num > 4 or w == 0:
+        return None
+    hi = min(e, n)
+    if hi > s:
+        nwin = -(-(hi - s) // w)
+        out = [vals[s + j * w: min(s + (j + 1) * w, hi)].max() for j in range(nwin)]
+    else:
+        nwin, out = 1, [-np.finfo(np.float64).max]
+    if nwin != ((e - s) % 2**32) // w:
+        return None
+    return np.array(out)
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_slice_max_range_vs_model(oracle, case):
+    name, x, scale = cond_cases()[case]
+    buf = oracle.slice_encode(x, scale)
+    h = oracle.header(buf)
+    fl = h.fixed_len
+    num = 1 if fl < 8 else (fl + 7) // 8
+    vals = oracle.slice_decode(buf, scale)
+    n = x.size
+    windows = [(0, 1000, 100), (13, 13 + 128 * 7, 128), (5, 8, 3), (0, n, 1), (31, 31 + 200, 200),
+               (0, n // 3, 7), (0, n, 100), (n - 50, n + 50, 100), (n - 50, n + 150, 100),
+               (n + 5, n + 105, 100), (n + 5, n + 5, 10), (10, 5, 3), (0, 100, 0),
+               (7, 7 + 3 * 64 + 1, 64)]
+    for s, e, w in windows:
+        exp = _model_max_range(vals, n, fl, num, s, e, w)
+        if exp is None:
+            with pytest.raises(oracle.OraclePanic):
+                oracle.slice_max_range(buf, scale, s, e, w)
+        else:
+            got = oracle.slice_max_range(buf, scale, s, e, w)
+            assert np.array_equal(got, exp), (name, s, e, w)
