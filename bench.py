@@ -184,6 +184,38 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def host_cpu() -> dict:
+    """The host the CPU baseline ran on: architecture, CPU model, logical CPUs."""
+    import platform
+
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                key = ln.split(":", 1)[0].strip().lower()
+                if key in ("model name", "cpu model"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if model is None:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for ln in out.splitlines():
+                if ln.lower().startswith("model name"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    return {"machine": platform.machine(), "cpu_model": model or platform.processor() or None,
+            "logical_cpus": os.cpu_count()}
+
+
+def mib_s(rows: float, seconds: float) -> float:
+    """The reference's own throughput unit: MiB/s of the f64 input (8 bytes a row)."""
+    return rows * 8 / (1 << 20) / seconds
+
+
 def cpu_reference_line(args, x_sample: np.ndarray, pred: float, threads: int, steps: int,
                        warmup: int):
     """Times the oracle's filter+sum (the reference algorithm) on host cores."""
@@ -223,7 +255,8 @@ def run_reference(args, rank, world):
         "config": {"workload": f"bounded_walk f64 scale 1e4, sample of {rows} rows of the "
                                f"{N_ROWS}-row column", "rows": rows, "selectivity": SELECTIVITY},
         "cpu_baseline": {"value": v, "unit": "Gvalues/s", "cores": threads, "kind": "port",
-                         "sample": f"{rows} rows, {args.steps} timed passes of filter+sum"},
+                         "sample": f"{rows} rows, {args.steps} timed passes of filter+sum",
+                         "mib_s": mib_s(rows, per_step), "host": host_cpu()},
         "e2e": {"value": v, "unit": "Gvalues/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -810,7 +843,7 @@ def main():
         per_step, rows, _, _ = cpu_reference_line(args, xs, pred, 1, 3, 1)
         cpu = {"value": rows / per_step / 1e9, "unit": "Gvalues/s", "cores": 1, "kind": "port",
                "sample": f"first {rows} rows of the column, 3 timed passes of filter+sum, "
-                         f"1 thread"}
+                         f"1 thread", "mib_s": mib_s(rows, per_step), "host": host_cpu()}
 
     batched_form = serving_form = outlier_form = None
     if rank == 0 and world == 1:
@@ -831,6 +864,7 @@ def main():
         line = {
             "metric": "filter+sum throughput (range filter 10% then sum)",
             "value": world * n / t_step / 1e9, "unit": "Gvalues/s", "n_gpus": world,
+            "value_mib_s": mib_s(world * n, t_step),
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
             "data": "synthetic",

@@ -2008,29 +2008,21 @@ int buff_slice_max_range(const buff_col *c, uint32_t start, uint32_t end, uint32
   if (!c || !nout) return BUFF_EINVAL;
   if (c->layout != 2) return BUFF_ENOTSUP;
   *nout = 0;
-  const bool intended = c->flags & BUFF_FLAG_INTENDED;
   const uint32_t fl = c->fixed_len - c->pad;
   const uint32_t n = c->n;
   uint32_t hi, nwin, empty_from = 0xFFFFFFFFu;
-  if (intended) {
-    if (window == 0 || end < start || end > n) return BUFF_EINVAL;
-    hi = end;
-    nwin = (uint32_t)(((uint64_t)end - start + window - 1) / window);
+  // buff_slice.rs:930-1099: widths 1..32 bits only; rows [start, min(end, n))
+  // read; then assert_eq!((cur_s - s) / window + 1, (e - s) / window) in u32
+  if (fl == 0 || c->k > 4 || window == 0) return BUFF_EREFPANIC;
+  hi = end < n ? end : n;
+  if (hi > start) {
+    nwin = (uint32_t)(((uint64_t)hi - start + window - 1) / window);
   } else {
-    // buff_slice.rs:930-1099: widths 1..32 bits only; rows [start, min(end, n))
-    // read; then assert_eq!((cur_s - s) / window + 1, (e - s) / window) in u32
-    if (fl == 0 || c->k > 4 || window == 0) return BUFF_EREFPANIC;
-    hi = end < n ? end : n;
-    if (hi > start) {
-      nwin = (uint32_t)(((uint64_t)hi - start + window - 1) / window);
-    } else {
-      nwin = 1;  // no row read: the pushed maximum is f64::min_value()
-      empty_from = 0;
-      hi = start;
-    }
-    if (nwin != (uint32_t)(end - start) / window) return BUFF_EREFPANIC;
+    nwin = 1;  // no row read: the pushed maximum is f64::min_value()
+    empty_from = 0;
+    hi = start;
   }
-  if (!nwin) return BUFF_OK;
+  if (nwin != (uint32_t)(end - start) / window) return BUFF_EREFPANIC;
   if (!out) return BUFF_EINVAL;
   cudaStream_t s = S(stream);
   int rc = BUFF_OK;

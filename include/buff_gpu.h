@@ -299,9 +299,7 @@ int buff_slice_buffmax(const buff_col *col, double *max_value, uint32_t *argmax_
  * panics (BUFF_EREFPANIC) unless the windows it started number
  * (end - start) / window (u32): a ragged last window panics unless end runs
  * past the rows; widths above 32 bits and window = 0 panic too.  When no row
- * is read the one window holds f64::min_value().  With BUFF_FLAG_INTENDED any
- * width is accepted, the ragged last window is kept and bad ranges return
- * BUFF_EINVAL. */
+ * is read the one window holds f64::min_value(). */
 int buff_slice_max_range(const buff_col *col, uint32_t start, uint32_t end, uint32_t window,
                          double *out, uint64_t *nout, void *stream);
 

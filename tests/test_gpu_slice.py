@@ -88,7 +88,7 @@ def test_slice_rejects_other_calls(gpu):
 @pytest.mark.parametrize("case", range(len(CASES)))
 def test_slice_max_range(oracle, gpu, case):
     from buff_gb300 import capi
-    from buff_gb300.compress import FLAG_INTENDED, SliceColumn
+    from buff_gb300.compress import SliceColumn
 
     name, x, scale = CASES[case]
     xd = x.astype(np.float64)
@@ -109,11 +109,14 @@ def test_slice_max_range(oracle, gpu, case):
                 col.max_range(s, e, w)
             continue
         assert np.array_equal(col.max_range(s, e, w), exp), (name, s, e, w)
-    ci = SliceColumn.encode(x, scale, FLAG_INTENDED)
-    vals = ci.decode()
-    e = min(n, 1037)
-    got = ci.max_range(3, e, 100)
-    assert np.array_equal(got, np.array([vals[a:min(a + 100, e)].max() for a in range(3, e, 100)]))
-    with pytest.raises(capi.BuffError) as err:
-        ci.max_range(0, n + 1, 10)
-    assert err.value.status == capi.EINVAL
+    if n > 4096:  # device output
+        import torch
+
+        out = torch.empty(n // 1000 + 1, dtype=torch.float64, device="cuda")
+        e = n // 1000 * 1000
+        try:
+            exp = oracle.slice_max_range(img, scale, 0, e, 1000)
+        except oracle.OraclePanic:
+            return
+        _, k = col.max_range(0, e, 1000, out=out)
+        assert k == exp.size and np.array_equal(out.cpu().numpy()[:k], exp)
