@@ -140,6 +140,33 @@ def test_column_parity(gpu, oracle, kind, n, scale, intended):
         assert col.sum_at_precision(p) == want_s, p
 
 
+def test_gaussian_walk_million(gpu, oracle):
+    """The 1,000,000-row CPU-runnable workload (gaussian walk, x0 = 1, steps
+    N(0, 0.01), 4 decimals, seed 1, scale 10^4): every op against the oracle."""
+    from buff_gb300.compress import Column
+    from buff_gb300.workloads import gaussian_walk
+
+    x = gaussian_walk(1_000_000, seed=1)
+    ref = oracle.encode(x, 10000)
+    col = Column.encode(x, 10000)
+    assert col.serialize() == ref
+    assert np.array_equal(col.decode(), oracle.decode(ref, 10000))
+    idx = int(np.random.default_rng(1).integers(0, x.size))
+    for name, p in (("equal_filter", float(x[idx])), ("range_filter", float(np.quantile(x, 0.9)))):
+        w, c, _ = getattr(oracle, name)(ref, 10000, p)
+        g = getattr(col, name)(p)
+        assert words_equal(g.words, w) and g.count == c, name
+    s, parts, exact = oracle.buff_sum(ref, 10000, True)
+    r = col.sum()
+    assert r.sum == s and r.exact_num == exact
+    mv, mc, aw, ac = oracle.buff_max(ref, 10000, True)
+    g = col.max(argmax=True)
+    assert g.code == mc and g.value == mv and words_equal(g.argmax_words, aw)
+    for p in (1, 2, 4):
+        assert np.array_equal(col.decode_at_precision(p),
+                              oracle.decode_at_precision(ref, 10000, p, True))
+
+
 def test_golden_vectors(gpu):
     import os
 
