@@ -187,6 +187,22 @@ int or_slice_max(const uint8_t *bytes, size_t len, uint64_t scale, int any_width
 int or_slice_max_range(const uint8_t *b, size_t len, uint64_t scale, uint32_t s, uint32_t e,
                        uint32_t window, double *out, size_t cap, size_t *nout);
 
+/* --- RAPG byte_residue formats (buff_oracle_rapg.c) --- */
+/* croaring Bitmap (create + ascending add + run_optimize) in the portable format. */
+int or_roaring_serialize(const uint32_t *rows, size_t cnt, uint8_t **out, size_t *out_len);
+int or_roaring_parse(const uint8_t *b, size_t len, uint32_t **rows_out, size_t *cnt_out);
+/* byte_residue_encode (split_double.rs:624-955). */
+int or_rapg_encode(const double *x, uint32_t n, uint64_t scale, uint8_t **out, size_t *out_len);
+/* byte_residue_decode (precision < 0) / _with_precision; *nout values (0 or n). */
+int or_rapg_decode(const uint8_t *bytes, size_t len, uint64_t scale, int precision, double *out,
+                   size_t *nout);
+/* byte_residue_sum (precision < 0) / _with_precision. */
+int or_rapg_sum(const uint8_t *bytes, size_t len, uint64_t scale, int precision, double *sum_out);
+/* Outlier-column directory: count, and per column (up to 8) bitmap size,
+ * outlier count, byte offset of the bitmap. */
+int or_rapg_layout(const uint8_t *bytes, size_t len, uint32_t *ncols, uint32_t *bm_sizes,
+                   uint32_t *nouts, uint64_t *bm_offs);
+
 #ifdef __cplusplus
 }
 #endif

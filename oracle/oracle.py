@@ -26,7 +26,8 @@ class OraclePanic(RuntimeError):
 
 def build() -> str:
     srcs = [os.path.join(_HERE, f) for f in ("buff_oracle.c", "buff_oracle_major.c",
-                                             "buff_oracle_cond.c", "buff_oracle_slice.c", "buff_oracle.h",
+                                             "buff_oracle_cond.c", "buff_oracle_slice.c", "buff_oracle_rapg.c",
+                                             "buff_oracle.h",
                                              "Makefile")]
     if (not os.path.exists(_LIB_PATH)) or any(os.path.getmtime(_LIB_PATH) < os.path.getmtime(s)
                                                for s in srcs):
@@ -103,6 +104,14 @@ def lib():
             getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, P, P, P]
         L.or_slice_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P]
         L.or_slice_max.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P, P, P]
+        L.or_roaring_serialize.argtypes = [P, C.c_size_t, C.POINTER(u8p), C.POINTER(C.c_size_t)]
+        L.or_roaring_parse.argtypes = [P, C.c_size_t, C.POINTER(C.POINTER(C.c_uint32)),
+                                       C.POINTER(C.c_size_t)]
+        L.or_rapg_encode.argtypes = [P, C.c_uint32, C.c_uint64, C.POINTER(u8p),
+                                     C.POINTER(C.c_size_t)]
+        L.or_rapg_decode.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P, P]
+        L.or_rapg_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P]
+        L.or_rapg_layout.argtypes = [P, C.c_size_t, P, P, P, P]
         L.or_slice_max_range.argtypes = [P, C.c_size_t, C.c_uint64, C.c_uint32, C.c_uint32,
                                          C.c_uint32, P, C.c_size_t, P]
         L.or_max_range.argtypes = [P, C.c_size_t, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
@@ -513,3 +522,71 @@ def slice_max_range(buf, scale, s, e, window):
     _check(lib().or_slice_max_range(_ptr(b), b.size, scale, s, e, window, _ptr(out), cap,
                                     C.byref(k)))
     return out[: k.value]
+
+
+# --- RAPG byte_residue formats (buff_oracle_rapg.c) --------------------------
+
+def roaring_serialize(rows) -> bytes:
+    """croaring Bitmap::create + ascending add + run_optimize + serialize."""
+    r = np.ascontiguousarray(np.asarray(rows, dtype=np.uint32))
+    out = C.POINTER(C.c_uint8)()
+    ln = C.c_size_t(0)
+    _check(lib().or_roaring_serialize(_ptr(r), r.size, C.byref(out), C.byref(ln)))
+    try:
+        return C.string_at(out, ln.value)
+    finally:
+        lib().or_free(out)
+
+
+def roaring_parse(buf) -> np.ndarray:
+    b = _buf(buf)
+    out = C.POINTER(C.c_uint32)()
+    n = C.c_size_t(0)
+    _check(lib().or_roaring_parse(_ptr(b), b.size, C.byref(out), C.byref(n)))
+    try:
+        return np.ctypeslib.as_array(out, shape=(n.value,)).copy() if n.value else \
+            np.zeros(0, dtype=np.uint32)
+    finally:
+        lib().or_free(out)
+
+
+def rapg_encode(x, scale: int) -> bytes:
+    """byte_residue_encode (split_double.rs:624-955)."""
+    arr = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    out = C.POINTER(C.c_uint8)()
+    ln = C.c_size_t(0)
+    _check(lib().or_rapg_encode(_ptr(arr), arr.size, scale, C.byref(out), C.byref(ln)))
+    try:
+        return C.string_at(out, ln.value)
+    finally:
+        lib().or_free(out)
+
+
+def rapg_decode(buf, scale, precision=-1):
+    """byte_residue_decode (precision -1) / byte_residue_decode_with_precision."""
+    b = _buf(buf)
+    n = header(buf).n
+    out = np.zeros(max(n, 1), dtype=np.float64)
+    k = C.c_size_t(0)
+    _check(lib().or_rapg_decode(_ptr(b), b.size, scale, precision, _ptr(out), C.byref(k)))
+    return out[: k.value]
+
+
+def rapg_sum(buf, scale, precision=-1) -> float:
+    """byte_residue_sum (precision -1) / byte_residue_sum_with_precision."""
+    b = _buf(buf)
+    s = np.zeros(1, dtype=np.float64)
+    _check(lib().or_rapg_sum(_ptr(b), b.size, scale, precision, _ptr(s)))
+    return float(s[0])
+
+
+def rapg_layout(buf):
+    """(columns, bitmap sizes, outlier counts, bitmap byte offsets)."""
+    b = _buf(buf)
+    nc = np.zeros(1, dtype=np.uint32)
+    sizes = np.zeros(8, dtype=np.uint32)
+    nouts = np.zeros(8, dtype=np.uint32)
+    offs = np.zeros(8, dtype=np.uint64)
+    _check(lib().or_rapg_layout(_ptr(b), b.size, _ptr(nc), _ptr(sizes), _ptr(nouts), _ptr(offs)))
+    c = int(nc[0])
+    return c, sizes[:c].tolist(), nouts[:c].tolist(), offs[:c].tolist()
