@@ -44,6 +44,8 @@ EXPORTED = [
     "buff_slice_encode_f64", "buff_slice_encode_f32", "buff_slice_deserialize",
     "buff_slice_decode", "buff_slice_range_filter", "buff_slice_equal_filter", "buff_slice_sum",
     "buff_slice_buffsum", "buff_slice_max", "buff_slice_buffmax",
+    "buff_rapg_encode_f64", "buff_rapg_encode_f32", "buff_rapg_deserialize", "buff_rapg_decode",
+    "buff_rapg_decode_at_precision", "buff_rapg_sum", "buff_rapg_sum_at_precision",
 ]
 
 Q_RANGE, Q_EQUAL, Q_SUM, Q_MAX, Q_DECODE = 0x1, 0x2, 0x4, 0x8, 0x10
@@ -204,6 +206,13 @@ def lib(build_if_missing: bool = True):
     L.buff_slice_buffsum.argtypes = [P, P, P]
     L.buff_slice_max.argtypes = [P, P, P, P, P]
     L.buff_slice_buffmax.argtypes = [P, P, P, P, P]
+    L.buff_rapg_encode_f64.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_rapg_encode_f32.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_rapg_deserialize.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_rapg_decode.argtypes = [P, P, P, P]
+    L.buff_rapg_decode_at_precision.argtypes = [P, C.c_uint32, P, P, P]
+    L.buff_rapg_sum.argtypes = [P, P, P]
+    L.buff_rapg_sum_at_precision.argtypes = [P, C.c_uint32, P, P]
     L.buff_status_string.argtypes = [C.c_int]
     L.buff_status_string.restype = C.c_char_p
     L.buff_last_cuda_error.restype = C.c_int

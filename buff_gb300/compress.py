@@ -395,6 +395,52 @@ class SliceColumn(Column):
     range_filter_decode = _unsupported
 
 
+class RapgColumn(Column):
+    """A RAPG byte_residue column resident in HBM
+    (compress/split_double.rs:624-955): sparse leading bytes as row sets
+    (major byte 0) plus nonzero bytes, dense slices, packed tail."""
+
+    _ENCODE = ("buff_rapg_encode_f32", "buff_rapg_encode_f64")
+    _DESERIALIZE = "buff_rapg_deserialize"
+
+    def _decode(self, precision, out, stream):
+        dst = out if out is not None else np.empty(max(self.n, 1), dtype=np.float64)
+        cnt = C.c_uint64(0)
+        if precision is None:
+            check(lib().buff_rapg_decode(self._h, ptr(dst), C.byref(cnt), stream_handle(stream)),
+                  "rapg_decode")
+        else:
+            check(lib().buff_rapg_decode_at_precision(self._h, precision, ptr(dst), C.byref(cnt),
+                                                      stream_handle(stream)), "rapg_decode")
+        return dst[: cnt.value] if out is None else (dst, cnt.value)
+
+    def decode(self, out=None, stream=None):
+        """byte_residue_decode (split_double.rs:1353-1610)."""
+        return self._decode(None, out, stream)
+
+    def decode_at_precision(self, precision: int, out=None, stream=None):
+        """byte_residue_decode_with_precision (split_double.rs:1612-1893)."""
+        return self._decode(precision, out, stream)
+
+    def rapg_sum(self, precision=None, stream=None) -> float:
+        """byte_residue_sum / byte_residue_sum_with_precision."""
+        v = C.c_double(0)
+        if precision is None:
+            check(lib().buff_rapg_sum(self._h, C.byref(v), stream_handle(stream)), "rapg_sum")
+        else:
+            check(lib().buff_rapg_sum_at_precision(self._h, precision, C.byref(v),
+                                                   stream_handle(stream)), "rapg_sum")
+        return v.value
+
+    def _unsupported(self, *a, **k):
+        raise capi.BuffError(capi.ENOTSUP, "not defined on RAPG columns")
+
+    sum = max = sum_at_precision = range_filter = equal_filter = _unsupported
+    range_filter_with_slice = equal_filter_with_slice = _unsupported
+    decode_condition = decode_selected = range_filter_condition = _unsupported
+    range_filter_decode = max_range = range_filter_sum = _unsupported
+
+
 class BuffSliceCompress:
     """GPU mirror of ``BuffSliceCompress`` (compress/buff_slice.rs:222-296)."""
 
@@ -438,6 +484,12 @@ def _as_major(comp: "SplitBDDoubleCompress", data) -> MajorColumn:
     if isinstance(data, MajorColumn):
         return data
     return MajorColumn.deserialize(data, comp.scale, comp.flags)
+
+
+def _as_rapg(comp: "SplitBDDoubleCompress", data) -> RapgColumn:
+    if isinstance(data, RapgColumn):
+        return data
+    return RapgColumn.deserialize(data, comp.scale, comp.flags)
 
 
 def _as_column(comp: "SplitBDDoubleCompress", data) -> Column:
@@ -487,13 +539,31 @@ class SplitBDDoubleCompress:
     def byte_fixed_max(self, data, stream=None) -> MaxResult:
         return _as_column(self, data).max(argmax=True, stream=stream)
 
-    # compress/split_double.rs:1612-1893
+    # ---- RAPG byte_residue format -----------------------------------
+    # compress/split_double.rs:624-955
+    def byte_residue_encode(self, values, stream=None) -> RapgColumn:
+        return RapgColumn.encode(values, self.scale, self.flags, stream)
+
+    # compress/split_double.rs:1353-1610
+    def byte_residue_decode(self, data, stream=None):
+        return _as_rapg(self, data).decode(stream=stream)
+
+    # compress/split_double.rs:1612-1893 (a buff-simd column: the same
+    # precision-limited read of its codes)
     def byte_residue_decode_with_precision(self, data, precision: int, stream=None):
-        return _as_column(self, data).decode_at_precision(precision, stream=stream)
+        if isinstance(data, Column) and not isinstance(data, RapgColumn):
+            return data.decode_at_precision(precision, stream=stream)
+        return _as_rapg(self, data).decode_at_precision(precision, stream=stream)
+
+    # compress/split_double.rs:2211-2407
+    def byte_residue_sum(self, data, stream=None) -> float:
+        return _as_rapg(self, data).rapg_sum(stream=stream)
 
     # compress/split_double.rs:2409-2630
     def byte_residue_sum_with_precision(self, data, precision: int, stream=None) -> float:
-        return _as_column(self, data).sum_at_precision(precision, stream=stream)
+        if isinstance(data, Column) and not isinstance(data, RapgColumn):
+            return data.sum_at_precision(precision, stream=stream)
+        return _as_rapg(self, data).rapg_sum(precision, stream=stream)
 
     # compress/buff_simd.rs:1528-1712 (buff layout; rows strictly ascending)
     def buff_decode_condition(self, data, rows, stream=None):
@@ -542,5 +612,6 @@ class SplitBDDoubleCompress:
 
 
 __all__ = ["SplitBDDoubleCompress", "BuffSliceCompress", "Column", "MajorColumn", "SliceColumn",
+           "RapgColumn",
            "FilterResult", "MaxResult",
            "FLAG_INTENDED", "FLAG_RAW_BITMAPS", "FLAG_BUFF_LAYOUT", "rows_to_words"]

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "buff_internal.h"
+#include "buff_roaring.h"
 #include "buff_snappy.h"
 
 using buffk::EncStats;
@@ -862,6 +863,8 @@ done:
   return rc;
 }
 
+// (defined with the RAPG entry points below)
+int rapg_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s);
 }  // namespace
 
 // ================================================================ C ABI
@@ -907,7 +910,7 @@ int buff_col_get_info(const buff_col *c, buff_col_info *info) {
   info->outlier_cols = c->m;
   info->serialized_bytes = serialized_size(c);
   info->device_bytes = (uint64_t)c->k * c->stride + c->tail_alloc;
-  if (c->layout == 1) {
+  if (c->layout == 1 || c->layout == 3) {
     info->device_bytes = (uint64_t)(c->k - c->m) * c->stride + c->tail_alloc +
                          (uint64_t)c->m * c->nwp * 8 + c->oofs[c->m];
     info->serialized_bytes = 0;  // known after compressing the bitmaps (buff_serialize)
@@ -917,9 +920,9 @@ int buff_col_get_info(const buff_col *c, buff_col_info *info) {
 
 int buff_serialize(const buff_col *c, uint8_t *out, uint64_t cap, uint64_t *len, void *stream) {
   if (!c || !len) return BUFF_EINVAL;
-  if (c->layout == 1) {
+  if (c->layout == 1 || c->layout == 3) {
     std::vector<uint8_t> img;
-    const int st = major_image(c, img, S(stream));
+    const int st = c->layout == 1 ? major_image(c, img, S(stream)) : rapg_image(c, img, S(stream));
     if (st) return st;
     *len = img.size();
     if (!out || cap < img.size()) return BUFF_EINVAL;
@@ -1731,6 +1734,501 @@ done:
   if (codes) cudaFreeAsync(codes, s);
   if (stage && d) cudaFreeAsync(d, s);
   return rc;
+}
+
+}  // extern "C"
+
+namespace {
+
+// ---------------------------------------------------------------- RAPG byte_residue
+
+// byte_residue_encode (compress/split_double.rs:624-955): exact min and max
+// (two ifs), width ceil(log2(max - min)).  When ilen > 15 -- a u32 compare,
+// so also when ilen wrapped because the codes are narrower than dlen -- the
+// image carries an outlier-column count byte, and the leading code bytes
+// that are nonzero in fewer than 200 of the first 2000 codes (counted
+// cumulatively from the top byte down, :693-716) become sparse columns: the
+// rows whose byte is nonzero and those bytes.  The remaining bytes are dense
+// slices, then the packed tail.
+template <typename T>
+int encode_rapg_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, cudaStream_t s,
+                     buff_col **out) {
+  if (!out) return BUFF_EINVAL;
+  *out = nullptr;
+  if (flags & BUFF_FLAG_INTENDED) return BUFF_ENOTSUP;
+  if (n64 >= (1ull << 32)) return BUFF_EINVAL;
+  if (n64 > 0 && !values) return BUFF_EINVAL;
+  const uint32_t n = (uint32_t)n64;
+  const int dl = dlen_of_prec(prec_of_scale(scale));
+  if (dl < 0) return BUFF_EREFPANIC;  // PRECISION_MAP.get(&prec).unwrap()
+  int rc = BUFF_OK;
+  buff_col *c = new_col(scale, flags);
+  if (!c) return BUFF_ENOMEM;
+  c->layout = 3;
+  c->n = n;
+  c->dlen = (uint32_t)dl;
+  T *staged = nullptr;
+  EncStats *dst = nullptr;
+  uint8_t *lead = nullptr;
+  const T *dx = values;
+  EncStats st;
+  memset(&st, 0, sizeof(st));
+  st.mn = INT64_MAX;
+  st.mx0 = INT64_MIN;
+  std::vector<T> head(n < 2000 ? n : 2000);
+  uint32_t fl = 0, m = 0;
+  if (n) {
+    if (!is_device_ptr(values) || (reinterpret_cast<uintptr_t>(values) & 15)) {
+      CK(scratch(&staged, n, s));
+      CK(cudaMemcpyAsync(staged, values, (size_t)n * sizeof(T), cudaMemcpyDefault, s));
+      dx = staged;
+    }
+    CK(scratch(&dst, 1, s));
+    const int keys = c->precision_exp >= -(int)c->dlen ? 1 : 0;
+    CK(reduce(dx, n, 1, c, keys, 0, dst, s));
+    CK(cudaMemcpyAsync(&st, dst, sizeof(st), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(head.data(), dx, head.size() * sizeof(T), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (!st.ok) {
+      CK(reduce(dx, n, 1, c, 0, 0, dst, s));
+      CK(cudaMemcpyAsync(&st, dst, sizeof(st), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    }
+  }
+  {
+    const int64_t mn = st.mn, mx = st.mx0;
+    const int64_t delta = (int64_t)((uint64_t)mx - (uint64_t)mn);
+    if (delta != 0) {
+      const double cl = ceil(log2((double)delta));
+      fl = (isnan(cl) || cl <= 0.0) ? 0u : (uint32_t)cl;
+    }
+    const uint64_t ilen64 = (uint64_t)fl - (uint64_t)c->dlen;  // usize, wraps
+    c->rg_count_byte = ilen64 > 15;
+    if (c->rg_count_byte) {
+      if (n < 2000) {  // fixed_vec[0..SAMPLE]
+        rc = BUFF_EREFPANIC;
+        goto done;
+      }
+      // leading zeros of each sample code within fixed_len bits; a code at
+      // 2^fixed_len (the width's lost top bit) wraps and is not counted
+      uint32_t counter[32] = {0};
+      const uint64_t head_len = 64u - fl;
+      for (uint32_t i = 0; i < 2000; ++i) {
+        const uint64_t u =
+            (uint64_t)fetch_fixed_host((double)head[i], c->precision_exp, c->dlen) - (uint64_t)mn;
+        const uint64_t lz = (uint64_t)(u ? __builtin_clzll(u) : 64) - head_len;
+        if (lz < 32) ++counter[lz];
+      }
+      const uint32_t ol = (uint32_t)(2000.0f * 0.1f);
+      const uint64_t adjusted = ilen64 / 8 * 8;
+      uint32_t sum = 0;
+      for (uint64_t i = 0; i < adjusted; ++i) {
+        if (i >= 32) {  // bits_counter[i]: index out of bounds
+          rc = BUFF_EREFPANIC;
+          goto done;
+        }
+        sum += counter[i];
+        if (i % 8 == 7) {
+          if (sum < ol)
+            ++m;
+          else
+            break;
+        }
+      }
+    }
+    c->base = mn;
+    set_layout(c, fl);
+    c->m = m;
+    c->ilen = (uint32_t)ilen64;
+    const uint32_t k = c->k;
+    c->k = k - m;  // allocate the dense slices only
+    rc = alloc_col(c, s);
+    c->k = k;
+    if (rc) goto done;
+    c->nwp = c->stride / 32;
+    if (n && fl) {
+      if (m) CK(scratch(&lead, (size_t)m * c->stride, s));
+      if (sizeof(T) == 8)
+        CK(buffk::launch_encode_scatter_f64(reinterpret_cast<const double *>(dx), c, s, lead, m));
+      else
+        CK(buffk::launch_encode_scatter_f32(reinterpret_cast<const float *>(dx), c, s, lead, m));
+      if (m) CK(buffk::major_build_sparse(c, lead, s));
+    }
+    if (c->rg_count_byte && fl > 0 && fl < 8) {
+      // packed codes narrower than a byte overwrite the count byte; the
+      // readers take that byte as the column count and read on from the next
+      uint8_t first = 0;
+      CK(cudaMemcpyAsync(&first, c->tail, 1, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      c->rg_skip = 1;
+      c->rg_bad = first != 0;
+    }
+    CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (staged) cudaFreeAsync(staged, s);
+  if (dst) cudaFreeAsync(dst, s);
+  if (lead) cudaFreeAsync(lead, s);
+  if (rc != BUFF_OK) {
+    cudaStreamSynchronize(s);
+    free_col(c);
+    return rc;
+  }
+  *out = c;
+  return BUFF_OK;
+}
+
+// The byte image byte_residue_encode writes: header; [count byte]; per
+// sparse column u32 bitmap size, roaring bitmap, u32 outlier count, outlier
+// bytes (each column's pad byte is overwritten by the next write, so one pad
+// byte follows the last column); unflipped dense slices; packed tail.  Codes
+// narrower than a byte are packed from byte 20, over the count byte.
+int rapg_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s) {
+  int rc = BUFF_OK;
+  const uint32_t n = c->n, kd = c->k - c->m;
+  const size_t nw = ((size_t)n + 31) / 32;
+  std::vector<uint32_t> bits((size_t)c->m * nw);
+  std::vector<uint8_t> ob(c->oofs[c->m]);
+  std::vector<uint8_t> dense((size_t)kd * n), tail(c->tail_bytes);
+  for (uint32_t col = 0; col < c->m; ++col)
+    CK(cudaMemcpyAsync(bits.data() + col * nw, c->obits + col * c->nwp, nw * 4,
+                       cudaMemcpyDeviceToHost, s));
+  if (!ob.empty()) CK(cudaMemcpyAsync(ob.data(), c->obytes, ob.size(), cudaMemcpyDeviceToHost, s));
+  if (kd && n)
+    CK(cudaMemcpy2DAsync(dense.data(), n, c->slices, c->stride, n, kd, cudaMemcpyDeviceToHost, s));
+  if (!tail.empty())
+    CK(cudaMemcpyAsync(tail.data(), c->tail, tail.size(), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  {
+    img.clear();
+    auto put32 = [&](uint32_t v) {
+      for (int b = 0; b < 4; ++b) img.push_back((uint8_t)(v >> (8 * b)));
+    };
+    const uint64_t ub = (uint64_t)c->base;
+    put32((uint32_t)ub);
+    put32((uint32_t)(ub >> 32));
+    put32(n);
+    put32(c->ilen);
+    put32(c->dlen);
+    if (c->fixed_len < 8) {
+      if (c->rg_count_byte && tail.empty()) img.push_back(0);
+      img.insert(img.end(), tail.begin(), tail.end());
+      return BUFF_OK;
+    }
+    if (c->rg_count_byte) img.push_back((uint8_t)c->m);
+    for (uint32_t col = 0; col < c->m; ++col) {
+      const std::vector<uint8_t> bm = buffroaring::serialize(bits.data() + col * nw, n);
+      put32((uint32_t)bm.size());
+      img.insert(img.end(), bm.begin(), bm.end());
+      put32(c->nout[col]);
+      img.insert(img.end(), ob.begin() + c->oofs[col], ob.begin() + c->oofs[col] + c->nout[col]);
+    }
+    if (c->m) img.push_back(0);
+    for (uint8_t &b : dense) b ^= 0x80;  // the dense slices are stored unflipped
+    img.insert(img.end(), dense.begin(), dense.end());
+    img.insert(img.end(), tail.begin(), tail.end());
+  }
+done:
+  return rc;
+}
+
+// The reads byte_residue_decode / byte_residue_sum make for R code bits
+// (compress/split_double.rs:1353-1610, 2211-2407; R < fixed_len for the
+// _with_precision forms, :1642-1664): one byte per sparse column, then
+// slices while at least 8 bits remain -- past the dense ones the reader
+// takes the bytes after them -- then ts-bit fields.  Reads past the image
+// panic there.
+struct RapgPlan {
+  uint32_t ks, ts;
+  uint64_t tbit0;  // bit of `tail` where the ts-bit fields start
+  bool emit;       // the decode returns values (not when R ends with the sparse columns)
+  bool no_base;    // the sum returns at its last slice, before the base term
+};
+
+int rapg_plan(const buff_col *c, uint32_t R, RapgPlan *p) {
+  if (c->rg_bad) return BUFF_EREFPANIC;
+  const uint32_t m = c->m, kd = c->k - m;
+  uint32_t remain = R;
+  if (m) {
+    if (R < 8 * m) return BUFF_EREFPANIC;  // `remain -= 8` wraps: slices read past the image
+    remain = R - 8 * m;
+  }
+  p->ks = remain / 8;
+  p->ts = remain % 8;
+  p->emit = !(m && remain == 0);
+  p->no_base = p->ks > 0 && p->ts == 0;
+  uint64_t at = c->rg_skip;  // bytes of the tail region consumed so far
+  if (p->ks > kd) at += (uint64_t)(p->ks - kd) * c->n;
+  if (at > c->tail_bytes) return BUFF_EREFPANIC;  // read_n_byte past the image
+  p->tbit0 = 8 * at;
+  if (p->ts) {
+    if (p->ks < kd) return BUFF_ENOTSUP;  // bit fields from inside a slice
+    if (p->tbit0 + (uint64_t)c->n * p->ts > 8ull * c->tail_bytes) return BUFF_EREFPANIC;
+  }
+  return BUFF_OK;
+}
+
+int rapg_bits(const buff_col *c, int precision, uint32_t *R) {
+  if (precision < 0) {
+    *R = c->ilen + c->dlen;
+    return BUFF_OK;
+  }
+  return precision_bits(c, (uint32_t)precision, R);
+}
+
+int rapg_decode_impl(const buff_col *c, int precision, double *out, uint64_t *nout,
+                     cudaStream_t s) {
+  if (!c || !nout || (!out && c->n)) return BUFF_EINVAL;
+  if (c->layout != 3) return BUFF_ENOTSUP;
+  *nout = 0;
+  uint32_t R;
+  int rc = rapg_bits(c, precision, &R);
+  if (rc) return rc;
+  RapgPlan p;
+  if ((rc = rapg_plan(c, R, &p))) return rc;
+  for (uint32_t col = 0; col < c->m; ++col)
+    if (c->nout[col] == 0) return BUFF_EREFPANIC;  // outlier_iter.next().unwrap() (:1393)
+  if (!p.emit || c->n == 0) return BUFF_OK;
+  const bool stage = !is_device_ptr(out);
+  double *d = stage ? nullptr : out;
+  if (stage) CK(scratch(&d, c->n, s));
+  CK(buffk::rapg_decode(c, R, p.ks, p.ts, p.tbit0, d, s));
+  if (stage) {
+    CK(cudaMemcpyAsync(out, d, (size_t)c->n * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  *nout = c->n;
+done:
+  if (stage && d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+int rapg_sum_impl(const buff_col *c, int precision, double *sum, cudaStream_t s) {
+  if (!c || !sum) return BUFF_EINVAL;
+  if (c->layout != 3) return BUFF_ENOTSUP;
+  uint32_t R;
+  int rc = rapg_bits(c, precision, &R);
+  if (rc) return rc;
+  RapgPlan p;
+  if ((rc = rapg_plan(c, R, &p))) return rc;
+  const uint32_t m = c->m, kd = c->k - m, n = c->n;
+  const uint32_t ks_dense = p.ks < kd ? p.ks : kd;
+  unsigned long long *d = nullptr;
+  uint64_t h[40] = {0};
+  CK(scratch(&d, 40, s));
+  CK(cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 40, s));
+  for (uint32_t col = 0; col < m; ++col)
+    if (c->nout[col]) CK(buffk::major_bytesum(c->obytes + c->oofs[col], c->nout[col], d + col, s));
+  if (n && ks_dense) CK(buffk::launch_sum(c, ks_dense, 0, d + 8, s));
+  for (uint32_t j = kd; j < p.ks && n; ++j)
+    CK(buffk::major_bytesum(c->tail + c->rg_skip + (size_t)(j - kd) * n, n, d + 8 + j, s));
+  if (p.ts) CK(buffk::field_sum(c->tail, p.tbit0, p.ts, n, d + 32, s));
+  CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  {
+    // the f64 steps of byte_residue_sum (:2229-2404): each partial over
+    // 2^(processed - ilen), the base term n * base / 2^dlen last
+    auto powi2 = [](int32_t e) -> double {
+      if (e >= 1024) return INFINITY;
+      if (e <= -1024) return 0.0;
+      return ldexp(1.0, e);
+    };
+    const int32_t ilen_i = (int32_t)c->ilen;
+    const double sum_base = ((double)n * (double)c->base) / ldexp(1.0, (int)c->dlen);
+    double acc = 0.0;
+    int32_t processed = 0;
+    for (uint32_t col = 0; col < m; ++col) {
+      processed += 8;
+      acc = acc + (double)h[col] / powi2(processed - ilen_i);
+    }
+    for (uint32_t j = 0; j < p.ks; ++j) {
+      processed += 8;
+      acc = acc + (double)h[8 + j] / powi2(processed - ilen_i);
+    }
+    if (!p.no_base) {
+      if (p.ts) {
+        processed += (int32_t)p.ts;
+        acc = acc + (double)h[32] / powi2(processed - ilen_i);
+      }
+      acc += sum_base;
+    }
+    *sum = acc;
+  }
+done:
+  if (d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int buff_rapg_encode_f64(const double *values, uint64_t n, uint64_t scale, uint32_t flags,
+                         void *stream, buff_col **out) {
+  return encode_rapg_impl<double>(values, n, scale, flags, S(stream), out);
+}
+
+int buff_rapg_encode_f32(const float *values, uint64_t n, uint64_t scale, uint32_t flags,
+                         void *stream, buff_col **out) {
+  return encode_rapg_impl<float>(values, n, scale, flags, S(stream), out);
+}
+
+// Reads an image the way the reference's decoders walk it (BitPack reads of
+// the header, the count byte, each column's directory) and rejects images
+// whose length differs from what byte_residue_encode writes for that
+// directory, or whose bitmaps do not list exactly their outlier rows.
+int buff_rapg_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                          void *stream, buff_col **out) {
+  if (!out || !bytes) return BUFF_EINVAL;
+  *out = nullptr;
+  if (flags & BUFF_FLAG_INTENDED) return BUFF_ENOTSUP;
+  if (len < 20) return BUFF_ECORRUPT;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  std::vector<uint8_t> host;
+  const uint8_t *b = bytes;
+  buff_col *c = nullptr;
+  std::vector<std::vector<uint32_t>> rows;
+  std::vector<const uint8_t *> outl;
+  if (is_device_ptr(bytes)) {
+    host.resize(len);
+    CK(cudaMemcpyAsync(host.data(), bytes, len, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    b = host.data();
+  }
+  {
+    auto rd32 = [&](uint64_t at) -> uint32_t {
+      return (uint32_t)b[at] | ((uint32_t)b[at + 1] << 8) | ((uint32_t)b[at + 2] << 16) |
+             ((uint32_t)b[at + 3] << 24);
+    };
+    c = new_col(scale, flags);
+    if (!c) return BUFF_ENOMEM;
+    c->layout = 3;
+    c->base = (int64_t)((uint64_t)rd32(0) | ((uint64_t)rd32(4) << 32));
+    c->n = rd32(8);
+    c->ilen = rd32(12);
+    c->dlen = rd32(16);
+    const uint32_t fl = c->ilen + c->dlen, n = c->n;
+    if (fl > 64) {
+      rc = BUFF_ECORRUPT;
+      goto done;
+    }
+    set_layout(c, fl);
+    c->rg_count_byte = c->ilen > 15;
+    uint32_t m = 0;
+    uint64_t pos = 20, dense_at = 20;
+    if (c->rg_count_byte && fl >= 8) {
+      if (len < 21) {
+        rc = BUFF_ECORRUPT;
+        goto done;
+      }
+      m = b[20];
+      pos = 21;
+      if (m > c->k) {
+        rc = BUFF_ECORRUPT;
+        goto done;
+      }
+      uint64_t off = 0;
+      for (uint32_t col = 0; col < m; ++col) {
+        if (pos + 4 > len) {
+          rc = BUFF_ECORRUPT;
+          goto done;
+        }
+        const uint32_t bml = rd32(pos);
+        if (pos + 8 + (uint64_t)bml > len) {
+          rc = BUFF_ECORRUPT;
+          goto done;
+        }
+        std::vector<uint32_t> r;
+        const uint32_t no = rd32(pos + 4 + bml);
+        if (!buffroaring::parse(b + pos + 4, bml, r) || r.size() != no ||
+            (no && r.back() >= n) || pos + 8 + (uint64_t)bml + no > len) {
+          rc = BUFF_ECORRUPT;
+          goto done;
+        }
+        rows.push_back(std::move(r));
+        outl.push_back(b + pos + 8 + bml);
+        c->nout[col] = no;
+        c->oofs[col] = off;
+        off += no;
+        pos += 8 + (uint64_t)bml + no;
+      }
+      c->oofs[m] = off;
+      dense_at = m ? pos + 1 : 21;
+    }
+    c->m = m;
+    // codes narrower than a byte are packed from byte 20, over the count byte
+    const uint64_t tail_len = ((uint64_t)n * c->r + 7) / 8;
+    const uint64_t need =
+        fl < 8 ? 20 + (tail_len > c->rg_count_byte ? tail_len : (uint64_t)c->rg_count_byte)
+               : dense_at + (uint64_t)(c->k - m) * n + tail_len;
+    if (need != len) {
+      rc = BUFF_ECORRUPT;
+      goto done;
+    }
+    if (fl < 8 && c->rg_count_byte && fl > 0) {
+      // the readers take byte 20 (the first packed byte) as the column count
+      // and read on from byte 21
+      c->rg_skip = 1;
+      c->rg_bad = b[20] != 0;
+    }
+    const uint32_t k = c->k, kd = k - m;
+    c->k = kd;
+    rc = alloc_col(c, s);
+    c->k = k;
+    if (rc) goto done;
+    c->nwp = c->stride / 32;
+    if (kd && n) {
+      CK(cudaMemcpy2DAsync(c->slices, c->stride, b + dense_at, n, n, kd, cudaMemcpyHostToDevice, s));
+      CK(buffk::flip_bytes(c->slices, (size_t)kd * c->stride, s));
+      if (c->stride > n)
+        CK(cudaMemset2DAsync(c->slices + n, c->stride, 0x80, c->stride - n, kd, s));
+    }
+    CK(cudaMemsetAsync(c->tail, 0, c->tail_alloc, s));
+    if (c->tail_bytes)
+      CK(cudaMemcpyAsync(c->tail, b + (fl < 8 ? 20 : dense_at + (uint64_t)kd * n), c->tail_bytes,
+                         cudaMemcpyHostToDevice, s));
+    if (m) {
+      std::vector<uint32_t> words((size_t)m * c->nwp, 0);
+      for (uint32_t col = 0; col < m; ++col)
+        for (uint32_t r : rows[col]) words[col * c->nwp + (r >> 5)] |= 1u << (r & 31);
+      CK(scratch(&c->obits, (size_t)m * c->nwp, s));
+      CK(scratch(&c->orank, (size_t)m * (c->nwp + 16), s));
+      CK(scratch(&c->obytes, c->oofs[m] + 16, s));
+      CK(cudaMemcpyAsync(c->obits, words.data(), words.size() * 4, cudaMemcpyHostToDevice, s));
+      for (uint32_t col = 0; col < m; ++col)
+        if (c->nout[col])
+          CK(cudaMemcpyAsync(c->obytes + c->oofs[col], outl[col], c->nout[col],
+                             cudaMemcpyHostToDevice, s));
+      CK(buffk::major_index(c, s));
+    }
+    CK(cudaStreamSynchronize(s));
+  }
+done:
+  if (rc != BUFF_OK) {
+    free_col(c);
+    return rc;
+  }
+  *out = c;
+  return BUFF_OK;
+}
+
+int buff_rapg_decode(const buff_col *c, double *out, uint64_t *nout, void *stream) {
+  return rapg_decode_impl(c, -1, out, nout, S(stream));
+}
+
+int buff_rapg_decode_at_precision(const buff_col *c, uint32_t precision, double *out,
+                                  uint64_t *nout, void *stream) {
+  return rapg_decode_impl(c, precision > 0x7FFFFFFFu ? 0x7FFFFFFF : (int)precision, out, nout,
+                          S(stream));
+}
+
+int buff_rapg_sum(const buff_col *c, double *sum, void *stream) {
+  return rapg_sum_impl(c, -1, sum, S(stream));
+}
+
+int buff_rapg_sum_at_precision(const buff_col *c, uint32_t precision, double *sum, void *stream) {
+  return rapg_sum_impl(c, precision > 0x7FFFFFFFu ? 0x7FFFFFFF : (int)precision, sum, S(stream));
 }
 
 // ---------------------------------------------------------------- buff-slice ABI

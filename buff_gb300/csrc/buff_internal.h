@@ -51,6 +51,11 @@ struct buff_col {
   uint8_t *obytes;      // outlier bytes of all sparse columns, row order
   uint64_t oofs[9];     // start of each column's outlier bytes
   buff_arena *arena;    // non-null: slices and tail live in a shared arena
+  // RAPG byte_residue layout (layout 3, compress/split_double.rs:624-955):
+  // the sparse columns above hold the rows whose byte is nonzero (major 0).
+  uint32_t rg_count_byte;  // the image carries the outlier-column count byte (ilen > 15)
+  uint32_t rg_skip;        // bytes of `tail` before where the readers start reading it
+  uint32_t rg_bad;         // the readers would take packed codes for a column directory
 };
 
 // Host helpers of the C ABI (buff_capi.cu) shared with the batched and
@@ -157,6 +162,14 @@ cudaError_t cand_select(const uint8_t *slice, const uint8_t *tail, uint32_t r, u
                         size_t nw, uint32_t value, unsigned long long *count, cudaStream_t s);
 cudaError_t popcount_words(const uint32_t *w, size_t nw, unsigned long long *out, cudaStream_t s);
 cudaError_t major_decode(const buff_col *c, double *out, cudaStream_t s);
+// RAPG decode of the top R bits: m sparse columns, ks slices (those past the
+// k - m dense ones read from the bytes after them, as the reference's reader
+// does), then ts-bit fields from bit `tbit0` of the tail buffer.
+cudaError_t rapg_decode(const buff_col *c, uint32_t R, uint32_t ks, uint32_t ts, uint64_t tbit0,
+                        double *out, cudaStream_t s);
+// Sum of n `width`-bit fields packed LSB-first from bit `bit0` of `p`.
+cudaError_t field_sum(const uint8_t *p, uint64_t bit0, uint32_t width, uint32_t n,
+                      unsigned long long *out, cudaStream_t s);
 
 // Row-conditioned decode (buff_cond.cu): rows from a list (rows != null,
 // nrows entries) or from a bitmap with its word ranks (word_ranks).

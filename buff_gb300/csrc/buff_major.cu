@@ -441,6 +441,68 @@ __global__ void __launch_bounds__(kThreads) k_decode_major(DecodeMajorArgs a) {
   }
 }
 
+// RAPG byte_residue_decode (compress/split_double.rs:1353-1610) and its
+// precision-limited form (:1612-1893) over the top R bits of each code: the
+// outlier bytes of the m sparse columns (zero elsewhere) and ks dense slices,
+// each placed `remain` bits up as the reference's reader places them, then a
+// ts-bit field of the packed tail; not shifted back when R < fixed_len.
+struct RapgDecodeArgs {
+  const uint32_t *obits, *orank;
+  const uint8_t *obytes;
+  uint64_t oofs[8];
+  size_t nwp, rs, stride;
+  const uint8_t *slices, *tail;
+  uint32_t n, m, kd, ks, ts, R, skip;
+  unsigned long long tbit0;
+  long long base;
+  int dlen;
+  double *out;
+};
+
+// `width`-bit field `row` of a stream packed LSB-first from bit `bit0`.
+__device__ __forceinline__ uint32_t field_from(const uint8_t *p, unsigned long long bit0,
+                                               uint32_t width, uint32_t row) {
+  const unsigned long long bit = bit0 + (unsigned long long)row * width;
+  const uint32_t b0 = p[bit >> 3];
+  const uint32_t b1 = ((bit & 7) + width > 8) ? p[(bit >> 3) + 1] : 0u;
+  return ((b0 | (b1 << 8)) >> (bit & 7)) & ((1u << width) - 1u);
+}
+
+__global__ void __launch_bounds__(kThreads) k_rapg_decode(RapgDecodeArgs a) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t w = i >> 5;
+    const uint32_t j = (uint32_t)(i & 31);
+    unsigned long long v = 0;
+    uint32_t remain = a.R;
+    for (uint32_t c = 0; c < a.m; ++c) {
+      remain -= 8;
+      const uint32_t B = a.obits[c * a.nwp + w];
+      if (B >> j & 1u) {
+        const uint32_t k = a.orank[c * a.rs + w] + __popc(B & ((1u << j) - 1u));
+        v |= (unsigned long long)a.obytes[a.oofs[c] + k] << (remain & 63);
+      }
+    }
+    for (uint32_t d = 0; d < a.ks; ++d) {
+      remain -= 8;
+      const uint32_t byte = d < a.kd ? (a.slices[d * a.stride + i] ^ 0x80u)
+                                     : a.tail[a.skip + (size_t)(d - a.kd) * a.n + i];
+      v |= (unsigned long long)byte << (remain & 63);
+    }
+    if (a.ts) v |= field_from(a.tail, a.tbit0, a.ts, (uint32_t)i);
+    a.out[i] = i64_to_f64_scaled((long long)((unsigned long long)a.base + v), a.dlen);
+  }
+}
+
+__global__ void k_field_sum(const uint8_t *p, unsigned long long bit0, uint32_t width, uint32_t n,
+                            unsigned long long *out) {
+  unsigned long long acc = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    acc += field_from(p, bit0, width, i);
+  acc = warp_sum_ull(acc);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
+
 __global__ void k_xor80(uint8_t *p, size_t nbytes) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nbytes;
        i += (size_t)gridDim.x * blockDim.x)
@@ -647,6 +709,44 @@ cudaError_t cand_select(const uint8_t *slice, const uint8_t *tail, uint32_t r, u
 
 cudaError_t popcount_words(const uint32_t *w, size_t nw, unsigned long long *out, cudaStream_t s) {
   k_popc<<<grid_of(nw, 256), 256, 0, s>>>(w, nw, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t field_sum(const uint8_t *p, uint64_t bit0, uint32_t width, uint32_t n,
+                      unsigned long long *out, cudaStream_t s) {
+  if (!n || !width) return cudaSuccess;
+  k_field_sum<<<grid_of(n, 256), 256, 0, s>>>(p, bit0, width, n, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t rapg_decode(const buff_col *c, uint32_t R, uint32_t ks, uint32_t ts, uint64_t tbit0,
+                        double *out, cudaStream_t s) {
+  if (!c->n) return cudaSuccess;
+  RapgDecodeArgs a;
+  memset(&a, 0, sizeof(a));
+  a.obits = c->obits;
+  a.orank = c->orank;
+  a.obytes = c->obytes;
+  for (uint32_t i = 0; i < 8; ++i) a.oofs[i] = c->oofs[i];
+  a.nwp = c->nwp;
+  a.rs = rank_stride(c);
+  a.stride = c->stride;
+  a.slices = c->slices;
+  a.tail = c->tail;
+  a.n = c->n;
+  a.m = c->m;
+  a.kd = c->k - c->m;
+  a.ks = ks;
+  a.ts = ts;
+  a.R = R;
+  a.skip = c->rg_skip;
+  a.tbit0 = tbit0;
+  a.base = c->base;
+  a.dlen = (int)c->dlen;
+  a.out = out;
+  k_rapg_decode<<<grid_of(c->n, kThreads), kThreads, 0, s>>>(a);
   count_launch();
   return cudaGetLastError();
 }

@@ -303,6 +303,40 @@ int buff_slice_buffmax(const buff_col *col, double *max_value, uint32_t *argmax_
 int buff_slice_max_range(const buff_col *col, uint32_t start, uint32_t end, uint32_t window,
                          double *out, uint64_t *nout, void *stream);
 
+/* ---- RAPG byte_residue layout (compress/split_double.rs:624-2630) ----
+ * The header, then -- when ilen > 15 -- a count of sparse leading bytes and
+ * per sparse byte the rows where it is nonzero (a croaring bitmap, portable
+ * format) and those bytes, then unflipped dense slices and the packed tail.
+ * Handles made by these calls answer only the buff_rapg_* queries (and
+ * buff_serialize, which writes the reference's image). */
+
+/* byte_residue_encode (:624-955).  Reference panics (BUFF_EREFPANIC): no
+ * PRECISION_MAP entry for the scale; ilen > 15 with fewer than 2000 rows;
+ * four sparse bytes of a code at least 48 bits wide (bits_counter[32]). */
+int buff_rapg_encode_f64(const double *values, uint64_t n, uint64_t scale, uint32_t flags,
+                         void *stream, buff_col **out);
+int buff_rapg_encode_f32(const float *values, uint64_t n, uint64_t scale, uint32_t flags,
+                         void *stream, buff_col **out);
+/* A byte_residue_encode image: BUFF_ECORRUPT when its length differs from
+ * what the encoder writes for its directory, or a bitmap does not list
+ * exactly its outlier rows (below n). */
+int buff_rapg_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                          void *stream, buff_col **out);
+/* byte_residue_decode (:1353-1610): out (host or device, n values); *nout =
+ * values written.  A sparse byte without outliers panics
+ * (outlier_iter.next().unwrap()), as do reads past the image. */
+int buff_rapg_decode(const buff_col *col, double *out, uint64_t *nout, void *stream);
+/* byte_residue_decode_with_precision (:1612-1893): the top R bits of each
+ * code (R from the precision as for buff_decode_at_precision), not shifted
+ * back; *nout = 0 when R ends with the sparse bytes (the reference returns
+ * an empty vector there). */
+int buff_rapg_decode_at_precision(const buff_col *col, uint32_t precision, double *out,
+                                  uint64_t *nout, void *stream);
+/* byte_residue_sum (:2211-2407) and byte_residue_sum_with_precision
+ * (:2409-2630): the reference's f64 steps; synchronizes. */
+int buff_rapg_sum(const buff_col *col, double *sum, void *stream);
+int buff_rapg_sum_at_precision(const buff_col *col, uint32_t precision, double *sum, void *stream);
+
 /* ---- batched form (no counterpart in the reference: it runs one column per
  *      call) ---- */
 

@@ -1,0 +1,119 @@
+"""GPU parity of the RAPG byte_residue layout (compress/split_double.rs:
+624-2630) against the oracle: the image from the GPU encode and after a
+round trip through buff_rapg_deserialize byte for byte, and the full and
+precision-limited decodes and sums on both handles, panics included."""
+import numpy as np
+import pytest
+
+from tests.test_oracle_rapg import rapg_cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases():
+    rng = np.random.default_rng(17)
+    big = np.round(rng.normal(100, 5, 300_001), 6)           # one sparse byte, bitset/run rows
+    pos = np.nonzero(rng.uniform(size=big.size) < 0.01)[0]
+    big[pos] = np.round(rng.uniform(1e5, 1e6, pos.size), 6)
+    runs = np.round(rng.normal(100, 0.5, 200_003), 6)         # two sparse bytes, clustered rows
+    runs[70_000:74_000] = np.round(rng.uniform(1e4, 1e6, 4000), 6)
+    runs[150_000:150_050] = 5e5
+    narrow = np.round(rng.uniform(3.0, 3.06, 5000), 2)        # codes narrower than dlen
+    narrow0 = narrow.copy()                                     # ... whose first packed byte is 0
+    narrow0[:2] = 3.0
+    narrow0[2:] = np.maximum(narrow0[2:], 3.01)
+    tenth = np.round(rng.uniform(0.0, 1.9, 4097), 1)          # scale 10: packed codes, no count byte
+    tiny = np.array([0.1, 0.5, 1.2])
+    f32 = np.round(rng.normal(10, 3, 50_001), 2).astype(np.float32)
+    return rapg_cases() + [("big", big, 1000000), ("runs", runs, 1000000),
+                           ("narrow", narrow, 100), ("narrow0", narrow0, 100),
+                           ("tenth", tenth, 10), ("tiny", tiny, 10),
+                           ("f32", f32, 100)]
+
+
+CASES = _cases()
+
+
+def _check(oracle, col, img, scale, name):
+    from buff_gb300 import capi
+
+    for p in [None] + list(range(16)):
+        prec = -1 if p is None else p
+        try:
+            want = oracle.rapg_decode(img, scale, prec)
+        except oracle.OraclePanic:
+            with pytest.raises(capi.ReferencePanic):
+                col.decode() if p is None else col.decode_at_precision(p)
+            with pytest.raises(capi.ReferencePanic):
+                col.rapg_sum(p)
+            continue
+        got = col.decode() if p is None else col.decode_at_precision(p)
+        assert got.size == want.size and np.array_equal(got, want), (name, p)
+        want_s = oracle.rapg_sum(img, scale, prec)
+        got_s = col.rapg_sum(p)
+        assert got_s == want_s or (np.isnan(got_s) and np.isnan(want_s)), (name, p)
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_rapg_parity(oracle, gpu, case):
+    from buff_gb300 import capi
+    from buff_gb300.compress import RapgColumn
+
+    name, x, scale = CASES[case]
+    xd = np.asarray(x, dtype=np.float64)
+    try:
+        img = oracle.rapg_encode(xd, scale)
+    except oracle.OraclePanic:
+        with pytest.raises(capi.ReferencePanic):
+            RapgColumn.encode(x, scale)
+        return
+    col = RapgColumn.encode(x, scale)
+    assert col.serialize() == img, name
+    try:
+        cols = oracle.rapg_layout(img)[0]
+    except oracle.OraclePanic:  # packed codes read as a column directory
+        cols = 0
+    assert col.info.outlier_cols == cols
+    back = RapgColumn.deserialize(img, scale)
+    assert back.serialize() == img
+    _check(oracle, col, img, scale, name)
+    _check(oracle, back, img, scale, name + "/image")
+
+
+def test_rapg_device_input_and_output(oracle, gpu):
+    import torch
+
+    from buff_gb300.compress import RapgColumn
+
+    name, x, scale = CASES[6]
+    img = oracle.rapg_encode(x, scale)
+    col = RapgColumn.encode(torch.from_numpy(x).cuda(), scale)
+    assert col.serialize() == img
+    out = torch.empty(x.size, dtype=torch.float64, device="cuda")
+    _, k = col.decode(out=out)
+    assert k == x.size and np.array_equal(out.cpu().numpy(), oracle.rapg_decode(img, scale))
+    dimg = torch.from_numpy(np.frombuffer(img, dtype=np.uint8).copy()).cuda()
+    back = RapgColumn.deserialize(dimg, scale)
+    assert back.serialize() == img
+
+
+def test_rapg_errors(oracle, gpu):
+    from buff_gb300 import capi
+    from buff_gb300.compress import Column, RapgColumn
+
+    name, x, scale = CASES[2]  # one sparse byte
+    img = oracle.rapg_encode(x, scale)
+    for bad in (img[:-1], img + b"\x00", img[:30]):
+        with pytest.raises(capi.BuffError) as e:
+            RapgColumn.deserialize(bad, scale)
+        assert e.value.status == capi.ECORRUPT
+    col = RapgColumn.encode(x, scale)
+    for fn in (lambda: Column.decode(col), lambda: Column.range_filter(col, 1.0),
+               lambda: Column.sum(col)):
+        with pytest.raises(capi.BuffError) as e:
+            fn()
+        assert e.value.status == capi.ENOTSUP
+    plain = Column.encode(x, scale)
+    with pytest.raises(capi.BuffError) as e:
+        RapgColumn.decode(plain)
+    assert e.value.status == capi.ENOTSUP
