@@ -113,7 +113,12 @@ def test_rapg_errors(oracle, gpu):
         with pytest.raises(capi.BuffError) as e:
             fn()
         assert e.value.status == capi.ENOTSUP
+    import ctypes as C
+
     plain = Column.encode(x, scale)
-    with pytest.raises(capi.BuffError) as e:
-        RapgColumn.decode(plain)
-    assert e.value.status == capi.ENOTSUP
+    out = np.empty(x.size, dtype=np.float64)
+    k = C.c_uint64(0)
+    v = C.c_double(0)
+    L = capi.lib()
+    assert L.buff_rapg_decode(plain.handle, out.ctypes.data, C.byref(k), None) == capi.ENOTSUP
+    assert L.buff_rapg_sum(plain.handle, C.byref(v), None) == capi.ENOTSUP
