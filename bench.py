@@ -398,6 +398,73 @@ def run_outlier_form(args, stream, peak):
     return out
 
 
+def run_rapg_form(args, stream):
+    """RAPG byte_residue layout on 67,108,864 rows with high outliers (99%
+    N(100,5), 1% U(1e5,1e6), 6 decimals, scale 1e6): encode, full and
+    precision-limited decode and sum (the p_scan sequence).  The CPU leg
+    times the oracle's byte_residue_decode and _sum on the first 2^22 rows
+    (one thread)."""
+    import ctypes as C
+
+    import torch
+
+    from buff_gb300 import capi
+    from buff_gb300.compress import RapgColumn
+    from buff_gb300.workloads import high_outlier_column_torch
+
+    L = capi.lib()
+    sh = stream.cuda_stream
+    n = args.outlier_rows
+    x = high_outlier_column_torch(n)
+    torch.cuda.synchronize()
+
+    def enc():
+        RapgColumn.encode(x, 1000000, stream=stream).free()
+
+    t_enc = time_op(enc, 3, stream)
+    col = RapgColumn.encode(x, 1000000, stream=stream)
+    info = col.info
+    h = col.handle
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    k = C.c_uint64(0)
+    ops = {"encode": {"ms": t_enc * 1e3, "gvalues_s": n / t_enc / 1e9,
+                      "gb_s_input": 8 * n / t_enc / 1e9}}
+    code_bytes = info.device_bytes
+    t = time_op(lambda: L.buff_rapg_decode(h, out.data_ptr(), C.byref(k), sh), 5, stream)
+    ops["decode"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
+                     "gb_s_alg": (code_bytes + 8 * n) / t / 1e9}
+    for p in (0, 3, 5):
+        t = time_op(lambda: L.buff_rapg_decode_at_precision(h, p, out.data_ptr(), C.byref(k), sh),
+                    5, stream)
+        ops[f"decode_p{p}"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9}
+    v = C.c_double(0)
+    t = time_op(lambda: L.buff_rapg_sum(h, C.byref(v), sh), 5, stream)
+    ops["sum"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "note": "includes the host combine"}
+    t = time_op(lambda: L.buff_rapg_sum_at_precision(h, 3, C.byref(v), sh), 5, stream)
+    ops["sum_p3"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9}
+    res = {"workload": f"{n} rows: 99% N(100,5), 1% U(1e5,1e6) at seeded random positions, "
+                       f"6 decimals, scale 1e6 (seed 6)", "rows": n,
+           "fixed_len": info.fixed_len, "outlier_cols": info.outlier_cols,
+           "device_bytes": code_bytes, "ops": ops}
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        xs = x[: 1 << 22].cpu().numpy()
+        img = O.rapg_encode(xs, 1000000)
+        t0 = time.perf_counter()
+        O.rapg_decode(img, 1000000)
+        t1 = time.perf_counter()
+        O.rapg_sum(img, 1000000)
+        t2 = time.perf_counter()
+        res["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": f"first {xs.size} rows",
+                               "decode_gvalues_s": xs.size / (t1 - t0) / 1e9,
+                               "sum_gvalues_s": xs.size / (t2 - t1) / 1e9}
+    col.free()
+    del x, out
+    torch.cuda.empty_cache()
+    return res
+
+
 # ---------------------------------------------------------------- batched form
 
 def run_batched_form(args, stream, peak):
@@ -886,7 +953,7 @@ def main():
                "sample": f"first {rows} rows of the column, 3 timed passes of filter+sum, "
                          f"1 thread", "mib_s": mib_s(rows, per_step), "host": host_cpu()}
 
-    batched_form = serving_form = outlier_form = small_form = None
+    batched_form = serving_form = outlier_form = small_form = rapg_form = None
     if rank == 0 and world == 1:
         col.free()
         col = None
@@ -897,6 +964,7 @@ def main():
             small_form = run_small_form(stream)
         if not args.no_outlier:
             outlier_form = run_outlier_form(args, stream, peak)
+            rapg_form = run_rapg_form(args, stream)
         if not args.no_batched:
             batched_form = run_batched_form(args, stream, peak)
         if not args.no_serve:
@@ -931,6 +999,7 @@ def main():
             "encode_once_s": time.time() - t0,
             "gaussian_walk_1e6": small_form,
             "outlier": outlier_form,
+            "rapg": rapg_form,
             "batched": batched_form,
             "serving": serving_form,
         }

@@ -1989,12 +1989,12 @@ int rapg_decode_impl(const buff_col *c, int precision, double *out, uint64_t *no
   for (uint32_t col = 0; col < c->m; ++col)
     if (c->nout[col] == 0) return BUFF_EREFPANIC;  // outlier_iter.next().unwrap() (:1393)
   if (!p.emit || c->n == 0) return BUFF_OK;
-  const bool stage = !is_device_ptr(out);
+  const bool stage = !is_device_ptr(out) || (reinterpret_cast<uintptr_t>(out) & 15);
   double *d = stage ? nullptr : out;
   if (stage) CK(scratch(&d, c->n, s));
   CK(buffk::rapg_decode(c, R, p.ks, p.ts, p.tbit0, d, s));
   if (stage) {
-    CK(cudaMemcpyAsync(out, d, (size_t)c->n * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out, d, (size_t)c->n * 8, cudaMemcpyDefault, s));
     CK(cudaStreamSynchronize(s));
   }
   *nout = c->n;

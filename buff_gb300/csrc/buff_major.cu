@@ -468,29 +468,158 @@ __device__ __forceinline__ uint32_t field_from(const uint8_t *p, unsigned long l
   return ((b0 | (b1 << 8)) >> (bit & 7)) & ((1u << width) - 1u);
 }
 
+// A thread takes 4 consecutive rows: one 32-bit load per dense slice, the
+// 4 rows' bits of each sparse column from one bitmap word, two 16-byte
+// stores (out 16-byte aligned).
 __global__ void __launch_bounds__(kThreads) k_rapg_decode(RapgDecodeArgs a) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const size_t w = i >> 5;
-    const uint32_t j = (uint32_t)(i & 31);
-    unsigned long long v = 0;
+  const uint32_t ngroups = (a.n + 3) / 4;
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups;
+       g += gridDim.x * blockDim.x) {
+    const uint32_t row0 = g * 4;
+    const size_t w = row0 >> 5;
+    const uint32_t j0 = row0 & 31;
+    unsigned long long v[4] = {0, 0, 0, 0};
     uint32_t remain = a.R;
     for (uint32_t c = 0; c < a.m; ++c) {
       remain -= 8;
-      const uint32_t B = a.obits[c * a.nwp + w];
-      if (B >> j & 1u) {
-        const uint32_t k = a.orank[c * a.rs + w] + __popc(B & ((1u << j) - 1u));
-        v |= (unsigned long long)a.obytes[a.oofs[c] + k] << (remain & 63);
+      const uint32_t B = __ldg(a.obits + c * a.nwp + w);
+      const uint32_t nib = (B >> j0) & 0xFu;
+      if (nib) {
+        uint32_t k = __ldg(a.orank + c * a.rs + w) + __popc(B & ((1u << j0) - 1u));
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (nib >> i & 1u) v[i] |= (unsigned long long)a.obytes[a.oofs[c] + k++] << (remain & 63);
       }
     }
     for (uint32_t d = 0; d < a.ks; ++d) {
       remain -= 8;
-      const uint32_t byte = d < a.kd ? (a.slices[d * a.stride + i] ^ 0x80u)
-                                     : a.tail[a.skip + (size_t)(d - a.kd) * a.n + i];
-      v |= (unsigned long long)byte << (remain & 63);
+      if (d < a.kd) {
+        const uint32_t x =
+            __ldg(reinterpret_cast<const uint32_t *>(a.slices + d * a.stride + row0)) ^ 0x80808080u;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) v[i] |= (unsigned long long)((x >> (8 * i)) & 0xFFu) << (remain & 63);
+      } else {  // past the dense slices the reader takes the bytes after them
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (row0 + i < a.n)
+            v[i] |= (unsigned long long)a.tail[a.skip + (size_t)(d - a.kd) * a.n + row0 + i]
+                    << (remain & 63);
+      }
     }
-    if (a.ts) v |= field_from(a.tail, a.tbit0, a.ts, (uint32_t)i);
-    a.out[i] = i64_to_f64_scaled((long long)((unsigned long long)a.base + v), a.dlen);
+    if (a.ts) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (row0 + i < a.n) v[i] |= field_from(a.tail, a.tbit0, a.ts, row0 + i);
+    }
+    double o[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      o[i] = i64_to_f64_scaled((long long)((unsigned long long)a.base + v[i]), a.dlen);
+    if (row0 + 4 <= a.n) {
+      double2 *dst = reinterpret_cast<double2 *>(a.out + row0);
+      __stcs(dst, make_double2(o[0], o[1]));
+      __stcs(dst + 1, make_double2(o[2], o[3]));
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (row0 + i < a.n) a.out[row0 + i] = o[i];
+    }
+  }
+}
+
+// The common plans (every slice read lies in the dense region, tail fields
+// from bit 0 with ts <= r): the code is the big-endian concatenation of the
+// sparse bytes, KS dense bytes and ts tail bits.  This kernel writes every
+// row with zero sparse bytes -- the value of every row that is an outlier in
+// no sparse column -- and k_rapg_fixup rewrites the outlier rows.  Lane L
+// produces rows 64m + 2L and 64m + 2L + 1 of each 512-row chunk (coalesced
+// 16-byte stores); slice bytes are 2-byte loads; the ts-bit fields of a
+// 64-row group (8*ts bytes) are loaded by the first 2*ts lanes and handed
+// out with shuffles.
+template <int KS>
+__global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nchunks = (a.n + kRowChunk - 1) / kRowChunk;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t ts = a.ts;
+  const unsigned long long tmask = ts ? ((1ull << ts) - 1ull) : 0ull;
+  for (uint32_t ch = warp; ch < nchunks; ch += nwarps) {
+    const uint32_t r0 = ch * kRowChunk;
+    uint32_t sb[8][KS > 0 ? KS : 1];
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+#pragma unroll
+      for (int s = 0; s < KS; ++s)
+        sb[m][s] = __ldg(reinterpret_cast<const uint16_t *>(a.slices + s * a.stride + r0 +
+                                                            m * 64 + 2 * lane));
+    uint32_t tw[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      tw[m] = 0;
+      if (ts && lane < 2 * ts)
+        tw[m] = __ldg(reinterpret_cast<const uint32_t *>(a.tail + (size_t)8 * ts * (r0 / 64 + m)) +
+                      lane);
+    }
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const uint32_t i0 = r0 + m * 64 + 2 * lane;
+      unsigned long long c0 = 0, c1 = 0;
+#pragma unroll
+      for (int s = 0; s < KS; ++s) {
+        c0 = (c0 << 8) | ((sb[m][s] & 0xFFu) ^ 0x80u);
+        c1 = (c1 << 8) | (((sb[m][s] >> 8) & 0xFFu) ^ 0x80u);
+      }
+      if (ts) {
+        const uint32_t bit = 2 * lane * ts, wi = bit >> 5;
+        const uint32_t w0 = __shfl_sync(0xFFFFFFFFu, tw[m], wi);
+        const uint32_t w1 = __shfl_sync(0xFFFFFFFFu, tw[m], (wi + 1) & 31);
+        const uint32_t f = __funnelshift_r(w0, w1, bit & 31);
+        c0 = (c0 << ts) | (f & tmask);
+        c1 = (c1 << ts) | ((f >> ts) & tmask);
+      }
+      const double v0 = i64_to_f64_scaled((long long)((unsigned long long)a.base + c0), a.dlen);
+      const double v1 = i64_to_f64_scaled((long long)((unsigned long long)a.base + c1), a.dlen);
+      if (i0 + 2 <= a.n)
+        __stcs(reinterpret_cast<double2 *>(a.out + i0), make_double2(v0, v1));
+      else if (i0 < a.n)
+        a.out[i0] = v0;
+    }
+  }
+}
+
+// Rows that are outliers in some sparse column, decoded in full after
+// k_rapg_decode_fast wrote them with zero sparse bytes: one thread per
+// 32-row bitmap word, the rows of the union of the columns' words.
+__global__ void __launch_bounds__(kThreads) k_rapg_fixup(RapgDecodeArgs a) {
+  const size_t nw = ((size_t)a.n + 31) / 32;
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
+       w += (size_t)gridDim.x * blockDim.x) {
+    // bitmap words and ranks of all sparse columns, loaded together
+    uint32_t Bw[8], Rk[8], any = 0;
+#pragma unroll
+    for (uint32_t c = 0; c < 8; ++c) {
+      Bw[c] = c < a.m ? __ldg(a.obits + c * a.nwp + w) : 0u;
+      Rk[c] = c < a.m ? __ldg(a.orank + c * a.rs + w) : 0u;
+      any |= Bw[c];
+    }
+    while (any) {
+      const uint32_t j = __ffs(any) - 1;
+      any &= any - 1;
+      const uint32_t i = (uint32_t)(w * 32 + j);
+      unsigned long long v = 0;
+#pragma unroll
+      for (uint32_t c = 0; c < 8; ++c) {
+        if (c < a.m) {
+          uint32_t b = 0;
+          if (Bw[c] >> j & 1u) b = a.obytes[a.oofs[c] + Rk[c] + __popc(Bw[c] & ((1u << j) - 1u))];
+          v = (v << 8) | b;
+        }
+      }
+      for (uint32_t d = 0; d < a.ks; ++d) v = (v << 8) | (a.slices[d * a.stride + i] ^ 0x80u);
+      if (a.ts) v = (v << a.ts) | field_from(a.tail, 0, a.ts, i);
+      a.out[i] = i64_to_f64_scaled((long long)((unsigned long long)a.base + v), a.dlen);
+    }
   }
 }
 
@@ -746,7 +875,26 @@ cudaError_t rapg_decode(const buff_col *c, uint32_t R, uint32_t ks, uint32_t ts,
   a.base = c->base;
   a.dlen = (int)c->dlen;
   a.out = out;
-  k_rapg_decode<<<grid_of(c->n, kThreads), kThreads, 0, s>>>(a);
+  if (ks <= a.kd && ks <= 8 && tbit0 == 0 && ts <= c->r) {
+    const int g = grid_of((size_t)(c->n + kRowChunk - 1) / kRowChunk * 32, kThreads);
+    switch (ks) {
+      case 0: k_rapg_decode_fast<0><<<g, kThreads, 0, s>>>(a); break;
+      case 1: k_rapg_decode_fast<1><<<g, kThreads, 0, s>>>(a); break;
+      case 2: k_rapg_decode_fast<2><<<g, kThreads, 0, s>>>(a); break;
+      case 3: k_rapg_decode_fast<3><<<g, kThreads, 0, s>>>(a); break;
+      case 4: k_rapg_decode_fast<4><<<g, kThreads, 0, s>>>(a); break;
+      case 5: k_rapg_decode_fast<5><<<g, kThreads, 0, s>>>(a); break;
+      case 6: k_rapg_decode_fast<6><<<g, kThreads, 0, s>>>(a); break;
+      case 7: k_rapg_decode_fast<7><<<g, kThreads, 0, s>>>(a); break;
+      default: k_rapg_decode_fast<8><<<g, kThreads, 0, s>>>(a); break;
+    }
+    if (a.m) {
+      count_launch();
+      k_rapg_fixup<<<grid_of(((size_t)c->n + 31) / 32, kThreads), kThreads, 0, s>>>(a);
+    }
+  } else {
+    k_rapg_decode<<<grid_of((c->n + 3) / 4, kThreads), kThreads, 0, s>>>(a);
+  }
   count_launch();
   return cudaGetLastError();
 }

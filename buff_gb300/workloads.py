@@ -61,6 +61,21 @@ def outlier_column_torch(n: int, seed: int = 3, device="cuda"):
     return torch.round(x * 1e6) / 1e6
 
 
+def high_outlier_column_torch(n: int, seed: int = 6, device="cuda"):
+    """99% N(100, 5) and 1% U(1e5, 1e6) at seeded random positions, 6
+    decimals, generated on the device (float64): the outliers sit above the
+    bulk, so the leading code byte is zero on 99% of the rows."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    x = torch.randn(n, generator=g, device=device, dtype=torch.float64) * 5.0 + 100.0
+    m = max(1, n // 100)
+    pos = torch.randperm(n, generator=g, device=device)[:m]
+    x[pos] = 1e5 + torch.rand(m, generator=g, device=device, dtype=torch.float64) * 9e5
+    return torch.round(x * 1e6) / 1e6
+
+
 def bounded_walk_torch(n: int, seed: int = 2, device="cuda"):
     """bounded_walk generated on the device (float64)."""
     import torch

@@ -92,6 +92,9 @@ def test_rapg_device_input_and_output(oracle, gpu):
     out = torch.empty(x.size, dtype=torch.float64, device="cuda")
     _, k = col.decode(out=out)
     assert k == x.size and np.array_equal(out.cpu().numpy(), oracle.rapg_decode(img, scale))
+    odd = torch.empty(x.size + 1, dtype=torch.float64, device="cuda")  # 8-byte aligned view
+    _, k = col.decode(out=odd[1:])
+    assert np.array_equal(odd[1:].cpu().numpy(), oracle.rapg_decode(img, scale))
     dimg = torch.from_numpy(np.frombuffer(img, dtype=np.uint8).copy()).cuda()
     back = RapgColumn.deserialize(dimg, scale)
     assert back.serialize() == img
