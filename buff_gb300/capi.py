@@ -46,6 +46,9 @@ EXPORTED = [
     "buff_slice_buffsum", "buff_slice_max", "buff_slice_buffmax",
     "buff_rapg_encode_f64", "buff_rapg_encode_f32", "buff_rapg_deserialize", "buff_rapg_decode",
     "buff_rapg_decode_at_precision", "buff_rapg_sum", "buff_rapg_sum_at_precision",
+    "buff_rapg_encode_outlieru8_f64", "buff_rapg_encode_outlieru8_f32",
+    "buff_rapg_major_deserialize", "buff_rapg_decode_majority", "buff_rapg_range_filter_majority",
+    "buff_rapg_equal_filter_majority", "buff_rapg_sum_majority", "buff_rapg_max_majority",
 ]
 
 Q_RANGE, Q_EQUAL, Q_SUM, Q_MAX, Q_DECODE = 0x1, 0x2, 0x4, 0x8, 0x10
@@ -213,6 +216,14 @@ def lib(build_if_missing: bool = True):
     L.buff_rapg_decode_at_precision.argtypes = [P, C.c_uint32, P, P, P]
     L.buff_rapg_sum.argtypes = [P, P, P]
     L.buff_rapg_sum_at_precision.argtypes = [P, C.c_uint32, P, P]
+    L.buff_rapg_encode_outlieru8_f64.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_rapg_encode_outlieru8_f32.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_rapg_major_deserialize.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
+    L.buff_rapg_decode_majority.argtypes = [P, P, P]
+    L.buff_rapg_range_filter_majority.argtypes = [P, C.c_double, P, P, P]
+    L.buff_rapg_equal_filter_majority.argtypes = [P, C.c_double, P, P, P]
+    L.buff_rapg_sum_majority.argtypes = [P, C.POINTER(SumResult), P]
+    L.buff_rapg_max_majority.argtypes = [P, P, P, P, P, P]
     L.buff_status_string.argtypes = [C.c_int]
     L.buff_status_string.restype = C.c_char_p
     L.buff_last_cuda_error.restype = C.c_int

@@ -292,6 +292,13 @@ class Column:
         return MaxResult(v.value, code.value, words, cnt.value)
 
 
+def _maj_fn(col, i):
+    """The i-th majority entry point for `col`'s kind (a plain handle gets
+    the buff-major ones, which reject it)."""
+    names = getattr(col, "_MAJ", None) or MajorColumn._MAJ
+    return getattr(lib(), names[i])
+
+
 class MajorColumn(Column):
     """A buff-major (outlier) column resident in HBM: sparse leading byte
     columns kept as (major byte, outlier bitmap, outlier bytes), the rest as
@@ -301,24 +308,27 @@ class MajorColumn(Column):
     _DESERIALIZE = "buff_deserialize_majority"
     _DECODE_CONDITION = "buff_major_decode_condition"
     _FILTER_CONDITION = "buff_range_filter_majority_condition"
+    _MAJ = ("buff_decode_majority", "buff_range_filter_majority", "buff_equal_filter_majority",
+            "buff_sum_majority", "buff_max_majority")
 
     def decode(self, out=None, stream=None):
+        fn = _maj_fn(self, 0)
         if out is None:
             out = np.empty(max(self.n, 1), dtype=np.float64)
-            check(lib().buff_decode_majority(self._h, ptr(out), stream_handle(stream)), "decode")
+            check(fn(self._h, ptr(out), stream_handle(stream)), "decode")
             return out[: self.n]
-        check(lib().buff_decode_majority(self._h, ptr(out), stream_handle(stream)), "decode")
+        check(fn(self._h, ptr(out), stream_handle(stream)), "decode")
         return out
 
     def range_filter(self, pred, out=None, stream=None):
-        return self._filter(lib().buff_range_filter_majority, pred, out, stream)
+        return self._filter(_maj_fn(self, 1), pred, out, stream)
 
     def equal_filter(self, pred, out=None, stream=None):
-        return self._filter(lib().buff_equal_filter_majority, pred, out, stream)
+        return self._filter(_maj_fn(self, 2), pred, out, stream)
 
     def sum(self, stream=None) -> capi.SumResult:
         res = capi.SumResult()
-        check(lib().buff_sum_majority(self._h, C.byref(res), stream_handle(stream)), "sum")
+        check(_maj_fn(self, 3)(self._h, C.byref(res), stream_handle(stream)), "sum")
         return res
 
     def max(self, argmax: bool = False, stream=None) -> MaxResult:
@@ -326,9 +336,9 @@ class MajorColumn(Column):
         code = C.c_uint64(0)
         cnt = C.c_uint64(0)
         words = np.zeros(max((self.n + 31) // 32, 1), dtype=np.uint32) if argmax else None
-        check(lib().buff_max_majority(self._h, C.byref(v), C.byref(code), ptr(words),
-                                      C.byref(cnt) if argmax else None, stream_handle(stream)),
-              "max")
+        check(_maj_fn(self, 4)(self._h, C.byref(v), C.byref(code), ptr(words),
+                                           C.byref(cnt) if argmax else None,
+                                           stream_handle(stream)), "max")
         if words is not None:
             words = words[: (self.n + 31) // 32]
         return MaxResult(v.value, code.value, words, cnt.value)
@@ -339,6 +349,23 @@ class MajorColumn(Column):
     decode_at_precision = sum_at_precision = _unsupported
     range_filter_with_slice = equal_filter_with_slice = _unsupported
     decode_selected = range_filter_decode = _unsupported
+
+
+class RapgMajorColumn(MajorColumn):
+    """A RAPG-major column (compress/split_double.rs:957-1240,
+    byte_residue_encode_outlieru8): the buff-major layout with the leading
+    byte as the one sparse column, major byte 69, croaring bitmap in the
+    image; queried through the byte_residue_*_majority entry points."""
+
+    _ENCODE = ("buff_rapg_encode_outlieru8_f32", "buff_rapg_encode_outlieru8_f64")
+    _DESERIALIZE = "buff_rapg_major_deserialize"
+    _MAJ = ("buff_rapg_decode_majority", "buff_rapg_range_filter_majority",
+            "buff_rapg_equal_filter_majority", "buff_rapg_sum_majority", "buff_rapg_max_majority")
+
+    def _unsupported(self, *a, **k):
+        raise capi.BuffError(capi.ENOTSUP, "not defined on RAPG-major columns")
+
+    decode_condition = range_filter_condition = _unsupported
 
 
 class SliceColumn(Column):
@@ -559,6 +586,35 @@ class SplitBDDoubleCompress:
     def byte_residue_sum(self, data, stream=None) -> float:
         return _as_rapg(self, data).rapg_sum(stream=stream)
 
+    # compress/split_double.rs:957-1240 (outlier_exp's encoder)
+    def byte_residue_encode_outlieru8(self, values, stream=None) -> RapgMajorColumn:
+        return RapgMajorColumn.encode(values, self.scale, self.flags, stream)
+
+    def _rapg_major(self, data) -> RapgMajorColumn:
+        if isinstance(data, RapgMajorColumn):
+            return data
+        return RapgMajorColumn.deserialize(data, self.scale, self.flags)
+
+    # compress/split_double.rs:1897-2125
+    def byte_residue_decode_majority(self, data, stream=None):
+        return self._rapg_major(data).decode(stream=stream)
+
+    # compress/split_double.rs:2958-3370 (the reference prints the count)
+    def byte_residue_range_filter_majority(self, data, pred, stream=None) -> FilterResult:
+        return self._rapg_major(data).range_filter(pred, stream=stream)
+
+    # compress/split_double.rs:3541-3918
+    def byte_residue_equal_filter_majority(self, data, pred, stream=None) -> FilterResult:
+        return self._rapg_major(data).equal_filter(pred, stream=stream)
+
+    # compress/split_double.rs:2632-2782
+    def byte_residue_sum_majority(self, data, stream=None) -> float:
+        return self._rapg_major(data).sum(stream=stream).sum
+
+    # compress/split_double.rs:4107-4676 (the reference prints the max)
+    def byte_residue_max_majority(self, data, stream=None) -> MaxResult:
+        return self._rapg_major(data).max(argmax=True, stream=stream)
+
     # compress/split_double.rs:2409-2630
     def byte_residue_sum_with_precision(self, data, precision: int, stream=None) -> float:
         if isinstance(data, Column) and not isinstance(data, RapgColumn):
@@ -612,6 +668,6 @@ class SplitBDDoubleCompress:
 
 
 __all__ = ["SplitBDDoubleCompress", "BuffSliceCompress", "Column", "MajorColumn", "SliceColumn",
-           "RapgColumn",
+           "RapgColumn", "RapgMajorColumn",
            "FilterResult", "MaxResult",
            "FLAG_INTENDED", "FLAG_RAW_BITMAPS", "FLAG_BUFF_LAYOUT", "rows_to_words"]

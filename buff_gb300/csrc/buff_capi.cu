@@ -506,9 +506,13 @@ static void bm_vote(const uint64_t *codes, uint32_t cnt, uint32_t sh, uint8_t *m
   *freq = f;
 }
 
+// forced_major >= 0: byte_residue_encode_outlieru8 (compress/split_double.rs:
+// 957-1240), whose vote result is overwritten with MAJOR = 69 and whose count
+// is never negative, so the leading byte is always the one sparse column; its
+// bitmaps are croaring images.
 template <typename T>
 int encode_major_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, cudaStream_t s,
-                      buff_col **out) {
+                      buff_col **out, int forced_major = -1) {
   if (!out) return BUFF_EINVAL;
   *out = nullptr;
   if (flags & BUFF_FLAG_INTENDED) return BUFF_ENOTSUP;
@@ -567,7 +571,10 @@ int encode_major_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t fl
     uint8_t major;
     int32_t freq;
     bm_vote(codes, 2000, rsf, &major, &freq);
-    if (freq > limit) {
+    if (forced_major >= 0) {
+      c->majors[m++] = (uint8_t)forced_major;
+      c->bm_roaring = 1;
+    } else if (freq > limit) {
       c->majors[m++] = major;
       while (rsf > 7 && m < 8) {
         rsf -= 8;
@@ -651,7 +658,8 @@ int major_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s) {
       for (int b = 0; b < 8; ++b) bin[b] = (uint8_t)((uint64_t)n >> (8 * b));
       for (size_t w = 0; w < nw; ++w)
         for (int b = 0; b < 4; ++b) bin[8 + 4 * w + b] = (uint8_t)(bits[col * nw + w] >> (8 * b));
-      std::vector<uint8_t> bm = (c->flags & BUFF_FLAG_RAW_BITMAPS)
+      std::vector<uint8_t> bm = c->bm_roaring ? buffroaring::serialize(bits.data() + col * nw, n)
+                                : (c->flags & BUFF_FLAG_RAW_BITMAPS)
                                     ? bin
                                     : buffsnappy::compress(bin.data(), bin.size());
       img.push_back(c->majors[col]);
@@ -1295,8 +1303,15 @@ int buff_encode_majority_f32(const float *values, uint64_t n, uint64_t scale, ui
   return encode_major_impl<float>(values, n, scale, flags, S(stream), out);
 }
 
-int buff_deserialize_majority(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
-                              void *stream, buff_col **out) {
+}  // extern "C"
+
+namespace {
+
+// A buff-major image (snappy or raw BitVec bitmaps), or with `roaring` the
+// RAPG-major image of byte_residue_encode_outlieru8 (croaring bitmaps, one
+// sparse column: its queries equal the buff-major ones only there).
+int deserialize_major_impl(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                           void *stream, buff_col **out, bool roaring) {
   if (!out || !bytes) return BUFF_EINVAL;
   *out = nullptr;
   if (flags & BUFF_FLAG_INTENDED) return BUFF_ENOTSUP;
@@ -1320,9 +1335,11 @@ int buff_deserialize_majority(const uint8_t *bytes, uint64_t len, uint64_t scale
     w5[i] = (uint32_t)b[4 * i] | ((uint32_t)b[4 * i + 1] << 8) | ((uint32_t)b[4 * i + 2] << 16) |
             ((uint32_t)b[4 * i + 3] << 24);
   m = b[20];
+  if (roaring && m != 1) return BUFF_ENOTSUP;
   c = new_col(scale, flags);
   if (!c) return BUFF_ENOMEM;
   c->layout = 1;
+  c->bm_roaring = roaring ? 1u : 0u;
   c->base = (int64_t)((uint64_t)w5[0] | ((uint64_t)w5[1] << 32));
   c->n = w5[2];
   c->ilen = w5[3];
@@ -1353,21 +1370,32 @@ int buff_deserialize_majority(const uint8_t *bytes, uint64_t len, uint64_t scale
         goto done;
       }
       std::vector<uint8_t> bin;
-      if (flags & BUFF_FLAG_RAW_BITMAPS) {
-        bin.assign(b + pos + 5, b + pos + 5 + bml);
-      } else if (!buffsnappy::decompress(b + pos + 5, bml, bin)) {
-        rc = BUFF_ECORRUPT;
-        goto done;
-      }
-      // BitVec::from_binary (bit-vec lib.rs:409-428)
       std::vector<uint32_t> words(nw, 0);
-      for (size_t at = 8, w = 0; at + 4 <= bin.size() && w < nw; at += 4, ++w)
-        words[w] = (uint32_t)bin[at] | ((uint32_t)bin[at + 1] << 8) |
-                   ((uint32_t)bin[at + 2] << 16) | ((uint32_t)bin[at + 3] << 24);
-      if (nw && (c->n & 31)) words[nw - 1] &= (1u << (c->n & 31)) - 1u;
-      bms.push_back(std::move(words));
       const size_t np = pos + 5 + bml;
       const uint32_t nout = rd32(np);
+      if (roaring) {
+        // Bitmap::deserialize: rows below n, one per outlier byte
+        std::vector<uint32_t> rows;
+        if (!buffroaring::parse(b + pos + 5, bml, rows) || rows.size() != nout ||
+            (nout && rows.back() >= c->n)) {
+          rc = BUFF_ECORRUPT;
+          goto done;
+        }
+        for (uint32_t r : rows) words[r >> 5] |= 1u << (r & 31);
+      } else {
+        if (flags & BUFF_FLAG_RAW_BITMAPS) {
+          bin.assign(b + pos + 5, b + pos + 5 + bml);
+        } else if (!buffsnappy::decompress(b + pos + 5, bml, bin)) {
+          rc = BUFF_ECORRUPT;
+          goto done;
+        }
+        // BitVec::from_binary (bit-vec lib.rs:409-428)
+        for (size_t at = 8, w = 0; at + 4 <= bin.size() && w < nw; at += 4, ++w)
+          words[w] = (uint32_t)bin[at] | ((uint32_t)bin[at + 1] << 8) |
+                     ((uint32_t)bin[at + 2] << 16) | ((uint32_t)bin[at + 3] << 24);
+        if (nw && (c->n & 31)) words[nw - 1] &= (1u << (c->n & 31)) - 1u;
+      }
+      bms.push_back(std::move(words));
       if (np + 4 + (uint64_t)nout > len) {
         rc = BUFF_ECORRUPT;
         goto done;
@@ -1426,6 +1454,63 @@ done:
   }
   *out = c;
   return BUFF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int buff_deserialize_majority(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                              void *stream, buff_col **out) {
+  return deserialize_major_impl(bytes, len, scale, flags, stream, out, false);
+}
+
+// ---- RAPG-major (byte_residue_encode_outlieru8 and its queries) ----
+
+int buff_rapg_encode_outlieru8_f64(const double *values, uint64_t n, uint64_t scale, uint32_t flags,
+                                   void *stream, buff_col **out) {
+  if (flags & BUFF_FLAG_RAW_BITMAPS) return BUFF_ENOTSUP;
+  return encode_major_impl<double>(values, n, scale, flags, S(stream), out, 69);
+}
+
+int buff_rapg_encode_outlieru8_f32(const float *values, uint64_t n, uint64_t scale, uint32_t flags,
+                                   void *stream, buff_col **out) {
+  if (flags & BUFF_FLAG_RAW_BITMAPS) return BUFF_ENOTSUP;
+  return encode_major_impl<float>(values, n, scale, flags, S(stream), out, 69);
+}
+
+int buff_rapg_major_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                                void *stream, buff_col **out) {
+  if (flags & BUFF_FLAG_RAW_BITMAPS) return BUFF_ENOTSUP;
+  return deserialize_major_impl(bytes, len, scale, flags, stream, out, true);
+}
+
+int buff_rapg_decode_majority(const buff_col *c, double *out, void *stream) {
+  if (c && !c->bm_roaring) return BUFF_ENOTSUP;
+  return buff_decode_majority(c, out, stream);
+}
+
+int buff_rapg_range_filter_majority(const buff_col *c, double pred, uint32_t *words,
+                                    uint64_t *count, void *stream) {
+  if (c && !c->bm_roaring) return BUFF_ENOTSUP;
+  return buff_range_filter_majority(c, pred, words, count, stream);
+}
+
+int buff_rapg_equal_filter_majority(const buff_col *c, double pred, uint32_t *words,
+                                    uint64_t *count, void *stream) {
+  if (c && !c->bm_roaring) return BUFF_ENOTSUP;
+  return buff_equal_filter_majority(c, pred, words, count, stream);
+}
+
+int buff_rapg_sum_majority(const buff_col *c, buff_sum_result *out, void *stream) {
+  if (c && !c->bm_roaring) return BUFF_ENOTSUP;
+  return buff_sum_majority(c, out, stream);
+}
+
+int buff_rapg_max_majority(const buff_col *c, double *value, uint64_t *code, uint32_t *argmax,
+                           uint64_t *argmax_count, void *stream) {
+  if (c && !c->bm_roaring) return BUFF_ENOTSUP;
+  return buff_max_majority(c, value, code, argmax, argmax_count, stream);
 }
 
 int buff_range_filter_majority(const buff_col *c, double pred, uint32_t *words, uint64_t *count,

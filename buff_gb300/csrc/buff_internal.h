@@ -56,6 +56,9 @@ struct buff_col {
   uint32_t rg_count_byte;  // the image carries the outlier-column count byte (ilen > 15)
   uint32_t rg_skip;        // bytes of `tail` before where the readers start reading it
   uint32_t rg_bad;         // the readers would take packed codes for a column directory
+  // buff-major columns of the RAPG-major image (byte_residue_encode_outlieru8):
+  // the outlier bitmaps are croaring portable images instead of snappy BitVecs
+  uint32_t bm_roaring;
 };
 
 // Host helpers of the C ABI (buff_capi.cu) shared with the batched and

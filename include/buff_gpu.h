@@ -337,6 +337,39 @@ int buff_rapg_decode_at_precision(const buff_col *col, uint32_t precision, doubl
 int buff_rapg_sum(const buff_col *col, double *sum, void *stream);
 int buff_rapg_sum_at_precision(const buff_col *col, uint32_t precision, double *sum, void *stream);
 
+/* ---- RAPG-major (compress/split_double.rs:957-4676, used by outlier_exp) ----
+ * byte_residue_encode_outlieru8 writes the buff-major image with exactly one
+ * sparse column -- the leading byte, major byte MAJOR = 69 (the vote it runs
+ * is overwritten, :1049) -- and the outlier rows as a croaring bitmap.  With
+ * one sparse column its queries are the buff-major ones (they differ from
+ * buff_simd.rs only in branches for further sparse columns), so these
+ * handles also answer buff_*_majority; the buff_rapg_* forms reject
+ * buff-major handles (BUFF_ENOTSUP). */
+/* byte_residue_encode_outlieru8 (:957-1240): fewer than 2000 rows or codes
+ * narrower than a byte panic (BUFF_EREFPANIC). */
+int buff_rapg_encode_outlieru8_f64(const double *values, uint64_t n, uint64_t scale, uint32_t flags,
+                                   void *stream, buff_col **out);
+int buff_rapg_encode_outlieru8_f32(const float *values, uint64_t n, uint64_t scale, uint32_t flags,
+                                   void *stream, buff_col **out);
+/* A byte_residue_encode_outlieru8 image; images with other than one sparse
+ * column return BUFF_ENOTSUP, a bitmap that does not list exactly its
+ * outlier rows BUFF_ECORRUPT. */
+int buff_rapg_major_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_t flags,
+                                void *stream, buff_col **out);
+/* byte_residue_decode_majority (:1897-2125). */
+int buff_rapg_decode_majority(const buff_col *col, double *out, void *stream);
+/* byte_residue_range_filter_majority (:2958-3370) / _equal_filter_majority
+ * (:3541-3918): the reference prints the count. */
+int buff_rapg_range_filter_majority(const buff_col *col, double pred, uint32_t *words,
+                                    uint64_t *count, void *stream);
+int buff_rapg_equal_filter_majority(const buff_col *col, double pred, uint32_t *words,
+                                    uint64_t *count, void *stream);
+/* byte_residue_sum_majority (:2632-2782). */
+int buff_rapg_sum_majority(const buff_col *col, buff_sum_result *out, void *stream);
+/* byte_residue_max_majority (:4107-4676): the reference prints the maximum. */
+int buff_rapg_max_majority(const buff_col *col, double *value, uint64_t *code, uint32_t *argmax,
+                           uint64_t *argmax_count, void *stream);
+
 /* ---- batched form (no counterpart in the reference: it runs one column per
  *      call) ---- */
 

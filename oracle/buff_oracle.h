@@ -140,11 +140,16 @@ double or_bench_filter_sum(const uint8_t *bytes, size_t len, uint64_t scale, dou
 /* --- buff-major (outlier) format: oracle/buff_oracle_major.c --- */
 #define OR_BM_SNAPPY 0 /* outlier bitmaps snappy-compressed (the reference) */
 #define OR_BM_RAW 1    /* outlier bitmaps stored as raw BitVec::to_binary bytes */
+#define OR_BM_ROARING 2 /* outlier bitmaps as croaring portable images (RAPG-major) */
 size_t or_snappy_max_compressed(size_t n);
 int or_snappy_compress(const uint8_t *in, size_t n, uint8_t *out, size_t cap, size_t *outlen);
 int or_snappy_decompress(const uint8_t *in, size_t n, uint8_t *out, size_t cap, size_t *outlen);
 int or_encode_majority(const double *x, uint32_t n, uint64_t scale, int bm_mode, uint8_t **out,
                        size_t *out_len);
+/* byte_residue_encode_outlieru8 (split_double.rs:957-1240): the majority
+ * image with one sparse column whose major byte is MAJOR (69), roaring bitmap. */
+int or_encode_outlieru8(const double *x, uint32_t n, uint64_t scale, uint8_t **out,
+                        size_t *out_len);
 int or_majority_layout(const uint8_t *bytes, size_t len, int bm_mode, uint32_t *ncols,
                        uint8_t *majors, uint32_t *nouts, size_t *dense_off);
 int or_decode_majority(const uint8_t *bytes, size_t len, uint64_t scale, int bm_mode, double *out);

@@ -200,6 +200,16 @@ int or_snappy_decompress(const uint8_t *in, size_t n, uint8_t *out, size_t cap, 
 /* bit_vec_compress (query/bit_vec_iter.rs:61-63) of BitVec::to_binary. */
 static int bm_serialize(const uint32_t *words, size_t nw, uint64_t nbits, int mode, uint8_t **out,
                         size_t *len) {
+  if (mode == OR_BM_ROARING) { /* Bitmap::create + add + run_optimize + serialize */
+    uint32_t *rows = (uint32_t *)malloc((nbits ? nbits : 1) * 4);
+    if (!rows) return OR_ENOMEM;
+    size_t cnt = 0;
+    for (uint64_t i = 0; i < nbits; i++)
+      if ((words[i >> 5] >> (i & 31)) & 1u) rows[cnt++] = (uint32_t)i;
+    int rc = or_roaring_serialize(rows, cnt, out, len);
+    free(rows);
+    return rc;
+  }
   size_t blen = 8 + 4 * nw;
   uint8_t *bin = (uint8_t *)malloc(blen);
   if (!bin) return OR_ENOMEM;
@@ -230,6 +240,17 @@ static int bm_serialize(const uint32_t *words, size_t nw, uint64_t nbits, int mo
 static int bm_parse(const uint8_t *bm, size_t bm_len, int mode, uint32_t *words, size_t nw) {
   uint8_t *bin = NULL;
   size_t blen = 0;
+  if (mode == OR_BM_ROARING) { /* Bitmap::deserialize; rows past the words are not kept */
+    uint32_t *rows = NULL;
+    size_t cnt = 0;
+    int rc = or_roaring_parse(bm, bm_len, &rows, &cnt);
+    if (rc) return rc;
+    memset(words, 0, nw * 4);
+    for (size_t i = 0; i < cnt; i++)
+      if ((rows[i] >> 5) < nw) words[rows[i] >> 5] |= 1u << (rows[i] & 31);
+    free(rows);
+    return OR_OK;
+  }
   if (mode == OR_BM_RAW) {
     bin = (uint8_t *)bm;
     blen = bm_len;
@@ -276,8 +297,27 @@ static void negate(uint32_t *w, size_t nw, uint64_t nbits) { /* BitVec::negate *
 /* buff_encode_majority (compress/buff_simd.rs:317-630)                */
 /* ------------------------------------------------------------------ */
 
+static int encode_major(const double *x, uint32_t n, uint64_t scale, int bm_mode, int forced,
+                        uint8_t **out, size_t *out_len);
+
 int or_encode_majority(const double *x, uint32_t n, uint64_t scale, int bm_mode, uint8_t **out,
                        size_t *out_len) {
+  return encode_major(x, n, scale, bm_mode, -1, out, out_len);
+}
+
+/* byte_residue_encode_outlieru8 (split_double.rs:957-1240) runs the same
+ * Boyer-Moore vote over the leading byte of the first 2000 codes, then
+ * overwrites its result with MAJOR = 69 (:1049, outlier/mod.rs:11); the
+ * vote's count is never negative, so the leading byte is always the one
+ * sparse column (:1051-1054).  The image is the buff-major image with a
+ * croaring bitmap per column. */
+int or_encode_outlieru8(const double *x, uint32_t n, uint64_t scale, uint8_t **out,
+                        size_t *out_len) {
+  return encode_major(x, n, scale, OR_BM_ROARING, 69, out, out_len);
+}
+
+static int encode_major(const double *x, uint32_t n, uint64_t scale, int bm_mode, int forced,
+                        uint8_t **out, size_t *out_len) {
   int prec = or_prec_of_scale(scale);
   int dl = or_dlen_of_prec(prec);
   if (dl < 0) return OR_PANIC;
@@ -331,7 +371,9 @@ int or_encode_majority(const double *x, uint32_t n, uint64_t scale, int bm_mode,
       else
         freq--;
     }
-    if (freq > m_limit) {
+    if (forced >= 0) {
+      majors[ncols++] = (uint8_t)forced;
+    } else if (freq > m_limit) {
       majors[ncols++] = major;
       while (rsf > 7 && ncols < 8) {
         rsf -= 8;

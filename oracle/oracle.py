@@ -85,6 +85,8 @@ def lib():
         L.or_snappy_max_compressed.restype = C.c_size_t
         L.or_snappy_compress.argtypes = [P, C.c_size_t, P, C.c_size_t, P]
         L.or_snappy_decompress.argtypes = [P, C.c_size_t, P, C.c_size_t, P]
+        L.or_encode_outlieru8.argtypes = [P, C.c_uint32, C.c_uint64, C.POINTER(u8p),
+                                          C.POINTER(C.c_size_t)]
         L.or_encode_majority.argtypes = [P, C.c_uint32, C.c_uint64, C.c_int, C.POINTER(u8p),
                                          C.POINTER(C.c_size_t)]
         L.or_majority_layout.argtypes = [P, C.c_size_t, C.c_int, P, P, P, P]
@@ -307,7 +309,7 @@ def bench_filter_sum(buf, scale, pred, nthreads=1, reps=1):
 
 
 # --- buff-major (outlier) format -------------------------------------------
-BM_SNAPPY, BM_RAW = 0, 1
+BM_SNAPPY, BM_RAW, BM_ROARING = 0, 1, 2
 
 
 def snappy_compress(data: bytes) -> bytes:
@@ -334,6 +336,19 @@ def encode_majority(x, scale: int, bm_mode: int = BM_SNAPPY) -> bytes:
     ln = C.c_size_t(0)
     _check(lib().or_encode_majority(_ptr(arr), arr.size, scale, bm_mode, C.byref(out),
                                     C.byref(ln)))
+    try:
+        return C.string_at(out, ln.value)
+    finally:
+        lib().or_free(out)
+
+
+def encode_outlieru8(x, scale: int) -> bytes:
+    """byte_residue_encode_outlieru8 (split_double.rs:957-1240): read the
+    image with bm_mode=BM_ROARING."""
+    arr = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    out = C.POINTER(C.c_uint8)()
+    ln = C.c_size_t(0)
+    _check(lib().or_encode_outlieru8(_ptr(arr), arr.size, scale, C.byref(out), C.byref(ln)))
     try:
         return C.string_at(out, ln.value)
     finally:

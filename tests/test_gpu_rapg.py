@@ -125,3 +125,55 @@ def test_rapg_errors(oracle, gpu):
     L = capi.lib()
     assert L.buff_rapg_decode(plain.handle, out.ctypes.data, C.byref(k), None) == capi.ENOTSUP
     assert L.buff_rapg_sum(plain.handle, C.byref(v), None) == capi.ENOTSUP
+
+
+# ---------------------------------------------------------------- RAPG-major
+
+@pytest.mark.parametrize("ratio,n,scale", [(0.9, 5003, 10), (0.99, 300_001, 100),
+                                           (0.5, 70_001, 1000), (0.999, 1_000_003, 10000)])
+def test_rapg_major_parity(oracle, gpu, ratio, n, scale):
+    """byte_residue_encode_outlieru8 image byte for byte from the GPU encode
+    and after a deserialize round trip; every byte_residue_*_majority query
+    against the oracle on both handles."""
+    from buff_gb300.compress import RapgMajorColumn
+    from tests.test_gpu_major import _check_queries
+    from tests.test_oracle_rapg import outlieru8_case
+
+    x, scale = outlieru8_case(ratio, n, 11, scale)
+    img = oracle.encode_outlieru8(x, scale)
+    col = RapgMajorColumn.encode(x, scale)
+    assert col.serialize() == img
+    assert col.info.outlier_cols == 1
+    _check_queries(oracle, col, img, scale, oracle.BM_ROARING, x)
+    back = RapgMajorColumn.deserialize(img, scale)
+    assert back.serialize() == img
+    _check_queries(oracle, back, img, scale, oracle.BM_ROARING, x)
+    col32 = RapgMajorColumn.encode(x.astype(np.float32), scale)
+    assert col32.serialize() == img
+
+
+def test_rapg_major_errors(oracle, gpu):
+    from buff_gb300 import capi
+    from buff_gb300.compress import MajorColumn, RapgMajorColumn
+    from tests.test_oracle_major import major_case
+    from tests.test_oracle_rapg import outlieru8_case
+
+    with pytest.raises(capi.ReferencePanic):
+        RapgMajorColumn.encode(np.full(1999, 69.0), 10)
+    with pytest.raises(capi.ReferencePanic):
+        RapgMajorColumn.encode(np.round(np.random.default_rng(1).uniform(0, 3, 3000), 0), 10)
+    x, scale = outlieru8_case(0.9, 5003, 3, 10)
+    img = oracle.encode_outlieru8(x, scale)
+    for bad in (img[:-1], img[:40]):
+        with pytest.raises(capi.BuffError):
+            RapgMajorColumn.deserialize(bad, scale)
+    # a buff-major handle is not a RAPG-major one
+    y, s2 = major_case("one", 5000, 3)
+    plain = MajorColumn.encode(y, s2)
+    out = np.empty(y.size, dtype=np.float64)
+    assert capi.lib().buff_rapg_decode_majority(plain.handle, out.ctypes.data, None) == capi.ENOTSUP
+    # images with two sparse columns are buff-major images, not RAPG-major ones
+    y, s2 = major_case("two", 5000, 3)
+    two = oracle.encode_majority(y, s2, oracle.BM_SNAPPY)
+    with pytest.raises(capi.BuffError):
+        RapgMajorColumn.deserialize(two, s2)

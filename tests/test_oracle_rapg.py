@@ -291,3 +291,49 @@ def test_rapg_panics(oracle):
     name, x, scale = rapg_cases()[0]
     with pytest.raises(oracle.OraclePanic):
         oracle.rapg_decode(oracle.rapg_encode(x, scale), scale, 5)
+
+
+# ---------------------------------------------------------------- RAPG-major
+
+def outlieru8_case(ratio, n, seed, scale):
+    """outlier_exp's input (outlier/mod.rs:13-60): byte values, MAJOR = 69
+    with probability `ratio`, otherwise uniform in [0, 256), one 0 and one
+    255 at random rows; as f64."""
+    rng = np.random.default_rng(seed)
+    v = np.where(rng.uniform(size=n) < ratio, 69, rng.integers(0, 256, n))
+    i0, i255 = rng.choice(n, 2, replace=False)
+    v[i0], v[i255] = 0, 255
+    return v.astype(np.float64), scale
+
+
+@pytest.mark.parametrize("ratio,scale", [(0.9, 10), (0.99, 100), (0.5, 1000), (0.999, 10000)])
+def test_outlieru8_vs_model(oracle, ratio, scale):
+    """byte_residue_encode_outlieru8 is the buff-major image with MAJOR as
+    the one sparse byte and a roaring bitmap; with one sparse column the
+    byte_residue_*_majority queries are the buff-major ones."""
+    x, scale = outlieru8_case(ratio, 5003, 7, scale)
+    L = M.major_layout(x, scale)
+    L["majors"] = [69]
+    buf = oracle.encode_outlieru8(x, scale)
+    ncols, majors, nouts, _ = oracle.majority_layout(buf, oracle.BM_ROARING)
+    assert ncols == 1 and majors == [69]
+    codes = M.major_decode_codes(L)
+    exp = np.array([float(M.wrap64(L["base"] + c)) / 2.0 ** L["dlen"] for c in codes])
+    assert np.array_equal(oracle.decode_majority(buf, scale, oracle.BM_ROARING), exp)
+    assert nouts[0] == int(np.sum([((c >> (L["fl"] - 8)) & 0xFF) != 69 for c in L["codes"]]))
+    for p in (float(x[3]), 69.0, 68.5, 200.0, -1.0, 255.0, 70.0):
+        w, _, _ = oracle.range_filter_majority(buf, scale, p, oracle.BM_ROARING)
+        assert np.array_equal(w, M.major_filter(L, p, True)), p
+        w, _, _ = oracle.equal_filter_majority(buf, scale, p, oracle.BM_ROARING)
+        assert np.array_equal(w, M.major_filter(L, p, False)), p
+    s, _ = oracle.sum_majority(buf, scale, oracle.BM_ROARING)
+    assert s == M.major_sum(L)
+    _, mc, _, _ = oracle.max_majority(buf, scale, oracle.BM_ROARING)
+    assert mc == M.major_max_code(L)
+
+
+def test_outlieru8_panics(oracle):
+    with pytest.raises(oracle.OraclePanic):  # fewer than 2000 rows
+        oracle.encode_outlieru8(np.full(1999, 69.0), 10)
+    with pytest.raises(oracle.OraclePanic):  # codes narrower than a byte: `remain -= 8` wraps
+        oracle.encode_outlieru8(np.round(np.random.default_rng(1).uniform(0, 3, 3000), 0), 10)
