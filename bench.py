@@ -398,6 +398,58 @@ def run_outlier_form(args, stream, peak):
     return out
 
 
+def run_rapg_major_form(args, stream):
+    """RAPG-major layout (byte_residue_encode_outlieru8) on outlier_exp's
+    input shape: 67,108,864 byte values, 69 with probability 0.9, otherwise
+    uniform (seed 8), scale 10 (outlier_exp itself passes scale 0, on which
+    the reference panics); queries at outlier_exp's predicate 69."""
+    import ctypes as C
+
+    import torch
+
+    from buff_gb300 import capi
+    from buff_gb300.compress import RapgMajorColumn
+    from buff_gb300.workloads import outlier_u8_torch
+
+    L = capi.lib()
+    sh = stream.cuda_stream
+    n = args.outlier_rows
+    x = outlier_u8_torch(n)
+    torch.cuda.synchronize()
+
+    def enc():
+        RapgMajorColumn.encode(x, 10, stream=stream).free()
+
+    t_enc = time_op(enc, 3, stream)
+    col = RapgMajorColumn.encode(x, 10, stream=stream)
+    info = col.info
+    h = col.handle
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    words = torch.empty((n + 31) // 32, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+    ops = {"encode": {"ms": t_enc * 1e3, "gvalues_s": n / t_enc / 1e9}}
+    t = time_op(lambda: L.buff_rapg_decode_majority(h, out.data_ptr(), sh), 5, stream)
+    ops["decode"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9}
+    for name, fn in (("range_69", L.buff_rapg_range_filter_majority),
+                     ("equal_69", L.buff_rapg_equal_filter_majority)):
+        t = time_op(lambda: fn(h, 69.0, words.data_ptr(), cnt.data_ptr(), sh), 10, stream)
+        ops[name] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9}
+    r = capi.SumResult()
+    t = time_op(lambda: L.buff_rapg_sum_majority(h, C.byref(r), sh), 5, stream)
+    ops["sum"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "note": "includes the host combine"}
+    mv, mc = C.c_double(0), C.c_uint64(0)
+    t = time_op(lambda: L.buff_rapg_max_majority(h, C.byref(mv), C.byref(mc), None, None, sh), 5,
+                stream)
+    ops["max"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "note": "per-column host loop"}
+    res = {"workload": f"{n} byte values, 69 w.p. 0.9 else uniform, scale 10 (seed 8)",
+           "rows": n, "fixed_len": info.fixed_len, "outlier_cols": info.outlier_cols,
+           "device_bytes": info.device_bytes, "ops": ops}
+    col.free()
+    del x, out
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_rapg_form(args, stream):
     """RAPG byte_residue layout on 67,108,864 rows with high outliers (99%
     N(100,5), 1% U(1e5,1e6), 6 decimals, scale 1e6): encode, full and
@@ -446,6 +498,7 @@ def run_rapg_form(args, stream):
                        f"6 decimals, scale 1e6 (seed 6)", "rows": n,
            "fixed_len": info.fixed_len, "outlier_cols": info.outlier_cols,
            "device_bytes": code_bytes, "ops": ops}
+    res["rapg_major"] = run_rapg_major_form(args, stream)
     if not args.no_cpu:
         from oracle import oracle as O
 

@@ -454,6 +454,8 @@ struct RapgDecodeArgs {
   const uint8_t *slices, *tail;
   uint32_t n, m, kd, ks, ts, R, skip;
   unsigned long long tbit0;
+  unsigned long long sdef;  // sparse bits of a row that is an outlier in no column
+  uint32_t smaj[8];         // a sparse column's byte on its non-outlier rows
   long long base;
   int dlen;
   double *out;
@@ -578,6 +580,8 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a)
         c0 = (c0 << ts) | (f & tmask);
         c1 = (c1 << ts) | ((f >> ts) & tmask);
       }
+      c0 |= a.sdef;
+      c1 |= a.sdef;
       const double v0 = i64_to_f64_scaled((long long)((unsigned long long)a.base + c0), a.dlen);
       const double v1 = i64_to_f64_scaled((long long)((unsigned long long)a.base + c1), a.dlen);
       if (i0 + 2 <= a.n)
@@ -611,7 +615,7 @@ __global__ void __launch_bounds__(kThreads) k_rapg_fixup(RapgDecodeArgs a) {
 #pragma unroll
       for (uint32_t c = 0; c < 8; ++c) {
         if (c < a.m) {
-          uint32_t b = 0;
+          uint32_t b = a.smaj[c];
           if (Bw[c] >> j & 1u) b = a.obytes[a.oofs[c] + Rk[c] + __popc(Bw[c] & ((1u << j) - 1u))];
           v = (v << 8) | b;
         }
@@ -850,6 +854,30 @@ cudaError_t field_sum(const uint8_t *p, uint64_t bit0, uint32_t width, uint32_t 
   return cudaGetLastError();
 }
 
+// The fast decode of a plan whose slice reads stay in the dense region and
+// whose tail fields start at bit 0, then the outlier rows.
+static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
+  {
+    const int g = grid_of((size_t)(a.n + kRowChunk - 1) / kRowChunk * 32, kThreads);
+    switch (a.ks) {
+      case 0: k_rapg_decode_fast<0><<<g, kThreads, 0, s>>>(a); break;
+      case 1: k_rapg_decode_fast<1><<<g, kThreads, 0, s>>>(a); break;
+      case 2: k_rapg_decode_fast<2><<<g, kThreads, 0, s>>>(a); break;
+      case 3: k_rapg_decode_fast<3><<<g, kThreads, 0, s>>>(a); break;
+      case 4: k_rapg_decode_fast<4><<<g, kThreads, 0, s>>>(a); break;
+      case 5: k_rapg_decode_fast<5><<<g, kThreads, 0, s>>>(a); break;
+      case 6: k_rapg_decode_fast<6><<<g, kThreads, 0, s>>>(a); break;
+      case 7: k_rapg_decode_fast<7><<<g, kThreads, 0, s>>>(a); break;
+      default: k_rapg_decode_fast<8><<<g, kThreads, 0, s>>>(a); break;
+    }
+    count_launch();
+    if (a.m) {
+      k_rapg_fixup<<<grid_of(((size_t)a.n + 31) / 32, kThreads), kThreads, 0, s>>>(a);
+      count_launch();
+    }
+  }
+}
+
 cudaError_t rapg_decode(const buff_col *c, uint32_t R, uint32_t ks, uint32_t ts, uint64_t tbit0,
                         double *out, cudaStream_t s) {
   if (!c->n) return cudaSuccess;
@@ -876,30 +904,45 @@ cudaError_t rapg_decode(const buff_col *c, uint32_t R, uint32_t ks, uint32_t ts,
   a.dlen = (int)c->dlen;
   a.out = out;
   if (ks <= a.kd && ks <= 8 && tbit0 == 0 && ts <= c->r) {
-    const int g = grid_of((size_t)(c->n + kRowChunk - 1) / kRowChunk * 32, kThreads);
-    switch (ks) {
-      case 0: k_rapg_decode_fast<0><<<g, kThreads, 0, s>>>(a); break;
-      case 1: k_rapg_decode_fast<1><<<g, kThreads, 0, s>>>(a); break;
-      case 2: k_rapg_decode_fast<2><<<g, kThreads, 0, s>>>(a); break;
-      case 3: k_rapg_decode_fast<3><<<g, kThreads, 0, s>>>(a); break;
-      case 4: k_rapg_decode_fast<4><<<g, kThreads, 0, s>>>(a); break;
-      case 5: k_rapg_decode_fast<5><<<g, kThreads, 0, s>>>(a); break;
-      case 6: k_rapg_decode_fast<6><<<g, kThreads, 0, s>>>(a); break;
-      case 7: k_rapg_decode_fast<7><<<g, kThreads, 0, s>>>(a); break;
-      default: k_rapg_decode_fast<8><<<g, kThreads, 0, s>>>(a); break;
-    }
-    if (a.m) {
-      count_launch();
-      k_rapg_fixup<<<grid_of(((size_t)c->n + 31) / 32, kThreads), kThreads, 0, s>>>(a);
-    }
+    launch_decode_fast(a, s);
   } else {
     k_rapg_decode<<<grid_of((c->n + 3) / 4, kThreads), kThreads, 0, s>>>(a);
+    count_launch();
   }
-  count_launch();
   return cudaGetLastError();
 }
 
+
 cudaError_t major_decode(const buff_col *c, double *out, cudaStream_t s) {
+  if (c->m == 1 && c->k - c->m <= 8) {
+    // one sparse column: the code is (outlier byte or major) << (fl - 8),
+    // then the dense bytes and the tail -- the RAPG fast decode with the
+    // major byte as the default of non-outlier rows
+    RapgDecodeArgs r;
+    memset(&r, 0, sizeof(r));
+    r.obits = c->obits;
+    r.orank = c->orank;
+    r.obytes = c->obytes;
+    r.oofs[0] = c->oofs[0];
+    r.nwp = c->nwp;
+    r.rs = rank_stride(c);
+    r.stride = c->stride;
+    r.slices = c->slices;
+    r.tail = c->tail;
+    r.n = c->n;
+    r.m = 1;
+    r.kd = c->k - 1;
+    r.ks = c->k - 1;
+    r.ts = c->r;
+    r.R = c->fixed_len;
+    r.sdef = (unsigned long long)c->majors[0] << (c->fixed_len - 8);
+    r.smaj[0] = c->majors[0];
+    r.base = c->base;
+    r.dlen = (int)c->dlen;
+    r.out = out;
+    launch_decode_fast(r, s);
+    return cudaGetLastError();
+  }
   DecodeMajorArgs a;
   memset(&a, 0, sizeof(a));
   a.n = c->n;

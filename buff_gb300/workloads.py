@@ -120,3 +120,18 @@ def fill_walk_torch(out, n: int, dec: int, sigma: float, start: float, seed: int
     s = 10.0 ** dec
     v.mul_(s).round_().div_(s)
     return v
+
+
+def outlier_u8_torch(n: int, ratio: float = 0.9, seed: int = 8, device="cuda"):
+    """outlier_exp's input on the device (float64): byte values, 69 with
+    probability `ratio`, otherwise uniform in [0, 256); one 0 and one 255."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    u = torch.rand(n, generator=g, device=device, dtype=torch.float64)
+    v = torch.randint(0, 256, (n,), generator=g, device=device).to(torch.float64)
+    x = torch.where(u < ratio, torch.full_like(u, 69.0), v)
+    x[n // 3] = 0.0
+    x[2 * n // 3] = 255.0
+    return x

@@ -163,6 +163,10 @@ def test_rapg_major_errors(oracle, gpu):
     with pytest.raises(capi.ReferencePanic):
         RapgMajorColumn.encode(np.round(np.random.default_rng(1).uniform(0, 3, 3000), 0), 10)
     x, scale = outlieru8_case(0.9, 5003, 3, 10)
+    with pytest.raises(capi.ReferencePanic):  # outlier_exp's scale 0: no PRECISION_MAP entry
+        RapgMajorColumn.encode(x, 0)
+    with pytest.raises(oracle.OraclePanic):
+        oracle.encode_outlieru8(x, 0)
     img = oracle.encode_outlieru8(x, scale)
     for bad in (img[:-1], img[:40]):
         with pytest.raises(capi.BuffError):
