@@ -5,16 +5,19 @@ walk reflected into [-500, 500], rounded to 4 decimals (seeded, generated on the
 device), encoded at scale 10^4 -> 25-bit codes = 3 byte slices + 1 tail bit.
 
 One step = the query pair "range filter at 10% selectivity, then sum" over the
-resident column.  `value` = column rows answered per second by that pair (rows
-/ step time), max over ranks, times the number of ranks (replicas: each rank
-owns its own column; weak scaling).  Inputs (slice 0: 268 MB, full column:
-839 MB) are larger than the 129 MB L2, so no flush is needed between steps.
+resident column, answered by buff_range_filter_sum (the bitmap, count and sum
+partials from one pass over the slices; bit-identical to buff_range_filter
+followed by buff_sum_partials_async, which the line also times as
+`two_call`).  `value` = column rows answered per second (rows / step time),
+max over ranks, times the number of ranks (replicas: each rank owns its own
+column; weak scaling).  Inputs (slice 0: 268 MB, full column: 839 MB) are
+larger than the 129 MB L2, so no flush is needed between steps.
 
 `e2e` runs the same pair through the C ABI the way the reference is called
 (compress/buff_simd.rs:3361, split_double.rs:2127 take the encoded Vec<u8> by
 value): per step the host byte image is uploaded from pinned memory
-(buff_deserialize), filtered into a pinned host bitmap, summed into a host
-result.
+(buff_deserialize), filtered and summed in one call into a pinned host
+bitmap and host partials, and the f64 sum finished on the host.
 
 `--impl reference` times the CPU restatement of the reference algorithm (the
 oracle: progressive slice refinement + per-slice byte sums, the reference
@@ -263,7 +266,8 @@ def run_reference(args, rank, world):
 
 
 def run_e2e(L, col, img_len, nw, pred, sh, count, res, args):
-    """The reference-style call: upload the byte image, filter, sum, free."""
+    """The reference-style call pattern: upload the byte image, filter and sum
+    (one pass), results to host buffers, free."""
     import torch
 
     from buff_gb300 import capi
@@ -273,12 +277,15 @@ def run_e2e(L, col, img_len, nw, pred, sh, count, res, args):
     hwords = torch.empty(nw, dtype=torch.int32, pin_memory=True)
     hcount = np.zeros(1, dtype=np.uint64)
 
+    hparts = np.zeros(9, dtype=np.uint64)
+
     def e2e_step():
         hc = C.c_void_p()
         capi.check(L.buff_deserialize(img.data_ptr(), img_len, SCALE, 0, sh, C.byref(hc)))
-        capi.check(L.buff_range_filter(hc, pred, hwords.data_ptr(), hcount.ctypes.data, sh))
+        capi.check(L.buff_range_filter_sum(hc, pred, hwords.data_ptr(), hcount.ctypes.data,
+                                           hparts.ctypes.data, sh))
         sres = capi.SumResult()
-        capi.check(L.buff_sum(hc, C.byref(sres), sh))
+        capi.check(L.buff_sum_finish(hc, hparts.ctypes.data, C.byref(sres)))
         capi.check(L.buff_col_free_async(hc, sh))
         return sres
 
@@ -871,12 +878,14 @@ def main():
     parts = torch.zeros(9, dtype=torch.int64, device="cuda")
     h = col.handle
 
+    # The step: the range filter's bitmap and count and the sum's partials
+    # from one pass over the slices (buff_range_filter_sum); the same results
+    # as the reference's two calls, which are timed after it.
     def step():
-        capi.check(L.buff_range_filter(h, pred, words.data_ptr(), cnt.data_ptr(), sh))
-        capi.check(L.buff_sum_partials_async(h, parts.data_ptr(), sh))
+        capi.check(L.buff_range_filter_sum(h, pred, words.data_ptr(), cnt.data_ptr(),
+                                           parts.data_ptr(), sh))
 
-    # per-kernel events inside the timed region (on the launching stream)
-    ev_f0, ev_f1, ev_s1 = [], [], []
+    ev_a, ev_b = [], []
     clocks = Clocks(local) if rank == 0 else None
     for _ in range(args.warmup):
         step()
@@ -888,6 +897,36 @@ def main():
     torch.cuda.synchronize()
     start.record(stream)
     for _ in range(args.steps):
+        a, b = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+        a.record(stream)
+        step()
+        b.record(stream)
+        ev_a.append(a)
+        ev_b.append(b)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    launches = capi.kernel_launches() - launches0
+    elapsed = start.elapsed_time(stop) / 1e3
+    clk = clocks.stop() if clocks else None
+    barrier(world)
+    elapsed = max_over_ranks(elapsed, world)
+    t_step = elapsed / args.steps
+    fs_s = statistics.median(a.elapsed_time(b) for a, b in zip(ev_a, ev_b)) / 1e3
+    count = int(cnt.item())
+    host_parts = np.ascontiguousarray(parts.cpu().numpy().view(np.uint64))
+    res = capi.SumResult()
+    capi.check(L.buff_sum_finish(h, host_parts.ctypes.data, C.byref(res)))
+
+    # the reference's two calls (buff_range_filter, then the sum), each timed
+    ev_f0, ev_f1, ev_s1 = [], [], []
+    for _ in range(3):
+        capi.check(L.buff_range_filter(h, pred, words.data_ptr(), cnt.data_ptr(), sh))
+        capi.check(L.buff_sum_partials_async(h, parts.data_ptr(), sh))
+    torch.cuda.synchronize()
+    t2a = torch.cuda.Event(enable_timing=True)
+    t2b = torch.cuda.Event(enable_timing=True)
+    t2a.record(stream)
+    for _ in range(args.steps):
         a, b, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         a.record(stream)
         capi.check(L.buff_range_filter(h, pred, words.data_ptr(), cnt.data_ptr(), sh))
@@ -897,20 +936,15 @@ def main():
         ev_f0.append(a)
         ev_f1.append(b)
         ev_s1.append(c2)
-    stop.record(stream)
+    t2b.record(stream)
     torch.cuda.synchronize()
-    launches = capi.kernel_launches() - launches0
-    elapsed = start.elapsed_time(stop) / 1e3
-    clk = clocks.stop() if clocks else None
-    barrier(world)
-    elapsed = max_over_ranks(elapsed, world)
-    t_step = elapsed / args.steps
+    two_call_s = t2a.elapsed_time(t2b) / 1e3 / args.steps
     filt_s = statistics.median(a.elapsed_time(b) for a, b in zip(ev_f0, ev_f1)) / 1e3
     sum_s = statistics.median(b.elapsed_time(c) for b, c in zip(ev_f1, ev_s1)) / 1e3
-    count = int(cnt.item())
-    host_parts = np.ascontiguousarray(parts.cpu().numpy().view(np.uint64))
-    res = capi.SumResult()
-    capi.check(L.buff_sum_finish(h, host_parts.ctypes.data, C.byref(res)))
+    res2 = capi.SumResult()
+    host_parts2 = np.ascontiguousarray(parts.cpu().numpy().view(np.uint64))
+    capi.check(L.buff_sum_finish(h, host_parts2.ctypes.data, C.byref(res2)))
+    assert int(cnt.item()) == count and res2.sum == res.sum  # the two forms agree
 
     peak, peak_kind = measured_peaks()
     k, r = info.k, info.r
@@ -918,6 +952,8 @@ def main():
     filt_bytes = n + 4 * nw  # slice 0 + bitmap (+ candidate sectors, counted by ncu)
     roof_sum = sum_bytes / sum_s / 1e9
     roof_filt = filt_bytes / filt_s / 1e9
+    fs_bytes = sum_bytes + 4 * nw  # every slice + the tail + the bitmap
+    roof_fs = fs_bytes / fs_s / 1e9
 
     # ---- e2e through the C ABI with host buffers --------------------------
     img_len = info.serialized_bytes
@@ -1024,7 +1060,6 @@ def main():
             serving_form = run_serving_form(args, stream, peak)
 
     if rank == 0:
-        tf = ncu_traffic("k_sum")
         line = {
             "metric": "filter+sum throughput (range filter 10% then sum)",
             "value": world * n / t_step / 1e9, "unit": "Gvalues/s", "n_gpus": world,
@@ -1037,9 +1072,17 @@ def main():
                        "selectivity": SELECTIVITY, "count": count,
                        "l2": "inputs larger than L2 (slice 0 268 MB, column 839 MB)",
                        "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": "hbm", "kernel": "k_sum", "achieved": roof_sum, "peak": peak,
-                         "unit": "GB/s", "frac": roof_sum / peak, "peak_kind": peak_kind,
-                         "traffic": tf, "alg_bytes_per_launch": sum_bytes},
+            "step": "buff_range_filter_sum: bitmap, count and sum partials in one pass "
+                    "(bit-identical to buff_range_filter + buff_sum_partials_async)",
+            "two_call": {"ms_per_step": two_call_s * 1e3,
+                         "value": world * n / two_call_s / 1e9, "unit": "Gvalues/s"},
+            "roofline": {"bound": "hbm", "kernel": "k_filter_sum", "achieved": roof_fs,
+                         "peak": peak, "unit": "GB/s", "frac": roof_fs / peak,
+                         "peak_kind": peak_kind, "traffic": ncu_traffic("k_filter_sum"),
+                         "alg_bytes_per_launch": fs_bytes},
+            "roofline_sum": {"kernel": "k_sum", "achieved": roof_sum, "peak": peak,
+                             "unit": "GB/s", "frac": roof_sum / peak,
+                             "traffic": ncu_traffic("k_sum"), "alg_bytes_per_launch": sum_bytes},
             "roofline_filter": {"kernel": "k_filter", "achieved": roof_filt, "peak": peak,
                                 "unit": "GB/s", "frac": roof_filt / peak,
                                 "traffic": ncu_traffic("k_filter"),
