@@ -622,6 +622,98 @@ __global__ void __launch_bounds__(kThreads) k_filter_sum(FilterArgs a, uint32_t 
   if (threadIdx.x == 8 && ts && s_acc[8]) atomicAdd(&partials[ks], s_acc[8]);
 }
 
+// The same one-pass filter + sum with the slices interleaved: a lane takes
+// one 32-row block at a time and loads that block's 32 bytes of every slice
+// and its r tail words together, so the filter's compare work on slice 0 is
+// spread over the whole stream instead of running while only slice 0 is read.
+// KS = k (1..4) slices.  The tail sum is the weighted popcount of the block's
+// r words (bits past n*r masked); candidate blocks are refined as in k_filter.
+template <bool TH, int KS>
+__global__ void __launch_bounds__(kThreads) k_filter_sum_il(FilterArgs a, uint32_t ts,
+                                                            unsigned long long tail_bits,
+                                                            unsigned long long *partials) {
+  __shared__ unsigned long long s_acc[9];
+  if (threadIdx.x < 9) s_acc[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nth = gridDim.x * blockDim.x;
+  const uint32_t nblk = (uint32_t)(a.stride / 32);
+  const uint32_t nwords = (a.n + 31) / 32;
+  unsigned long long tb = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) tb |= (unsigned long long)a.tbyte[j] << (8 * j);
+  const uint32_t t0 = (uint32_t)(tb & 0xFFu);
+  const uint32_t lo0 = (t0 & 0x7Fu) * 0x01010101u, lo1 = ((t0 & 0x7Fu) + 1u) * 0x01010101u;
+  const bool deep = a.k_used > 1 || a.r;
+  uint32_t acc[KS];
+#pragma unroll
+  for (int s = 0; s < KS; ++s) acc[s] = 0;
+  unsigned long long tacc = 0;
+  uint32_t cnt = 0;
+  for (uint32_t blk = tid; blk < nblk; blk += nth) {
+    Bytes32 d[KS];
+#pragma unroll
+    for (int s = 0; s < KS; ++s) d[s] = ld_stream32(a.slices + (size_t)s * a.stride + (size_t)blk * 32);
+    uint32_t tw[7];
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+      tw[q] = (q < (int)ts && blk < nwords)
+                  ? __ldcs(reinterpret_cast<const uint32_t *>(a.tail) + (size_t)ts * blk + q)
+                  : 0u;
+#pragma unroll
+    for (int s = 0; s < KS; ++s)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[s] = __dp4a(d[s].w[q] ^ H, 0x01010101u, acc[s]);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+      if (q < (int)ts) {
+        const unsigned long long b0 = ((unsigned long long)ts * blk + q) * 32;
+        uint32_t word = tw[q];
+        if (b0 >= tail_bits)
+          word = 0;
+        else if (b0 + 32 > tail_bits)
+          word &= (1u << (uint32_t)(tail_bits - b0)) - 1u;
+        tacc += wpopc(word, (uint32_t)((32u * q) % ts), ts);
+      }
+    }
+    if (blk >= nwords) continue;  // padding blocks: summed (zero bytes), never filtered
+    uint32_t me[8], mg[8], eor = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      me[q] = eq4t<TH>(d[0].w[q], lo0, lo1);
+      mg[q] = gt4t<TH>(d[0].w[q], lo1);
+      eor |= me[q];
+    }
+    uint32_t eq = eor ? gather32(me) : 0u;
+    uint32_t gt = gather32(mg);
+    const uint32_t row0 = blk * 32;
+    if (eq && deep) refine32(a.slices, a.stride, a.k_used, tb, a.tail, a.r, a.ttail, row0, gt, eq);
+    if (row0 + 32 > a.full_rows) {
+      const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
+      gt &= lim >= 32 ? 0xFFFFFFFFu : ((1u << lim) - 1u);
+    }
+    __stcs(a.words + blk, gt);
+    cnt += __popc(gt);
+  }
+#pragma unroll
+  for (int s = 0; s < KS; ++s) {
+    const unsigned long long w = warp_sum_ull(acc[s]);
+    if (lane == 0 && w) atomicAdd(&s_acc[s], w);
+  }
+  {
+    const unsigned long long w = warp_sum_ull(tacc);
+    if (lane == 0 && w) atomicAdd(&s_acc[8], w);
+  }
+  if (a.count) {
+    const unsigned long long c = warp_sum_ull(cnt);
+    if (lane == 0 && c) atomicAdd(a.count, c);
+  }
+  __syncthreads();
+  if (threadIdx.x < KS && s_acc[threadIdx.x]) atomicAdd(&partials[threadIdx.x], s_acc[threadIdx.x]);
+  if (threadIdx.x == 8 && ts && s_acc[8]) atomicAdd(&partials[KS], s_acc[8]);
+}
+
 // ---------------------------------------------------------------- max
 
 
@@ -1054,10 +1146,36 @@ cudaError_t launch_sum(const buff_col *c, uint32_t k_used, uint32_t tail_bits,
   return cudaGetLastError();
 }
 
+template <bool TH, int KS>
+cudaError_t launch_filter_sum_il(const FilterArgs &a, const buff_col *c,
+                                 unsigned long long *d_partials, cudaStream_t s) {
+  const void *fn = (const void *)k_filter_sum_il<TH, KS>;
+  int grid = grid_for(fn, kThreads, 0, c->device);
+  const size_t nblk = c->stride / 32;
+  const int need = (int)((nblk + kThreads - 1) / kThreads);
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  k_filter_sum_il<TH, KS><<<grid, kThreads, 0, s>>>(a, c->r, (unsigned long long)c->n * c->r,
+                                                     d_partials);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_filter_sum(const FilterArgs &a, const buff_col *c,
                               unsigned long long *d_partials, cudaStream_t s) {
   if (c->n == 0) return cudaSuccess;
   const bool th = a.tbyte[0] & 0x80u;
+  switch (c->k) {
+    case 1: return th ? launch_filter_sum_il<true, 1>(a, c, d_partials, s)
+                      : launch_filter_sum_il<false, 1>(a, c, d_partials, s);
+    case 2: return th ? launch_filter_sum_il<true, 2>(a, c, d_partials, s)
+                      : launch_filter_sum_il<false, 2>(a, c, d_partials, s);
+    case 3: return th ? launch_filter_sum_il<true, 3>(a, c, d_partials, s)
+                      : launch_filter_sum_il<false, 3>(a, c, d_partials, s);
+    case 4: return th ? launch_filter_sum_il<true, 4>(a, c, d_partials, s)
+                      : launch_filter_sum_il<false, 4>(a, c, d_partials, s);
+    default: break;
+  }
   const void *fn = th ? (const void *)k_filter_sum<true> : (const void *)k_filter_sum<false>;
   int grid = grid_for(fn, kThreads, 0, c->device);
   const size_t nv = c->stride / 16;
