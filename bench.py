@@ -1076,7 +1076,7 @@ def main():
                     "(bit-identical to buff_range_filter + buff_sum_partials_async)",
             "two_call": {"ms_per_step": two_call_s * 1e3,
                          "value": world * n / two_call_s / 1e9, "unit": "Gvalues/s"},
-            "roofline": {"bound": "hbm", "kernel": "k_filter_sum", "achieved": roof_fs,
+            "roofline": {"bound": "hbm", "kernel": "k_filter_sum_il", "achieved": roof_fs,
                          "peak": peak, "unit": "GB/s", "frac": roof_fs / peak,
                          "peak_kind": peak_kind, "traffic": ncu_traffic("k_filter_sum"),
                          "alg_bytes_per_launch": fs_bytes},
