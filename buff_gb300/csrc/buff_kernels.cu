@@ -894,6 +894,12 @@ __global__ void __launch_bounds__(kThreads) k_max(const uint8_t *__restrict__ sl
     m = warp_max_ull(m);
     if (!have || m > best) best = m;
     have = true;
+    // publish the warp's best and take the best any warp has published, so
+    // that every warp's threshold rises with the column's running maximum
+    unsigned long long g = 0;
+    if (lane == 0) g = atomicMax(out, best);
+    g = __shfl_sync(0xFFFFFFFFu, g, 0);
+    if (g > best) best = g;
     top = (uint32_t)(best >> (fl - 8)) & 0xFFu;
   }
   if (lane == 0 && have) atomicMax(out, best);
