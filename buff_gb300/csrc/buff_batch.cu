@@ -527,8 +527,9 @@ __device__ __forceinline__ uint32_t eqb4(uint32_t w, uint32_t bb) {
 template <int STAGE>
 __device__ __forceinline__ void tile_max(const BQ &q, uint32_t r0, uint32_t r1, uint32_t lane) {
   const uint32_t fl = q.k ? 8 * q.k + q.r : q.r;
-  unsigned long long best = 0;
-  bool have = false;
+  // start from the best code other tiles of the query have published
+  unsigned long long best = *reinterpret_cast<volatile unsigned long long *>(q.acc + 10);
+  bool have = best != 0;
   for (uint32_t sb = r0; sb < r1; sb += 512 * STAGE) {
     uint4 v[STAGE];
 #pragma unroll
@@ -593,7 +594,13 @@ __device__ __forceinline__ void tile_max(const BQ &q, uint32_t r0, uint32_t r1, 
         }
         code = (code << q.r) | __reduce_max_sync(0xFFFFFFFFu, mt);
       }
-      if (!have || code > best) best = code;
+      if (!have || code > best) {
+        // publish it, and take a larger one another tile has published
+        unsigned long long g = 0;
+        if (lane == 0) g = atomicMax(q.acc + 10, code);
+        g = __shfl_sync(0xFFFFFFFFu, g, 0);
+        best = g > code ? g : code;
+      }
       have = true;
     }
   }
