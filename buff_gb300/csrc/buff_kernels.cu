@@ -13,8 +13,10 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <type_traits>
 
 #include "buff_device.cuh"
+
 #include "buff_internal.h"
 
 namespace buffk {
@@ -946,13 +948,18 @@ __global__ void __launch_bounds__(kThreads) k_argmax(const uint8_t *__restrict__
 // pair are 2-byte loads (64 contiguous bytes per warp), and the packed bits of
 // a 64-row group (8*ts bytes) are loaded by the first 2*ts lanes and handed out
 // with shuffles.
-template <int KS>
+//
+// N32: every value base + code of the column fits in 32 bits (checked on the
+// host), so the code is built in 32 bits and converted with the exact 32-bit
+// path.
+template <int KS, bool N32 = false>
 __global__ void __launch_bounds__(kThreads) k_decode(const uint8_t *__restrict__ slices,
                                                      size_t stride,
                                                      const uint8_t *__restrict__ tail,
                                                      uint32_t ts, uint32_t n, long long base,
                                                      int dlen, unsigned long long keep,
                                                      uint32_t rshift, double *__restrict__ out) {
+  using CodeT = typename std::conditional<N32, uint32_t, unsigned long long>::type;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nchunks = (n + kRowChunk - 1) / kRowChunk;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -977,7 +984,7 @@ __global__ void __launch_bounds__(kThreads) k_decode(const uint8_t *__restrict__
     }
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
-      unsigned long long c0 = 0, c1 = 0;
+      CodeT c0 = 0, c1 = 0;
 #pragma unroll
       for (int s = 0; s < KS; ++s) {
         c0 = (c0 << 8) | ((sb[m][s] & 0xFFu) ^ 0x80u);
@@ -994,8 +1001,14 @@ __global__ void __launch_bounds__(kThreads) k_decode(const uint8_t *__restrict__
       const uint32_t i0 = r0 + m * 64 + 2 * lane;
       c0 >>= rshift;
       c1 >>= rshift;
-      const double v0 = i64_to_f64_scaled((long long)((unsigned long long)base + (c0 & keep)), dlen);
-      const double v1 = i64_to_f64_scaled((long long)((unsigned long long)base + (c1 & keep)), dlen);
+      double v0, v1;
+      if (N32) {
+        v0 = i32_to_f64_scaled((int)((uint32_t)base + (uint32_t)(c0 & (CodeT)keep)), dlen);
+        v1 = i32_to_f64_scaled((int)((uint32_t)base + (uint32_t)(c1 & (CodeT)keep)), dlen);
+      } else {
+        v0 = i64_to_f64_scaled((long long)((unsigned long long)base + (c0 & keep)), dlen);
+        v1 = i64_to_f64_scaled((long long)((unsigned long long)base + (c1 & keep)), dlen);
+      }
       if (i0 + 2 <= n)
         __stcs(reinterpret_cast<double2 *>(out + i0), make_double2(v0, v1));
       else if (i0 < n)
@@ -1224,13 +1237,23 @@ cudaError_t launch_argmax(const buff_col *c, const unsigned long long *d_max, ui
 template <int KS>
 static cudaError_t decode_ks(const buff_col *c, uint32_t ts, unsigned long long keep, double *out,
                              cudaStream_t s) {
-  const void *fn = (const void *)k_decode<KS>;
+  // the code is built in 32 bits (8 KS + ts <= 32) and every value base +
+  // (code >> pad) fits in 32 bits
+  const uint32_t bits = 8 * KS + ts;
+  const long long maxc = bits >= 63 ? -1 : (long long)(((1ull << bits) - 1ull) >> c->pad);
+  const bool n32 = bits <= 32 && c->base >= INT32_MIN && maxc >= 0 &&
+                   c->base + maxc <= (long long)INT32_MAX;
+  const void *fn = n32 ? (const void *)k_decode<KS, true> : (const void *)k_decode<KS, false>;
   int grid = grid_for(fn, kThreads, 0, c->device);
   const uint32_t nchunks = (c->n + kRowChunk - 1) / kRowChunk;
   const int need = (int)((nchunks + (kThreads / 32) - 1) / (kThreads / 32));
   if (grid > need) grid = need;
-  k_decode<KS><<<grid, kThreads, 0, s>>>(c->slices, c->stride, c->tail, ts, c->n, c->base,
-                                         (int)c->dlen, keep, c->pad, out);
+  if (n32)
+    k_decode<KS, true><<<grid, kThreads, 0, s>>>(c->slices, c->stride, c->tail, ts, c->n, c->base,
+                                                 (int)c->dlen, keep, c->pad, out);
+  else
+    k_decode<KS, false><<<grid, kThreads, 0, s>>>(c->slices, c->stride, c->tail, ts, c->n,
+                                                  c->base, (int)c->dlen, keep, c->pad, out);
   count_launch();
   return cudaGetLastError();
 }
