@@ -18,11 +18,13 @@
 // when every candidate outlier is below it; the decode ORs the major byte
 // shifted twice, and only into rows before the column's last outlier.
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
 
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "buff_device.cuh"
@@ -538,8 +540,9 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode(RapgDecodeArgs a) {
 // 16-byte stores); slice bytes are 2-byte loads; the ts-bit fields of a
 // 64-row group (8*ts bytes) are loaded by the first 2*ts lanes and handed
 // out with shuffles.
-template <int KS>
+template <int KS, bool N32 = false>
 __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a) {
+  using CodeT = typename std::conditional<N32, uint32_t, unsigned long long>::type;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nchunks = (a.n + kRowChunk - 1) / kRowChunk;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -566,7 +569,7 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a)
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
       const uint32_t i0 = r0 + m * 64 + 2 * lane;
-      unsigned long long c0 = 0, c1 = 0;
+      CodeT c0 = 0, c1 = 0;
 #pragma unroll
       for (int s = 0; s < KS; ++s) {
         c0 = (c0 << 8) | ((sb[m][s] & 0xFFu) ^ 0x80u);
@@ -580,10 +583,16 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a)
         c0 = (c0 << ts) | (f & tmask);
         c1 = (c1 << ts) | ((f >> ts) & tmask);
       }
-      c0 |= a.sdef;
-      c1 |= a.sdef;
-      const double v0 = i64_to_f64_scaled((long long)((unsigned long long)a.base + c0), a.dlen);
-      const double v1 = i64_to_f64_scaled((long long)((unsigned long long)a.base + c1), a.dlen);
+      c0 |= (CodeT)a.sdef;
+      c1 |= (CodeT)a.sdef;
+      double v0, v1;
+      if (N32) {
+        v0 = i32_to_f64_scaled((int)((uint32_t)a.base + (uint32_t)c0), a.dlen);
+        v1 = i32_to_f64_scaled((int)((uint32_t)a.base + (uint32_t)c1), a.dlen);
+      } else {
+        v0 = i64_to_f64_scaled((long long)((unsigned long long)a.base + c0), a.dlen);
+        v1 = i64_to_f64_scaled((long long)((unsigned long long)a.base + c1), a.dlen);
+      }
       if (i0 + 2 <= a.n)
         __stcs(reinterpret_cast<double2 *>(a.out + i0), make_double2(v0, v1));
       else if (i0 < a.n)
@@ -856,20 +865,30 @@ cudaError_t field_sum(const uint8_t *p, uint64_t bit0, uint32_t width, uint32_t 
 
 // The fast decode of a plan whose slice reads stay in the dense region and
 // whose tail fields start at bit 0, then the outlier rows.
+template <bool N32>
+static void launch_fast_ks(const RapgDecodeArgs &a, int g, cudaStream_t s) {
+  switch (a.ks) {
+    case 0: k_rapg_decode_fast<0, N32><<<g, kThreads, 0, s>>>(a); break;
+    case 1: k_rapg_decode_fast<1, N32><<<g, kThreads, 0, s>>>(a); break;
+    case 2: k_rapg_decode_fast<2, N32><<<g, kThreads, 0, s>>>(a); break;
+    case 3: k_rapg_decode_fast<3, N32><<<g, kThreads, 0, s>>>(a); break;
+    case 4: k_rapg_decode_fast<4, N32><<<g, kThreads, 0, s>>>(a); break;
+    case 5: k_rapg_decode_fast<5, N32><<<g, kThreads, 0, s>>>(a); break;
+    case 6: k_rapg_decode_fast<6, N32><<<g, kThreads, 0, s>>>(a); break;
+    case 7: k_rapg_decode_fast<7, N32><<<g, kThreads, 0, s>>>(a); break;
+    default: k_rapg_decode_fast<8, N32><<<g, kThreads, 0, s>>>(a); break;
+  }
+}
+
 static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
   {
     const int g = grid_of((size_t)(a.n + kRowChunk - 1) / kRowChunk * 32, kThreads);
-    switch (a.ks) {
-      case 0: k_rapg_decode_fast<0><<<g, kThreads, 0, s>>>(a); break;
-      case 1: k_rapg_decode_fast<1><<<g, kThreads, 0, s>>>(a); break;
-      case 2: k_rapg_decode_fast<2><<<g, kThreads, 0, s>>>(a); break;
-      case 3: k_rapg_decode_fast<3><<<g, kThreads, 0, s>>>(a); break;
-      case 4: k_rapg_decode_fast<4><<<g, kThreads, 0, s>>>(a); break;
-      case 5: k_rapg_decode_fast<5><<<g, kThreads, 0, s>>>(a); break;
-      case 6: k_rapg_decode_fast<6><<<g, kThreads, 0, s>>>(a); break;
-      case 7: k_rapg_decode_fast<7><<<g, kThreads, 0, s>>>(a); break;
-      default: k_rapg_decode_fast<8><<<g, kThreads, 0, s>>>(a); break;
-    }
+    // every value base + code (R bits) in 32 bits: the 32-bit build and conversion
+    const long long maxc = a.R >= 63 ? -1 : (long long)((1ull << a.R) - 1ull);
+    if (a.R <= 32 && a.base >= INT32_MIN && maxc >= 0 && a.base + maxc <= (long long)INT32_MAX)
+      launch_fast_ks<true>(a, g, s);
+    else
+      launch_fast_ks<false>(a, g, s);
     count_launch();
     if (a.m) {
       k_rapg_fixup<<<grid_of(((size_t)a.n + 31) / 32, kThreads), kThreads, 0, s>>>(a);
