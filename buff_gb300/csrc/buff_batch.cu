@@ -335,6 +335,8 @@ struct BQ {
 
 constexpr uint32_t kOpRange = BUFF_Q_RANGE, kOpEqual = BUFF_Q_EQUAL, kOpSum = BUFF_Q_SUM,
                    kOpMax = BUFF_Q_MAX, kOpDecode = BUFF_Q_DECODE;
+// Descriptor-only flag: every decoded value base + code fits in 32 bits.
+constexpr uint32_t kOpN32 = 0x100;
 constexpr int kAcc = kBatchAcc;
 
 // tw[i] for a runtime i without indexing a register array (which would
@@ -647,16 +649,30 @@ __device__ __forceinline__ void tile_decode(const BQ &q, uint32_t r0, uint32_t r
         f = __funnelshift_r(w0, w1, bit & 31);
       }
       double val[4];
+      if (q.ops & kOpN32) {  // 32-bit codes and values (warp-uniform)
 #pragma unroll
-      for (uint32_t i = 0; i < 4; ++i) {
-        unsigned long long d = 0;
+        for (uint32_t i = 0; i < 4; ++i) {
+          uint32_t d = 0;
 #pragma unroll
-        for (uint32_t j = 0; j < 8; ++j) {
-          if (j >= q.dks) break;
-          d = (d << 8) | (((sw[u][j] >> (8 * i)) & 0xFFu) ^ 0x80u);
+          for (uint32_t j = 0; j < 4; ++j) {
+            if (j >= q.dks) break;
+            d = (d << 8) | (((sw[u][j] >> (8 * i)) & 0xFFu) ^ 0x80u);
+          }
+          if (db) d = (d << db) | ((f >> (i * db)) & dmask);
+          val[i] = i32_to_f64_scaled((int)((uint32_t)q.base + (d & (uint32_t)q.keep)), q.dlen);
         }
-        if (db) d = (d << db) | ((f >> (i * db)) & dmask);
-        val[i] = i64_to_f64_scaled((long long)((unsigned long long)q.base + (d & q.keep)), q.dlen);
+      } else {
+#pragma unroll
+        for (uint32_t i = 0; i < 4; ++i) {
+          unsigned long long d = 0;
+#pragma unroll
+          for (uint32_t j = 0; j < 8; ++j) {
+            if (j >= q.dks) break;
+            d = (d << 8) | (((sw[u][j] >> (8 * i)) & 0xFFu) ^ 0x80u);
+          }
+          if (db) d = (d << db) | ((f >> (i * db)) & dmask);
+          val[i] = i64_to_f64_scaled((long long)((unsigned long long)q.base + (d & q.keep)), q.dlen);
+        }
       }
       if (row + 4 <= r1) {
         __stcs(reinterpret_cast<double2 *>(q.values + row), make_double2(val[0], val[1]));
@@ -1201,6 +1217,10 @@ int plan_query(const buff_query &uq, unsigned long long *acc, BQ *q) {
       q->dks = total < 8 ? 0 : total / 8;
       q->dts = total < 8 ? total : total % 8;
     }
+    const uint32_t bits = 8 * q->dks + q->dts;
+    const long long maxc = bits >= 63 ? -1 : (long long)((1ull << bits) - 1ull);
+    if (bits <= 32 && c->base >= INT32_MIN && maxc >= 0 && c->base + maxc <= (long long)INT32_MAX)
+      q->ops |= kOpN32;
   }
   return BUFF_OK;
 }
