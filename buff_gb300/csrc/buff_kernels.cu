@@ -338,7 +338,7 @@ __device__ __noinline__ void refine32(const uint8_t *__restrict__ slices, size_t
 // loop that never reaches the rows after the last full 32-row block.  TH is
 // the top bit of the slice-0 target byte.
 template <bool IS_RANGE, bool TH>
-__global__ void __launch_bounds__(kThreads) k_filter(FilterArgs a) {
+__global__ void __launch_bounds__(kThreads, 5) k_filter(FilterArgs a) {
   constexpr int U = 2;  // 32-byte loads in flight per lane
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwords = (a.n + 31) / 32;
