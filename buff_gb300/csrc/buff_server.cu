@@ -10,7 +10,8 @@
 // Requests that arrive while earlier batches run are admitted into the next
 // free slot at once, so up to `max_inflight` batches overlap on the device.
 // With `batched = 0` the same loop runs one query per launch through the
-// single-column entry points (the baseline the batched form is compared to).
+// single-column entry points (the baseline the batched form is compared to);
+// in batched mode a batch that holds a single request takes that path too.
 //
 // Output memory (bitmaps, decoded values) comes from one device arena of
 // `output_budget_bytes`, handed out in power-of-two size classes; a request
@@ -106,6 +107,7 @@ struct Slot {
   PlainRes *h_plain = nullptr, *d_plain = nullptr;
   std::vector<Req> reqs;
   bool busy = false;
+  bool plain = false;  // this launch went through the single-column calls
   uint64_t seq = 0;
 };
 
@@ -215,7 +217,7 @@ void retire(buff_server *S, Slot &sl) {
       memset(&uq, 0, sizeof(uq));
       uq.col = q.col;
       uq.ops = q.r.ops;
-      if (S->cfg.batched) {
+      if (!sl.plain) {
         buffk::batch_result(uq, sl.h_acc + (size_t)buffk::kBatchAcc * i, &res);
       } else {
         const PlainRes &p = sl.h_plain[i];
@@ -345,10 +347,15 @@ void loop(buff_server *S) {
         worked = true;
       }
     }
-    // admit in arrival order into free slots
+    // admit in arrival order into free slots; while the waiting requests do
+    // not outnumber the free slots each takes a slot of its own (light load:
+    // latency), beyond that slots take batches (throughput)
+    uint32_t free_slots = 0;
+    for (const Slot &sl : S->slots) free_slots += !sl.busy;
+    const uint32_t take = S->waiting.size() > free_slots ? maxb : 1;
     for (Slot &sl : S->slots) {
       if (sl.busy || S->waiting.empty()) continue;
-      while (!S->waiting.empty() && sl.reqs.size() < maxb) {
+      while (!S->waiting.empty() && sl.reqs.size() < take) {
         Req &q = S->waiting.front();
         if (out_need(q) > S->out.cap) {  // larger than the whole budget
           q.status = BUFF_EFULL;
@@ -372,7 +379,11 @@ void loop(buff_server *S) {
         S->waiting.pop_front();
       }
       if (sl.reqs.empty()) break;
-      const int st = S->cfg.batched ? launch_batched(S, sl) : launch_plain(sl);
+      // a batch of one request goes through the single-column calls: fewer
+      // steps (no descriptor upload, class lists or accumulator download)
+      // and the lower latency at light load
+      sl.plain = !S->cfg.batched || sl.reqs.size() == 1;
+      const int st = sl.plain ? launch_plain(sl) : launch_batched(S, sl);
       if (st) {
         S->loop_status.store(st);
         for (Req &r : sl.reqs) r.status = st;
