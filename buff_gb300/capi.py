@@ -40,7 +40,7 @@ EXPORTED = [
     "buff_batch_autotune",
     "buff_server_create", "buff_server_add_column", "buff_server_start", "buff_server_submit",
     "buff_server_poll", "buff_server_release", "buff_server_stop", "buff_server_free",
-    "buff_server_stats", "buff_server_replay", "buff_copy", "buff_max_range", "buff_slice_max_range",
+    "buff_server_stats", "buff_server_replay", "buff_copy", "buff_max_range", "buff_slice_max_range", "buff_max_majority_range",
     "buff_slice_encode_f64", "buff_slice_encode_f32", "buff_slice_deserialize",
     "buff_slice_decode", "buff_slice_range_filter", "buff_slice_equal_filter", "buff_slice_sum",
     "buff_slice_buffsum", "buff_slice_max", "buff_slice_buffmax",
@@ -199,6 +199,7 @@ def lib(build_if_missing: bool = True):
     L.buff_copy.argtypes = [P, P, C.c_uint64, P]
     L.buff_max_range.argtypes = [P, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P]
     L.buff_slice_max_range.argtypes = [P, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P]
+    L.buff_max_majority_range.argtypes = [P, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P]
     L.buff_slice_encode_f64.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
     L.buff_slice_encode_f32.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]
     L.buff_slice_deserialize.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]

@@ -343,6 +343,15 @@ class MajorColumn(Column):
             words = words[: (self.n + 31) // 32]
         return MaxResult(v.value, code.value, words, cnt.value)
 
+    def max_range(self, start: int, end: int, window: int, out=None, stream=None):
+        """buff_max_majority_range: windowed maxima (none with sparse columns)."""
+        nwin = (end - start) // window + 1 if window and end >= start else 1
+        dst = out if out is not None else np.empty(max(nwin, 1), dtype=np.float64)
+        cnt = C.c_uint64(0)
+        check(lib().buff_max_majority_range(self._h, start, end, window, ptr(dst), C.byref(cnt),
+                                            stream_handle(stream)), "max_majority_range")
+        return dst[: cnt.value] if out is None else (dst, cnt.value)
+
     def _unsupported(self, *a, **k):
         raise capi.BuffError(capi.ENOTSUP, "not defined on buff-major columns")
 
@@ -365,7 +374,7 @@ class RapgMajorColumn(MajorColumn):
     def _unsupported(self, *a, **k):
         raise capi.BuffError(capi.ENOTSUP, "not defined on RAPG-major columns")
 
-    decode_condition = range_filter_condition = _unsupported
+    decode_condition = range_filter_condition = max_range = _unsupported
 
 
 class SliceColumn(Column):
@@ -657,6 +666,10 @@ class SplitBDDoubleCompress:
     # compress/buff_simd.rs:2444-2861 (the reference prints the max)
     def buff_max_majority(self, data, stream=None) -> MaxResult:
         return _as_major(self, data).max(argmax=True, stream=stream)
+
+    # compress/buff_simd.rs:2863-3115 (the reference prints the count)
+    def buff_max_majority_range(self, data, s: int, e: int, window: int, stream=None):
+        return _as_major(self, data).max_range(s, e, window, stream=stream)
 
     # compress/buff_simd.rs:1714-1914
     def buff_major_decode_condition(self, data, rows, stream=None):

@@ -1783,6 +1783,20 @@ done:
 
 // ---------------------------------------------------------------- windowed max
 
+int buff_max_majority_range(const buff_col *c, uint32_t start, uint32_t end, uint32_t window,
+                            double *out, uint64_t *nout, void *stream) {
+  if (!c || !nout) return BUFF_EINVAL;
+  if (c->layout != 1) return BUFF_ENOTSUP;
+  *nout = 0;
+  // with sparse columns the reference logs "not implemented" and returns no
+  // windows (buff_simd.rs:2898-2902); without, it is buff_max_range on the
+  // slices and tail that follow the count byte
+  if (c->m) return BUFF_OK;
+  buff_col view = *c;
+  view.layout = 0;
+  return buff_max_range(&view, start, end, window, out, nout, stream);
+}
+
 int buff_max_range(const buff_col *c, uint32_t start, uint32_t end, uint32_t window, double *out,
                    uint64_t *nout, void *stream) {
   if (!c || !nout) return BUFF_EINVAL;

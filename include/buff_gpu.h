@@ -258,6 +258,11 @@ int buff_range_filter_decode(const buff_col *col, double pred, uint32_t *words, 
  * BUFF_EINVAL. */
 int buff_max_range(const buff_col *col, uint32_t start, uint32_t end, uint32_t window,
                    double *out, uint64_t *nout, void *stream);
+/* buff_max_majority_range (compress/buff_simd.rs:2863-3115): buff_max_range
+ * on a buff-major column; with sparse columns the reference returns no
+ * windows (*nout = 0). */
+int buff_max_majority_range(const buff_col *col, uint32_t start, uint32_t end, uint32_t window,
+                            double *out, uint64_t *nout, void *stream);
 
 /* ---- buff-slice layout (compress/buff_slice.rs) ----
  * ceil(fixed_len/8) flipped byte slices, the last one holding the low code

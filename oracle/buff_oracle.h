@@ -177,6 +177,10 @@ int or_range_filter_majority_condition(const uint8_t *bytes, size_t len, uint64_
 /* buff_max_range: the maxima of the full windows of `window` rows in [s, e). */
 int or_max_range(const uint8_t *bytes, size_t len, uint64_t scale, uint32_t s, uint32_t e,
                  uint32_t window, double *out, size_t *nout);
+/* buff_max_majority_range: the same on a buff-major image (no windows when it
+ * has sparse columns). */
+int or_max_majority_range(const uint8_t *bytes, size_t len, uint64_t scale, uint32_t s, uint32_t e,
+                          uint32_t window, double *out, size_t *nout);
 
 /* --- buff-slice layout: oracle/buff_oracle_slice.c --- */
 int or_slice_encode(const double *x, uint32_t n, uint64_t scale, uint8_t **out, size_t *out_len);

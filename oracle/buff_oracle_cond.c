@@ -474,3 +474,26 @@ done:
   free(cur.v);
   return rc;
 }
+
+/* buff_max_majority_range (compress/buff_simd.rs:2863-3115): the windowed
+ * max of buff_max_range on a buff-major image.  It reads the column-count
+ * byte after the header; with sparse columns it logs "not implemented" and
+ * returns no windows; without, the rest of the image is the buff layout and
+ * the steps are buff_max_range's (its BitVec remove_range clears the same
+ * rows as croaring's in every call the loop makes).  Codes narrower than a
+ * byte (packed over the count byte) are not restated: OR_EINVAL. */
+int or_max_majority_range(const uint8_t *bytes, size_t len, uint64_t scale, uint32_t s, uint32_t e,
+                          uint32_t window, double *out, size_t *nout) {
+  *nout = 0;
+  or_header h;
+  if (len < 21 || or_parse_header(bytes, len, &h)) return OR_PANIC;
+  if (h.fixed_len < 8) return OR_EINVAL;
+  if (bytes[20] != 0) return OR_OK; /* error!("handle groupby for outlier is not implemented") */
+  uint8_t *img = (uint8_t *)malloc(len - 1);
+  if (!img) return OR_ENOMEM;
+  memcpy(img, bytes, 20);
+  memcpy(img + 20, bytes + 21, len - 21);
+  const int rc = or_max_range(img, len - 1, scale, s, e, window, out, nout);
+  free(img);
+  return rc;
+}

@@ -118,6 +118,8 @@ def lib():
                                          C.c_uint32, P, C.c_size_t, P]
         L.or_max_range.argtypes = [P, C.c_size_t, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                    P, P]
+        L.or_max_majority_range.argtypes = [P, C.c_size_t, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
+                                   P, P]
         L.or_bench_filter_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, C.c_int,
                                           C.c_int, P, P]
         L.or_bench_filter_sum.restype = C.c_double
@@ -605,3 +607,14 @@ def rapg_layout(buf):
     _check(lib().or_rapg_layout(_ptr(b), b.size, _ptr(nc), _ptr(sizes), _ptr(nouts), _ptr(offs)))
     c = int(nc[0])
     return c, sizes[:c].tolist(), nouts[:c].tolist(), offs[:c].tolist()
+
+
+def max_majority_range(buf, scale, s, e, window):
+    """buff_max_majority_range (buff_simd.rs:2863-3115) on a buff-major image."""
+    b = _buf(buf)
+    nw = (e - s) // window if (window and e >= s) else 0
+    out = np.zeros(max(nw, 1), dtype=np.float64)
+    n = C.c_size_t(0)
+    _check(lib().or_max_majority_range(_ptr(b), b.size, scale, s, e, window, _ptr(out),
+                                       C.byref(n)))
+    return out[: n.value]

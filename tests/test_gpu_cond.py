@@ -172,3 +172,23 @@ def test_max_range(oracle, gpu, case):
     got = ci.max_range(3, e, 100)
     exp = np.array([full[a:min(a + 100, e)].max() for a in range(3, e, 100)])
     assert np.array_equal(got, exp)
+
+
+@pytest.mark.parametrize("kind", ["none", "one"])
+def test_max_majority_range(oracle, gpu, kind):
+    from buff_gb300 import capi
+    from buff_gb300.compress import FLAG_RAW_BITMAPS, MajorColumn
+
+    x, scale = major_case(kind, 70_001, 21)
+    img = oracle.encode_majority(x, scale, 1)
+    col = MajorColumn.deserialize(img, scale, FLAG_RAW_BITMAPS)
+    n = x.size
+    for s, e, w in ((0, 1000, 100), (13, 13 + 128 * 70, 128), (5, 8, 3), (0, n // 1000 * 1000, 1000),
+                    (31, 31 + 40 * 333, 333)):
+        try:
+            exp = oracle.max_majority_range(img, scale, s, e, w)
+        except oracle.OraclePanic:
+            with pytest.raises(capi.ReferencePanic):
+                col.max_range(s, e, w)
+            continue
+        assert np.array_equal(col.max_range(s, e, w), exp), (kind, s, e, w)

@@ -100,3 +100,21 @@ def test_max_range_vs_model(oracle, case):
             oracle.max_range(buf, scale, 0, 105, 10)
     with pytest.raises(oracle.OraclePanic):
         oracle.max_range(buf, scale, 0, n + 1, 10)
+
+
+@pytest.mark.parametrize("kind", ["none", "one"])
+def test_max_majority_range_vs_max_range(oracle, kind):
+    """buff_max_majority_range: buff_max_range on the slices after the count
+    byte, no windows with sparse columns."""
+    from tests.test_oracle_major import major_case
+
+    x, scale = major_case(kind, 5003, 9)
+    img = oracle.encode_majority(x, scale, 1)
+    ncols = oracle.majority_layout(img, 1)[0]
+    plain = oracle.encode(x, scale, flipped=False)
+    for s, e, w in ((0, 1000, 100), (13, 13 + 128 * 7, 128), (7, 7 + 40 * 33, 33), (0, 4096, 4096)):
+        got = oracle.max_majority_range(img, scale, s, e, w)
+        if ncols:
+            assert got.size == 0
+        else:
+            assert np.array_equal(got, oracle.max_range(plain, scale, s, e, w)), (s, e, w)
