@@ -15,9 +15,13 @@ larger than the 129 MB L2, so no flush is needed between steps.
 
 `e2e` runs the same pair through the C ABI the way the reference is called
 (compress/buff_simd.rs:3361, split_double.rs:2127 take the encoded Vec<u8> by
-value): per step the host byte image is uploaded from pinned memory
-(buff_deserialize), filtered and summed in one call into a pinned host
-bitmap and host partials, and the f64 sum finished on the host.
+value): per step buff_range_filter_sum_image answers both queries from the
+host byte image in pinned memory, the kernel reading the image over the host
+link itself (each byte crosses once) and writing the bitmap into a pinned
+host buffer; the count and the finished f64 sum come back to the host.  The
+line also times the two-step form (`via_column`: buff_deserialize uploads the
+image into a resident column, then buff_range_filter_sum and the host
+finish).
 
 `--impl reference` times the CPU restatement of the reference algorithm (the
 oracle: progressive slice refinement + per-slice byte sums, the reference
@@ -266,8 +270,9 @@ def run_reference(args, rank, world):
 
 
 def run_e2e(L, col, img_len, nw, pred, sh, count, res, args):
-    """The reference-style call pattern: upload the byte image, filter and sum
-    (one pass), results to host buffers, free."""
+    """The reference-style call pattern on a host byte image: the one-call
+    image query, and the two-step upload + resident query.  Returns the
+    seconds per step of each."""
     import torch
 
     from buff_gb300 import capi
@@ -276,10 +281,16 @@ def run_e2e(L, col, img_len, nw, pred, sh, count, res, args):
     col.serialize(out=img.numpy())
     hwords = torch.empty(nw, dtype=torch.int32, pin_memory=True)
     hcount = np.zeros(1, dtype=np.uint64)
-
     hparts = np.zeros(9, dtype=np.uint64)
 
-    def e2e_step():
+    def image_step():
+        sres = capi.SumResult()
+        capi.check(L.buff_range_filter_sum_image(img.data_ptr(), img_len, SCALE, 0, pred,
+                                                 hwords.data_ptr(), hcount.ctypes.data,
+                                                 C.byref(sres), sh))
+        return sres
+
+    def column_step():
         hc = C.c_void_p()
         capi.check(L.buff_deserialize(img.data_ptr(), img_len, SCALE, 0, sh, C.byref(hc)))
         capi.check(L.buff_range_filter_sum(hc, pred, hwords.data_ptr(), hcount.ctypes.data,
@@ -289,17 +300,19 @@ def run_e2e(L, col, img_len, nw, pred, sh, count, res, args):
         capi.check(L.buff_col_free_async(hc, sh))
         return sres
 
-    for _ in range(3):
-        e2e_step()
-    torch.cuda.synchronize()
-    reps = max(3, min(args.steps, 20))
-    t1 = time.perf_counter()
-    for _ in range(reps):
-        sres = e2e_step()
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t1) / reps
-    assert int(hcount[0]) == count and sres.sum == res.sum
-    return e2e_s
+    out = []
+    for step in (image_step, column_step):
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        reps = max(3, min(args.steps, 20))
+        t1 = time.perf_counter()
+        for _ in range(reps):
+            sres = step()
+        torch.cuda.synchronize()
+        out.append((time.perf_counter() - t1) / reps)
+        assert int(hcount[0]) == count and sres.sum == res.sum
+    return out[0], out[1]
 
 
 # ---------------------------------------------------------------- outlier column
@@ -961,10 +974,15 @@ def main():
     if args.no_e2e:
         e2e_line = None
     else:
-        e2e_s = run_e2e(L, col, img_len, nw, pred, sh, count, res, args)
+        e2e_s, e2e_col_s = run_e2e(L, col, img_len, nw, pred, sh, count, res, args)
         e2e_line = {"value": world * n / e2e_s / 1e9, "unit": "Gvalues/s",
-                    "h2d_bytes_per_step": img_len, "d2h_bytes_per_step": 4 * nw + 8 + 72,
-                    "ms_per_step": e2e_s * 1e3}
+                    "h2d_bytes_per_step": img_len, "d2h_bytes_per_step": 4 * nw + 80,
+                    "ms_per_step": e2e_s * 1e3,
+                    "call": "buff_range_filter_sum_image (host image read in place)",
+                    "link_gb_s": img_len / e2e_s / 1e9,
+                    "via_column": {"value": world * n / e2e_col_s / 1e9,
+                                   "ms_per_step": e2e_col_s * 1e3,
+                                   "call": "buff_deserialize + buff_range_filter_sum"}}
 
     # ---- per-op table (the measured rows of the single-column config) -------
     ops = {}

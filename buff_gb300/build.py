@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libbuffgpu.so")
-SOURCES = ["buff_kernels.cu", "buff_capi.cu", "buff_noalloc.cu", "buff_major.cu", "buff_cond.cu", "buff_batch.cu", "buff_server.cu", "buff_snappy.cpp", "buff_roaring.cpp"]
+SOURCES = ["buff_kernels.cu", "buff_capi.cu", "buff_noalloc.cu", "buff_image.cu", "buff_major.cu", "buff_cond.cu", "buff_batch.cu", "buff_server.cu", "buff_snappy.cpp", "buff_roaring.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
               "--expt-relaxed-constexpr"]

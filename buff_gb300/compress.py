@@ -516,6 +516,44 @@ class BuffSliceCompress:
         return self._col(data).max_range(s, e, window, stream=stream)
 
 
+def range_filter_sum_image(image, scale: int, pred: float, flags: int = 0, words=None,
+                           stream=None):
+    """Range filter and sum straight from a serialized image (host or device
+    memory) in one pass, without a resident column: (FilterResult, SumResult).
+
+    ``image``: bytes, a uint8 numpy array, or a uint8 torch tensor (pinned host
+    or device).  ``words``: optional output buffer of ceil(n/32) uint32 (numpy
+    or torch); a new host array by default."""
+    if isinstance(image, (bytes, bytearray)):
+        arr = np.frombuffer(bytes(image), dtype=np.uint8)
+        ln = arr.size
+    elif isinstance(image, np.ndarray):
+        arr = np.ascontiguousarray(image, dtype=np.uint8)
+        ln = arr.size
+    else:
+        arr = image
+        ln = image.numel()
+    if ln < 20:
+        raise capi.BuffError(capi.ECORRUPT, "range_filter_sum_image")
+    if isinstance(arr, np.ndarray):
+        hdr = arr[:20].tobytes()
+    elif getattr(arr, "is_cuda", False):
+        hdr = capi.copy_bytes(ptr(arr), 20)
+    else:
+        hdr = arr[:20].numpy().tobytes()
+    n = int.from_bytes(hdr[8:12], "little")
+    nw = (n + 31) // 32
+    out = words if words is not None else np.zeros(max(nw, 1), dtype=np.uint32)
+    cnt = np.zeros(1, dtype=np.uint64)
+    res = capi.SumResult()
+    check(lib().buff_range_filter_sum_image(ptr(arr), ln, scale, flags, float(pred), ptr(out),
+                                            ptr(cnt), C.byref(res), stream_handle(stream)),
+          "range_filter_sum_image")
+    if words is None:
+        out = out[:nw]
+    return FilterResult(out, int(cnt[0]), n), res
+
+
 def _as_major(comp: "SplitBDDoubleCompress", data) -> MajorColumn:
     if isinstance(data, MajorColumn):
         return data
@@ -681,6 +719,7 @@ class SplitBDDoubleCompress:
 
 
 __all__ = ["SplitBDDoubleCompress", "BuffSliceCompress", "Column", "MajorColumn", "SliceColumn",
+           "range_filter_sum_image",
            "RapgColumn", "RapgMajorColumn",
            "FilterResult", "MaxResult",
            "FLAG_INTENDED", "FLAG_RAW_BITMAPS", "FLAG_BUFF_LAYOUT", "rows_to_words"]

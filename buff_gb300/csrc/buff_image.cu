@@ -1,0 +1,355 @@
+// The headline query pair on a serialized image that has not been uploaded:
+// buff_range_filter_sum_image.
+//
+// The reference answers every query from the encoded Vec<u8> it is handed
+// (compress/buff_simd.rs:3361 takes `bytes: Vec<u8>`, split_double.rs:2127
+// likewise).  When that image sits in host memory, uploading it first
+// (buff_deserialize) costs one pass over the host link and a second over
+// HBM; here the kernel itself reads the image where it lies -- pinned host
+// memory through its device mapping, pageable memory directly where the
+// device shares the host's page tables, or device memory -- and answers the
+// range filter and the sum in that single pass.  The link, not HBM, bounds
+// the call, and every byte crosses it once.
+//
+// The image's slices start at byte 20 + j*n, so they are aligned to nothing.
+// Each CTA stages one 4,096-row chunk of every slice (and of the packed tail)
+// into shared memory with aligned 16-byte loads covering the misaligned span,
+// then thread t realigns the 32 bytes of its 32-row block with funnel shifts
+// and runs the same integer steps as the resident kernels: byte sums of every
+// slice (dp4a on the unflipped bytes), the tail field sum, the slice-0
+// compare, refinement of candidate rows through the later slices and the
+// tail, the Q3 row limit.  The partial sums are exactly those of buff_sum.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "buff_device.cuh"
+#include "buff_internal.h"
+
+namespace {
+
+using namespace buffk::dev;
+
+constexpr uint32_t kImgRows = 4096;                // rows per chunk
+constexpr uint32_t kImgThreads = kImgRows / 32;    // one 32-row block per thread
+constexpr uint32_t kRegion = kImgRows + 32;        // staged bytes per slice (16-byte slack)
+
+struct ImgArgs {
+  const uint8_t *slices;  // image + 20: slice j at j * n
+  const uint8_t *tail;    // image + 20 + k * n
+  uint32_t n, k, r;
+  uint32_t flipx;         // XOR that yields flipped bytes: 0 (buff-simd) or 0x80808080 (buff layout)
+  uint32_t full_rows;     // rows that may be set (32 * floor(n / 32))
+  uint32_t ttail;         // target tail bits
+  uint64_t tail_bytes;    // ceil(n * r / 8)
+  unsigned long long tb;  // target byte per slice (unflipped), slice j in bits 8j..8j+7
+  uint32_t *words;        // bitmap (device-accessible)
+  unsigned long long *count;
+  unsigned long long *parts;  // k slice sums, then the tail field sum
+};
+
+// Copies [src, src + len) (len > 0) into dst with aligned 16-byte loads of the
+// smallest aligned span covering it; returns the offset of src within dst.
+// The span never leaves the 16-byte granules holding the first and the last
+// byte, so it stays within the pages of the source.
+__device__ __forceinline__ uint32_t stage(uint8_t *dst, const uint8_t *src, uint64_t len) {
+  const uintptr_t s = reinterpret_cast<uintptr_t>(src);
+  const uintptr_t a0 = s & ~(uintptr_t)15;
+  const uint32_t nvec = (uint32_t)((((s + len + 15) & ~(uintptr_t)15) - a0) / 16);
+  const uint4 *from = reinterpret_cast<const uint4 *>(a0);
+  for (uint32_t i = threadIdx.x; i < nvec; i += kImgThreads)
+    reinterpret_cast<uint4 *>(dst)[i] = from[i];
+  return (uint32_t)(s - a0);
+}
+
+// The 32-byte row block starting at byte `off` of a staged region (any alignment).
+__device__ __forceinline__ void unaligned32(const uint8_t *region, uint32_t off, uint32_t *w) {
+  const uint32_t *x = reinterpret_cast<const uint32_t *>(region) + (off >> 2);
+  const uint32_t sh = (off & 3u) * 8u;
+  uint32_t lo = x[0];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const uint32_t hi = x[i + 1];
+    w[i] = __funnelshift_r(lo, hi, sh);
+    lo = hi;
+  }
+}
+
+// The 32 R-bit tail fields of one block (words tw[0..R)): compares with the
+// target, and sums the fields of the rows in `live` (rows below n).
+template <int R>
+__device__ __forceinline__ void tail_block(const uint32_t *tw, uint32_t ttail, uint32_t live,
+                                           uint32_t &gtt, uint32_t &eqt, uint32_t &fsum) {
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    const int bit = i * R, wi = bit >> 5, sh = bit & 31;
+    const uint32_t hi = (wi + 1 < R) ? tw[wi + 1] : 0u;
+    const uint32_t f = __funnelshift_r(tw[wi], hi, sh) & ((1u << R) - 1u);
+    gtt |= (uint32_t)(f > ttail) << i;
+    eqt |= (uint32_t)(f == ttail) << i;
+    fsum += (live >> i & 1u) ? f : 0u;
+  }
+}
+
+__global__ void __launch_bounds__(kImgThreads) k_filter_sum_image(ImgArgs a) {
+  extern __shared__ __align__(16) uint8_t sm[];
+  uint8_t *tail_sm = sm + (size_t)a.k * kRegion;
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
+  const uint32_t nchunks = (a.n + kImgRows - 1) / kImgRows;
+  const uint32_t t0 = (uint32_t)(a.tb & 0xFFu);
+  const uint32_t lo0 = (t0 & 0x7Fu) * 0x01010101u, lo1 = ((t0 & 0x7Fu) + 1u) * 0x01010101u;
+  const bool th = t0 & 0x80u;
+  unsigned long long ssum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned long long tsum = 0, cnt = 0;
+  for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const uint32_t r0 = c * kImgRows;
+    const uint32_t rows = a.n - r0 < kImgRows ? a.n - r0 : kImgRows;
+    __syncthreads();  // the previous chunk's reads of the staging area are done
+    uint32_t m[8];
+#pragma unroll
+    for (uint32_t j = 0; j < 8; ++j)
+      if (j < a.k) m[j] = stage(sm + j * kRegion, a.slices + (size_t)j * a.n + r0, rows);
+    uint32_t mt = 0;
+    const uint64_t toff = (uint64_t)r0 * a.r / 8;  // r0 is a multiple of 8
+    uint64_t tlen = 0;
+    if (a.r) {
+      const uint64_t tend = ((uint64_t)(r0 + rows) * a.r + 7) / 8;
+      tlen = (tend < a.tail_bytes ? tend : a.tail_bytes) - toff;
+      mt = stage(tail_sm, a.tail + toff, tlen);
+    }
+    __syncthreads();
+    if (rows < kImgRows) {
+      // rows past n: the zero code (flipped 0x80 in the slices, zero tail bits)
+      const uint8_t pad = (uint8_t)(0x80u ^ (a.flipx & 0xFFu));
+      for (uint32_t j = 0; j < a.k; ++j)
+        for (uint32_t i = rows + tid; i < kImgRows + 4; i += kImgThreads)
+          sm[j * kRegion + m[j] + i] = pad;
+      if (a.r)
+        for (uint32_t i = (uint32_t)tlen + tid; i < kImgRows / 8 * a.r + 4; i += kImgThreads)
+          tail_sm[mt + i] = 0;
+      __syncthreads();
+    }
+    if (tid * 32 >= rows) continue;
+    const uint32_t row0 = r0 + tid * 32;
+    uint32_t eq = 0, gt = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < 8; ++j) {
+      if (j >= a.k) break;
+      uint32_t w[8];
+      unaligned32(sm + j * kRegion, m[j] + tid * 32, w);
+      uint32_t bs = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        w[q] ^= a.flipx;
+        bs = __dp4a(w[q] ^ H, 0x01010101u, bs);
+      }
+      ssum[j] += bs;
+      uint32_t g[8], e[8];
+      if (j == 0) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          e[q] = th ? eq4t<true>(w[q], lo0, lo1) : eq4t<false>(w[q], lo0, lo1);
+          g[q] = th ? gt4t<true>(w[q], lo1) : gt4t<false>(w[q], lo1);
+        }
+        gt = gather32(g);
+        eq = gather32(e);
+      } else if (eq) {
+        const ByteTarget t = make_target((uint32_t)(a.tb >> (8 * j)) & 0xFFu);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) cmp4(w[q], t, g[q], e[q]);
+        gt |= eq & gather32(g);
+        eq &= gather32(e);
+      }
+    }
+    if (a.r) {
+      // 32 rows of r bits = 4r bytes at tail offset 4r * tid (4-aligned)
+      const uint32_t off = mt + 4u * a.r * tid;
+      const uint32_t *x = reinterpret_cast<const uint32_t *>(tail_sm) + (off >> 2);
+      const uint32_t sh = (off & 3u) * 8u;
+      uint32_t tw[7];
+#pragma unroll
+      for (uint32_t i = 0; i < 7; ++i) tw[i] = i < a.r ? __funnelshift_r(x[i], x[i + 1], sh) : 0u;
+      const uint32_t nlive = a.n - row0;
+      const uint32_t live = nlive >= 32 ? 0xFFFFFFFFu : ((1u << nlive) - 1u);
+      uint32_t gtt = 0, eqt = 0, fsum = 0;
+      switch (a.r) {
+        case 1: tail_block<1>(tw, a.ttail, live, gtt, eqt, fsum); break;
+        case 2: tail_block<2>(tw, a.ttail, live, gtt, eqt, fsum); break;
+        case 3: tail_block<3>(tw, a.ttail, live, gtt, eqt, fsum); break;
+        case 4: tail_block<4>(tw, a.ttail, live, gtt, eqt, fsum); break;
+        case 5: tail_block<5>(tw, a.ttail, live, gtt, eqt, fsum); break;
+        case 6: tail_block<6>(tw, a.ttail, live, gtt, eqt, fsum); break;
+        default: tail_block<7>(tw, a.ttail, live, gtt, eqt, fsum); break;
+      }
+      tsum += fsum;
+      gt |= eq & gtt;
+    }
+    if (row0 + 32 > a.full_rows) {
+      const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
+      gt &= lim >= 32 ? 0xFFFFFFFFu : ((1u << lim) - 1u);
+    }
+    a.words[row0 / 32] = gt;
+    cnt += __popc(gt);
+  }
+  // partials: one atomic per warp and value
+#pragma unroll
+  for (uint32_t j = 0; j < 8; ++j) {
+    if (j >= a.k) break;
+    const unsigned long long v = warp_sum_ull(ssum[j]);
+    if (lane == 0 && v) atomicAdd(a.parts + j, v);
+  }
+  if (a.r) {
+    const unsigned long long v = warp_sum_ull(tsum);
+    if (lane == 0 && v) atomicAdd(a.parts + a.k, v);
+  }
+  const unsigned long long cv = warp_sum_ull(cnt);
+  if (lane == 0 && cv && a.count) atomicAdd(a.count, cv);
+}
+
+inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// A device-accessible address for `p`: device memory as is, pinned host
+// memory through its mapping, pageable host memory when the device reads the
+// host's page tables; nullptr when the device cannot reach it.
+const void *device_view(const void *p, int device) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return p;
+  if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+  int pageable = 0;
+  cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+  return pageable ? p : nullptr;
+}
+
+int parse_header(const uint8_t *image, uint64_t len, uint64_t scale, uint32_t flags,
+                 cudaStream_t s, buff_col **out) {
+  uint8_t hdr[20];
+  if (buffh::is_device_ptr(image)) {
+    cudaError_t e = cudaMemcpyAsync(hdr, image, 20, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return buffh::cuda_status(e);
+  } else {
+    memcpy(hdr, image, 20);
+  }
+  uint32_t w[5];
+  for (int i = 0; i < 5; ++i)
+    w[i] = (uint32_t)hdr[4 * i] | ((uint32_t)hdr[4 * i + 1] << 8) |
+           ((uint32_t)hdr[4 * i + 2] << 16) | ((uint32_t)hdr[4 * i + 3] << 24);
+  buff_col *c = buffh::new_col(scale, flags);
+  if (!c) return BUFF_ENOMEM;
+  c->base = (int64_t)((uint64_t)w[0] | ((uint64_t)w[1] << 32));
+  c->n = w[2];
+  c->ilen = w[3];
+  c->dlen = w[4];
+  const uint32_t fl = c->ilen + c->dlen;  // the decoders' `dlen + ilen` (u32)
+  if (fl > 64 || c->dlen > 1000) {
+    buffh::free_col(c);
+    return BUFF_ECORRUPT;
+  }
+  buffh::set_layout(c, fl);
+  if (20ull + (uint64_t)c->k * c->n + ((uint64_t)c->n * c->r + 7) / 8 > len) {
+    buffh::free_col(c);
+    return BUFF_ECORRUPT;
+  }
+  c->tail_bytes = ((uint64_t)c->n * c->r + 7) / 8;
+  *out = c;
+  return BUFF_OK;
+}
+
+// The two-step path: upload into a resident column, then the resident call.
+int via_column(const uint8_t *image, uint64_t len, uint64_t scale, uint32_t flags, double pred,
+               uint32_t *words, uint64_t *count, buff_sum_result *sum, void *stream) {
+  buff_col *col = nullptr;
+  int rc = buff_deserialize(image, len, scale, flags, stream, &col);
+  if (rc) return rc;
+  uint64_t parts[9] = {0};
+  rc = buff_range_filter_sum(col, pred, words, count, parts, stream);
+  if (!rc) rc = buff_sum_finish(col, parts, sum);
+  const int rf = buff_col_free_async(col, stream);
+  return rc ? rc : rf;
+}
+
+}  // namespace
+
+extern "C" int buff_range_filter_sum_image(const uint8_t *image, uint64_t len, uint64_t scale,
+                                           uint32_t flags, double pred, uint32_t *words,
+                                           uint64_t *count, buff_sum_result *sum,
+                                           void *stream) {
+  if (!image || !sum) return BUFF_EINVAL;
+  if (len < 20) return BUFF_ECORRUPT;
+  cudaStream_t s = S(stream);
+  buff_col *c = nullptr;
+  int rc = parse_header(image, len, scale, flags, s, &c);
+  if (rc) return rc;
+  if (c->n && !words) {
+    buffh::free_col(c);
+    return BUFF_EINVAL;
+  }
+  const int64_t fp = buffh::fetch_fixed(pred, c->precision_exp, c->dlen);
+  const uint8_t *img = static_cast<const uint8_t *>(device_view(image, c->device));
+  uint32_t *dwords = c->n ? static_cast<uint32_t *>(const_cast<void *>(device_view(words, c->device)))
+                          : nullptr;
+  // Plans that are not one pass over full slices (the intended semantics,
+  // codes narrower than a byte, the early return, no rows), and buffers the
+  // device cannot reach, take the two-step path.
+  if ((flags & BUFF_FLAG_INTENDED) || c->k == 0 || fp < c->base || c->n == 0 || !img ||
+      !dwords) {
+    buffh::free_col(c);
+    return via_column(image, len, scale, flags, pred, words, count, sum, stream);
+  }
+  ImgArgs a;
+  memset(&a, 0, sizeof(a));
+  const uint64_t t = (uint64_t)(fp - c->base);
+  const uint32_t fl = c->fixed_len;
+  a.slices = img + 20;
+  a.tail = img + 20 + (uint64_t)c->k * c->n;
+  a.n = c->n;
+  a.k = c->k;
+  a.r = c->r;
+  a.flipx = (flags & BUFF_FLAG_BUFF_LAYOUT) ? 0x80808080u : 0u;
+  a.full_rows = c->n / 32 * 32;
+  for (uint32_t j = 0; j < c->k; ++j)
+    a.tb |= (unsigned long long)(uint8_t)(t >> (fl - 8 * (j + 1))) << (8 * j);
+  a.ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
+  a.tail_bytes = c->tail_bytes;
+  a.words = dwords;
+  unsigned long long *d = nullptr;  // 9 partials, then the count
+  uint64_t host[10] = {0};
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&d), 10 * sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, 10 * sizeof(unsigned long long), s);
+  if (e == cudaSuccess) {
+    a.parts = d;
+    a.count = d + 9;
+    // k slice regions, then the tail: 512r bytes of a chunk plus 64 of slack
+    // (16 of misalignment, the word past a block's last tail word, the pad)
+    const size_t smem = (size_t)c->k * kRegion + kImgRows / 8 * c->r + 64;
+    int per_sm = 0, sms = buffk::num_sms(c->device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_filter_sum_image, kImgThreads, smem);
+    if (per_sm < 1) per_sm = 1;
+    const uint32_t nchunks = (c->n + kImgRows - 1) / kImgRows;
+    uint32_t grid = (uint32_t)(per_sm * sms);
+    if (grid > nchunks) grid = nchunks;
+    k_filter_sum_image<<<grid, kImgThreads, smem, s>>>(a);
+    buffk::count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(host, d, 10 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (d) cudaFreeAsync(d, s);
+  rc = buffh::cuda_status(e);
+  if (!rc) {
+    if (count) {
+      if (buffh::is_device_ptr(count))
+        rc = buffh::cuda_status(cudaMemcpyAsync(count, host + 9, 8, cudaMemcpyHostToDevice, s));
+      else
+        *count = host[9];
+    }
+    if (!rc) rc = buff_sum_finish(c, host, sum);
+  }
+  buffh::free_col(c);
+  return rc;
+}

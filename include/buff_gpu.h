@@ -171,6 +171,22 @@ int buff_sum_finish(const buff_col *col, const uint64_t *host_partials, buff_sum
  * u64 (device or host); buff_sum_finish turns them into the sum. */
 int buff_range_filter_sum(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
                           uint64_t *partials, void *stream);
+/* buff_simd_range_filter (compress/buff_simd.rs:3361-3547) then byte_fixed_sum
+ * (compress/split_double.rs:2127-2208) on the serialized image itself -- the
+ * reference's calling pattern, where each query takes the encoded Vec<u8>.
+ * No resident column is made: the kernel reads the image where it lies
+ * (device memory, pinned host memory through its mapping, or pageable host
+ * memory when the device shares the host's page tables) and answers both
+ * queries in one pass, so each byte crosses the host link once.  scale and
+ * flags as buff_deserialize.  words: ceil(n/32) u32 (host or device; written
+ * in place when the device can reach them); count may be NULL; *sum (host)
+ * receives what buff_sum returns.  Plans that are not a single pass (the
+ * early return, fixed_len < 8, BUFF_FLAG_INTENDED) and buffers the device
+ * cannot reach run as buff_deserialize + buff_range_filter_sum; the results
+ * are the same either way.  Synchronizes the stream. */
+int buff_range_filter_sum_image(const uint8_t *image, uint64_t len, uint64_t scale,
+                                uint32_t flags, double pred, uint32_t *words, uint64_t *count,
+                                buff_sum_result *sum, void *stream);
 
 /* SplitBDDoubleCompress::byte_fixed_max (compress/split_double.rs:3919-4105):
  * the column maximum, its code, and optionally the arg-max bitmap and its
