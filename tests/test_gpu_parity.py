@@ -342,3 +342,37 @@ def test_full_size_properties(gpu):
     assert fr.count == g.count and np.array_equal(fr.words, g.words)
     assert fs.exact_num == s.exact_num and fs.sum == s.sum
     assert col.max().code == int(q.max().item()) - base
+
+
+@pytest.mark.parametrize("offset,scale,n", [(0.0, 10000, 300_017), (1e6, 10000, 300_017),
+                                            (-3e5, 1000, 65_539), (0.0, 100, 100_000),
+                                            (50.0, 10, 4_099)])
+def test_decode_paths_and_output_alignment(oracle, gpu, offset, scale, n):
+    """Full and precision decodes through every output placement (host,
+    32-byte and 16-byte aligned device buffers), with codes that carry tail
+    bits and bases inside and outside the 32-bit range."""
+    import torch
+
+    from buff_gb300.compress import Column
+
+    rng = np.random.default_rng(n)
+    x = np.round(offset + np.cumsum(rng.uniform(-0.5, 0.5, n)), 4)
+    img = oracle.encode(x, scale)
+    col = Column.encode(x, scale)
+    assert col.serialize() == img
+    want = oracle.decode(img, scale)
+    assert np.array_equal(col.decode(), want)
+    buf = torch.empty(n + 4, dtype=torch.float64, device="cuda")
+    for shift in (0, 2):  # 32-byte aligned, then 16-byte aligned
+        o = buf[shift: shift + n]
+        col.decode(out=o)
+        assert np.array_equal(o.cpu().numpy(), want), shift
+    for p in range(0, 5):
+        try:
+            want_p = oracle.decode_at_precision(img, scale, p)
+        except oracle.OraclePanic:
+            continue
+        assert np.array_equal(col.decode_at_precision(p), want_p), p
+        o = buf[2: 2 + n]
+        col.decode_at_precision(p, out=o)
+        assert np.array_equal(o.cpu().numpy(), want_p), p
