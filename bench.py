@@ -300,8 +300,20 @@ def run_e2e(L, col, img_len, nw, pred, sh, count, res, args):
         capi.check(L.buff_col_free_async(hc, sh))
         return sres
 
+    def filter_image_step():
+        capi.check(L.buff_filter_image(img.data_ptr(), img_len, SCALE, 0, 0, pred,
+                                       hwords.data_ptr(), hcount.ctypes.data, sh))
+        return res
+
+    def filter_column_step():
+        hc = C.c_void_p()
+        capi.check(L.buff_deserialize(img.data_ptr(), img_len, SCALE, 0, sh, C.byref(hc)))
+        capi.check(L.buff_range_filter(hc, pred, hwords.data_ptr(), hcount.ctypes.data, sh))
+        capi.check(L.buff_col_free_async(hc, sh))
+        return res
+
     out = []
-    for step in (image_step, column_step):
+    for step in (image_step, column_step, filter_image_step, filter_column_step):
         for _ in range(3):
             step()
         torch.cuda.synchronize()
@@ -312,7 +324,7 @@ def run_e2e(L, col, img_len, nw, pred, sh, count, res, args):
         torch.cuda.synchronize()
         out.append((time.perf_counter() - t1) / reps)
         assert int(hcount[0]) == count and sres.sum == res.sum
-    return out[0], out[1]
+    return out
 
 
 # ---------------------------------------------------------------- outlier column
@@ -974,7 +986,8 @@ def main():
     if args.no_e2e:
         e2e_line = None
     else:
-        e2e_s, e2e_col_s = run_e2e(L, col, img_len, nw, pred, sh, count, res, args)
+        e2e_s, e2e_col_s, filt_img_s, filt_col_s = run_e2e(L, col, img_len, nw, pred, sh, count,
+                                                            res, args)
         e2e_line = {"value": world * n / e2e_s / 1e9, "unit": "Gvalues/s",
                     "h2d_bytes_per_step": img_len, "d2h_bytes_per_step": 4 * nw + 80,
                     "ms_per_step": e2e_s * 1e3,
@@ -982,7 +995,11 @@ def main():
                     "link_gb_s": img_len / e2e_s / 1e9,
                     "via_column": {"value": world * n / e2e_col_s / 1e9,
                                    "ms_per_step": e2e_col_s * 1e3,
-                                   "call": "buff_deserialize + buff_range_filter_sum"}}
+                                   "call": "buff_deserialize + buff_range_filter_sum"},
+                    "range_filter_alone": {"image_ms": filt_img_s * 1e3,
+                                           "via_column_ms": filt_col_s * 1e3,
+                                           "call": "buff_filter_image vs buff_deserialize + "
+                                                   "buff_range_filter"}}
 
     # ---- per-op table (the measured rows of the single-column config) -------
     ops = {}

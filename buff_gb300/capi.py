@@ -26,7 +26,7 @@ EXPORTED = [
     "buff_range_filter", "buff_equal_filter", "buff_range_filter_with_slice",
     "buff_equal_filter_with_slice", "buff_sum", "buff_sum_at_precision",
     "buff_sum_partials_async", "buff_sum_finish", "buff_max", "buff_max_async",
-    "buff_range_filter_sum", "buff_range_filter_sum_image",
+    "buff_range_filter_sum", "buff_range_filter_sum_image", "buff_filter_image",
     "buff_status_string", "buff_last_cuda_error", "buff_kernel_launches",
     "buff_range_filter_noalloc",
     "buff_encode_majority_f64", "buff_encode_majority_f32", "buff_deserialize_majority",
@@ -163,6 +163,8 @@ def lib(build_if_missing: bool = True):
     L.buff_range_filter_sum.argtypes = [P, C.c_double, P, P, P, P]
     L.buff_range_filter_sum_image.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, C.c_double,
                                               P, P, C.POINTER(SumResult), P]
+    L.buff_filter_image.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, C.c_int, C.c_double,
+                                    P, P, P]
     L.buff_max.argtypes = [P, P, P, P, P, P]
     L.buff_max_async.argtypes = [P, P, P]
     L.buff_encode_majority_f64.argtypes = [P, C.c_uint64, C.c_uint64, C.c_uint32, P, pp]

@@ -516,6 +516,46 @@ class BuffSliceCompress:
         return self._col(data).max_range(s, e, window, stream=stream)
 
 
+def _image_arg(image):
+    """(address-bearing array, length, header bytes) of a serialized image."""
+    if isinstance(image, (bytes, bytearray)):
+        arr = np.frombuffer(bytes(image), dtype=np.uint8)
+    elif isinstance(image, np.ndarray):
+        arr = np.ascontiguousarray(image, dtype=np.uint8)
+    else:
+        arr = image
+    ln = arr.size if isinstance(arr, np.ndarray) else arr.numel()
+    if ln < 20:
+        raise capi.BuffError(capi.ECORRUPT, "image")
+    if isinstance(arr, np.ndarray):
+        hdr = arr[:20].tobytes()
+    elif getattr(arr, "is_cuda", False):
+        hdr = capi.copy_bytes(ptr(arr), 20)
+    else:
+        hdr = arr[:20].numpy().tobytes()
+    return arr, ln, hdr
+
+
+FILTER_KINDS = {"range": 0, "equal": 1, "range_with_slice": 2, "equal_with_slice": 3}
+
+
+def filter_image(image, scale: int, pred: float, kind: str = "range", flags: int = 0,
+                 words=None, stream=None) -> FilterResult:
+    """A buff-simd filter straight from a serialized image (host or device
+    memory), without a resident column.  kind: range, equal,
+    range_with_slice or equal_with_slice."""
+    arr, ln, hdr = _image_arg(image)
+    n = int.from_bytes(hdr[8:12], "little")
+    nw = (n + 31) // 32
+    out = words if words is not None else np.zeros(max(nw, 1), dtype=np.uint32)
+    cnt = np.zeros(1, dtype=np.uint64)
+    check(lib().buff_filter_image(ptr(arr), ln, scale, flags, FILTER_KINDS[kind], float(pred),
+                                  ptr(out), ptr(cnt), stream_handle(stream)), "filter_image")
+    if words is None:
+        out = out[:nw]
+    return FilterResult(out, int(cnt[0]), n)
+
+
 def range_filter_sum_image(image, scale: int, pred: float, flags: int = 0, words=None,
                            stream=None):
     """Range filter and sum straight from a serialized image (host or device
@@ -524,23 +564,7 @@ def range_filter_sum_image(image, scale: int, pred: float, flags: int = 0, words
     ``image``: bytes, a uint8 numpy array, or a uint8 torch tensor (pinned host
     or device).  ``words``: optional output buffer of ceil(n/32) uint32 (numpy
     or torch); a new host array by default."""
-    if isinstance(image, (bytes, bytearray)):
-        arr = np.frombuffer(bytes(image), dtype=np.uint8)
-        ln = arr.size
-    elif isinstance(image, np.ndarray):
-        arr = np.ascontiguousarray(image, dtype=np.uint8)
-        ln = arr.size
-    else:
-        arr = image
-        ln = image.numel()
-    if ln < 20:
-        raise capi.BuffError(capi.ECORRUPT, "range_filter_sum_image")
-    if isinstance(arr, np.ndarray):
-        hdr = arr[:20].tobytes()
-    elif getattr(arr, "is_cuda", False):
-        hdr = capi.copy_bytes(ptr(arr), 20)
-    else:
-        hdr = arr[:20].numpy().tobytes()
+    arr, ln, hdr = _image_arg(image)
     n = int.from_bytes(hdr[8:12], "little")
     nw = (n + 31) // 32
     out = words if words is not None else np.zeros(max(nw, 1), dtype=np.uint32)
@@ -719,7 +743,7 @@ class SplitBDDoubleCompress:
 
 
 __all__ = ["SplitBDDoubleCompress", "BuffSliceCompress", "Column", "MajorColumn", "SliceColumn",
-           "range_filter_sum_image",
+           "range_filter_sum_image", "filter_image",
            "RapgColumn", "RapgMajorColumn",
            "FilterResult", "MaxResult",
            "FLAG_INTENDED", "FLAG_RAW_BITMAPS", "FLAG_BUFF_LAYOUT", "rows_to_words"]

@@ -373,13 +373,61 @@ done:
 
 enum FilterKind { kRange = 0, kEqual = 1, kRangeSlice = 2, kEqualSlice = 3 };
 
+// The filter plan of buff_simd_range_filter / _equal_filter and their
+// `_with_slice` forms for a buff-simd column: *action = 0 (no row set),
+// 1 (every row set) or 2 (the filter kernel with *a, whose device pointers
+// the caller fills in).  Returns BUFF_EREFPANIC where the reference panics.
+int plan_filter(const buff_col *c, double pred, int kind, FilterArgs *a, int *action) {
+  const bool intended = c->flags & BUFF_FLAG_INTENDED;
+  const bool is_range = (kind == kRange || kind == kRangeSlice);
+  const bool with_slice = (kind == kRangeSlice || kind == kEqualSlice);
+  const uint32_t n = c->n;
+  *action = 2;
+  memset(a, 0, sizeof(*a));
+  const int64_t fixed_part = fetch_fixed_host(pred, c->precision_exp, c->dlen);
+  if (fixed_part < c->base) {
+    // early return (buff_simd.rs:3385-3388, 3573-3576, 3769-3772, 3919-3922):
+    // the printed count is n for range and both fused forms, 0 for equality.
+    *action = (kind == kEqual) ? 0 : 1;
+    return BUFF_OK;
+  }
+  const uint64_t t = (uint64_t)(fixed_part - c->base);
+  const uint32_t fl = c->fixed_len;
+  if (with_slice && !intended && (c->k == 0 || n < 32)) return BUFF_EREFPANIC;
+  a->n = n;
+  a->is_range = is_range ? 1u : 0u;
+  if (intended || c->k == 0) {
+    // full compare of every row against the untruncated target
+    // (fixed_len < 8: buff_simd.rs:3395-3402, 3583-3590)
+    const bool above = fl < 64 && (t >> fl) != 0;
+    if (above) {
+      *action = 0;
+    } else {
+      a->full_rows = n;
+      a->k_used = c->k;
+      a->r = c->r;
+      for (uint32_t j = 0; j < c->k; ++j) a->tbyte[j] = (uint8_t)(t >> (fl - 8 * (j + 1)));
+      a->ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
+    }
+  } else {
+    // byte slices with truncated per-slice targets (buff_simd.rs:3407, 3425, 3448)
+    a->full_rows = n / 32 * 32;
+    a->k_used = with_slice ? (c->k < 4 ? c->k : 4u) : c->k;
+    a->r = c->r;
+    for (uint32_t j = 0; j < a->k_used; ++j) a->tbyte[j] = (uint8_t)(t >> (fl - 8 * (j + 1)));
+    a->ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
+    if (!is_range) {
+      a->tail_only_eq = 1;  // only the tail step writes `res` (buff_simd.rs:3684-3729)
+      if (c->r == 0) *action = 0;
+    }
+  }
+  return BUFF_OK;
+}
+
 int filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t *count, cudaStream_t s,
                 FilterKind kind) {
   if (!c || (!words && c->n > 0)) return BUFF_EINVAL;
   if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns: the *_majority calls
-  const bool intended = c->flags & BUFF_FLAG_INTENDED;
-  const bool is_range = (kind == kRange || kind == kRangeSlice);
-  const bool with_slice = (kind == kRangeSlice || kind == kEqualSlice);
   const uint32_t n = c->n, nw = (n + 31) / 32;
   int rc = BUFF_OK;
   uint32_t *dwords = words;
@@ -390,47 +438,10 @@ int filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t *count
   // 0: fill zeros, 1: fill ones, 2: kernel
   int action = 2;
   FilterArgs a;
-  memset(&a, 0, sizeof(a));
-  const int64_t fixed_part = fetch_fixed_host(pred, c->precision_exp, c->dlen);
-  if (fixed_part < c->base) {
-    // early return (buff_simd.rs:3385-3388, 3573-3576, 3769-3772, 3919-3922):
-    // the printed count is n for range and both fused forms, 0 for equality.
-    action = (kind == kEqual) ? 0 : 1;
-  } else {
-    const uint64_t t = (uint64_t)(fixed_part - c->base);
-    const uint32_t fl = c->fixed_len;
-    if (with_slice && !intended && (c->k == 0 || n < 32)) return BUFF_EREFPANIC;
-    a.slices = c->slices;
-    a.stride = c->stride;
-    a.tail = c->tail;
-    a.n = n;
-    a.is_range = is_range ? 1u : 0u;
-    if (intended || c->k == 0) {
-      // full compare of every row against the untruncated target
-      // (fixed_len < 8: buff_simd.rs:3395-3402, 3583-3590)
-      const bool above = fl < 64 && (t >> fl) != 0;
-      if (above) {
-        action = 0;
-      } else {
-        a.full_rows = n;
-        a.k_used = c->k;
-        a.r = c->r;
-        for (uint32_t j = 0; j < c->k; ++j) a.tbyte[j] = (uint8_t)(t >> (fl - 8 * (j + 1)));
-        a.ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
-      }
-    } else {
-      // byte slices with truncated per-slice targets (buff_simd.rs:3407, 3425, 3448)
-      a.full_rows = n / 32 * 32;
-      a.k_used = with_slice ? (c->k < 4 ? c->k : 4u) : c->k;
-      a.r = c->r;
-      for (uint32_t j = 0; j < a.k_used; ++j) a.tbyte[j] = (uint8_t)(t >> (fl - 8 * (j + 1)));
-      a.ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
-      if (!is_range) {
-        a.tail_only_eq = 1;  // only the tail step writes `res` (buff_simd.rs:3684-3729)
-        if (c->r == 0) action = 0;
-      }
-    }
-  }
+  if ((rc = plan_filter(c, pred, kind, &a, &action))) return rc;
+  a.slices = c->slices;
+  a.stride = c->stride;
+  a.tail = c->tail;
   if (n == 0) {
     if (count) {
       if (count_host)
@@ -2686,6 +2697,9 @@ int precision_bits(const buff_col *c, uint32_t precision, uint32_t *total) {
 }
 double combine_sum(const buff_col *c, uint32_t total, const uint64_t *parts, bool intended) {
   return ::combine_sum(c, total, parts, intended);
+}
+int plan_filter(const buff_col *c, double pred, int kind, buffk::FilterArgs *a, int *action) {
+  return ::plan_filter(c, pred, kind, a, action);
 }
 int dlen_of_scale(uint64_t scale) { return dlen_of_prec(prec_of_scale(scale)); }
 }  // namespace buffh

@@ -19,6 +19,12 @@
 // slice (dp4a on the unflipped bytes), the tail field sum, the slice-0
 // compare, refinement of candidate rows through the later slices and the
 // tail, the Q3 row limit.  The partial sums are exactly those of buff_sum.
+//
+// buff_filter_image does the same for the four filters alone.  They need only
+// slice 0 in full: it is staged as above, and the few candidate blocks (rows
+// still equal to the target prefix) read their later slices and tail bytes
+// straight from the image, so a filter moves about a third of the image
+// across the link.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -206,6 +212,129 @@ __global__ void __launch_bounds__(kImgThreads) k_filter_sum_image(ImgArgs a) {
   if (lane == 0 && cv && a.count) atomicAdd(a.count, cv);
 }
 
+struct ImgFilterArgs {
+  const uint8_t *slices;  // image + 20: slice j at j * n
+  const uint8_t *tail;    // image + 20 + k * n
+  uint32_t n, k_used, r;
+  uint32_t flipx;         // as ImgArgs
+  uint32_t full_rows;
+  uint32_t ttail;
+  uint32_t tail_only_eq;  // equality rows are set only by the tail step
+  uint64_t tail_bytes;
+  unsigned long long tb;
+  uint32_t *words;
+  unsigned long long *count;
+};
+
+// The `vb` valid bytes (1..32) at p, read from the image through 16-byte
+// granules that hold valid bytes (so never past the pages of the image), as
+// 8 words; bytes past vb read as `pad`.  scr: 16 words of this thread's
+// shared scratch.
+__device__ __forceinline__ void block_from_image(const uint8_t *p, uint32_t vb, uint32_t pad,
+                                                 uint32_t *scr, uint32_t *w) {
+  const uintptr_t s = reinterpret_cast<uintptr_t>(p);
+  const uintptr_t a0 = s & ~(uintptr_t)15;
+  const uint32_t m = (uint32_t)(s - a0);
+  const uint32_t nv = (uint32_t)((((s + vb + 15) & ~(uintptr_t)15) - a0) / 16);
+  const uint4 *from = reinterpret_cast<const uint4 *>(a0);
+  uint4 *sc = reinterpret_cast<uint4 *>(scr);
+#pragma unroll
+  for (uint32_t v = 0; v < 3; ++v) sc[v] = v < nv ? from[v] : make_uint4(0u, 0u, 0u, 0u);
+  if (vb < 32) {
+    uint8_t *b = reinterpret_cast<uint8_t *>(scr);
+    for (uint32_t i = m + vb; i < m + 32; ++i) b[i] = (uint8_t)pad;
+  }
+  unaligned32(reinterpret_cast<const uint8_t *>(scr), m, w);
+}
+
+template <bool IS_RANGE>
+__global__ void __launch_bounds__(kImgThreads) k_filter_image(ImgFilterArgs a) {
+  extern __shared__ __align__(16) uint8_t sm[];
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
+  uint32_t *scr = reinterpret_cast<uint32_t *>(sm + kRegion) + tid * 16;
+  const uint32_t nchunks = (a.n + kImgRows - 1) / kImgRows;
+  const uint32_t t0 = (uint32_t)(a.tb & 0xFFu);
+  const uint32_t lo0 = (t0 & 0x7Fu) * 0x01010101u, lo1 = ((t0 & 0x7Fu) + 1u) * 0x01010101u;
+  const bool th = t0 & 0x80u;
+  const bool deep = a.k_used > 1 || a.r;
+  const uint32_t pad = 0x80u ^ (a.flipx & 0xFFu);
+  unsigned long long cnt = 0;
+  for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const uint32_t r0 = c * kImgRows;
+    const uint32_t rows = a.n - r0 < kImgRows ? a.n - r0 : kImgRows;
+    __syncthreads();
+    const uint32_t m0 = stage(sm, a.slices + r0, rows);
+    __syncthreads();
+    if (rows < kImgRows) {
+      for (uint32_t i = rows + tid; i < kImgRows + 4; i += kImgThreads) sm[m0 + i] = (uint8_t)pad;
+      __syncthreads();
+    }
+    if (tid * 32 >= rows) continue;
+    const uint32_t row0 = r0 + tid * 32;
+    const uint32_t vb = a.n - row0 < 32 ? a.n - row0 : 32u;
+    uint32_t w[8], g[8], e[8];
+    unaligned32(sm, m0 + tid * 32, w);
+    uint32_t eor = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      w[q] ^= a.flipx;
+      e[q] = th ? eq4t<true>(w[q], lo0, lo1) : eq4t<false>(w[q], lo0, lo1);
+      eor |= e[q];
+    }
+    uint32_t eq = eor ? gather32(e) : 0u;
+    uint32_t gt = 0;
+    if (IS_RANGE) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) g[q] = th ? gt4t<true>(w[q], lo1) : gt4t<false>(w[q], lo1);
+      gt = gather32(g);
+    }
+    if (eq) {
+      if (deep) {
+        for (uint32_t j = 1; j < a.k_used && eq; ++j) {
+          block_from_image(a.slices + (size_t)j * a.n + row0, vb, pad, scr, w);
+          const ByteTarget t = make_target((uint32_t)(a.tb >> (8 * j)) & 0xFFu);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) cmp4(w[q] ^ a.flipx, t, g[q], e[q]);
+          gt |= eq & gather32(g);
+          eq &= gather32(e);
+        }
+        if (a.r && eq) {
+          // 32 rows of r bits = 4r bytes at tail byte 4r * (row0 / 32)
+          const uint64_t off = (uint64_t)4 * a.r * (row0 / 32);
+          const uint64_t left = a.tail_bytes - off;
+          const uint32_t tlen = (uint32_t)(left < 4 * a.r ? left : 4 * a.r);
+          uint32_t tw[8];
+          block_from_image(a.tail + off, tlen, 0u, scr, tw);
+          const uint32_t live = vb >= 32 ? 0xFFFFFFFFu : ((1u << vb) - 1u);
+          uint32_t gtt = 0, eqt = 0, fs = 0;
+          switch (a.r) {
+            case 1: tail_block<1>(tw, a.ttail, live, gtt, eqt, fs); break;
+            case 2: tail_block<2>(tw, a.ttail, live, gtt, eqt, fs); break;
+            case 3: tail_block<3>(tw, a.ttail, live, gtt, eqt, fs); break;
+            case 4: tail_block<4>(tw, a.ttail, live, gtt, eqt, fs); break;
+            case 5: tail_block<5>(tw, a.ttail, live, gtt, eqt, fs); break;
+            case 6: tail_block<6>(tw, a.ttail, live, gtt, eqt, fs); break;
+            default: tail_block<7>(tw, a.ttail, live, gtt, eqt, fs); break;
+          }
+          gt |= eq & gtt;
+          eq &= eqt;
+        }
+      } else if (a.tail_only_eq) {
+        eq = 0;
+      }
+    }
+    uint32_t res = IS_RANGE ? gt : eq;
+    if (row0 + 32 > a.full_rows) {
+      const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
+      res &= lim >= 32 ? 0xFFFFFFFFu : ((1u << lim) - 1u);
+    }
+    a.words[row0 / 32] = res;
+    cnt += __popc(res);
+  }
+  const unsigned long long cv = warp_sum_ull(cnt);
+  if (lane == 0 && cv && a.count) atomicAdd(a.count, cv);
+}
+
 inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // A device-accessible address for `p`: device memory as is, pinned host
@@ -272,7 +401,114 @@ int via_column(const uint8_t *image, uint64_t len, uint64_t scale, uint32_t flag
   return rc ? rc : rf;
 }
 
+using FilterFn = int (*)(const buff_col *, double, uint32_t *, uint64_t *, void *);
+
+int via_column_filter(const uint8_t *image, uint64_t len, uint64_t scale, uint32_t flags,
+                      int kind, double pred, uint32_t *words, uint64_t *count, void *stream) {
+  static const FilterFn fns[4] = {buff_range_filter, buff_equal_filter,
+                                  buff_range_filter_with_slice, buff_equal_filter_with_slice};
+  buff_col *col = nullptr;
+  int rc = buff_deserialize(image, len, scale, flags, stream, &col);
+  if (rc) return rc;
+  rc = fns[kind](col, pred, words, count, stream);
+  const int rf = buff_col_free_async(col, stream);
+  return rc ? rc : rf;
+}
+
 }  // namespace
+
+extern "C" int buff_filter_image(const uint8_t *image, uint64_t len, uint64_t scale,
+                                 uint32_t flags, int kind, double pred, uint32_t *words,
+                                 uint64_t *count, void *stream) {
+  if (!image || kind < 0 || kind > 3) return BUFF_EINVAL;
+  if (len < 20) return BUFF_ECORRUPT;
+  cudaStream_t s = S(stream);
+  buff_col *c = nullptr;
+  int rc = parse_header(image, len, scale, flags, s, &c);
+  if (rc) return rc;
+  const uint32_t n = c->n, nw = (n + 31) / 32;
+  if (n && !words) {
+    buffh::free_col(c);
+    return BUFF_EINVAL;
+  }
+  buffk::FilterArgs fa;
+  int action = 2;
+  if ((rc = buffh::plan_filter(c, pred, kind, &fa, &action))) {
+    buffh::free_col(c);
+    return rc;
+  }
+  if (n == 0 || action != 2) {
+    // no kernel: every word is 0, or every word is ones up to row n
+    buffh::free_col(c);
+    const uint32_t fill = action == 1 ? 0xFFFFFFFFu : 0u;
+    const uint64_t cnt = action == 1 ? n : 0u;
+    if (nw && buffh::is_device_ptr(words)) {
+      rc = buffh::cuda_status(buffk::launch_fill_words(words, n, fill, nullptr, s));
+    } else {
+      for (uint32_t i = 0; i < nw; ++i)
+        words[i] = (i == nw - 1 && (n & 31)) ? (fill & ((1u << (n & 31)) - 1u)) : fill;
+    }
+    if (!rc && count) {
+      if (buffh::is_device_ptr(count))
+        rc = buffh::cuda_status(cudaMemcpyAsync(count, &cnt, 8, cudaMemcpyHostToDevice, s));
+      else
+        *count = cnt;
+    }
+    if (!rc) rc = buffh::cuda_status(cudaStreamSynchronize(s));
+    return rc;
+  }
+  const uint8_t *img = static_cast<const uint8_t *>(device_view(image, c->device));
+  uint32_t *dwords = static_cast<uint32_t *>(const_cast<void *>(device_view(words, c->device)));
+  if (c->k == 0 || !img || !dwords) {  // packed codes, or buffers the device cannot reach
+    buffh::free_col(c);
+    return via_column_filter(image, len, scale, flags, kind, pred, words, count, stream);
+  }
+  ImgFilterArgs a;
+  memset(&a, 0, sizeof(a));
+  a.slices = img + 20;
+  a.tail = img + 20 + (uint64_t)c->k * n;
+  a.n = n;
+  a.k_used = fa.k_used;
+  a.r = fa.r;
+  a.flipx = (flags & BUFF_FLAG_BUFF_LAYOUT) ? 0x80808080u : 0u;
+  a.full_rows = fa.full_rows;
+  a.ttail = fa.ttail;
+  a.tail_only_eq = fa.tail_only_eq;
+  a.tail_bytes = c->tail_bytes;
+  for (uint32_t j = 0; j < fa.k_used; ++j) a.tb |= (unsigned long long)fa.tbyte[j] << (8 * j);
+  a.words = dwords;
+  unsigned long long *d = nullptr;
+  unsigned long long host = 0;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&d), sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(unsigned long long), s);
+  if (e == cudaSuccess) {
+    a.count = d;
+    void (*fn)(ImgFilterArgs) = fa.is_range ? k_filter_image<true> : k_filter_image<false>;
+    const size_t smem = kRegion + (size_t)kImgThreads * 64;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kImgThreads, smem);
+    if (per_sm < 1) per_sm = 1;
+    const uint32_t nchunks = (n + kImgRows - 1) / kImgRows;
+    uint32_t grid = (uint32_t)(per_sm * buffk::num_sms(c->device));
+    if (grid > nchunks) grid = nchunks;
+    fn<<<grid, kImgThreads, smem, s>>>(a);
+    buffk::count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&host, d, 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (d) cudaFreeAsync(d, s);
+  rc = buffh::cuda_status(e);
+  if (!rc && count) {
+    if (buffh::is_device_ptr(count))
+      rc = buffh::cuda_status(cudaMemcpyAsync(count, &host, 8, cudaMemcpyHostToDevice, s));
+    else
+      *count = host;
+    if (!rc && buffh::is_device_ptr(count)) rc = buffh::cuda_status(cudaStreamSynchronize(s));
+  }
+  buffh::free_col(c);
+  return rc;
+}
 
 extern "C" int buff_range_filter_sum_image(const uint8_t *image, uint64_t len, uint64_t scale,
                                            uint32_t flags, double pred, uint32_t *words,

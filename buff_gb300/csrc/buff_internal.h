@@ -213,3 +213,11 @@ void count_launch(uint64_t n = 1);
 uint64_t launches();
 
 }  // namespace buffk
+
+namespace buffh {
+// The filter plan of the buff-simd range/equality filters (kind: 0 range,
+// 1 equality, 2 range _with_slice, 3 equality _with_slice): *action 0 = no
+// row set, 1 = every row set, 2 = run the filter kernel with *a (device
+// pointers left null).  BUFF_EREFPANIC where the reference panics.
+int plan_filter(const buff_col *c, double pred, int kind, buffk::FilterArgs *a, int *action);
+}  // namespace buffh

@@ -22,8 +22,10 @@ the reference.  By default the encode reads the host array and every query
 returns its result in host memory, as the reference's calls take and return
 ``Vec``s; the encoded column stays resident in device memory between calls
 (the reference clones the encoded ``Vec<u8>`` outside its timed regions).
-``--from-bytes`` charges each query with a fresh upload of the serialized image
-instead, the closest analogue of taking ``Vec<u8>`` by value.
+``--from-bytes`` hands every query the serialized image instead, the closest
+analogue of taking ``Vec<u8>`` by value: the buff-simd filters read it in
+place (buff_filter_image: slice 0 and the candidates' later bytes cross the
+host link, nothing else), the other queries upload it first.
 
 The arms ``buff`` and ``buff-slice-scalar`` run other code paths of the
 reference (the scalar buff-layout filters) and are rejected, as the reference
@@ -199,8 +201,16 @@ def run(test_file: str, compression: str, scl: int, pred: float, from_bytes: boo
     print(f"Time elapsed in {enc_label} is: {rust_duration_debug(t_enc)}", file=out)
     times = [t_enc]
     results = {}
+    from .compress import FILTER_KINDS, filter_image
+
+    in_place = {"range": "range", "equal": "equal", "range_with_slice": "range_with_slice",
+                "equal_with_slice": "equal_with_slice"} if compression == "buff-simd" else {}
+    host_image = np.frombuffer(image, dtype=np.uint8)
     for label, name in queries:
-        if from_bytes:
+        if from_bytes and name in in_place:
+            assert in_place[name] in FILTER_KINDS
+            r, t = timed(lambda: filter_image(host_image, scl, pred, in_place[name]))
+        elif from_bytes:
             r, t = timed(lambda: qfn[name](deserialize(image), pred))
         else:
             r, t = timed(lambda: qfn[name](col, pred))

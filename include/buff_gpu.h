@@ -187,6 +187,20 @@ int buff_range_filter_sum(const buff_col *col, double pred, uint32_t *words, uin
 int buff_range_filter_sum_image(const uint8_t *image, uint64_t len, uint64_t scale,
                                 uint32_t flags, double pred, uint32_t *words, uint64_t *count,
                                 buff_sum_result *sum, void *stream);
+/* buff_simd_range_filter, buff_simd_equal_filter and their _with_slice forms
+ * (compress/buff_simd.rs:3361-4025) on the serialized image itself, read
+ * where it lies as in buff_range_filter_sum_image: slice 0 in full, later
+ * slices and tail bytes only for the candidate rows, so about 1/k of the
+ * image crosses the host link.  kind: BUFF_FILTER_*.  Results, panics
+ * (BUFF_EREFPANIC) and the early return are those of the column calls;
+ * fixed_len < 8 and buffers the device cannot reach run as
+ * buff_deserialize + the column call.  Synchronizes the stream. */
+#define BUFF_FILTER_RANGE 0
+#define BUFF_FILTER_EQUAL 1
+#define BUFF_FILTER_RANGE_WITH_SLICE 2
+#define BUFF_FILTER_EQUAL_WITH_SLICE 3
+int buff_filter_image(const uint8_t *image, uint64_t len, uint64_t scale, uint32_t flags,
+                      int kind, double pred, uint32_t *words, uint64_t *count, void *stream);
 
 /* SplitBDDoubleCompress::byte_fixed_max (compress/split_double.rs:3919-4105):
  * the column maximum, its code, and optionally the arg-max bitmap and its

@@ -113,3 +113,73 @@ def test_image_errors(gpu):
     img = Column.encode(x, 10000).serialize()
     with pytest.raises(capi.BuffError):  # truncated image
         range_filter_sum_image(img[:-5], 10000, 100.0)
+
+
+KINDS = ["range", "equal", "range_with_slice", "equal_with_slice"]
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+@pytest.mark.parametrize("where", ["pageable", "pinned", "device"])
+def test_filter_image_matches_oracle(oracle, gpu, case, where):
+    """The four filters on an image in place: bitmaps and counts as the
+    oracle's (and the same panics), for every memory kind."""
+    import torch
+
+    from buff_gb300 import capi
+    from buff_gb300.compress import filter_image
+
+    name, x, scale = CASES[case]
+    xd = x.astype(np.float64)
+    img = oracle.encode(xd, scale)
+    xs = np.sort(xd)
+    preds = [float(xs[len(xs) // 2]), float(xs[-1]), float(xs[0]) - 1.0,
+             float(xs[int(len(xs) * 0.9)]), float(xd[len(xd) // 3])]
+    if where == "pageable":
+        src = np.frombuffer(img, dtype=np.uint8).copy()
+    elif where == "pinned":
+        src = torch.frombuffer(bytearray(img), dtype=torch.uint8).pin_memory()
+    else:
+        src = torch.frombuffer(bytearray(img), dtype=torch.uint8).cuda()
+    fns = {"range": oracle.range_filter, "equal": oracle.equal_filter,
+           "range_with_slice": oracle.range_filter_with_slice,
+           "equal_with_slice": oracle.equal_filter_with_slice}
+    for kind in KINDS:
+        for pred in preds:
+            try:
+                words, cnt = fns[kind](img, scale, pred)[:2]
+            except oracle.OraclePanic:
+                with pytest.raises(capi.ReferencePanic):
+                    filter_image(src, scale, pred, kind)
+                continue
+            fr = filter_image(src, scale, pred, kind)
+            assert fr.count == cnt, (name, kind, pred)
+            assert np.array_equal(np.asarray(fr.words, dtype=np.uint32), words), (name, kind, pred)
+
+
+def test_filter_image_layout_intended_and_device_words(oracle, gpu):
+    import torch
+
+    from buff_gb300.capi import FLAG_BUFF_LAYOUT, FLAG_INTENDED
+    from buff_gb300.compress import Column, filter_image
+
+    x = _walk(200_003, 31)
+    flipped = oracle.encode(x, 10000)
+    plain = oracle.encode(x, 10000, flipped=False)
+    for pred in (float(np.quantile(x, 0.2)), float(x[777])):
+        for kind in KINDS:
+            a = filter_image(np.frombuffer(flipped, dtype=np.uint8), 10000, pred, kind)
+            b = filter_image(np.frombuffer(plain, dtype=np.uint8), 10000, pred, kind,
+                             flags=FLAG_BUFF_LAYOUT)
+            assert a.count == b.count and np.array_equal(a.words, b.words), kind
+            dw = torch.zeros((x.size + 31) // 32, dtype=torch.int32, device="cuda")
+            c = filter_image(torch.frombuffer(bytearray(flipped), dtype=torch.uint8).cuda(), 10000,
+                             pred, kind, words=dw)
+            assert c.count == a.count
+            assert np.array_equal(dw.cpu().numpy().view(np.uint32), a.words), kind
+        # the intended semantics: same as the column call with the flag
+        col = Column.deserialize(flipped, 10000, FLAG_INTENDED)
+        for kind, fn in (("range", col.range_filter), ("equal", col.equal_filter)):
+            want = fn(pred)
+            got = filter_image(np.frombuffer(flipped, dtype=np.uint8), 10000, pred, kind,
+                               flags=FLAG_INTENDED)
+            assert got.count == want.count and np.array_equal(got.words, want.words), kind
