@@ -123,9 +123,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
+def ncu_traffic(kernel: str, rows: int = N_ROWS):
     """Per-launch DRAM bytes of `kernel` from the committed ncu summary
-    (profiles/*.txt lines 'dram_bytes_per_launch <kernel> <bytes>')."""
+    (profiles/*.txt lines 'dram_bytes_per_launch <kernel> <bytes>', captured
+    on the 2^28-row column), scaled to `rows` (traffic grows with the rows)."""
     pdir = os.path.join(ROOT, "profiles")
     if not os.path.isdir(pdir):
         return None
@@ -135,7 +136,7 @@ def ncu_traffic(kernel: str):
         for line in open(os.path.join(pdir, fn)):
             m = re.match(rf"\s*dram_bytes_per_launch\s+{kernel}\s+([0-9.eE+]+)", line)
             if m:
-                return float(m.group(1))
+                return float(m.group(1)) * rows / N_ROWS
     return None
 
 
@@ -1113,14 +1114,14 @@ def main():
                          "value": world * n / two_call_s / 1e9, "unit": "Gvalues/s"},
             "roofline": {"bound": "hbm", "kernel": "k_filter_sum_il", "achieved": roof_fs,
                          "peak": peak, "unit": "GB/s", "frac": roof_fs / peak,
-                         "peak_kind": peak_kind, "traffic": ncu_traffic("k_filter_sum"),
+                         "peak_kind": peak_kind, "traffic": ncu_traffic("k_filter_sum", n),
                          "alg_bytes_per_launch": fs_bytes},
             "roofline_sum": {"kernel": "k_sum", "achieved": roof_sum, "peak": peak,
                              "unit": "GB/s", "frac": roof_sum / peak,
-                             "traffic": ncu_traffic("k_sum"), "alg_bytes_per_launch": sum_bytes},
+                             "traffic": ncu_traffic("k_sum", n), "alg_bytes_per_launch": sum_bytes},
             "roofline_filter": {"kernel": "k_filter", "achieved": roof_filt, "peak": peak,
                                 "unit": "GB/s", "frac": roof_filt / peak,
-                                "traffic": ncu_traffic("k_filter"),
+                                "traffic": ncu_traffic("k_filter", n),
                                 "alg_bytes_per_launch": filt_bytes},
             "e2e": e2e_line,
             "gpu_launches": launches,
