@@ -1623,81 +1623,27 @@ int buff_max_majority(const buff_col *c, double *max_value, uint64_t *max_code,
   if (c->layout != 1) return BUFF_ENOTSUP;
   cudaStream_t s = S(stream);
   int rc = BUFF_OK;
-  uint32_t *cand = nullptr, *buf = nullptr;
-  unsigned long long *cnt = nullptr;
-  uint64_t mx = 0, amc = 0;
+  uint32_t *cand = nullptr;
+  unsigned char *st = nullptr;
+  uint64_t res[2] = {0, 0};  // max code, arg-max count
   const size_t nw = ((size_t)c->n + 31) / 32;
-  const uint32_t kd = c->k - c->m;
-  uint32_t hb[2];
-  auto fetch = [&](uint32_t *hv) -> cudaError_t {
-    cudaError_t e = cudaMemcpyAsync(hv, buf, 8, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    return e;
-  };
+  const size_t sb = buffk::major_max_state_bytes(), mo = buffk::major_max_state_mx_offset();
   CK(scratch(&cand, c->nwp, s));
-  CK(scratch(&buf, 2, s));
-  CK(scratch(&cnt, 1, s));
-  CK(cudaMemsetAsync(cand, 0, sizeof(uint32_t) * c->nwp, s));
-  CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+  CK(scratch(&st, sb, s));
   if (c->n) {
     CK(buffk::launch_fill_words(cand, c->n, 0xFFFFFFFFu, nullptr, s));
-    for (uint32_t col = 0; col < c->m; ++col) {  // buff_simd.rs:2466-2557
-      const uint32_t sh = c->fixed_len - 8 * (col + 1), M = c->majors[col];
-      CK(cudaMemsetAsync(buf, 0, 8, s));
-      CK(buffk::major_candmax(c, col, col == 0 ? nullptr : cand, buf, s));
-      CK(fetch(hb));
-      if (col == 0) {
-        if (hb[1] && hb[0] > M) {
-          CK(buffk::major_select(c, 0, cand, 1, hb[0], s));
-          mx |= (uint64_t)hb[0] << sh;
-        } else {
-          CK(buffk::major_select(c, 0, cand, 0, 0, s));
-          mx |= (uint64_t)M << sh;
-        }
-        continue;
-      }
-      if (!hb[1]) {  // no candidate is an outlier: the major byte is not added
-        CK(buffk::major_select(c, col, cand, 2, 0, s));
-        continue;
-      }
-      if (hb[0] > M) {
-        CK(buffk::major_select(c, col, cand, 1, hb[0], s));
-        mx |= (uint64_t)hb[0] << sh;
-      } else {
-        CK(buffk::major_select(c, col, cand, 2, 0, s));
-        mx |= (uint64_t)M << sh;
-      }
-    }
-    for (uint32_t j = 0; j < kd; ++j) {  // dense slices (:2560-2612)
-      const uint32_t sh = c->fixed_len - 8 * (c->m + j + 1);
-      const uint8_t *sl = c->slices + (size_t)j * c->stride;
-      CK(cudaMemsetAsync(buf, 0, 8, s));
-      CK(buffk::cand_max(sl, nullptr, 0, cand, nw, buf, s));
-      CK(fetch(hb));
-      CK(buffk::cand_select(sl, nullptr, 0, cand, nw, hb[0], nullptr, s));
-      mx |= (uint64_t)hb[0] << sh;
-    }
-    if (c->r) {  // tail (:2613-2651): its candidates are the arg-max rows
-      CK(cudaMemsetAsync(buf, 0, 8, s));
-      CK(buffk::cand_max(nullptr, c->tail, c->r, cand, nw, buf, s));
-      CK(fetch(hb));
-      CK(buffk::cand_select(nullptr, c->tail, c->r, cand, nw, hb[0], cnt, s));
-      mx |= hb[0];
-    } else {
-      CK(cudaMemsetAsync(cand, 0, sizeof(uint32_t) * c->nwp, s));
-    }
+    CK(buffk::major_max(c, cand, st, s));
+    if (argmax_words) CK(cudaMemcpyAsync(argmax_words, cand, nw * 4, cudaMemcpyDefault, s));
+    CK(cudaMemcpyAsync(res, st + mo, 16, cudaMemcpyDeviceToHost, s));
   }
-  if (argmax_words && c->n)
-    CK(cudaMemcpyAsync(argmax_words, cand, nw * 4, cudaMemcpyDefault, s));
-  CK(cudaMemcpyAsync(&amc, cnt, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  if (max_code) *max_code = mx;
-  if (max_value) *max_value = (double)(int64_t)((uint64_t)c->base + mx) / ldexp(1.0, (int)c->dlen);
-  if (argmax_count) *argmax_count = amc;
+  if (max_code) *max_code = res[0];
+  if (max_value)
+    *max_value = (double)(int64_t)((uint64_t)c->base + res[0]) / ldexp(1.0, (int)c->dlen);
+  if (argmax_count) *argmax_count = res[1];
 done:
   if (cand) cudaFreeAsync(cand, s);
-  if (buf) cudaFreeAsync(buf, s);
-  if (cnt) cudaFreeAsync(cnt, s);
+  if (st) cudaFreeAsync(st, s);
   return rc;
 }
 

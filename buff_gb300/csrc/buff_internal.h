@@ -155,14 +155,13 @@ cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, 
 cudaError_t word_ranks(const uint32_t *words, size_t nw, uint32_t *rank, cudaStream_t s);
 cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out,
                           cudaStream_t s);
-cudaError_t major_candmax(const buff_col *c, uint32_t col, const uint32_t *cand, uint32_t *out,
-                          cudaStream_t s);
-cudaError_t major_select(const buff_col *c, uint32_t col, uint32_t *cand, int mode,
-                         uint32_t value, cudaStream_t s);
-cudaError_t cand_max(const uint8_t *slice, const uint8_t *tail, uint32_t r, const uint32_t *cand,
-                     size_t nw, uint32_t *out, cudaStream_t s);
-cudaError_t cand_select(const uint8_t *slice, const uint8_t *tail, uint32_t r, uint32_t *cand,
-                        size_t nw, uint32_t value, unsigned long long *count, cudaStream_t s);
+// buff_max_majority's progressive max on the device: cand (nwp words) ends
+// as the arg-max bitmap; state_dev (major_max_state_bytes(), device) holds
+// the max code (u64 at major_max_state_mx_offset()) and, after it, the
+// arg-max count (u64).
+cudaError_t major_max(const buff_col *c, uint32_t *cand, void *state_dev, cudaStream_t s);
+size_t major_max_state_bytes();
+size_t major_max_state_mx_offset();
 cudaError_t popcount_words(const uint32_t *w, size_t nw, unsigned long long *out, cudaStream_t s);
 cudaError_t major_decode(const buff_col *c, double *out, cudaStream_t s);
 // RAPG decode of the top R bits: m sparse columns, ks slices (those past the

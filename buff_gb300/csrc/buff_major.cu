@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 #include <limits.h>
 #include <math.h>
+#include <stddef.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -293,30 +294,81 @@ __global__ void k_bytesum(const uint8_t *__restrict__ p, size_t nbytes, unsigned
 
 // Largest outlier byte among rows set in `cand` (all outlier rows when cand is
 // null) of sparse column c; any[0] |= 1 when there is such a row.
+// The value of one row in a dense slice (flipped bytes; r == 0) or the
+// packed tail (r bits).
+__device__ __forceinline__ uint32_t field_at(const uint8_t *slice, const uint8_t *tail, uint32_t r,
+                                             uint32_t row) {
+  if (!r) return (uint32_t)(slice[row] ^ 0x80u);
+  const unsigned long long bit = (unsigned long long)row * r;
+  const uint32_t b0 = tail[bit >> 3];
+  const uint32_t b1 = ((bit & 7) + r > 8) ? tail[(bit >> 3) + 1] : 0u;
+  return ((b0 | (b1 << 8)) >> (bit & 7)) & ((1u << r) - 1u);
+}
+
+// The progressive max of buff_max_majority (buff_simd.rs:2444-2861) runs as
+// a chain of candidate steps whose decisions never leave the device: each
+// "max" kernel folds the largest byte among the candidate rows into
+// st->best[step] (one atomic per warp), and the following "select" kernel
+// reads it back, applies the reference's rule for that column, narrows the
+// candidate bitmap and ORs the chosen byte into st->mx.
+struct MaxState {
+  uint32_t best[20];
+  uint32_t flag[20];  // a sparse column's candidates include an outlier
+  unsigned long long mx;
+  unsigned long long count;
+};
+
+// Largest outlier byte among the candidate rows of a sparse column (all its
+// outliers when cand is null).
 __global__ void k_major_candmax(const uint32_t *__restrict__ bits, const uint32_t *__restrict__ rank,
                                 const uint8_t *__restrict__ ob, const uint32_t *__restrict__ cand,
-                                size_t nw, uint32_t *out) {
+                                size_t nw, uint32_t *best, uint32_t *flag) {
+  uint32_t bm = 0, any = 0;
   for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
        w += (size_t)gridDim.x * blockDim.x) {
     const uint32_t B = bits[w];
     const uint32_t sel = cand ? B & cand[w] : B;
     if (!sel) continue;
-    uint32_t b = B, best = 0;
+    any = 1;
+    uint32_t b = B;
     for (uint32_t k = rank[w]; b; ++k) {
       const uint32_t j = __ffs(b) - 1;
       b &= b - 1;
-      if (sel >> j & 1u) best = max(best, (uint32_t)ob[k]);
+      if (sel >> j & 1u) bm = max(bm, (uint32_t)ob[k]);
     }
-    atomicMax(out, best);
-    atomicOr(out + 1, 1u);
+  }
+  bm = __reduce_max_sync(0xFFFFFFFFu, bm);
+  any = __reduce_or_sync(0xFFFFFFFFu, any);
+  if ((threadIdx.x & 31) == 0 && any) {
+    atomicMax(best, bm);
+    atomicOr(flag, 1u);
   }
 }
 
-// New candidate words for a sparse column: mode 0: ~B (valid rows); mode 1:
-// rows of (B & cand) whose outlier byte equals `value`; mode 2: cand & ~B.
+// New candidate words for sparse column `col` (buff_simd.rs:2466-2557):
+// first column: the outlier rows holding the largest outlier byte if it
+// exceeds the major byte M, else every non-outlier row; later columns: if no
+// candidate is an outlier, the candidates stay (minus outliers, i.e. all);
+// if the largest candidate outlier byte exceeds M, those rows; else the
+// candidates that are not outliers.  The chosen byte goes into *mx at `sh`.
 __global__ void k_major_select(const uint32_t *__restrict__ bits, const uint32_t *__restrict__ rank,
                                const uint8_t *__restrict__ ob, uint32_t *cand, size_t nw,
-                               uint32_t n, int mode, uint32_t value) {
+                               uint32_t n, const uint32_t *best, const uint32_t *flag,
+                               uint32_t M, uint32_t sh, int first, unsigned long long *mx) {
+  const uint32_t bv = *best, fl = *flag;
+  int mode;  // 0: ~B (valid rows); 1: rows of (B & cand) whose byte is bv; 2: cand & ~B
+  unsigned long long add;
+  if (first) {
+    mode = (fl && bv > M) ? 1 : 0;
+    add = (unsigned long long)(mode == 1 ? bv : M) << sh;
+  } else if (!fl) {
+    mode = 2;
+    add = 0;
+  } else {
+    mode = bv > M ? 1 : 2;
+    add = (unsigned long long)(bv > M ? bv : M) << sh;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && add) atomicOr(mx, add);
   for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
        w += (size_t)gridDim.x * blockDim.x) {
     const uint32_t row0 = (uint32_t)(w * 32);
@@ -334,53 +386,104 @@ __global__ void k_major_select(const uint32_t *__restrict__ bits, const uint32_t
       for (uint32_t k = rank[w]; b; ++k) {
         const uint32_t j = __ffs(b) - 1;
         b &= b - 1;
-        if ((sel >> j & 1u) && ob[k] == value) out |= 1u << j;
+        if ((sel >> j & 1u) && ob[k] == bv) out |= 1u << j;
       }
     }
     cand[w] = out;
   }
 }
 
-// Progressive max step over a dense slice (flipped bytes; r == 0) or the
-// packed tail (r bits): the largest value among candidate rows.
-__device__ __forceinline__ uint32_t field_at(const uint8_t *slice, const uint8_t *tail, uint32_t r,
-                                             uint32_t row) {
-  if (!r) return (uint32_t)(slice[row] ^ 0x80u);
-  const unsigned long long bit = (unsigned long long)row * r;
-  const uint32_t b0 = tail[bit >> 3];
-  const uint32_t b1 = ((bit & 7) + r > 8) ? tail[(bit >> 3) + 1] : 0u;
-  return ((b0 | (b1 << 8)) >> (bit & 7)) & ((1u << r) - 1u);
+// 0xFF in byte i of the result for each set bit i of the 4-bit x.
+__device__ __forceinline__ uint32_t bytemask4(uint32_t x) {
+  return ((x * 0x00204081u) & 0x01010101u) * 0xFFu;
 }
 
-__global__ void k_cand_max(const uint8_t *__restrict__ slice, const uint8_t *__restrict__ tail,
-                           uint32_t r, const uint32_t *__restrict__ cand, size_t nw, uint32_t *out) {
-  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
-       w += (size_t)gridDim.x * blockDim.x) {
-    uint32_t b = cand[w];
-    if (!b) continue;
-    uint32_t best = 0;
-    while (b) {
-      const uint32_t j = __ffs(b) - 1;
-      b &= b - 1;
-      best = max(best, field_at(slice, tail, r, (uint32_t)(w * 32 + j)));
-    }
-    atomicMax(out, best);
+// The 32 unflipped slice bytes of rows w*32 .. w*32+31 (one 32-byte block).
+__device__ __forceinline__ void block_bytes(const uint8_t *slice, size_t w, uint32_t *u) {
+  const uint4 lo = __ldg(reinterpret_cast<const uint4 *>(slice + w * 32));
+  const uint4 hi = __ldg(reinterpret_cast<const uint4 *>(slice + w * 32 + 16));
+  const uint32_t v[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+  for (int q = 0; q < 8; ++q) u[q] = v[q] ^ 0x80808080u;
+}
+
+// The 32 R-bit tail fields of rows w*32 .. w*32+31 (4R bytes at 4R*w).
+template <int R>
+__device__ __forceinline__ void block_fields(const uint8_t *tail, size_t w, uint32_t *f) {
+  const uint32_t *p = reinterpret_cast<const uint32_t *>(tail + (size_t)4 * R * w);
+  uint32_t tw[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) tw[i] = __ldg(p + i);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    const int bit = i * R, wi = bit >> 5, sh = bit & 31;
+    const uint32_t hi = (wi + 1 < R) ? tw[wi + 1] : 0u;
+    f[i] = __funnelshift_r(tw[wi], hi, sh) & ((1u << R) - 1u);
   }
 }
 
+// Progressive max step over a dense slice (R == 0) or the R-bit tail: the
+// largest value among the candidate rows, folded into *best.
+template <int R>
+__global__ void k_cand_max(const uint8_t *__restrict__ slice, const uint8_t *__restrict__ tail,
+                           const uint32_t *__restrict__ cand, size_t nw, uint32_t *best) {
+  uint32_t bm = 0;
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
+       w += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t b = cand[w];
+    if (!b) continue;
+    if (R == 0) {
+      uint32_t u[8], m = 0;
+      block_bytes(slice, w, u);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) m = __vmaxu4(m, u[q] & bytemask4((b >> (4 * q)) & 0xFu));
+      m = __vmaxu4(m, m >> 16);
+      m = __vmaxu4(m, m >> 8);
+      bm = max(bm, m & 0xFFu);
+    } else {
+      uint32_t f[32];
+      block_fields<R == 0 ? 1 : R>(tail, w, f);
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        if (b >> i & 1u) bm = max(bm, f[i]);
+    }
+  }
+  bm = __reduce_max_sync(0xFFFFFFFFu, bm);
+  if ((threadIdx.x & 31) == 0 && bm) atomicMax(best, bm);
+}
+
+// Keeps the candidate rows whose value equals *best and ORs *best << sh
+// into *mx; count (may be null) receives the kept rows.
+template <int R>
 __global__ void k_cand_select(const uint8_t *__restrict__ slice, const uint8_t *__restrict__ tail,
-                              uint32_t r, uint32_t *cand, size_t nw, uint32_t value,
-                              unsigned long long *count) {
+                              uint32_t *cand, size_t nw, const uint32_t *best, uint32_t sh,
+                              unsigned long long *mx, unsigned long long *count) {
+  const uint32_t v = *best;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && v) atomicOr(mx, (unsigned long long)v << sh);
   unsigned long long c = 0;
   for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
        w += (size_t)gridDim.x * blockDim.x) {
-    uint32_t b = cand[w], out = 0;
-    while (b) {
-      const uint32_t j = __ffs(b) - 1;
-      b &= b - 1;
-      if (field_at(slice, tail, r, (uint32_t)(w * 32 + j)) == value) out |= 1u << j;
+    const uint32_t b = cand[w];
+    uint32_t out = 0;
+    if (b) {
+      if (R == 0) {
+        uint32_t u[8], e[8];
+        block_bytes(slice, w, u);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const uint32_t x = u[q] ^ (v * 0x01010101u);  // zero bytes where equal
+          e[q] = ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
+        }
+        out = b & gather32(e);
+      } else {
+        uint32_t f[32];
+        block_fields<R == 0 ? 1 : R>(tail, w, f);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) out |= (uint32_t)(f[i] == v) << i;
+        out &= b;
+      }
+      cand[w] = out;
     }
-    cand[w] = out;
     c += __popc(out);
   }
   if (count) {
@@ -815,39 +918,58 @@ cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *o
   return cudaGetLastError();
 }
 
-cudaError_t major_candmax(const buff_col *c, uint32_t col, const uint32_t *cand, uint32_t *out,
-                          cudaStream_t s) {
-  k_major_candmax<<<grid_of(c->nwp, 256), 256, 0, s>>>(c->obits + col * c->nwp,
-                                                        c->orank + col * rank_stride(c),
-                                                        c->obytes + c->oofs[col], cand, c->nwp,
-                                                        out);
-  count_launch();
+// buff_max_majority's progressive max (buff_simd.rs:2444-2861) with every
+// step's decision made on the device; one host synchronization at the end.
+cudaError_t major_max(const buff_col *c, uint32_t *cand, void *state_dev, cudaStream_t s) {
+  MaxState *st = static_cast<MaxState *>(state_dev);
+  const size_t nw = ((size_t)c->n + 31) / 32;
+  const uint32_t kd = c->k - c->m;
+  const int g = grid_of(c->nwp, 256);
+  cudaError_t e = cudaMemsetAsync(st, 0, sizeof(MaxState), s);
+  if (e != cudaSuccess) return e;
+  uint32_t step = 0;
+  for (uint32_t col = 0; col < c->m; ++col, ++step) {
+    const uint32_t *bits = c->obits + col * c->nwp, *rank = c->orank + col * rank_stride(c);
+    const uint8_t *ob = c->obytes + c->oofs[col];
+    k_major_candmax<<<g, 256, 0, s>>>(bits, rank, ob, col == 0 ? nullptr : cand, c->nwp,
+                                      st->best + step, st->flag + step);
+    k_major_select<<<g, 256, 0, s>>>(bits, rank, ob, cand, c->nwp, c->n, st->best + step,
+                                     st->flag + step, c->majors[col],
+                                     c->fixed_len - 8 * (col + 1), col == 0 ? 1 : 0, &st->mx);
+    count_launch(2);
+  }
+  const int gw = grid_of(nw, 256);
+  for (uint32_t j = 0; j < kd; ++j, ++step) {  // dense slices (:2560-2612)
+    const uint8_t *sl = c->slices + (size_t)j * c->stride;
+    const uint32_t sh = c->fixed_len - 8 * (c->m + j + 1);
+    k_cand_max<0><<<gw, 256, 0, s>>>(sl, nullptr, cand, nw, st->best + step);
+    k_cand_select<0><<<gw, 256, 0, s>>>(sl, nullptr, cand, nw, st->best + step, sh, &st->mx,
+                                        nullptr);
+    count_launch(2);
+  }
+  if (c->r) {  // tail (:2613-2651): its candidates are the arg-max rows
+    switch (c->r) {
+#define TAIL_STEP(R)                                                                        \
+  case R:                                                                                   \
+    k_cand_max<R><<<gw, 256, 0, s>>>(nullptr, c->tail, cand, nw, st->best + step);          \
+    k_cand_select<R><<<gw, 256, 0, s>>>(nullptr, c->tail, cand, nw, st->best + step, 0,     \
+                                        &st->mx, &st->count);                               \
+    break;
+      TAIL_STEP(1) TAIL_STEP(2) TAIL_STEP(3) TAIL_STEP(4) TAIL_STEP(5) TAIL_STEP(6)
+      TAIL_STEP(7)
+#undef TAIL_STEP
+      default: return cudaErrorInvalidValue;
+    }
+    count_launch(2);
+  } else {
+    e = cudaMemsetAsync(cand, 0, sizeof(uint32_t) * c->nwp, s);
+    if (e != cudaSuccess) return e;
+  }
   return cudaGetLastError();
 }
 
-cudaError_t major_select(const buff_col *c, uint32_t col, uint32_t *cand, int mode, uint32_t value,
-                         cudaStream_t s) {
-  k_major_select<<<grid_of(c->nwp, 256), 256, 0, s>>>(c->obits + col * c->nwp,
-                                                       c->orank + col * rank_stride(c),
-                                                       c->obytes + c->oofs[col], cand, c->nwp,
-                                                       c->n, mode, value);
-  count_launch();
-  return cudaGetLastError();
-}
-
-cudaError_t cand_max(const uint8_t *slice, const uint8_t *tail, uint32_t r, const uint32_t *cand,
-                     size_t nw, uint32_t *out, cudaStream_t s) {
-  k_cand_max<<<grid_of(nw, 256), 256, 0, s>>>(slice, tail, r, cand, nw, out);
-  count_launch();
-  return cudaGetLastError();
-}
-
-cudaError_t cand_select(const uint8_t *slice, const uint8_t *tail, uint32_t r, uint32_t *cand,
-                        size_t nw, uint32_t value, unsigned long long *count, cudaStream_t s) {
-  k_cand_select<<<grid_of(nw, 256), 256, 0, s>>>(slice, tail, r, cand, nw, value, count);
-  count_launch();
-  return cudaGetLastError();
-}
+size_t major_max_state_bytes() { return sizeof(MaxState); }
+size_t major_max_state_mx_offset() { return offsetof(MaxState, mx); }
 
 cudaError_t popcount_words(const uint32_t *w, size_t nw, unsigned long long *out, cudaStream_t s) {
   k_popc<<<grid_of(nw, 256), 256, 0, s>>>(w, nw, out);
