@@ -704,6 +704,90 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a)
   }
 }
 
+// The same plans for 1..4 dense slices (every row written with the default
+// sparse bytes; k_rapg_fixup then rewrites the outlier rows): lane L takes 4
+// consecutive rows of each 128-row group -- one 4-byte load per dense slice,
+// a 4x4 byte transpose into the 4 rows' dense bytes, the tail fields by one
+// shuffle pair -- and the 4 values leave in one 32-byte store when the
+// output is 32-byte aligned (ST32), else in two 16-byte stores.  Merging the
+// outlier rows into this pass was measured slower: with 1 % outliers most
+// warps then wait on a dependent rank-and-byte load in most steps.
+template <int KS, bool N32, bool ST32>
+__global__ void __launch_bounds__(kThreads) k_rapg_decode_fast4(RapgDecodeArgs a) {
+  static_assert(KS >= 1 && KS <= 4, "k_rapg_decode_fast4 transposes at most 4 slices");
+  using CodeT = typename std::conditional<N32, uint32_t, unsigned long long>::type;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nchunks = (a.n + kRowChunk - 1) / kRowChunk;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t ts = a.ts;
+  const uint32_t tmask = ts ? ((1u << ts) - 1u) : 0u;
+  const uint32_t kx = KS == 4 ? 0x80808080u : (0x80808080u & ((1u << (8 * (KS & 3))) - 1u));
+  for (uint32_t ch = warp; ch < nchunks; ch += nwarps) {
+    const uint32_t r0 = ch * kRowChunk;
+    uint32_t sw[4][KS];
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+      for (int s = 0; s < KS; ++s)
+        sw[m][s] = __ldg(reinterpret_cast<const uint32_t *>(a.slices + s * a.stride + r0 +
+                                                            m * 128 + 4 * lane));
+    uint32_t tw[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      tw[m] = 0;
+      // a 128-row group's ts-bit fields: 4 ts words at byte 16 ts * group
+      if (ts && lane < 4 * ts)
+        tw[m] = __ldg(reinterpret_cast<const uint32_t *>(a.tail + (size_t)16 * ts * (r0 / 128 + m)) +
+                      lane);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const uint32_t row0 = r0 + m * 128 + 4 * lane;
+      uint32_t W[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) W[j] = j < KS ? sw[m][KS - 1 - j] : 0u;
+      const uint32_t t0 = __byte_perm(W[0], W[1], 0x5140), t1 = __byte_perm(W[0], W[1], 0x7362);
+      const uint32_t t2 = __byte_perm(W[2], W[3], 0x5140), t3 = __byte_perm(W[2], W[3], 0x7362);
+      const uint32_t c[4] = {__byte_perm(t0, t2, 0x5410), __byte_perm(t0, t2, 0x7632),
+                             __byte_perm(t1, t3, 0x5410), __byte_perm(t1, t3, 0x7632)};
+      uint32_t f = 0;
+      if (ts) {
+        const uint32_t bit = 4 * lane * ts, wi = bit >> 5;
+        const uint32_t w0 = __shfl_sync(0xFFFFFFFFu, tw[m], wi);
+        const uint32_t w1 = __shfl_sync(0xFFFFFFFFu, tw[m], (wi + 1) & 31);
+        f = __funnelshift_r(w0, w1, bit & 31);
+      }
+      double v[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        CodeT code = (CodeT)(c[i] ^ kx);
+        if (ts) code = (code << ts) | (CodeT)((f >> (i * ts)) & tmask);
+        code |= (CodeT)a.sdef;
+        if (N32)
+          v[i] = i32_to_f64_scaled((int)((uint32_t)a.base + (uint32_t)code), a.dlen);
+        else
+          v[i] = i64_to_f64_scaled((long long)((unsigned long long)a.base + code), a.dlen);
+      }
+      double *o = a.out + row0;
+      if (row0 + 4 <= a.n) {
+        if (ST32) {
+          asm volatile("st.global.cs.v4.f64 [%0], {%1, %2, %3, %4};" ::"l"(o), "d"(v[0]),
+                       "d"(v[1]), "d"(v[2]), "d"(v[3])
+                       : "memory");
+        } else {
+          __stcs(reinterpret_cast<double2 *>(o), make_double2(v[0], v[1]));
+          __stcs(reinterpret_cast<double2 *>(o + 2), make_double2(v[2], v[3]));
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (row0 + i < a.n) o[i] = v[i];
+      }
+    }
+  }
+}
+
 // Rows that are outliers in some sparse column, decoded in full after
 // k_rapg_decode_fast wrote them with zero sparse bytes: one thread per
 // 32-row bitmap word, the rows of the union of the columns' words.
@@ -1002,7 +1086,33 @@ static void launch_fast_ks(const RapgDecodeArgs &a, int g, cudaStream_t s) {
   }
 }
 
+template <int KS, bool N32>
+static void launch_fast4(const RapgDecodeArgs &a, int g, cudaStream_t s) {
+  if ((reinterpret_cast<uintptr_t>(a.out) & 31u) == 0)
+    k_rapg_decode_fast4<KS, N32, true><<<g, kThreads, 0, s>>>(a);
+  else
+    k_rapg_decode_fast4<KS, N32, false><<<g, kThreads, 0, s>>>(a);
+}
+
 static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
+  if (a.ks >= 1 && a.ks <= 4) {
+    const int g = grid_of((size_t)(a.n + kRowChunk - 1) / kRowChunk * 32, kThreads);
+    const long long maxc = a.R >= 63 ? -1 : (long long)((1ull << a.R) - 1ull);
+    const bool n32 =
+        a.R <= 32 && a.base >= INT32_MIN && maxc >= 0 && a.base + maxc <= (long long)INT32_MAX;
+    switch (a.ks) {
+      case 1: n32 ? launch_fast4<1, true>(a, g, s) : launch_fast4<1, false>(a, g, s); break;
+      case 2: n32 ? launch_fast4<2, true>(a, g, s) : launch_fast4<2, false>(a, g, s); break;
+      case 3: n32 ? launch_fast4<3, true>(a, g, s) : launch_fast4<3, false>(a, g, s); break;
+      default: n32 ? launch_fast4<4, true>(a, g, s) : launch_fast4<4, false>(a, g, s); break;
+    }
+    count_launch();
+    if (a.m) {
+      k_rapg_fixup<<<grid_of(((size_t)a.n + 31) / 32, kThreads), kThreads, 0, s>>>(a);
+      count_launch();
+    }
+    return;
+  }
   {
     const int g = grid_of((size_t)(a.n + kRowChunk - 1) / kRowChunk * 32, kThreads);
     // every value base + code (R bits) in 32 bits: the 32-bit build and conversion
