@@ -823,6 +823,47 @@ __global__ void __launch_bounds__(kThreads) k_rapg_fixup(RapgDecodeArgs a) {
   }
 }
 
+// The same fix-up when every value the fast pass wrote is exact (|base| +
+// 2^R < 2^53): an outlier row's written value is read back as its integer
+// code -- exact, since value * 2^dlen is an integer below 2^53 -- and only
+// its sparse bytes are replaced, so the dense slices and the tail are not
+// read again.  `low` = bits below the sparse bytes.
+__global__ void __launch_bounds__(kThreads) k_rapg_fixup_patch(RapgDecodeArgs a, uint32_t low,
+                                                               double scale) {
+  const size_t nw = ((size_t)a.n + 31) / 32;
+  const unsigned long long lowmask = (1ull << low) - 1ull;
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nw;
+       w += (size_t)gridDim.x * blockDim.x) {
+    uint32_t Bw[8], Rk[8], any = 0;
+#pragma unroll
+    for (uint32_t c = 0; c < 8; ++c) {
+      Bw[c] = c < a.m ? __ldg(a.obits + c * a.nwp + w) : 0u;
+      any |= Bw[c];
+    }
+    if (!any) continue;
+#pragma unroll
+    for (uint32_t c = 0; c < 8; ++c) Rk[c] = c < a.m ? __ldg(a.orank + c * a.rs + w) : 0u;
+    while (any) {
+      const uint32_t j = __ffs(any) - 1;
+      any &= any - 1;
+      const uint32_t i = (uint32_t)(w * 32 + j);
+      unsigned long long sp = 0;
+#pragma unroll
+      for (uint32_t c = 0; c < 8; ++c) {
+        if (c < a.m) {
+          uint32_t b = a.smaj[c];
+          if (Bw[c] >> j & 1u) b = a.obytes[a.oofs[c] + Rk[c] + __popc(Bw[c] & ((1u << j) - 1u))];
+          sp = (sp << 8) | b;
+        }
+      }
+      const long long whole = __double2ll_rn(a.out[i] * scale);  // base + written code
+      const unsigned long long code =
+          ((unsigned long long)(whole - a.base) & lowmask) | (sp << low);
+      a.out[i] = i64_to_f64_scaled((long long)((unsigned long long)a.base + code), a.dlen);
+    }
+  }
+}
+
 __global__ void k_field_sum(const uint8_t *p, unsigned long long bit0, uint32_t width, uint32_t n,
                             unsigned long long *out) {
   unsigned long long acc = 0;
@@ -1108,7 +1149,14 @@ static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
     }
     count_launch();
     if (a.m) {
-      k_rapg_fixup<<<grid_of(((size_t)a.n + 31) / 32, kThreads), kThreads, 0, s>>>(a);
+      const uint32_t low = 8 * a.ks + a.ts;
+      const unsigned long long ab = a.base < 0 ? 0ull - (unsigned long long)a.base
+                                               : (unsigned long long)a.base;
+      const int gw = grid_of(((size_t)a.n + 31) / 32, kThreads);
+      if (a.R <= 52 && low < 64 && ab < (1ull << 53) - (1ull << a.R) && a.dlen <= 1000)
+        k_rapg_fixup_patch<<<gw, kThreads, 0, s>>>(a, low, ldexp(1.0, a.dlen));
+      else
+        k_rapg_fixup<<<gw, kThreads, 0, s>>>(a);
       count_launch();
     }
     return;

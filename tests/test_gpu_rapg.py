@@ -25,10 +25,15 @@ def _cases():
     tenth = np.round(rng.uniform(0.0, 1.9, 4097), 1)          # scale 10: packed codes, no count byte
     tiny = np.array([0.1, 0.5, 1.2])
     f32 = np.round(rng.normal(10, 3, 50_001), 2).astype(np.float32)
+    # codes wider than 52 bits: values past 2^53 / 2^dlen, where the decode
+    # rounds and outlier rows are rebuilt from the slices, not patched
+    wide = np.round(rng.normal(3e6, 50, 20_011), 9)
+    pos = np.nonzero(rng.uniform(size=wide.size) < 0.01)[0]
+    wide[pos] = np.round(rng.uniform(1e8, 4e9, pos.size), 9)
     return rapg_cases() + [("big", big, 1000000), ("runs", runs, 1000000),
                            ("narrow", narrow, 100), ("narrow0", narrow0, 100),
                            ("tenth", tenth, 10), ("tiny", tiny, 10),
-                           ("f32", f32, 100)]
+                           ("f32", f32, 100), ("wide_codes", wide, 10 ** 9)]
 
 
 CASES = _cases()
