@@ -183,3 +183,43 @@ def test_filter_image_layout_intended_and_device_words(oracle, gpu):
             got = filter_image(np.frombuffer(flipped, dtype=np.uint8), 10000, pred, kind,
                                flags=FLAG_INTENDED)
             assert got.count == want.count and np.array_equal(got.words, want.words), kind
+
+
+def test_image_edge_plans(oracle, gpu):
+    """Plans without the image kernel: no rows, packed codes (fixed_len < 8),
+    the early return, bad kinds and truncated images."""
+    from buff_gb300 import capi
+    from buff_gb300.compress import Column, filter_image, range_filter_sum_image
+
+    empty = Column.encode(np.zeros(0), 10000).serialize()
+    fr = filter_image(empty, 10000, 1.0)
+    assert fr.count == 0 and fr.n == 0
+    fr, sr = range_filter_sum_image(empty, 10000, 1.0)
+    assert fr.count == 0 and sr.n_partials == Column.deserialize(empty, 10000).sum().n_partials
+    rng = np.random.default_rng(3)
+    packed = np.round(rng.uniform(1.0, 1.5, 1000), 1)  # scale 10: 3-bit codes, no slice
+    img = oracle.encode(packed, 10)
+    h = oracle.header(img)
+    assert (h.ilen + h.dlen) & 0xFFFFFFFF < 8  # ilen is stored wrapped when fixed_len < dlen
+    for kind, fn in (("range", oracle.range_filter), ("equal", oracle.equal_filter)):
+        words, cnt = fn(img, 10, 1.2)[:2]
+        got = filter_image(img, 10, 1.2, kind)
+        assert got.count == cnt and np.array_equal(got.words, words), kind
+    words, cnt = oracle.range_filter(img, 10, 1.2)[:2]
+    fr, sr = range_filter_sum_image(img, 10, 1.2)
+    assert fr.count == cnt and sr.sum == oracle.buff_sum(img, 10)[0]
+    walk = _walk(5000, 9)
+    wimg = oracle.encode(walk, 10000)
+    for kind, fn in (("range", oracle.range_filter), ("equal", oracle.equal_filter),
+                     ("range_with_slice", oracle.range_filter_with_slice)):
+        words, cnt = fn(wimg, 10000, -1e6)[:2]  # below the base: the early return
+        got = filter_image(wimg, 10000, -1e6, kind)
+        assert got.count == cnt and np.array_equal(got.words, words), kind
+    with pytest.raises(capi.BuffError):
+        capi.check(capi.lib().buff_filter_image(np.frombuffer(wimg, dtype=np.uint8).ctypes.data,
+                                                len(wimg), 10000, 0, 7, 1.0, None, None, None))
+    with pytest.raises(capi.BuffError):
+        filter_image(wimg[:-3], 10000, 100.0)
+    small = oracle.encode(walk[:20], 10000)  # _with_slice on fewer than 32 rows panics
+    with pytest.raises(capi.ReferencePanic):
+        filter_image(small, 10000, float(walk[5]), "equal_with_slice")
