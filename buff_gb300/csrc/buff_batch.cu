@@ -757,13 +757,17 @@ __device__ __forceinline__ void tile_filter32(const BQ &q, uint32_t r0, uint32_t
 
 // ---- filter + sum with the slices staged through shared memory
 //
-// Each lane copies its own 16-byte pieces (16 rows of up to 4 slices) and the
-// first 4r lanes the step's 64r tail bytes into a per-warp ring of kDepth
-// 512-row steps with cp.async, so kDepth steps of every slice are in flight
-// without holding registers; a lane reads back only what it copied (the
-// tail group excepted, hence the warp barrier around each step).
-constexpr int kDepth = 4;
-constexpr uint32_t kSlotBytes = 4 * 512 + 512;  // 4 slices + up to 448 tail bytes
+// Each lane copies its own 16-byte pieces (16 rows of up to 3 slices; a 4th
+// and later slice are loaded directly) and the first 4r lanes the step's 64r
+// tail bytes into a per-warp ring of kDepth 512-row steps with cp.async, so
+// kDepth steps of every slice are in flight without holding registers; a
+// lane reads back only what it copied (the tail group excepted, hence the
+// warp barrier around each step).  Ring shape measured on the 4,096-column
+// plan: 3 steps of 3 slices (6 KB per warp) 1.47 ms per replay, against 1.80
+// (4 x 4 slices), 1.51 (2 x 3), 1.54 (4 x 3), 1.55 (3 x 2), 1.83 (5 x 3):
+// the smaller ring lets more warps stay resident.
+constexpr int kDepth = 3;
+constexpr uint32_t kSlotBytes = 3 * 512 + 512;  // 3 slices + up to 448 tail bytes
 constexpr uint32_t kRingBytes = kDepth * kSlotBytes;
 
 __device__ __forceinline__ void cp16(uint8_t *dst, const uint8_t *src) {
@@ -784,7 +788,7 @@ __device__ __forceinline__ void fs_issue(const BQ &q, uint32_t sb, uint32_t r1, 
       for (uint32_t j = 0; j < nst; ++j)
         cp16(slot + j * 512 + lane * 16, q.slices + j * q.stride + row0);
     if (q.r && lane < 4 * q.r)
-      cp16(slot + 4 * 512 + lane * 16, q.tail + (size_t)(sb >> 9) * 64 * q.r + lane * 16);
+      cp16(slot + 3 * 512 + lane * 16, q.tail + (size_t)(sb >> 9) * 64 * q.r + lane * 16);
   }
   cp_commit();  // every lane commits one group per step, even an empty one
 }
@@ -794,7 +798,7 @@ __device__ __forceinline__ void tile_fs_async(const BQ &q, uint32_t r0, uint32_t
                                               uint32_t lane, uint8_t *ring) {
   const bool is_range = q.ops & kOpRange;
   const bool cmp = DO_F && q.fill == 0;
-  const uint32_t nst = q.k < 4 ? q.k : 4u;  // slices staged; later ones load directly
+  const uint32_t nst = q.k < 3 ? q.k : 3u;  // slices staged; later ones load directly
   const unsigned long long pat = q.r > 1 ? every_r(q.r) : 0ull;
   const uint32_t qh0 = q.r > 1 ? (q.r - 64 % q.r) % q.r : 0u;
   uint32_t sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -822,7 +826,7 @@ __device__ __forceinline__ void tile_fs_async(const BQ &q, uint32_t r0, uint32_t
       for (uint32_t j = 0; j < 8; ++j) {
         if (j >= q.k) break;
         const bool need_f = cmp && j < q.k_used && eq;
-        const uint4 w = j < 4 ? *reinterpret_cast<const uint4 *>(slot + j * 512 + lane * 16)
+        const uint4 w = j < 3 ? *reinterpret_cast<const uint4 *>(slot + j * 512 + lane * 16)
                               : __ldcs(reinterpret_cast<const uint4 *>(q.slices + j * q.stride + row0));
         sacc[j] = __dp4a(w.x ^ H, 0x01010101u, sacc[j]);
         sacc[j] = __dp4a(w.y ^ H, 0x01010101u, sacc[j]);
@@ -839,7 +843,7 @@ __device__ __forceinline__ void tile_fs_async(const BQ &q, uint32_t r0, uint32_t
       }
       if (q.r) {
         const unsigned short *tp =
-            reinterpret_cast<const unsigned short *>(slot + 4 * 512 + lane * 2 * q.r);
+            reinterpret_cast<const unsigned short *>(slot + 3 * 512 + lane * 2 * q.r);
         unsigned long long lo = 0, hi = 0;
 #pragma unroll
         for (uint32_t i = 0; i < 7; ++i) {

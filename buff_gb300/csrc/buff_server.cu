@@ -317,6 +317,9 @@ int launch_plain(Slot &sl) {
   return buffh::cuda_status(e);
 }
 
+// Waiting requests beyond the free slots before slots take batches.
+constexpr size_t kQueueForBatch = 8;
+
 void loop(buff_server *S) {
   cudaSetDevice(S->device);
   const uint32_t maxb = S->cfg.batched ? S->cfg.max_batch : 1;
@@ -347,12 +350,14 @@ void loop(buff_server *S) {
         worked = true;
       }
     }
-    // admit in arrival order into free slots; while the waiting requests do
-    // not outnumber the free slots each takes a slot of its own (light load:
-    // latency), beyond that slots take batches (throughput)
+    // admit in arrival order into free slots; until the waiting requests
+    // outnumber the free slots by more than kQueueForBatch each takes a slot
+    // of its own (light load: latency -- a batched launch of a handful of
+    // requests costs more than the same requests one by one), beyond that
+    // slots take batches (throughput)
     uint32_t free_slots = 0;
     for (const Slot &sl : S->slots) free_slots += !sl.busy;
-    const uint32_t take = S->waiting.size() > free_slots ? maxb : 1;
+    const uint32_t take = S->waiting.size() > free_slots + kQueueForBatch ? maxb : 1;
     for (Slot &sl : S->slots) {
       if (sl.busy || S->waiting.empty()) continue;
       while (!S->waiting.empty() && sl.reqs.size() < take) {
