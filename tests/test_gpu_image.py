@@ -223,3 +223,32 @@ def test_image_edge_plans(oracle, gpu):
     small = oracle.encode(walk[:20], 10000)  # _with_slice on fewer than 32 rows panics
     with pytest.raises(capi.ReferencePanic):
         filter_image(small, 10000, float(walk[5]), "equal_with_slice")
+
+
+def test_concurrent_streams_on_one_column(oracle, gpu):
+    """Queries on one resident column from two streams at once return what
+    each returns alone (the handle is read-only after encode)."""
+    import torch
+
+    from buff_gb300 import capi
+    from buff_gb300.compress import Column
+
+    x = _walk(2_000_003, 77)
+    img = oracle.encode(x, 10000)
+    col = Column.encode(x, 10000)
+    L = capi.lib()
+    preds = [float(np.quantile(x, q)) for q in (0.05, 0.5, 0.95, 0.3)]
+    nw = (x.size + 31) // 32
+    streams = [torch.cuda.Stream() for _ in preds]
+    words = [torch.zeros(nw, dtype=torch.int32, device="cuda") for _ in preds]
+    counts = [torch.zeros(1, dtype=torch.int64, device="cuda") for _ in preds]
+    for _ in range(3):
+        for st, p, w, c in zip(streams, preds, words, counts):
+            with torch.cuda.stream(st):
+                capi.check(L.buff_range_filter(col.handle, p, w.data_ptr(), c.data_ptr(),
+                                               st.cuda_stream))
+        torch.cuda.synchronize()
+        for p, w, c in zip(preds, words, counts):
+            ow, oc = oracle.range_filter(img, 10000, p)[:2]
+            assert int(c.item()) == oc
+            assert np.array_equal(w.cpu().numpy().view(np.uint32), ow)
