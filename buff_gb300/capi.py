@@ -15,6 +15,7 @@ from . import build as _build
 
 OK, EINVAL, ENOMEM, ECUDA, EREFPANIC, ECORRUPT, ETIMEDOUT, ENOTSUP, EFULL, ESCRATCH = range(10)
 NOALLOC_MAX_ROWS = 1 << 26
+MAX_ROWS = (1 << 32) - 512  # BUFF_MAX_ROWS
 FLAG_INTENDED = 0x1
 FLAG_RAW_BITMAPS = 0x2
 FLAG_BUFF_LAYOUT = 0x4

@@ -1470,7 +1470,7 @@ int buff_batch_encode_f64(const double *const *values, const uint64_t *lens,
   // pass 1 inputs: every column with >= 2 rows, a PRECISION_MAP entry, key-mode
   // precision and a 16-byte aligned device pointer takes the batched path
   for (uint32_t i = 0; i < ncols; ++i) {
-    if (lens[i] >= (1ull << 32)) {
+    if (lens[i] > BUFF_MAX_ROWS) {
       rc = BUFF_EINVAL;
       goto done;
     }

@@ -268,7 +268,7 @@ int encode_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, c
   if (!out) return BUFF_EINVAL;
   *out = nullptr;
   if (slice && (flags & BUFF_FLAG_INTENDED)) return BUFF_ENOTSUP;
-  if (n64 >= (1ull << 32)) return BUFF_EINVAL;  // the header stores n as u32
+  if (n64 > BUFF_MAX_ROWS) return BUFF_EINVAL;  // the header stores n as u32 (BUFF_MAX_ROWS)
   if (n64 > 0 && !values) return BUFF_EINVAL;
   const uint32_t n = (uint32_t)n64;
   const bool intended = flags & BUFF_FLAG_INTENDED;
@@ -527,7 +527,7 @@ int encode_major_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t fl
   if (!out) return BUFF_EINVAL;
   *out = nullptr;
   if (flags & BUFF_FLAG_INTENDED) return BUFF_ENOTSUP;
-  if (n64 >= (1ull << 32)) return BUFF_EINVAL;
+  if (n64 > BUFF_MAX_ROWS) return BUFF_EINVAL;
   if (n64 > 0 && !values) return BUFF_EINVAL;
   const uint32_t n = (uint32_t)n64;
   const int prec = prec_of_scale(scale);
@@ -1008,6 +1008,10 @@ int buff_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_
   c->n = w[2];
   c->ilen = w[3];
   c->dlen = w[4];
+  if (c->n > BUFF_MAX_ROWS) {
+    rc = BUFF_ENOTSUP;
+    goto done;
+  }
   {
     const uint32_t fl = c->ilen + c->dlen;  // the decoders' `dlen + ilen` (u32)
     if (fl > 64 || c->dlen > 1000) {
@@ -1355,6 +1359,10 @@ int deserialize_major_impl(const uint8_t *bytes, uint64_t len, uint64_t scale, u
   c->n = w5[2];
   c->ilen = w5[3];
   c->dlen = w5[4];
+  if (c->n > BUFF_MAX_ROWS) {
+    rc = BUFF_ENOTSUP;
+    goto done;
+  }
   {
     const uint32_t fl = c->ilen + c->dlen;
     if (fl > 64 || c->dlen > 1000 || fl < 8 || m > fl / 8) {
@@ -1812,7 +1820,7 @@ int encode_rapg_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t fla
   if (!out) return BUFF_EINVAL;
   *out = nullptr;
   if (flags & BUFF_FLAG_INTENDED) return BUFF_ENOTSUP;
-  if (n64 >= (1ull << 32)) return BUFF_EINVAL;
+  if (n64 > BUFF_MAX_ROWS) return BUFF_EINVAL;
   if (n64 > 0 && !values) return BUFF_EINVAL;
   const uint32_t n = (uint32_t)n64;
   const int dl = dlen_of_prec(prec_of_scale(scale));
@@ -2165,6 +2173,10 @@ int buff_rapg_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, ui
     c->ilen = rd32(12);
     c->dlen = rd32(16);
     const uint32_t fl = c->ilen + c->dlen, n = c->n;
+    if (n > BUFF_MAX_ROWS) {
+      rc = BUFF_ENOTSUP;
+      goto done;
+    }
     if (fl > 64) {
       rc = BUFF_ECORRUPT;
       goto done;
@@ -2325,6 +2337,10 @@ int buff_slice_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, u
   c->n = w[2];
   c->ilen = w[3];
   c->dlen = w[4];
+  if (c->n > BUFF_MAX_ROWS) {
+    rc = BUFF_ENOTSUP;
+    goto done;
+  }
   {
     const uint32_t fl = c->ilen + c->dlen;
     if (fl > 64 || c->dlen > 1000) {

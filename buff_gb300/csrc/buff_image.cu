@@ -374,6 +374,10 @@ int parse_header(const uint8_t *image, uint64_t len, uint64_t scale, uint32_t fl
   c->ilen = w[3];
   c->dlen = w[4];
   const uint32_t fl = c->ilen + c->dlen;  // the decoders' `dlen + ilen` (u32)
+  if (c->n > BUFF_MAX_ROWS) {
+    buffh::free_col(c);
+    return BUFF_ENOTSUP;
+  }
   if (fl > 64 || c->dlen > 1000) {
     buffh::free_col(c);
     return BUFF_ECORRUPT;

@@ -66,6 +66,11 @@ extern "C" {
  * the ^0x80 flip of buff_simd256_encode.  Affects buff_serialize and
  * buff_deserialize only; every query returns the same results. */
 #define BUFF_FLAG_BUFF_LAYOUT 0x4u
+/* Largest row count a column may have: the header stores n as u32, and the
+ * library rounds row counts up to whole 512-row steps in 32-bit arithmetic,
+ * so the last 511 values of u32 are refused (encode: BUFF_EINVAL,
+ * deserialize: BUFF_ENOTSUP). */
+#define BUFF_MAX_ROWS 4294966784u
 
 typedef struct buff_col buff_col;
 

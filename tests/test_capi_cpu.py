@@ -83,3 +83,24 @@ def test_product_path_does_not_import_the_oracle():
             if f.endswith((".py", ".cu", ".h", ".cuh", ".cpp")):
                 src = open(os.path.join(dirpath, f)).read()
                 assert "oracle" not in src.replace("oracle.", "").lower() or f == "__init__.py", f
+
+
+def test_row_limit_is_refused_before_any_device_work():
+    """Columns of more than BUFF_MAX_ROWS rows (2^32 - 512) are refused: on
+    encode as EINVAL, from an image header as ENOTSUP."""
+    L = capi.lib()
+    h = C.c_void_p()
+    x = np.zeros(4)
+    assert L.buff_encode_f64(x.ctypes.data, capi.MAX_ROWS + 1, 10000, 0, None,
+                             C.byref(h)) == capi.EINVAL
+    assert L.buff_encode_majority_f64(x.ctypes.data, capi.MAX_ROWS + 1, 10000, 0, None,
+                                      C.byref(h)) == capi.EINVAL
+    hdr = np.zeros(64, dtype=np.uint8)
+    hdr[8:12] = np.frombuffer(np.uint32(0xFFFFFFFF).tobytes(), dtype=np.uint8)
+    hdr[16] = 15
+    for fn in ("buff_deserialize", "buff_slice_deserialize"):
+        assert getattr(L, fn)(hdr.ctypes.data, hdr.size, 10000, 0, None,
+                              C.byref(h)) == capi.ENOTSUP, fn
+    cnt = np.zeros(1, dtype=np.uint64)
+    assert L.buff_filter_image(hdr.ctypes.data, hdr.size, 10000, 0, 0, 1.0, None,
+                               cnt.ctypes.data, None) == capi.ENOTSUP
