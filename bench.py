@@ -1025,7 +1025,23 @@ def main():
         mx = torch.zeros(1, dtype=torch.int64, device="cuda")
         t = time_op(lambda: L.buff_max_async(h, mx.data_ptr(), sh), 10, stream)
         ops["max"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "gb_s_alg": n / t / 1e9}
+        # windowed max (buff_max_range): every 65,536-row window of the column
+        win = 1 << 16
+        wout = torch.empty(n // win + 1, dtype=torch.float64, device="cuda")
+        nwin = np.zeros(1, dtype=np.uint64)
+        t = time_op(lambda: L.buff_max_range(h, 0, n - n % win, win, wout.data_ptr(),
+                                             nwin.ctypes.data, sh), 10, stream)
+        ops["max_range_w65536"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
+                                   "windows": int(nwin[0]), "note": "synchronizes"}
+        del wout
         out = torch.empty(n, dtype=torch.float64, device="cuda")
+        # filter -> materialize (buff_range_filter_decode): the 10 % of rows
+        # above the predicate, decoded into a dense array
+        fd = np.zeros(1, dtype=np.uint64)
+        t = time_op(lambda: L.buff_range_filter_decode(h, pred, words.data_ptr(), out.data_ptr(),
+                                                       fd.ctypes.data, sh), 5, stream)
+        ops["range_0.1_then_decode"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
+                                        "rows_out": int(fd[0]), "note": "synchronizes"}
         t = time_op(lambda: L.buff_decode(h, out.data_ptr(), sh), 5, stream)
         ops["decode_full"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
                               "gb_s_alg": (sum_bytes + 8 * n) / t / 1e9}

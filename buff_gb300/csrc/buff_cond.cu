@@ -172,7 +172,121 @@ __global__ void __launch_bounds__(kThreads) k_max_range(WinArgs a) {
   }
 }
 
-// Window maxima as values.  `shift` drops the right padding of a buff-slice
+// The same maxima for windows of at least 1,024 rows on columns with byte
+// slices, as the progressive max of byte_fixed_max per window, in two
+// passes over 1,024-row chunks (a warp per chunk, a lane per 32-row block;
+// a chunk touches at most two windows).  Pass 1 reads slice 0 only: the
+// largest leading byte of each (chunk, window) part goes to tops[] and is
+// folded into the window's wtop[].  Pass 2 revisits only the parts whose
+// leading byte equals their window's, refines the rows holding it through
+// the later slices and the tail (max_in_block) and folds the code into the
+// window with one atomic.  Rows outside a window read as the zero code.
+
+// This lane's rows of [ra, re) among its 32 rows from row0, and the
+// unflipped slice-0 bytes of those rows (others zero).
+__device__ __forceinline__ uint32_t window_bytes(const Bytes32 &d, uint32_t row0, uint32_t ra,
+                                                 uint32_t re, uint32_t *u) {
+  uint32_t live = 0;
+  if (row0 < re && row0 + 32 > ra) {
+    const uint32_t from = ra > row0 ? ra - row0 : 0u;
+    const uint32_t to = re - row0 < 32 ? re - row0 : 32u;
+    live = (to >= 32 ? 0xFFFFFFFFu : ((1u << to) - 1u)) & ~((1u << from) - 1u);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) u[q] = (d.w[q] ^ H) & expand4((live >> (4 * q)) & 0xFu);
+  return live;
+}
+
+__device__ __forceinline__ Bytes32 chunk_block(const WinArgs &a, uint32_t row0) {
+  Bytes32 d;
+  if (row0 < a.hi && row0 + 32 > a.lo) {
+    d = ld_cand32(a.slices + row0);
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) d.w[q] = H;
+  }
+  return d;
+}
+
+// The window rows [ra, re) of window x.
+__device__ __forceinline__ void window_rows(const WinArgs &a, uint32_t x, uint32_t &ra,
+                                            uint32_t &re) {
+  const uint32_t ws = a.s + x * a.w;
+  const uint64_t we = (uint64_t)ws + a.w;
+  ra = ws > a.lo ? ws : a.lo;
+  re = we < a.hi ? (uint32_t)we : a.hi;
+}
+
+__device__ __forceinline__ void chunk_windows(const WinArgs &a, uint32_t cr0, uint32_t &wa,
+                                              uint32_t &wb) {
+  const uint32_t first = cr0 > a.lo ? cr0 : a.lo;
+  const uint32_t last = cr0 + 1023 < a.hi - 1 ? cr0 + 1023 : a.hi - 1;
+  wa = (first - a.s) / a.w;
+  wb = (last - a.s) / a.w;
+}
+
+__global__ void __launch_bounds__(kThreads) k_max_range_tops(WinArgs a, uint8_t *tops,
+                                                             unsigned int *wtop) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t c0 = a.lo / 1024, c1 = (a.hi - 1) / 1024;
+  for (uint32_t ch = c0 + warp; ch <= c1; ch += nwarps) {
+    const uint32_t cr0 = ch * 1024, row0 = cr0 + lane * 32;
+    const Bytes32 d = chunk_block(a, row0);
+    uint32_t wa, wb;
+    chunk_windows(a, cr0, wa, wb);
+    for (uint32_t x = wa; x <= wb; ++x) {
+      uint32_t ra, re, u[8], mx = 0;
+      window_rows(a, x, ra, re);
+      window_bytes(d, row0, ra, re, u);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) mx = __vmaxu4(mx, u[q]);
+      mx = __vmaxu4(mx, mx >> 16);
+      mx = __vmaxu4(mx, mx >> 8);
+      const uint32_t top = __reduce_max_sync(0xFFFFFFFFu, mx & 0xFFu);
+      if (lane == 0) {
+        tops[2 * (size_t)(ch - c0) + (x - wa)] = (uint8_t)top;
+        atomicMax(wtop + x, top);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_max_range_refine(WinArgs a,
+                                                               const uint8_t *__restrict__ tops,
+                                                               const unsigned int *__restrict__ wtop) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t c0 = a.lo / 1024, c1 = (a.hi - 1) / 1024;
+  for (uint32_t ch = c0 + warp; ch <= c1; ch += nwarps) {
+    const uint32_t cr0 = ch * 1024, row0 = cr0 + lane * 32;
+    uint32_t wa, wb;
+    chunk_windows(a, cr0, wa, wb);
+    bool any = false;
+    for (uint32_t x = wa; x <= wb; ++x)
+      any |= tops[2 * (size_t)(ch - c0) + (x - wa)] == (uint8_t)wtop[x];
+    if (!any) continue;  // no row of this chunk can hold a window's maximum
+    const Bytes32 d = chunk_block(a, row0);
+    for (uint32_t x = wa; x <= wb; ++x) {
+      const uint32_t top = wtop[x];
+      if (tops[2 * (size_t)(ch - c0) + (x - wa)] != (uint8_t)top) continue;
+      uint32_t ra, re, u[8], e[8];
+      window_rows(a, x, ra, re);
+      const uint32_t live = window_bytes(d, row0, ra, re, u);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) e[q] = eqbytes(u[q], top * 0x01010101u);
+      const uint32_t cand = gather32(e) & live;
+      const unsigned long long code =
+          cand ? max_in_block(a.slices, a.stride, a.k, a.tail, a.r, row0, cand, top) : 0ull;
+      const unsigned long long m = warp_max_ull(code);
+      if (lane == 0) atomicMax(a.codes + x, m);
+    }
+  }
+}
+
+// Window maxima as values.  `shift` drops the right padding of a buff-slice// Window maxima as values.  `shift` drops the right padding of a buff-slice
 // code; `empty` marks windows that read no row (f64::min_value()).
 __global__ void k_codes_to_values(const unsigned long long *codes, uint32_t n, long long base,
                                   int dlen, uint32_t shift, uint32_t empty_from, double *out) {
@@ -238,7 +352,24 @@ cudaError_t max_range(const buff_col *c, uint32_t lo, uint32_t hi, uint32_t s, u
   if (hi > lo) {
     const uint64_t steps = (hi - (lo & ~127u) + 127) / 128;
     const int grid = grid_for_items(steps * 32);
-    if (w >= 128)
+    if (w >= 1024 && c->k >= 1) {
+      const uint64_t chunks = (hi - 1) / 1024 - lo / 1024 + 1;
+      uint8_t *tops = nullptr;
+      unsigned int *wtop = nullptr;
+      e = cudaMallocAsync(reinterpret_cast<void **>(&tops), 2 * chunks, st);
+      if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&wtop), sizeof(unsigned int) * nwin, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(wtop, 0, sizeof(unsigned int) * nwin, st);
+      if (e == cudaSuccess) {
+        const int g = grid_for_items(chunks * 32);
+        k_max_range_tops<<<g, kThreads, 0, st>>>(a, tops, wtop);
+        k_max_range_refine<<<g, kThreads, 0, st>>>(a, tops, wtop);
+        count_launch();  // with the one below: two launches
+      }
+      if (tops) cudaFreeAsync(tops, st);
+      if (wtop) cudaFreeAsync(wtop, st);
+      if (e != cudaSuccess) return e;
+    } else if (w >= 128)
       k_max_range<true><<<grid, kThreads, 0, st>>>(a);
     else
       k_max_range<false><<<grid, kThreads, 0, st>>>(a);

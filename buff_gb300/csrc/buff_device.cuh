@@ -291,5 +291,69 @@ __device__ __forceinline__ double i32_to_f64_scaled(int v, int dlen) {
   return __hiloint2double((int)hi, (int)(A << 21));
 }
 
+// Bit i of a 4-bit value -> byte i all ones: x * (1 + 2^7 + 2^14 + 2^21)
+// places bit i at 8i without overlapping carries.
+__device__ __forceinline__ uint32_t expand4(uint32_t x) {
+  return ((x * 0x00204081u) & 0x01010101u) * 0xFFu;
+}
+
+// MSB of every byte of w equal to the byte in every lane of bb.
+__device__ __forceinline__ uint32_t eqbytes(uint32_t w, uint32_t bb) {
+  const uint32_t x = w ^ bb;
+  return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
+}
+
+// Largest full code among rows row0..row0+31 whose leading byte is `top`
+// (bit i of `cand`): every surviving candidate shares the prefix built so
+// far, so one prefix and a candidate mask describe the MSB-first progressive
+// max.  Each later slice is one 32-byte load; the candidates' largest byte
+// and the rows holding it come from per-byte SWAR on the unflipped words.
+// Out of line: it runs for few blocks.
+static __device__ __noinline__ unsigned long long max_in_block(const uint8_t *__restrict__ slices,
+                                                               size_t stride, uint32_t k,
+                                                               const uint8_t *__restrict__ tail,
+                                                               uint32_t r, uint32_t row0,
+                                                               uint32_t cand, uint32_t top) {
+  unsigned long long prefix = top;
+  for (uint32_t s = 1; s < k; ++s) {
+    const Bytes32 b = ld_cand32(slices + s * stride + row0);
+    uint32_t u[8], mx = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      u[q] = (b.w[q] ^ H) & expand4((cand >> (4 * q)) & 0xFu);
+      mx = __vmaxu4(mx, u[q]);
+    }
+    mx = __vmaxu4(mx, mx >> 16);
+    mx = __vmaxu4(mx, mx >> 8);
+    const uint32_t best = mx & 0xFFu;
+    uint32_t e[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) e[q] = eqbytes(u[q], best * 0x01010101u);
+    cand &= gather32(e);
+    prefix = (prefix << 8) | best;
+  }
+  if (!r) return prefix;
+  // 32 rows of r bits = r words at byte (row0 / 32) * 4r
+  const uint32_t *tp = reinterpret_cast<const uint32_t *>(tail + (size_t)(row0 >> 5) * 4 * r);
+  uint32_t tw[8];
+#pragma unroll
+  for (int i = 0; i < 7; ++i) tw[i] = (uint32_t)i < r ? __ldg(tp + i) : 0u;
+  tw[7] = 0;
+  uint32_t bt = 0;
+  for (uint32_t c = cand; c; c &= c - 1) {
+    const uint32_t i = __ffs(c) - 1;
+    const uint32_t bit = i * r, wi = bit >> 5;
+    uint32_t w0 = tw[0], w1 = tw[1];
+#pragma unroll
+    for (uint32_t j = 1; j < 7; ++j)
+      if (wi == j) {
+        w0 = tw[j];
+        w1 = tw[j + 1];
+      }
+    bt = max(bt, __funnelshift_r(w0, w1, bit & 31) & ((1u << r) - 1u));
+  }
+  return (prefix << r) | bt;
+}
+
 }  // namespace dev
 }  // namespace buffk

@@ -152,7 +152,8 @@ def test_max_range(oracle, gpu, case):
     col = Column.encode(x, scale)
     n = x.size
     fl = oracle.header(img).fixed_len
-    for s, w in ((0, 1000), (13, 128), (5, 3), (0, 1), (100, 4096), (0, n // 3), (31, 200)):
+    for s, w in ((0, 1000), (13, 128), (5, 3), (0, 1), (100, 4096), (0, n // 3), (31, 200),
+                 (0, 1024), (7, 1500), (1000, 5000), (33, 2048)):
         if w == 0 or s + w > n:
             continue
         e = s + (n - s) // w * w
@@ -172,6 +173,11 @@ def test_max_range(oracle, gpu, case):
     got = ci.max_range(3, e, 100)
     exp = np.array([full[a:min(a + 100, e)].max() for a in range(3, e, 100)])
     assert np.array_equal(got, exp)
+    if n > 4000:  # windows of >= 1,024 rows, the last one ragged
+        e2 = n - 17
+        got = ci.max_range(5, e2, 1700)
+        exp = np.array([full[a:min(a + 1700, e2)].max() for a in range(5, e2, 1700)])
+        assert np.array_equal(got, exp)
 
 
 @pytest.mark.parametrize("kind", ["none", "one"])
