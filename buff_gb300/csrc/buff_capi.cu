@@ -785,7 +785,6 @@ int decode_words_impl(const buff_col *c, const uint32_t *dwords, double *out, ui
                       int tail_shift, cudaStream_t s) {
   int rc = BUFF_OK;
   const uint32_t n = c->n;
-  const size_t nw = ((size_t)n + 31) / 32;
   uint32_t *rank = nullptr;
   uint32_t tailw[2] = {0, 0};
   uint64_t cnt = 0;
@@ -795,14 +794,13 @@ int decode_words_impl(const buff_col *c, const uint32_t *dwords, double *out, ui
     if (count) *count = 0;
     return BUFF_OK;
   }
-  CK(scratch(&rank, nw + 1, s));
-  CK(buffk::word_ranks(dwords, nw, rank, s));
-  CK(cudaMemcpyAsync(&tailw[0], rank + nw - 1, 4, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&tailw[1], dwords + nw - 1, 4, cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
   {
-    const uint32_t valid = (n & 31) ? ((1u << (n & 31)) - 1u) : 0xFFFFFFFFu;
-    cnt = (uint64_t)tailw[0] + (uint64_t)__builtin_popcount(tailw[1] & valid);
+    const size_t nsteps = ((size_t)n + 127) / 128;
+    CK(scratch(&rank, nsteps + 1, s));
+    CK(buffk::step_ranks(dwords, n, rank, s));
+    CK(cudaMemcpyAsync(&tailw[0], rank + nsteps, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    cnt = tailw[0];
   }
   if (count) *count = cnt;
   if (out && cnt) {

@@ -4,11 +4,12 @@
 //
 // The reference walks each slice once per listed row with the BitPack
 // reader; here every selected row is rebuilt independently from its k slice
-// bytes and its packed tail field.  For the bitmap form one thread owns one
-// row, so a warp covers one 32-row bitmap word and its slice reads coalesce;
-// the output slot of a row is the prefix count of set bits before its word
-// plus the set bits below it in the word.
+// bytes and its packed tail field.  For the bitmap form a lane owns 4
+// consecutive rows, so a warp covers four 32-row bitmap words and its slice
+// reads coalesce; the output slot of a row is the prefix count of set bits
+// before its word plus the set bits below it in the word.
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <stdint.h>
 
 #include "buff_device.cuh"
@@ -60,16 +61,105 @@ __global__ void __launch_bounds__(kThreads) k_decode_list(RowArgs a, const uint3
     a.out[i] = row_value(a, rows[i]);
 }
 
-__global__ void __launch_bounds__(kThreads) k_decode_words(RowArgs a, const uint32_t *__restrict__ words,
-                                                           const uint32_t *__restrict__ rank) {
+// The bitmap form with 4 rows per lane: a warp covers 128 rows (4 bitmap
+// words) per step and takes kDecSteps steps per iteration, their bitmap
+// words loaded together so that sparse selections skip empty steps
+// kDecSteps at a time; a step's first output slot is its entry of `rank`
+// (selected rows before the step), a lane's place within it a warp scan.  For a step with selected rows each lane reads
+// its 4 rows of every slice with one 4-byte load (128 bytes per warp
+// request) and their 4 tail fields from at most 5 tail bytes, and writes the
+// selected values to their slots.  N32: every base + code fits in 32 bits
+// (the exact 32-bit conversion).
+constexpr uint32_t kDecSteps = 4;
+
+template <bool N32>
+__global__ void __launch_bounds__(kThreads) k_decode_words4(RowArgs a, const uint32_t *__restrict__ words,
+                                                            const uint32_t *__restrict__ rank) {
   const uint32_t lane = threadIdx.x & 31;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < a.n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t w = i >> 5;
-    const uint32_t b = __ldg(words + w);
-    if (!(b >> lane & 1u)) continue;
-    const uint32_t at = __ldg(rank + w) + __popc(b & ((1u << lane) - 1u));
-    a.out[at] = row_value(a, (uint32_t)i);
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t nsteps = (uint32_t)(((uint64_t)a.n + 127) / 128);
+  const uint32_t rmask = a.r ? ((1u << a.r) - 1u) : 0u;
+  for (uint32_t st0 = warp * kDecSteps; st0 < nsteps; st0 += nwarps * kDecSteps) {
+    uint32_t word[kDecSteps], nib[kDecSteps], any = 0;
+#pragma unroll
+    for (uint32_t u = 0; u < kDecSteps; ++u) {
+      const uint32_t row0 = (st0 + u) * 128 + lane * 4;
+      word[u] = (st0 + u < nsteps && row0 < a.n) ? __ldg(words + (row0 >> 5)) : 0u;
+      nib[u] = (word[u] >> (row0 & 31)) & 0xFu;
+      if (row0 + 4 > a.n) nib[u] &= row0 < a.n ? (1u << (a.n - row0)) - 1u : 0u;  // rows past n
+      any |= nib[u];
+    }
+    if (!__any_sync(0xFFFFFFFFu, any != 0)) continue;
+    // each lane's place among the selected rows of its step (lanes in row order)
+    uint32_t excl[kDecSteps];
+#pragma unroll
+    for (uint32_t u = 0; u < kDecSteps; ++u) {
+      const uint32_t cl = __popc(nib[u]);
+      uint32_t incl = cl;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+      }
+      excl[u] = incl - cl;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < kDecSteps; ++u) {
+      if (!nib[u]) continue;
+      const uint32_t row0 = (st0 + u) * 128 + lane * 4;
+      unsigned long long c[4] = {0, 0, 0, 0};
+      for (uint32_t j = 0; j < a.k; ++j) {
+        const uint32_t x =
+            __ldg(reinterpret_cast<const uint32_t *>(a.slices + (size_t)j * a.stride + row0)) ^
+            0x80808080u;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) c[i] = (c[i] << 8) | ((x >> (8 * i)) & 0xFFu);
+      }
+      if (a.r) {
+        // fields of rows row0..row0+3: bits row0*r .. +4r (4r <= 28) of the tail
+        const unsigned long long bit = (unsigned long long)row0 * a.r;
+        const uint8_t *tb = a.tail + (bit >> 3);
+        const uint32_t nb = (uint32_t)(((bit & 7) + 4 * a.r + 7) >> 3);  // <= 5
+        unsigned long long f = 0;
+        for (uint32_t b = 0; b < nb; ++b) f |= (unsigned long long)__ldg(tb + b) << (8 * b);
+        f >>= (bit & 7);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const unsigned long long t = (f >> (i * a.r)) & rmask;
+          if (a.k == 0)
+            c[i] = t;
+          else
+            c[i] = (c[i] << a.r) | (a.tail_shift ? (t << a.r) : t);
+        }
+      }
+      uint32_t at = __ldg(rank + st0 + u) + excl[u];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (nib[u] >> i & 1u)
+          a.out[at++] = N32 ? i32_to_f64_scaled((int)((uint32_t)a.base + (uint32_t)c[i]), a.dlen)
+                            : i64_to_f64_scaled((long long)((unsigned long long)a.base + c[i]),
+                                                a.dlen);
+    }
+  }
+}
+
+// Selected rows of each 128-row step (rows below n only), for step_ranks.
+__global__ void k_step_popc(const uint32_t *__restrict__ words, uint32_t n, uint32_t nsteps,
+                            uint32_t *cnt) {
+  const uint32_t nw = (uint32_t)(((uint64_t)n + 31) / 32);
+  for (uint32_t st = blockIdx.x * blockDim.x + threadIdx.x; st < nsteps;
+       st += gridDim.x * blockDim.x) {
+    uint32_t c = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < 4; ++i) {
+      const uint32_t w = st * 4 + i;
+      if (w >= nw) break;
+      uint32_t b = __ldg(words + w);
+      if (w == nw - 1 && (n & 31)) b &= (1u << (n & 31)) - 1u;
+      c += __popc(b);
+    }
+    cnt[st] = c;
   }
 }
 
@@ -327,10 +417,33 @@ cudaError_t decode_rows(const buff_col *c, const uint32_t *rows, uint64_t nrows,
     k_decode_list<<<grid_for_items(nrows), kThreads, 0, s>>>(a, rows, nrows);
   } else {
     if (!c->n) return cudaSuccess;
-    k_decode_words<<<grid_for_items(c->n), kThreads, 0, s>>>(a, words, rank);
+    // every value base + code in 32 bits: the exact 32-bit conversion
+    const uint32_t bits = 8 * a.k + a.r + (tail_shift && a.k && a.r ? a.r : 0u);
+    const long long maxc = bits >= 63 ? -1 : (long long)((1ull << bits) - 1ull);
+    const bool n32 = bits <= 32 && c->base >= INT32_MIN && maxc >= 0 &&
+                     c->base + maxc <= (long long)INT32_MAX;
+    const int g = grid_for_items(((uint64_t)c->n + 3) / 4);
+    if (n32)
+      k_decode_words4<true><<<g, kThreads, 0, s>>>(a, words, rank);
+    else
+      k_decode_words4<false><<<g, kThreads, 0, s>>>(a, words, rank);
   }
   count_launch();
   return cudaGetLastError();
+}
+
+cudaError_t step_ranks(const uint32_t *words, uint32_t n, uint32_t *rank, cudaStream_t s) {
+  const uint32_t nsteps = (uint32_t)(((uint64_t)n + 127) / 128);
+  if (!nsteps) return cudaMemsetAsync(rank, 0, sizeof(uint32_t), s);
+  uint32_t *tmp = nullptr;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&tmp),
+                                  sizeof(uint32_t) * exclusive_scan_tmp(nsteps), s);
+  if (e != cudaSuccess) return e;
+  k_step_popc<<<grid_for_items(nsteps), kThreads, 0, s>>>(words, n, nsteps, rank);
+  count_launch();
+  e = exclusive_scan(rank, nsteps, tmp, s);  // rank[nsteps] = the total
+  cudaFreeAsync(tmp, s);
+  return e;
 }
 
 cudaError_t max_range(const buff_col *c, uint32_t lo, uint32_t hi, uint32_t s, uint32_t w,

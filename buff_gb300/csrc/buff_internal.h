@@ -153,6 +153,13 @@ cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, 
                          uint32_t *words, unsigned long long *count, cudaStream_t s,
                          const uint32_t *cand = nullptr);
 cudaError_t word_ranks(const uint32_t *words, size_t nw, uint32_t *rank, cudaStream_t s);
+// Exclusive scan of `count` u32 in place (data holds count + 1; data[count]
+// receives the total), with exclusive_scan_tmp(count) u32 of device scratch.
+size_t exclusive_scan_tmp(size_t count);
+cudaError_t exclusive_scan(uint32_t *data, size_t count, uint32_t *tmp, cudaStream_t s);
+// Selected rows before each 128-row step of a bitmap over n rows (bits of
+// rows >= n ignored): rank holds ceil(n/128) + 1 u32, the last the total.
+cudaError_t step_ranks(const uint32_t *words, uint32_t n, uint32_t *rank, cudaStream_t s);
 cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out,
                           cudaStream_t s);
 // buff_max_majority's progressive max on the device: cand (nwp words) ends
@@ -174,7 +181,7 @@ cudaError_t field_sum(const uint8_t *p, uint64_t bit0, uint32_t width, uint32_t 
                       unsigned long long *out, cudaStream_t s);
 
 // Row-conditioned decode (buff_cond.cu): rows from a list (rows != null,
-// nrows entries) or from a bitmap with its word ranks (word_ranks).
+// nrows entries) or from a bitmap with its step ranks (step_ranks).
 // tail_shift: 1 ORs the packed tail shifted by r (buff_decode_condition).
 cudaError_t decode_rows(const buff_col *c, const uint32_t *rows, uint64_t nrows,
                         const uint32_t *words, const uint32_t *rank, int tail_shift, double *out,

@@ -145,6 +145,8 @@ __global__ void k_scan_add(uint32_t *data, size_t count, const uint32_t *totals)
   if (i < count) data[i] += totals[i / kScanItems];
 }
 
+size_t scan_blocks(size_t count) { return (count + kScanItems - 1) / kScanItems; }
+
 cudaError_t scan_exclusive(uint32_t *data, size_t count, uint32_t *tmp, cudaStream_t s) {
   const uint32_t nb = (uint32_t)((count + kScanItems - 1) / kScanItems);
   k_scan_local<<<nb, kScanThreads, 0, s>>>(data, count, tmp);
@@ -895,6 +897,13 @@ int grid_of(size_t items, int threads) {
 }
 
 }  // namespace
+
+// Exclusive scan of `count` u32 in place; data[count] receives the total.
+// tmp: exclusive_scan_tmp(count) u32 of device scratch.
+size_t exclusive_scan_tmp(size_t count) { return scan_blocks(count) + 1; }
+cudaError_t exclusive_scan(uint32_t *data, size_t count, uint32_t *tmp, cudaStream_t s) {
+  return scan_exclusive(data, count, tmp, s);
+}
 
 // ================================================================ host side
 
