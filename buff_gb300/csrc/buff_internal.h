@@ -152,7 +152,6 @@ cudaError_t flip_bytes(uint8_t *p, size_t nbytes, cudaStream_t s);
 cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, uint32_t ttail,
                          uint32_t *words, unsigned long long *count, cudaStream_t s,
                          const uint32_t *cand = nullptr);
-cudaError_t word_ranks(const uint32_t *words, size_t nw, uint32_t *rank, cudaStream_t s);
 // Exclusive scan of `count` u32 in place (data holds count + 1; data[count]
 // receives the total), with exclusive_scan_tmp(count) u32 of device scratch.
 size_t exclusive_scan_tmp(size_t count);

@@ -1030,22 +1030,6 @@ cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, 
 
 // Exclusive prefix counts of set bits per word (rank[0..nw), total at
 // rank[nw]); rank needs nw + 1 entries.
-cudaError_t word_ranks(const uint32_t *words, size_t nw, uint32_t *rank, cudaStream_t s) {
-  uint32_t *tmp = nullptr;
-  const size_t nb = (nw + kScanItems - 1) / kScanItems + 1;
-  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&tmp), sizeof(uint32_t) * nb, s);
-  if (e != cudaSuccess) return e;
-  if (nw) {
-    k_word_popc<<<grid_of(nw, 256), 256, 0, s>>>(words, nw, rank);
-    count_launch();
-    e = scan_exclusive(rank, nw, tmp, s);
-  } else {
-    e = cudaMemsetAsync(rank, 0, sizeof(uint32_t), s);
-  }
-  cudaFreeAsync(tmp, s);
-  return e;
-}
-
 cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out, cudaStream_t s) {
   k_bytesum<<<grid_of(nbytes, 256), 256, 0, s>>>(p, nbytes, out);
   count_launch();
