@@ -278,6 +278,15 @@ __device__ __forceinline__ double i64_to_f64_scaled(long long v, int dlen) {
 }
 
 
+// The same for 0 <= a < 2^53 (exact): the leading one placed at bit 52 and
+// the exponent added on top of it, without sign handling or rounding.
+__device__ __forceinline__ double u53_to_f64_scaled(unsigned long long a, int dlen) {
+  if (a == 0) return 0.0;
+  const int e = 63 - __clzll(a);
+  return __longlong_as_double(
+      (long long)((a << (52 - e)) + ((unsigned long long)(e - dlen + 1022) << 52)));
+}
+
 // The same for a value that fits in 32 bits: exact (|v| < 2^32 <= 2^53), so
 // only the leading one is found and the significand placed -- a third of the
 // 64-bit path's integer instructions.

@@ -714,7 +714,7 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a)
 // output is 32-byte aligned (ST32), else in two 16-byte stores.  Merging the
 // outlier rows into this pass was measured slower: with 1 % outliers most
 // warps then wait on a dependent rank-and-byte load in most steps.
-template <int KS, bool N32, bool ST32>
+template <int KS, bool N32, bool ST32, bool POS = false>
 __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast4(RapgDecodeArgs a) {
   static_assert(KS >= 1 && KS <= 4, "k_rapg_decode_fast4 transposes at most 4 slices");
   using CodeT = typename std::conditional<N32, uint32_t, unsigned long long>::type;
@@ -768,6 +768,8 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast4(RapgDecodeArgs a
         code |= (CodeT)a.sdef;
         if (N32)
           v[i] = i32_to_f64_scaled((int)((uint32_t)a.base + (uint32_t)code), a.dlen);
+        else if (POS)
+          v[i] = u53_to_f64_scaled((unsigned long long)a.base + code, a.dlen);
         else
           v[i] = i64_to_f64_scaled((long long)((unsigned long long)a.base + code), a.dlen);
       }
@@ -1122,7 +1124,14 @@ static void launch_fast_ks(const RapgDecodeArgs &a, int g, cudaStream_t s) {
 
 template <int KS, bool N32>
 static void launch_fast4(const RapgDecodeArgs &a, int g, cudaStream_t s) {
-  if ((reinterpret_cast<uintptr_t>(a.out) & 31u) == 0)
+  const bool st32 = (reinterpret_cast<uintptr_t>(a.out) & 31u) == 0;
+  // every base + code in [0, 2^53): the unsigned exact conversion
+  const bool pos = !N32 && a.base >= 0 && a.R <= 52 &&
+                   (unsigned long long)a.base < (1ull << 53) - (1ull << a.R);
+  if (pos)
+    st32 ? k_rapg_decode_fast4<KS, false, true, true><<<g, kThreads, 0, s>>>(a)
+         : k_rapg_decode_fast4<KS, false, false, true><<<g, kThreads, 0, s>>>(a);
+  else if (st32)
     k_rapg_decode_fast4<KS, N32, true><<<g, kThreads, 0, s>>>(a);
   else
     k_rapg_decode_fast4<KS, N32, false><<<g, kThreads, 0, s>>>(a);
