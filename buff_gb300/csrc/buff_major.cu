@@ -172,13 +172,17 @@ __global__ void k_major_compact(const uint8_t *__restrict__ lead, const uint32_t
   }
 }
 
-// 1 + the last outlier row of a sparse column (0 when it has none).
+// 1 + the last outlier row of a sparse column (0 when it has none): each
+// thread keeps its own maximum, one atomic per warp.
 __global__ void k_major_last(const uint32_t *__restrict__ bits, size_t nwp, uint32_t *last) {
+  uint32_t best = 0;
   for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nwp;
        w += (size_t)gridDim.x * blockDim.x) {
     const uint32_t b = bits[w];
-    if (b) atomicMax(last, (uint32_t)(w * 32) + (31 - __clz(b)) + 1);
+    if (b) best = max(best, (uint32_t)(w * 32) + (31 - __clz(b)) + 1);
   }
+  best = __reduce_max_sync(0xFFFFFFFFu, best);
+  if ((threadIdx.x & 31) == 0 && best) atomicMax(last, best);
 }
 
 // ---------------------------------------------------------------- filters
