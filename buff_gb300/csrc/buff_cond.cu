@@ -72,9 +72,12 @@ __global__ void __launch_bounds__(kThreads) k_decode_list(RowArgs a, const uint3
 // (the exact 32-bit conversion).
 constexpr uint32_t kDecSteps = 4;
 
-template <bool N32>
+template <bool N32, int KS>
 __global__ void __launch_bounds__(kThreads) k_decode_words4(RowArgs a, const uint32_t *__restrict__ words,
                                                             const uint32_t *__restrict__ rank) {
+  // KS > 0: the slice count is a constant, so every step's slice words are
+  // loaded together before any is used; KS == 0: a.k slices, loaded in turn
+  const uint32_t ks = KS > 0 ? (uint32_t)KS : a.k;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -104,26 +107,48 @@ __global__ void __launch_bounds__(kThreads) k_decode_words4(RowArgs a, const uin
       }
       excl[u] = incl - cl;
     }
+    constexpr int KL = KS > 0 ? KS : 1;
+    uint32_t xs[kDecSteps][KL];
+    // the 5 tail bytes holding each step's 4 fields (the tail buffer is padded
+    // past its last row), loaded with the slices
+    unsigned long long tf[kDecSteps];
+#pragma unroll
+    for (uint32_t u = 0; u < kDecSteps; ++u) {
+      tf[u] = 0;
+      if (a.r && nib[u]) {
+        const unsigned long long bit = (unsigned long long)((st0 + u) * 128 + lane * 4) * a.r;
+        const uint8_t *tb = a.tail + (bit >> 3);
+#pragma unroll
+        for (int b = 0; b < 5; ++b) tf[u] |= (unsigned long long)__ldg(tb + b) << (8 * b);
+        tf[u] >>= (bit & 7);
+      }
+    }
+    if (KS > 0) {
+#pragma unroll
+      for (uint32_t u = 0; u < kDecSteps; ++u)
+#pragma unroll
+        for (int j = 0; j < KL; ++j)
+          xs[u][j] = nib[u] ? __ldg(reinterpret_cast<const uint32_t *>(
+                                  a.slices + (size_t)j * a.stride + (st0 + u) * 128 + lane * 4))
+                            : 0u;
+    }
 #pragma unroll
     for (uint32_t u = 0; u < kDecSteps; ++u) {
       if (!nib[u]) continue;
       const uint32_t row0 = (st0 + u) * 128 + lane * 4;
       unsigned long long c[4] = {0, 0, 0, 0};
-      for (uint32_t j = 0; j < a.k; ++j) {
+      for (uint32_t j = 0; j < ks; ++j) {
         const uint32_t x =
-            __ldg(reinterpret_cast<const uint32_t *>(a.slices + (size_t)j * a.stride + row0)) ^
+            (KS > 0 ? xs[u][j < (uint32_t)KL ? j : 0]
+                    : __ldg(reinterpret_cast<const uint32_t *>(a.slices + (size_t)j * a.stride +
+                                                               row0))) ^
             0x80808080u;
 #pragma unroll
         for (int i = 0; i < 4; ++i) c[i] = (c[i] << 8) | ((x >> (8 * i)) & 0xFFu);
       }
       if (a.r) {
         // fields of rows row0..row0+3: bits row0*r .. +4r (4r <= 28) of the tail
-        const unsigned long long bit = (unsigned long long)row0 * a.r;
-        const uint8_t *tb = a.tail + (bit >> 3);
-        const uint32_t nb = (uint32_t)(((bit & 7) + 4 * a.r + 7) >> 3);  // <= 5
-        unsigned long long f = 0;
-        for (uint32_t b = 0; b < nb; ++b) f |= (unsigned long long)__ldg(tb + b) << (8 * b);
-        f >>= (bit & 7);
+        const unsigned long long f = tf[u];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const unsigned long long t = (f >> (i * a.r)) & rmask;
@@ -423,10 +448,17 @@ cudaError_t decode_rows(const buff_col *c, const uint32_t *rows, uint64_t nrows,
     const bool n32 = bits <= 32 && c->base >= INT32_MIN && maxc >= 0 &&
                      c->base + maxc <= (long long)INT32_MAX;
     const int g = grid_for_items(((uint64_t)c->n + 3) / 4);
-    if (n32)
-      k_decode_words4<true><<<g, kThreads, 0, s>>>(a, words, rank);
-    else
-      k_decode_words4<false><<<g, kThreads, 0, s>>>(a, words, rank);
+#define DW4(KSV)                                                           \
+  (n32 ? k_decode_words4<true, KSV><<<g, kThreads, 0, s>>>(a, words, rank) \
+       : k_decode_words4<false, KSV><<<g, kThreads, 0, s>>>(a, words, rank))
+    switch (a.k) {
+      case 1: DW4(1); break;
+      case 2: DW4(2); break;
+      case 3: DW4(3); break;
+      case 4: DW4(4); break;
+      default: DW4(0); break;
+    }
+#undef DW4
   }
   count_launch();
   return cudaGetLastError();
