@@ -1022,14 +1022,22 @@ int buff_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, uint32_
       goto done;
     }
     if ((rc = alloc_col(c, s))) goto done;
-    if (c->k && c->n)
-      CK(cudaMemcpy2DAsync(c->slices, c->stride, bytes + 20, c->n, c->n, c->k, cudaMemcpyDefault,
-                           s));
-    if (c->k && c->n && (flags & BUFF_FLAG_BUFF_LAYOUT))
-      CK(buffk::flip_bytes(c->slices, (size_t)c->k * c->stride, s));
-    // padding rows of every slice hold the flipped zero byte (what encode writes)
-    if (c->k && c->stride > c->n)
-      CK(cudaMemset2DAsync(c->slices + c->n, c->stride, 0x80, c->stride - c->n, c->k, s));
+    cudaError_t ue = cudaSuccess;
+    if (!dev && buffk::upload_slices(bytes, c,
+                                     (flags & BUFF_FLAG_BUFF_LAYOUT) ? 0x80808080u : 0u, s,
+                                     &ue)) {
+      // slices read in place by the device, flipped and padded on the way
+      CK(ue);
+    } else {
+      if (c->k && c->n)
+        CK(cudaMemcpy2DAsync(c->slices, c->stride, bytes + 20, c->n, c->n, c->k,
+                             cudaMemcpyDefault, s));
+      if (c->k && c->n && (flags & BUFF_FLAG_BUFF_LAYOUT))
+        CK(buffk::flip_bytes(c->slices, (size_t)c->k * c->stride, s));
+      // padding rows of every slice hold the flipped zero byte (what encode writes)
+      if (c->k && c->stride > c->n)
+        CK(cudaMemset2DAsync(c->slices + c->n, c->stride, 0x80, c->stride - c->n, c->k, s));
+    }
     CK(cudaMemsetAsync(c->tail, 0, c->tail_alloc, s));
     if (c->tail_bytes)
       CK(cudaMemcpyAsync(c->tail, bytes + 20 + (uint64_t)c->k * c->n, c->tail_bytes,

@@ -335,6 +335,50 @@ __global__ void __launch_bounds__(kImgThreads) k_filter_image(ImgFilterArgs a) {
   if (lane == 0 && cv && a.count) atomicAdd(a.count, cv);
 }
 
+// The slices of a serialized image copied into a column's aligned slices
+// (buff_deserialize from host memory the device can reach): a CTA stages one
+// 4,096-row chunk of one slice with aligned 16-byte loads, then writes it to
+// slice j at j * stride with 16-byte stores (XOR flipx: the buff layout's
+// unflipped bytes become flipped), rows from n to the end of the chunk
+// holding the flipped zero byte.  Each image byte crosses the host link
+// once and lands in place, where a pitched copy engine transfer runs
+// slower.
+__global__ void __launch_bounds__(kImgThreads) k_upload_slices(const uint8_t *slices, uint32_t n,
+                                                               uint32_t k, size_t stride,
+                                                               uint32_t flipx, uint8_t *dst) {
+  __shared__ __align__(16) uint8_t sm[kRegion + 16];
+  const uint32_t tid = threadIdx.x;
+  const uint32_t nchunks = (uint32_t)((stride + kImgRows - 1) / kImgRows);
+  for (uint64_t it = blockIdx.x; it < (uint64_t)nchunks * k; it += gridDim.x) {
+    const uint32_t j = (uint32_t)(it / nchunks), c = (uint32_t)(it % nchunks);
+    const uint32_t r0 = c * kImgRows;
+    const uint32_t rows = r0 < n ? (n - r0 < kImgRows ? n - r0 : kImgRows) : 0u;
+    const uint32_t span = (uint32_t)(stride - r0 < kImgRows ? stride - r0 : kImgRows);
+    __syncthreads();
+    const uint32_t m = rows ? stage(sm, slices + (size_t)j * n + r0, rows) : 0u;
+    __syncthreads();
+    uint8_t *out = dst + (size_t)j * stride + r0;
+    for (uint32_t v = tid; v * 16 < span; v += kImgThreads) {
+      const uint32_t o = v * 16;
+      uint32_t w[4];
+      const uint32_t *x = reinterpret_cast<const uint32_t *>(sm) + ((m + o) >> 2);
+      const uint32_t sh = ((m + o) & 3u) * 8u;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        w[q] = __funnelshift_r(x[q], x[q + 1], sh) ^ flipx;
+        // rows past n: the flipped zero byte
+        const uint32_t row = o + 4 * q;
+        if (row + 4 > rows) {
+#pragma unroll
+          for (int b = 0; b < 4; ++b)
+            if (row + b >= rows) w[q] = (w[q] & ~(0xFFu << (8 * b))) | (0x80u << (8 * b));
+        }
+      }
+      *reinterpret_cast<uint4 *>(out + o) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+}
+
 inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // A device-accessible address for `p`: device memory as is, pinned host
@@ -593,3 +637,26 @@ extern "C" int buff_range_filter_sum_image(const uint8_t *image, uint64_t len, u
   buffh::free_col(c);
   return rc;
 }
+
+namespace buffk {
+// Copies the k slices of a serialized image (image + 20, slice j at j * n;
+// host or device memory) into c->slices through k_upload_slices when the
+// device can read the image in place; returns false (nothing done) when it
+// cannot, so the caller uses a pitched copy.
+bool upload_slices(const uint8_t *image, buff_col *c, uint32_t flipx, cudaStream_t s,
+                   cudaError_t *err) {
+  const uint8_t *img = static_cast<const uint8_t *>(device_view(image, c->device));
+  if (!img || !c->k || !c->n) return false;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_upload_slices, kImgThreads, 0);
+  if (per_sm < 1) per_sm = 1;
+  const uint64_t items = (uint64_t)c->k * ((c->stride + kImgRows - 1) / kImgRows);
+  uint64_t grid = (uint64_t)per_sm * num_sms(c->device);
+  if (grid > items) grid = items;
+  k_upload_slices<<<(unsigned)grid, kImgThreads, 0, s>>>(img + 20, c->n, c->k, c->stride, flipx,
+                                                        c->slices);
+  count_launch();
+  *err = cudaGetLastError();
+  return true;
+}
+}  // namespace buffk

@@ -147,6 +147,11 @@ cudaError_t launch_decode(const buff_col *c, uint32_t total, int intended_mask, 
 cudaError_t major_build_sparse(buff_col *c, const uint8_t *lead, cudaStream_t s);
 cudaError_t major_index(buff_col *c, cudaStream_t s);
 cudaError_t flip_bytes(uint8_t *p, size_t nbytes, cudaStream_t s);
+// The k slices of a serialized image into c->slices (flipped; padding rows
+// 0x80) read in place by the device; false when the device cannot reach the
+// image (nothing launched).  flipx = 0x80808080 for the buff layout.
+bool upload_slices(const uint8_t *image, buff_col *c, uint32_t flipx, cudaStream_t s,
+                   cudaError_t *err);
 // Filters of the buff-major layout; with m == 0 the same compare runs over a
 // plain column's slices and tail.  cand (may be null) restricts the rows.
 cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, uint32_t ttail,
