@@ -2359,11 +2359,16 @@ int buff_slice_deserialize(const uint8_t *bytes, uint64_t len, uint64_t scale, u
       goto done;
     }
     if ((rc = alloc_col(c, s))) goto done;
-    if (c->n)
-      CK(cudaMemcpy2DAsync(c->slices, c->stride, bytes + 20, c->n, c->n, c->k, cudaMemcpyDefault,
-                           s));
-    if (c->stride > c->n)
-      CK(cudaMemset2DAsync(c->slices + c->n, c->stride, 0x80, c->stride - c->n, c->k, s));
+    cudaError_t ue = cudaSuccess;
+    if (!dev && buffk::upload_slices(bytes, c, 0u, s, &ue)) {
+      CK(ue);  // slices read in place by the device, padding rows on the way
+    } else {
+      if (c->n)
+        CK(cudaMemcpy2DAsync(c->slices, c->stride, bytes + 20, c->n, c->n, c->k,
+                             cudaMemcpyDefault, s));
+      if (c->stride > c->n)
+        CK(cudaMemset2DAsync(c->slices + c->n, c->stride, 0x80, c->stride - c->n, c->k, s));
+    }
     CK(cudaMemsetAsync(c->tail, 0, c->tail_alloc, s));
     if (!dev) CK(cudaStreamSynchronize(s));
   }
