@@ -6,6 +6,14 @@
  * function cites the reference file:line it follows.  Integer behaviour of the
  * reference's release build is kept: i64/u32 arithmetic wraps, shift amounts
  * are masked to the operand width, f64->int casts saturate.
+ *
+ * Pinning: checked against every known-answer test the reference carries for
+ * this path (BitPack, BitVec serialization, BVIter order, the movemask lane
+ * order; tests/test_oracle_golden.py).  The codec outputs themselves (encoded
+ * bytes, bitmaps, sums, maxima, precision decodes) are parity unpinned: no
+ * reference test or recorded output asserts them, and the reference (a Rust
+ * crate) cannot be built here; they are cross-checked against an independent
+ * numpy statement (tests/model.py).
  */
 #include "buff_oracle.h"
 
