@@ -8,14 +8,13 @@
 // outputs are host memory; this variant uses a fixed scratch array that lives
 // in the library's device image instead.
 //
-// The scratch array below is part of this library's device code, so every GPU
-// on which the library is loaded holds it (about 8 MiB) until the process
-// exits.  All calls share it: two calls whose work overlaps on the GPU (for
-// example on two streams) race on it, so callers must order them.
+// The scratch array below is part of this library's device code.  CUDA loads
+// device code lazily, so a device reserves the array (about 8 MiB) the first
+// time this entry point runs on it, and holds it until the process exits.  All
+// calls share it: two calls whose work overlaps on the GPU (for example on two
+// streams) race on it, so callers must order them.
 #include <cuda_runtime.h>
 #include <stdint.h>
-#include <string.h>
-
 #include <mutex>
 
 #include "buff_internal.h"
@@ -39,23 +38,13 @@ int scratch_address(int device, uint32_t **out) {
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
       cudaGetLastError();
-      return BUFF_ECUDA;
+      // the lookup loads this file's device code, which reserves the array
+      return e == cudaErrorMemoryAllocation ? BUFF_ENOMEM : BUFF_ECUDA;
     }
     g_addr[device] = static_cast<uint32_t *>(p);
   }
   *out = g_addr[device];
   return BUFF_OK;
-}
-
-int64_t fetch_fixed(double v, int pexp, uint32_t dlen) {
-  uint64_t b;
-  memcpy(&b, &v, 8);
-  const int exp = (int)((b >> 52) & 0x7FF) - 1023;
-  if (exp < pexp) return 0;
-  const int sh = 63 - exp - (int)dlen;
-  uint64_t f = ((b << 11) | 0x8000000000000000ull) >> (sh & 63);
-  if (b >> 63) f = ~(f - 1);
-  return (int64_t)f;
 }
 
 }  // namespace
@@ -73,38 +62,25 @@ extern "C" int buff_range_filter_noalloc(const buff_col *c, double pred, uint32_
   if (rc != BUFF_OK) return rc;
   const uint32_t n = c->n, nw = (n + 31) / 32;
   unsigned long long *dcount = reinterpret_cast<unsigned long long *>(scratch + kNoallocWords);
-  if (n == 0) {
-    if (count) *count = 0;
-    return BUFF_OK;
-  }
-  // The plan of buff_simd_range_filter (compress/buff_simd.rs:3361-3547), as in
-  // buff_range_filter: early return, full compare for fixed_len < 8 (or the
-  // intended semantics), truncated per-slice target bytes otherwise.
-  const bool intended = c->flags & BUFF_FLAG_INTENDED;
+  // The plan of buff_simd_range_filter (compress/buff_simd.rs:3361-3547), the
+  // one buff_range_filter runs: early return, full compare for fixed_len < 8
+  // (or the intended semantics), truncated per-slice target bytes otherwise.
   int action = 2;  // 0: no rows, 1: all rows, 2: kernel
   buffk::FilterArgs a;
-  memset(&a, 0, sizeof(a));
-  const int64_t fixed_part = fetch_fixed(pred, c->precision_exp, c->dlen);
-  if (fixed_part < c->base) {
-    action = 1;
-  } else {
-    const uint64_t t = (uint64_t)(fixed_part - c->base);
-    const uint32_t fl = c->fixed_len;
-    a.slices = c->slices;
-    a.stride = c->stride;
-    a.tail = c->tail;
-    a.n = n;
-    a.is_range = 1;
-    a.k_used = c->k;
-    a.r = c->r;
-    for (uint32_t j = 0; j < c->k; ++j) a.tbyte[j] = (uint8_t)(t >> (fl - 8 * (j + 1)));
-    a.ttail = c->r ? (uint32_t)(t & ((1ull << c->r) - 1)) : 0u;
-    if (intended || c->k == 0) {
-      if (fl < 64 && (t >> fl) != 0) action = 0;
-      a.full_rows = n;
-    } else {
-      a.full_rows = n / 32 * 32;
+  rc = buffh::plan_filter(c, pred, 0 /* range */, &a, &action);
+  if (rc != BUFF_OK) return rc;
+  a.slices = c->slices;
+  a.stride = c->stride;
+  a.tail = c->tail;
+  if (n == 0) {
+    if (!count) return BUFF_OK;
+    if (!buffh::is_device_ptr(count)) {
+      *count = 0;
+      return BUFF_OK;
     }
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint64_t), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e == cudaSuccess ? BUFF_OK : buffh::cuda_status(e);
   }
   cudaError_t e = cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s);
   if (e == cudaSuccess) {
@@ -123,7 +99,7 @@ extern "C" int buff_range_filter_noalloc(const buff_col *c, double pred, uint32_
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    return e == cudaErrorMemoryAllocation ? BUFF_ENOMEM : BUFF_ECUDA;
+    return buffh::cuda_status(e);
   }
   return BUFF_OK;
 }

@@ -556,12 +556,15 @@ int buff_server_replay(buff_server *srv, const buff_request *reqs, const uint64_
  * (ceil(n/32) u32) and `count` (may be NULL) may be host or device memory.
  * It calls no cudaMalloc/cudaFree or other allocating routine: the bitmap and
  * count are staged in a fixed scratch array of about 8 MiB that belongs to the
- * library's device image, so every GPU that loads the library holds it until
- * the process exits.  Columns with more than BUFF_NOALLOC_MAX_ROWS rows return
- * BUFF_ESCRATCH.  The first call on a device looks up the scratch address for
- * that device (make it before any stream capture); all calls share the array,
- * so calls whose work overlaps on the GPU race and must be ordered by the
- * caller.  The call synchronizes `stream`. */
+ * library's device code.  CUDA loads device code lazily, so a device reserves
+ * the array the first time this call runs on it -- that first call returns
+ * BUFF_ENOMEM if the device has no memory left, so make a warm-up call at
+ * start-up, before any stream capture -- and holds it until the process
+ * exits.  Columns with more than BUFF_NOALLOC_MAX_ROWS rows return
+ * BUFF_ESCRATCH.  The first call on a device also looks up the scratch
+ * address for that device; all calls share the array, so calls whose work
+ * overlaps on the GPU race and must be ordered by the caller.  The call
+ * synchronizes `stream`. */
 int buff_range_filter_noalloc(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
                               void *stream);
 
