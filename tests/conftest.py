@@ -7,8 +7,6 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE_DATA = "/root/reference/database/data/randomwalkdatasample1k-1k"
-
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu)")
@@ -35,3 +33,12 @@ def gpu():
     capi.lib()
     torch.cuda.init()
     return capi
+
+
+@pytest.fixture(scope="session")
+def readme_input():
+    """Path of the reference's README input (randomwalkdatasample1k-1k),
+    decompressed from the committed copy under tests/golden/."""
+    from tests.golden.make_golden import fixture_path
+
+    return fixture_path()

@@ -5,10 +5,14 @@
 - ``vectors.npz``: small seeded columns with the oracle's byte images, decoded
   values, filter bitmaps, sums and maxima (the GPU tests compare against these
   as well as against the live oracle).
-- ``fixture_digest.json``: digests of the oracle's outputs on the reference's
-  own README input (database/data/randomwalkdatasample1k-1k, scale 10000,
-  pred 1.1509); written only where that file exists.  The fixture's values are
-  not copied into this repository.
+- ``randomwalkdatasample1k-1k.xz``: the reference's own README input
+  (database/data/randomwalkdatasample1k-1k, 500,000 comma-separated values),
+  an xz-compressed byte-for-byte copy of the reference-held test vector, so
+  the tests and the GPU machine need no reference checkout.  The copy is made
+  from ``$BUFF_REFERENCE_DIR`` (default: the reference checkout below) and
+  only where that file exists.
+- ``fixture_digest.json``: digests of the oracle's outputs on that input
+  (scale 10000, pred 1.1509, README.md:11 of the reference).
 """
 from __future__ import annotations
 
@@ -24,7 +28,26 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-FIXTURE = "/root/reference/database/data/randomwalkdatasample1k-1k"
+REFERENCE_DIR = os.environ.get("BUFF_REFERENCE_DIR", "/root/reference")
+FIXTURE = os.path.join(REFERENCE_DIR, "database", "data", "randomwalkdatasample1k-1k")
+FIXTURE_XZ = os.path.join(HERE, "randomwalkdatasample1k-1k.xz")
+_FIXTURE_CACHE = {}
+
+
+def fixture_path() -> str:
+    """Path of the README input, decompressed once per process from the
+    committed copy into a temporary file (the CSV readers take a path)."""
+    if "path" not in _FIXTURE_CACHE:
+        import lzma
+        import tempfile
+
+        with lzma.open(FIXTURE_XZ, "rb") as f:
+            data = f.read()
+        fd, path = tempfile.mkstemp(prefix="randomwalkdatasample1k-1k.")
+        with os.fdopen(fd, "wb") as f:
+            f.write(data)
+        _FIXTURE_CACHE["path"] = path
+    return _FIXTURE_CACHE["path"]
 
 
 def load_fixture(path: str) -> np.ndarray:
@@ -127,7 +150,15 @@ def main():
     np.savez_compressed(os.path.join(HERE, "vectors.npz"), **arrays)
     print("wrote vectors.npz with", len(CASES), "cases")
     if os.path.exists(FIXTURE):
-        dig = fixture_digest(O, load_fixture(FIXTURE))
+        import lzma
+
+        with open(FIXTURE, "rb") as f:
+            raw = f.read()
+        with lzma.open(FIXTURE_XZ, "wb", preset=9 | lzma.PRESET_EXTREME) as f:
+            f.write(raw)
+        print("wrote", os.path.basename(FIXTURE_XZ))
+    if os.path.exists(FIXTURE_XZ):
+        dig = fixture_digest(O, load_fixture(fixture_path()))
         with open(os.path.join(HERE, "fixture_digest.json"), "w") as f:
             json.dump(dig, f, indent=1, sort_keys=True)
         print("wrote fixture_digest.json:", dig["range"], dig["equal"])

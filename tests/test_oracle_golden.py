@@ -8,7 +8,6 @@ import numpy as np
 import pytest
 
 from tests import model as M
-from tests.conftest import REFERENCE_DATA
 
 
 # ---- known-answer tests carried by the reference --------------------------
@@ -246,8 +245,7 @@ def test_precision_decode_semantics(oracle):
         oracle.decode_at_precision(buf, 10000, 5)  # dlen 15 < bits for 5 decimals
 
 
-@pytest.mark.skipif(not os.path.exists(REFERENCE_DATA), reason="reference fixture not present")
-def test_reference_fixture_readme_query(oracle):
+def test_reference_fixture_readme_query(oracle, readme_input):
     """The README quick-start input (database/data/randomwalkdatasample1k-1k,
     scale 10000, pred 1.1509): the oracle's results agree with the model and
     with the committed digests in tests/golden/fixture_digest.json."""
@@ -255,7 +253,7 @@ def test_reference_fixture_readme_query(oracle):
 
     from tests.golden.make_golden import fixture_digest, load_fixture
 
-    x = load_fixture(REFERENCE_DATA)
+    x = load_fixture(readme_input)
     assert x.size == 500000
     got = fixture_digest(oracle, x)
     with open(os.path.join(os.path.dirname(__file__), "golden", "fixture_digest.json")) as f:

@@ -8,7 +8,6 @@ import numpy as np
 import pytest
 
 from buff_gb300 import profiler as P
-from tests.conftest import REFERENCE_DATA
 
 
 def test_rust_f64_tokens():
@@ -31,13 +30,12 @@ def test_read_values(tmp_path):
     assert P.read_values(str(f), skip=1).tolist() == [1.5, -2.0, 5.0]
 
 
-@pytest.mark.skipif(not os.path.exists(REFERENCE_DATA), reason="reference fixture not present")
-def test_read_values_reference_fixture():
+def test_read_values_reference_fixture(readme_input):
     from tests.golden.make_golden import load_fixture
 
-    x = P.read_values(REFERENCE_DATA)
+    x = P.read_values(readme_input)
     assert x.size == 500000
-    assert np.array_equal(x, load_fixture(REFERENCE_DATA))
+    assert np.array_equal(x, load_fixture(readme_input))
 
 
 def test_segment_size_and_formats():
