@@ -41,7 +41,7 @@ EXPORTED = [
     "buff_batch_autotune",
     "buff_server_create", "buff_server_add_column", "buff_server_start", "buff_server_submit",
     "buff_server_poll", "buff_server_release", "buff_server_stop", "buff_server_free",
-    "buff_server_stats", "buff_server_replay", "buff_copy", "buff_max_range", "buff_slice_max_range", "buff_max_majority_range",
+    "buff_server_stats", "buff_server_replay", "buff_server_column", "buff_server_store_stats", "buff_copy", "buff_max_range", "buff_slice_max_range", "buff_max_majority_range",
     "buff_slice_encode_f64", "buff_slice_encode_f32", "buff_slice_deserialize",
     "buff_slice_decode", "buff_slice_range_filter", "buff_slice_equal_filter", "buff_slice_sum",
     "buff_slice_buffsum", "buff_slice_max", "buff_slice_buffmax",
@@ -52,7 +52,7 @@ EXPORTED = [
     "buff_rapg_equal_filter_majority", "buff_rapg_sum_majority", "buff_rapg_max_majority",
 ]
 
-Q_RANGE, Q_EQUAL, Q_SUM, Q_MAX, Q_DECODE = 0x1, 0x2, 0x4, 0x8, 0x10
+Q_RANGE, Q_EQUAL, Q_SUM, Q_MAX, Q_DECODE, Q_ENCODE = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20
 
 
 class BuffError(RuntimeError):
@@ -114,11 +114,13 @@ class ServerConfig(C.Structure):
 
 class Request(C.Structure):
     _fields_ = [("column", C.c_uint32), ("ops", C.c_uint32), ("precision", C.c_uint32),
-                ("reserved", C.c_uint32), ("pred", C.c_double), ("tag", C.c_uint64)]
+                ("reserved", C.c_uint32), ("pred", C.c_double), ("tag", C.c_uint64),
+                ("values", C.c_void_p), ("n", C.c_uint64), ("scale", C.c_uint64),
+                ("flags", C.c_uint32), ("is_f32", C.c_uint32)]
 
 
 class Completion(C.Structure):
-    _fields_ = [("tag", C.c_uint64), ("status", C.c_int32), ("reserved", C.c_uint32),
+    _fields_ = [("tag", C.c_uint64), ("status", C.c_int32), ("column", C.c_uint32),
                 ("result", QueryResult), ("words", C.c_void_p), ("values", C.c_void_p),
                 ("submit_ns", C.c_uint64), ("done_ns", C.c_uint64),
                 ("out_off", C.c_uint64 * 2), ("out_cls", C.c_int32 * 2)]
@@ -200,6 +202,8 @@ def lib(build_if_missing: bool = True):
     L.buff_server_stop.argtypes = [P]
     L.buff_server_free.argtypes = [P]
     L.buff_server_stats.argtypes = [P, P, P, P]
+    L.buff_server_column.argtypes = [P, C.c_uint32, pp]
+    L.buff_server_store_stats.argtypes = [P, P, P]
     L.buff_server_replay.argtypes = [P, P, P, C.c_uint32, P, P, P]
     L.buff_copy.argtypes = [P, P, C.c_uint64, P]
     L.buff_max_range.argtypes = [P, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P]

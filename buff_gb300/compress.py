@@ -109,7 +109,18 @@ class Column:
                                                C.byref(h)), "deserialize")
         return cls(h.value)
 
+    @classmethod
+    def borrow(cls, handle: int) -> "Column":
+        """A view of a handle owned elsewhere (a server's store): never freed
+        through this object."""
+        c = cls(handle)
+        c._borrowed = True
+        return c
+
     def free(self):
+        if getattr(self, "_borrowed", False):
+            self._h = C.c_void_p()
+            return
         if self._h and self._h.value:
             lib().buff_col_free(self._h)
             self._h = C.c_void_p()

@@ -262,9 +262,18 @@ void set_slice_layout(buff_col *c, uint32_t fl) {
   c->pad = c->fixed_len - fl;
 }
 
+// Device bytes alloc_col takes for a column (slices and padded tail).
+uint64_t col_alloc_bytes(const buff_col *c) {
+  const uint64_t rows = buffk::round_up(c->n ? c->n : 1, buffk::kRowChunk);
+  return (uint64_t)c->k * rows + rows / 8 * c->r + 64;
+}
+
+// `admit` (may be null) is asked for the column's device bytes once its
+// width is known, before the column is allocated; a nonzero answer ends the
+// encode with that status.
 template <typename T>
 int encode_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, cudaStream_t s,
-                buff_col **out, bool slice = false) {
+                buff_col **out, bool slice = false, const buffh::EncodeAdmit *admit = nullptr) {
   if (!out) return BUFF_EINVAL;
   *out = nullptr;
   if (slice && (flags & BUFF_FLAG_INTENDED)) return BUFF_ENOTSUP;
@@ -349,6 +358,7 @@ int encode_impl(const T *values, uint64_t n64, uint64_t scale, uint32_t flags, c
     else
       set_layout(c, fl);
     c->ilen = (uint32_t)((uint64_t)fl - (uint64_t)c->dlen);
+    if (admit && (rc = admit->fn(admit->ctx, col_alloc_bytes(c)))) goto done;
     if ((rc = alloc_col(c, s))) goto done;
     if (n > 0) {
       if (sizeof(T) == 8)
@@ -2675,4 +2685,12 @@ int plan_filter(const buff_col *c, double pred, int kind, buffk::FilterArgs *a, 
   return ::plan_filter(c, pred, kind, a, action);
 }
 int dlen_of_scale(uint64_t scale) { return dlen_of_prec(prec_of_scale(scale)); }
+int encode_admitted(const void *values, int is_f32, uint64_t n, uint64_t scale, uint32_t flags,
+                    cudaStream_t s, const EncodeAdmit *admit, buff_col **out) {
+  if (is_f32)
+    return encode_impl<float>(static_cast<const float *>(values), n, scale, flags, s, out, false,
+                              admit);
+  return encode_impl<double>(static_cast<const double *>(values), n, scale, flags, s, out, false,
+                             admit);
+}
 }  // namespace buffh

@@ -73,6 +73,14 @@ void free_col(buff_col *c);
 int precision_bits(const buff_col *c, uint32_t precision, uint32_t *total);
 double combine_sum(const buff_col *c, uint32_t total, const uint64_t *parts, bool intended);
 int dlen_of_scale(uint64_t scale);  // -1: PRECISION_MAP has no entry
+// buff_encode_f64 / _f32 with a hook that is given the column's device
+// bytes before they are allocated (see encode_impl).
+struct EncodeAdmit {
+  int (*fn)(void *ctx, uint64_t bytes);
+  void *ctx;
+};
+int encode_admitted(const void *values, int is_f32, uint64_t n, uint64_t scale, uint32_t flags,
+                    cudaStream_t s, const EncodeAdmit *admit, buff_col **out);
 }  // namespace buffh
 
 namespace buffk {

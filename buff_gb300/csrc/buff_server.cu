@@ -13,16 +13,26 @@
 // single-column entry points (the baseline the batched form is compared to);
 // in batched mode a batch that holds a single request takes that path too.
 //
-// Output memory (bitmaps, decoded values) comes from one device arena of
+// Transient memory (query outputs, and the device copy of an encode
+// request's host input) comes from one device arena of
 // `output_budget_bytes`, handed out in power-of-two size classes; a request
-// whose outputs do not fit waits (and blocks later ones, keeping arrival
+// whose memory does not fit waits (and blocks later ones, keeping arrival
 // order) until completions return memory.
+//
+// Encode requests (BUFF_Q_ENCODE) are admitted in the same arrival order but
+// take no batch slot: a second host thread runs them one after another on
+// its own stream (the encode reads its column's extremes back to the host to
+// size the code, so it must not run on the loop thread), while the loop keeps
+// admitting and retiring queries.  The new column's bytes are charged to
+// `store_budget_bytes` before they are allocated; the column joins the store
+// when its encode completes.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
 
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <deque>
 #include <mutex>
 #include <new>
@@ -80,15 +90,20 @@ struct OutAlloc {
   }
 };
 
+enum ReqKind : uint32_t { kQuery = 0, kEncode = 1, kRelease = 2 };
+
 struct Req {
   buff_request r;
   uint64_t submit_ns;
   const buff_col *col;
   uint32_t *words;
   double *values;
-  uint64_t off[2];
-  int cls[2];  // -1: no allocation
+  uint64_t off[2];  // encode: off[0]/cls[0] hold the staging of host input
+  int cls[2];       // -1: no allocation
   int32_t status;
+  uint32_t kind;
+  uint64_t stage_bytes;  // encode: arena bytes for the device copy of host input
+  uint32_t stage_rel;    // release message of an encode's staging
 };
 
 // Result area of one plain-mode request (pinned): count, 9 partials, max.
@@ -116,8 +131,9 @@ struct Slot {
 struct buff_server {
   buff_server_config cfg;
   int device = 0;
-  std::vector<buff_col *> store;
-  uint64_t store_bytes = 0;
+  std::vector<buff_col *> store;  // guarded by mu once serving (encodes add to it)
+  std::vector<bool> owned;        // columns made by encode requests
+  uint64_t store_bytes = 0;       // guarded by mu
   OutAlloc out;
   std::vector<Slot> slots;
   uint64_t seq = 0;
@@ -134,6 +150,16 @@ struct buff_server {
   std::deque<Req> waiting;  // loop thread only
   uint64_t batches = 0, launched_reqs = 0;
   uint32_t warp_slots = 0;  // resident warps of the device (SMs x 64)
+  uint64_t stages_out = 0;  // loop thread: encode stagings not yet returned
+
+  // encoder thread: admitted encode requests, run one at a time on enc_s
+  std::mutex enc_mu;
+  std::condition_variable enc_cv;
+  std::deque<Req> enc_queue;
+  std::atomic<int> enc_inflight{0};  // handed to the encoder, not yet completed
+  bool enc_stop = false;             // guarded by enc_mu
+  std::thread enc_th;
+  cudaStream_t enc_s = nullptr;
 };
 
 namespace {
@@ -183,16 +209,19 @@ bool alloc_outputs(buff_server *S, Req &q) {
   return true;
 }
 
-void finish(buff_server *S, Req &q, const buff_query_result &res) {
+void finish(buff_server *S, Req &q, const buff_query_result &res, uint32_t column) {
   buff_completion c;
   memset(&c, 0, sizeof(c));
   c.tag = q.r.tag;
   c.status = q.status;
+  c.column = column;
   c.result = res;
   c.result.status = q.status;
   c.submit_ns = q.submit_ns;
   c.done_ns = now_ns();
-  if (S->cfg.auto_release) {
+  if (q.kind == kEncode) {
+    c.out_cls[0] = c.out_cls[1] = -1;  // its staging goes back to the loop on its own
+  } else if (S->cfg.auto_release) {
     free_outputs(S, q);
   } else {
     c.words = q.words;
@@ -236,7 +265,7 @@ void retire(buff_server *S, Slot &sl) {
         }
       }
     }
-    finish(S, q, res);
+    finish(S, q, res, q.r.column);
   }
   sl.reqs.clear();
   sl.busy = false;
@@ -317,6 +346,138 @@ int launch_plain(Slot &sl) {
   return buffh::cuda_status(e);
 }
 
+// ---- encode requests ----
+
+// Charges an encode's column bytes to the store budget (called by the encode
+// once the code width is known, before the column is allocated).
+struct EncCharge {
+  buff_server *S;
+  uint64_t charged;
+};
+
+int charge_store(void *ctx, uint64_t bytes) {
+  EncCharge *ch = static_cast<EncCharge *>(ctx);
+  buff_server *S = ch->S;
+  std::lock_guard<std::mutex> lk(S->mu);
+  const uint64_t cap = S->cfg.store_budget_bytes;
+  if (cap && (bytes > cap || S->store_bytes > cap - bytes)) return BUFF_EFULL;
+  S->store_bytes += bytes;
+  ch->charged = bytes;
+  return BUFF_OK;
+}
+
+// One encode request on the encoder thread: the host input is copied into
+// its arena staging first, the column joins the store on success, and the
+// staging returns to the loop as a release message.
+void run_encode(buff_server *S, Req &q) {
+  cudaStream_t s = S->enc_s;
+  const void *src = q.r.values;
+  int st = BUFF_OK;
+  if (q.cls[0] >= 0) {
+    void *dst = S->out.base + q.off[0];
+    const cudaError_t e = cudaMemcpyAsync(dst, src, q.stage_bytes, cudaMemcpyDefault, s);
+    if (e != cudaSuccess)
+      st = buffh::cuda_status(e);
+    else
+      src = dst;
+  }
+  EncCharge ch{S, 0};
+  buffh::EncodeAdmit adm{charge_store, &ch};
+  buff_col *col = nullptr;
+  if (st == BUFF_OK)
+    st = buffh::encode_admitted(src, (int)q.r.is_f32, q.r.n, q.r.scale, q.r.flags, s, &adm, &col);
+  if (st == BUFF_OK) {
+    const cudaError_t e = cudaStreamSynchronize(s);  // the column is complete
+    if (e != cudaSuccess) st = buffh::cuda_status(e);
+  } else {
+    cudaStreamSynchronize(s);  // the staging copy may still be reading
+  }
+  buff_query_result res;
+  memset(&res, 0, sizeof(res));
+  uint32_t id = 0xFFFFFFFFu;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (st == BUFF_OK) {
+      S->store.push_back(col);
+      S->owned.push_back(true);
+      id = (uint32_t)(S->store.size() - 1);
+      res.count = q.r.n;
+    } else {
+      S->store_bytes -= ch.charged;
+    }
+    if (q.cls[0] >= 0) {  // the staging back to the loop (it owns the arena)
+      Req rel;
+      memset(&rel, 0, sizeof(rel));
+      rel.kind = kRelease;
+      rel.stage_rel = 1;
+      rel.off[0] = q.off[0];
+      rel.cls[0] = q.cls[0];
+      rel.cls[1] = -1;
+      S->pending.push_front(rel);
+    }
+  }
+  if (st != BUFF_OK && col) buff_col_free(col);
+  q.status = st;
+  finish(S, q, res, id);
+}
+
+void encoder(buff_server *S) {
+  cudaSetDevice(S->device);
+  for (;;) {
+    Req q;
+    {
+      std::unique_lock<std::mutex> lk(S->enc_mu);
+      S->enc_cv.wait(lk, [&] { return !S->enc_queue.empty() || S->enc_stop; });
+      if (S->enc_queue.empty()) break;
+      q = S->enc_queue.front();
+      S->enc_queue.pop_front();
+    }
+    run_encode(S, q);
+    S->enc_inflight.fetch_sub(1, std::memory_order_acq_rel);
+  }
+}
+
+void fail_request(buff_server *S, Req &q, int status) {
+  q.status = status;
+  buff_query_result res;
+  memset(&res, 0, sizeof(res));
+  finish(S, q, res, q.kind == kEncode ? 0xFFFFFFFFu : q.r.column);
+}
+
+// Nothing holds arena memory (no batch in flight, no encode staging out,
+// no outputs held by callers): the size classes may be rebuilt from scratch.
+bool arena_idle(buff_server *S) {
+  for (const Slot &o : S->slots)
+    if (o.busy || !o.reqs.empty()) return false;
+  return S->stages_out == 0 && S->cfg.auto_release;
+}
+
+// Admits the encode request at the head of the waiting queue: its staging
+// (for host input) from the arena, then the encoder thread.  False when the
+// staging does not fit now (the request waits at the head).
+bool admit_encode(buff_server *S, Req &q) {
+  q.cls[0] = q.cls[1] = -1;
+  if (q.stage_bytes) {
+    if (class_bytes(q.stage_bytes) > S->out.cap) {  // larger than the whole arena
+      fail_request(S, q, BUFF_EFULL);
+      return true;
+    }
+    if (!S->out.alloc(q.stage_bytes, &q.off[0], &q.cls[0])) {
+      if (!arena_idle(S)) return false;
+      S->out.reset();
+      if (!S->out.alloc(q.stage_bytes, &q.off[0], &q.cls[0])) return false;
+    }
+    S->stages_out++;
+  }
+  S->enc_inflight.fetch_add(1, std::memory_order_acq_rel);
+  {
+    std::lock_guard<std::mutex> lk(S->enc_mu);
+    S->enc_queue.push_back(q);
+  }
+  S->enc_cv.notify_one();
+  return true;
+}
+
 // Waiting requests beyond the free slots before slots take batches.
 constexpr size_t kQueueForBatch = 8;
 
@@ -342,10 +503,13 @@ void loop(buff_server *S) {
       std::lock_guard<std::mutex> lk(S->mu);
       while (!S->pending.empty()) {
         Req &q = S->pending.front();
-        if (!q.col)
-          free_outputs(S, q);  // buff_server_release of a completed request's outputs
-        else
+        if (q.kind == kRelease) {
+          // a completed request's outputs (buff_server_release) or an encode's staging
+          free_outputs(S, q);
+          if (q.stage_rel) S->stages_out--;
+        } else {
           S->waiting.push_back(q);
+        }
         S->pending.pop_front();
         worked = true;
       }
@@ -355,6 +519,12 @@ void loop(buff_server *S) {
     // of its own (light load: latency -- a batched launch of a handful of
     // requests costs more than the same requests one by one), beyond that
     // slots take batches (throughput)
+    // encode requests at the head need no slot
+    while (!S->waiting.empty() && S->waiting.front().kind == kEncode) {
+      if (!admit_encode(S, S->waiting.front())) break;
+      S->waiting.pop_front();
+      worked = true;
+    }
     uint32_t free_slots = 0;
     for (const Slot &sl : S->slots) free_slots += !sl.busy;
     const uint32_t take = S->waiting.size() > free_slots + kQueueForBatch ? maxb : 1;
@@ -362,21 +532,21 @@ void loop(buff_server *S) {
       if (sl.busy || S->waiting.empty()) continue;
       while (!S->waiting.empty() && sl.reqs.size() < take) {
         Req &q = S->waiting.front();
+        if (q.kind == kEncode) {
+          if (!admit_encode(S, q)) break;
+          S->waiting.pop_front();
+          continue;
+        }
         if (out_need(q) > S->out.cap) {  // larger than the whole budget
-          q.status = BUFF_EFULL;
-          buff_query_result res;
-          memset(&res, 0, sizeof(res));
-          finish(S, q, res);
+          fail_request(S, q, BUFF_EFULL);
           S->waiting.pop_front();
           continue;
         }
         if (!alloc_outputs(S, q)) {
-          bool any = false;
-          for (Slot &o : S->slots) any |= o.busy;
           // wait for completions (or the caller's releases) to return memory;
           // with nothing in flight and nothing held by callers, the size
           // classes are rebuilt from scratch
-          if (any || !sl.reqs.empty() || !S->cfg.auto_release) break;
+          if (!arena_idle(S)) break;
           S->out.reset();
           if (!alloc_outputs(S, q)) break;
         }
@@ -402,7 +572,7 @@ void loop(buff_server *S) {
       worked = true;
     }
     if (!worked) {
-      bool idle = S->waiting.empty();
+      bool idle = S->waiting.empty() && S->enc_inflight.load(std::memory_order_acquire) == 0;
       for (Slot &sl : S->slots) idle &= !sl.busy;
       if (idle && S->stop.load()) {
         std::lock_guard<std::mutex> lk(S->mu);
@@ -411,6 +581,16 @@ void loop(buff_server *S) {
       std::this_thread::yield();
     }
   }
+}
+
+void stop_encoder(buff_server *S) {
+  if (!S->enc_th.joinable()) return;
+  {
+    std::lock_guard<std::mutex> lk(S->enc_mu);
+    S->enc_stop = true;
+  }
+  S->enc_cv.notify_all();
+  S->enc_th.join();
 }
 
 void destroy_slots(buff_server *S) {
@@ -459,6 +639,12 @@ int buff_server_create(const buff_server_config *cfg, buff_server **out) {
   }
   S->out.cap = c.output_budget_bytes;
   S->warp_slots = (uint32_t)buffk::num_sms(S->device) * 64u;
+  if ((e = cudaStreamCreateWithFlags(&S->enc_s, cudaStreamNonBlocking)) != cudaSuccess) {
+    rc = buffh::cuda_status(e);
+    cudaFree(S->out.base);
+    delete S;
+    return rc;
+  }
   S->slots.resize(c.max_inflight);
   const uint32_t mb = c.batched ? c.max_batch : 1;
   const size_t dsz = buffk::batch_desc_size();
@@ -485,6 +671,7 @@ int buff_server_create(const buff_server_config *cfg, buff_server **out) {
   if (e != cudaSuccess) {
     rc = buffh::cuda_status(e);
     destroy_slots(S);
+    cudaStreamDestroy(S->enc_s);
     cudaFree(S->out.base);
     delete S;
     return rc;
@@ -500,16 +687,39 @@ int buff_server_add_column(buff_server *S, buff_col *col, uint32_t *id) {
   const uint64_t b = col_bytes(col);
   if (S->cfg.store_budget_bytes && S->store_bytes + b > S->cfg.store_budget_bytes)
     return BUFF_EFULL;
+  std::lock_guard<std::mutex> lk(S->mu);
   S->store.push_back(col);
+  S->owned.push_back(false);
   S->store_bytes += b;
   *id = (uint32_t)(S->store.size() - 1);
+  return BUFF_OK;
+}
+
+int buff_server_column(buff_server *S, uint32_t id, const buff_col **col) {
+  if (!S || !col) return BUFF_EINVAL;
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (id >= S->store.size()) return BUFF_EINVAL;
+  *col = S->store[id];
+  return BUFF_OK;
+}
+
+int buff_server_store_stats(buff_server *S, uint64_t *store_bytes, uint32_t *columns) {
+  if (!S) return BUFF_EINVAL;
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (store_bytes) *store_bytes = S->store_bytes;
+  if (columns) *columns = (uint32_t)S->store.size();
   return BUFF_OK;
 }
 
 int buff_server_start(buff_server *S) {
   if (!S || S->running.load()) return BUFF_EINVAL;
   S->stop.store(false);
+  {
+    std::lock_guard<std::mutex> lk(S->enc_mu);
+    S->enc_stop = false;
+  }
   S->running.store(true);
+  S->enc_th = std::thread(encoder, S);
   S->th = std::thread(loop, S);
   return BUFF_OK;
 }
@@ -517,6 +727,18 @@ int buff_server_start(buff_server *S) {
 int buff_server_submit(buff_server *S, const buff_request *reqs, uint32_t n) {
   if (!S || (n && !reqs)) return BUFF_EINVAL;
   const uint64_t t = now_ns();
+  // where an encode's input lies (a device pointer query per encode request),
+  // before taking the lock
+  bool any_encode = false;
+  for (uint32_t i = 0; i < n; ++i) any_encode |= (reqs[i].ops & BUFF_Q_ENCODE) != 0;
+  std::vector<uint64_t> stage(any_encode ? n : 0, 0);
+  for (uint32_t i = 0; any_encode && i < n; ++i) {
+    const buff_request &r = reqs[i];
+    if (r.ops != BUFF_Q_ENCODE || !r.values || !r.n) continue;
+    const uint64_t bytes = r.n * (r.is_f32 ? 4u : 8u);
+    if (!buffh::is_device_ptr(r.values) || (reinterpret_cast<uintptr_t>(r.values) & 15))
+      stage[i] = bytes;
+  }
   std::lock_guard<std::mutex> lk(S->mu);
   for (uint32_t i = 0; i < n; ++i) {
     Req q;
@@ -524,18 +746,30 @@ int buff_server_submit(buff_server *S, const buff_request *reqs, uint32_t n) {
     q.r = reqs[i];
     q.submit_ns = t;
     q.cls[0] = q.cls[1] = -1;
-    if (reqs[i].column >= S->store.size()) {
+    bool bad;
+    if (reqs[i].ops & BUFF_Q_ENCODE) {
+      q.kind = kEncode;
+      q.stage_bytes = any_encode ? stage[i] : 0;
+      bad = reqs[i].ops != BUFF_Q_ENCODE || (reqs[i].n && !reqs[i].values) ||
+            reqs[i].n > BUFF_MAX_ROWS;
+    } else {
+      q.kind = kQuery;
+      bad = reqs[i].column >= S->store.size();
+    }
+    if (bad) {
       buff_completion c;
       memset(&c, 0, sizeof(c));
       c.tag = reqs[i].tag;
       c.status = BUFF_EINVAL;
+      c.column = reqs[i].column;
       c.result.status = BUFF_EINVAL;
+      c.out_cls[0] = c.out_cls[1] = -1;
       c.submit_ns = c.done_ns = t;
       S->done.push_back(c);
       S->n_done.fetch_add(1, std::memory_order_release);
       continue;
     }
-    q.col = S->store[reqs[i].column];
+    if (q.kind == kQuery) q.col = S->store[reqs[i].column];
     S->pending.push_back(q);
   }
   return BUFF_OK;
@@ -557,6 +791,7 @@ int buff_server_release(buff_server *S, const buff_completion *c) {
   // a request without a column, taken before any waiting request.
   Req q;
   memset(&q, 0, sizeof(q));
+  q.kind = kRelease;
   q.cls[0] = c->out_cls[0];
   q.cls[1] = c->out_cls[1];
   q.off[0] = c->out_off[0];
@@ -571,7 +806,8 @@ int buff_server_stop(buff_server *S) {
   if (!S) return BUFF_EINVAL;
   if (S->running.load()) {
     S->stop.store(true);
-    if (S->th.joinable()) S->th.join();
+    if (S->th.joinable()) S->th.join();  // exits once every request has completed
+    stop_encoder(S);
     S->running.store(false);
   }
   return S->loop_status.load();
@@ -582,6 +818,9 @@ int buff_server_free(buff_server *S) {
   buff_server_stop(S);
   cudaDeviceSynchronize();
   destroy_slots(S);
+  for (size_t i = 0; i < S->store.size(); ++i)
+    if (S->owned[i]) buff_col_free(S->store[i]);
+  if (S->enc_s) cudaStreamDestroy(S->enc_s);
   cudaFree(S->out.base);
   delete S;
   return BUFF_OK;

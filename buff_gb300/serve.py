@@ -1,6 +1,8 @@
 """Serving form (buff_server_* in the C ABI): resident columns, a request
-loop with continuous batching under an output-memory budget, and a load
-replay that reports per-request latency."""
+loop with continuous batching under a memory budget (transient outputs and
+encode inputs in one arena, resident columns in a store budget), encode
+requests that add columns while queries run, and a load replay that reports
+per-request latency."""
 from __future__ import annotations
 
 import ctypes as C
@@ -61,7 +63,19 @@ class Server:
     def stats(self):
         b, r, u = C.c_uint64(0), C.c_uint64(0), C.c_uint64(0)
         check(lib().buff_server_stats(self._h, C.byref(b), C.byref(r), C.byref(u)), "stats")
-        return {"batches": b.value, "requests": r.value, "output_bytes_in_use": u.value}
+        sb, nc = C.c_uint64(0), C.c_uint32(0)
+        check(lib().buff_server_store_stats(self._h, C.byref(sb), C.byref(nc)), "store_stats")
+        return {"batches": b.value, "requests": r.value, "output_bytes_in_use": u.value,
+                "store_bytes": sb.value, "columns": nc.value}
+
+    def column(self, cid: int):
+        """A store column as a Column view (the server keeps ownership of
+        columns made by encode requests)."""
+        from .compress import Column
+
+        h = C.c_void_p()
+        check(lib().buff_server_column(self._h, cid, C.byref(h)), "server_column")
+        return Column.borrow(h.value)
 
     def replay(self, reqs, arrival_ns: np.ndarray, results: bool = True):
         """Plays requests (a list of Request or an array of REQ_DTYPE) at
@@ -98,7 +112,9 @@ class Server:
 
 # numpy layout of buff_request (for request streams built as arrays)
 REQ_DTYPE = np.dtype([("column", "<u4"), ("ops", "<u4"), ("precision", "<u4"),
-                      ("reserved", "<u4"), ("pred", "<f8"), ("tag", "<u8")])
+                      ("reserved", "<u4"), ("pred", "<f8"), ("tag", "<u8"),
+                      ("values", "<u8"), ("n", "<u8"), ("scale", "<u8"), ("flags", "<u4"),
+                      ("is_f32", "<u4")])
 assert REQ_DTYPE.itemsize == C.sizeof(Request)
 
 
@@ -106,4 +122,21 @@ def request(column: int, ops: int, pred: float = 0.0, precision: int = 0, tag: i
     return Request(column, ops, precision, 0, float(pred), tag)
 
 
-__all__ = ["Server", "request", "REQ_DTYPE"]
+def encode_request(values, scale: int, flags: int = 0, tag: int = 0):
+    """BUFF_Q_ENCODE of a host (numpy) or device (torch) f64/f32 array; the
+    array must stay alive and unchanged until the request completes."""
+    from .capi import Q_ENCODE
+
+    if hasattr(values, "data_ptr"):
+        ptr, n = values.data_ptr(), values.numel()
+        f32 = str(values.dtype) == "torch.float32"
+    else:
+        a = np.asarray(values)
+        assert a.flags.c_contiguous and a.dtype in (np.float64, np.float32)
+        ptr, n, f32 = a.ctypes.data, a.size, a.dtype == np.float32
+    r = Request(0, Q_ENCODE, 0, 0, 0.0, tag)
+    r.values, r.n, r.scale, r.flags, r.is_f32 = ptr, n, scale, flags, 1 if f32 else 0
+    return r
+
+
+__all__ = ["Server", "request", "encode_request", "REQ_DTYPE"]

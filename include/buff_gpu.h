@@ -436,6 +436,7 @@ int buff_batch_encode_f64(const double *const *values, const uint64_t *lens,
 #define BUFF_Q_SUM 0x4u    /* byte_fixed_sum */
 #define BUFF_Q_MAX 0x8u    /* byte_fixed_max value (no arg-max bitmap) */
 #define BUFF_Q_DECODE 0x10u /* buff_simd256_decode / byte_residue_decode_with_precision */
+#define BUFF_Q_ENCODE 0x20u /* buff_simd256_encode into a new column (serving requests only) */
 
 /* One query of a batch: ops is one of RANGE or EQUAL (optionally with SUM),
  * or any of SUM, MAX, DECODE.  Outputs are device memory. */
@@ -485,8 +486,19 @@ int buff_batch_autotune(const buff_query *queries, uint32_t nq, void *stream,
  * is free (continuous batching: up to max_inflight batches run at once, each
  * one persistent launch of up to max_batch queries); with batched = 0 every
  * request runs alone through the single-column calls (one query per launch).
- * Outputs (bitmaps, decoded values) come from a device arena of
- * output_budget_bytes; a request waits until its outputs fit. */
+ *
+ * Memory.  The server's HBM is two budgets.  Transient device memory --
+ * query outputs (bitmaps, decoded values) and the device copy of an encode
+ * request's host input -- comes from one arena of output_budget_bytes,
+ * allocated at create; requests are admitted into it in arrival order, and a
+ * request whose memory does not fit now waits (and holds back the requests
+ * behind it) until completions return memory, or fails with BUFF_EFULL when
+ * it is larger than the whole arena.  Resident columns (added before start
+ * or encoded by requests while serving) are charged to store_budget_bytes:
+ * an encode request reserves its column's exact bytes once the column's code
+ * width is known, before the column is allocated, and fails with BUFF_EFULL
+ * when they exceed what is left (the store never shrinks while serving, so
+ * it could never fit). */
 typedef struct buff_server_config {
   uint64_t output_budget_bytes;
   uint64_t store_budget_bytes; /* 0: no limit on resident columns */
@@ -497,19 +509,33 @@ typedef struct buff_server_config {
   buff_batch_tune tune;  /* tile_rows = 0: defaults */
 } buff_server_config;
 
+/* A request: a query on a store column (ops as in buff_query), or
+ * ops = BUFF_Q_ENCODE: buff_simd256_encode (compress/buff_simd.rs:3116-3250)
+ * of `values` into a new resident column, with `scale` and `flags` as in
+ * buff_encode_f64.  The encode runs on the server's own encoder thread and
+ * stream while queries keep running; its completion carries the new
+ * column's store id (`column`) and its rows (result.count), after which
+ * queries may name that id. */
 typedef struct buff_request {
-  uint32_t column;    /* store id from buff_server_add_column */
-  uint32_t ops;       /* BUFF_Q_* as in buff_query */
+  uint32_t column;    /* store id (queries) */
+  uint32_t ops;       /* BUFF_Q_* */
   uint32_t precision; /* DECODE: 0 = full precision */
   uint32_t reserved;
   double pred;
   uint64_t tag;       /* returned in the completion */
+  /* ENCODE only: n values (f64, or f32 when is_f32) in host or device
+   * memory, which must stay valid and unchanged until the completion */
+  const void *values;
+  uint64_t n;
+  uint64_t scale;
+  uint32_t flags;
+  uint32_t is_f32;
 } buff_request;
 
 typedef struct buff_completion {
   uint64_t tag;
   int32_t status;
-  uint32_t reserved;
+  uint32_t column;       /* the request's column; for ENCODE the new column's id */
   buff_query_result result;
   const uint32_t *words; /* device bitmap (auto_release = 0; NULL otherwise) */
   const double *values;  /* device values (auto_release = 0; NULL otherwise) */
@@ -523,6 +549,9 @@ int buff_server_create(const buff_server_config *cfg, buff_server **out);
 /* Adds a resident column (borrowed: it must outlive the server); BUFF_EFULL
  * beyond store_budget_bytes.  Only before buff_server_start. */
 int buff_server_add_column(buff_server *srv, buff_col *col, uint32_t *id);
+/* The handle of store column `id` (e.g. for buff_serialize); columns made by
+ * ENCODE requests belong to the server and are freed with it. */
+int buff_server_column(buff_server *srv, uint32_t id, const buff_col **col);
 int buff_server_start(buff_server *srv);
 /* Thread-safe. */
 int buff_server_submit(buff_server *srv, const buff_request *reqs, uint32_t n);
@@ -534,6 +563,8 @@ int buff_server_stop(buff_server *srv);
 int buff_server_free(buff_server *srv);
 int buff_server_stats(buff_server *srv, uint64_t *batches, uint64_t *requests,
                       uint64_t *output_bytes_in_use);
+/* Resident column bytes charged to store_budget_bytes, and the columns. */
+int buff_server_store_stats(buff_server *srv, uint64_t *store_bytes, uint32_t *columns);
 /* Load replay for measurement: submits reqs[i] at arrival_ns[i] after the
  * start (a feeder thread), waits for every completion and returns each
  * request's latency from its arrival time to its completion, its result

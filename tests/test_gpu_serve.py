@@ -171,3 +171,144 @@ def test_replay_reports_latency(gpu):
         s.free()
         assert lat.size == len(reqs) and (lat > 0).all() and wall > 0
         assert all(r.status == 0 for r in res)
+
+
+def _encode_inputs(seed):
+    """Host f64 / f32 arrays and one device array to encode while serving."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for i, n in enumerate((70_001, 250_000, 3_000, 131_072)):
+        dec = int(rng.integers(2, 7))
+        x = np.round(np.cumsum(rng.normal(0, 0.2, n)) + rng.uniform(-20, 20), dec)
+        out.append((x, 10 ** dec))
+    x32 = np.round(rng.uniform(-5, 5, 40_000), 2).astype(np.float32)
+    out.append((x32, 100))
+    xd = np.round(np.cumsum(rng.normal(0, 1.0, 90_000)), 3)
+    out.append((torch.from_numpy(xd).cuda(), 1000))
+    return out
+
+
+def test_encode_requests_while_serving(oracle, gpu):
+    """Encode requests mixed into a query stream: each new column is the
+    oracle's byte image, queries on it then match a column encoded alone, and
+    every query of the mix is the same as when it runs alone."""
+    import torch
+
+    from buff_gb300.capi import Q_RANGE, Q_SUM
+    from buff_gb300.compress import Column
+    from buff_gb300.serve import Server, encode_request, request
+
+    cols, data = _store(seed=14, ncols=10)
+    queries = _mix(data, 200, 10)
+    inputs = _encode_inputs(15)
+    s = Server(1 << 30, max_batch=32, max_inflight=3, batched=True, auto_release=False)
+    for c in cols:
+        s.add_column(c)
+    base_bytes = s.stats()["store_bytes"]
+    s.start()
+    torch.cuda.synchronize()
+    mixed_reqs = list(queries)
+    enc_tag = {}
+    for i, (x, scale) in enumerate(inputs):
+        tag = 10_000 + i
+        enc_tag[tag] = i
+        mixed_reqs.insert(30 * i + 7, encode_request(x, scale, tag=tag))
+    s.submit(mixed_reqs)
+    done = s.wait(len(mixed_reqs))
+    mixed, new_ids = {}, {}
+    for c in done:
+        if c.tag in enc_tag:
+            assert c.status == 0, c.status
+            new_ids[enc_tag[c.tag]] = c.column
+            continue
+        r = queries[c.tag]
+        mixed[c.tag] = _snapshot(c, r, data[r.column].size)
+        s.release(c)
+    assert sorted(new_ids) == list(range(len(inputs)))
+    alone = _run(s, queries, data, True)
+    for t in range(len(queries)):
+        assert alone[t] == mixed[t], t
+    # every new column is the oracle's image; queries on it match a column
+    # encoded alone through the single-column call
+    grown = 0
+    follow, refs = [], {}
+    for i, (x, scale) in enumerate(inputs):
+        xh = x.cpu().numpy() if hasattr(x, "cpu") else x
+        col = s.column(new_ids[i])
+        assert col.serialize() == oracle.encode(xh, scale), i
+        grown += col.info.device_bytes
+        ref = Column.encode(xh, scale)
+        p = float(np.quantile(xh.astype(np.float64), 0.6))
+        follow.append(request(new_ids[i], Q_RANGE | Q_SUM, p, tag=20_000 + i))
+        refs[20_000 + i] = (ref.range_filter(p), ref.sum(), xh.size)
+    assert s.stats()["store_bytes"] == base_bytes + grown
+    s.submit(follow)
+    for c in s.wait(len(follow)):
+        f, sm, n = refs[c.tag]
+        assert c.status == 0 and c.result.count == f.count and c.result.sum == sm.sum
+        from buff_gb300.capi import copy_bytes
+
+        assert copy_bytes(c.words, 4 * ((n + 31) // 32)) == f.words.astype("<u4").tobytes()
+        s.release(c)
+    s.stop()
+    s.free()
+
+
+def test_encode_budgets(oracle, gpu):
+    """Resident columns are charged to the store budget (an encode that can
+    never fit fails with BUFF_EFULL and charges nothing); an encode's host
+    input is staged in the arena in arrival order with the queries' outputs."""
+    import torch
+
+    from buff_gb300.capi import Q_DECODE
+    from buff_gb300.compress import Column
+    from buff_gb300.serve import Server, encode_request, request
+
+    rng = np.random.default_rng(3)
+    x = np.round(np.cumsum(rng.normal(0, 1, 200_000)), 2)
+    col = Column.encode(x, 100)
+    cb = col.info.device_bytes
+    small = np.round(rng.uniform(0, 1, 5_000), 2)
+    big = np.round(np.cumsum(rng.normal(0, 1, 400_000)), 2)
+    # store budget: the resident column plus room for the small encode only
+    s = Server(1 << 26, max_batch=8, max_inflight=2, store_budget_bytes=cb + (1 << 16))
+    cid = s.add_column(col)
+    s.start()
+    s.submit([encode_request(big, 100, tag=1), encode_request(small, 100, tag=2)])
+    got = {c.tag: c for c in s.wait(2)}
+    assert got[1].status == 8 and got[2].status == 0  # BUFF_EFULL, then OK
+    st = s.stats()
+    assert st["columns"] == 2
+    assert st["store_bytes"] == cb + s.column(got[2].column).info.device_bytes
+    assert s.column(got[2].column).serialize() == oracle.encode(small, 100)
+    s.stop()
+    s.free()
+    # arena of 4 MiB: each 2 MiB decode output and each host input's staging
+    # (1.6 MB -> a 2 MiB class) wait for one another in arrival order
+    s = Server(4 << 20, max_batch=8, max_inflight=4, auto_release=True)
+    cid = s.add_column(col)
+    s.start()
+    ins = [np.round(np.cumsum(rng.normal(0, 1, 200_000)), 2) for _ in range(4)]
+    reqs = []
+    for i in range(12):
+        reqs.append(request(cid, Q_DECODE, tag=i))
+        if i % 3 == 0:
+            reqs.append(encode_request(ins[i // 3], 100, tag=100 + i // 3))
+    s.submit(reqs)
+    done = {c.tag: c for c in s.wait(len(reqs))}
+    assert all(c.status == 0 for c in done.values())
+    for j in range(4):
+        assert s.column(done[100 + j].column).serialize() == oracle.encode(ins[j], 100)
+    assert s.stats()["output_bytes_in_use"] == 0
+    # host input larger than the whole arena: BUFF_EFULL; device input needs
+    # no staging and is encoded
+    huge = np.round(np.cumsum(rng.normal(0, 1, 1_000_000)), 2)
+    dev = torch.from_numpy(huge).cuda()
+    s.submit([encode_request(huge, 100, tag=200), encode_request(dev, 100, tag=201)])
+    got = {c.tag: c for c in s.wait(2)}
+    assert got[200].status == 8 and got[201].status == 0
+    assert s.column(got[201].column).serialize() == oracle.encode(huge, 100)
+    s.stop()
+    s.free()
