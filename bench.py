@@ -25,8 +25,12 @@ finish).
 
 `--impl reference` times the CPU restatement of the reference algorithm (the
 oracle: progressive slice refinement + per-slice byte sums, the reference
-having no GPU path and no Rust toolchain here) on all host cores over a
-bounded sample of the same column.
+having no GPU path and no Rust toolchain here) on the same full column with
+every host thread, and reports the one-thread time beside it (the reference
+is single-threaded).  This arm's own line also carries the one-thread time
+of the step on the full column (`cpu_baseline`, checked against the GPU's
+count and sum), the all-threads time (`cpu_all_threads`, not the reference)
+and a one-thread time for every operation of the per-op tables (`cpu_ops`).
 """
 from __future__ import annotations
 
@@ -67,6 +71,8 @@ def parse_args():
                     help="release the f64 input after encode (small-footprint profiling runs)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched form")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving form")
+    ap.add_argument("--no-serve-encode", action="store_true",
+                    help="skip the serving run with encode requests")
     ap.add_argument("--no-outlier", action="store_true", help="skip the outlier-column form")
     ap.add_argument("--outlier-rows", type=int, default=1 << 26)
     ap.add_argument("--batched-cols", type=int, default=4096)
@@ -228,47 +234,94 @@ def mib_s(rows: float, seconds: float) -> float:
     return rows * 8 / (1 << 20) / seconds
 
 
-def cpu_reference_line(args, x_sample: np.ndarray, pred: float, threads: int, steps: int,
-                       warmup: int):
-    """Times the oracle's filter+sum (the reference algorithm) on host cores."""
+def cpu_time(fn, reps: int = 2) -> float:
+    """Seconds per call of a CPU oracle function (best of `reps` after one
+    untimed call)."""
+    fn()
+    best = float("inf")
+    for _ in range(reps):
+        t = time.perf_counter()
+        fn()
+        best = min(best, time.perf_counter() - t)
+    return best
+
+
+def cpu_op_table(xh: np.ndarray, scale: int, range_preds: dict, peq: float, precisions,
+                 sample: str) -> dict:
+    """The CPU restatement of the reference (the oracle) on ONE host core for
+    each operation of a configuration: encode, the range filters, equality,
+    sum, max, full decode and decode at the given precisions, in Gvalues/s
+    and in the reference's MiB/s of f64 input (compress/buff_simd.rs:84-94)."""
     from oracle import oracle as O
 
-    buf = O.encode(x_sample, SCALE)
-    for _ in range(warmup):
-        O.bench_filter_sum(buf, SCALE, pred, threads, 1)
-    t, cnt, s = O.bench_filter_sum(buf, SCALE, pred, threads, steps)
-    rows = x_sample.size
-    return t / steps, rows, cnt, s
+    n = xh.size
+    buf = O.encode(xh, scale)
+    fns = {"encode": lambda: O.encode(xh, scale)}
+    for name, p in range_preds.items():
+        fns[name] = (lambda p=p: O.range_filter(buf, scale, p))
+    fns["equal"] = lambda: O.equal_filter(buf, scale, peq)
+    fns["sum"] = lambda: O.buff_sum(buf, scale)
+    fns["max"] = lambda: O.buff_max(buf, scale)
+    fns["decode_full"] = lambda: O.decode(buf, scale)
+    for p in precisions:
+        fns[f"decode_p{p}"] = (lambda p=p: O.decode_at_precision(buf, scale, p))
+    out = {}
+    for name, fn in fns.items():
+        t = cpu_time(fn)
+        out[name] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "mib_s": mib_s(n, t)}
+    return {"cores": 1, "kind": "port", "rows": n, "sample": sample, "ops": out}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the CPU restatement of the reference algorithm (the
+    oracle) answers the step's query pair -- range filter at 10 % then sum --
+    on the same full column as the GPU arm (same seed, same predicate), with
+    every host thread.  The reference itself is single-threaded; the line
+    also carries the one-thread time, and the count and f64 sum bits that the
+    GPU arm's line carries for the same column."""
     if rank != 0:
         return
     import torch
 
     from buff_gb300.workloads import bounded_walk_torch
+    from oracle import oracle as O
 
     dev = "cuda" if torch.cuda.is_available() else "cpu"
-    x = bounded_walk_torch(CPU_SAMPLE_ROWS, seed=2, device=dev).cpu().numpy()
-    pred = float(np.quantile(x[::64], 1.0 - SELECTIVITY))
+    n = args.rows
+    xt = bounded_walk_torch(n, seed=2, device=dev)
+    pred = float(torch.quantile(xt[:: max(1, n >> 20)], 1.0 - SELECTIVITY).item())
+    x = xt.cpu().numpy()
+    del xt
+    buf = O.encode(x, SCALE)  # the reference's encoder, restated (one thread)
+    del x
     threads = os.cpu_count() or 1
-    # size each step's sample so that the K timed steps take about a minute
-    t1, _, _ = cpu_reference_line(args, x, pred, threads, 1, 0)[:3]
-    frac = min(1.0, 60.0 / max(args.steps, 1) / max(t1, 1e-9))
-    rows_step = max(1 << 16, int(x.size * frac) // 32 * 32)
-    x = x[:rows_step]
-    per_step, rows, cnt, s = cpu_reference_line(args, x, pred, threads, args.steps, args.warmup)
-    v = rows / per_step / 1e9
+    for _ in range(args.warmup):
+        O.bench_filter_sum(buf, SCALE, pred, threads, 1)
+    t, cnt, s = O.bench_filter_sum(buf, SCALE, pred, threads, args.steps)
+    per_step = t / args.steps
+    t1, cnt1, s1 = O.bench_filter_sum(buf, SCALE, pred, 1, 2)
+    assert cnt1 == cnt and s1 == s  # threads change only the time
+    one = t1 / 2
+    v = n / per_step / 1e9
     line = {
         "impl": "reference", "metric": "filter+sum throughput (range filter 10% then sum)",
         "value": v, "unit": "Gvalues/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": f"bounded_walk f64 scale 1e4, sample of {rows} rows of the "
-                               f"{N_ROWS}-row column", "rows": rows, "selectivity": SELECTIVITY},
+        "config": {"workload": "bounded_walk f64 [-500,500] 4 decimals, scale 1e4",
+                   "rows": n, "selectivity": SELECTIVITY, "same_config": True,
+                   "data_device": dev},
+        "check": {"count": cnt, "sum_hex": s.hex()},
         "cpu_baseline": {"value": v, "unit": "Gvalues/s", "cores": threads, "kind": "port",
-                         "sample": f"{rows} rows, {args.steps} timed passes of filter+sum",
-                         "mib_s": mib_s(rows, per_step), "host": host_cpu()},
+                         "sample": f"the full {n}-row column, {args.steps} timed passes of "
+                                   f"filter+sum on {threads} threads",
+                         "mib_s": mib_s(n, per_step), "host": host_cpu(),
+                         "note": "all host threads (the reference itself is single-threaded: "
+                                 "see single_thread)"},
+        "single_thread": {"value": n / one / 1e9, "unit": "Gvalues/s", "cores": 1,
+                          "ms_per_step": one * 1e3, "mib_s": mib_s(n, one),
+                          "note": "the reference-equivalent timing: one core, as the "
+                                  "reference runs"},
         "e2e": {"value": v, "unit": "Gvalues/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -334,7 +387,7 @@ def run_e2e(L, col, img_len, nw, pred, sh, count, res, args):
 
 # ---------------------------------------------------------------- outlier column
 
-def run_small_form(stream):
+def run_small_form(stream, with_cpu=True):
     """The 1,000,000-row CPU-runnable workload (gaussian walk, x0 = 1, steps
     N(0, 0.01), 4 decimals, seed 1, scale 10^4).  Its 3 MB of codes stay in
     L2 between launches, so these times are reported, not headlined."""
@@ -355,6 +408,7 @@ def run_small_form(stream):
     words = torch.empty(nw, dtype=torch.int32, device="cuda")
     cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
     parts = torch.zeros(9, dtype=torch.int64, device="cuda")
+    mx = torch.zeros(1, dtype=torch.int64, device="cuda")
     out = torch.empty(n, dtype=torch.float64, device="cuda")
     peq = float(xh[int(np.random.default_rng(1).integers(0, n))])
     prange = float(np.quantile(xh, 0.9))
@@ -367,12 +421,20 @@ def run_small_form(stream):
                                                             cnt.data_ptr(), sh), 50, stream),
            "equal": time_op(lambda: L.buff_equal_filter(h, peq, words.data_ptr(),
                                                         cnt.data_ptr(), sh), 50, stream),
-           "sum_partials": time_op(lambda: L.buff_sum_partials_async(h, parts.data_ptr(), sh),
-                                   50, stream),
-           "decode": time_op(lambda: L.buff_decode(h, out.data_ptr(), sh), 20, stream)}
+           "sum": time_op(lambda: L.buff_sum_partials_async(h, parts.data_ptr(), sh), 50, stream),
+           "max": time_op(lambda: L.buff_max_async(h, mx.data_ptr(), sh), 50, stream),
+           "decode_full": time_op(lambda: L.buff_decode(h, out.data_ptr(), sh), 20, stream)}
     col.free()
+    table = {k: {"ms": t * 1e3, "gvalues_s": n / t / 1e9} for k, t in ops.items()}
+    cpu = None
+    if with_cpu:
+        cpu = cpu_op_table(xh, 10000, {"range_q90": prange}, peq, (), "all rows, 1 thread")
+        for k, v in cpu["ops"].items():
+            if k in table:
+                table[k]["cpu_1core_gvalues_s"] = v["gvalues_s"]
+                table[k]["cpu_1core_mib_s"] = v["mib_s"]
     return {"workload": "gaussian_walk f64, 1,000,000 rows, seed 1, scale 1e4 (L2-resident)",
-            "ops": {k: {"ms": t * 1e3, "gvalues_s": n / t / 1e9} for k, t in ops.items()}}
+            "ops": table, "cpu_ops": cpu}
 
 
 def run_outlier_form(args, stream, peak):
@@ -840,6 +902,61 @@ def run_serving_form(args, stream, peak):
         bp, bb = best_under(sweep["plain"], slo), best_under(sweep["batched"], slo)
         slo_table.append({"p99_ms_max": slo, "plain_qps": bp, "batched_qps": bb,
                           "ratio": (bb / bp) if (bp and bb) else None})
+    # the same mix with encode requests: new columns from pinned host arrays
+    # (random walks, lengths log-uniform [64K, 1M], 2-6 decimals) admitted
+    # while the queries run, at a rate the batched loop sustains
+    enc_mix = None
+    if not args.no_serve_encode:
+        from buff_gb300.capi import Q_ENCODE
+
+        erng = np.random.default_rng(56)
+        pool, pool_dec = [], []
+        for i in range(32):
+            m = int(np.exp(erng.uniform(np.log(64 << 10), np.log(1 << 20))))
+            d = int(erng.integers(2, 7))
+            v = np.round(np.cumsum(erng.normal(0, 0.1, m)) + erng.uniform(-100, 100), d)
+            t = torch.from_numpy(v).pin_memory()
+            pool.append(t)
+            pool_dec.append(d)
+        rate = 2.0 * plain_max
+        nreq = int(max(2000, min(2e6, rate * dur)))
+        frac = 0.002
+        reqs = _serve_requests(nreq, ncols, samples, dec, rng)
+        is_enc = erng.uniform(size=nreq) < frac
+        pick = erng.integers(0, len(pool), nreq)
+        for i in np.nonzero(is_enc)[0]:
+            t = pool[pick[i]]
+            reqs[i]["ops"] = Q_ENCODE
+            reqs[i]["values"] = t.data_ptr()
+            reqs[i]["n"] = t.numel()
+            reqs[i]["scale"] = 10 ** pool_dec[pick[i]]
+            reqs[i]["precision"] = 0
+        arrivals = np.cumsum(rng.exponential(1e9 / rate, nreq)).astype(np.uint64)
+        srv = Server(budget, max_batch=2048, max_inflight=4, batched=True, auto_release=True,
+                     store_budget_bytes=code_bytes + (8 << 30))
+        for c in cols:
+            srv.add_column(c)
+        srv.start()
+        lat, res, wall = srv.replay(reqs, arrivals, results=True)
+        st = srv.stats()
+        srv.stop()
+        srv.free()
+        ok = all(r.status == 0 for r in res)
+        lq, le = lat[~is_enc] / 1e6, lat[is_enc] / 1e6
+        base = run(True, rate, nreq)
+        enc_mix = {
+            "offered_qps": rate, "requests": nreq, "encodes": int(is_enc.sum()),
+            "encoded_rows": int(sum(pool[pick[i]].numel() for i in np.nonzero(is_enc)[0])),
+            "achieved_qps": nreq / wall, "all_ok": ok,
+            "query_p50_ms": float(np.percentile(lq, 50)), "query_p99_ms": float(np.percentile(lq, 99)),
+            "encode_p50_ms": float(np.percentile(le, 50)) if le.size else None,
+            "encode_p99_ms": float(np.percentile(le, 99)) if le.size else None,
+            "store_bytes_after": st["store_bytes"], "columns_after": st["columns"],
+            "same_rate_without_encodes": {"p50_ms": base["p50_ms"], "p99_ms": base["p99_ms"],
+                                          "achieved_qps": base["achieved_qps"]},
+            "mix": "the request mix above with 0.2% of requests replaced by encodes of pinned "
+                   "host arrays (64K-1M rows) into new resident columns",
+        }
     for c in cols:
         c.free()
     return {
@@ -856,6 +973,7 @@ def run_serving_form(args, stream, peak):
                                     "and that run's p99; batched: highest sustained rate with "
                                     "p99 at or below it"},
         "by_p99_target": slo_table,
+        "with_encodes": enc_mix,
         "latency": "from each request's scheduled arrival to its completion seen by the loop",
     }
 
@@ -1090,13 +1208,41 @@ def main():
             ops["encode"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
                              "gb_s_alg": (16 * n + sum_bytes) / t / 1e9}
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu and not args.free_input:
-        xs = x[:CPU_SAMPLE_ROWS].cpu().numpy()
-        per_step, rows, _, _ = cpu_reference_line(args, xs, pred, 1, 3, 1)
-        cpu = {"value": rows / per_step / 1e9, "unit": "Gvalues/s", "cores": 1, "kind": "port",
-               "sample": f"first {rows} rows of the column, 3 timed passes of filter+sum, "
-                         f"1 thread", "mib_s": mib_s(rows, per_step), "host": host_cpu()}
+    cpu = cpu_all = cpu_ops = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import oracle as O
+
+        # the step on the CPU restatement of the reference, on the same
+        # column's byte image (the GPU image equals the oracle's byte for byte)
+        image = col.serialize()
+        t1, c1, s1 = O.bench_filter_sum(image, SCALE, pred, 1, 2)
+        assert c1 == count and s1 == res.sum, "CPU restatement disagrees with the GPU"
+        per_step = t1 / 2
+        cpu = {"value": n / per_step / 1e9, "unit": "Gvalues/s", "cores": 1, "kind": "port",
+               "sample": f"the full {n}-row column, 2 timed passes of filter+sum, 1 thread",
+               "mib_s": mib_s(n, per_step), "host": host_cpu(),
+               "check": {"count": c1, "sum_hex": s1.hex()}}
+        threads = os.cpu_count() or 1
+        ta, ca, sa = O.bench_filter_sum(image, SCALE, pred, threads, 5)
+        assert ca == count and sa == res.sum
+        cpu_all = {"value": n / (ta / 5) / 1e9, "unit": "Gvalues/s", "cores": threads,
+                   "kind": "port", "ms_per_step": ta / 5 * 1e3,
+                   "note": "not the reference: the reference is single-threaded; rows split "
+                           "over every host thread"}
+        del image
+        if not args.free_input and not args.no_ops:
+            # every operation of the per-op table on one core, on the first
+            # 2^25 rows of the same column (bounded CPU time)
+            xh = x[:CPU_SAMPLE_ROWS].cpu().numpy()
+            rp = {f"range_{sel:g}": float(torch.quantile(xs, 1.0 - sel).item())
+                  for sel in (0.001, 0.01, 0.1, 0.5)}
+            cpu_ops = cpu_op_table(xh, SCALE, rp, peq, (1, 2, 4),
+                                   f"first {xh.size} rows of the column, 1 thread")
+            del xh
+            for name, v in cpu_ops["ops"].items():
+                if name in ops:
+                    ops[name]["cpu_1core_gvalues_s"] = v["gvalues_s"]
+                    ops[name]["cpu_1core_mib_s"] = v["mib_s"]
 
     batched_form = serving_form = outlier_form = small_form = rapg_form = None
     if rank == 0 and world == 1:
@@ -1106,7 +1252,7 @@ def main():
             del x
         torch.cuda.empty_cache()
         if not args.no_ops:
-            small_form = run_small_form(stream)
+            small_form = run_small_form(stream, with_cpu=not args.no_cpu)
         if not args.no_outlier:
             outlier_form = run_outlier_form(args, stream, peak)
             rapg_form = run_rapg_form(args, stream)
@@ -1147,6 +1293,8 @@ def main():
             "gpu_launches": launches,
             "clocks": clk,
             "cpu_baseline": cpu,
+            "cpu_all_threads": cpu_all,
+            "cpu_ops": cpu_ops,
             "ops": ops,
             "encode_once_s": time.time() - t0,
             "gaussian_walk_1e6": small_form,
