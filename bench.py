@@ -437,6 +437,39 @@ def run_small_form(stream, with_cpu=True):
             "ops": table, "cpu_ops": cpu}
 
 
+def filter_alg_bytes(q, t, fixed_len, m, r, is_range=True):
+    """Bytes a byte-sliced filter must touch on a column whose codes are q
+    (device int64, code = quantized value - base) for target code t: slice 0
+    (or, for buff-major, the n/8-byte outlier bitmap of each of the m sparse
+    leading bytes), then for every later slice and the tail the 32-byte
+    sectors of the 32-row blocks that still hold rows equal to the target
+    prefix, and the n/8-byte result bitmap.  (Outlier bytes themselves, about
+    1 % of a sparse byte column, are not counted.)"""
+    import torch
+
+    n = q.numel()
+    nb = (n + 31) // 32
+    pad = nb * 32 - n
+    k = fixed_len // 8
+    total = n / 8  # result words
+    eq = None
+    for j in range(k):
+        sh = fixed_len - 8 * (j + 1)
+        if j < m:
+            total += n / 8
+        elif eq is None:
+            total += n
+        else:
+            total += 32 * int(eq.any(dim=1).sum().item())
+        bj = torch.bitwise_and(torch.bitwise_right_shift(q, sh), 0xFF)
+        e = bj == ((t >> sh) & 0xFF)
+        e = torch.nn.functional.pad(e, (0, pad)).view(nb, 32)
+        eq = e if eq is None else (eq & e)
+    if r and eq is not None:
+        total += 4 * r * int(eq.any(dim=1).sum().item())
+    return total
+
+
 def run_outlier_form(args, stream, peak):
     """67,108,864 rows: 99% N(100, 5) and 1% U(-1e6, 1e6) at seeded random
     positions, 6 decimals (scale 10^6).  The buff-major encode keeps the
@@ -471,20 +504,41 @@ def run_outlier_form(args, stream, peak):
     ops = {"encode": {"ms": t_enc * 1e3, "gvalues_s": n / t_enc / 1e9,
                       "gb_s_input": 8 * n / t_enc / 1e9}}
     h, ph = col.handle, plain.handle
+    dl = info.dlen
+    q = torch.trunc(x * float(1 << dl)).to(torch.int64) - info.base  # codes (exact: |x| <= 1e6)
     for name, p in list(preds.items()) + [("equal", peq)]:
         fn = L.buff_equal_filter_majority if name == "equal" else L.buff_range_filter_majority
         pfn = L.buff_equal_filter if name == "equal" else L.buff_range_filter
         t = time_op(lambda: fn(h, p, words.data_ptr(), cnt.data_ptr(), sh), 10, stream)
         tp = time_op(lambda: pfn(ph, p, words.data_ptr(), cnt.data_ptr(), sh), 10, stream)
-        ops[name] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "plain_layout_ms": tp * 1e3}
+        tc = int(np.trunc(p * float(1 << dl))) - info.base
+        ab = filter_alg_bytes(q, tc, info.fixed_len, info.outlier_cols, info.r)
+        ops[name] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "alg_bytes": ab,
+                     "gb_s_alg": ab / t / 1e9, "frac": ab / t / 1e9 / peak,
+                     "plain_layout_ms": tp * 1e3}
+    del q
     res = capi.SumResult()
-    t = time_op(lambda: L.buff_sum_majority(h, C.byref(res), sh), 5, stream)
-    ops["sum"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "note": "includes the host combine"}
+    dsum = torch.zeros(1, dtype=torch.float64, device="cuda")
+    dmax = torch.zeros(1, dtype=torch.int64, device="cuda")
+    kd = info.k - info.outlier_cols
+    sum_bytes = kd * n + (n * info.r + 7) // 8  # dense slices + tail (+ outlier bytes, ~1%)
+    t = time_op(lambda: L.buff_sum_majority_async(h, dsum.data_ptr(), None, sh), 10, stream)
+    ts = time_op(lambda: L.buff_sum_majority(h, C.byref(res), sh), 5, stream)
+    torch.cuda.synchronize()
+    assert float(dsum.item()).hex() == res.sum.hex()  # the device combine gives the same bits
+    ops["sum"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "gb_s_alg": sum_bytes / t / 1e9,
+                  "frac": sum_bytes / t / 1e9 / peak,
+                  "note": "buff_sum_majority_async (device combine, no host sync)",
+                  "synchronous_call_ms": ts * 1e3}
     mv = C.c_double(0)
     mc = C.c_uint64(0)
-    t = time_op(lambda: L.buff_max_majority(h, C.byref(mv), C.byref(mc), None, None, sh), 5,
-                stream)
-    ops["max"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "note": "one host synchronization"}
+    t = time_op(lambda: L.buff_max_majority_async(h, dmax.data_ptr(), sh), 10, stream)
+    ts = time_op(lambda: L.buff_max_majority(h, C.byref(mv), C.byref(mc), None, None, sh), 5,
+                 stream)
+    torch.cuda.synchronize()
+    assert int(dmax.item()) == mc.value
+    ops["max"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
+                  "note": "buff_max_majority_async (no host sync)", "synchronous_call_ms": ts * 1e3}
     out = {"workload": f"{n} rows: 99% N(100,5), 1% U(-1e6,1e6) at seeded random positions, "
                        f"6 decimals, scale 1e6 (seed 3)", "rows": n,
            "fixed_len": info.fixed_len, "outlier_cols": info.outlier_cols,

@@ -24,7 +24,9 @@ EXPORTED = [
     "buff_encode_f64", "buff_encode_f32", "buff_col_free", "buff_col_free_async",
     "buff_col_get_info",
     "buff_serialize", "buff_deserialize", "buff_decode", "buff_decode_at_precision",
-    "buff_range_filter", "buff_equal_filter", "buff_range_filter_with_slice",
+    "buff_range_filter", "buff_equal_filter", "buff_scalar_range_filter",
+    "buff_scalar_equal_filter", "buff_slice_range_filter_nosimd",
+    "buff_slice_equal_filter_nosimd", "buff_slice_decode_bs", "buff_range_filter_with_slice",
     "buff_equal_filter_with_slice", "buff_sum", "buff_sum_at_precision",
     "buff_sum_partials_async", "buff_sum_finish", "buff_max", "buff_max_async",
     "buff_range_filter_sum", "buff_range_filter_sum_image", "buff_filter_image",
@@ -32,7 +34,8 @@ EXPORTED = [
     "buff_range_filter_noalloc",
     "buff_encode_majority_f64", "buff_encode_majority_f32", "buff_deserialize_majority",
     "buff_decode_majority", "buff_range_filter_majority", "buff_equal_filter_majority",
-    "buff_sum_majority", "buff_max_majority",
+    "buff_sum_majority", "buff_max_majority", "buff_sum_majority_async",
+    "buff_max_majority_async",
     "buff_decode_condition", "buff_major_decode_condition", "buff_decode_selected",
     "buff_range_filter_condition", "buff_range_filter_majority_condition",
     "buff_range_filter_decode",
@@ -156,8 +159,11 @@ def lib(build_if_missing: bool = True):
     L.buff_decode.argtypes = [P, P, P]
     L.buff_decode_at_precision.argtypes = [P, C.c_uint32, P, P]
     for nm in ("buff_range_filter", "buff_equal_filter", "buff_range_filter_with_slice",
-               "buff_equal_filter_with_slice"):
+               "buff_equal_filter_with_slice", "buff_scalar_range_filter",
+               "buff_scalar_equal_filter", "buff_slice_range_filter_nosimd",
+               "buff_slice_equal_filter_nosimd"):
         getattr(L, nm).argtypes = [P, C.c_double, P, P, P]
+    L.buff_slice_decode_bs.argtypes = [P, P, P]
     L.buff_range_filter_noalloc.argtypes = [P, C.c_double, P, P, P]
     L.buff_sum.argtypes = [P, C.POINTER(SumResult), P]
     L.buff_sum_at_precision.argtypes = [P, C.c_uint32, P, P]
@@ -178,6 +184,8 @@ def lib(build_if_missing: bool = True):
     L.buff_equal_filter_majority.argtypes = [P, C.c_double, P, P, P]
     L.buff_sum_majority.argtypes = [P, C.POINTER(SumResult), P]
     L.buff_max_majority.argtypes = [P, P, P, P, P, P]
+    L.buff_sum_majority_async.argtypes = [P, P, P, P]
+    L.buff_max_majority_async.argtypes = [P, P, P]
     L.buff_decode_condition.argtypes = [P, P, C.c_uint64, P, P]
     L.buff_major_decode_condition.argtypes = [P, P, C.c_uint64, P, P, P]
     L.buff_decode_selected.argtypes = [P, P, P, P, P]

@@ -199,6 +199,14 @@ class Column:
     def range_filter_with_slice(self, pred, out=None, stream=None):
         return self._filter(lib().buff_range_filter_with_slice, pred, out, stream)
 
+    def scalar_range_filter(self, pred, out=None, stream=None):
+        """buff_range_filter (buff_simd.rs:4507-4679): every row compared."""
+        return self._filter(lib().buff_scalar_range_filter, pred, out, stream)
+
+    def scalar_equal_filter(self, pred, out=None, stream=None):
+        """buff_equal_filter (buff_simd.rs:4925-5094): every row compared."""
+        return self._filter(lib().buff_scalar_equal_filter, pred, out, stream)
+
     def equal_filter_with_slice(self, pred, out=None, stream=None):
         return self._filter(lib().buff_equal_filter_with_slice, pred, out, stream)
 
@@ -407,6 +415,17 @@ class SliceColumn(Column):
     def equal_filter(self, pred, out=None, stream=None):
         return self._filter(lib().buff_slice_equal_filter, pred, out, stream)
 
+    def range_filter_nosimd(self, pred, out=None, stream=None):
+        return self._filter(lib().buff_slice_range_filter_nosimd, pred, out, stream)
+
+    def equal_filter_nosimd(self, pred, out=None, stream=None):
+        return self._filter(lib().buff_slice_equal_filter_nosimd, pred, out, stream)
+
+    def decode_bs(self, out=None, stream=None):
+        dst = out if out is not None else np.empty(max(self.n, 1), dtype=np.float64)
+        check(lib().buff_slice_decode_bs(self._h, ptr(dst), stream_handle(stream)), "decode_bs")
+        return dst[: self.n] if out is None else dst
+
     def slice_sum(self, any_width: bool = False, stream=None) -> float:
         v = C.c_double(0)
         fn = lib().buff_slice_buffsum if any_width else lib().buff_slice_sum
@@ -510,6 +529,16 @@ class BuffSliceCompress:
 
     def buff_slice_equal_filter(self, data, pred, stream=None) -> FilterResult:
         return self._col(data).equal_filter(pred, stream=stream)
+
+    # buff_slice.rs:1184-1262, :1753-1871, :1873-1991 (the buff-slice-scalar arm)
+    def buff_slice_decode_bs(self, data, stream=None):
+        return self._col(data).decode_bs(stream=stream)
+
+    def buff_slice_range_filter_nosimd(self, data, pred, stream=None) -> FilterResult:
+        return self._col(data).range_filter_nosimd(pred, stream=stream)
+
+    def buff_slice_equal_filter_nosimd(self, data, pred, stream=None) -> FilterResult:
+        return self._col(data).equal_filter_nosimd(pred, stream=stream)
 
     def buff_slice_sum(self, data, stream=None) -> float:
         return self._col(data).slice_sum(False, stream=stream)
@@ -639,6 +668,28 @@ class SplitBDDoubleCompress:
     # compress/buff_simd.rs:3888-4025
     def buff_simd_equal_filter_with_slice(self, data, pred, stream=None) -> FilterResult:
         return _as_column(self, data).equal_filter_with_slice(pred, stream=stream)
+
+    # ---- buff layout (the `buff` profiler arm, buff_simd.rs:167-245) ----
+    # compress/split_double.rs:298-432: the image without the ^0x80 flip
+    def byte_fixed_encode(self, values, stream=None) -> Column:
+        return Column.encode(values, self.scale, self.flags | FLAG_BUFF_LAYOUT, stream)
+
+    # compress/split_double.rs:1243-1350
+    def byte_fixed_decode(self, data, stream=None):
+        return self._buff_layout(data).decode(stream=stream)
+
+    # compress/buff_simd.rs:4507-4679 (the reference prints the count)
+    def buff_range_filter(self, data, pred, stream=None) -> FilterResult:
+        return self._buff_layout(data).scalar_range_filter(pred, stream=stream)
+
+    # compress/buff_simd.rs:4925-5094
+    def buff_equal_filter(self, data, pred, stream=None) -> FilterResult:
+        return self._buff_layout(data).scalar_equal_filter(pred, stream=stream)
+
+    def _buff_layout(self, data) -> Column:
+        if isinstance(data, Column):
+            return data
+        return Column.deserialize(data, self.scale, self.flags | FLAG_BUFF_LAYOUT)
 
     # compress/split_double.rs:2127-2208 (on the unflipped slices)
     def byte_fixed_sum(self, data, stream=None) -> float:

@@ -780,12 +780,48 @@ __device__ __forceinline__ void cp_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-__device__ __forceinline__ void fs_issue(const BQ &q, uint32_t sb, uint32_t r1, uint32_t lane,
-                                         uint32_t nst, uint8_t *slot) {
+// The descriptor fields one filter/sum tile reads, loaded once into
+// registers (the descriptor lives in global memory, and reading its fields
+// inside the step loop would reload them every step).
+struct FsTile {
+  const uint8_t *slices, *tail;
+  unsigned long long stride;
+  uint32_t n, k, r, full_rows, k_used, r_used, ttail, nst;
+  uint32_t t0lo0, t0lo1;  // slice-0 compare constants ((t & 0x7f) [+1]) x 0x01010101
+  unsigned long long tb;  // target bytes of slices 1..7 (byte j-1 = slice j)
+  bool cmp, is_range, th0;
+};
+
+__device__ __forceinline__ FsTile fs_tile(const BQ &q, bool do_f) {
+  FsTile t;
+  t.slices = q.slices;
+  t.tail = q.tail;
+  t.stride = q.stride;
+  t.n = q.n;
+  t.k = q.k;
+  t.r = q.r;
+  t.full_rows = q.full_rows;
+  t.k_used = q.k_used;
+  t.r_used = q.r_used;
+  t.ttail = q.ttail;
+  t.nst = q.k < 3 ? q.k : 3u;  // slices staged; later ones load directly
+  const uint32_t t0 = q.tbyte[0];
+  t.t0lo0 = (t0 & 0x7Fu) * 0x01010101u;
+  t.t0lo1 = t.t0lo0 + 0x01010101u;
+  t.th0 = t0 & 0x80u;
+  t.tb = 0;
+  for (int j = 1; j < 8; ++j) t.tb |= (unsigned long long)q.tbyte[j] << (8 * (j - 1));
+  t.cmp = do_f && q.fill == 0;
+  t.is_range = q.ops & kOpRange;
+  return t;
+}
+
+__device__ __forceinline__ void fs_issue(const FsTile &q, uint32_t sb, uint32_t r1, uint32_t lane,
+                                         uint8_t *slot) {
   if (sb < r1) {
     const uint32_t row0 = sb + lane * 16;
     if (row0 < r1)
-      for (uint32_t j = 0; j < nst; ++j)
+      for (uint32_t j = 0; j < q.nst; ++j)
         cp16(slot + j * 512 + lane * 16, q.slices + j * q.stride + row0);
     if (q.r && lane < 4 * q.r)
       cp16(slot + 3 * 512 + lane * 16, q.tail + (size_t)(sb >> 9) * 64 * q.r + lane * 16);
@@ -793,23 +829,38 @@ __device__ __forceinline__ void fs_issue(const BQ &q, uint32_t sb, uint32_t r1, 
   cp_commit();  // every lane commits one group per step, even an empty one
 }
 
+// Slice-0 compare of 16 rows (four words) against a target byte whose top
+// bit is TH: the rows above it (gt) and equal to it (eq), as 16-bit masks.
+template <bool TH>
+__device__ __forceinline__ void cmp16_t(const uint4 &w, uint32_t lo0, uint32_t lo1, uint32_t &gt,
+                                        uint32_t &eq) {
+  uint32_t g[4], e[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    g[i] = gt4t<TH>(w4(w, i), lo1);
+    e[i] = eq4t<TH>(w4(w, i), lo0, lo1);
+  }
+  gt = gather16(g);
+  eq = gather16(e);
+}
+
 template <bool DO_F>
-__device__ __forceinline__ void tile_fs_async(const BQ &q, uint32_t r0, uint32_t r1,
+__device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_t r1,
                                               uint32_t lane, uint8_t *ring) {
-  const bool is_range = q.ops & kOpRange;
-  const bool cmp = DO_F && q.fill == 0;
-  const uint32_t nst = q.k < 3 ? q.k : 3u;  // slices staged; later ones load directly
+  const FsTile q = fs_tile(qd, DO_F);
+  uint32_t *const words = qd.words;
+  unsigned long long *const acc = qd.acc;
+  const uint32_t fill = qd.fill;
   const unsigned long long pat = q.r > 1 ? every_r(q.r) : 0ull;
   const uint32_t qh0 = q.r > 1 ? (q.r - 64 % q.r) % q.r : 0u;
   uint32_t sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   uint32_t tacc = 0, cnt = 0;
   __syncwarp();  // the ring may still be read by the previous item
 #pragma unroll
-  for (int d = 0; d < kDepth - 1; ++d) fs_issue(q, r0 + d * 512, r1, lane, nst, ring + d * kSlotBytes);
+  for (int d = 0; d < kDepth - 1; ++d) fs_issue(q, r0 + d * 512, r1, lane, ring + d * kSlotBytes);
   uint32_t t = 0;
   for (uint32_t sb = r0; sb < r1; sb += 512, ++t) {
-    fs_issue(q, sb + (kDepth - 1) * 512, r1, lane, nst,
-             ring + ((t + kDepth - 1) % kDepth) * kSlotBytes);
+    fs_issue(q, sb + (kDepth - 1) * 512, r1, lane, ring + ((t + kDepth - 1) % kDepth) * kSlotBytes);
     cp_wait<kDepth - 1>();
     __syncwarp();
     const uint8_t *slot = ring + (t % kDepth) * kSlotBytes;
@@ -822,10 +873,26 @@ __device__ __forceinline__ void tile_fs_async(const BQ &q, uint32_t r0, uint32_t
       eq = valid;
       if (row0 + 16 > q.full_rows)
         eq &= row0 >= q.full_rows ? 0u : ((1u << (q.full_rows - row0)) - 1u);
+      {  // slice 0: sums and the compare
+        const uint4 w = *reinterpret_cast<const uint4 *>(slot + lane * 16);
+        sacc[0] = __dp4a(w.x ^ H, 0x01010101u, sacc[0]);
+        sacc[0] = __dp4a(w.y ^ H, 0x01010101u, sacc[0]);
+        sacc[0] = __dp4a(w.z ^ H, 0x01010101u, sacc[0]);
+        sacc[0] = __dp4a(w.w ^ H, 0x01010101u, sacc[0]);
+        if (q.cmp && q.k_used && eq) {
+          uint32_t g, e;
+          if (q.th0)
+            cmp16_t<true>(w, q.t0lo0, q.t0lo1, g, e);
+          else
+            cmp16_t<false>(w, q.t0lo0, q.t0lo1, g, e);
+          gt = eq & g;
+          eq &= e;
+        }
+      }
 #pragma unroll
-      for (uint32_t j = 0; j < 8; ++j) {
+      for (uint32_t j = 1; j < 8; ++j) {
         if (j >= q.k) break;
-        const bool need_f = cmp && j < q.k_used && eq;
+        const bool need_f = q.cmp && j < q.k_used && eq;
         const uint4 w = j < 3 ? *reinterpret_cast<const uint4 *>(slot + j * 512 + lane * 16)
                               : __ldcs(reinterpret_cast<const uint4 *>(q.slices + j * q.stride + row0));
         sacc[j] = __dp4a(w.x ^ H, 0x01010101u, sacc[j]);
@@ -833,7 +900,7 @@ __device__ __forceinline__ void tile_fs_async(const BQ &q, uint32_t r0, uint32_t
         sacc[j] = __dp4a(w.z ^ H, 0x01010101u, sacc[j]);
         sacc[j] = __dp4a(w.w ^ H, 0x01010101u, sacc[j]);
         if (need_f) {
-          const ByteTarget tg = make_target(q.tbyte[j]);
+          const ByteTarget tg = make_target((uint32_t)(q.tb >> (8 * (j - 1))) & 0xFFu);
           uint32_t g[4], e[4];
 #pragma unroll
           for (int i = 0; i < 4; ++i) cmp4(w4(w, i), tg, g[i], e[i]);
@@ -856,7 +923,7 @@ __device__ __forceinline__ void tile_fs_async(const BQ &q, uint32_t r0, uint32_t
           }
         }
         tacc += fields16_sum(lo, hi, q.r, pat, qh0);
-        if (cmp && q.r_used && eq) {
+        if (q.cmp && q.r_used && eq) {
           uint32_t gtt = 0, eqt = 0, b = eq;
           while (b) {
             const uint32_t i = __ffs(b) - 1;
@@ -871,12 +938,12 @@ __device__ __forceinline__ void tile_fs_async(const BQ &q, uint32_t r0, uint32_t
       }
     }
     if (DO_F) {
-      const uint32_t res = !act ? 0u : q.fill == 1 ? valid : q.fill == 2 ? 0u
-                                                    : (is_range ? gt : eq);
+      const uint32_t res = !act ? 0u : fill == 1 ? valid : fill == 2 ? 0u
+                                                  : (q.is_range ? gt : eq);
       const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
       if (act && !(lane & 1)) {
         const uint32_t word = res | (hi16 << 16);
-        q.words[row0 >> 5] = word;
+        words[row0 >> 5] = word;
         cnt += __popc(word);
       }
     }
@@ -887,15 +954,15 @@ __device__ __forceinline__ void tile_fs_async(const BQ &q, uint32_t r0, uint32_t
   for (uint32_t j = 0; j < 8; ++j) {
     if (j >= q.k) break;
     const unsigned long long sj = warp_sum_ull(sacc[j]);
-    if (lane == 0 && sj) atomicAdd(q.acc + 1 + j, sj);
+    if (lane == 0 && sj) atomicAdd(acc + 1 + j, sj);
   }
   if (q.r) {
     const unsigned long long st = warp_sum_ull(tacc);
-    if (lane == 0 && st) atomicAdd(q.acc + 9, st);
+    if (lane == 0 && st) atomicAdd(acc + 9, st);
   }
   if (DO_F) {
     const unsigned long long sc = warp_sum_ull(cnt);
-    if (lane == 0 && sc) atomicAdd(q.acc, sc);
+    if (lane == 0 && sc) atomicAdd(acc, sc);
   }
 }
 
@@ -1036,12 +1103,24 @@ void class_prepare(int cls, int stage) {
   done[cls][stage].store(true, std::memory_order_release);  // setting it twice is harmless
 }
 
-int class_grid(int cls, const buff_batch_tune &t, uint32_t nitems) {
-  int per_sm = 0;
-  class_prepare(cls, (int)t.stage);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, class_fn(cls, t.stage), kBT,
+// Resident CTAs per SM of a class worker, asked of the runtime once per
+// (class, stage): the query costs microseconds of host time, which every
+// batch of the serving loop would otherwise pay per class.
+int worker_per_sm(int cls, int stage) {
+  static std::atomic<int> cache[kClasses][5];
+  std::atomic<int> &slot = cache[cls][stage];
+  int per_sm = slot.load(std::memory_order_relaxed);
+  if (per_sm) return per_sm;
+  class_prepare(cls, stage);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, class_fn(cls, stage), kBT,
                                                 class_smem(cls));
   if (per_sm < 1) per_sm = 1;
+  slot.store(per_sm, std::memory_order_relaxed);
+  return per_sm;
+}
+
+int class_grid(int cls, const buff_batch_tune &t, uint32_t nitems) {
+  const int per_sm = worker_per_sm(cls, (int)t.stage);
   const int bps = (int)t.blocks_per_sm < per_sm ? (int)t.blocks_per_sm : per_sm;
   int grid = bps * dev_sms();
   const uint32_t need = (nitems + kWarps - 1) / kWarps;

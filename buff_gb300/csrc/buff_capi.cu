@@ -14,6 +14,7 @@
 #include <new>
 #include <vector>
 
+#include "buff_device.cuh"
 #include "buff_internal.h"
 #include "buff_roaring.h"
 #include "buff_snappy.h"
@@ -381,7 +382,14 @@ done:
 
 // ---------------------------------------------------------------- filters
 
-enum FilterKind { kRange = 0, kEqual = 1, kRangeSlice = 2, kEqualSlice = 3 };
+enum FilterKind {
+  kRange = 0,
+  kEqual = 1,
+  kRangeSlice = 2,
+  kEqualSlice = 3,
+  kRangeScalar = 4,  // buff_range_filter (buff_simd.rs:4507-4679): every row
+  kEqualScalar = 5   // buff_equal_filter (buff_simd.rs:4925-5094): every row
+};
 
 // The filter plan of buff_simd_range_filter / _equal_filter and their
 // `_with_slice` forms for a buff-simd column: *action = 0 (no row set),
@@ -389,8 +397,11 @@ enum FilterKind { kRange = 0, kEqual = 1, kRangeSlice = 2, kEqualSlice = 3 };
 // the caller fills in).  Returns BUFF_EREFPANIC where the reference panics.
 int plan_filter(const buff_col *c, double pred, int kind, FilterArgs *a, int *action) {
   const bool intended = c->flags & BUFF_FLAG_INTENDED;
-  const bool is_range = (kind == kRange || kind == kRangeSlice);
+  const bool is_range = (kind == kRange || kind == kRangeSlice || kind == kRangeScalar);
   const bool with_slice = (kind == kRangeSlice || kind == kEqualSlice);
+  // the scalar buff-layout filters read slice 0 byte by byte for every row,
+  // so rows after the last full 32-row block are compared too
+  const bool scalar = (kind == kRangeScalar || kind == kEqualScalar);
   const uint32_t n = c->n;
   *action = 2;
   memset(a, 0, sizeof(*a));
@@ -398,7 +409,7 @@ int plan_filter(const buff_col *c, double pred, int kind, FilterArgs *a, int *ac
   if (fixed_part < c->base) {
     // early return (buff_simd.rs:3385-3388, 3573-3576, 3769-3772, 3919-3922):
     // the printed count is n for range and both fused forms, 0 for equality.
-    *action = (kind == kEqual) ? 0 : 1;
+    *action = (kind == kEqual || kind == kEqualScalar) ? 0 : 1;
     return BUFF_OK;
   }
   const uint64_t t = (uint64_t)(fixed_part - c->base);
@@ -421,7 +432,7 @@ int plan_filter(const buff_col *c, double pred, int kind, FilterArgs *a, int *ac
     }
   } else {
     // byte slices with truncated per-slice targets (buff_simd.rs:3407, 3425, 3448)
-    a->full_rows = n / 32 * 32;
+    a->full_rows = scalar ? n : n / 32 * 32;
     a->k_used = with_slice ? (c->k < 4 ? c->k : 4u) : c->k;
     a->r = c->r;
     for (uint32_t j = 0; j < a->k_used; ++j) a->tbyte[j] = (uint8_t)(t >> (fl - 8 * (j + 1)));
@@ -1118,6 +1129,14 @@ int buff_equal_filter(const buff_col *c, double pred, uint32_t *words, uint64_t 
                       void *stream) {
   return filter_impl(c, pred, words, count, S(stream), kEqual);
 }
+int buff_scalar_range_filter(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                             void *stream) {
+  return filter_impl(c, pred, words, count, S(stream), kRangeScalar);
+}
+int buff_scalar_equal_filter(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
+                             void *stream) {
+  return filter_impl(c, pred, words, count, S(stream), kEqualScalar);
+}
 int buff_range_filter_with_slice(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
                                  void *stream) {
   return filter_impl(c, pred, words, count, S(stream), kRangeSlice);
@@ -1582,51 +1601,54 @@ done:
   return rc;
 }
 
+namespace {
+buffk::dev::MajorSumArgs major_sum_args(const buff_col *c) {
+  buffk::dev::MajorSumArgs a;
+  memset(&a, 0, sizeof(a));
+  a.n = c->n;
+  a.base = c->base;
+  a.m = c->m;
+  a.k = c->k;
+  a.r = c->r;
+  a.fixed_len = c->fixed_len;
+  a.ilen = (int32_t)c->ilen;
+  a.dlen = (int32_t)c->dlen;
+  for (uint32_t i = 0; i < 8; ++i) {
+    a.majors[i] = c->majors[i];
+    a.nout[i] = c->nout[i];
+  }
+  return a;
+}
+
+// The raw byte sums of a buff-major column into d (24 u64, device): sparse
+// columns' outlier bytes at d[0..m), dense slices and tail from d[8].
+int major_raw_sums(const buff_col *c, unsigned long long *d, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 24, s);
+  for (uint32_t col = 0; col < c->m && e == cudaSuccess; ++col)
+    if (c->nout[col]) e = buffk::major_bytesum(c->obytes + c->oofs[col], c->nout[col], d + col, s);
+  if (e == cudaSuccess && c->n) e = buffk::launch_sum(c, c->k - c->m, c->r, d + 8, s);
+  return cuda_status(e);
+}
+}  // namespace
+
 int buff_sum_majority(const buff_col *c, buff_sum_result *out, void *stream) {
   if (!c || !out) return BUFF_EINVAL;
   if (c->layout != 1) return BUFF_ENOTSUP;
   cudaStream_t s = S(stream);
   int rc = BUFF_OK;
   unsigned long long *d = nullptr;
-  uint64_t h[24] = {0};
-  const uint32_t kd = c->k - c->m;
+  unsigned long long h[24] = {0};
   CK(scratch(&d, 24, s));
-  CK(cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 24, s));
-  for (uint32_t col = 0; col < c->m; ++col)
-    if (c->nout[col]) CK(buffk::major_bytesum(c->obytes + c->oofs[col], c->nout[col], d + col, s));
-  if (c->n) CK(buffk::launch_sum(c, kd, c->r, d + 8, s));
+  if ((rc = major_raw_sums(c, d, s))) goto done;
   CK(cudaMemcpyAsync(h, d, sizeof(uint64_t) * 24, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   {
     // buff_sum_majority (buff_simd.rs:2294-2442)
+    const buffk::dev::MajorSumArgs a = major_sum_args(c);
+    unsigned long long parts[9] = {0};
     memset(out, 0, sizeof(*out));
-    uint64_t parts[9] = {0};
-    uint32_t np = 0;
-    for (uint32_t col = 0; col < c->m; ++col)
-      parts[np++] = h[col] + (uint64_t)c->majors[col] * ((uint64_t)c->n - c->nout[col]);
-    for (uint32_t j = 0; j < kd; ++j) parts[np++] = h[8 + j];
-    if (c->r) parts[np++] = h[8 + kd];
-    const int32_t ilen_i = (int32_t)c->ilen;
-    double sum_base = (double)c->n * (double)c->base;
-    sum_base = sum_base / ldexp(1.0, (int)c->dlen);
-    double sum = 0.0;
-    int32_t processed = 0;
-    uint32_t remain = c->fixed_len;
-    bool no_base = false;
-    for (uint32_t i = 0; i < c->k; ++i) {
-      remain -= 8;
-      processed += 8;
-      sum = sum + (double)parts[i] / ldexp(1.0, processed - ilen_i);
-      if (i >= c->m && remain == 0) no_base = true;  // a dense slice ends the code
-    }
-    if (!no_base) {
-      if (remain > 0) {
-        processed += (int32_t)remain;
-        sum = sum + (double)parts[c->k] / ldexp(1.0, processed - ilen_i);
-      }
-      sum += sum_base;
-    }
-    out->sum = sum;
+    const uint32_t np = buffk::dev::major_sum_parts(a, h, parts);
+    out->sum = buffk::dev::major_sum_f64(a, parts);
     __int128 acc = (__int128)c->n * (__int128)c->base;
     for (uint32_t j = 0; j < c->k; ++j) acc += (__int128)parts[j] << (c->fixed_len - 8 * (j + 1));
     if (c->r) acc += (__int128)parts[c->k];
@@ -1636,6 +1658,22 @@ int buff_sum_majority(const buff_col *c, buff_sum_result *out, void *stream) {
     out->n_partials = np;
     for (uint32_t j = 0; j < np; ++j) out->partials[j] = parts[j];
   }
+done:
+  if (d) cudaFreeAsync(d, s);
+  return rc;
+}
+
+int buff_sum_majority_async(const buff_col *c, double *dev_sum, uint64_t *dev_partials,
+                            void *stream) {
+  if (!c || !dev_sum) return BUFF_EINVAL;
+  if (c->layout != 1) return BUFF_ENOTSUP;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  unsigned long long *d = nullptr;
+  CK(scratch(&d, 24, s));
+  if ((rc = major_raw_sums(c, d, s))) goto done;
+  CK(buffk::major_sum_combine(major_sum_args(c), d, dev_sum,
+                              reinterpret_cast<unsigned long long *>(dev_partials), s));
 done:
   if (d) cudaFreeAsync(d, s);
   return rc;
@@ -1665,6 +1703,26 @@ int buff_max_majority(const buff_col *c, double *max_value, uint64_t *max_code,
   if (max_value)
     *max_value = (double)(int64_t)((uint64_t)c->base + res[0]) / ldexp(1.0, (int)c->dlen);
   if (argmax_count) *argmax_count = res[1];
+done:
+  if (cand) cudaFreeAsync(cand, s);
+  if (st) cudaFreeAsync(st, s);
+  return rc;
+}
+
+int buff_max_majority_async(const buff_col *c, uint64_t *dev_max_code, void *stream) {
+  if (!c || !dev_max_code) return BUFF_EINVAL;
+  if (c->layout != 1) return BUFF_ENOTSUP;
+  cudaStream_t s = S(stream);
+  int rc = BUFF_OK;
+  uint32_t *cand = nullptr;
+  unsigned char *st = nullptr;
+  const size_t sb = buffk::major_max_state_bytes(), mo = buffk::major_max_state_mx_offset();
+  if (!c->n) return cuda_status(cudaMemsetAsync(dev_max_code, 0, 8, s));
+  CK(scratch(&cand, c->nwp, s));
+  CK(scratch(&st, sb, s));
+  CK(buffk::launch_fill_words(cand, c->n, 0xFFFFFFFFu, nullptr, s));
+  CK(buffk::major_max(c, cand, st, s));
+  CK(cudaMemcpyAsync(dev_max_code, st + mo, 8, cudaMemcpyDeviceToDevice, s));
 done:
   if (cand) cudaFreeAsync(cand, s);
   if (st) cudaFreeAsync(st, s);
@@ -2415,9 +2473,11 @@ namespace {
 // buff_slice_range_filter / buff_slice_equal_filter (buff_slice.rs:1348-1751):
 // target byte per slice (`t >> (fl - 8(j+1))`, or `t << pad` for the padded
 // last slice), at most 4 slices, rows of full 32-row blocks only; a target
-// below the base prints n for both.
+// below the base prints n for both.  nosimd: the row-by-row forms
+// buff_slice_range_filter_nosimd / _equal_filter_nosimd (:1753-1991), the
+// same compare over every row.
 int slice_filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
-                      cudaStream_t s, bool is_range) {
+                      cudaStream_t s, bool is_range, bool nosimd = false) {
   if (!c || (!words && c->n > 0)) return BUFF_EINVAL;
   if (c->layout != 2) return BUFF_ENOTSUP;
   const uint32_t n = c->n, nw = (n + 31) / 32;
@@ -2432,7 +2492,8 @@ int slice_filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t 
   buffk::FilterArgs a;
   memset(&a, 0, sizeof(a));
   if (!early) {
-    if (fl == 0 || n < 32) return BUFF_EREFPANIC;  // ceil(0, 8) / `len - 32` underflow
+    if (fl == 0) return BUFF_EREFPANIC;                // ceil(0, 8) underflows
+    if (!nosimd && n < 32) return BUFF_EREFPANIC;  // `len - 32` underflows
     const uint64_t t = (uint64_t)(fp - c->base);
     a.slices = c->slices;
     a.stride = c->stride;
@@ -2441,7 +2502,7 @@ int slice_filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t 
     a.is_range = is_range ? 1u : 0u;
     a.k_used = c->k < 4 ? c->k : 4u;
     a.r = 0;
-    a.full_rows = n / 32 * 32;
+    a.full_rows = nosimd ? n : n / 32 * 32;
     for (uint32_t j = 0; j < a.k_used; ++j)
       a.tbyte[j] = (fl >= 8 * (j + 1)) ? (uint8_t)(t >> (fl - 8 * (j + 1)))
                                        : (uint8_t)(t << ((8 * (j + 1) - fl) & 63));
@@ -2574,6 +2635,25 @@ int buff_slice_range_filter(const buff_col *c, double pred, uint32_t *words, uin
 int buff_slice_equal_filter(const buff_col *c, double pred, uint32_t *words, uint64_t *count,
                             void *stream) {
   return slice_filter_impl(c, pred, words, count, S(stream), false);
+}
+
+int buff_slice_range_filter_nosimd(const buff_col *c, double pred, uint32_t *words,
+                                   uint64_t *count, void *stream) {
+  return slice_filter_impl(c, pred, words, count, S(stream), true, true);
+}
+
+int buff_slice_equal_filter_nosimd(const buff_col *c, double pred, uint32_t *words,
+                                   uint64_t *count, void *stream) {
+  return slice_filter_impl(c, pred, words, count, S(stream), false, true);
+}
+
+int buff_slice_decode_bs(const buff_col *c, double *out, void *stream) {
+  if (!c || (!out && c->n)) return BUFF_EINVAL;
+  if (c->layout != 2) return BUFF_ENOTSUP;
+  // `match num { 1..=4 => ..., _ => panic!(..) }`: ceil(0, 8) underflows
+  const uint32_t fl = c->fixed_len - c->pad;
+  if (fl == 0 || c->k > 4) return BUFF_EREFPANIC;
+  return buff_slice_decode(c, out, stream);
 }
 
 int buff_slice_sum(const buff_col *c, double *sum, void *stream) {

@@ -6,7 +6,9 @@
 
 #include <cuda_runtime.h>
 #include <limits.h>
+#include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 namespace buffk {
 namespace dev {
@@ -230,18 +232,24 @@ __device__ __forceinline__ uint32_t eq4t(uint32_t w, uint32_t lo0, uint32_t lo1)
 }
 
 // Weighted popcount of one 32-bit word of a packed stream of `ts`-bit fields
-// whose first bit sits at stream bit `bit0`: sum over set bits b of
-// 2^((bit0 + b) mod ts).  (The sum of all fields of a stream only depends on
-// each bit's position mod ts, not on row boundaries.)
-__device__ __forceinline__ uint32_t wpopc(uint32_t w, uint32_t bit0, uint32_t ts) {
+// whose first bit sits at a stream bit of residue `phase` (= its position
+// mod ts, < ts): sum over set bits b of 2^((phase + b) mod ts).  (The sum of
+// all fields of a stream only depends on each bit's position mod ts, not on
+// row boundaries.)
+__device__ __forceinline__ uint32_t wpopc(uint32_t w, uint32_t phase, uint32_t ts) {
   if (ts == 1) return __popc(w);
-  uint32_t pat = 0;  // bits 0, ts, 2ts, ...
-  for (uint32_t j = 0; j < 32; j += ts) pat |= 1u << j;
-  const uint32_t phase = bit0 % ts;
+  // bits 0, ts, 2ts, ... of a word (ts = 2..7)
+  const uint32_t pat = ts == 2 ? 0x55555555u : ts == 3 ? 0x49249249u : ts == 4 ? 0x11111111u
+                     : ts == 5 ? 0x42108421u : ts == 6 ? 0x41041041u : 0x10204081u;
+  // bits of class c (index = c mod ts) weigh 2^((phase + c) mod ts); phase < ts
   uint32_t acc = 0;
-  for (uint32_t p = 0; p < ts; ++p) {
-    const uint32_t sh = (p + ts - phase) % ts;  // bits j with (phase + j) % ts == p
-    acc += (uint32_t)__popc(w & (pat << sh)) << p;
+#pragma unroll
+  for (uint32_t c = 0; c < 7; ++c) {
+    if (c < ts) {
+      uint32_t sh = phase + c;
+      if (sh >= ts) sh -= ts;
+      acc += (uint32_t)__popc(w & (pat << c)) << sh;
+    }
   }
   return acc;
 }
@@ -362,6 +370,71 @@ static __device__ __noinline__ unsigned long long max_in_block(const uint8_t *__
     bt = max(bt, __funnelshift_r(w0, w1, bit & 31) & ((1u << r) - 1u));
   }
   return (prefix << r) | bt;
+}
+
+// buff_sum_majority's combine (compress/buff_simd.rs:2294-2442), shared by
+// the host call and the device-only form so both give the same bits: the
+// per-byte partials (a sparse column's outlier byte sum plus its major byte
+// times its other rows, then the dense slices, then the tail) scaled slice
+// by slice in the reference's order; the base term is left out when a dense
+// slice ends the code (Q5).
+struct MajorSumArgs {
+  uint64_t n;
+  int64_t base;
+  uint32_t m, k, r, fixed_len;
+  int32_t ilen, dlen;
+  uint8_t majors[8];
+  uint32_t nout[8];
+};
+
+// raw: sparse byte sums at raw[0..m), dense and tail sums at raw[8..8+k-m+1).
+// parts receives k (+1 with a tail) partials; returns their count.
+__host__ __device__ inline uint32_t major_sum_parts(const MajorSumArgs &a,
+                                                    const unsigned long long *raw,
+                                                    unsigned long long *parts) {
+  uint32_t np = 0;
+  for (uint32_t c = 0; c < a.m; ++c)
+    parts[np++] = raw[c] + (unsigned long long)a.majors[c] * (a.n - a.nout[c]);
+  const uint32_t kd = a.k - a.m;
+  for (uint32_t j = 0; j < kd; ++j) parts[np++] = raw[8 + j];
+  if (a.r) parts[np++] = raw[8 + kd];
+  return np;
+}
+
+// 2^e as a double, built from its exponent field (-1022 <= e <= 1023).
+__host__ __device__ inline double pow2_exact(int e) {
+  const unsigned long long bits = (unsigned long long)(e + 1023) << 52;
+  double d;
+  memcpy(&d, &bits, sizeof(d));
+  return d;
+}
+
+// x / 2^e of the reference, as x * 2^-e: scaling by a power of two is exact,
+// so both round the same real number and give the same bits.
+__host__ __device__ inline double div_pow2(double x, int e) { return x * pow2_exact(-e); }
+
+__host__ __device__ inline double major_sum_f64(const MajorSumArgs &a,
+                                                const unsigned long long *parts) {
+  double sum_base = (double)a.n * (double)a.base;
+  sum_base = div_pow2(sum_base, a.dlen);
+  double sum = 0.0;
+  int32_t processed = 0;
+  uint32_t remain = a.fixed_len;
+  bool no_base = false;
+  for (uint32_t i = 0; i < a.k; ++i) {
+    remain -= 8;
+    processed += 8;
+    sum = sum + div_pow2((double)parts[i], processed - a.ilen);
+    if (i >= a.m && remain == 0) no_base = true;  // a dense slice ends the code
+  }
+  if (!no_base) {
+    if (remain > 0) {
+      processed += (int32_t)remain;
+      sum = sum + div_pow2((double)parts[a.k], processed - a.ilen);
+    }
+    sum += sum_base;
+  }
+  return sum;
 }
 
 }  // namespace dev

@@ -84,6 +84,9 @@ int encode_admitted(const void *values, int is_f32, uint64_t n, uint64_t scale, 
 }  // namespace buffh
 
 namespace buffk {
+namespace dev {
+struct MajorSumArgs;
+}
 
 constexpr uint32_t kRowChunk = 512;  // rows one warp covers per step (32 lanes x 16 rows)
 
@@ -174,6 +177,11 @@ cudaError_t exclusive_scan(uint32_t *data, size_t count, uint32_t *tmp, cudaStre
 cudaError_t step_ranks(const uint32_t *words, uint32_t n, uint32_t *rank, cudaStream_t s);
 cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out,
                           cudaStream_t s);
+// buff_sum_majority's combine on the device (one thread): the raw sums
+// (sparse columns at raw[0..m), dense slices and tail from raw[8]) into the
+// f64 sum and, when parts is not null, the k (+1) partials.
+cudaError_t major_sum_combine(const dev::MajorSumArgs &a, const unsigned long long *raw,
+                              double *sum, unsigned long long *parts, cudaStream_t s);
 // buff_max_majority's progressive max on the device: cand (nwp words) ends
 // as the arg-max bitmap; state_dev (major_max_state_bytes(), device) holds
 // the max code (u64 at major_max_state_mx_offset()) and, after it, the

@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <mutex>
 #include <type_traits>
 
 #include "buff_device.cuh"
@@ -457,10 +458,17 @@ __global__ void __launch_bounds__(kThreads) k_sum(const uint8_t *__restrict__ sl
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t nth = gridDim.x * blockDim.x;
   const uint32_t nv = (uint32_t)(stride / 16);
+  // A slice rarely divides evenly into grid-stride steps, so some threads
+  // take one step more than the others.  Each slice (and the tail) starts the
+  // threads at a different offset (whole warps), so no thread takes the
+  // extra step in every slice: the kernel ends when the average thread does.
+  const uint32_t rot = (nth / (ks + 1)) & ~31u;
   for (uint32_t s = 0; s < ks; ++s) {
     const uint8_t *sl = slices + (size_t)s * stride;
     uint32_t acc = 0;
-    for (uint32_t v0 = tid; v0 < nv; v0 += kU * nth) {
+    uint32_t vt = tid + s * rot;
+    if (vt >= nth) vt -= nth;
+    for (uint32_t v0 = vt; v0 < nv; v0 += kU * nth) {
       uint4 d[kU];
 #pragma unroll
       for (int u = 0; u < kU; ++u) {
@@ -482,9 +490,18 @@ __global__ void __launch_bounds__(kThreads) k_sum(const uint8_t *__restrict__ sl
     const unsigned long long nbytes = (tail_bits + 7) / 8;
     const uint32_t ntv = (uint32_t)((nbytes + 15) / 16);
     unsigned long long acc = 0;
-    for (uint32_t v = tid; v < ntv; v += nth) {
+    uint32_t vt = tid + ks * rot;
+    if (vt >= nth) vt -= nth;
+    // A word starting at stream bit b0 has phase b0 mod ts (wpopc); the
+    // phases are advanced by conditional subtraction, without a division in
+    // the loop.
+    const uint32_t c32 = 32 % ts;                                            // phase step per word
+    const uint32_t cstep = (uint32_t)(((unsigned long long)nth * 128) % ts);  // per grid step
+    uint32_t pv = (uint32_t)(((unsigned long long)vt * 128) % ts);
+    for (uint32_t v = vt; v < ntv; v += nth) {
       uint4 d = *reinterpret_cast<const uint4 *>(tail + (size_t)v * 16);
       const uint32_t *w = reinterpret_cast<const uint32_t *>(&d);
+      uint32_t ph = pv;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const unsigned long long b0 = (unsigned long long)v * 128 + 32 * q;
@@ -493,8 +510,12 @@ __global__ void __launch_bounds__(kThreads) k_sum(const uint8_t *__restrict__ sl
           word = 0;
         else if (b0 + 32 > tail_bits)
           word &= (1u << (uint32_t)(tail_bits - b0)) - 1u;
-        acc += wpopc(word, (uint32_t)(b0 % ts), ts);
+        acc += wpopc(word, ph, ts);
+        ph += c32;
+        if (ph >= ts) ph -= ts;
       }
+      pv += cstep;
+      if (pv >= ts) pv -= ts;
     }
     acc = warp_sum_ull(acc);
     if (lane == 0 && acc) atomicAdd(&s_acc[8], acc);
@@ -598,9 +619,13 @@ __global__ void __launch_bounds__(kThreads) k_filter_sum(FilterArgs a, uint32_t 
     const unsigned long long nbytes = (tail_bits + 7) / 8;
     const uint32_t ntv = (uint32_t)((nbytes + 15) / 16);
     unsigned long long acc = 0;
+    const uint32_t c32 = 32 % ts;
+    const uint32_t cstep = (uint32_t)(((unsigned long long)nth * 128) % ts);
+    uint32_t pv = (uint32_t)(((unsigned long long)tid * 128) % ts);  // phase of word 0 of v
     for (uint32_t v = tid; v < ntv; v += nth) {
       uint4 d = *reinterpret_cast<const uint4 *>(a.tail + (size_t)v * 16);
       const uint32_t *w = reinterpret_cast<const uint32_t *>(&d);
+      uint32_t ph = pv;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const unsigned long long b0 = (unsigned long long)v * 128 + 32 * q;
@@ -609,8 +634,12 @@ __global__ void __launch_bounds__(kThreads) k_filter_sum(FilterArgs a, uint32_t 
           word = 0;
         else if (b0 + 32 > tail_bits)
           word &= (1u << (uint32_t)(tail_bits - b0)) - 1u;
-        acc += wpopc(word, (uint32_t)(b0 % ts), ts);
+        acc += wpopc(word, ph, ts);
+        ph += c32;
+        if (ph >= ts) ph -= ts;
       }
+      pv += cstep;
+      if (pv >= ts) pv -= ts;
     }
     acc = warp_sum_ull(acc);
     if (lane == 0 && acc) atomicAdd(&s_acc[8], acc);
@@ -648,6 +677,7 @@ __global__ void __launch_bounds__(kThreads) k_filter_sum_il(FilterArgs a, uint32
   const uint32_t t0 = (uint32_t)(tb & 0xFFu);
   const uint32_t lo0 = (t0 & 0x7Fu) * 0x01010101u, lo1 = ((t0 & 0x7Fu) + 1u) * 0x01010101u;
   const bool deep = a.k_used > 1 || a.r;
+  const uint32_t c32 = ts ? 32 % ts : 0u;  // phase step of one tail word
   uint32_t acc[KS];
 #pragma unroll
   for (int s = 0; s < KS; ++s) acc[s] = 0;
@@ -667,6 +697,7 @@ __global__ void __launch_bounds__(kThreads) k_filter_sum_il(FilterArgs a, uint32
     for (int s = 0; s < KS; ++s)
 #pragma unroll
       for (int q = 0; q < 8; ++q) acc[s] = __dp4a(d[s].w[q] ^ H, 0x01010101u, acc[s]);
+    uint32_t ph = 0;  // a block's tail starts at a stream bit that is a multiple of ts
 #pragma unroll
     for (int q = 0; q < 7; ++q) {
       if (q < (int)ts) {
@@ -676,7 +707,9 @@ __global__ void __launch_bounds__(kThreads) k_filter_sum_il(FilterArgs a, uint32
           word = 0;
         else if (b0 + 32 > tail_bits)
           word &= (1u << (uint32_t)(tail_bits - b0)) - 1u;
-        tacc += wpopc(word, (uint32_t)((32u * q) % ts), ts);
+        tacc += wpopc(word, ph, ts);
+        ph += c32;
+        if (ph >= ts) ph -= ts;
       }
     }
     if (blk >= nwords) continue;  // padding blocks: summed (zero bytes), never filtered
@@ -1040,10 +1073,34 @@ __global__ void __launch_bounds__(kThreads) k_decode4(const uint8_t *__restrict_
   }
 }
 
+// Resident CTAs per SM of a kernel, asked of the runtime once per (kernel,
+// threads, shared memory) and kept: the occupancy query costs microseconds
+// of host time, which a small column's launch would otherwise pay every call.
 int grid_for(const void *fn, int threads, size_t smem, int device) {
+  struct Entry {
+    const void *fn;
+    int threads;
+    size_t smem;
+    int per_sm;
+  };
+  static Entry table[256];
+  static int used = 0;
+  static std::mutex mu;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
-  if (per_sm < 1) per_sm = 1;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    for (int i = 0; i < used; ++i)
+      if (table[i].fn == fn && table[i].threads == threads && table[i].smem == smem) {
+        per_sm = table[i].per_sm;
+        break;
+      }
+  }
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+    if (per_sm < 1) per_sm = 1;
+    std::lock_guard<std::mutex> lk(mu);
+    if (used < 256) table[used++] = Entry{fn, threads, smem, per_sm};
+  }
   return per_sm * num_sms(device);
 }
 

@@ -287,13 +287,192 @@ __global__ void __launch_bounds__(kThreads) k_filter_major(MajorArgs a) {
   }
 }
 
+// The rest of one block's compare after its leading byte and first two dense
+// bytes: the later dense slices (from slice index j0) while rows still equal
+// the target prefix, then the packed tail.  Returns the block's bitmap word.
+template <bool IS_RANGE>
+__device__ __forceinline__ uint32_t finish_block(const MajorArgs &a, uint32_t row0, uint32_t j0,
+                                                 uint32_t gt, uint32_t eq) {
+  for (uint32_t j = j0; j < a.kd && eq; ++j) {
+    const Bytes32 dj = ld_cand32(a.slices + j * a.stride + row0);
+    const ByteTarget tj = make_target(a.tbyte[1 + j]);
+    uint32_t g[8], e[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) cmp4(dj.w[q], tj, g[q], e[q]);
+    gt |= eq & gather32(g);
+    eq &= gather32(e);
+  }
+  if (a.r && eq) {
+    const uint32_t *tp = reinterpret_cast<const uint32_t *>(a.tail + (size_t)(row0 >> 5) * 4 * a.r);
+    uint32_t tw[8];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) tw[i] = (uint32_t)i < a.r ? __ldg(tp + i) : 0u;
+    tw[7] = 0;
+    uint32_t gtt = 0, eqt = 0;
+    for (uint32_t i = 0; i < 32; ++i) {
+      if (!(eq >> i & 1u)) continue;
+      const uint32_t bit = i * a.r, wi = bit >> 5;
+      const uint32_t f = __funnelshift_r(tw[wi], tw[wi + 1], bit & 31) & ((1u << a.r) - 1u);
+      gtt |= (uint32_t)(f > a.ttail) << i;
+      eqt |= (uint32_t)(f == a.ttail) << i;
+    }
+    gt |= eq & gtt;
+    eq &= eqt;
+    return IS_RANGE ? gt : eq;
+  }
+  return IS_RANGE ? gt : 0u;  // equality only sets rows in the tail step
+}
+
+// The same filters for one sparse column whose major byte equals the
+// target's leading byte -- a predicate inside the bulk of the values, where
+// every non-outlier row stays a candidate for the dense slices.  Those rows
+// stream like the plain filter (lane = 32 rows): the bitmap word, its
+// outlier rank and 32 bytes of the first dense slice are loaded together,
+// and the second dense slice with them while most lanes of the warp needed
+// it in its previous step; outlier rows enter the compare with their own
+// leading byte.  Blocks that still hold rows equal to the target after two
+// dense bytes are queued per warp and refined 32 at a time, one per lane,
+// so the later slices are compared with every lane busy instead of by the
+// few lanes of each step that need them.  Results are those of
+// k_filter_major.
+template <bool IS_RANGE, bool TH1, bool TH2>
+__global__ void __launch_bounds__(kThreads, 4) k_filter_major1(MajorArgs a) {
+  constexpr int kQ = 64;  // queue entries per warp
+  __shared__ uint32_t s_q[kThreads / 32][3][kQ];
+  const uint32_t lane = threadIdx.x & 31;
+  uint32_t(*q)[kQ] = s_q[threadIdx.x >> 5];
+  const uint32_t nwords = (a.n + 31) / 32;
+  const uint32_t T = a.tbyte[0];
+  // per-byte compare constants of the first two dense target bytes, whose
+  // top bits are the template arguments
+  const uint32_t a0 = (a.tbyte[1] & 0x7Fu) * 0x01010101u, a1 = a0 + 0x01010101u;
+  const uint32_t b0 = (a.tbyte[2] & 0x7Fu) * 0x01010101u, b1 = b0 + 0x01010101u;
+  const uint8_t *ob0 = a.obytes + a.oofs[0];
+  const uint8_t *s1 = a.slices + a.stride;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const bool two = a.kd >= 2;
+  const bool deep = a.kd >= 3 || a.r;  // levels after the second dense byte
+  bool pre = two;  // warp-uniform: load the second dense slice with the first
+  uint32_t qn = 0;  // warp-uniform queue length
+  uint32_t cnt = 0;
+  for (uint32_t base = warp * 32; base < nwords; base += nwarps * 32) {
+    const uint32_t w = base + lane;
+    const bool live = w < nwords;
+    uint32_t B = 0, R = 0;
+    Bytes32 d0, d1;
+    if (live) {
+      B = __ldg(a.obits + w);
+      R = __ldg(a.orank + w);
+      d0 = ld_stream32(a.slices + (size_t)w * 32);
+      if (pre) d1 = ld_stream32(s1 + (size_t)w * 32);
+    }
+    const uint32_t row0 = w * 32;
+    const uint32_t valid =
+        !live ? 0u : (a.n - row0 >= 32 ? 0xFFFFFFFFu : ((1u << (a.n - row0)) - 1u));
+    uint32_t gt = 0, eq = ~B & valid;  // leading byte: major == target for non-outliers
+    for (uint32_t b = B, k = 0; b; ++k) {
+      const uint32_t j = __ffs(b) - 1;
+      b &= b - 1;
+      const uint32_t v = __ldg(ob0 + R + k);
+      gt |= (uint32_t)(v > T) << j;
+      eq |= (uint32_t)(v == T) << j;
+    }
+    gt &= valid;
+    eq &= valid;
+    {
+      uint32_t m[8];
+#pragma unroll
+      for (int qq = 0; qq < 8; ++qq) m[qq] = eq4t<TH1>(d0.w[qq], a0, a1);
+      const uint32_t e = gather32(m);
+      if (IS_RANGE) {
+#pragma unroll
+        for (int qq = 0; qq < 8; ++qq) m[qq] = gt4t<TH1>(d0.w[qq], a1);
+        gt |= eq & gather32(m);
+      }
+      eq &= e;
+    }
+    const bool need1 = two && eq != 0;
+    const uint32_t vote = __ballot_sync(0xFFFFFFFFu, need1);
+    if (need1) {
+      if (!pre) d1 = ld_cand32(s1 + row0);
+      uint32_t m[8];
+#pragma unroll
+      for (int qq = 0; qq < 8; ++qq) m[qq] = eq4t<TH2>(d1.w[qq], b0, b1);
+      const uint32_t e = gather32(m);
+      if (IS_RANGE) {
+#pragma unroll
+        for (int qq = 0; qq < 8; ++qq) m[qq] = gt4t<TH2>(d1.w[qq], b1);
+        gt |= eq & gather32(m);
+      }
+      eq &= e;
+    }
+    pre = two && __popc(vote) >= 16;
+    // blocks with rows still equal to the target go to the queue
+    const bool more = live && deep && eq != 0;
+    const uint32_t qv = __ballot_sync(0xFFFFFFFFu, more);
+    if (more) {
+      const uint32_t at = qn + __popc(qv & ((1u << lane) - 1u));
+      q[0][at] = w;
+      q[1][at] = gt;
+      q[2][at] = eq;
+    } else if (live) {
+      const uint32_t res = IS_RANGE ? gt : ((a.r == 0 || !eq) ? 0u : eq);
+      __stcs(a.words + w, res);
+      cnt += __popc(res);
+    }
+    qn += __popc(qv);
+    __syncwarp();
+    if (qn >= 32) {  // refine 32 queued blocks, one per lane
+      qn -= 32;
+      const uint32_t qw = q[0][qn + lane], qg = q[1][qn + lane], qe = q[2][qn + lane];
+      __syncwarp();
+      const uint32_t res = finish_block<IS_RANGE>(a, qw * 32, two ? 2u : 1u, qg, qe);
+      __stcs(a.words + qw, res);
+      cnt += __popc(res);
+    }
+  }
+  if (lane < qn) {  // what is left in the queue
+    const uint32_t qw = q[0][lane];
+    const uint32_t res = finish_block<IS_RANGE>(a, qw * 32, two ? 2u : 1u, q[1][lane], q[2][lane]);
+    __stcs(a.words + qw, res);
+    cnt += __popc(res);
+  }
+  if (a.count) {
+    const unsigned long long c = warp_sum_ull(cnt);
+    if (lane == 0 && c) atomicAdd(a.count, c);
+  }
+}
+
 // ---------------------------------------------------------------- sum / max helpers
 
+// Sum of nbytes bytes from p (any alignment): the bytes before the first
+// 16-byte boundary and after the last one singly, the rest as 16-byte
+// vectors through dp4a.
 __global__ void k_bytesum(const uint8_t *__restrict__ p, size_t nbytes, unsigned long long *out) {
+  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t nth = (size_t)gridDim.x * blockDim.x;
+  size_t head = (16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15;
+  if (head > nbytes) head = nbytes;
+  const size_t nvec = (nbytes - head) / 16;
+  const uint8_t *body = p + head;
   unsigned long long acc = 0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nbytes;
-       i += (size_t)gridDim.x * blockDim.x)
-    acc += p[i];
+  uint32_t part = 0;
+  for (size_t v = tid; v < nvec; v += nth) {
+    const uint4 d = __ldg(reinterpret_cast<const uint4 *>(body + v * 16));
+    part = __dp4a(d.x, 0x01010101u, part);
+    part = __dp4a(d.y, 0x01010101u, part);
+    part = __dp4a(d.z, 0x01010101u, part);
+    part = __dp4a(d.w, 0x01010101u, part);
+    if (part >= 0xF0000000u) {  // keep the 32-bit partial far from overflow
+      acc += part;
+      part = 0;
+    }
+  }
+  acc += part;
+  const size_t rest = head + nvec * 16;  // bytes before `rest` not in vectors: [0, head)
+  if (tid < head) acc += p[tid];
+  for (size_t i = rest + tid; i < nbytes; i += nth) acc += p[i];
   acc = warp_sum_ull(acc);
   if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
 }
@@ -1025,6 +1204,28 @@ cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, 
   a.words = words;
   a.count = count;
   const size_t nw = (c->n + 31) / 32;
+  if (c->m == 1 && !cand && a.kd >= 1 && c->majors[0] == tbyte[0]) {
+    // one wave: 4 resident CTAs per SM (the kernel's launch bounds), fewer
+    // when the column needs fewer warps
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const size_t need = (nw + kThreads - 1) / kThreads;
+    const size_t cap = (size_t)4 * num_sms(dev);
+    const int grid = (int)(need < cap ? (need ? need : 1) : cap);
+    const int th = (a.tbyte[1] >> 7) | ((a.kd >= 2 ? a.tbyte[2] >> 7 : 0) << 1);
+    void (*fn)(MajorArgs);
+    if (is_range)
+      fn = th == 0 ? k_filter_major1<true, false, false>
+         : th == 1 ? k_filter_major1<true, true, false>
+         : th == 2 ? k_filter_major1<true, false, true> : k_filter_major1<true, true, true>;
+    else
+      fn = th == 0 ? k_filter_major1<false, false, false>
+         : th == 1 ? k_filter_major1<false, true, false>
+         : th == 2 ? k_filter_major1<false, false, true> : k_filter_major1<false, true, true>;
+    fn<<<grid, kThreads, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+  }
   const int grid = grid_of(nw, kThreads);
   if (is_range)
     k_filter_major<true><<<grid, kThreads, 0, s>>>(a);
@@ -1036,8 +1237,26 @@ cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, 
 
 // Exclusive prefix counts of set bits per word (rank[0..nw), total at
 // rank[nw]); rank needs nw + 1 entries.
+namespace {
+__global__ void k_major_sum_combine(MajorSumArgs a, const unsigned long long *__restrict__ raw,
+                                    double *sum, unsigned long long *parts_out) {
+  unsigned long long parts[9];
+  const uint32_t np = major_sum_parts(a, raw, parts);
+  *sum = major_sum_f64(a, parts);
+  if (parts_out)
+    for (uint32_t i = 0; i < np; ++i) parts_out[i] = parts[i];
+}
+}  // namespace
+
+cudaError_t major_sum_combine(const MajorSumArgs &a, const unsigned long long *raw, double *sum,
+                              unsigned long long *parts, cudaStream_t s) {
+  k_major_sum_combine<<<1, 1, 0, s>>>(a, raw, sum, parts);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out, cudaStream_t s) {
-  k_bytesum<<<grid_of(nbytes, 256), 256, 0, s>>>(p, nbytes, out);
+  k_bytesum<<<grid_of(nbytes / 16 + 1, 256), 256, 0, s>>>(p, nbytes, out);
   count_launch();
   return cudaGetLastError();
 }

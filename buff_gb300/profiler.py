@@ -14,7 +14,17 @@ public calls for the arms it covers:
 - ``buff-slice`` -> run_buff_slice_encoding_decoding (compress/buff_slice.rs:30-101):
   encode, decode, range, equality, buffsum, buffmax;
 - ``buff-major`` -> run_buff_majority_encoding_decoding (compress/buff_simd.rs:246-312):
-  the outlier encode, decode, range, equality, sum, max.
+  the outlier encode, decode, range, equality, sum, max;
+- ``buff`` -> run_buff_encoding_decoding_mybitvec (compress/buff_simd.rs:167-245):
+  byte_fixed_encode (the buff layout, without the ^0x80 flip), decode, the
+  scalar range and equality filters (buff_simd.rs:4507-4679, :4925-5094),
+  byte_fixed_sum, byte_fixed_max.  The reference takes its min/max from a
+  table of its authors' file paths (FILE_MIN_MAX, compress/mod.rs:50-67) when
+  the input is one of them; for every other path it prints ``no min/max`` and
+  runs byte_fixed_encode, which is what this arm does;
+- ``buff-slice-scalar`` -> run_buff_slice_scalar_encoding_decoding
+  (compress/buff_slice.rs:103-171): encode, buff_slice_decode_bs, the
+  row-by-row range and equality filters, buff_slice_sum, buff_slice_max.
 
 Each operation is timed on the host clock around the call, with the device
 synchronised on both sides, as ``Instant::now()``/``elapsed()`` brackets it in
@@ -27,9 +37,7 @@ analogue of taking ``Vec<u8>`` by value: the buff-simd filters read it in
 place (buff_filter_image: slice 0 and the candidates' later bytes cross the
 host link, nothing else), the other queries upload it first.
 
-The arms ``buff`` and ``buff-slice-scalar`` run other code paths of the
-reference (the scalar buff-layout filters) and are rejected, as the reference
-rejects an unknown compression name.
+An unknown compression name is rejected, as the reference rejects it.
 """
 from __future__ import annotations
 
@@ -139,7 +147,26 @@ ARMS = {
         ("buff-major sum function()", "sum"),
         ("buff-major max function()", "max"),
     ]),
+    "buff": ("splitbd byte compress function()", [
+        ("splitbd byte decompress function()", "decode"),
+        ("splitbd byte range filter function()", "range"),
+        ("splitbd byte equal filter function()", "equal"),
+        ("byte_splitbd sum function()", "sum"),
+        ("byte_splitbd max function()", "max"),
+    ]),
+    "buff-slice-scalar": ("buff slice compress function()", [
+        ("buff slice decompress function()", "decode"),
+        ("buff slice range filter function()", "range"),
+        ("buff slice equal filter function()", "equal"),
+        ("buff slice sum function()", "sum"),
+        ("buff slice max function()", "max"),
+    ]),
 }
+
+# Lines the reference prints inside the encode's timed region, before its
+# `Time elapsed` line (buff_simd.rs:183-186: the input is not one of its
+# FILE_MIN_MAX paths).
+PRE_ENCODE = {"buff": "no min/max"}
 
 
 def _ops(arm: str, scale: int):
@@ -156,7 +183,27 @@ def _ops(arm: str, scale: int):
              "buffsum": lambda c, p: comp.buff_slice_buffsum(c),
              "buffmax": lambda c, p: comp.buff_slice_buffmax(c)}
         return enc, (lambda b: Col.deserialize(b, scale)), q
+    if arm == "buff-slice-scalar":
+        comp = BuffSliceCompress(10, 10, scale)
+        from .compress import SliceColumn as Col
+        enc = comp.buff_slice_encode
+        q = {"decode": lambda c, p: comp.buff_slice_decode_bs(c),
+             "range": lambda c, p: comp.buff_slice_range_filter_nosimd(c, p),
+             "equal": lambda c, p: comp.buff_slice_equal_filter_nosimd(c, p),
+             "sum": lambda c, p: comp.buff_slice_sum(c),
+             "max": lambda c, p: comp.buff_slice_max(c)}
+        return enc, (lambda b: Col.deserialize(b, scale)), q
     comp = SplitBDDoubleCompress(10, 10, scale)
+    if arm == "buff":
+        from .compress import FLAG_BUFF_LAYOUT
+        from .compress import Column as Col
+        enc = comp.byte_fixed_encode
+        q = {"decode": lambda c, p: comp.byte_fixed_decode(c),
+             "range": lambda c, p: comp.buff_range_filter(c, p),
+             "equal": lambda c, p: comp.buff_equal_filter(c, p),
+             "sum": lambda c, p: comp.byte_fixed_sum(c),
+             "max": lambda c, p: comp.byte_fixed_max(c)}
+        return enc, (lambda b: Col.deserialize(b, scale, FLAG_BUFF_LAYOUT)), q
     if arm == "buff-major":
         from .compress import MajorColumn as Col
         enc = comp.buff_encode_majority
@@ -195,6 +242,8 @@ def run(test_file: str, compression: str, scl: int, pred: float, from_bytes: boo
         torch.cuda.synchronize()
         return r, max(time.perf_counter_ns() - t0, 1)
 
+    if compression in PRE_ENCODE:
+        print(PRE_ENCODE[compression], file=out)
     col, t_enc = timed(lambda: encode(vals))
     image = col.serialize()
     comp_size = len(image)
@@ -236,7 +285,8 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser(prog="python -m buff_gb300.profiler",
                                  description="comp_profiler on the GPU library")
     ap.add_argument("input_file")
-    ap.add_argument("compression", help="buff-simd | buff-slice | buff-major")
+    ap.add_argument("compression",
+                    help="buff | buff-simd | buff-slice | buff-slice-scalar | buff-major")
     ap.add_argument("int_scale", type=int)
     ap.add_argument("pred", type=_pred_arg)
     ap.add_argument("--from-bytes", action="store_true",

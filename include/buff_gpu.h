@@ -152,6 +152,18 @@ int buff_range_filter(const buff_col *col, double pred, uint32_t *words, uint64_
 /* SplitBDDoubleCompress::buff_simd_equal_filter (compress/buff_simd.rs:3549-3733). */
 int buff_equal_filter(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
                       void *stream);
+/* SplitBDDoubleCompress::buff_range_filter (compress/buff_simd.rs:4507-4679),
+ * the scalar filter of the `buff` profiler arm on byte_fixed_encode's
+ * layout: the same target bytes as buff_range_filter above, but slice 0 is
+ * read byte by byte for every row, so rows after the last full 32-row block
+ * are set too.  (The layout affects only the byte image, not the result.) */
+int buff_scalar_range_filter(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
+                             void *stream);
+/* SplitBDDoubleCompress::buff_equal_filter (compress/buff_simd.rs:4925-5094):
+ * rows equal to pred, set only in the tail step (no rows when r = 0), every
+ * row compared; a target below the base gives no rows. */
+int buff_scalar_equal_filter(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
+                             void *stream);
 /* buff_simd_range_filter_with_slice (compress/buff_simd.rs:3736-3884): the
  * fused form that compares at most 4 leading slices. */
 int buff_range_filter_with_slice(const buff_col *col, double pred, uint32_t *words,
@@ -243,6 +255,16 @@ int buff_sum_majority(const buff_col *col, buff_sum_result *out, void *stream);
  * arg-max rows of the tail step (argmax_words/argmax_count may be NULL). */
 int buff_max_majority(const buff_col *col, double *max_value, uint64_t *max_code,
                       uint32_t *argmax_words, uint64_t *argmax_count, void *stream);
+/* Device-only buff_sum_majority (compress/buff_simd.rs:2294-2442): enqueues
+ * the reference's f64 sum into *dev_sum (device) and, when dev_partials is
+ * not NULL, its k (+1 with a tail) per-byte partials (device u64) -- the
+ * same bits as buff_sum_majority's `sum` and `partials`, combined on the
+ * device; nothing waits for the stream. */
+int buff_sum_majority_async(const buff_col *col, double *dev_sum, uint64_t *dev_partials,
+                            void *stream);
+/* Device-only buff_max_majority (compress/buff_simd.rs:2444-2861): enqueues
+ * the maximum code into *dev_max_code (device u64). */
+int buff_max_majority_async(const buff_col *col, uint64_t *dev_max_code, void *stream);
 
 /* ---- row-conditioned reads ---- */
 
@@ -320,6 +342,18 @@ int buff_slice_range_filter(const buff_col *col, double pred, uint32_t *words, u
                             void *stream);
 int buff_slice_equal_filter(const buff_col *col, double pred, uint32_t *words, uint64_t *count,
                             void *stream);
+/* buff_slice_range_filter_nosimd / buff_slice_equal_filter_nosimd
+ * (:1753-1871, :1873-1991), the filters of the `buff-slice-scalar` arm:
+ * the same per-slice targets and at most 4 slices, compared row by row for
+ * every row (no 32-row blocks, no panic below 32 rows); a target below the
+ * base prints n for both (every row set); a constant column panics. */
+int buff_slice_range_filter_nosimd(const buff_col *col, double pred, uint32_t *words,
+                                   uint64_t *count, void *stream);
+int buff_slice_equal_filter_nosimd(const buff_col *col, double pred, uint32_t *words,
+                                   uint64_t *count, void *stream);
+/* buff_slice_decode_bs (:1184-1262): buff_slice_decode for codes of 1 to 4
+ * slices; wider codes and constant columns panic (BUFF_EREFPANIC). */
+int buff_slice_decode_bs(const buff_col *col, double *out, void *stream);
 /* buff_slice_sum (:1101-1182, at most 4 slices) and buff_slice_buffsum
  * (:702-814): the reference adds the decoded values in row order in f64;
  * the result here is that sum whenever it is exact (every value and partial

@@ -958,6 +958,166 @@ done:
   return rc;
 }
 
+/* ------------------------------------------------------------------ */
+/* scalar filters of the buff layout: buff_range_filter                 */
+/* (buff_simd.rs:4507-4679) and buff_equal_filter (:4925-5094), the     */
+/* `buff` arm of comp_profiler (buff_simd.rs:167-245)                   */
+/* ------------------------------------------------------------------ */
+
+/* Both filters read slice 0 for every row (no 32-row SIMD blocks), then
+ * refine the rows still equal to the target byte by byte through BVIter
+ * gathers, then the packed tail bits.  The range filter sets a row when a
+ * byte exceeds the target byte; the equality filter sets rows only in its
+ * tail step.  `flipped` = 0 reads the buff layout (byte_fixed_encode,
+ * unflipped slices), 1 the buff-simd layout. */
+static int scalar_filter(const uint8_t *bytes, size_t blen, uint64_t scale, double pred,
+                         int is_range, int flipped, uint32_t *words, uint64_t *count,
+                         int *early) {
+  or_br br;
+  or_br_init(&br, bytes, blen);
+  or_header h;
+  if (parse_header_r(&br, &h)) return OR_PANIC;
+  size_t len = h.n, nw = nwords_for(len);
+  uint64_t ft;
+  *early = 0;
+  memset(words, 0, (nw ? nw : 1) * 4);
+  if (filter_target(&h, scale, pred, &ft)) {
+    /* :4528-4531 prints len; :4948-4951 prints 0 */
+    *early = 1;
+    if (is_range) {
+      for (size_t i = 0; i < nw; i++) words[i] = 0xFFFFFFFFu;
+      bv_fix_last(words, len);
+      *count = len;
+    } else {
+      *count = 0;
+    }
+    return OR_OK;
+  }
+  uint32_t remain = h.ilen + h.dlen; /* u32 add, wrapping as `dlen+ilen` */
+  uint32_t *res = words;
+  uint32_t *rb1 = (uint32_t *)calloc(nw ? nw : 1, 4);
+  uint32_t *cur_rb = (uint32_t *)calloc(nw ? nw : 1, 4);
+  int rc = OR_OK;
+  if (!rb1 || !cur_rb) {
+    rc = OR_ENOMEM;
+    goto done;
+  }
+  if (remain < 8) { /* :4535-4543 / :4959-4967: every row against the full target */
+    for (size_t i = 0; i < len; i++) {
+      uint8_t cur;
+      if (or_br_read_bits(&br, remain, &cur)) {
+        rc = OR_PANIC;
+        goto done;
+      }
+      if (is_range ? ((uint64_t)cur > ft) : ((uint64_t)cur == ft)) bv_set(res, i);
+    }
+    remain = 0;
+  } else { /* :4544-4558 / :4968-4979 */
+    remain -= 8;
+    const uint8_t *chunk;
+    if (or_br_read_n_byte(&br, len, &chunk)) {
+      rc = OR_PANIC;
+      goto done;
+    }
+    uint8_t cur_tar = (uint8_t)(ft >> remain);
+    for (size_t i = 0; i < len; i++) {
+      uint8_t c = flipped ? flip(chunk[i]) : chunk[i];
+      if (is_range && c > cur_tar)
+        bv_set(res, i);
+      else if (c == cur_tar)
+        bv_set(rb1, i);
+    }
+  }
+  while (remain > 0) {
+    if (remain >= 8) { /* :4565-4622 / :4987-5039 */
+      remain -= 8;
+      memset(cur_rb, 0, (nw ? nw : 1) * 4);
+      if (bv_card(rb1, nw) != 0) {
+        uint8_t cur_tar = (uint8_t)(ft >> remain);
+        size_t dec_pre = 0;
+        int first = 1;
+        for (size_t wi = 0; wi < nw; wi++) {
+          uint32_t c = rb1[wi];
+          while (c) {
+            size_t dec_cur = (wi << 5) + (size_t)__builtin_ctz(c);
+            c &= c - 1;
+            if (first) {
+              if (dec_cur != 0) or_br_skip_n_byte(&br, dec_cur);
+              first = 0;
+            } else {
+              size_t delta = dec_cur - dec_pre;
+              if (delta != 1) or_br_skip_n_byte(&br, delta - 1);
+            }
+            uint8_t b;
+            if (or_br_read_byte(&br, &b)) {
+              rc = OR_PANIC;
+              goto done;
+            }
+            uint8_t dec = flipped ? flip(b) : b;
+            if (is_range && dec > cur_tar)
+              bv_set(res, dec_cur);
+            else if (dec == cur_tar)
+              bv_set(cur_rb, dec_cur);
+            dec_pre = dec_cur;
+          }
+        }
+        if (len - dec_pre > 1) or_br_skip_n_byte(&br, len - dec_pre - 1);
+      } else {
+        or_br_skip_n_byte(&br, len);
+        break;
+      }
+      uint32_t *sw = rb1;
+      rb1 = cur_rb;
+      cur_rb = sw;
+    } else { /* packed tail, :4625-4673 / :5042-5090 */
+      uint8_t cur_tar = (uint8_t)((uint8_t)((uint8_t)ft << (8 - remain)) >> (8 - remain));
+      or_br_finish_read_byte(&br);
+      if (bv_card(rb1, nw) != 0) {
+        size_t dec_pre = 0;
+        int first = 1;
+        for (size_t wi = 0; wi < nw; wi++) {
+          uint32_t c = rb1[wi];
+          while (c) {
+            size_t dec_cur = (wi << 5) + (size_t)__builtin_ctz(c);
+            c &= c - 1;
+            if (first) {
+              if (dec_cur != 0) or_br_skip(&br, dec_cur * remain);
+              first = 0;
+            } else {
+              size_t delta = dec_cur - dec_pre;
+              if (delta != 1) or_br_skip(&br, (delta - 1) * remain);
+            }
+            uint8_t dec;
+            if (or_br_read_bits(&br, remain, &dec)) {
+              rc = OR_PANIC;
+              goto done;
+            }
+            if (is_range ? (dec > cur_tar) : (dec == cur_tar)) bv_set(res, dec_cur);
+            dec_pre = dec_cur;
+          }
+        }
+        remain = 0;
+      } else {
+        break;
+      }
+    }
+  }
+done:
+  if (rc == OR_OK) *count = bv_card(res, nw);
+  free(rb1);
+  free(cur_rb);
+  return rc;
+}
+
+int or_scalar_range_filter(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                           int flipped, uint32_t *words, uint64_t *count, int *early) {
+  return scalar_filter(bytes, len, scale, pred, 1, flipped, words, count, early);
+}
+int or_scalar_equal_filter(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                           int flipped, uint32_t *words, uint64_t *count, int *early) {
+  return scalar_filter(bytes, len, scale, pred, 0, flipped, words, count, early);
+}
+
 /* buff_simd_range_filter_with_slice / buff_simd_equal_filter_with_slice
  * (buff_simd.rs:3736-3884, 3888-4025): fused compare of up to 4 leading
  * slices per 32 rows, then the packed tail for the surviving rows. */

@@ -113,6 +113,13 @@ int or_range_filter(const uint8_t *bytes, size_t len, uint64_t scale, double pre
                     unsigned flags, uint32_t *words, uint64_t *count, int *early);
 int or_equal_filter(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
                     unsigned flags, uint32_t *words, uint64_t *count, int *early);
+/* buff_range_filter (buff_simd.rs:4507-4679) / buff_equal_filter
+ * (:4925-5094): the scalar filters of the `buff` profiler arm; flipped = 0
+ * for the buff layout they run on. */
+int or_scalar_range_filter(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                           int flipped, uint32_t *words, uint64_t *count, int *early);
+int or_scalar_equal_filter(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                           int flipped, uint32_t *words, uint64_t *count, int *early);
 int or_range_filter_with_slice(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
                                uint32_t *words, uint64_t *count, int *early);
 int or_equal_filter_with_slice(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
@@ -189,6 +196,11 @@ int or_slice_range_filter(const uint8_t *bytes, size_t len, uint64_t scale, doub
                           uint32_t *words, uint64_t *count, int *early);
 int or_slice_equal_filter(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
                           uint32_t *words, uint64_t *count, int *early);
+int or_slice_range_filter_nosimd(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                                 uint32_t *words, uint64_t *count, int *early);
+int or_slice_equal_filter_nosimd(const uint8_t *bytes, size_t len, uint64_t scale, double pred,
+                                 uint32_t *words, uint64_t *count, int *early);
+int or_slice_decode_bs(const uint8_t *bytes, size_t len, uint64_t scale, double *out);
 int or_slice_sum(const uint8_t *bytes, size_t len, uint64_t scale, int any_width, double *sum);
 int or_slice_max(const uint8_t *bytes, size_t len, uint64_t scale, int any_width, double *maxv,
                  uint32_t *words, uint64_t *count);

@@ -127,7 +127,7 @@ int or_slice_decode(const uint8_t *b, size_t len, uint64_t scale, double *out) {
  * every slice up to 4 (`remain - 8*cnt >= 8 ? t >> (remain - 8(cnt+1)) :
  * t << pad`), MSB-first refinement, movemask words for full blocks only. */
 static int slice_filter(const uint8_t *b, size_t len, uint64_t scale, double pred, int is_range,
-                        uint32_t *words, uint64_t *count, int *early) {
+                        int nosimd, uint32_t *words, uint64_t *count, int *early) {
   slice_hdr h;
   if (slice_header(b, len, &h)) return OR_PANIC;
   const size_t nw = ((size_t)h.n + 31) / 32;
@@ -142,7 +142,8 @@ static int slice_filter(const uint8_t *b, size_t len, uint64_t scale, double pre
     return OR_OK;
   }
   if (h.fl == 0) return OR_PANIC; /* ceil(0, 8) underflows: 2^29 slices */
-  if (h.n < 32) return OR_PANIC;  /* `while i <= len - BYTE_WORD` underflows */
+  /* `while i <= len - BYTE_WORD` underflows (the SIMD forms only) */
+  if (!nosimd && h.n < 32) return OR_PANIC;
   const uint64_t t = (uint64_t)(fp - h.base);
   uint32_t remain = h.fl, nsl = h.num;
   uint8_t tb[8];
@@ -154,10 +155,14 @@ static int slice_filter(const uint8_t *b, size_t len, uint64_t scale, double pre
   }
   uint32_t used = nsl < 4 ? nsl : 4;
   uint64_t c = 0;
-  for (uint32_t blk = 0; blk + 1 <= h.n / 32; blk++) {
+  /* SIMD forms: full 32-row blocks only; nosimd forms (:1753-1991): every
+   * row, one at a time */
+  const uint32_t nblk = nosimd ? (h.n + 31) / 32 : h.n / 32;
+  for (uint32_t blk = 0; blk < nblk; blk++) {
     uint32_t gt = 0, eq = 0;
     for (uint32_t i = 0; i < 32; i++) {
       uint32_t row = blk * 32 + i;
+      if (row >= h.n) break;
       int g = 0, e = 1;
       for (uint32_t j = 0; j < used && e; j++) {
         uint8_t v = b[20 + (size_t)j * h.n + row] ^ 0x80u;
@@ -180,12 +185,35 @@ static int slice_filter(const uint8_t *b, size_t len, uint64_t scale, double pre
 
 int or_slice_range_filter(const uint8_t *b, size_t len, uint64_t scale, double pred,
                           uint32_t *words, uint64_t *count, int *early) {
-  return slice_filter(b, len, scale, pred, 1, words, count, early);
+  return slice_filter(b, len, scale, pred, 1, 0, words, count, early);
 }
 
 int or_slice_equal_filter(const uint8_t *b, size_t len, uint64_t scale, double pred,
                           uint32_t *words, uint64_t *count, int *early) {
-  return slice_filter(b, len, scale, pred, 0, words, count, early);
+  return slice_filter(b, len, scale, pred, 0, 0, words, count, early);
+}
+
+/* buff_slice_range_filter_nosimd / buff_slice_equal_filter_nosimd
+ * (buff_slice.rs:1753-1871, :1873-1991): the same per-slice targets and at
+ * most 4 slices, row by row over every row (the `buff-slice-scalar` arm). */
+int or_slice_range_filter_nosimd(const uint8_t *b, size_t len, uint64_t scale, double pred,
+                                 uint32_t *words, uint64_t *count, int *early) {
+  return slice_filter(b, len, scale, pred, 1, 1, words, count, early);
+}
+
+int or_slice_equal_filter_nosimd(const uint8_t *b, size_t len, uint64_t scale, double pred,
+                                 uint32_t *words, uint64_t *count, int *early) {
+  return slice_filter(b, len, scale, pred, 0, 1, words, count, early);
+}
+
+/* buff_slice_decode_bs (buff_slice.rs:1184-1262): the full decode for codes
+ * of 1 to 4 slices; `_ => panic!("bit length greater than 32 ...")` for the
+ * rest, ceil(0, 8)'s underflow included. */
+int or_slice_decode_bs(const uint8_t *b, size_t len, uint64_t scale, double *out) {
+  slice_hdr h;
+  if (slice_header(b, len, &h)) return OR_PANIC;
+  if (h.fl == 0 || h.num > 4) return OR_PANIC;
+  return or_slice_decode(b, len, scale, out);
 }
 
 /* Sequential f64 sum of the decoded values (`sum += f_cur`). */

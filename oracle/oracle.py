@@ -77,6 +77,8 @@ def lib():
             getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, C.c_uint, P, P, P]
         for nm in ("or_range_filter_with_slice", "or_equal_filter_with_slice"):
             getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, P, P, P]
+        for nm in ("or_scalar_range_filter", "or_scalar_equal_filter"):
+            getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, C.c_int, P, P, P]
         L.or_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, C.c_uint, P, P, P]
         L.or_max.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, C.c_uint, P, P, P, P]
         L.or_decode_at_precision.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, C.c_uint32,
@@ -104,8 +106,10 @@ def lib():
         L.or_slice_encode.argtypes = [P, C.c_uint32, C.c_uint64, C.POINTER(u8p),
                                       C.POINTER(C.c_size_t)]
         L.or_slice_decode.argtypes = [P, C.c_size_t, C.c_uint64, P]
-        for nm in ("or_slice_range_filter", "or_slice_equal_filter"):
+        for nm in ("or_slice_range_filter", "or_slice_equal_filter",
+                   "or_slice_range_filter_nosimd", "or_slice_equal_filter_nosimd"):
             getattr(L, nm).argtypes = [P, C.c_size_t, C.c_uint64, C.c_double, P, P, P]
+        L.or_slice_decode_bs.argtypes = [P, C.c_size_t, C.c_uint64, P]
         L.or_slice_sum.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P]
         L.or_slice_max.argtypes = [P, C.c_size_t, C.c_uint64, C.c_int, P, P, P]
         L.or_roaring_serialize.argtypes = [P, C.c_size_t, C.POINTER(u8p), C.POINTER(C.c_size_t)]
@@ -258,6 +262,18 @@ def range_filter_with_slice(buf, scale, pred):
 
 def equal_filter_with_slice(buf, scale, pred):
     return _filter(lib().or_equal_filter_with_slice, buf, scale, pred)
+
+
+def scalar_range_filter(buf, scale, pred, flipped=False):
+    """buff_range_filter (buff_simd.rs:4507-4679) on a buff-layout image."""
+    return _filter(lambda *a: lib().or_scalar_range_filter(*a[:4], int(flipped), *a[4:]),
+                   buf, scale, pred)
+
+
+def scalar_equal_filter(buf, scale, pred, flipped=False):
+    """buff_equal_filter (buff_simd.rs:4925-5094) on a buff-layout image."""
+    return _filter(lambda *a: lib().or_scalar_equal_filter(*a[:4], int(flipped), *a[4:]),
+                   buf, scale, pred)
 
 
 def buff_sum(buf, scale, flipped=True, flags=0):
@@ -511,6 +527,25 @@ def slice_range_filter(buf, scale, pred):
 
 def slice_equal_filter(buf, scale, pred):
     return _slice_filter(lib().or_slice_equal_filter, buf, scale, pred)
+
+
+def slice_range_filter_nosimd(buf, scale, pred):
+    """buff_slice_range_filter_nosimd (buff_slice.rs:1753-1871)."""
+    return _slice_filter(lib().or_slice_range_filter_nosimd, buf, scale, pred)
+
+
+def slice_equal_filter_nosimd(buf, scale, pred):
+    """buff_slice_equal_filter_nosimd (buff_slice.rs:1873-1991)."""
+    return _slice_filter(lib().or_slice_equal_filter_nosimd, buf, scale, pred)
+
+
+def slice_decode_bs(buf, scale):
+    """buff_slice_decode_bs (buff_slice.rs:1184-1262)."""
+    b = _buf(buf)
+    n = header(buf).n
+    out = np.zeros(max(n, 1), dtype=np.float64)
+    _check(lib().or_slice_decode_bs(_ptr(b), b.size, scale, _ptr(out)))
+    return out[:n]
 
 
 def slice_sum(buf, scale, any_width=False):

@@ -84,7 +84,11 @@ def bits_to_words(bits: np.ndarray) -> np.ndarray:
     return np.packbits(pad, bitorder="little").view("<u4")[:nw].astype(np.uint32)
 
 
-def filter_words(L, pred: float, is_range: bool, intended: bool) -> np.ndarray:
+def filter_words(L, pred: float, is_range: bool, intended: bool,
+                 full_blocks: bool = True) -> np.ndarray:
+    """The range / equality filter bitmap.  full_blocks: the SIMD filters
+    never set rows after the last full 32-row block; the scalar buff-layout
+    filters (full_blocks=False) cover every row."""
     n = L["codes"].size
     fp = int(fetch_fixed(np.array([pred]), L["pexp"], L["dlen"])[0])
     if fp < L["base"]:
@@ -96,7 +100,7 @@ def filter_words(L, pred: float, is_range: bool, intended: bool) -> np.ndarray:
         hit = [(c > t) if is_range else (c == t) for c in codes]
         return bits_to_words(np.array(hit, dtype=np.uint8))
     tt = t & ((1 << fl) - 1)
-    full = n // 32 * 32
+    full = n // 32 * 32 if full_blocks else n
     if (not is_range) and r == 0:
         return bits_to_words(np.zeros(n, dtype=np.uint8))
     hit = [((c > tt) if is_range else (c == tt)) and i < full for i, c in enumerate(codes)]

@@ -152,6 +152,16 @@ def test_oracle_vs_model(oracle, kind, n, scale, intended):
         assert np.array_equal(w, M.filter_words(L, p, True, intended)), p
         w, c, _ = oracle.equal_filter(buf, scale, p, flags)
         assert np.array_equal(w, M.filter_words(L, p, False, intended)), p
+    if not intended:
+        # the scalar buff-layout filters of the `buff` profiler arm
+        # (buff_simd.rs:4507-4679, :4925-5094) on the byte_fixed_encode image
+        bbuf = oracle.encode(x, scale, False)
+        for p in [x[n // 3], x[0], float(np.quantile(x, 0.9)), float(x.max()) + 1.0,
+                  float(x.min()) - 1.0, float(x.min())]:
+            w, c, _ = oracle.scalar_range_filter(bbuf, scale, p)
+            assert np.array_equal(w, M.filter_words(L, p, True, False, False)), p
+            w, c, _ = oracle.scalar_equal_filter(bbuf, scale, p)
+            assert np.array_equal(w, M.filter_words(L, p, False, False, False)), p
     s, parts, exact = oracle.buff_sum(buf, scale, True, flags)
     assert s == M.ref_sum(L, n, intended)
     assert exact == n * L["base"] + sum(int(c) for c in L["codes"])

@@ -62,6 +62,19 @@ def test_slice_layout_vs_model(oracle, case):
         eq = np.array([key(c) == tk and i < full for i, c in enumerate(codes)], dtype=np.uint8)
         assert np.array_equal(wr, M.bits_to_words(gt)), (name, p)
         assert np.array_equal(we, M.bits_to_words(eq)), (name, p)
+        # the nosimd forms of the buff-slice-scalar arm: every row
+        wr, cr, _ = oracle.slice_range_filter_nosimd(buf, scale, p)
+        we, ce, _ = oracle.slice_equal_filter_nosimd(buf, scale, p)
+        gt = np.array([key(c) > tk for c in codes], dtype=np.uint8)
+        eq = np.array([key(c) == tk for c in codes], dtype=np.uint8)
+        assert np.array_equal(wr, M.bits_to_words(gt)) and cr == int(gt.sum()), (name, p)
+        assert np.array_equal(we, M.bits_to_words(eq)) and ce == int(eq.sum()), (name, p)
+    # decode_bs: the full decode for 1-4 slices, a panic beyond
+    if num <= 4 and fl > 0:
+        assert np.array_equal(oracle.slice_decode_bs(buf, scale), vals)
+    else:
+        with pytest.raises(oracle.OraclePanic):
+            oracle.slice_decode_bs(buf, scale)
 
 
 def _model_max_range(vals, n, fl, num, s, e, w):

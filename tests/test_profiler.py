@@ -56,7 +56,7 @@ def test_unknown_arm_rejected(tmp_path):
     f = tmp_path / "in.csv"
     f.write_text("1,2,3\n")
     with pytest.raises(ValueError):
-        P.run(str(f), "buff", 10, 1.0)
+        P.run(str(f), "buff-zip", 10, 1.0)
     with pytest.raises(SystemExit):
         P.main([str(f), "buff-simd", "10", "1.0 "])
 
@@ -115,6 +115,39 @@ def test_profiler_arms(oracle, gpu, tmp_path, from_bytes):
     assert res["range"].count == cnt and np.array_equal(res["range"].words, words)
     assert res["buffsum"] == oracle.slice_sum(img, scale, True)
     assert res["buffmax"].value == oracle.slice_max(img, scale, True)[0]
+    assert len(_perf_fields(out.getvalue())) == 10
+
+    # the `buff` arm: the buff-layout image and the scalar filters
+    out = io.StringIO()
+    r = P.run(path, "buff", scale, pred, from_bytes, out)
+    img = oracle.encode(x, scale, flipped=False)
+    assert r["image"] == img
+    text = out.getvalue()
+    assert text.splitlines()[0] == "no min/max"
+    assert "Time elapsed in splitbd byte range filter function() is:" in text
+    res = r["results"]
+    assert np.array_equal(res["decode"], oracle.decode(img, scale, flipped=False))
+    for name, fn in (("range", oracle.scalar_range_filter), ("equal", oracle.scalar_equal_filter)):
+        words, cnt = fn(img, scale, pred)[:2]
+        assert res[name].count == cnt and np.array_equal(res[name].words, words), name
+    assert res["sum"] == oracle.buff_sum(img, scale, flipped=False)[0]
+    mv, mc, aw, ac = oracle.buff_max(img, scale, flipped=False)
+    assert res["max"].value == mv and res["max"].argmax_count == ac
+    assert len(_perf_fields(text)) == 10
+
+    # the `buff-slice-scalar` arm: decode_bs, the row-by-row filters, sum, max
+    out = io.StringIO()
+    r = P.run(path, "buff-slice-scalar", scale, pred, from_bytes, out)
+    img = oracle.slice_encode(x, scale)
+    assert r["image"] == img
+    res = r["results"]
+    assert np.array_equal(res["decode"], oracle.slice_decode_bs(img, scale))
+    for name, fn in (("range", oracle.slice_range_filter_nosimd),
+                     ("equal", oracle.slice_equal_filter_nosimd)):
+        words, cnt = fn(img, scale, pred)[:2]
+        assert res[name].count == cnt and np.array_equal(res[name].words, words), name
+    assert res["sum"] == oracle.slice_sum(img, scale)
+    assert res["max"].value == oracle.slice_max(img, scale)[0]
     assert len(_perf_fields(out.getvalue())) == 10
 
     out = io.StringIO()
