@@ -79,6 +79,10 @@ def parse_args():
     ap.add_argument("--batched-tune", default=None,
                     help="tile_rows,blocks_per_sm,stage for the batched plan (default: autotune)")
     ap.add_argument("--serve-cols", type=int, default=2048)
+    ap.add_argument("--serve-inflight", type=int, default=4,
+                    help="batches (streams) the serving loop keeps in flight")
+    ap.add_argument("--serve-max-batch", type=int, default=2048,
+                    help="requests per batch of the serving loop")
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="length of each offered-load run of the serving sweep")
     return ap.parse_args()
@@ -478,7 +482,7 @@ def run_outlier_form(args, stream, peak):
     import torch
 
     from buff_gb300 import capi
-    from buff_gb300.compress import Column, MajorColumn
+    from buff_gb300.compress import FLAG_RAW_BITMAPS, Column, MajorColumn
     from buff_gb300.workloads import outlier_column_torch
 
     L = capi.lib()
@@ -539,8 +543,38 @@ def run_outlier_form(args, stream, peak):
     assert int(dmax.item()) == mc.value
     ops["max"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
                   "note": "buff_max_majority_async (no host sync)", "synchronous_call_ms": ts * 1e3}
+    # the byte images and the host-side bitmap codec: serialize / deserialize
+    # of the buff-major column with snappy-compressed outlier bitmaps (the
+    # reference's format), with raw bitmaps, and of the plain layout
+    def wall(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return best
+
+    raw = MajorColumn.encode(x, 1000000, FLAG_RAW_BITMAPS, stream=stream)
+    img_s, img_r, img_p = col.serialize(), raw.serialize(), plain.serialize()
+    codec = {
+        "snappy_image_bytes": len(img_s), "raw_image_bytes": len(img_r),
+        "plain_image_bytes": len(img_p),
+        "serialize_snappy_ms": wall(lambda: col.serialize()) * 1e3,
+        "serialize_raw_ms": wall(lambda: raw.serialize()) * 1e3,
+        "serialize_plain_ms": wall(lambda: plain.serialize()) * 1e3,
+        "deserialize_snappy_ms": wall(lambda: MajorColumn.deserialize(img_s, 1000000).free()) * 1e3,
+        "deserialize_raw_ms": wall(lambda: MajorColumn.deserialize(img_r, 1000000,
+                                                                   FLAG_RAW_BITMAPS).free()) * 1e3,
+        "deserialize_plain_ms": wall(lambda: Column.deserialize(img_p, 1000000).free()) * 1e3,
+        "note": "host wall clock of the C calls (host byte images); the snappy - raw "
+                "difference is the host-side bitmap codec"}
+    raw.free()
+    del img_s, img_r, img_p
     out = {"workload": f"{n} rows: 99% N(100,5), 1% U(-1e6,1e6) at seeded random positions, "
-                       f"6 decimals, scale 1e6 (seed 3)", "rows": n,
+                       f"6 decimals, scale 1e6 (seed 3)", "rows": n, "image_codec": codec,
            "fixed_len": info.fixed_len, "outlier_cols": info.outlier_cols,
            "device_bytes": info.device_bytes, "plain_layout_device_bytes": pinfo.device_bytes,
            "ops": ops}
@@ -647,8 +681,25 @@ def run_rapg_form(args, stream):
     ops["sum"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "note": "includes the host combine"}
     t = time_op(lambda: L.buff_rapg_sum_at_precision(h, 3, C.byref(v), sh), 5, stream)
     ops["sum_p3"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9}
+    img = col.serialize()
+
+    def wall(fn, reps=3):
+        fn()
+        best = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            best = min(best, time.perf_counter() - t0)
+        return best
+
+    codec = {"image_bytes": len(img),
+             "serialize_ms": wall(lambda: col.serialize()) * 1e3,
+             "deserialize_ms": wall(lambda: RapgColumn.deserialize(img, 1000000).free()) * 1e3,
+             "note": "host wall clock of the C calls: the outlier rows go to and from croaring "
+                     "portable bitmaps on the host"}
+    del img
     res = {"workload": f"{n} rows: 99% N(100,5), 1% U(1e5,1e6) at seeded random positions, "
-                       f"6 decimals, scale 1e6 (seed 6)", "rows": n,
+                       f"6 decimals, scale 1e6 (seed 6)", "rows": n, "image_codec": codec,
            "fixed_len": info.fixed_len, "outlier_cols": info.outlier_cols,
            "device_bytes": code_bytes, "ops": ops}
     res["rapg_major"] = run_rapg_major_form(args, stream)
@@ -902,7 +953,8 @@ def run_serving_form(args, stream, peak):
     budget = 8 << 30
 
     def make_server(batched):
-        s = Server(budget, max_batch=2048, max_inflight=4, batched=batched, auto_release=True)
+        s = Server(budget, max_batch=args.serve_max_batch, max_inflight=args.serve_inflight,
+                   batched=batched, auto_release=True)
         for c in cols:
             s.add_column(c)
         s.start()
@@ -986,7 +1038,8 @@ def run_serving_form(args, stream, peak):
             reqs[i]["scale"] = 10 ** pool_dec[pick[i]]
             reqs[i]["precision"] = 0
         arrivals = np.cumsum(rng.exponential(1e9 / rate, nreq)).astype(np.uint64)
-        srv = Server(budget, max_batch=2048, max_inflight=4, batched=True, auto_release=True,
+        srv = Server(budget, max_batch=args.serve_max_batch, max_inflight=args.serve_inflight,
+                     batched=True, auto_release=True,
                      store_budget_bytes=code_bytes + (8 << 30))
         for c in cols:
             srv.add_column(c)
@@ -1018,7 +1071,8 @@ def run_serving_form(args, stream, peak):
                     f"2-6 decimals; mix 50% range, 20% equality, 20% sum/max, "
                     f"10% decode at a random precision; Poisson arrivals",
         "columns": ncols, "rows": int(lens.sum()), "code_bytes": code_bytes,
-        "output_budget_bytes": budget, "max_batch": 2048, "max_inflight": 4,
+        "output_budget_bytes": budget, "max_batch": args.serve_max_batch,
+        "max_inflight": args.serve_inflight,
         "saturation": {"batched": sat_b, "plain": sat_p},
         "sweep": sweep,
         "equal_p99": {"p99_ms": ref["p99_ms"], "plain_qps": ref["achieved_qps"],

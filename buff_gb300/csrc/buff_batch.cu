@@ -364,29 +364,6 @@ __device__ __forceinline__ Bytes32 ld32(const uint8_t *p) {
   return v;
 }
 
-// Bits at multiples of r in a 64-bit word (r = 1..7).
-__device__ __forceinline__ unsigned long long every_r(uint32_t r) {
-  unsigned long long m = 0;
-  for (uint32_t j = 0; j < 64; j += r) m |= 1ull << j;
-  return m;
-}
-
-// Sum of the 16 r-bit fields packed LSB-first in (lo, hi): every set bit b
-// of the 16r-bit stream adds 2^(b mod r).  pat = every_r(r); bit j of hi is
-// stream bit 64 + j, whose residue class starts at qh0 = (r - 64 mod r) mod r
-// (computed once per tile).
-__device__ __forceinline__ uint32_t fields16_sum(unsigned long long lo, unsigned long long hi,
-                                                 uint32_t r, unsigned long long pat,
-                                                 uint32_t qh0) {
-  if (r == 1) return __popcll(lo) + __popcll(hi);
-  uint32_t acc = 0, qh = qh0;
-  for (uint32_t p = 0; p < r; ++p) {
-    acc += (uint32_t)(__popcll(lo & (pat << p)) + __popcll(hi & (pat << qh))) << p;
-    qh = qh + 1 == r ? 0u : qh + 1;
-  }
-  return acc;
-}
-
 // MSBs of the bytes of four words -> 16 row-ordered bits.
 __device__ __forceinline__ uint32_t gather16(const uint32_t *m) {
   return __byte_perm(msb8(m[0], m[1]), msb8(m[2], m[3]), 0x0040);
@@ -394,118 +371,6 @@ __device__ __forceinline__ uint32_t gather16(const uint32_t *m) {
 
 __device__ __forceinline__ uint32_t w4(const uint4 &v, int i) {
   return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
-}
-
-// Filters and sums over rows [r0, r1) of one query.  Lane L owns the 16
-// rows row0 = step + 16L .. +15 of each 512-row step; STAGE steps are
-// loaded together (every slice when summing, slice 0 otherwise).  Lane
-// pairs combine their 16-row results into one bitmap word.
-template <int STAGE, bool DO_F, bool DO_S>
-__device__ __forceinline__ void tile_filter_sum(const BQ &q, uint32_t r0, uint32_t r1,
-                                                uint32_t lane) {
-  constexpr bool do_f = DO_F;
-  constexpr bool do_s = DO_S;
-  const bool is_range = q.ops & kOpRange;
-  const bool cmp = do_f && q.fill == 0;
-  const uint32_t nload = do_s ? (q.k < 4 ? q.k : 4u) : (q.k ? 1u : 0u);
-  const unsigned long long pat = q.r > 1 ? every_r(q.r) : 0ull;
-  const uint32_t qh0 = q.r > 1 ? (q.r - 64 % q.r) % q.r : 0u;
-  uint32_t sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  uint32_t tacc = 0;
-  uint32_t cnt = 0;
-  for (uint32_t sb = r0; sb < r1; sb += 512 * STAGE) {
-    uint4 v[STAGE][4];
-#pragma unroll
-    for (int u = 0; u < STAGE; ++u) {
-      const uint32_t row0 = sb + u * 512 + lane * 16;
-#pragma unroll
-      for (uint32_t j = 0; j < 4; ++j)
-        if (j < nload && row0 < r1) v[u][j] = __ldcs(reinterpret_cast<const uint4 *>(
-                                          q.slices + j * q.stride + row0));
-    }
-#pragma unroll
-    for (int u = 0; u < STAGE; ++u) {
-      const uint32_t row0 = sb + u * 512 + lane * 16;
-      const bool act = row0 < r1;
-      uint32_t valid = 0, eq = 0, gt = 0;
-      if (act) {
-        const uint32_t left = q.n - row0;
-        valid = left >= 16 ? 0xFFFFu : ((1u << left) - 1u);
-        eq = valid;
-        if (row0 + 16 > q.full_rows)
-          eq &= row0 >= q.full_rows ? 0u : ((1u << (q.full_rows - row0)) - 1u);
-#pragma unroll
-        for (uint32_t j = 0; j < 8; ++j) {
-          if (j >= q.k) break;
-          const bool need_f = cmp && j < q.k_used && eq;
-          if (!do_s && !need_f) break;
-          const uint4 w = j < nload ? v[u][j & 3]
-                                    : __ldcs(reinterpret_cast<const uint4 *>(
-                                          q.slices + j * q.stride + row0));
-          if (do_s) {
-            sacc[j] = __dp4a(w.x ^ H, 0x01010101u, sacc[j]);
-            sacc[j] = __dp4a(w.y ^ H, 0x01010101u, sacc[j]);
-            sacc[j] = __dp4a(w.z ^ H, 0x01010101u, sacc[j]);
-            sacc[j] = __dp4a(w.w ^ H, 0x01010101u, sacc[j]);
-          }
-          if (need_f) {
-            const ByteTarget t = make_target(q.tbyte[j]);
-            uint32_t g[4], e[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) cmp4(w4(w, i), t, g[i], e[i]);
-            gt |= eq & gather16(g);
-            eq &= gather16(e);
-          }
-        }
-        if (q.r) {
-          const bool need_tf = cmp && q.r_used && eq;
-          if (do_s || need_tf) {
-            unsigned long long lo, hi;
-            load_tail16(q.tail, row0 >> 4, q.r, lo, hi);
-            if (do_s) tacc += fields16_sum(lo, hi, q.r, pat, qh0);  // rows past n hold zeros
-            if (need_tf) {
-              uint32_t gtt = 0, eqt = 0, b = eq;
-              while (b) {
-                const uint32_t i = __ffs(b) - 1;
-                b &= b - 1;
-                const uint32_t f = field16(lo, hi, i, q.r);
-                gtt |= (uint32_t)(f > q.ttail) << i;
-                eqt |= (uint32_t)(f == q.ttail) << i;
-              }
-              gt |= eq & gtt;
-              eq &= eqt;
-            }
-          }
-        }
-      }
-      if (do_f) {
-        const uint32_t res = !act ? 0u : q.fill == 1 ? valid : q.fill == 2 ? 0u
-                                                      : (is_range ? gt : eq);
-        const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
-        if (act && !(lane & 1)) {
-          const uint32_t word = res | (hi16 << 16);
-          q.words[row0 >> 5] = word;
-          cnt += __popc(word);
-        }
-      }
-    }
-  }
-  if (do_s) {
-#pragma unroll
-    for (uint32_t j = 0; j < 8; ++j) {
-      if (j >= q.k) break;
-      const unsigned long long s = warp_sum_ull(sacc[j]);
-      if (lane == 0 && s) atomicAdd(q.acc + 1 + j, s);
-    }
-    if (q.r) {
-      const unsigned long long s = warp_sum_ull(tacc);
-      if (lane == 0 && s) atomicAdd(q.acc + 9, s);
-    }
-  }
-  if (do_f) {
-    const unsigned long long s = warp_sum_ull(cnt);
-    if (lane == 0 && s) atomicAdd(q.acc, s);
-  }
 }
 
 // Largest byte of a word.
@@ -757,17 +622,21 @@ __device__ __forceinline__ void tile_filter32(const BQ &q, uint32_t r0, uint32_t
 
 // ---- filter + sum with the slices staged through shared memory
 //
-// Each lane copies its own 16-byte pieces (16 rows of up to 3 slices; a 4th
-// and later slice are loaded directly) and the first 4r lanes the step's 64r
-// tail bytes into a per-warp ring of kDepth 512-row steps with cp.async, so
-// kDepth steps of every slice are in flight without holding registers; a
-// lane reads back only what it copied (the tail group excepted, hence the
-// warp barrier around each step).  Ring shape measured on the 4,096-column
-// plan: 3 steps of 3 slices (6 KB per warp) 1.47 ms per replay, against 1.80
-// (4 x 4 slices), 1.51 (2 x 3), 1.54 (4 x 3), 1.55 (3 x 2), 1.83 (5 x 3):
-// the smaller ring lets more warps stay resident.
-constexpr int kDepth = 3;
-constexpr uint32_t kSlotBytes = 3 * 512 + 512;  // 3 slices + up to 448 tail bytes
+// Lane L owns the 32 rows step + 32L .. +31 of each 1,024-row step -- one
+// bitmap word, as in the single-column one-pass kernel -- and copies its own
+// 32 bytes of up to 3 slices (a 4th and later slice are loaded directly),
+// while the first 8r lanes copy the step's 128r tail bytes, into a per-warp
+// ring of kDepth steps with cp.async: kDepth - 1 steps of every slice are in
+// flight without holding registers, and a lane reads back only what it
+// copied (the tail group excepted, hence the warp barrier around each step).
+// Per 32 rows a lane does 8 dp4a per slice, one byte compare of slice 0 with
+// the target's top bit specialised, and r weighted popcounts for the tail.
+// The 16-rows-per-lane form of this worker (3 steps of 512 rows) ran
+// 1.40-1.48 ms per replay of the 4,096-query plan, issue-bound at ~335
+// instructions per 512 rows.
+constexpr int kDepth = 2;
+constexpr uint32_t kStepRows = 1024;
+constexpr uint32_t kSlotBytes = 3 * kStepRows + 1024;  // 3 slices + up to 896 tail bytes
 constexpr uint32_t kRingBytes = kDepth * kSlotBytes;
 
 __device__ __forceinline__ void cp16(uint8_t *dst, const uint8_t *src) {
@@ -819,29 +688,58 @@ __device__ __forceinline__ FsTile fs_tile(const BQ &q, bool do_f) {
 __device__ __forceinline__ void fs_issue(const FsTile &q, uint32_t sb, uint32_t r1, uint32_t lane,
                                          uint8_t *slot) {
   if (sb < r1) {
-    const uint32_t row0 = sb + lane * 16;
-    if (row0 < r1)
-      for (uint32_t j = 0; j < q.nst; ++j)
-        cp16(slot + j * 512 + lane * 16, q.slices + j * q.stride + row0);
-    if (q.r && lane < 4 * q.r)
-      cp16(slot + 3 * 512 + lane * 16, q.tail + (size_t)(sb >> 9) * 64 * q.r + lane * 16);
+    const uint32_t row0 = sb + lane * 32;
+    if (row0 < r1)  // row0 + 32 <= the slice stride (a multiple of 512 >= n)
+      for (uint32_t j = 0; j < q.nst; ++j) {
+        const uint8_t *src = q.slices + j * q.stride + row0;
+        cp16(slot + j * kStepRows + lane * 32, src);
+        cp16(slot + j * kStepRows + lane * 32 + 16, src + 16);
+      }
+    // the step's 128r tail bytes = 8r pieces of 16 (up to 56: a lane copies
+    // pieces lane and lane + 32), none past the tail the rows below r1 use
+    // (the tail allocation covers that, rounded up to 16)
+    const size_t tend = ((size_t)r1 * q.r + 7) / 8;
+    for (uint32_t pc = lane; pc < 8 * q.r; pc += 32) {
+      const size_t t0 = (size_t)(sb / kStepRows) * 128 * q.r + pc * 16;
+      if (t0 < tend) cp16(slot + 3 * kStepRows + pc * 16, q.tail + t0);
+    }
   }
   cp_commit();  // every lane commits one group per step, even an empty one
 }
 
-// Slice-0 compare of 16 rows (four words) against a target byte whose top
-// bit is TH: the rows above it (gt) and equal to it (eq), as 16-bit masks.
+// Tail bits of the 32 rows from row0 that lie below n (each row r bits).
+__device__ __forceinline__ uint32_t left_bits(uint32_t n, uint32_t row0, uint32_t r) {
+  const uint32_t rows = n - row0 >= 32 ? 32u : n - row0;
+  return rows * r;
+}
+
+// Slice-0 compare of 32 rows (eight words) against a target byte whose top
+// bit is TH: the rows above it (gt) and equal to it (eq).
 template <bool TH>
-__device__ __forceinline__ void cmp16_t(const uint4 &w, uint32_t lo0, uint32_t lo1, uint32_t &gt,
-                                        uint32_t &eq) {
-  uint32_t g[4], e[4];
+__device__ __forceinline__ void cmp32_t(const uint4 &a, const uint4 &b, uint32_t lo0,
+                                        uint32_t lo1, uint32_t &gt, uint32_t &eq) {
+  uint32_t g[8], e[8];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    g[i] = gt4t<TH>(w4(w, i), lo1);
-    e[i] = eq4t<TH>(w4(w, i), lo0, lo1);
+    g[i] = gt4t<TH>(w4(a, i), lo1);
+    e[i] = eq4t<TH>(w4(a, i), lo0, lo1);
+    g[4 + i] = gt4t<TH>(w4(b, i), lo1);
+    e[4 + i] = eq4t<TH>(w4(b, i), lo0, lo1);
   }
-  gt = gather16(g);
-  eq = gather16(e);
+  gt = gather32(g);
+  eq = gather32(e);
+}
+
+__device__ __forceinline__ uint32_t dp4a_sum8(const uint4 &a, const uint4 &b, uint32_t acc) {
+  acc = __dp4a(a.x ^ H, 0x01010101u, acc);
+  acc = __dp4a(a.y ^ H, 0x01010101u, acc);
+  acc = __dp4a(a.z ^ H, 0x01010101u, acc);
+  acc = __dp4a(a.w ^ H, 0x01010101u, acc);
+  acc = __dp4a(b.x ^ H, 0x01010101u, acc);
+  acc = __dp4a(b.y ^ H, 0x01010101u, acc);
+  acc = __dp4a(b.z ^ H, 0x01010101u, acc);
+  acc = __dp4a(b.w ^ H, 0x01010101u, acc);
+  return acc;
 }
 
 template <bool DO_F>
@@ -851,40 +749,39 @@ __device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_
   uint32_t *const words = qd.words;
   unsigned long long *const acc = qd.acc;
   const uint32_t fill = qd.fill;
-  const unsigned long long pat = q.r > 1 ? every_r(q.r) : 0ull;
-  const uint32_t qh0 = q.r > 1 ? (q.r - 64 % q.r) % q.r : 0u;
+  const uint32_t c32 = q.r ? 32 % q.r : 0u;  // tail phase step per word
   uint32_t sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   uint32_t tacc = 0, cnt = 0;
   __syncwarp();  // the ring may still be read by the previous item
 #pragma unroll
-  for (int d = 0; d < kDepth - 1; ++d) fs_issue(q, r0 + d * 512, r1, lane, ring + d * kSlotBytes);
+  for (int d = 0; d < kDepth - 1; ++d)
+    fs_issue(q, r0 + d * kStepRows, r1, lane, ring + d * kSlotBytes);
   uint32_t t = 0;
-  for (uint32_t sb = r0; sb < r1; sb += 512, ++t) {
-    fs_issue(q, sb + (kDepth - 1) * 512, r1, lane, ring + ((t + kDepth - 1) % kDepth) * kSlotBytes);
+  for (uint32_t sb = r0; sb < r1; sb += kStepRows, ++t) {
+    fs_issue(q, sb + (kDepth - 1) * kStepRows, r1, lane,
+             ring + ((t + kDepth - 1) % kDepth) * kSlotBytes);
     cp_wait<kDepth - 1>();
     __syncwarp();
     const uint8_t *slot = ring + (t % kDepth) * kSlotBytes;
-    const uint32_t row0 = sb + lane * 16;
+    const uint32_t row0 = sb + lane * 32;
     const bool act = row0 < r1;
     uint32_t valid = 0, eq = 0, gt = 0;
     if (act) {
       const uint32_t left = q.n - row0;
-      valid = left >= 16 ? 0xFFFFu : ((1u << left) - 1u);
+      valid = left >= 32 ? 0xFFFFFFFFu : ((1u << left) - 1u);
       eq = valid;
-      if (row0 + 16 > q.full_rows)
+      if (row0 + 32 > q.full_rows)
         eq &= row0 >= q.full_rows ? 0u : ((1u << (q.full_rows - row0)) - 1u);
       {  // slice 0: sums and the compare
-        const uint4 w = *reinterpret_cast<const uint4 *>(slot + lane * 16);
-        sacc[0] = __dp4a(w.x ^ H, 0x01010101u, sacc[0]);
-        sacc[0] = __dp4a(w.y ^ H, 0x01010101u, sacc[0]);
-        sacc[0] = __dp4a(w.z ^ H, 0x01010101u, sacc[0]);
-        sacc[0] = __dp4a(w.w ^ H, 0x01010101u, sacc[0]);
+        const uint4 a = *reinterpret_cast<const uint4 *>(slot + lane * 32);
+        const uint4 b = *reinterpret_cast<const uint4 *>(slot + lane * 32 + 16);
+        sacc[0] = dp4a_sum8(a, b, sacc[0]);
         if (q.cmp && q.k_used && eq) {
           uint32_t g, e;
           if (q.th0)
-            cmp16_t<true>(w, q.t0lo0, q.t0lo1, g, e);
+            cmp32_t<true>(a, b, q.t0lo0, q.t0lo1, g, e);
           else
-            cmp16_t<false>(w, q.t0lo0, q.t0lo1, g, e);
+            cmp32_t<false>(a, b, q.t0lo0, q.t0lo1, g, e);
           gt = eq & g;
           eq &= e;
         }
@@ -892,43 +789,57 @@ __device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_
 #pragma unroll
       for (uint32_t j = 1; j < 8; ++j) {
         if (j >= q.k) break;
-        const bool need_f = q.cmp && j < q.k_used && eq;
-        const uint4 w = j < 3 ? *reinterpret_cast<const uint4 *>(slot + j * 512 + lane * 16)
-                              : __ldcs(reinterpret_cast<const uint4 *>(q.slices + j * q.stride + row0));
-        sacc[j] = __dp4a(w.x ^ H, 0x01010101u, sacc[j]);
-        sacc[j] = __dp4a(w.y ^ H, 0x01010101u, sacc[j]);
-        sacc[j] = __dp4a(w.z ^ H, 0x01010101u, sacc[j]);
-        sacc[j] = __dp4a(w.w ^ H, 0x01010101u, sacc[j]);
-        if (need_f) {
+        uint4 a, b;
+        if (j < 3) {
+          a = *reinterpret_cast<const uint4 *>(slot + j * kStepRows + lane * 32);
+          b = *reinterpret_cast<const uint4 *>(slot + j * kStepRows + lane * 32 + 16);
+        } else {
+          const uint8_t *p = q.slices + j * q.stride + row0;
+          a = __ldcs(reinterpret_cast<const uint4 *>(p));
+          b = __ldcs(reinterpret_cast<const uint4 *>(p + 16));
+        }
+        sacc[j] = dp4a_sum8(a, b, sacc[j]);
+        if (q.cmp && j < q.k_used && eq) {
           const ByteTarget tg = make_target((uint32_t)(q.tb >> (8 * (j - 1))) & 0xFFu);
-          uint32_t g[4], e[4];
+          uint32_t g[8], e[8];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) cmp4(w4(w, i), tg, g[i], e[i]);
-          gt |= eq & gather16(g);
-          eq &= gather16(e);
+          for (int i = 0; i < 4; ++i) {
+            cmp4(w4(a, i), tg, g[i], e[i]);
+            cmp4(w4(b, i), tg, g[4 + i], e[4 + i]);
+          }
+          gt |= eq & gather32(g);
+          eq &= gather32(e);
         }
       }
       if (q.r) {
-        const unsigned short *tp =
-            reinterpret_cast<const unsigned short *>(slot + 3 * 512 + lane * 2 * q.r);
-        unsigned long long lo = 0, hi = 0;
+        // the lane's 32 fields: r words at byte 4r * lane of the step's tail
+        const uint32_t *tp = reinterpret_cast<const uint32_t *>(slot + 3 * kStepRows) + lane * q.r;
+        uint32_t tw[8];
+#pragma unroll
+        for (uint32_t i = 0; i < 8; ++i) tw[i] = i < q.r ? tp[i] : 0u;
+        const uint32_t nbits = left_bits(q.n, row0, q.r);  // stream bits of the lane's rows
+        uint32_t ph = 0;  // the lane's fields start at a multiple of r
 #pragma unroll
         for (uint32_t i = 0; i < 7; ++i) {
           if (i < q.r) {
-            const unsigned long long h = tp[i];
-            if (i < 4)
-              lo |= h << (16 * i);
-            else
-              hi |= h << (16 * (i - 4));
+            uint32_t word = tw[i];
+            if (32 * i >= nbits)
+              word = 0;
+            else if (32 * i + 32 > nbits)
+              word &= (1u << (nbits - 32 * i)) - 1u;
+            tacc += wpopc(word, ph, q.r);
+            ph += c32;
+            if (ph >= q.r) ph -= q.r;
           }
         }
-        tacc += fields16_sum(lo, hi, q.r, pat, qh0);
         if (q.cmp && q.r_used && eq) {
           uint32_t gtt = 0, eqt = 0, b = eq;
           while (b) {
             const uint32_t i = __ffs(b) - 1;
             b &= b - 1;
-            const uint32_t f = field16(lo, hi, i, q.r);
+            const uint32_t bit = i * q.r, wi = bit >> 5;
+            const uint32_t f =
+                __funnelshift_r(pick8(tw, wi), pick8(tw, wi + 1), bit & 31) & ((1u << q.r) - 1u);
             gtt |= (uint32_t)(f > q.ttail) << i;
             eqt |= (uint32_t)(f == q.ttail) << i;
           }
@@ -937,15 +848,10 @@ __device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_
         }
       }
     }
-    if (DO_F) {
-      const uint32_t res = !act ? 0u : fill == 1 ? valid : fill == 2 ? 0u
-                                                  : (q.is_range ? gt : eq);
-      const uint32_t hi16 = __shfl_down_sync(0xFFFFFFFFu, res, 1);
-      if (act && !(lane & 1)) {
-        const uint32_t word = res | (hi16 << 16);
-        words[row0 >> 5] = word;
-        cnt += __popc(word);
-      }
+    if (DO_F && act) {
+      const uint32_t res = fill == 1 ? valid : fill == 2 ? 0u : (q.is_range ? gt : eq);
+      words[row0 >> 5] = res;
+      cnt += __popc(res);
     }
     __syncwarp();  // the slot is refilled by the next step's copies
   }
@@ -975,7 +881,8 @@ enum { kClsF = 0, kClsFS = 1, kClsS = 2, kClsMD = 3, kClasses = 4 };
 // list holds query indices qidx[] and the exclusive prefix of their tile
 // counts, so item i belongs to the query found by binary search.
 template <int CLS, int STAGE>
-__global__ void __launch_bounds__(kBT) k_bq(const BQ *__restrict__ qs,
+__global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
+    k_bq(const BQ *__restrict__ qs,
                                             const uint32_t *__restrict__ qidx,
                                             const uint32_t *__restrict__ prefix, uint32_t nq,
                                             uint32_t nitems, uint32_t tile,

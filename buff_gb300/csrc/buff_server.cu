@@ -117,8 +117,7 @@ struct Slot {
   cudaStream_t s = nullptr;
   cudaEvent_t ev = nullptr;
   void *h_desc = nullptr, *d_desc = nullptr;
-  unsigned long long *h_acc = nullptr, *d_acc = nullptr;
-  unsigned int *d_counter = nullptr;
+  unsigned long long *h_acc = nullptr;
   PlainRes *h_plain = nullptr, *d_plain = nullptr;
   std::vector<Req> reqs;
   bool busy = false;
@@ -275,6 +274,17 @@ void retire(buff_server *S, Slot &sl) {
 int launch_batched(buff_server *S, Slot &sl) {
   const size_t dsz = buffk::batch_desc_size();
   const uint32_t nq = (uint32_t)sl.reqs.size();
+  // one upload and one staging layout: the descriptors, the class lists, then
+  // the work counters (16 bytes, padded to 64) and the accumulators, whose
+  // zeros travel with the upload instead of a separate memset
+  const size_t soff = (dsz * nq + 15) / 16 * 16;
+  const size_t aoff = (soff + 4 * buffk::batch_sched_words(nq) + 63) / 64 * 64;
+  const size_t abytes = sizeof(unsigned long long) * buffk::kBatchAcc * nq;
+  uint8_t *h_base = static_cast<uint8_t *>(sl.h_desc);
+  uint8_t *d_base = static_cast<uint8_t *>(sl.d_desc);
+  unsigned int *d_counter = reinterpret_cast<unsigned int *>(d_base + aoff);
+  unsigned long long *d_acc = reinterpret_cast<unsigned long long *>(d_base + aoff + 64);
+  memset(h_base + aoff, 0, 64 + abytes);
   for (uint32_t i = 0; i < nq; ++i) {
     Req &q = sl.reqs[i];
     buff_query uq;
@@ -286,11 +296,9 @@ int launch_batched(buff_server *S, Slot &sl) {
     uq.words = q.words;
     uq.values = q.values;
     void *d = static_cast<uint8_t *>(sl.h_desc) + dsz * i;
-    q.status = buffk::batch_plan_query(uq, sl.d_acc + (size_t)buffk::kBatchAcc * i, d);
+    q.status = buffk::batch_plan_query(uq, d_acc + (size_t)buffk::kBatchAcc * i, d);
     if (q.status != BUFF_OK) memset(d, 0, dsz);  // an invalid request: zero rows, no work
   }
-  // one upload: the descriptors, then the class lists right after them
-  const size_t soff = (dsz * nq + 15) / 16 * 16;
   uint32_t *h_sched = reinterpret_cast<uint32_t *>(static_cast<uint8_t *>(sl.h_desc) + soff);
   const uint32_t *d_sched =
       reinterpret_cast<const uint32_t *>(static_cast<uint8_t *>(sl.d_desc) + soff);
@@ -308,15 +316,10 @@ int launch_batched(buff_server *S, Slot &sl) {
   buffk::BatchSched sc;
   buffk::batch_schedule(sl.h_desc, nq, t.tile_rows, h_sched, &sc);
   cudaStream_t s = sl.s;
-  cudaError_t e = cudaMemcpyAsync(sl.d_desc, sl.h_desc, soff + 4 * (size_t)sc.words,
+  cudaError_t e = cudaMemcpyAsync(sl.d_desc, sl.h_desc, aoff + 64 + abytes,
                                   cudaMemcpyHostToDevice, s);
-  // counters (16 bytes, padded to 64) precede the accumulators
-  if (e == cudaSuccess)
-    e = cudaMemsetAsync(sl.d_counter, 0, 64 + sizeof(unsigned long long) * buffk::kBatchAcc * nq, s);
-  if (e == cudaSuccess) e = buffk::batch_launch(sl.d_desc, d_sched, sc, t, sl.d_counter, s);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(sl.h_acc, sl.d_acc, sizeof(unsigned long long) * buffk::kBatchAcc * nq,
-                        cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = buffk::batch_launch(sl.d_desc, d_sched, sc, t, d_counter, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(sl.h_acc, d_acc, abytes, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaEventRecord(sl.ev, s);
   return buffh::cuda_status(e);
 }
@@ -481,6 +484,8 @@ bool admit_encode(buff_server *S, Req &q) {
 // Waiting requests beyond the free slots before slots take batches.
 constexpr size_t kQueueForBatch = 8;
 
+
+
 void loop(buff_server *S) {
   cudaSetDevice(S->device);
   const uint32_t maxb = S->cfg.batched ? S->cfg.max_batch : 1;
@@ -601,7 +606,6 @@ void destroy_slots(buff_server *S) {
     if (sl.h_acc) cudaFreeHost(sl.h_acc);
     if (sl.h_plain) cudaFreeHost(sl.h_plain);
     if (sl.d_desc) cudaFree(sl.d_desc);
-    if (sl.d_counter) cudaFree(sl.d_counter);
     if (sl.d_plain) cudaFree(sl.d_plain);
   }
   S->slots.clear();
@@ -652,7 +656,9 @@ int buff_server_create(const buff_server_config *cfg, buff_server **out) {
     if ((e = cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking)) != cudaSuccess) break;
     if ((e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming)) != cudaSuccess) break;
     const size_t sw = 4 * buffk::batch_sched_words(mb);
-    const size_t stage = (dsz * mb + 15) / 16 * 16 + sw;
+    // descriptors, class lists, work counters (64) and accumulators
+    const size_t stage = ((dsz * mb + 15) / 16 * 16 + sw + 63) / 64 * 64 + 64 +
+                         sizeof(unsigned long long) * buffk::kBatchAcc * mb;
     if ((e = cudaMallocHost(&sl.h_desc, stage)) != cudaSuccess) break;
     if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_acc),
                             8 * buffk::kBatchAcc * mb)) != cudaSuccess)
@@ -660,10 +666,6 @@ int buff_server_create(const buff_server_config *cfg, buff_server **out) {
     if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_plain), sizeof(PlainRes))) != cudaSuccess)
       break;
     if ((e = cudaMalloc(&sl.d_desc, stage)) != cudaSuccess) break;
-    if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_counter), 64 + 8 * buffk::kBatchAcc * mb)) !=
-        cudaSuccess)
-      break;
-    sl.d_acc = reinterpret_cast<unsigned long long *>(reinterpret_cast<uint8_t *>(sl.d_counter) + 64);
     if ((e = cudaMalloc(reinterpret_cast<void **>(&sl.d_plain), sizeof(PlainRes))) != cudaSuccess)
       break;
     sl.reqs.reserve(mb);
