@@ -656,18 +656,22 @@ done:
 // The byte image of a buff-major column (buff_simd.rs:449-528): header,
 // column count, per sparse column (major, bitmap size, bitmap, outlier
 // count, outlier bytes), a pad byte, the unflipped dense slices, the tail.
-int major_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s) {
+// The buff-major image (buff_simd.rs:317-630).  prefix_only: only the header
+// and the sparse columns (up to the dense slices), which buff_serialize
+// follows with the dense slices and tail written in place.
+int major_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s,
+                bool prefix_only = false) {
   int rc = BUFF_OK;
   const uint32_t n = c->n, kd = c->k - c->m;
   const size_t nw = ((size_t)n + 31) / 32;
   std::vector<uint32_t> bits((size_t)c->m * nw);
   std::vector<uint8_t> ob(c->oofs[c->m]);
-  std::vector<uint8_t> dense((size_t)kd * n), tail(c->tail_bytes);
+  std::vector<uint8_t> dense(prefix_only ? 0 : (size_t)kd * n), tail(prefix_only ? 0 : c->tail_bytes);
   for (uint32_t col = 0; col < c->m; ++col)
     CK(cudaMemcpyAsync(bits.data() + col * nw, c->obits + col * c->nwp, nw * 4,
                        cudaMemcpyDeviceToHost, s));
   if (!ob.empty()) CK(cudaMemcpyAsync(ob.data(), c->obytes, ob.size(), cudaMemcpyDeviceToHost, s));
-  if (kd && n)
+  if (!prefix_only && kd && n)
     CK(cudaMemcpy2DAsync(dense.data(), n, c->slices, c->stride, n, kd, cudaMemcpyDeviceToHost, s));
   if (!tail.empty())
     CK(cudaMemcpyAsync(tail.data(), c->tail, tail.size(), cudaMemcpyDeviceToHost, s));
@@ -701,6 +705,7 @@ int major_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s) {
       img.insert(img.end(), ob.begin() + c->oofs[col], ob.begin() + c->oofs[col] + c->nout[col]);
     }
     if (c->m) img.push_back(0);  // finish_write_byte before the dense region
+    if (prefix_only) return BUFF_OK;
     for (uint8_t &b : dense) b ^= 0x80;  // the dense slices are stored unflipped
     img.insert(img.end(), dense.begin(), dense.end());
     img.insert(img.end(), tail.begin(), tail.end());
@@ -902,7 +907,8 @@ done:
 }
 
 // (defined with the RAPG entry points below)
-int rapg_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s);
+int rapg_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s,
+               bool prefix_only = false, bool *complete = nullptr);
 }  // namespace
 
 // ================================================================ C ABI
@@ -960,10 +966,27 @@ int buff_serialize(const buff_col *c, uint8_t *out, uint64_t cap, uint64_t *len,
   if (!c || !len) return BUFF_EINVAL;
   if (c->layout == 1 || c->layout == 3) {
     std::vector<uint8_t> img;
-    const int st = c->layout == 1 ? major_image(c, img, S(stream)) : rapg_image(c, img, S(stream));
+    // the header and sparse columns first; the dense slices and tail follow
+    // it, written in place by the device when it can reach `out`
+    bool complete = false;
+    int st = c->layout == 1 ? major_image(c, img, S(stream), true)
+                            : rapg_image(c, img, S(stream), true, &complete);
     if (st) return st;
-    *len = img.size();
-    if (!out || cap < img.size()) return BUFF_EINVAL;
+    const uint64_t body = complete ? 0 : (uint64_t)(c->k - c->m) * c->n + c->tail_bytes;
+    *len = img.size() + body;
+    if (!out || cap < *len) return BUFF_EINVAL;
+    if (!complete && !is_device_ptr(out)) {
+      cudaError_t e = cudaSuccess;
+      memcpy(out, img.data(), img.size());
+      if (buffk::download_body(c, out + img.size(), c->k - c->m, 0x80808080u, S(stream), &e)) {
+        if (e == cudaSuccess) e = cudaStreamSynchronize(S(stream));
+        return cuda_status(e);
+      }
+    }
+    if (!complete) {  // the whole image on the host, then copied
+      st = c->layout == 1 ? major_image(c, img, S(stream)) : rapg_image(c, img, S(stream));
+      if (st) return st;
+    }
     if (is_device_ptr(out)) {
       const cudaError_t e = cudaMemcpy(out, img.data(), img.size(), cudaMemcpyHostToDevice);
       return cuda_status(e);
@@ -982,10 +1005,20 @@ int buff_serialize(const buff_col *c, uint8_t *out, uint64_t cap, uint64_t *len,
   const uint32_t words5[5] = {(uint32_t)ub, (uint32_t)(ub >> 32), c->n, c->ilen, c->dlen};
   for (int i = 0; i < 5; ++i)
     for (int b = 0; b < 4; ++b) hdr[4 * i + b] = (uint8_t)(words5[i] >> (8 * b));
-  if (dev)
+  if (dev) {
     CK(cudaMemcpyAsync(out, hdr, 20, cudaMemcpyHostToDevice, s));
-  else
+  } else {
     memcpy(out, hdr, 20);
+    // host memory the device can write: the kernel puts every slice and tail
+    // byte in place (unflipped for the buff layout)
+    cudaError_t e = cudaSuccess;
+    const uint32_t flipx = (c->flags & BUFF_FLAG_BUFF_LAYOUT) ? 0x80808080u : 0u;
+    if (buffk::download_body(c, out + 20, c->k, flipx, s, &e)) {
+      CK(e);
+      CK(cudaStreamSynchronize(s));
+      goto done;
+    }
+  }
   if (c->k && c->n)
     CK(cudaMemcpy2DAsync(out + 20, c->n, c->slices, c->stride, c->n, c->k, cudaMemcpyDefault, s));
   // the buff layout (byte_fixed_encode) stores the slice bytes unflipped
@@ -2021,18 +2054,24 @@ done:
 // bytes (each column's pad byte is overwritten by the next write, so one pad
 // byte follows the last column); unflipped dense slices; packed tail.  Codes
 // narrower than a byte are packed from byte 20, over the count byte.
-int rapg_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s) {
+// The RAPG image (split_double.rs:624-955).  prefix_only: as major_image,
+// except that codes narrower than a byte (the image is the header and the
+// packed codes) are built whole, *complete set.
+int rapg_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s, bool prefix_only,
+               bool *complete) {
   int rc = BUFF_OK;
   const uint32_t n = c->n, kd = c->k - c->m;
   const size_t nw = ((size_t)n + 31) / 32;
+  if (c->fixed_len < 8) prefix_only = false;
+  if (complete) *complete = !prefix_only;
   std::vector<uint32_t> bits((size_t)c->m * nw);
   std::vector<uint8_t> ob(c->oofs[c->m]);
-  std::vector<uint8_t> dense((size_t)kd * n), tail(c->tail_bytes);
+  std::vector<uint8_t> dense(prefix_only ? 0 : (size_t)kd * n), tail(prefix_only ? 0 : c->tail_bytes);
   for (uint32_t col = 0; col < c->m; ++col)
     CK(cudaMemcpyAsync(bits.data() + col * nw, c->obits + col * c->nwp, nw * 4,
                        cudaMemcpyDeviceToHost, s));
   if (!ob.empty()) CK(cudaMemcpyAsync(ob.data(), c->obytes, ob.size(), cudaMemcpyDeviceToHost, s));
-  if (kd && n)
+  if (!prefix_only && kd && n)
     CK(cudaMemcpy2DAsync(dense.data(), n, c->slices, c->stride, n, kd, cudaMemcpyDeviceToHost, s));
   if (!tail.empty())
     CK(cudaMemcpyAsync(tail.data(), c->tail, tail.size(), cudaMemcpyDeviceToHost, s));
@@ -2062,6 +2101,7 @@ int rapg_image(const buff_col *c, std::vector<uint8_t> &img, cudaStream_t s) {
       img.insert(img.end(), ob.begin() + c->oofs[col], ob.begin() + c->oofs[col] + c->nout[col]);
     }
     if (c->m) img.push_back(0);
+    if (prefix_only) return BUFF_OK;
     for (uint8_t &b : dense) b ^= 0x80;  // the dense slices are stored unflipped
     img.insert(img.end(), dense.begin(), dense.end());
     img.insert(img.end(), tail.begin(), tail.end());

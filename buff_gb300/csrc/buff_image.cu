@@ -379,6 +379,69 @@ __global__ void __launch_bounds__(kImgThreads) k_upload_slices(const uint8_t *sl
   }
 }
 
+// The body of a serialized image (the k slices, then the packed tail)
+// written by the device straight into its destination -- host memory the
+// device can reach (buff_serialize): blockIdx.y names the segment (slice j,
+// or the tail at y = k), whose bytes go to dst + y * n.  A thread writes one
+// 16-byte aligned block of the destination with one store, gathered from
+// the two aligned 16-byte source vectors that hold it (the source offset of
+// every block of a segment has the same remainder mod 16); the partial
+// blocks at a segment's two ends are written byte by byte, so neighbouring
+// segments and the header are never overwritten.  flipx is XORed into the
+// slice bytes (0x80808080 for the buff layout's unflipped image).
+__global__ void __launch_bounds__(256) k_download_image(const uint8_t *__restrict__ slices,
+                                                        size_t stride, uint32_t n, uint32_t k,
+                                                        const uint8_t *__restrict__ tail,
+                                                        uint64_t tail_bytes, uint64_t tail_alloc,
+                                                        uint32_t flipx, uint8_t *dst) {
+  const uint32_t y = blockIdx.y;
+  const uint8_t *src = y < k ? slices + (size_t)y * stride : tail;
+  const uint64_t len = y < k ? n : tail_bytes;
+  const uint64_t cap = y < k ? stride : tail_alloc;  // source bytes that may be read
+  const uint32_t fx = y < k ? flipx : 0u;
+  uint8_t *out = dst + (uint64_t)y * n;  // the segment's first destination byte
+  if (!len) return;
+  const uintptr_t a0 = reinterpret_cast<uintptr_t>(out);
+  const uint64_t head = (16 - (a0 & 15)) & 15;        // bytes before the first aligned block
+  uint64_t nfull = len > head ? (len - head) / 16 : 0;
+  // a block with an unaligned source also reads the next 16 source bytes:
+  // keep those inside the source allocation (the rest go byte by byte)
+  if (head && nfull && 16 * (nfull + 1) > cap) nfull = cap / 16 - 1;
+  const uint64_t tstart = head + nfull * 16;           // bytes after the last aligned block
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t nth = (uint64_t)gridDim.x * blockDim.x;
+  // source offset head + 16b of block b: remainder s = head mod 16, words at
+  // src + 16 * floor((head + 16 b) / 16)
+  const uint32_t srem = (uint32_t)(head & 15), sw = srem >> 2, sb = (srem & 3) * 8;
+  const uint8_t *sbase = src + (head & ~15ull);
+  for (uint64_t b = tid; b < nfull; b += nth) {
+    const uint4 lo = __ldg(reinterpret_cast<const uint4 *>(sbase + 16 * b));
+    uint4 hi = make_uint4(0, 0, 0, 0);
+    if (srem) hi = __ldg(reinterpret_cast<const uint4 *>(sbase + 16 * b + 16));
+    const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+    uint32_t o[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t a = w[q], c = w[q + 1];
+#pragma unroll
+      for (uint32_t t = 1; t < 4; ++t)
+        if (sw == t) {
+          a = w[q + t];
+          c = w[q + t + 1];
+        }
+      o[q] = __funnelshift_r(a, c, sb) ^ fx;
+    }
+    *reinterpret_cast<uint4 *>(out + head + 16 * b) = make_uint4(o[0], o[1], o[2], o[3]);
+  }
+  // the partial blocks at both ends, byte by byte
+  const uint64_t nhead = head < len ? head : len;
+  const uint64_t ntail = len > tstart ? len - tstart : 0;
+  for (uint64_t e = tid; e < nhead + ntail; e += nth) {
+    const uint64_t i = e < nhead ? e : tstart + (e - nhead);
+    out[i] = src[i] ^ (uint8_t)fx;
+  }
+}
+
 inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // A device-accessible address for `p`: device memory as is, pinned host
@@ -639,6 +702,26 @@ extern "C" int buff_range_filter_sum_image(const uint8_t *image, uint64_t len, u
 }
 
 namespace buffk {
+// Writes the `nslices` slices of c (XOR flipx) and then its packed tail into
+// `dst` through k_download_image when the device can write there in place;
+// returns false (nothing done) when it cannot.
+bool download_body(const buff_col *c, uint8_t *dst, uint32_t nslices, uint32_t flipx,
+                   cudaStream_t s, cudaError_t *err) {
+  uint8_t *d = static_cast<uint8_t *>(const_cast<void *>(device_view(dst, c->device)));
+  if (!d || !c->n) return false;
+  const uint64_t big = c->n > c->tail_bytes ? c->n : c->tail_bytes;
+  uint64_t gx = (big / 16 + 255) / 256;
+  const uint64_t cap = (uint64_t)8 * num_sms(c->device) / (nslices + 1) + 1;
+  if (gx > cap) gx = cap;
+  if (gx < 1) gx = 1;
+  dim3 grid((unsigned)gx, nslices + 1);
+  k_download_image<<<grid, 256, 0, s>>>(c->slices, c->stride, c->n, nslices, c->tail,
+                                        c->tail_bytes, c->tail_alloc, flipx, d);
+  count_launch();
+  *err = cudaGetLastError();
+  return true;
+}
+
 // Copies the k slices of a serialized image (image + 20, slice j at j * n;
 // host or device memory) into c->slices through k_upload_slices when the
 // device can read the image in place; returns false (nothing done) when it

@@ -163,6 +163,12 @@ cudaError_t flip_bytes(uint8_t *p, size_t nbytes, cudaStream_t s);
 // image (nothing launched).  flipx = 0x80808080 for the buff layout.
 bool upload_slices(const uint8_t *image, buff_col *c, uint32_t flipx, cudaStream_t s,
                    cudaError_t *err);
+// The first `nslices` slices of c (XOR flipx), then its packed tail, written
+// by the device at dst where it lies (host memory the device can write: the
+// body of a serialized image); false when the device cannot reach it
+// (nothing launched).
+bool download_body(const buff_col *c, uint8_t *dst, uint32_t nslices, uint32_t flipx,
+                   cudaStream_t s, cudaError_t *err);
 // Filters of the buff-major layout; with m == 0 the same compare runs over a
 // plain column's slices and tail.  cand (may be null) restricts the rows.
 cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, uint32_t ttail,
