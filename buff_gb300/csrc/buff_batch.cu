@@ -730,15 +730,18 @@ __device__ __forceinline__ void cmp32_t(const uint4 &a, const uint4 &b, uint32_t
   eq = gather32(e);
 }
 
-__device__ __forceinline__ uint32_t dp4a_sum8(const uint4 &a, const uint4 &b, uint32_t acc) {
-  acc = __dp4a(a.x ^ H, 0x01010101u, acc);
-  acc = __dp4a(a.y ^ H, 0x01010101u, acc);
-  acc = __dp4a(a.z ^ H, 0x01010101u, acc);
-  acc = __dp4a(a.w ^ H, 0x01010101u, acc);
-  acc = __dp4a(b.x ^ H, 0x01010101u, acc);
-  acc = __dp4a(b.y ^ H, 0x01010101u, acc);
-  acc = __dp4a(b.z ^ H, 0x01010101u, acc);
-  acc = __dp4a(b.w ^ H, 0x01010101u, acc);
+// Sum of the 32 bytes as signed int8: a stored (flipped) byte s holds the
+// code byte s ^ 0x80 = int8(s) + 128, so the code-byte sum is this plus 128
+// per byte, added once per lane at the end (no per-word flip).
+__device__ __forceinline__ int dp4a_sum8(const uint4 &a, const uint4 &b, int acc) {
+  acc = __dp4a((int)a.x, 0x01010101, acc);
+  acc = __dp4a((int)a.y, 0x01010101, acc);
+  acc = __dp4a((int)a.z, 0x01010101, acc);
+  acc = __dp4a((int)a.w, 0x01010101, acc);
+  acc = __dp4a((int)b.x, 0x01010101, acc);
+  acc = __dp4a((int)b.y, 0x01010101, acc);
+  acc = __dp4a((int)b.z, 0x01010101, acc);
+  acc = __dp4a((int)b.w, 0x01010101, acc);
   return acc;
 }
 
@@ -750,8 +753,8 @@ __device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_
   unsigned long long *const acc = qd.acc;
   const uint32_t fill = qd.fill;
   const uint32_t c32 = q.r ? 32 % q.r : 0u;  // tail phase step per word
-  uint32_t sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  uint32_t tacc = 0, cnt = 0;
+  int sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // signed byte sums (dp4a_sum8)
+  uint32_t tacc = 0, cnt = 0, nact = 0;  // nact: steps the lane summed 32 bytes of each slice
   __syncwarp();  // the ring may still be read by the previous item
 #pragma unroll
   for (int d = 0; d < kDepth - 1; ++d)
@@ -767,6 +770,7 @@ __device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_
     const bool act = row0 < r1;
     uint32_t valid = 0, eq = 0, gt = 0;
     if (act) {
+      ++nact;
       const uint32_t left = q.n - row0;
       valid = left >= 32 ? 0xFFFFFFFFu : ((1u << left) - 1u);
       eq = valid;
@@ -859,7 +863,8 @@ __device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_
 #pragma unroll
   for (uint32_t j = 0; j < 8; ++j) {
     if (j >= q.k) break;
-    const unsigned long long sj = warp_sum_ull(sacc[j]);
+    const unsigned long long sj =
+        warp_sum_ull((unsigned long long)((long long)sacc[j] + 4096ll * nact));
     if (lane == 0 && sj) atomicAdd(acc + 1 + j, sj);
   }
   if (q.r) {

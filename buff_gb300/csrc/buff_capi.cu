@@ -478,7 +478,7 @@ int filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t *count
       CK(scratch(&dcount, 1, s));
     else
       dcount = reinterpret_cast<unsigned long long *>(count);
-    CK(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s));
+    CK(buffk::zero_u64(dcount, 1, s));
   }
   if (action == 2) {
     a.words = dwords;
@@ -512,7 +512,7 @@ int sum_partials(const buff_col *c, uint32_t total, unsigned long long *d, cudaS
   if (ks > c->k) return BUFF_EREFPANIC;  // reads past the slices (slice index panic)
   if (c->k && ks < c->k && ts) return BUFF_ENOTSUP;
   if (c->k && total < 8 && total > 0) return BUFF_ENOTSUP;
-  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 9, s);
+  cudaError_t e = buffk::zero_u64(d, 9, s);
   if (e != cudaSuccess) return cuda_status(e);
   return cuda_status(buffk::launch_sum(c, ks, ts, d, s));
 }
@@ -1232,13 +1232,12 @@ int buff_range_filter_sum(const buff_col *c, double pred, uint32_t *words, uint6
         CK(scratch(&dcount, 1, s));
       else
         dcount = reinterpret_cast<unsigned long long *>(count);
-      CK(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s));
     }
     if (parts_host)
       CK(scratch(&dparts, 9, s));
     else
       dparts = reinterpret_cast<unsigned long long *>(partials);
-    CK(cudaMemsetAsync(dparts, 0, sizeof(unsigned long long) * 9, s));
+    CK(buffk::zero_u64(dparts, 9, s, dcount, 1));
     a.words = dwords;
     a.count = dcount;
     CK(buffk::launch_filter_sum(a, c, dparts, s));
@@ -1318,7 +1317,7 @@ int buff_max_async(const buff_col *c, uint64_t *dev_max_code, void *stream) {
   if (!c || !dev_max_code) return BUFF_EINVAL;
   if (c->layout != 0) return BUFF_ENOTSUP;  // buff-major columns: the *_majority calls
   cudaStream_t s = S(stream);
-  cudaError_t e = cudaMemsetAsync(dev_max_code, 0, sizeof(uint64_t), s);
+  cudaError_t e = buffk::zero_u64(reinterpret_cast<unsigned long long *>(dev_max_code), 1, s);
   if (e != cudaSuccess) return cuda_status(e);
   return cuda_status(
       buffk::launch_max(c, reinterpret_cast<unsigned long long *>(dev_max_code), s));
@@ -1337,7 +1336,7 @@ int buff_max(const buff_col *c, double *max_value, uint64_t *max_code, uint32_t 
   const bool intended = c->flags & BUFF_FLAG_INTENDED;
   const bool words_dev = argmax_words && is_device_ptr(argmax_words);
   CK(scratch(&d, 2, s));
-  CK(cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), s));
+  CK(buffk::zero_u64(d, 2, s));
   if (c->n) CK(buffk::launch_max(c, d, s));
   if (argmax_words || argmax_count) {
     // byte_fixed_max fills `res` only in the tail step (or for fixed_len < 8).

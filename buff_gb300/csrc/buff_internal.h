@@ -137,6 +137,10 @@ cudaError_t launch_encode_scatter_f64(const double *x, const buff_col *c, cudaSt
 cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStream_t s,
                                       uint8_t *lead = nullptr, uint32_t nlead = 0);
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t s);
+// n u64 words at p and m at q (8-byte aligned device memory; q may be null)
+// set to 0 by one kernel.
+cudaError_t zero_u64(unsigned long long *p, uint32_t n, cudaStream_t s,
+                     unsigned long long *q = nullptr, uint32_t m = 0);
 cudaError_t launch_fill_words(uint32_t *words, uint32_t n, uint32_t value,
                               unsigned long long *count, cudaStream_t s);
 // Sums of the first k_used slices and of the packed tail read as `tail_bits`-bit

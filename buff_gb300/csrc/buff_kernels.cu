@@ -439,6 +439,16 @@ __global__ void k_fill_words(uint32_t *words, uint32_t n, uint32_t value,
   if (count && blockIdx.x == 0 && threadIdx.x == 0) *count = value ? n : 0;
 }
 
+// Zeroes n u64 result words (counts, partial sums) ahead of the kernel that
+// accumulates into them: a kernel node, so the stream (or a graph recorded
+// from it) stays on the SMs instead of switching to a copy engine for a
+// memset of a few bytes.
+__global__ void k_zero_u64(unsigned long long *p, uint32_t n, unsigned long long *q, uint32_t m) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0;
+  if (i < m) q[i] = 0;
+}
+
 // ---------------------------------------------------------------- sum
 
 // byte_fixed_sum (compress/split_double.rs:2127-2208): the per-slice sums of
@@ -1227,6 +1237,16 @@ cudaError_t launch_fill_words(uint32_t *words, uint32_t n, uint32_t value,
   if (grid < 1) grid = 1;
   if (grid > 8 * num_sms(cur_device())) grid = 8 * num_sms(cur_device());
   k_fill_words<<<grid, kThreads, 0, s>>>(words, n, value, count);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t zero_u64(unsigned long long *p, uint32_t n, cudaStream_t s, unsigned long long *q,
+                     uint32_t m) {
+  if (!q) m = 0;
+  const uint32_t big = n > m ? n : m;
+  if (!big) return cudaSuccess;
+  k_zero_u64<<<(big + 255) / 256, 256, 0, s>>>(p, n, q, m);
   count_launch();
   return cudaGetLastError();
 }

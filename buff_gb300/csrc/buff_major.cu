@@ -356,16 +356,37 @@ __global__ void __launch_bounds__(kThreads, 4) k_filter_major1(MajorArgs a) {
   bool pre = two;  // warp-uniform: load the second dense slice with the first
   uint32_t qn = 0;  // warp-uniform queue length
   uint32_t cnt = 0;
-  for (uint32_t base = warp * 32; base < nwords; base += nwarps * 32) {
+  const uint32_t step = nwarps * 32;
+  // the loads of a lane's next block are issued before the compares of its
+  // current one (two blocks in flight per lane)
+  uint32_t nB = 0, nR = 0;
+  Bytes32 nd0, nd1;
+  bool npre = pre;
+  {
+    const uint32_t w = warp * 32 + lane;
+    if (w < nwords) {
+      nB = __ldg(a.obits + w);
+      nR = __ldg(a.orank + w);
+      nd0 = ld_stream32(a.slices + (size_t)w * 32);
+      if (npre) nd1 = ld_stream32(s1 + (size_t)w * 32);
+    }
+  }
+  for (uint32_t base = warp * 32; base < nwords; base += step) {
     const uint32_t w = base + lane;
     const bool live = w < nwords;
-    uint32_t B = 0, R = 0;
-    Bytes32 d0, d1;
-    if (live) {
-      B = __ldg(a.obits + w);
-      R = __ldg(a.orank + w);
-      d0 = ld_stream32(a.slices + (size_t)w * 32);
-      if (pre) d1 = ld_stream32(s1 + (size_t)w * 32);
+    const uint32_t B = nB, R = nR;
+    const Bytes32 d0 = nd0;
+    Bytes32 d1 = nd1;
+    const bool dpre = npre;
+    {
+      const uint32_t wn = w + step;
+      npre = pre;
+      if (wn < nwords) {
+        nB = __ldg(a.obits + wn);
+        nR = __ldg(a.orank + wn);
+        nd0 = ld_stream32(a.slices + (size_t)wn * 32);
+        if (npre) nd1 = ld_stream32(s1 + (size_t)wn * 32);
+      }
     }
     const uint32_t row0 = w * 32;
     const uint32_t valid =
@@ -395,7 +416,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_filter_major1(MajorArgs a) {
     const bool need1 = two && eq != 0;
     const uint32_t vote = __ballot_sync(0xFFFFFFFFu, need1);
     if (need1) {
-      if (!pre) d1 = ld_cand32(s1 + row0);
+      if (!dpre) d1 = ld_cand32(s1 + row0);
       uint32_t m[8];
 #pragma unroll
       for (int qq = 0; qq < 8; ++qq) m[qq] = eq4t<TH2>(d1.w[qq], b0, b1);
