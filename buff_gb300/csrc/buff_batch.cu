@@ -745,6 +745,33 @@ __device__ __forceinline__ int dp4a_sum8(const uint4 &a, const uint4 &b, int acc
   return acc;
 }
 
+// Bits 0, R, 2R, ... of a word.
+constexpr uint32_t every_bit(int R) {
+  uint32_t p = 0;
+  for (int b = 0; b < 32; b += R) p |= 1u << b;
+  return p;
+}
+
+// Tail sum of a lane's 32 rows whose R-bit fields fill the R words at tp
+// (the rows all below n): bit b of word i sits at stream position 32i + b,
+// which weighs 2^((32i + b) mod R) -- wpopc with the phase of every word and
+// the class masks resolved at compile time (3 R^2 operations instead of
+// about 7 R^2 with a run-time width).
+template <int R>
+__device__ __forceinline__ uint32_t tail_sum32(const uint32_t *tp) {
+  uint32_t acc = 0;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const uint32_t w = tp[i];
+#pragma unroll
+    for (int c = 0; c < R; ++c) {
+      const int sh = ((c - 32 * i) % R + R) % R;  // bits of class c in word i
+      acc += (uint32_t)__popc(w & (every_bit(R) << sh)) << c;
+    }
+  }
+  return acc;
+}
+
 template <bool DO_F>
 __device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_t r1,
                                               uint32_t lane, uint8_t *ring) {
@@ -818,25 +845,37 @@ __device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_
       if (q.r) {
         // the lane's 32 fields: r words at byte 4r * lane of the step's tail
         const uint32_t *tp = reinterpret_cast<const uint32_t *>(slot + 3 * kStepRows) + lane * q.r;
-        uint32_t tw[8];
+        if (valid == 0xFFFFFFFFu) {
+          switch (q.r) {  // warp-uniform
+            case 1: tacc += tail_sum32<1>(tp); break;
+            case 2: tacc += tail_sum32<2>(tp); break;
+            case 3: tacc += tail_sum32<3>(tp); break;
+            case 4: tacc += tail_sum32<4>(tp); break;
+            case 5: tacc += tail_sum32<5>(tp); break;
+            case 6: tacc += tail_sum32<6>(tp); break;
+            default: tacc += tail_sum32<7>(tp); break;
+          }
+        } else {  // the column's last rows: only the fields of rows below n
+          const uint32_t nbits = left_bits(q.n, row0, q.r);  // stream bits of the lane's rows
+          uint32_t ph = 0;  // the lane's fields start at a multiple of r
 #pragma unroll
-        for (uint32_t i = 0; i < 8; ++i) tw[i] = i < q.r ? tp[i] : 0u;
-        const uint32_t nbits = left_bits(q.n, row0, q.r);  // stream bits of the lane's rows
-        uint32_t ph = 0;  // the lane's fields start at a multiple of r
-#pragma unroll
-        for (uint32_t i = 0; i < 7; ++i) {
-          if (i < q.r) {
-            uint32_t word = tw[i];
-            if (32 * i >= nbits)
-              word = 0;
-            else if (32 * i + 32 > nbits)
-              word &= (1u << (nbits - 32 * i)) - 1u;
-            tacc += wpopc(word, ph, q.r);
-            ph += c32;
-            if (ph >= q.r) ph -= q.r;
+          for (uint32_t i = 0; i < 7; ++i) {
+            if (i < q.r) {
+              uint32_t word = tp[i];
+              if (32 * i >= nbits)
+                word = 0;
+              else if (32 * i + 32 > nbits)
+                word &= (1u << (nbits - 32 * i)) - 1u;
+              tacc += wpopc(word, ph, q.r);
+              ph += c32;
+              if (ph >= q.r) ph -= q.r;
+            }
           }
         }
         if (q.cmp && q.r_used && eq) {
+          uint32_t tw[8];
+#pragma unroll
+          for (uint32_t i = 0; i < 8; ++i) tw[i] = i < q.r ? tp[i] : 0u;
           uint32_t gtt = 0, eqt = 0, b = eq;
           while (b) {
             const uint32_t i = __ffs(b) - 1;
@@ -900,13 +939,18 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
     if (lane == 0) it = atomicAdd(counter, 1u);
     it = __shfl_sync(0xFFFFFFFFu, it, 0);
     if (it >= nitems) return;
+    // the query of item `it`: the last i with prefix[i] <= it, found by the
+    // whole warp 32-ary (lane l probes lo + l*step), two or three dependent
+    // loads for thousands of queries instead of a binary search's dozen
     uint32_t lo = 0, hi = nq;
     while (hi - lo > 1) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (__ldg(prefix + mid) <= it)
-        lo = mid;
-      else
-        hi = mid;
+      const uint32_t step = (hi - lo + 31) >> 5;
+      const uint32_t pos = lo + lane * step;
+      const bool le = pos < hi && __ldg(prefix + pos) <= it;
+      const uint32_t b = __ballot_sync(0xFFFFFFFFu, le);  // lane 0 always: prefix[lo] <= it
+      const uint32_t j = 31 - __clz(b);
+      lo += j * step;
+      hi = min(hi, lo + step);
     }
     const BQ &q = qs[__ldg(qidx + lo)];
     const uint32_t r0 = (it - __ldg(prefix + lo)) * tile;
@@ -1253,9 +1297,10 @@ cudaError_t enqueue(buff_plan *p, cudaStream_t s) {
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(p->d_sched, p->h_sched, sizeof(uint32_t) * p->sc.words,
                         cudaMemcpyHostToDevice, s);
+  // the accumulators and the 4 work counters (2 u64 words) zeroed by one kernel
   if (e == cudaSuccess)
-    e = cudaMemsetAsync(p->d_acc, 0, sizeof(unsigned long long) * kAcc * p->nq, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned int) * 4, s);
+    e = zero_u64(p->d_acc, kAcc * p->nq, s,
+                 reinterpret_cast<unsigned long long *>(p->d_counter), 2);
   if (e == cudaSuccess) e = batch_launch(p->d_q, p->d_sched, p->sc, p->tune, p->d_counter, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(p->h_acc, p->d_acc, sizeof(unsigned long long) * kAcc * p->nq,

@@ -739,7 +739,7 @@ int filter_major_impl(const buff_col *c, double pred, uint32_t *words, uint64_t 
       CK(scratch(&dcount, 1, s));
     else
       dcount = reinterpret_cast<unsigned long long *>(count);
-    CK(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s));
+    CK(buffk::zero_u64(dcount, 1, s));
   }
   if (early)
     CK(buffk::launch_fill_words(dwords, n, is_range ? 0xFFFFFFFFu : 0u, dcount, s));
@@ -885,7 +885,7 @@ int filter_cond_impl(const buff_col *c, double pred, const uint32_t *cand, uint3
       CK(scratch(&dcount, 1, s));
     else
       dcount = reinterpret_cast<unsigned long long *>(count);
-    CK(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s));
+    CK(buffk::zero_u64(dcount, 1, s));
   }
   if (none) {
     CK(buffk::launch_fill_words(dwords, n, 0u, dcount, s));
@@ -1655,7 +1655,7 @@ buffk::dev::MajorSumArgs major_sum_args(const buff_col *c) {
 // The raw byte sums of a buff-major column into d (24 u64, device): sparse
 // columns' outlier bytes at d[0..m), dense slices and tail from d[8].
 int major_raw_sums(const buff_col *c, unsigned long long *d, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 24, s);
+  cudaError_t e = buffk::zero_u64(d, 24, s);
   for (uint32_t col = 0; col < c->m && e == cudaSuccess; ++col)
     if (c->nout[col]) e = buffk::major_bytesum(c->obytes + c->oofs[col], c->nout[col], d + col, s);
   if (e == cudaSuccess && c->n) e = buffk::launch_sum(c, c->k - c->m, c->r, d + 8, s);
@@ -2193,7 +2193,7 @@ int rapg_sum_impl(const buff_col *c, int precision, double *sum, cudaStream_t s)
   unsigned long long *d = nullptr;
   uint64_t h[40] = {0};
   CK(scratch(&d, 40, s));
-  CK(cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 40, s));
+  CK(buffk::zero_u64(d, 40, s));
   for (uint32_t col = 0; col < m; ++col)
     if (c->nout[col]) CK(buffk::major_bytesum(c->obytes + c->oofs[col], c->nout[col], d + col, s));
   if (n && ks_dense) CK(buffk::launch_sum(c, ks_dense, 0, d + 8, s));
@@ -2561,7 +2561,7 @@ int slice_filter_impl(const buff_col *c, double pred, uint32_t *words, uint64_t 
       CK(scratch(&dcount, 1, s));
     else
       dcount = reinterpret_cast<unsigned long long *>(count);
-    CK(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s));
+    CK(buffk::zero_u64(dcount, 1, s));
   }
   if (early) {
     CK(buffk::launch_fill_words(dwords, n, 0xFFFFFFFFu, dcount, s));
@@ -2604,7 +2604,7 @@ int slice_sum_impl(const buff_col *c, double *sum, cudaStream_t s, bool any_widt
   unsigned long long *d = nullptr;
   uint64_t parts[9] = {0};
   CK(scratch(&d, 9, s));
-  CK(cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 9, s));
+  CK(buffk::zero_u64(d, 9, s));
   CK(buffk::launch_sum(c, c->k, 0, d, s));
   CK(cudaMemcpyAsync(parts, d, sizeof(parts), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -2641,7 +2641,7 @@ int slice_max_impl(const buff_col *c, double *max_value, uint32_t *argmax_words,
     return BUFF_OK;
   }
   CK(scratch(&d, 2, s));
-  CK(cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), s));
+  CK(buffk::zero_u64(d, 2, s));
   CK(buffk::launch_max(c, d, s));
   if (argmax_words || argmax_count) {
     if (argmax_words && words_dev)

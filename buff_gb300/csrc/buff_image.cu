@@ -591,7 +591,7 @@ extern "C" int buff_filter_image(const uint8_t *image, uint64_t len, uint64_t sc
   unsigned long long *d = nullptr;
   unsigned long long host = 0;
   cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&d), sizeof(unsigned long long), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = buffk::zero_u64(d, 1, s);
   if (e == cudaSuccess) {
     a.count = d;
     void (*fn)(ImgFilterArgs) = fa.is_range ? k_filter_image<true> : k_filter_image<false>;
@@ -666,7 +666,7 @@ extern "C" int buff_range_filter_sum_image(const uint8_t *image, uint64_t len, u
   unsigned long long *d = nullptr;  // 9 partials, then the count
   uint64_t host[10] = {0};
   cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&d), 10 * sizeof(unsigned long long), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, 10 * sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = buffk::zero_u64(d, 10, s);
   if (e == cudaSuccess) {
     a.parts = d;
     a.count = d + 9;

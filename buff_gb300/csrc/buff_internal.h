@@ -138,7 +138,8 @@ cudaError_t launch_encode_scatter_f32(const float *x, const buff_col *c, cudaStr
                                       uint8_t *lead = nullptr, uint32_t nlead = 0);
 cudaError_t launch_filter(const FilterArgs &a, cudaStream_t s);
 // n u64 words at p and m at q (8-byte aligned device memory; q may be null)
-// set to 0 by one kernel.
+// set to 0: by one kernel while s is being captured or when q is given, else
+// by a memset (less host time per call).
 cudaError_t zero_u64(unsigned long long *p, uint32_t n, cudaStream_t s,
                      unsigned long long *q = nullptr, uint32_t m = 0);
 cudaError_t launch_fill_words(uint32_t *words, uint32_t n, uint32_t value,

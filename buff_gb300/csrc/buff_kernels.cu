@@ -440,9 +440,9 @@ __global__ void k_fill_words(uint32_t *words, uint32_t n, uint32_t value,
 }
 
 // Zeroes n u64 result words (counts, partial sums) ahead of the kernel that
-// accumulates into them: a kernel node, so the stream (or a graph recorded
-// from it) stays on the SMs instead of switching to a copy engine for a
-// memset of a few bytes.
+// accumulates into them.  In a graph a kernel node keeps the chain on the
+// SMs: a copy-engine memset node between two kernels costs about a
+// microsecond of engine switching on each side.
 __global__ void k_zero_u64(unsigned long long *p, uint32_t n, unsigned long long *q, uint32_t m) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = 0;
@@ -1246,6 +1246,11 @@ cudaError_t zero_u64(unsigned long long *p, uint32_t n, cudaStream_t s, unsigned
   if (!q) m = 0;
   const uint32_t big = n > m ? n : m;
   if (!big) return cudaSuccess;
+  // issued from the host, one memset costs the caller less than a launch;
+  // recorded into a graph, the kernel keeps the nodes on the SMs
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (!m && cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone)
+    return cudaMemsetAsync(p, 0, sizeof(unsigned long long) * n, s);
   k_zero_u64<<<(big + 255) / 256, 256, 0, s>>>(p, n, q, m);
   count_launch();
   return cudaGetLastError();

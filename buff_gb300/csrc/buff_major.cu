@@ -1289,7 +1289,9 @@ cudaError_t major_max(const buff_col *c, uint32_t *cand, void *state_dev, cudaSt
   const size_t nw = ((size_t)c->n + 31) / 32;
   const uint32_t kd = c->k - c->m;
   const int g = grid_of(c->nwp, 256);
-  cudaError_t e = cudaMemsetAsync(st, 0, sizeof(MaxState), s);
+  static_assert(sizeof(MaxState) % 8 == 0, "MaxState is zeroed as u64 words");
+  cudaError_t e =
+      zero_u64(reinterpret_cast<unsigned long long *>(st), sizeof(MaxState) / 8, s);
   if (e != cudaSuccess) return e;
   uint32_t step = 0;
   for (uint32_t col = 0; col < c->m; ++col, ++step) {
@@ -1326,7 +1328,8 @@ cudaError_t major_max(const buff_col *c, uint32_t *cand, void *state_dev, cudaSt
     }
     count_launch(2);
   } else {
-    e = cudaMemsetAsync(cand, 0, sizeof(uint32_t) * c->nwp, s);
+    // nwp is a multiple of 16 (the slice stride is a multiple of 512 rows)
+    e = zero_u64(reinterpret_cast<unsigned long long *>(cand), c->nwp / 2, s);
     if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
