@@ -1655,11 +1655,7 @@ buffk::dev::MajorSumArgs major_sum_args(const buff_col *c) {
 // The raw byte sums of a buff-major column into d (24 u64, device): sparse
 // columns' outlier bytes at d[0..m), dense slices and tail from d[8].
 int major_raw_sums(const buff_col *c, unsigned long long *d, cudaStream_t s) {
-  cudaError_t e = buffk::zero_u64(d, 24, s);
-  for (uint32_t col = 0; col < c->m && e == cudaSuccess; ++col)
-    if (c->nout[col]) e = buffk::major_bytesum(c->obytes + c->oofs[col], c->nout[col], d + col, s);
-  if (e == cudaSuccess && c->n) e = buffk::launch_sum(c, c->k - c->m, c->r, d + 8, s);
-  return cuda_status(e);
+  return cuda_status(buffk::major_sums(c, major_sum_args(c), d, nullptr, nullptr, s));
 }
 }  // namespace
 
@@ -1703,9 +1699,8 @@ int buff_sum_majority_async(const buff_col *c, double *dev_sum, uint64_t *dev_pa
   int rc = BUFF_OK;
   unsigned long long *d = nullptr;
   CK(scratch(&d, 24, s));
-  if ((rc = major_raw_sums(c, d, s))) goto done;
-  CK(buffk::major_sum_combine(major_sum_args(c), d, dev_sum,
-                              reinterpret_cast<unsigned long long *>(dev_partials), s));
+  CK(buffk::major_sums(c, major_sum_args(c), d, dev_sum,
+                       reinterpret_cast<unsigned long long *>(dev_partials), s));
 done:
   if (d) cudaFreeAsync(d, s);
   return rc;
@@ -1722,6 +1717,18 @@ int buff_max_majority(const buff_col *c, double *max_value, uint64_t *max_code,
   uint64_t res[2] = {0, 0};  // max code, arg-max count
   const size_t nw = ((size_t)c->n + 31) / 32;
   const size_t sb = buffk::major_max_state_bytes(), mo = buffk::major_max_state_mx_offset();
+  if (c->n && !argmax_words && !argmax_count && buffk::major1_max_applies(c)) {
+    // the value alone: one pass (the arg-max rows need the candidate steps)
+    CK(scratch(&st, sb, s));
+    unsigned long long *mx = reinterpret_cast<unsigned long long *>(st + mo);
+    CK(buffk::major1_max(c, mx, s));
+    CK(cudaMemcpyAsync(res, mx, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (max_code) *max_code = res[0];
+    if (max_value)
+      *max_value = (double)(int64_t)((uint64_t)c->base + res[0]) / ldexp(1.0, (int)c->dlen);
+    goto done;
+  }
   CK(scratch(&cand, c->nwp, s));
   CK(scratch(&st, sb, s));
   if (c->n) {
@@ -1750,6 +1757,9 @@ int buff_max_majority_async(const buff_col *c, uint64_t *dev_max_code, void *str
   unsigned char *st = nullptr;
   const size_t sb = buffk::major_max_state_bytes(), mo = buffk::major_max_state_mx_offset();
   if (!c->n) return cuda_status(cudaMemsetAsync(dev_max_code, 0, 8, s));
+  if (buffk::major1_max_applies(c))
+    return cuda_status(
+        buffk::major1_max(c, reinterpret_cast<unsigned long long *>(dev_max_code), s));
   CK(scratch(&cand, c->nwp, s));
   CK(scratch(&st, sb, s));
   CK(buffk::launch_fill_words(cand, c->n, 0xFFFFFFFFu, nullptr, s));

@@ -254,6 +254,81 @@ __device__ __forceinline__ uint32_t wpopc(uint32_t w, uint32_t phase, uint32_t t
   return acc;
 }
 
+// The slice sums (first ks slices, each a flat array of `stride` bytes whose
+// padding rows hold the flipped zero 0x80) and the packed tail sum (n * ts
+// bits, fields weighed by wpopc) of thread tid of nth, added into the
+// block's s_acc[0..ks) and s_acc[8] (byte_fixed_sum, split_double.rs:2127-2208).
+__device__ __forceinline__ void sum_slices_tail(const uint8_t *__restrict__ slices, size_t stride,
+                                                uint32_t ks, const uint8_t *__restrict__ tail,
+                                                uint32_t ts, unsigned long long tail_bits,
+                                                uint32_t tid, uint32_t nth,
+                                                unsigned long long *s_acc) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nv = (uint32_t)(stride / 16);
+  // A slice rarely divides evenly into grid-stride steps, so some threads
+  // take one step more than the others.  Each slice (and the tail) starts the
+  // threads at a different offset (whole warps), so no thread takes the
+  // extra step in every slice: the kernel ends when the average thread does.
+  const uint32_t rot = (nth / (ks + 1)) & ~31u;
+  for (uint32_t s = 0; s < ks; ++s) {
+    const uint8_t *sl = slices + (size_t)s * stride;
+    uint32_t acc = 0;
+    uint32_t vt = tid + s * rot;
+    if (vt >= nth) vt -= nth;
+    for (uint32_t v0 = vt; v0 < nv; v0 += kU * nth) {
+      uint4 d[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const uint32_t v = v0 + u * nth;
+        d[u] = v < nv ? ld_stream(sl + (size_t)v * 16) : make_uint4(H, H, H, H);
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        acc = __dp4a(d[u].x ^ H, 0x01010101u, acc);
+        acc = __dp4a(d[u].y ^ H, 0x01010101u, acc);
+        acc = __dp4a(d[u].z ^ H, 0x01010101u, acc);
+        acc = __dp4a(d[u].w ^ H, 0x01010101u, acc);
+      }
+    }
+    const unsigned long long w = warp_sum_ull(acc);
+    if (lane == 0 && w) atomicAdd(&s_acc[s], w);
+  }
+  if (ts) {
+    const unsigned long long nbytes = (tail_bits + 7) / 8;
+    const uint32_t ntv = (uint32_t)((nbytes + 15) / 16);
+    unsigned long long acc = 0;
+    uint32_t vt = tid + ks * rot;
+    if (vt >= nth) vt -= nth;
+    // A word starting at stream bit b0 has phase b0 mod ts (wpopc); the
+    // phases are advanced by conditional subtraction, without a division in
+    // the loop.
+    const uint32_t c32 = 32 % ts;                                            // phase step per word
+    const uint32_t cstep = (uint32_t)(((unsigned long long)nth * 128) % ts);  // per grid step
+    uint32_t pv = (uint32_t)(((unsigned long long)vt * 128) % ts);
+    for (uint32_t v = vt; v < ntv; v += nth) {
+      uint4 d = *reinterpret_cast<const uint4 *>(tail + (size_t)v * 16);
+      const uint32_t *w = reinterpret_cast<const uint32_t *>(&d);
+      uint32_t ph = pv;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const unsigned long long b0 = (unsigned long long)v * 128 + 32 * q;
+        uint32_t word = w[q];
+        if (b0 >= tail_bits)
+          word = 0;
+        else if (b0 + 32 > tail_bits)
+          word &= (1u << (uint32_t)(tail_bits - b0)) - 1u;
+        acc += wpopc(word, ph, ts);
+        ph += c32;
+        if (ph >= ts) ph -= ts;
+      }
+      pv += cstep;
+      if (pv >= ts) pv -= ts;
+    }
+    acc = warp_sum_ull(acc);
+    if (lane == 0 && acc) atomicAdd(&s_acc[8], acc);
+  }
+}
+
 // `(v as f64) / 2^dlen` with integer operations only: round-to-nearest-even
 // of the 64-bit integer to a 53-bit significand, then the exponent lowered by
 // dlen (exact: the result stays a normal double for |v| >= 1 and dlen <= 64).
@@ -326,14 +401,16 @@ __device__ __forceinline__ uint32_t eqbytes(uint32_t w, uint32_t bb) {
 // max.  Each later slice is one 32-byte load; the candidates' largest byte
 // and the rows holding it come from per-byte SWAR on the unflipped words.
 // Out of line: it runs for few blocks.
-static __device__ __noinline__ unsigned long long max_in_block(const uint8_t *__restrict__ slices,
-                                                               size_t stride, uint32_t k,
-                                                               const uint8_t *__restrict__ tail,
-                                                               uint32_t r, uint32_t row0,
-                                                               uint32_t cand, uint32_t top) {
+// `next` is the slice after the leading byte and `nmore` the slices from it
+// (a buff-major column's leading byte is a sparse one, its slices all dense).
+static __device__ __noinline__ unsigned long long max_after_top(const uint8_t *__restrict__ next,
+                                                                size_t stride, uint32_t nmore,
+                                                                const uint8_t *__restrict__ tail,
+                                                                uint32_t r, uint32_t row0,
+                                                                uint32_t cand, uint32_t top) {
   unsigned long long prefix = top;
-  for (uint32_t s = 1; s < k; ++s) {
-    const Bytes32 b = ld_cand32(slices + s * stride + row0);
+  for (uint32_t s = 0; s < nmore; ++s) {
+    const Bytes32 b = ld_cand32(next + s * stride + row0);
     uint32_t u[8], mx = 0;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -370,6 +447,15 @@ static __device__ __noinline__ unsigned long long max_in_block(const uint8_t *__
     bt = max(bt, __funnelshift_r(w0, w1, bit & 31) & ((1u << r) - 1u));
   }
   return (prefix << r) | bt;
+}
+
+// The same with slice 0 holding the leading byte (k slices).
+__device__ __forceinline__ unsigned long long max_in_block(const uint8_t *__restrict__ slices,
+                                                           size_t stride, uint32_t k,
+                                                           const uint8_t *__restrict__ tail,
+                                                           uint32_t r, uint32_t row0,
+                                                           uint32_t cand, uint32_t top) {
+  return max_after_top(slices + stride, stride, k ? k - 1 : 0u, tail, r, row0, cand, top);
 }
 
 // buff_sum_majority's combine (compress/buff_simd.rs:2294-2442), shared by

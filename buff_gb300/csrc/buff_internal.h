@@ -188,16 +188,21 @@ cudaError_t exclusive_scan(uint32_t *data, size_t count, uint32_t *tmp, cudaStre
 cudaError_t step_ranks(const uint32_t *words, uint32_t n, uint32_t *rank, cudaStream_t s);
 cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out,
                           cudaStream_t s);
-// buff_sum_majority's combine on the device (one thread): the raw sums
-// (sparse columns at raw[0..m), dense slices and tail from raw[8]) into the
-// f64 sum and, when parts is not null, the k (+1) partials.
-cudaError_t major_sum_combine(const dev::MajorSumArgs &a, const unsigned long long *raw,
-                              double *sum, unsigned long long *parts, cudaStream_t s);
+// buff_sum_majority's sums in one launch after zeroing raw (24 u64): the
+// sparse columns' outlier-byte sums at raw[0..m), the dense slices and the
+// tail from raw[8]; with `sum` set, the last block also combines them into
+// the f64 sum and, when parts is not null, the k (+1) partials.
+cudaError_t major_sums(const buff_col *c, const dev::MajorSumArgs &a, unsigned long long *raw,
+                       double *sum, unsigned long long *parts, cudaStream_t s);
 // buff_max_majority's progressive max on the device: cand (nwp words) ends
 // as the arg-max bitmap; state_dev (major_max_state_bytes(), device) holds
 // the max code (u64 at major_max_state_mx_offset()) and, after it, the
 // arg-max count (u64).
 cudaError_t major_max(const buff_col *c, uint32_t *cand, void *state_dev, cudaStream_t s);
+// One sparse column with rows outside it: the progressive max is the
+// largest code, found in one launch (major1_max) into *out (device u64).
+bool major1_max_applies(const buff_col *c);
+cudaError_t major1_max(const buff_col *c, unsigned long long *out, cudaStream_t s);
 size_t major_max_state_bytes();
 size_t major_max_state_mx_offset();
 cudaError_t popcount_words(const uint32_t *w, size_t nw, unsigned long long *out, cudaStream_t s);

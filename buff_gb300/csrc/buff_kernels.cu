@@ -464,72 +464,8 @@ __global__ void __launch_bounds__(kThreads) k_sum(const uint8_t *__restrict__ sl
   __shared__ unsigned long long s_acc[9];
   if (threadIdx.x < 9) s_acc[threadIdx.x] = 0;
   __syncthreads();
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t nth = gridDim.x * blockDim.x;
-  const uint32_t nv = (uint32_t)(stride / 16);
-  // A slice rarely divides evenly into grid-stride steps, so some threads
-  // take one step more than the others.  Each slice (and the tail) starts the
-  // threads at a different offset (whole warps), so no thread takes the
-  // extra step in every slice: the kernel ends when the average thread does.
-  const uint32_t rot = (nth / (ks + 1)) & ~31u;
-  for (uint32_t s = 0; s < ks; ++s) {
-    const uint8_t *sl = slices + (size_t)s * stride;
-    uint32_t acc = 0;
-    uint32_t vt = tid + s * rot;
-    if (vt >= nth) vt -= nth;
-    for (uint32_t v0 = vt; v0 < nv; v0 += kU * nth) {
-      uint4 d[kU];
-#pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        const uint32_t v = v0 + u * nth;
-        d[u] = v < nv ? ld_stream(sl + (size_t)v * 16) : make_uint4(H, H, H, H);
-      }
-#pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        acc = __dp4a(d[u].x ^ H, 0x01010101u, acc);
-        acc = __dp4a(d[u].y ^ H, 0x01010101u, acc);
-        acc = __dp4a(d[u].z ^ H, 0x01010101u, acc);
-        acc = __dp4a(d[u].w ^ H, 0x01010101u, acc);
-      }
-    }
-    const unsigned long long w = warp_sum_ull(acc);
-    if (lane == 0 && w) atomicAdd(&s_acc[s], w);
-  }
-  if (ts) {
-    const unsigned long long nbytes = (tail_bits + 7) / 8;
-    const uint32_t ntv = (uint32_t)((nbytes + 15) / 16);
-    unsigned long long acc = 0;
-    uint32_t vt = tid + ks * rot;
-    if (vt >= nth) vt -= nth;
-    // A word starting at stream bit b0 has phase b0 mod ts (wpopc); the
-    // phases are advanced by conditional subtraction, without a division in
-    // the loop.
-    const uint32_t c32 = 32 % ts;                                            // phase step per word
-    const uint32_t cstep = (uint32_t)(((unsigned long long)nth * 128) % ts);  // per grid step
-    uint32_t pv = (uint32_t)(((unsigned long long)vt * 128) % ts);
-    for (uint32_t v = vt; v < ntv; v += nth) {
-      uint4 d = *reinterpret_cast<const uint4 *>(tail + (size_t)v * 16);
-      const uint32_t *w = reinterpret_cast<const uint32_t *>(&d);
-      uint32_t ph = pv;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const unsigned long long b0 = (unsigned long long)v * 128 + 32 * q;
-        uint32_t word = w[q];
-        if (b0 >= tail_bits)
-          word = 0;
-        else if (b0 + 32 > tail_bits)
-          word &= (1u << (uint32_t)(tail_bits - b0)) - 1u;
-        acc += wpopc(word, ph, ts);
-        ph += c32;
-        if (ph >= ts) ph -= ts;
-      }
-      pv += cstep;
-      if (pv >= ts) pv -= ts;
-    }
-    acc = warp_sum_ull(acc);
-    if (lane == 0 && acc) atomicAdd(&s_acc[8], acc);
-  }
+  sum_slices_tail(slices, stride, ks, tail, ts, tail_bits, blockIdx.x * blockDim.x + threadIdx.x,
+                  gridDim.x * blockDim.x, s_acc);
   __syncthreads();
   if (threadIdx.x < ks && s_acc[threadIdx.x]) atomicAdd(&partials[threadIdx.x], s_acc[threadIdx.x]);
   if (threadIdx.x == 8 && ts && s_acc[8]) atomicAdd(&partials[ks], s_acc[8]);

@@ -470,9 +470,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_filter_major1(MajorArgs a) {
 // Sum of nbytes bytes from p (any alignment): the bytes before the first
 // 16-byte boundary and after the last one singly, the rest as 16-byte
 // vectors through dp4a.
-__global__ void k_bytesum(const uint8_t *__restrict__ p, size_t nbytes, unsigned long long *out) {
-  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  const size_t nth = (size_t)gridDim.x * blockDim.x;
+__device__ __forceinline__ unsigned long long bytesum_thread(const uint8_t *__restrict__ p,
+                                                             size_t nbytes, size_t tid,
+                                                             size_t nth) {
   size_t head = (16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15;
   if (head > nbytes) head = nbytes;
   const size_t nvec = (nbytes - head) / 16;
@@ -494,8 +494,67 @@ __global__ void k_bytesum(const uint8_t *__restrict__ p, size_t nbytes, unsigned
   const size_t rest = head + nvec * 16;  // bytes before `rest` not in vectors: [0, head)
   if (tid < head) acc += p[tid];
   for (size_t i = rest + tid; i < nbytes; i += nth) acc += p[i];
+  return acc;
+}
+
+__global__ void k_bytesum(const uint8_t *__restrict__ p, size_t nbytes, unsigned long long *out) {
+  unsigned long long acc = bytesum_thread(p, nbytes, blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+                                          (size_t)gridDim.x * blockDim.x);
   acc = warp_sum_ull(acc);
   if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
+
+// The outlier bytes of each sparse column of a buff-major column.
+struct SparseBytes {
+  const uint8_t *p[8];
+  uint32_t n[8];
+  uint32_t m;
+};
+
+// buff_sum_majority's sums (buff_simd.rs:2294-2442) in one launch: the dense
+// slices and the tail as k_sum does (into raw[8..]) and the outlier bytes of
+// every sparse column (into raw[0..m)).  With `sum` set, the last block to
+// finish -- a ticket in raw[23], taken after each block's sums are added and
+// fenced -- combines them into the f64 sum (and the partials) as the host
+// does; raw (24 u64) is zeroed beforehand.
+__global__ void __launch_bounds__(kThreads) k_sum_major(const uint8_t *__restrict__ slices,
+                                                        size_t stride, uint32_t kd,
+                                                        const uint8_t *__restrict__ tail,
+                                                        uint32_t ts, unsigned long long tail_bits,
+                                                        SparseBytes sb, MajorSumArgs a,
+                                                        unsigned long long *raw, double *sum,
+                                                        unsigned long long *parts_out) {
+  __shared__ unsigned long long s_acc[9], s_out[8];
+  __shared__ bool s_last;
+  if (threadIdx.x < 9) s_acc[threadIdx.x] = 0;
+  if (threadIdx.x < 8) s_out[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nth = gridDim.x * blockDim.x;
+  if (a.n) sum_slices_tail(slices, stride, kd, tail, ts, tail_bits, tid, nth, s_acc);
+#pragma unroll
+  for (uint32_t c = 0; c < 8; ++c) {  // unrolled: the parameter arrays stay out of local memory
+    if (c >= sb.m || !sb.n[c]) continue;
+    const unsigned long long v = warp_sum_ull(bytesum_thread(sb.p[c], sb.n[c], tid, nth));
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(&s_out[c], v);
+  }
+  __syncthreads();
+  if (threadIdx.x < kd && s_acc[threadIdx.x]) atomicAdd(&raw[8 + threadIdx.x], s_acc[threadIdx.x]);
+  if (threadIdx.x == 8 && ts && s_acc[8]) atomicAdd(&raw[8 + kd], s_acc[8]);
+  if (threadIdx.x < sb.m && s_out[threadIdx.x]) atomicAdd(&raw[threadIdx.x], s_out[threadIdx.x]);
+  if (!sum) return;
+  if (threadIdx.x < 9) __threadfence();  // the threads that added to raw
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&raw[23], 1ull) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return;
+  __threadfence();
+  unsigned long long r[24], parts[9];
+  for (int i = 0; i < 23; ++i) r[i] = __ldcg(raw + i);
+  const uint32_t np = major_sum_parts(a, r, parts);
+  *sum = major_sum_f64(a, parts);
+  if (parts_out)
+    for (uint32_t i = 0; i < np; ++i) parts_out[i] = parts[i];
 }
 
 // Largest outlier byte among rows set in `cand` (all outlier rows when cand is
@@ -1259,25 +1318,149 @@ cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, 
 // Exclusive prefix counts of set bits per word (rank[0..nw), total at
 // rank[nw]); rank needs nw + 1 entries.
 namespace {
-__global__ void k_major_sum_combine(MajorSumArgs a, const unsigned long long *__restrict__ raw,
-                                    double *sum, unsigned long long *parts_out) {
-  unsigned long long parts[9];
-  const uint32_t np = major_sum_parts(a, raw, parts);
-  *sum = major_sum_f64(a, parts);
-  if (parts_out)
-    for (uint32_t i = 0; i < np; ++i) parts_out[i] = parts[i];
-}
 }  // namespace
 
-cudaError_t major_sum_combine(const MajorSumArgs &a, const unsigned long long *raw, double *sum,
-                              unsigned long long *parts, cudaStream_t s) {
-  k_major_sum_combine<<<1, 1, 0, s>>>(a, raw, sum, parts);
+cudaError_t major_sums(const buff_col *c, const MajorSumArgs &a, unsigned long long *raw,
+                       double *sum, unsigned long long *parts, cudaStream_t s) {
+  cudaError_t e = zero_u64(raw, 24, s);
+  if (e != cudaSuccess) return e;
+  SparseBytes sb;
+  memset(&sb, 0, sizeof(sb));
+  sb.m = c->m;
+  for (uint32_t col = 0; col < c->m; ++col) {
+    sb.p[col] = c->obytes + c->oofs[col];
+    sb.n[col] = c->nout[col];
+  }
+  static std::atomic<int> per_sm_cache{0};
+  int per_sm = per_sm_cache.load(std::memory_order_relaxed);
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sum_major, kThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+    per_sm_cache.store(per_sm, std::memory_order_relaxed);
+  }
+  // enough threads for the larger of a slice's 16-byte vectors and the
+  // outlier bytes, at most the resident grid
+  size_t big = c->stride / 16;
+  for (uint32_t col = 0; col < c->m; ++col) big = std::max(big, (size_t)c->nout[col] / 16 + 1);
+  size_t grid = (big + kThreads - 1) / kThreads;
+  const size_t cap = (size_t)per_sm * num_sms(c->device);
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  k_sum_major<<<(unsigned)grid, kThreads, 0, s>>>(c->slices, c->stride, c->k - c->m, c->tail, c->r,
+                                                  (unsigned long long)c->n * c->r, sb, a, raw, sum,
+                                                  parts);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t major_bytesum(const uint8_t *p, size_t nbytes, unsigned long long *out, cudaStream_t s) {
   k_bytesum<<<grid_of(nbytes / 16 + 1, 256), 256, 0, s>>>(p, nbytes, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+namespace {
+// buff_max_majority (buff_simd.rs:2444-2861) of a column with one sparse
+// byte column and rows outside it: its progressive max is then the largest
+// full code, whose leading byte is a row's outlier byte or else the major
+// byte M.  One pass finds it as k_max does: a lane owns 32 rows (one bitmap
+// word, its outlier bytes reached through the warp's rank and a prefix count
+// of the lanes before it); a step whose largest leading byte is below the
+// running maximum's is skipped without touching the dense slices, otherwise
+// the lanes holding that byte take the largest code among those rows
+// (max_after_top over the dense slices and the tail), and the warp
+// publishes its best into *out and raises its threshold from it.
+__global__ void __launch_bounds__(kThreads) k_major1_max(const uint32_t *__restrict__ bits,
+                                                         const uint32_t *__restrict__ rank,
+                                                         const uint8_t *__restrict__ ob,
+                                                         uint32_t M, uint32_t n,
+                                                         const uint8_t *__restrict__ slices,
+                                                         size_t stride, uint32_t kd,
+                                                         const uint8_t *__restrict__ tail,
+                                                         uint32_t r, uint32_t fl,
+                                                         unsigned long long *out) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t nwords = (n + 31) / 32;
+  const uint32_t step = nwarps * 32;
+  unsigned long long best = 0;
+  bool have = false;
+  uint32_t top = 0;  // leading byte of best
+  // the bitmap word and the warp's rank of the next step are loaded before
+  // this step's outlier bytes are read
+  uint32_t nB = 0, nR0 = 0;
+  if (warp * 32 < nwords) nR0 = __ldg(rank + warp * 32);
+  if (warp * 32 + lane < nwords) nB = __ldg(bits + warp * 32 + lane);
+  for (uint32_t base = warp * 32; base < nwords; base += step) {
+    const uint32_t w = base + lane;
+    const bool live = w < nwords;
+    const uint32_t B = live ? nB : 0u, R0 = nR0;
+    if (base + step < nwords) nR0 = __ldg(rank + base + step);
+    if (w + step < nwords) nB = __ldg(bits + w + step);
+    const uint32_t row0 = w * 32;
+    const uint32_t valid =
+        !live ? 0u : (n - row0 >= 32 ? 0xFFFFFFFFu : ((1u << (n - row0)) - 1u));
+    uint32_t R;
+    {
+      const uint32_t v = __popc(B);
+      uint32_t x = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+      }
+      R = R0 + x - v;
+    }
+    const uint32_t non = ~B & valid;
+    uint32_t L = non ? M : 0u;  // the lane's largest leading byte
+    for (uint32_t b = B, k = 0; b; ++k, b &= b - 1) L = max(L, (uint32_t)__ldg(ob + R + k));
+    const bool rows = valid != 0;
+    const uint32_t wl = __reduce_max_sync(0xFFFFFFFFu, rows ? L : 0u);
+    if (have && wl < top) continue;  // nothing in this step reaches the running maximum
+    unsigned long long m = 0;
+    if (rows && L == wl) {
+      uint32_t cand = wl == M ? non : 0u;  // outlier bytes differ from M
+      if (wl != M) {
+        uint32_t b = B;
+        for (uint32_t k = 0; b; ++k, b &= b - 1)
+          if (__ldg(ob + R + k) == wl) cand |= b & (0u - b);
+      }
+      m = max_after_top(slices, stride, kd, tail, r, row0, cand, wl);
+    }
+    m = warp_max_ull(m);
+    if (!have || m > best) best = m;
+    have = true;
+    unsigned long long g = 0;
+    if (lane == 0) g = atomicMax(out, best);
+    g = __shfl_sync(0xFFFFFFFFu, g, 0);
+    if (g > best) best = g;
+    top = (uint32_t)(best >> (fl - 8)) & 0xFFu;
+  }
+  if (lane == 0 && have) atomicMax(out, best);
+}
+}  // namespace
+
+bool major1_max_applies(const buff_col *c) { return c->m == 1 && c->nout[0] < c->n; }
+
+cudaError_t major1_max(const buff_col *c, unsigned long long *out, cudaStream_t s) {
+  cudaError_t e = zero_u64(out, 1, s);
+  if (e != cudaSuccess || !c->n) return e;
+  static std::atomic<int> per_sm_cache{0};
+  int per_sm = per_sm_cache.load(std::memory_order_relaxed);
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_major1_max, kThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+    per_sm_cache.store(per_sm, std::memory_order_relaxed);
+  }
+  const size_t steps = ((size_t)c->n + 1023) / 1024;  // one per warp at a time
+  size_t grid = (steps + kThreads / 32 - 1) / (kThreads / 32);
+  const size_t cap = (size_t)per_sm * num_sms(c->device);
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  k_major1_max<<<(unsigned)grid, kThreads, 0, s>>>(c->obits, c->orank, c->obytes + c->oofs[0],
+                                                   c->majors[0], c->n, c->slices, c->stride,
+                                                   c->k - 1, c->tail, c->r, c->fixed_len, out);
   count_launch();
   return cudaGetLastError();
 }

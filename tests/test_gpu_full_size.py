@@ -160,6 +160,10 @@ def test_outlier_column_full_size_bit_exact(oracle, gpu):
     m = col.max(argmax=True)
     assert m.value.hex() == mv.hex() and m.code == mc
     assert _same_words(m.argmax_words, aw) and m.argmax_count == ac
+    # the device-only sum and max, and the max value without its arg-max rows
+    from tests.test_gpu_major import _check_async
+
+    _check_async(col, s, parts[: g.n_partials], mc)
     assert np.array_equal(col.decode(), oracle.decode_majority(ref, scale, raw))
     col.free()
     # the plain (buff-simd) image of the same column

@@ -52,7 +52,38 @@ def _check_queries(oracle, col, ref, scale, mode, x):
     m = col.max(argmax=True)
     assert m.code == mc and m.value == mv
     assert np.array_equal(m.argmax_words, aw) and m.argmax_count == ac
+    _check_async(col, s, parts[: res.n_partials], mc)
     assert n == col.n
+
+
+def _check_async(col, s, parts, mc):
+    """buff_sum_majority_async (the f64 sum and the partials combined on the
+    device) and buff_max_majority_async into device memory."""
+    import torch
+
+    from buff_gb300 import capi
+
+    L = capi.lib()
+    dsum = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    dparts = torch.full((9,), -1, dtype=torch.int64, device="cuda")
+    dmax = torch.full((1,), -1, dtype=torch.int64, device="cuda")
+    st = torch.cuda.Stream()
+    assert L.buff_sum_majority_async(col.handle, dsum.data_ptr(), dparts.data_ptr(),
+                                     st.cuda_stream) == capi.OK
+    assert L.buff_sum_majority_async(col.handle, dsum.data_ptr(), None, st.cuda_stream) == capi.OK
+    assert L.buff_max_majority_async(col.handle, dmax.data_ptr(), st.cuda_stream) == capi.OK
+    st.synchronize()
+    assert float(dsum.item()).hex() == float(s).hex()
+    got = dparts.cpu().numpy().view(np.uint64)
+    assert list(got[: len(parts)]) == list(parts)
+    assert int(dmax.cpu().numpy().view(np.uint64)[0]) == mc
+    # the value alone through the synchronous call (no arg-max requested)
+    import ctypes as C
+
+    mv, code = C.c_double(0), C.c_uint64(0)
+    assert L.buff_max_majority(col.handle, C.byref(mv), C.byref(code), None, None,
+                               None) == capi.OK
+    assert code.value == mc
 
 
 @pytest.mark.parametrize("kind", ["one", "two", "three", "none"])
