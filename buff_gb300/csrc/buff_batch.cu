@@ -930,15 +930,16 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
                                             const uint32_t *__restrict__ qidx,
                                             const uint32_t *__restrict__ prefix, uint32_t nq,
                                             uint32_t nitems, uint32_t tile,
-                                            unsigned int *counter) {
+                                            unsigned int *counter, BatchDone done) {
   extern __shared__ __align__(16) uint8_t dyn_smem[];
+  __shared__ bool s_last;
   const uint32_t lane = threadIdx.x & 31;
   uint8_t *ring = dyn_smem + (threadIdx.x >> 5) * kRingBytes;  // FS / S classes only
   for (;;) {
     uint32_t it = 0;
     if (lane == 0) it = atomicAdd(counter, 1u);
     it = __shfl_sync(0xFFFFFFFFu, it, 0);
-    if (it >= nitems) return;
+    if (it >= nitems) break;
     // the query of item `it`: the last i with prefix[i] <= it, found by the
     // whole warp 32-ary (lane l probes lo + l*step), two or three dependent
     // loads for thousands of queries instead of a binary search's dozen
@@ -963,6 +964,21 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
       if (q.ops & kOpDecode) tile_decode<STAGE>(q, r0, r1, lane);
     }
   }
+  if (!done.flag) return;
+  // the batch's completion: the last block to finish (every block's sums
+  // added and fenced before its ticket; the earlier class launches of the
+  // batch ended before this one began) publishes the accumulators, then the
+  // flag, to host memory
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done.ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (uint32_t i = threadIdx.x; i < done.nacc; i += blockDim.x) done.hacc[i] = __ldcg(done.acc + i);
+  __threadfence_system();
+  __syncthreads();
+  if (threadIdx.x == 0) *reinterpret_cast<volatile uint32_t *>(done.flag) = done.seq;
 }
 
 template <int CLS>
@@ -1087,12 +1103,25 @@ int class_grid(int cls, const buff_batch_tune &t, uint32_t nitems) {
 // One persistent launch per non-empty class, in order on `s`; counters
 // holds kClasses zeroed work counters.
 cudaError_t batch_launch(const void *d_desc, const uint32_t *d_buf, const BatchSched &sc,
-                         const buff_batch_tune &t, unsigned int *counters, cudaStream_t s) {
+                         const buff_batch_tune &t, unsigned int *counters, cudaStream_t s,
+                         const BatchDone *done) {
   const BQ *qs = static_cast<const BQ *>(d_desc);
   const int order[kClasses] = {kClsMD, kClsFS, kClsS, kClsF};
+  int last = -1;  // the completion rides on the last class launched
+  for (int oi = 0; oi < kClasses; ++oi)
+    if (sc.items[order[oi]]) last = oi;
+  BatchDone none;
+  memset(&none, 0, sizeof(none));
+  if (done && last < 0) {  // nothing to launch: one empty worker still completes the batch
+    BatchDone d = *done;
+    k_bq<kClsF, 1><<<1, kBT, 0, s>>>(qs, d_buf, d_buf, 0, 0, t.tile_rows, counters, d);
+    count_launch();
+    return cudaGetLastError();
+  }
   for (int oi = 0; oi < kClasses; ++oi) {
     const int c = order[oi];
     if (!sc.items[c]) continue;
+    const BatchDone &bd = (done && oi == last) ? *done : none;
     const int grid = class_grid(c, t, sc.items[c]);
     const uint32_t *qi = d_buf + sc.qidx_off[c], *pf = d_buf + sc.prefix_off[c];
     const size_t sm = class_smem(c);
@@ -1100,13 +1129,13 @@ cudaError_t batch_launch(const void *d_desc, const uint32_t *d_buf, const BatchS
   do {                                                                                         \
     if (t.stage == 4)                                                                          \
       k_bq<CLS, 4><<<grid, kBT, sm, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,        \
-                                        counters + c);                                         \
+                                        counters + c, bd);                                     \
     else if (t.stage == 2)                                                                     \
       k_bq<CLS, 2><<<grid, kBT, sm, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,        \
-                                        counters + c);                                         \
+                                        counters + c, bd);                                     \
     else                                                                                       \
       k_bq<CLS, 1><<<grid, kBT, sm, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,        \
-                                        counters + c);                                         \
+                                        counters + c, bd);                                     \
   } while (0)
     switch (c) {
       case kClsF: BQ_LAUNCH(kClsF); break;

@@ -245,9 +245,23 @@ struct BatchSched {
 size_t batch_sched_words(uint32_t nq);
 void batch_schedule(const void *h_desc, uint32_t nq, uint32_t tile, uint32_t *buf,
                     BatchSched *sc);
+// A batch's completion, written by its last launch: the last block to finish
+// copies the nacc accumulator words to hacc (host memory the device writes)
+// and then stores seq into *flag, so the host reads the results once the
+// flag shows seq (no read-back copy, no event to ask).
+struct BatchDone {
+  unsigned int *ticket;  // a zeroed device word
+  const unsigned long long *acc;
+  unsigned long long *hacc;
+  uint32_t nacc;
+  uint32_t *flag;  // device address of the host flag
+  uint32_t seq;
+};
 // Launches every class of a scheduled batch on s; counters: 4 zeroed u32.
+// With `done`, the last class launch also writes the batch's completion.
 cudaError_t batch_launch(const void *d_desc, const uint32_t *d_buf, const BatchSched &sc,
-                         const buff_batch_tune &t, unsigned int *counters, cudaStream_t s);
+                         const buff_batch_tune &t, unsigned int *counters, cudaStream_t s,
+                         const BatchDone *done = nullptr);
 void batch_result(const buff_query &q, const unsigned long long *acc, buff_query_result *out);
 
 int num_sms(int device);

@@ -117,12 +117,14 @@ struct Slot {
   cudaStream_t s = nullptr;
   cudaEvent_t ev = nullptr;
   void *h_desc = nullptr, *d_desc = nullptr;
-  unsigned long long *h_acc = nullptr;
+  unsigned long long *h_acc = nullptr, *dv_acc = nullptr;  // pinned; its device address
+  uint32_t *h_flag = nullptr, *dv_flag = nullptr;         // batch completion (pinned)
   PlainRes *h_plain = nullptr, *d_plain = nullptr;
   std::vector<Req> reqs;
   bool busy = false;
   bool plain = false;  // this launch went through the single-column calls
   uint64_t seq = 0;
+  uint32_t polls = 0;  // flag polls since the event was last asked
 };
 
 }  // namespace
@@ -316,10 +318,19 @@ int launch_batched(buff_server *S, Slot &sl) {
   buffk::BatchSched sc;
   buffk::batch_schedule(sl.h_desc, nq, t.tile_rows, h_sched, &sc);
   cudaStream_t s = sl.s;
+  // the batch's last launch copies the accumulators to sl.h_acc and then
+  // writes the batch's sequence number into sl.h_flag (the loop polls it);
+  // the event stays for errors
+  buffk::BatchDone done;
+  done.ticket = d_counter + 4;  // in the zeroed counter words
+  done.acc = d_acc;
+  done.hacc = sl.dv_acc;
+  done.nacc = (uint32_t)(buffk::kBatchAcc * nq);
+  done.flag = sl.dv_flag;
+  done.seq = (uint32_t)sl.seq;
   cudaError_t e = cudaMemcpyAsync(sl.d_desc, sl.h_desc, aoff + 64 + abytes,
                                   cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = buffk::batch_launch(sl.d_desc, d_sched, sc, t, d_counter, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(sl.h_acc, d_acc, abytes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = buffk::batch_launch(sl.d_desc, d_sched, sc, t, d_counter, s, &done);
   if (e == cudaSuccess) e = cudaEventRecord(sl.ev, s);
   return buffh::cuda_status(e);
 }
@@ -483,6 +494,8 @@ bool admit_encode(buff_server *S, Req &q) {
 
 // Waiting requests beyond the free slots before slots take batches.
 constexpr size_t kQueueForBatch = 8;
+// Flag polls of a busy batched slot between two questions to its event.
+constexpr uint32_t kEventEvery = 64;
 
 
 
@@ -491,9 +504,20 @@ void loop(buff_server *S) {
   const uint32_t maxb = S->cfg.batched ? S->cfg.max_batch : 1;
   for (;;) {
     bool worked = false;
-    // retire finished batches
+    // retire finished batches: a batched launch shows its completion in its
+    // flag (the event is asked only now and then, for errors); a plain one
+    // in its event
     for (Slot &sl : S->slots) {
       if (!sl.busy) continue;
+      if (!sl.plain) {
+        if (__atomic_load_n(sl.h_flag, __ATOMIC_ACQUIRE) == (uint32_t)sl.seq) {
+          retire(S, sl);
+          worked = true;
+          continue;
+        }
+        if (++sl.polls < kEventEvery) continue;
+        sl.polls = 0;
+      }
       const cudaError_t q = cudaEventQuery(sl.ev);
       if (q == cudaSuccess) {
         retire(S, sl);
@@ -563,6 +587,8 @@ void loop(buff_server *S) {
       // steps (no descriptor upload, class lists or accumulator download)
       // and the lower latency at light load
       sl.plain = !S->cfg.batched || sl.reqs.size() == 1;
+      sl.seq = ++S->seq;
+      sl.polls = 0;
       const int st = sl.plain ? launch_plain(sl) : launch_batched(S, sl);
       if (st) {
         S->loop_status.store(st);
@@ -571,7 +597,6 @@ void loop(buff_server *S) {
         continue;
       }
       sl.busy = true;
-      sl.seq = ++S->seq;
       S->batches++;
       S->launched_reqs += sl.reqs.size();
       worked = true;
@@ -604,6 +629,7 @@ void destroy_slots(buff_server *S) {
     if (sl.s) cudaStreamDestroy(sl.s);
     if (sl.h_desc) cudaFreeHost(sl.h_desc);
     if (sl.h_acc) cudaFreeHost(sl.h_acc);
+    if (sl.h_flag) cudaFreeHost(sl.h_flag);
     if (sl.h_plain) cudaFreeHost(sl.h_plain);
     if (sl.d_desc) cudaFree(sl.d_desc);
     if (sl.d_plain) cudaFree(sl.d_plain);
@@ -662,6 +688,14 @@ int buff_server_create(const buff_server_config *cfg, buff_server **out) {
     if ((e = cudaMallocHost(&sl.h_desc, stage)) != cudaSuccess) break;
     if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_acc),
                             8 * buffk::kBatchAcc * mb)) != cudaSuccess)
+      break;
+    if ((e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&sl.dv_acc), sl.h_acc, 0)) !=
+        cudaSuccess)
+      break;
+    if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_flag), 64)) != cudaSuccess) break;
+    *sl.h_flag = 0;
+    if ((e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&sl.dv_flag), sl.h_flag, 0)) !=
+        cudaSuccess)
       break;
     if ((e = cudaMallocHost(reinterpret_cast<void **>(&sl.h_plain), sizeof(PlainRes))) != cudaSuccess)
       break;
