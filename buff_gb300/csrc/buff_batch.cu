@@ -935,10 +935,17 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
   __shared__ bool s_last;
   const uint32_t lane = threadIdx.x & 31;
   uint8_t *ring = dyn_smem + (threadIdx.x >> 5) * kRingBytes;  // FS / S classes only
-  for (;;) {
-    uint32_t it = 0;
-    if (lane == 0) it = atomicAdd(counter, 1u);
-    it = __shfl_sync(0xFFFFFFFFu, it, 0);
+  // a warp's first item is its own index; later items come from the work
+  // counter, past the first round (the counter is one address that every
+  // taking warp hits: tens of thousands of small items queued on it for
+  // tens of microseconds)
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  uint32_t it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (bool first = true;; first = false) {
+    if (!first) {
+      if (lane == 0) it = nw + atomicAdd(counter, 1u);
+      it = __shfl_sync(0xFFFFFFFFu, it, 0);
+    }
     if (it >= nitems) break;
     // the query of item `it`: the last i with prefix[i] <= it, found by the
     // whole warp 32-ary (lane l probes lo + l*step), two or three dependent

@@ -305,7 +305,9 @@ int launch_batched(buff_server *S, Slot &sl) {
   const uint32_t *d_sched =
       reinterpret_cast<const uint32_t *>(static_cast<uint8_t *>(sl.d_desc) + soff);
   // tile per batch: small batches split each query over many warps (latency),
-  // large ones use the configured tile (fewer, longer items)
+  // large ones use the configured tile (fewer, longer items).  About four
+  // items per resident warp: with one (longer tiles) a batch of mixed
+  // requests waited on its slowest warps (24 requests: 128 -> 169 us)
   uint64_t rows = 0;
   for (uint32_t i = 0; i < nq; ++i) rows += sl.reqs[i].col->n;
   const uint64_t slots = (uint64_t)S->warp_slots * 4;
