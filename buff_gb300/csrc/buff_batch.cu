@@ -939,6 +939,9 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
   // counter, past the first round (the counter is one address that every
   // taking warp hits: tens of thousands of small items queued on it for
   // tens of microseconds)
+  // the batch's next class launch (programmatic dependent launch) may start
+  // once every block of this one runs: the classes are independent
+  asm volatile("griddepcontrol.launch_dependents;");
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   uint32_t it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   for (bool first = true;; first = false) {
@@ -971,11 +974,15 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
       if (q.ops & kOpDecode) tile_decode<STAGE>(q, r0, r1, lane);
     }
   }
+  // a class launch started early ends only after the launch before it has
+  // ended (a no-op for a launch without a predecessor of its own): so the
+  // batch's last launch ends after every class of the batch
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   if (!done.flag) return;
   // the batch's completion: the last block to finish (every block's sums
   // added and fenced before its ticket; the earlier class launches of the
-  // batch ended before this one began) publishes the accumulators, then the
-  // flag, to host memory
+  // batch have ended, see above) publishes the accumulators, then the flag,
+  // to host memory
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) s_last = atomicAdd(done.ticket, 1u) == gridDim.x - 1;
@@ -1125,24 +1132,39 @@ cudaError_t batch_launch(const void *d_desc, const uint32_t *d_buf, const BatchS
     count_launch();
     return cudaGetLastError();
   }
+  bool started = false;
   for (int oi = 0; oi < kClasses; ++oi) {
     const int c = order[oi];
     if (!sc.items[c]) continue;
     const BatchDone &bd = (done && oi == last) ? *done : none;
-    const int grid = class_grid(c, t, sc.items[c]);
+    const uint32_t grid = (uint32_t)class_grid(c, t, sc.items[c]);
     const uint32_t *qi = d_buf + sc.qidx_off[c], *pf = d_buf + sc.prefix_off[c];
-    const size_t sm = class_smem(c);
+    // after the first class of a completed batch, a programmatic dependent
+    // launch: it starts while the class before it finishes
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kBT);
+    cfg.dynamicSmemBytes = class_smem(c);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = (done && started) ? 1 : 0;
+    started = true;
+    cudaError_t e;
 #define BQ_LAUNCH(CLS)                                                                          \
   do {                                                                                         \
     if (t.stage == 4)                                                                          \
-      k_bq<CLS, 4><<<grid, kBT, sm, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,        \
-                                        counters + c, bd);                                     \
+      e = cudaLaunchKernelEx(&cfg, k_bq<CLS, 4>, qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows, \
+                             counters + c, bd);                                               \
     else if (t.stage == 2)                                                                     \
-      k_bq<CLS, 2><<<grid, kBT, sm, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,        \
-                                        counters + c, bd);                                     \
+      e = cudaLaunchKernelEx(&cfg, k_bq<CLS, 2>, qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows, \
+                             counters + c, bd);                                               \
     else                                                                                       \
-      k_bq<CLS, 1><<<grid, kBT, sm, s>>>(qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows,        \
-                                        counters + c, bd);                                     \
+      e = cudaLaunchKernelEx(&cfg, k_bq<CLS, 1>, qs, qi, pf, sc.n[c], sc.items[c], t.tile_rows, \
+                             counters + c, bd);                                               \
   } while (0)
     switch (c) {
       case kClsF: BQ_LAUNCH(kClsF); break;
@@ -1152,7 +1174,6 @@ cudaError_t batch_launch(const void *d_desc, const uint32_t *d_buf, const BatchS
     }
 #undef BQ_LAUNCH
     count_launch();
-    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
