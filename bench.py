@@ -1021,7 +1021,7 @@ def run_serving_form(args, stream, peak):
     for f in (0.5, 0.7, 0.85, 0.95):
         rate = f * plain_max
         sweep["plain"].append(run(False, rate, int(max(2000, min(2e6, rate * dur)))))
-    for f in (0.5, 0.7, 0.85, 0.95, 1.0, 1.5, 2.0, 2.5, 3.0, 3.5, 4.0, 5.0, 6.0, 8.0):
+    for f in (0.5, 0.7, 0.85, 0.95, 1.0, 1.5, 2.0, 2.25, 2.5, 2.75, 3.0, 3.5, 4.0, 5.0, 6.0, 8.0):
         rate = f * plain_max
         if rate > 0.95 * batched_max:
             break

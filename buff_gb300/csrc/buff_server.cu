@@ -495,7 +495,7 @@ bool admit_encode(buff_server *S, Req &q) {
 }
 
 // Waiting requests beyond the free slots before slots take batches.
-constexpr size_t kQueueForBatch = 8;
+constexpr size_t kQueueForBatch = 4;
 // Flag polls of a busy batched slot between two questions to its event.
 constexpr uint32_t kEventEvery = 64;
 
