@@ -639,15 +639,6 @@ constexpr uint32_t kStepRows = 1024;
 constexpr uint32_t kSlotBytes = 3 * kStepRows + 1024;  // 3 slices + up to 896 tail bytes
 constexpr uint32_t kRingBytes = kDepth * kSlotBytes;
 
-__device__ __forceinline__ void cp16(uint8_t *dst, const uint8_t *src) {
-  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
 
 // The descriptor fields one filter/sum tile reads, loaded once into
 // registers (the descriptor lives in global memory, and reading its fields

@@ -180,6 +180,20 @@ struct Bytes32 {
   uint32_t w[8];
 };
 
+// 16 bytes global -> shared without registers (both 16-byte aligned); a
+// thread's copies complete group by group (cp_commit / cp_wait<N>: at most N
+// of its groups still in flight), and a warp barrier after the wait makes
+// every lane's finished copies visible to the others.
+__device__ __forceinline__ void cp16(uint8_t *dst, const void *src) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // 256-bit non-allocating load (sm_100+; the address is 32-byte aligned).
 __device__ __forceinline__ Bytes32 ld_stream32(const uint8_t *p) {
   Bytes32 b;
