@@ -644,7 +644,7 @@ def run_rapg_major_form(args, stream):
     return res
 
 
-def run_rapg_form(args, stream):
+def run_rapg_form(args, stream, peak=None):
     """RAPG byte_residue layout on 67,108,864 rows with high outliers (99%
     N(100,5), 1% U(1e5,1e6), 6 decimals, scale 1e6): encode, full and
     precision-limited decode and sum (the p_scan sequence).  The CPU leg
@@ -678,7 +678,9 @@ def run_rapg_form(args, stream):
     code_bytes = info.device_bytes
     t = time_op(lambda: L.buff_rapg_decode(h, out.data_ptr(), C.byref(k), sh), 5, stream)
     ops["decode"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9,
-                     "gb_s_alg": (code_bytes + 8 * n) / t / 1e9}
+                     "gb_s_alg": (code_bytes + 8 * n) / t / 1e9,
+                     "alg_bytes": code_bytes + 8 * n,
+                     "frac": (code_bytes + 8 * n) / t / 1e9 / peak if peak else None}
     for p in (0, 3, 5):
         t = time_op(lambda: L.buff_rapg_decode_at_precision(h, p, out.data_ptr(), C.byref(k), sh),
                     5, stream)
@@ -1406,7 +1408,7 @@ def main():
             small_form = run_small_form(stream, with_cpu=not args.no_cpu)
         if not args.no_outlier:
             outlier_form = run_outlier_form(args, stream, peak)
-            rapg_form = run_rapg_form(args, stream)
+            rapg_form = run_rapg_form(args, stream, peak)
         if not args.no_batched:
             batched_form = run_batched_form(args, stream, peak)
         if not args.no_serve:

@@ -1131,6 +1131,47 @@ __global__ void __launch_bounds__(kThreads) k_rapg_fixup_patch(RapgDecodeArgs a,
   }
 }
 
+// k_rapg_fixup_patch for one sparse column: a warp takes 32 bitmap words
+// (1,024 rows) per step, the lanes' outlier ranks come from the step's first
+// rank word plus a prefix count of the lanes before, and the next step's
+// bitmap and rank words are loaded before this step's outlier bytes and
+// written values are read -- one dependent load per step instead of three
+// per word.
+__global__ void __launch_bounds__(kThreads) k_rapg_fixup_patch1(RapgDecodeArgs a, uint32_t low,
+                                                                double scale) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t step = ((gridDim.x * blockDim.x) >> 5) * 32;
+  const uint32_t nwords = (a.n + 31) / 32;
+  const unsigned long long lowmask = (1ull << low) - 1ull;
+  const uint8_t *ob = a.obytes + a.oofs[0];
+  uint32_t nB = 0, nR0 = 0;
+  if (warp * 32 < nwords) nR0 = __ldg(a.orank + warp * 32);
+  if (warp * 32 + lane < nwords) nB = __ldg(a.obits + warp * 32 + lane);
+  for (uint32_t base = warp * 32; base < nwords; base += step) {
+    const uint32_t w = base + lane;
+    const uint32_t B = w < nwords ? nB : 0u, R0 = nR0;
+    if (base + step < nwords) nR0 = __ldg(a.orank + base + step);
+    if (w + step < nwords) nB = __ldg(a.obits + w + step);
+    const uint32_t v = __popc(B);
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (lane >= (uint32_t)o) x += y;
+    }
+    uint32_t k = R0 + x - v;  // rank of the lane's first outlier
+    for (uint32_t b = B; b; b &= b - 1, ++k) {
+      const uint32_t i = w * 32 + (__ffs(b) - 1);
+      const unsigned long long sp = (unsigned long long)__ldg(ob + k);
+      const long long whole = __double2ll_rn(a.out[i] * scale);  // base + written code
+      const unsigned long long code =
+          ((unsigned long long)(whole - a.base) & lowmask) | (sp << low);
+      a.out[i] = i64_to_f64_scaled((long long)((unsigned long long)a.base + code), a.dlen);
+    }
+  }
+}
+
 __global__ void k_field_sum(const uint8_t *p, unsigned long long bit0, uint32_t width, uint32_t n,
                             unsigned long long *out) {
   unsigned long long acc = 0;
@@ -1585,7 +1626,12 @@ static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
       const unsigned long long ab = a.base < 0 ? 0ull - (unsigned long long)a.base
                                                : (unsigned long long)a.base;
       const int gw = grid_of(((size_t)a.n + 31) / 32, kThreads);
-      if (a.R <= 52 && low < 64 && ab < (1ull << 53) - (1ull << a.R) && a.dlen <= 1000)
+      const bool patch = a.R <= 52 && low < 64 && ab < (1ull << 53) - (1ull << a.R) &&
+                         a.dlen <= 1000;
+      if (patch && a.m == 1)
+        k_rapg_fixup_patch1<<<grid_of(((size_t)a.n + 1023) / 1024 * 32, kThreads), kThreads, 0,
+                              s>>>(a, low, ldexp(1.0, a.dlen));
+      else if (patch)
         k_rapg_fixup_patch<<<gw, kThreads, 0, s>>>(a, low, ldexp(1.0, a.dlen));
       else
         k_rapg_fixup<<<gw, kThreads, 0, s>>>(a);
