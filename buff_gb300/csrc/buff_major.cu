@@ -981,6 +981,9 @@ template <int KS, bool N32, bool ST32, bool POS = false>
 __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast4(RapgDecodeArgs a) {
   static_assert(KS >= 1 && KS <= 4, "k_rapg_decode_fast4 transposes at most 4 slices");
   using CodeT = typename std::conditional<N32, uint32_t, unsigned long long>::type;
+  // the outlier fix-up (a programmatic dependent launch) may start once every
+  // block of this pass runs; it waits for this pass before reading the values
+  asm volatile("griddepcontrol.launch_dependents;");
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nchunks = (a.n + kRowChunk - 1) / kRowChunk;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1148,6 +1151,9 @@ __global__ void __launch_bounds__(kThreads) k_rapg_fixup_patch1(RapgDecodeArgs a
   uint32_t nB = 0, nR0 = 0;
   if (warp * 32 < nwords) nR0 = __ldg(a.orank + warp * 32);
   if (warp * 32 + lane < nwords) nB = __ldg(a.obits + warp * 32 + lane);
+  // the written values are the dense pass's: wait for it (the bitmap and
+  // rank loads above do not depend on it; a no-op when launched plainly)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   for (uint32_t base = warp * 32; base < nwords; base += step) {
     const uint32_t w = base + lane;
     const uint32_t B = w < nwords ? nB : 0u, R0 = nR0;
@@ -1628,10 +1634,20 @@ static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
       const int gw = grid_of(((size_t)a.n + 31) / 32, kThreads);
       const bool patch = a.R <= 52 && low < 64 && ab < (1ull << 53) - (1ull << a.R) &&
                          a.dlen <= 1000;
-      if (patch && a.m == 1)
-        k_rapg_fixup_patch1<<<grid_of(((size_t)a.n + 1023) / 1024 * 32, kThreads), kThreads, 0,
-                              s>>>(a, low, ldexp(1.0, a.dlen));
-      else if (patch)
+      if (patch && a.m == 1) {
+        // a programmatic dependent launch of the dense pass (see the two kernels)
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t cfg;
+        memset(&cfg, 0, sizeof(cfg));
+        cfg.gridDim = dim3((unsigned)grid_of(((size_t)a.n + 1023) / 1024 * 32, kThreads));
+        cfg.blockDim = dim3(kThreads);
+        cfg.stream = s;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_rapg_fixup_patch1, a, low, ldexp(1.0, a.dlen));
+      } else if (patch)
         k_rapg_fixup_patch<<<gw, kThreads, 0, s>>>(a, low, ldexp(1.0, a.dlen));
       else
         k_rapg_fixup<<<gw, kThreads, 0, s>>>(a);
