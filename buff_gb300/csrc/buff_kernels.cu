@@ -444,6 +444,9 @@ __global__ void k_fill_words(uint32_t *words, uint32_t n, uint32_t value,
 // SMs: a copy-engine memset node between two kernels costs about a
 // microsecond of engine switching on each side.
 __global__ void k_zero_u64(unsigned long long *p, uint32_t n, unsigned long long *q, uint32_t m) {
+  // the accumulating kernel after it may start now (a programmatic dependent
+  // launch that waits for this one before its first atomic)
+  asm volatile("griddepcontrol.launch_dependents;");
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = 0;
   if (i < m) q[i] = 0;
@@ -677,6 +680,9 @@ __global__ void __launch_bounds__(kThreads) k_filter_sum_il(FilterArgs a, uint32
     __stcs(a.words + blk, gt);
     cnt += __popc(gt);
   }
+  // the zeroed count and partials (the launch before this one, when this is
+  // its programmatic dependent) are added to only from here on
+  asm volatile("griddepcontrol.wait;" ::: "memory");
 #pragma unroll
   for (int s = 0; s < KS; ++s) {
     const unsigned long long w = warp_sum_ull(acc[s]);
@@ -1215,10 +1221,23 @@ cudaError_t launch_filter_sum_il(const FilterArgs &a, const buff_col *c,
   const int need = (int)((nblk + kThreads - 1) / kThreads);
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
-  k_filter_sum_il<TH, KS><<<grid, kThreads, 0, s>>>(a, c->r, (unsigned long long)c->n * c->r,
-                                                     d_partials);
+  // a programmatic dependent launch: the streaming starts while the zeroing
+  // kernel before it runs; the kernel waits for it before adding to the
+  // results (a plain launch when the stream's last operation is no kernel)
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(kThreads);
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, k_filter_sum_il<TH, KS>, a, c->r,
+                                           (unsigned long long)c->n * c->r, d_partials);
   count_launch();
-  return cudaGetLastError();
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_filter_sum(const FilterArgs &a, const buff_col *c,
