@@ -911,6 +911,7 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode(RapgDecodeArgs a) {
 template <int KS, bool N32 = false>
 __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a) {
   using CodeT = typename std::conditional<N32, uint32_t, unsigned long long>::type;
+  asm volatile("griddepcontrol.launch_dependents;");  // see k_rapg_decode_fast4
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nchunks = (a.n + kRowChunk - 1) / kRowChunk;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1614,6 +1615,37 @@ static void launch_fast4(const RapgDecodeArgs &a, int g, cudaStream_t s) {
     k_rapg_decode_fast4<KS, N32, false><<<g, kThreads, 0, s>>>(a);
 }
 
+// The rows that are outliers in some sparse column, after a fast pass wrote
+// every row with the default sparse bytes: patched in place while every value
+// is exact (one sparse column: k_rapg_fixup_patch1, launched as a
+// programmatic dependent of the pass), else rebuilt from the slices.
+static void launch_fixup(const RapgDecodeArgs &a, cudaStream_t s) {
+  const uint32_t low = 8 * a.ks + a.ts;
+  const unsigned long long ab =
+      a.base < 0 ? 0ull - (unsigned long long)a.base : (unsigned long long)a.base;
+  const int gw = grid_of(((size_t)a.n + 31) / 32, kThreads);
+  const bool patch =
+      a.R <= 52 && low < 64 && ab < (1ull << 53) - (1ull << a.R) && a.dlen <= 1000;
+  if (patch && a.m == 1) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3((unsigned)grid_of(((size_t)a.n + 1023) / 1024 * 32, kThreads));
+    cfg.blockDim = dim3(kThreads);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_rapg_fixup_patch1, a, low, ldexp(1.0, a.dlen));
+  } else if (patch) {
+    k_rapg_fixup_patch<<<gw, kThreads, 0, s>>>(a, low, ldexp(1.0, a.dlen));
+  } else {
+    k_rapg_fixup<<<gw, kThreads, 0, s>>>(a);
+  }
+  count_launch();
+}
+
 static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
   if (a.ks >= 1 && a.ks <= 4) {
     const int g = grid_of((size_t)(a.n + kRowChunk - 1) / kRowChunk * 32, kThreads);
@@ -1627,32 +1659,7 @@ static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
       default: n32 ? launch_fast4<4, true>(a, g, s) : launch_fast4<4, false>(a, g, s); break;
     }
     count_launch();
-    if (a.m) {
-      const uint32_t low = 8 * a.ks + a.ts;
-      const unsigned long long ab = a.base < 0 ? 0ull - (unsigned long long)a.base
-                                               : (unsigned long long)a.base;
-      const int gw = grid_of(((size_t)a.n + 31) / 32, kThreads);
-      const bool patch = a.R <= 52 && low < 64 && ab < (1ull << 53) - (1ull << a.R) &&
-                         a.dlen <= 1000;
-      if (patch && a.m == 1) {
-        // a programmatic dependent launch of the dense pass (see the two kernels)
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        attr[0].val.programmaticStreamSerializationAllowed = 1;
-        cudaLaunchConfig_t cfg;
-        memset(&cfg, 0, sizeof(cfg));
-        cfg.gridDim = dim3((unsigned)grid_of(((size_t)a.n + 1023) / 1024 * 32, kThreads));
-        cfg.blockDim = dim3(kThreads);
-        cfg.stream = s;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        cudaLaunchKernelEx(&cfg, k_rapg_fixup_patch1, a, low, ldexp(1.0, a.dlen));
-      } else if (patch)
-        k_rapg_fixup_patch<<<gw, kThreads, 0, s>>>(a, low, ldexp(1.0, a.dlen));
-      else
-        k_rapg_fixup<<<gw, kThreads, 0, s>>>(a);
-      count_launch();
-    }
+    if (a.m) launch_fixup(a, s);
     return;
   }
   {
@@ -1664,10 +1671,7 @@ static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
     else
       launch_fast_ks<false>(a, g, s);
     count_launch();
-    if (a.m) {
-      k_rapg_fixup<<<grid_of(((size_t)a.n + 31) / 32, kThreads), kThreads, 0, s>>>(a);
-      count_launch();
-    }
+    if (a.m) launch_fixup(a, s);
   }
 }
 
