@@ -521,6 +521,14 @@ def run_outlier_form(args, stream, peak):
                      "gb_s_alg": ab / t / 1e9, "frac": ab / t / 1e9 / peak,
                      "plain_layout_ms": tp * 1e3}
     del q
+    # full decode (buff_decode_majority): every row's f64 from the sparse
+    # bytes, the dense slices and the tail
+    dec = torch.empty(n, dtype=torch.float64, device="cuda")
+    t = time_op(lambda: L.buff_decode_majority(h, dec.data_ptr(), sh), 10, stream)
+    dec_bytes = info.device_bytes + 8 * n
+    ops["decode"] = {"ms": t * 1e3, "gvalues_s": n / t / 1e9, "alg_bytes": dec_bytes,
+                     "gb_s_alg": dec_bytes / t / 1e9, "frac": dec_bytes / t / 1e9 / peak}
+    del dec
     res = capi.SumResult()
     dsum = torch.zeros(1, dtype=torch.float64, device="cuda")
     dmax = torch.zeros(1, dtype=torch.int64, device="cuda")
