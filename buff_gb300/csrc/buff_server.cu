@@ -791,8 +791,13 @@ int buff_server_submit(buff_server *S, const buff_request *reqs, uint32_t n) {
       bad = reqs[i].ops != BUFF_Q_ENCODE || (reqs[i].n && !reqs[i].values) ||
             reqs[i].n > BUFF_MAX_ROWS;
     } else {
+      // the batched plan's checks, so that a request answers the same
+      // whether it runs in a batch or through the single-column calls
+      const uint32_t ops = reqs[i].ops;
+      const uint32_t known = BUFF_Q_RANGE | BUFF_Q_EQUAL | BUFF_Q_SUM | BUFF_Q_MAX | BUFF_Q_DECODE;
       q.kind = kQuery;
-      bad = reqs[i].column >= S->store.size();
+      bad = reqs[i].column >= S->store.size() || !ops || (ops & ~known) ||
+            ((ops & BUFF_Q_RANGE) && (ops & BUFF_Q_EQUAL));
     }
     if (bad) {
       buff_completion c;

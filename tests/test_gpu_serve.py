@@ -124,6 +124,62 @@ def test_results_match_single_column(gpu):
             assert g["values"] == np.ascontiguousarray(ref).tobytes()
 
 
+def test_requests_that_fail(gpu):
+    """A request asking for both filters is refused at submission in either
+    mode; a batch whose requests all fail planning (a decode at a precision
+    the reference has no bound for) still completes, each request with the
+    single-column call's status; in a batch mixing them with valid requests
+    the valid ones get their single-column results."""
+    import ctypes as C
+
+    import torch
+
+    from buff_gb300 import capi
+    from buff_gb300.capi import Q_DECODE, Q_EQUAL, Q_RANGE
+    from buff_gb300.serve import Server, request
+
+    cols, data = _store(seed=14, ncols=6)
+    out = torch.empty(max(x.size for x in data), dtype=torch.float64, device="cuda")
+    want = capi.lib().buff_decode_at_precision(cols[0].handle, 99, C.c_void_p(out.data_ptr()),
+                                               None)
+    assert want != 0
+    for batched in (True, False):
+        s = Server(1 << 30, max_batch=64, max_inflight=2, batched=batched, auto_release=False)
+        for c in cols:
+            s.add_column(c)
+        s.start()
+        s.submit([request(0, Q_RANGE | Q_EQUAL, 1.0, tag=0)])
+        (c,) = s.wait(1)
+        assert c.status == capi.EINVAL
+        s.release(c)
+        bad = [request(i % 6, Q_DECODE, 0.0, 99, tag=i) for i in range(40)]
+        s.submit(bad)
+        done = s.wait(len(bad))
+        assert sorted(c.tag for c in done) == list(range(40))
+        assert all(c.status == want for c in done)
+        for c in done:
+            s.release(c)
+        reqs = []
+        for i in range(40):
+            x = data[i % 6]
+            if i % 2:
+                reqs.append(request(i % 6, Q_DECODE, 0.0, 99, tag=i))
+            else:
+                reqs.append(request(i % 6, Q_RANGE, float(x[x.size // 3]), tag=i))
+        s.submit(reqs)
+        got = {c.tag: c for c in s.wait(len(reqs))}
+        for i, r in enumerate(reqs):
+            c = got[i]
+            if i % 2:
+                assert c.status == want, i
+            else:
+                assert c.status == 0, i
+                assert c.result.count == cols[i % 6].range_filter(r.pred).count
+            s.release(c)
+        s.stop()
+        s.free()
+
+
 def test_budget_forces_waits_and_efull(gpu):
     from buff_gb300.capi import Q_DECODE, Q_SUM
     from buff_gb300.compress import Column
