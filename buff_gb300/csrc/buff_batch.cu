@@ -926,10 +926,10 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
   __shared__ bool s_last;
   const uint32_t lane = threadIdx.x & 31;
   uint8_t *ring = dyn_smem + (threadIdx.x >> 5) * kRingBytes;  // FS / S classes only
-  // a warp's first item is its own index; later items come from the work
-  // counter, past the first round (the counter is one address that every
-  // taking warp hits: tens of thousands of small items queued on it for
-  // tens of microseconds)
+  // a warp's first item is its own index; its later items come from the
+  // work counter, offset past the items the warps took that way (the counter
+  // is one address that every taking warp hits: tens of thousands of small
+  // items queued on it for tens of microseconds)
   // the batch's next class launch (programmatic dependent launch) may start
   // once every block of this one runs: the classes are independent
   asm volatile("griddepcontrol.launch_dependents;");
