@@ -143,6 +143,11 @@ struct buff_server {
   std::deque<Req> pending;
   std::vector<buff_completion> done;
   std::atomic<uint64_t> n_done{0};
+  // requests pushed to `pending` and completions taken from `done` so far:
+  // the loop and the pollers look at these before taking the mutex, which
+  // callers spinning on an empty poll would otherwise hold for every pass
+  std::atomic<uint64_t> n_pending_in{0}, n_polled{0};
+  uint64_t n_pending_out = 0;  // loop thread only
 
   std::thread th;
   std::atomic<bool> running{false};
@@ -430,6 +435,7 @@ void run_encode(buff_server *S, Req &q) {
       rel.cls[0] = q.cls[0];
       rel.cls[1] = -1;
       S->pending.push_front(rel);
+      S->n_pending_in.fetch_add(1, std::memory_order_release);
     }
   }
   if (st != BUFF_OK && col) buff_col_free(col);
@@ -530,7 +536,7 @@ void loop(buff_server *S) {
         retire(S, sl);
       }
     }
-    {
+    if (S->n_pending_in.load(std::memory_order_acquire) != S->n_pending_out) {
       std::lock_guard<std::mutex> lk(S->mu);
       while (!S->pending.empty()) {
         Req &q = S->pending.front();
@@ -542,6 +548,7 @@ void loop(buff_server *S) {
           S->waiting.push_back(q);
         }
         S->pending.pop_front();
+        S->n_pending_out++;
         worked = true;
       }
     }
@@ -814,16 +821,21 @@ int buff_server_submit(buff_server *S, const buff_request *reqs, uint32_t n) {
     }
     if (q.kind == kQuery) q.col = S->store[reqs[i].column];
     S->pending.push_back(q);
+    S->n_pending_in.fetch_add(1, std::memory_order_release);
   }
   return BUFF_OK;
 }
 
 int buff_server_poll(buff_server *S, buff_completion *out, uint32_t cap, uint32_t *n) {
   if (!S || !n || (cap && !out)) return BUFF_EINVAL;
+  *n = 0;
+  if (S->n_done.load(std::memory_order_acquire) == S->n_polled.load(std::memory_order_relaxed))
+    return BUFF_OK;  // nothing new: no mutex
   std::lock_guard<std::mutex> lk(S->mu);
   const uint32_t m = (uint32_t)(S->done.size() < cap ? S->done.size() : cap);
   for (uint32_t i = 0; i < m; ++i) out[i] = S->done[i];
   S->done.erase(S->done.begin(), S->done.begin() + m);
+  S->n_polled.fetch_add(m, std::memory_order_relaxed);
   *n = m;
   return BUFF_OK;
 }
@@ -842,6 +854,7 @@ int buff_server_release(buff_server *S, const buff_completion *c) {
   q.col = nullptr;
   std::lock_guard<std::mutex> lk(S->mu);
   S->pending.push_front(q);
+  S->n_pending_in.fetch_add(1, std::memory_order_release);
   return BUFF_OK;
 }
 
