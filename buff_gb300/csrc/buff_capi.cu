@@ -967,7 +967,7 @@ int buff_serialize(const buff_col *c, uint8_t *out, uint64_t cap, uint64_t *len,
   if (c->layout == 1 || c->layout == 3) {
     std::vector<uint8_t> img;
     // the header and sparse columns first; the dense slices and tail follow
-    // it, written in place by the device when it can reach `out`
+    // it from one kernel (in place into pinned memory, else staged and copied)
     bool complete = false;
     int st = c->layout == 1 ? major_image(c, img, S(stream), true)
                             : rapg_image(c, img, S(stream), true, &complete);
@@ -978,7 +978,8 @@ int buff_serialize(const buff_col *c, uint8_t *out, uint64_t cap, uint64_t *len,
     if (!complete && !is_device_ptr(out)) {
       cudaError_t e = cudaSuccess;
       memcpy(out, img.data(), img.size());
-      if (buffk::download_body(c, out + img.size(), c->k - c->m, 0x80808080u, S(stream), &e)) {
+      if (buffk::body_to_host(c, out + img.size(), body, c->k - c->m, 0x80808080u, S(stream),
+                              &e)) {
         if (e == cudaSuccess) e = cudaStreamSynchronize(S(stream));
         return cuda_status(e);
       }
@@ -1009,11 +1010,12 @@ int buff_serialize(const buff_col *c, uint8_t *out, uint64_t cap, uint64_t *len,
     CK(cudaMemcpyAsync(out, hdr, 20, cudaMemcpyHostToDevice, s));
   } else {
     memcpy(out, hdr, 20);
-    // host memory the device can write: the kernel puts every slice and tail
-    // byte in place (unflipped for the buff layout)
+    // every slice and tail byte (unflipped for the buff layout) from one
+    // kernel: written in place into pinned memory, else staged on the device
+    // and copied once
     cudaError_t e = cudaSuccess;
     const uint32_t flipx = (c->flags & BUFF_FLAG_BUFF_LAYOUT) ? 0x80808080u : 0u;
-    if (buffk::download_body(c, out + 20, c->k, flipx, s, &e)) {
+    if (buffk::body_to_host(c, out + 20, need - 20, c->k, flipx, s, &e)) {
       CK(e);
       CK(cudaStreamSynchronize(s));
       goto done;

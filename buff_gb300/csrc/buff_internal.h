@@ -174,6 +174,10 @@ bool upload_slices(const uint8_t *image, buff_col *c, uint32_t flipx, cudaStream
 // (nothing launched).
 bool download_body(const buff_col *c, uint8_t *dst, uint32_t nslices, uint32_t flipx,
                    cudaStream_t s, cudaError_t *err);
+// The same body (body_bytes long) into host memory: in place when dst is
+// pinned, else staged in device memory and copied by the copy engine.
+bool body_to_host(const buff_col *c, uint8_t *dst, uint64_t body_bytes, uint32_t nslices,
+                  uint32_t flipx, cudaStream_t s, cudaError_t *err);
 // Filters of the buff-major layout; with m == 0 the same compare runs over a
 // plain column's slices and tail.  cand (may be null) restricts the rows.
 cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, uint32_t ttail,

@@ -125,11 +125,10 @@ int buff_col_get_info(const buff_col *col, buff_col_info *info);
 /* The exact reference byte image (the Vec<u8> buff_simd256_encode returns):
  * 20-byte header, k flipped byte slices of n bytes, packed tail.  *len
  * receives the image size; out = NULL (or cap < *len) returns BUFF_EINVAL
- * after setting it.  out is device or host memory the caller may write: a
- * host image that the device can reach (pinned memory, or pageable memory
- * on a system whose device uses the host page tables) has its slices and
- * tail written there by the device directly, so it must be writable memory,
- * not a read-only mapping.  Returns when the image is complete. */
+ * after setting it.  out is device or host memory the caller may write; a
+ * pinned host image has its slices and tail written there by the device
+ * directly, a pageable one receives them in one copy.  Returns when the
+ * image is complete. */
 int buff_serialize(const buff_col *col, uint8_t *out, uint64_t cap, uint64_t *len,
                    void *stream);
 /* Rebuilds a handle from a reference byte image.  The image does not carry
