@@ -375,13 +375,36 @@ __device__ __forceinline__ double i64_to_f64_scaled(long long v, int dlen) {
 }
 
 
-// The same for 0 <= a < 2^53 (exact): the leading one placed at bit 52 and
-// the exponent added on top of it, without sign handling or rounding.
-__device__ __forceinline__ double u53_to_f64_scaled(unsigned long long a, int dlen) {
-  if (a == 0) return 0.0;
-  const int e = 63 - __clzll(a);
-  return __longlong_as_double(
-      (long long)((a << (52 - e)) + ((unsigned long long)(e - dlen + 1022) << 52)));
+// The same for a = hi:lo in [1, 2^53) in 32-bit steps: the word holding the
+// leading one (hi, or lo when hi is 0) shifted so that the one lands on bit
+// 63 of the pair, the pair moved right 11 bits into the significand field,
+// and the exponent added on top of the leading one.  Returns the high and
+// low words of the double.
+__device__ __forceinline__ void u53w_bits(uint32_t hi, uint32_t lo, int dlen, uint32_t &oh,
+                                          uint32_t &ol) {
+  const bool z = hi == 0u;
+  const uint32_t H = z ? lo : hi, L = z ? 0u : lo;
+  const uint32_t lz = __clz(H);
+  const uint32_t NH = __funnelshift_l(L, H, lz), NL = __funnelshift_l(0u, L, lz);
+  const int e1 = (z ? 31 : 63) - (int)lz - dlen + 1022;  // biased exponent - 1
+  oh = (NH >> 11) + ((uint32_t)e1 << 20);
+  ol = __funnelshift_r(NL, NH, 11);
+}
+__device__ __forceinline__ double u53w_to_f64_scaled(uint32_t hi, uint32_t lo, int dlen) {
+  uint32_t oh, ol;
+  u53w_bits(hi, lo, dlen, oh, ol);
+  return __hiloint2double((int)oh, (int)ol);
+}
+
+// The same for a signed v with |v| < 2^53 (two's complement in 64 bits; 0
+// gives +0).
+__device__ __forceinline__ double s53_to_f64_scaled(unsigned long long v, int dlen) {
+  const unsigned long long sg = (unsigned long long)((long long)v >> 63);
+  const unsigned long long m = (v ^ sg) - sg;
+  uint32_t oh, ol;
+  u53w_bits((uint32_t)(m >> 32), (uint32_t)m, dlen, oh, ol);
+  oh |= (uint32_t)sg & 0x80000000u;
+  return m ? __hiloint2double((int)oh, (int)ol) : 0.0;
 }
 
 // The same for a value that fits in 32 bits: exact (|v| < 2^32 <= 2^53), so

@@ -831,6 +831,9 @@ struct RapgDecodeArgs {
   double *out;
 };
 
+// Conversion forms of the fast decodes (k_rapg_decode_fast4's CV).
+constexpr int kCvI32 = 0, kCvU53 = 1, kCvS53 = 2, kCvI64 = 3;
+
 // `width`-bit field `row` of a stream packed LSB-first from bit `bit0`.
 __device__ __forceinline__ uint32_t field_from(const uint8_t *p, unsigned long long bit0,
                                                uint32_t width, uint32_t row) {
@@ -911,7 +914,9 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode(RapgDecodeArgs a) {
 template <int KS, bool N32 = false>
 __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a) {
   using CodeT = typename std::conditional<N32, uint32_t, unsigned long long>::type;
-  asm volatile("griddepcontrol.launch_dependents;");  // see k_rapg_decode_fast4
+  // the outlier fix-up (a programmatic dependent launch) may start once every
+  // block of this pass runs; it waits for this pass before reading the values
+  asm volatile("griddepcontrol.launch_dependents;");
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nchunks = (a.n + kRowChunk - 1) / kRowChunk;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -970,21 +975,28 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a)
   }
 }
 
-// The same plans for 1..4 dense slices (every row written with the default
-// sparse bytes; k_rapg_fixup then rewrites the outlier rows): lane L takes 4
-// consecutive rows of each 128-row group -- one 4-byte load per dense slice,
-// a 4x4 byte transpose into the 4 rows' dense bytes, the tail fields by one
-// shuffle pair -- and the 4 values leave in one 32-byte store when the
-// output is 32-byte aligned (ST32), else in two 16-byte stores.  Merging the
-// outlier rows into this pass was measured slower: with 1 % outliers most
-// warps then wait on a dependent rank-and-byte load in most steps.
-template <int KS, bool N32, bool ST32, bool POS = false>
+// The same plans for 1..4 dense slices: lane L takes 4 consecutive rows of
+// each 128-row group -- one 4-byte load per dense slice, a 4x4 byte
+// transpose into the 4 rows' dense bytes, the tail fields by one shuffle
+// pair -- and the 4 values leave in one 32-byte store when the output is
+// 32-byte aligned (ST32), else in two 16-byte stores.  Without SP1 every row
+// is written with the default sparse bytes and a fix-up pass rewrites the
+// outlier rows.  With SP1 (one sparse column) the outlier rows are decoded
+// here: the chunk's 16 bitmap words and its first rank word are loaded one
+// chunk ahead, a prefix count over the words gives each lane its first
+// outlier's rank, and the chunk's outlier bytes (consecutive in the outlier
+// byte array) arrive as one window of up to 32 aligned 4-byte words loaded
+// with the slices -- no load of this chunk waits on another.  A chunk with
+// more than 124 outliers reads its bytes one by one.  (A first merge, one
+// dependent rank-and-byte load per outlier row, ran slower than the
+// separate fix-up.)  A row's code is assembled as two 32-bit words (the
+// sparse byte above KS dense bytes, the pair shifted left ts by one funnel
+// shift, the tail field below) and converted by the form CV names:
+// kCvI32 (every value in 32 bits), kCvU53 (every value in [1, 2^53)),
+// kCvS53 (every |value| below 2^53) or kCvI64 (rounding conversion).
+template <int KS, int CV, bool ST32, bool SP1>
 __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast4(RapgDecodeArgs a) {
   static_assert(KS >= 1 && KS <= 4, "k_rapg_decode_fast4 transposes at most 4 slices");
-  using CodeT = typename std::conditional<N32, uint32_t, unsigned long long>::type;
-  // the outlier fix-up (a programmatic dependent launch) may start once every
-  // block of this pass runs; it waits for this pass before reading the values
-  asm volatile("griddepcontrol.launch_dependents;");
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nchunks = (a.n + kRowChunk - 1) / kRowChunk;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -992,8 +1004,29 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast4(RapgDecodeArgs a
   const uint32_t ts = a.ts;
   const uint32_t tmask = ts ? ((1u << ts) - 1u) : 0u;
   const uint32_t kx = KS == 4 ? 0x80808080u : (0x80808080u & ((1u << (8 * (KS & 3))) - 1u));
+  const uint32_t sdef_hi = (uint32_t)(a.sdef >> 32), sdef_lo = (uint32_t)a.sdef;
+  // SP1: the default sparse byte in every byte of a word; bitmap word
+  // `lane` (< 16) of the chunk and the chunk's first rank
+  const uint32_t spd4 = SP1 ? (uint32_t)(a.sdef >> (8 * KS + ts)) * 0x01010101u : 0u;
+  const uint32_t nwords = (a.n + 31) / 32;
+  const uint8_t *ob = a.obytes + a.oofs[0];
+  uint32_t nW = 0, nR = 0;
+  if (SP1 && warp < nchunks) {
+    if (lane < 16 && warp * 16 + lane < nwords) nW = __ldg(a.obits + warp * 16 + lane);
+    nR = __ldg(a.orank + warp * 16);
+  }
   for (uint32_t ch = warp; ch < nchunks; ch += nwarps) {
     const uint32_t r0 = ch * kRowChunk;
+    uint32_t Bw = 0, Rc = 0;
+    if (SP1) {
+      Bw = nW;
+      Rc = nR;
+      const uint32_t cn = ch + nwarps;
+      if (cn < nchunks) {
+        nW = lane < 16 && cn * 16 + lane < nwords ? __ldg(a.obits + cn * 16 + lane) : 0u;
+        nR = __ldg(a.orank + cn * 16);
+      }
+    }
     uint32_t sw[4][KS];
 #pragma unroll
     for (int m = 0; m < 4; ++m)
@@ -1010,9 +1043,63 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast4(RapgDecodeArgs a
         tw[m] = __ldg(reinterpret_cast<const uint32_t *>(a.tail + (size_t)16 * ts * (r0 / 128 + m)) +
                       lane);
     }
+    // SP1: outliers before each lane's word within the chunk, the chunk's
+    // count, and the window of its outlier bytes (from the aligned word
+    // holding the first; the allocation extends 16 bytes past the last)
+    uint32_t ex = 0, tot = 0, off = 0, win = 0;
+    bool wide = false;
+    if (SP1) {
+      const uint32_t v = __popc(Bw);
+      uint32_t x = v;
+#pragma unroll
+      for (int o = 1; o < 16; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+      }
+      ex = x - v;
+      tot = __shfl_sync(0xFFFFFFFFu, x, 15);
+      if (tot) {
+        const uintptr_t p0 = reinterpret_cast<uintptr_t>(ob + Rc);
+        off = (uint32_t)(p0 & 3u);
+        const uint32_t nwin = (off + tot + 3) >> 2;
+        wide = nwin > 32;
+        if (!wide && lane < nwin) win = __ldg(reinterpret_cast<const uint32_t *>(p0 - off) + lane);
+      }
+    }
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
       const uint32_t row0 = r0 + m * 128 + 4 * lane;
+      // SP1: the 4 rows' sparse bytes in one word (byte i = row i): the
+      // default byte, or an outlier row's byte -- from the lane's 4 outlier
+      // bits in this group and the 4 outlier bytes from its first outlier's
+      // rank within the chunk
+      uint32_t spw = spd4;
+      if (SP1 && tot) {
+        const uint32_t src = 4 * m + (lane >> 3), sh = 4 * (lane & 7);
+        const uint32_t Wm = __shfl_sync(0xFFFFFFFFu, Bw, src);
+        const uint32_t Em = __shfl_sync(0xFFFFFFFFu, ex, src);
+        const uint32_t nib = (Wm >> sh) & 0xFu;
+        const uint32_t k0 = Em + __popc(Wm & ((1u << sh) - 1u));
+        uint32_t b4 = 0;
+        if (!wide) {
+          const uint32_t pos = off + k0;
+          const uint32_t w0 = __shfl_sync(0xFFFFFFFFu, win, (pos >> 2) & 31);
+          const uint32_t w1 = __shfl_sync(0xFFFFFFFFu, win, ((pos >> 2) + 1) & 31);
+          b4 = __funnelshift_r(w0, w1, 8 * (pos & 3));
+        } else {
+          const uint32_t no = __popc(nib);
+#pragma unroll
+          for (uint32_t j = 0; j < 4; ++j)
+            if (j < no) b4 |= (uint32_t)__ldg(ob + Rc + k0 + j) << (8 * j);
+        }
+        // row i takes byte popc(nib & (2^i - 1)): bit k < 3 of nib moved to
+        // nibble k + 1 (the three shifted copies do not overlap), then each
+        // nibble summed with those below it
+        const uint32_t e = ((nib & 7u) * 0x490u) & 0x1110u;
+        const uint32_t rows = __byte_perm(b4, 0u, e * 0x1111u);
+        const uint32_t msk = expand4(nib);
+        spw = (rows & msk) | (spd4 & ~msk);
+      }
       uint32_t W[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) W[j] = j < KS ? sw[m][KS - 1 - j] : 0u;
@@ -1030,15 +1117,31 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast4(RapgDecodeArgs a
       double v[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        CodeT code = (CodeT)(c[i] ^ kx);
-        if (ts) code = (code << ts) | (CodeT)((f >> (i * ts)) & tmask);
-        code |= (CodeT)a.sdef;
-        if (N32)
-          v[i] = i32_to_f64_scaled((int)((uint32_t)a.base + (uint32_t)code), a.dlen);
-        else if (POS)
-          v[i] = u53_to_f64_scaled((unsigned long long)a.base + code, a.dlen);
+        // (xhi:xlo) = sparse byte above the dense bytes; then << ts | field
+        uint32_t xlo = c[i] ^ kx, xhi = 0;
+        if (SP1) {
+          const uint32_t sp = __byte_perm(spw, 0u, 0x4440 + i);
+          if (KS == 4)
+            xhi = sp;
+          else
+            xlo |= sp << (8 * (KS & 3));
+        }
+        uint32_t hi = __funnelshift_l(xlo, xhi, ts);
+        uint32_t lo = (xlo << ts) | ((f >> (i * ts)) & tmask);
+        if (!SP1) {
+          hi |= sdef_hi;
+          lo |= sdef_lo;
+        }
+        const unsigned long long A =
+            (unsigned long long)a.base + (((unsigned long long)hi << 32) | lo);
+        if (CV == kCvI32)
+          v[i] = i32_to_f64_scaled((int)((uint32_t)a.base + lo), a.dlen);
+        else if (CV == kCvU53)
+          v[i] = u53w_to_f64_scaled((uint32_t)(A >> 32), (uint32_t)A, a.dlen);
+        else if (CV == kCvS53)
+          v[i] = s53_to_f64_scaled(A, a.dlen);
         else
-          v[i] = i64_to_f64_scaled((long long)((unsigned long long)a.base + code), a.dlen);
+          v[i] = i64_to_f64_scaled((long long)A, a.dlen);
       }
       double *o = a.out + row0;
       if (row0 + 4 <= a.n) {
@@ -1644,19 +1747,38 @@ static void launch_fast_ks(const RapgDecodeArgs &a, int g, cudaStream_t s) {
   }
 }
 
-template <int KS, bool N32>
-static void launch_fast4(const RapgDecodeArgs &a, int g, cudaStream_t s) {
-  const bool st32 = (reinterpret_cast<uintptr_t>(a.out) & 31u) == 0;
-  // every base + code in [0, 2^53): the unsigned exact conversion
-  const bool pos = !N32 && a.base >= 0 && a.R <= 52 &&
-                   (unsigned long long)a.base < (1ull << 53) - (1ull << a.R);
-  if (pos)
-    st32 ? k_rapg_decode_fast4<KS, false, true, true><<<g, kThreads, 0, s>>>(a)
-         : k_rapg_decode_fast4<KS, false, false, true><<<g, kThreads, 0, s>>>(a);
-  else if (st32)
-    k_rapg_decode_fast4<KS, N32, true><<<g, kThreads, 0, s>>>(a);
+template <int KS, int CV, bool SP1>
+static void launch_fast4_cv(const RapgDecodeArgs &a, int g, cudaStream_t s) {
+  if ((reinterpret_cast<uintptr_t>(a.out) & 31u) == 0)
+    k_rapg_decode_fast4<KS, CV, true, SP1><<<g, kThreads, 0, s>>>(a);
   else
-    k_rapg_decode_fast4<KS, N32, false><<<g, kThreads, 0, s>>>(a);
+    k_rapg_decode_fast4<KS, CV, false, SP1><<<g, kThreads, 0, s>>>(a);
+}
+
+// The conversion form: every value in 32 bits; else every base + code in
+// [1, 2^53) (unsigned, exact, no zero); else every |base + code| below 2^53
+// (exact); else the rounding 64-bit form.  One sparse column: the outlier rows are
+// decoded in the pass itself.
+template <int KS, bool SP1>
+static void launch_fast4_sp(const RapgDecodeArgs &a, bool n32, int g, cudaStream_t s) {
+  const unsigned long long ab =
+      a.base < 0 ? 0ull - (unsigned long long)a.base : (unsigned long long)a.base;
+  const bool exact = a.R <= 52 && ab < (1ull << 53) - (1ull << a.R) && a.dlen <= 1000;
+  if (n32)
+    launch_fast4_cv<KS, kCvI32, SP1>(a, g, s);
+  else if (exact && a.base >= 1)
+    launch_fast4_cv<KS, kCvU53, SP1>(a, g, s);
+  else if (exact)
+    launch_fast4_cv<KS, kCvS53, SP1>(a, g, s);
+  else
+    launch_fast4_cv<KS, kCvI64, SP1>(a, g, s);
+}
+template <int KS>
+static void launch_fast4(const RapgDecodeArgs &a, bool n32, int g, cudaStream_t s) {
+  if (a.m == 1)
+    launch_fast4_sp<KS, true>(a, n32, g, s);
+  else
+    launch_fast4_sp<KS, false>(a, n32, g, s);
 }
 
 // The rows that are outliers in some sparse column, after a fast pass wrote
@@ -1697,13 +1819,13 @@ static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
     const bool n32 =
         a.R <= 32 && a.base >= INT32_MIN && maxc >= 0 && a.base + maxc <= (long long)INT32_MAX;
     switch (a.ks) {
-      case 1: n32 ? launch_fast4<1, true>(a, g, s) : launch_fast4<1, false>(a, g, s); break;
-      case 2: n32 ? launch_fast4<2, true>(a, g, s) : launch_fast4<2, false>(a, g, s); break;
-      case 3: n32 ? launch_fast4<3, true>(a, g, s) : launch_fast4<3, false>(a, g, s); break;
-      default: n32 ? launch_fast4<4, true>(a, g, s) : launch_fast4<4, false>(a, g, s); break;
+      case 1: launch_fast4<1>(a, n32, g, s); break;
+      case 2: launch_fast4<2>(a, n32, g, s); break;
+      case 3: launch_fast4<3>(a, n32, g, s); break;
+      default: launch_fast4<4>(a, n32, g, s); break;
     }
     count_launch();
-    if (a.m) launch_fixup(a, s);
+    if (a.m > 1) launch_fixup(a, s);
     return;
   }
   {

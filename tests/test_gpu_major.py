@@ -132,6 +132,24 @@ def test_major_outlier_workload(oracle, gpu):
     _check_queries(oracle, col, ref, 1000000, RAW, x)
 
 
+def test_major_dense_outlier_runs(oracle, gpu):
+    """One sparse byte column (the first 2,000 rows vote) with 512-row
+    chunks that are outliers in every row or in half of them: the decode
+    reads those chunks' outlier bytes one by one instead of as one window."""
+    from buff_gb300.compress import FLAG_RAW_BITMAPS, MajorColumn
+
+    x, scale = major_case("one", 70_001, 13)
+    rng = np.random.default_rng(14)
+    pos = np.concatenate([np.arange(6_000, 10_100),
+                          40_000 + np.nonzero(rng.uniform(size=30_001) < 0.5)[0]])
+    x[pos] = np.round(rng.uniform(-1e4, 1e4, pos.size), 6)
+    ref = oracle.encode_majority(x, scale, RAW)
+    assert oracle.majority_layout(ref, RAW)[0] == 1
+    col = MajorColumn.encode(x, scale, FLAG_RAW_BITMAPS)
+    assert col.serialize() == ref
+    _check_queries(oracle, col, ref, scale, RAW, x)
+
+
 def test_major_f32_and_device_input(oracle, gpu):
     import torch
 

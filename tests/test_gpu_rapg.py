@@ -30,7 +30,16 @@ def _cases():
     wide = np.round(rng.normal(3e6, 50, 20_011), 9)
     pos = np.nonzero(rng.uniform(size=wide.size) < 0.01)[0]
     wide[pos] = np.round(rng.uniform(1e8, 4e9, pos.size), 9)
-    return rapg_cases() + [("big", big, 1000000), ("runs", runs, 1000000),
+    # one sparse byte (the first 2,000 rows decide) with 512-row chunks that
+    # are outliers throughout or in half their rows: chunks whose outlier
+    # bytes exceed one 128-byte window of the decode
+    dense = np.round(rng.normal(100, 5, 60_001), 6)
+    pos = np.nonzero(rng.uniform(size=dense.size) < 0.01)[0]
+    pos = np.concatenate([pos, np.arange(5_000, 9_000), 30_000 + np.nonzero(
+        rng.uniform(size=30_001) < 0.5)[0]])
+    dense[pos] = np.round(rng.uniform(1e5, 1e6, pos.size), 6)
+    return rapg_cases() + [("big", big, 1000000), ("dense_runs", dense, 1000000),
+                           ("runs", runs, 1000000),
                            ("narrow", narrow, 100), ("narrow0", narrow0, 100),
                            ("tenth", tenth, 10), ("tiny", tiny, 10),
                            ("f32", f32, 100), ("wide_codes", wide, 10 ** 9)]
