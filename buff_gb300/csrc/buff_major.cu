@@ -465,6 +465,130 @@ __global__ void __launch_bounds__(kThreads, 4) k_filter_major1(MajorArgs a) {
   }
 }
 
+// The 32 R-bit tail fields of a 32-row block (R words, LSB-first) compared
+// with `t`: four fields at a time spread into the bytes of a word (constant
+// shifts), then per-byte SWAR -- field > t is the MSB of field + 127 - t,
+// field == t the clear MSB of (field ^ t) + 127 (no byte carries: fields and
+// t are below 128) -- and the MSBs gathered into row bitmaps.
+template <int R>
+__device__ __forceinline__ void tail_cmp32(const uint32_t *tw, uint32_t t, uint32_t &gtt,
+                                           uint32_t &eqt) {
+  constexpr uint32_t fm = (1u << R) - 1u;
+  const uint32_t cg = (127u - t) * 0x01010101u, t4 = t * 0x01010101u;
+  uint32_t mg[8], me[8];
+#pragma unroll
+  for (int g = 0; g < 8; ++g) {
+    const int bit = 4 * g * R, wi = bit >> 5, sh = bit & 31;
+    const uint32_t x = sh == 0 ? tw[wi] : __funnelshift_r(tw[wi], wi + 1 < R ? tw[wi + 1] : 0u, sh);
+    const uint32_t y = (x & fm) | ((x << (8 - R)) & (fm << 8)) | ((x << (16 - 2 * R)) & (fm << 16)) |
+                       ((x << (24 - 3 * R)) & (fm << 24));
+    mg[g] = (y + cg) & H;
+    me[g] = ~((y ^ t4) + 0x7F7F7F7Fu) & H;
+  }
+  gtt = gather32(mg);
+  eqt = gather32(me);
+}
+
+// buff-major filters of a column with one sparse byte column and no dense
+// slices (the RAPG-major layout of 8-bit values: the code is the byte, then
+// R tail bits): thread = 32 rows -- the bitmap word, its outlier rank and
+// the block's R tail words, loaded one block ahead; the block's outlier
+// bytes (consecutive from its rank) come from three aligned words loaded
+// together when it has at most 8 outliers, singly beyond; the tail fields
+// of the rows still equal to the target are compared 4 at a time
+// (tail_cmp32).  Results are those of k_filter_major.
+template <bool IS_RANGE, int R>
+__global__ void __launch_bounds__(kThreads) k_filter_major0(MajorArgs a) {
+  const uint32_t nwords = (a.n + 31) / 32;
+  const uint32_t M = a.majors[0], T = a.tbyte[0];
+  const uint8_t *ob0 = a.obytes + a.oofs[0];
+  uint32_t cnt = 0;
+  const uint32_t step = gridDim.x * blockDim.x;
+  // a thread's next block (bitmap word, rank, tail words) is loaded before
+  // its current one is compared
+  uint32_t nB = 0, nrk = 0, ntw[R > 0 ? R : 1];
+  {
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w < nwords) {
+      nB = __ldg(a.obits + w);
+      nrk = __ldg(a.orank + w);
+#pragma unroll
+      for (int i = 0; i < R; ++i)
+        ntw[i] = __ldg(reinterpret_cast<const uint32_t *>(a.tail + (size_t)w * 4 * R) + i);
+    }
+  }
+  for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += step) {
+    const uint32_t row0 = w * 32;
+    const uint32_t valid = a.n - row0 >= 32 ? 0xFFFFFFFFu : ((1u << (a.n - row0)) - 1u);
+    const uint32_t B = nB, rk = nrk;
+    uint32_t tw[R > 0 ? R : 1];
+#pragma unroll
+    for (int i = 0; i < R; ++i) tw[i] = ntw[i];
+    if (w + step < nwords) {
+      nB = __ldg(a.obits + w + step);
+      nrk = __ldg(a.orank + w + step);
+#pragma unroll
+      for (int i = 0; i < R; ++i)
+        ntw[i] = __ldg(reinterpret_cast<const uint32_t *>(a.tail + (size_t)(w + step) * 4 * R) + i);
+    }
+    uint32_t og = 0, oe = 0;
+    if (B) {
+      const uint32_t no = __popc(B);
+      const uintptr_t p = reinterpret_cast<uintptr_t>(ob0 + rk);
+      uint32_t w0 = 0, w1 = 0, w2 = 0;
+      if (no <= 8) {  // bytes p .. p + 7 lie in the 3 aligned words from p & ~3
+        const uint32_t *q = reinterpret_cast<const uint32_t *>(p & ~(uintptr_t)3);
+        w0 = __ldg(q);
+        w1 = __ldg(q + 1);
+        w2 = __ldg(q + 2);
+      }
+      const uint32_t o8 = 8 * (uint32_t)(p & 3u);
+      const uint32_t lo4 = __funnelshift_r(w0, w1, o8), hi4 = __funnelshift_r(w1, w2, o8);
+      for (uint32_t b = B, k = 0; b; ++k) {
+        const uint32_t j = __ffs(b) - 1;
+        b &= b - 1;
+        const uint32_t v = no > 8 ? (uint32_t)__ldg(ob0 + rk + k)
+                                  : ((k < 4 ? lo4 : hi4) >> (8 * (k & 3))) & 0xFFu;
+        og |= (uint32_t)(v > T) << j;
+        oe |= (uint32_t)(v == T) << j;
+      }
+    }
+    const uint32_t non = ~B & valid;
+    uint32_t gt = IS_RANGE ? og | (M > T ? non : 0u) : 0u;
+    uint32_t eq = (oe | (M == T ? non : 0u)) & valid;
+    uint32_t res = IS_RANGE ? gt : 0u;  // equality only sets rows in the tail step
+    if constexpr (R > 0) {
+      if (eq) {
+        uint32_t gtt, eqt;
+        tail_cmp32<R>(tw, a.ttail, gtt, eqt);
+        gt |= eq & gtt;
+        eq &= eqt;
+        res = IS_RANGE ? gt : eq;
+      }
+    }
+    __stcs(a.words + w, res);
+    cnt += __popc(res);
+  }
+  if (a.count) {
+    const unsigned long long c = warp_sum_ull(cnt);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(a.count, c);
+  }
+}
+
+template <bool IS_RANGE>
+static void launch_filter_major0(const MajorArgs &a, int grid, cudaStream_t s) {
+  switch (a.r) {
+    case 0: k_filter_major0<IS_RANGE, 0><<<grid, kThreads, 0, s>>>(a); break;
+    case 1: k_filter_major0<IS_RANGE, 1><<<grid, kThreads, 0, s>>>(a); break;
+    case 2: k_filter_major0<IS_RANGE, 2><<<grid, kThreads, 0, s>>>(a); break;
+    case 3: k_filter_major0<IS_RANGE, 3><<<grid, kThreads, 0, s>>>(a); break;
+    case 4: k_filter_major0<IS_RANGE, 4><<<grid, kThreads, 0, s>>>(a); break;
+    case 5: k_filter_major0<IS_RANGE, 5><<<grid, kThreads, 0, s>>>(a); break;
+    case 6: k_filter_major0<IS_RANGE, 6><<<grid, kThreads, 0, s>>>(a); break;
+    default: k_filter_major0<IS_RANGE, 7><<<grid, kThreads, 0, s>>>(a); break;
+  }
+}
+
 // ---------------------------------------------------------------- sum / max helpers
 
 // Sum of nbytes bytes from p (any alignment): the bytes before the first
@@ -996,7 +1120,8 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast(RapgDecodeArgs a)
 // kCvS53 (every |value| below 2^53) or kCvI64 (rounding conversion).
 template <int KS, int CV, bool ST32, bool SP1>
 __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast4(RapgDecodeArgs a) {
-  static_assert(KS >= 1 && KS <= 4, "k_rapg_decode_fast4 transposes at most 4 slices");
+  static_assert(KS >= 0 && KS <= 4, "k_rapg_decode_fast4 transposes at most 4 slices");
+  static_assert(KS > 0 || SP1, "without dense slices the pass takes one sparse column");
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nchunks = (a.n + kRowChunk - 1) / kRowChunk;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1027,7 +1152,7 @@ __global__ void __launch_bounds__(kThreads) k_rapg_decode_fast4(RapgDecodeArgs a
         nR = __ldg(a.orank + cn * 16);
       }
     }
-    uint32_t sw[4][KS];
+    uint32_t sw[4][KS > 0 ? KS : 1];
 #pragma unroll
     for (int m = 0; m < 4; ++m)
 #pragma unroll
@@ -1496,10 +1621,16 @@ cudaError_t major_filter(const buff_col *c, int is_range, const uint8_t *tbyte, 
     return cudaGetLastError();
   }
   const int grid = grid_of(nw, kThreads);
-  if (is_range)
+  if (c->m == 1 && !cand && a.kd == 0 && a.r <= 7) {
+    if (is_range)
+      launch_filter_major0<true>(a, grid, s);
+    else
+      launch_filter_major0<false>(a, grid, s);
+  } else if (is_range) {
     k_filter_major<true><<<grid, kThreads, 0, s>>>(a);
-  else
+  } else {
     k_filter_major<false><<<grid, kThreads, 0, s>>>(a);
+  }
   count_launch();
   return cudaGetLastError();
 }
@@ -1775,10 +1906,10 @@ static void launch_fast4_sp(const RapgDecodeArgs &a, bool n32, int g, cudaStream
 }
 template <int KS>
 static void launch_fast4(const RapgDecodeArgs &a, bool n32, int g, cudaStream_t s) {
-  if (a.m == 1)
+  if (KS == 0 || a.m == 1)
     launch_fast4_sp<KS, true>(a, n32, g, s);
   else
-    launch_fast4_sp<KS, false>(a, n32, g, s);
+    launch_fast4_sp<KS, KS == 0>(a, n32, g, s);
 }
 
 // The rows that are outliers in some sparse column, after a fast pass wrote
@@ -1813,12 +1944,13 @@ static void launch_fixup(const RapgDecodeArgs &a, cudaStream_t s) {
 }
 
 static void launch_decode_fast(const RapgDecodeArgs &a, cudaStream_t s) {
-  if (a.ks >= 1 && a.ks <= 4) {
+  if ((a.ks >= 1 && a.ks <= 4) || (a.ks == 0 && a.m == 1)) {
     const int g = grid_of((size_t)(a.n + kRowChunk - 1) / kRowChunk * 32, kThreads);
     const long long maxc = a.R >= 63 ? -1 : (long long)((1ull << a.R) - 1ull);
     const bool n32 =
         a.R <= 32 && a.base >= INT32_MIN && maxc >= 0 && a.base + maxc <= (long long)INT32_MAX;
     switch (a.ks) {
+      case 0: launch_fast4<0>(a, n32, g, s); break;
       case 1: launch_fast4<1>(a, n32, g, s); break;
       case 2: launch_fast4<2>(a, n32, g, s); break;
       case 3: launch_fast4<3>(a, n32, g, s); break;
