@@ -329,6 +329,22 @@ __device__ __noinline__ void refine32(const uint8_t *__restrict__ slices, size_t
   }
 }
 
+// A queued block's refinement (the later slices, the tail), its row limit,
+// its result word; returns the rows set.
+template <bool IS_RANGE>
+__device__ __forceinline__ uint32_t finish_filter_block(const FilterArgs &a, unsigned long long tb,
+                                                        uint32_t blk, uint32_t gt, uint32_t eq) {
+  const uint32_t row0 = blk * 32;
+  refine32(a.slices, a.stride, a.k_used, tb, a.tail, a.r, a.ttail, row0, gt, eq);
+  uint32_t res = IS_RANGE ? gt : eq;
+  if (row0 + 32 > a.full_rows) {
+    const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
+    res &= lim >= 32 ? 0xFFFFFFFFu : ((1u << lim) - 1u);
+  }
+  __stcs(a.words + blk, res);
+  return __popc(res);
+}
+
 // buff_simd_range_filter / buff_simd_equal_filter (compress/buff_simd.rs:
 // 3361-3733) and their fused `_with_slice` forms (:3736-4025).  Lane L owns
 // 32 consecutive rows -- one bitmap word -- per load: 32 bytes of slice 0 are
@@ -337,11 +353,18 @@ __device__ __noinline__ void refine32(const uint8_t *__restrict__ slices, size_t
 // next slice refines them (gt |= eq & gt_j, eq &= eq_j), then the packed tail.
 // Rows >= full_rows stay clear, which reproduces the reference's 32-byte SIMD
 // loop that never reaches the rows after the last full 32-row block.  TH is
-// the top bit of the slice-0 target byte.
+// the top bit of the slice-0 target byte.  Blocks that still hold rows equal
+// to the target after slice 0 go to a per-warp queue and are refined 32 at a
+// time, one per lane, so the dependent loads of the later slices are waited
+// on once per 32 such blocks instead of in every step that meets one.
 template <bool IS_RANGE, bool TH>
 __global__ void __launch_bounds__(kThreads, 5) k_filter(FilterArgs a) {
   constexpr int U = 2;  // 32-byte loads in flight per lane
+  constexpr int kQ = 96;  // queue entries per warp (at most 31 + 2 * 32)
+  __shared__ uint32_t s_q[kThreads / 32][3][kQ];
   const uint32_t lane = threadIdx.x & 31;
+  uint32_t(*q)[kQ] = s_q[threadIdx.x >> 5];
+  uint32_t qn = 0;  // warp-uniform queue length
   const uint32_t nwords = (a.n + 31) / 32;
   const uint32_t nblk = a.k_used ? (a.n + 31) / 32 : 0u;  // 32-row blocks with a slice byte
   const uint32_t nsteps = (nblk + U * 32 - 1) / (U * 32);
@@ -360,41 +383,60 @@ __global__ void __launch_bounds__(kThreads, 5) k_filter(FilterArgs a) {
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const uint32_t blk = blk0 + u * 32;
+      d[u] = Bytes32{};
       if (blk < nblk) d[u] = ld_stream32(a.slices + (size_t)blk * 32);
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const uint32_t blk = blk0 + u * 32;
-      if (blk >= nblk) continue;
+      const bool live = blk < nblk;
       const uint32_t row0 = blk * 32;
       uint32_t m[8];
       uint32_t eor = 0;
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        m[q] = eq4t<TH>(d[u].w[q], lo0, lo1);
-        eor |= m[q];
+      for (int qq = 0; qq < 8; ++qq) {
+        m[qq] = eq4t<TH>(d[u].w[qq], lo0, lo1);
+        eor |= m[qq];
       }
       uint32_t eq = eor ? gather32(m) : 0u;
       uint32_t gt = 0;
       if (IS_RANGE) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) m[q] = gt4t<TH>(d[u].w[q], lo1);
+        for (int qq = 0; qq < 8; ++qq) m[qq] = gt4t<TH>(d[u].w[qq], lo1);
         gt = gather32(m);
       }
-      if (eq) {
-        if (deep)
-          refine32(a.slices, a.stride, a.k_used, tb, a.tail, a.r, a.ttail, row0, gt, eq);
-        else if (a.tail_only_eq)
-          eq = 0;
+      if (eq && !deep && a.tail_only_eq) eq = 0;
+      const bool more = live && deep && eq != 0;
+      const uint32_t qv = __ballot_sync(0xFFFFFFFFu, more);
+      if (more) {
+        const uint32_t at = qn + __popc(qv & ((1u << lane) - 1u));
+        q[0][at] = blk;
+        q[1][at] = gt;
+        q[2][at] = eq;
+      } else if (live) {
+        uint32_t res = IS_RANGE ? gt : eq;
+        if (row0 + 32 > a.full_rows) {
+          const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
+          res &= lim >= 32 ? 0xFFFFFFFFu : ((1u << lim) - 1u);
+        }
+        __stcs(a.words + blk, res);
+        cnt += __popc(res);
       }
-      uint32_t res = IS_RANGE ? gt : eq;
-      if (row0 + 32 > a.full_rows) {
-        const uint32_t lim = a.full_rows > row0 ? a.full_rows - row0 : 0u;
-        res &= lim >= 32 ? 0xFFFFFFFFu : ((1u << lim) - 1u);
-      }
-      __stcs(a.words + blk, res);
-      cnt += __popc(res);
+      qn += __popc(qv);
     }
+    __syncwarp();
+    while (qn >= 32) {  // refine 32 queued blocks, one per lane
+      qn -= 32;
+      const uint32_t blk = q[0][qn + lane];
+      uint32_t gt = q[1][qn + lane], eq = q[2][qn + lane];
+      __syncwarp();
+      cnt += finish_filter_block<IS_RANGE>(a, tb, blk, gt, eq);
+    }
+  }
+  if (lane < qn) {  // what is left in the queue
+    const uint32_t blk = q[0][lane];
+    uint32_t gt = q[1][lane], eq = q[2][lane];
+    cnt += finish_filter_block<IS_RANGE>(a, tb, blk, gt, eq);
   }
   // fixed_len < 8: no slices, every row compared in full on its packed code
   if (!a.k_used) {
