@@ -203,6 +203,15 @@ __device__ __forceinline__ Bytes32 ld_stream32(const uint8_t *p) {
                : "l"(p));
   return b;
 }
+// The same with an L2 prefetch of the 256-byte block around the address.
+__device__ __forceinline__ Bytes32 ld_stream32_pf(const uint8_t *p) {
+  Bytes32 b;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::256B.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(b.w[0]), "=r"(b.w[1]), "=r"(b.w[2]), "=r"(b.w[3]), "=r"(b.w[4]),
+                 "=r"(b.w[5]), "=r"(b.w[6]), "=r"(b.w[7])
+               : "l"(p));
+  return b;
+}
 __device__ __forceinline__ Bytes32 ld_cand32(const uint8_t *p) {
   const uint4 lo = __ldg(reinterpret_cast<const uint4 *>(p));
   const uint4 hi = __ldg(reinterpret_cast<const uint4 *>(p + 16));

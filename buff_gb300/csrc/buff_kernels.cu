@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_filter(FilterArgs a) {
     for (int u = 0; u < U; ++u) {
       const uint32_t blk = blk0 + u * 32;
       d[u] = Bytes32{};
-      if (blk < nblk) d[u] = ld_stream32(a.slices + (size_t)blk * 32);
+      if (blk < nblk) d[u] = ld_stream32_pf(a.slices + (size_t)blk * 32);
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
