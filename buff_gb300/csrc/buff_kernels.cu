@@ -356,9 +356,11 @@ __device__ __forceinline__ uint32_t finish_filter_block(const FilterArgs &a, uns
 // the top bit of the slice-0 target byte.  Blocks that still hold rows equal
 // to the target after slice 0 go to a per-warp queue and are refined 32 at a
 // time, one per lane, so the dependent loads of the later slices are waited
-// on once per 32 such blocks instead of in every step that meets one.
+// on once per 32 such blocks instead of in every step that meets one.  A
+// step's slice-0 loads are issued before the previous step is compared (two
+// steps, 128 bytes per lane, in flight; 4 CTAs per SM at 64 registers).
 template <bool IS_RANGE, bool TH>
-__global__ void __launch_bounds__(kThreads, 5) k_filter(FilterArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) k_filter(FilterArgs a) {
   constexpr int U = 2;  // 32-byte loads in flight per lane
   constexpr int kQ = 96;  // queue entries per warp (at most 31 + 2 * 32)
   __shared__ uint32_t s_q[kThreads / 32][3][kQ];
@@ -377,14 +379,25 @@ __global__ void __launch_bounds__(kThreads, 5) k_filter(FilterArgs a) {
   const uint32_t lo0 = (t0 & 0x7Fu) * 0x01010101u, lo1 = ((t0 & 0x7Fu) + 1u) * 0x01010101u;
   const bool deep = a.k_used > 1 || a.r;
   uint32_t cnt = 0;
+  // a step's slice-0 loads are issued before the previous step is compared
+  Bytes32 nd[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const uint32_t blk = warp * (U * 32) + lane + u * 32;
+    nd[u] = Bytes32{};
+    if (warp < nsteps && blk < nblk) nd[u] = ld_stream32_pf(a.slices + (size_t)blk * 32);
+  }
   for (uint32_t st = warp; st < nsteps; st += nwarps) {
     const uint32_t blk0 = st * (U * 32) + lane;
     Bytes32 d[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const uint32_t blk = blk0 + u * 32;
-      d[u] = Bytes32{};
-      if (blk < nblk) d[u] = ld_stream32_pf(a.slices + (size_t)blk * 32);
+    for (int u = 0; u < U; ++u) d[u] = nd[u];
+    if (st + nwarps < nsteps) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t blk = blk0 + nwarps * (U * 32) + u * 32;
+        if (blk < nblk) nd[u] = ld_stream32_pf(a.slices + (size_t)blk * 32);
+      }
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
