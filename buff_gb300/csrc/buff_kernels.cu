@@ -808,14 +808,30 @@ __global__ void __launch_bounds__(kThreads) k_max(const uint8_t *__restrict__ sl
   unsigned long long best = 0;
   bool have = false;
   uint32_t top = 0;  // leading byte of best
+  // a step's loads are issued before the previous step is tested
+  Bytes32 nd[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const uint32_t blk = warp * (U * 32) + lane + u * 32;
+    nd[u] = Bytes32{};
+    if (warp < nsteps && blk < nblk) nd[u] = ld_stream32_pf(slices + (size_t)blk * 32);
+  }
   for (uint32_t st = warp; st < nsteps; st += nwarps) {
     const uint32_t blk0 = st * (U * 32) + lane;
     Bytes32 d[U];
 #pragma unroll
+    for (int u = 0; u < U; ++u) d[u] = nd[u];
+    if (st + nwarps < nsteps) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t blk = blk0 + nwarps * (U * 32) + u * 32;
+        if (blk < nblk) nd[u] = ld_stream32_pf(slices + (size_t)blk * 32);
+      }
+    }
+#pragma unroll
     for (int u = 0; u < U; ++u) {
       const uint32_t blk = blk0 + u * 32;
       if (blk < nblk) {
-        d[u] = ld_stream32(slices + (size_t)blk * 32);
         const uint32_t row0 = blk * 32;
         if (row0 + 32 > n) {  // padding rows -> flipped zero
 #pragma unroll
