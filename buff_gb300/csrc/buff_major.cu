@@ -401,32 +401,51 @@ __global__ void __launch_bounds__(kThreads, 4) k_filter_major1(MajorArgs a) {
     }
     gt &= valid;
     eq &= valid;
-    {
-      uint32_t m[8];
+    uint32_t vote;
+    if (dpre) {
+      // both dense bytes at hand: their per-byte results are combined before
+      // the one gather per result (row above the two target bytes: first
+      // byte above, or equal and the second above; equal: both equal)
+      uint32_t mg[8], me[8], eor = 0;
 #pragma unroll
-      for (int qq = 0; qq < 8; ++qq) m[qq] = eq4t<TH1>(d0.w[qq], a0, a1);
-      const uint32_t e = gather32(m);
-      if (IS_RANGE) {
-#pragma unroll
-        for (int qq = 0; qq < 8; ++qq) m[qq] = gt4t<TH1>(d0.w[qq], a1);
-        gt |= eq & gather32(m);
+      for (int qq = 0; qq < 8; ++qq) {
+        const uint32_t e0 = eq4t<TH1>(d0.w[qq], a0, a1), e1 = eq4t<TH2>(d1.w[qq], b0, b1);
+        eor |= e0;
+        me[qq] = e0 & e1;
+        if (IS_RANGE) mg[qq] = gt4t<TH1>(d0.w[qq], a1) | (e0 & gt4t<TH2>(d1.w[qq], b1));
       }
-      eq &= e;
-    }
-    const bool need1 = two && eq != 0;
-    const uint32_t vote = __ballot_sync(0xFFFFFFFFu, need1);
-    if (need1) {
-      if (!dpre) d1 = ld_cand32(s1 + row0);
-      uint32_t m[8];
+      if (IS_RANGE) gt |= eq & gather32(mg);
+      eq &= gather32(me);
+      vote = __ballot_sync(0xFFFFFFFFu, live && eor != 0);
+    } else {
+      // the first dense byte, then the second for the lanes that still need it
+      {
+        uint32_t m[8];
 #pragma unroll
-      for (int qq = 0; qq < 8; ++qq) m[qq] = eq4t<TH2>(d1.w[qq], b0, b1);
-      const uint32_t e = gather32(m);
-      if (IS_RANGE) {
+        for (int qq = 0; qq < 8; ++qq) m[qq] = eq4t<TH1>(d0.w[qq], a0, a1);
+        const uint32_t e = gather32(m);
+        if (IS_RANGE) {
 #pragma unroll
-        for (int qq = 0; qq < 8; ++qq) m[qq] = gt4t<TH2>(d1.w[qq], b1);
-        gt |= eq & gather32(m);
+          for (int qq = 0; qq < 8; ++qq) m[qq] = gt4t<TH1>(d0.w[qq], a1);
+          gt |= eq & gather32(m);
+        }
+        eq &= e;
       }
-      eq &= e;
+      const bool need1 = two && eq != 0;
+      vote = __ballot_sync(0xFFFFFFFFu, need1);
+      if (need1) {
+        d1 = ld_cand32(s1 + row0);
+        uint32_t m[8];
+#pragma unroll
+        for (int qq = 0; qq < 8; ++qq) m[qq] = eq4t<TH2>(d1.w[qq], b0, b1);
+        const uint32_t e = gather32(m);
+        if (IS_RANGE) {
+#pragma unroll
+          for (int qq = 0; qq < 8; ++qq) m[qq] = gt4t<TH2>(d1.w[qq], b1);
+          gt |= eq & gather32(m);
+        }
+        eq &= e;
+      }
     }
     pre = two && __popc(vote) >= 16;
     // blocks with rows still equal to the target go to the queue
