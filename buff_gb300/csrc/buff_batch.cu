@@ -911,6 +911,7 @@ __device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_
 // ops only.  A query with a filter and a sum is one FS item; a query with a
 // sum (without a filter) and a max or decode is an S item and an MD item.
 enum { kClsF = 0, kClsFS = 1, kClsS = 2, kClsMD = 3, kClasses = 4 };
+constexpr uint32_t kBqShared = 512;  // class lists up to this size are read from shared memory
 
 // Persistent worker of one class: warp-granular items; the batch's class
 // list holds query indices qidx[] and the exclusive prefix of their tile
@@ -924,6 +925,17 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
                                             unsigned int *counter, BatchDone done) {
   extern __shared__ __align__(16) uint8_t dyn_smem[];
   __shared__ bool s_last;
+  // a class list of up to kBqShared queries is copied to shared memory once
+  // per block, so finding an item's query costs no global round trip
+  __shared__ uint32_t s_pf[kBqShared], s_qi[kBqShared];
+  const bool lists_shared = nq <= kBqShared;
+  if (lists_shared) {
+    for (uint32_t i = threadIdx.x; i < nq; i += blockDim.x) {
+      s_pf[i] = __ldg(prefix + i);
+      s_qi[i] = __ldg(qidx + i);
+    }
+    __syncthreads();
+  }
   const uint32_t lane = threadIdx.x & 31;
   uint8_t *ring = dyn_smem + (threadIdx.x >> 5) * kRingBytes;  // FS / S classes only
   // a warp's first item is its own index; its later items come from the
@@ -935,10 +947,18 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
   asm volatile("griddepcontrol.launch_dependents;");
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   uint32_t it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // a launch with a few items per warp (a serving batch split for latency)
+  // strides them statically: warp w takes w, w + nw, ... without the work
+  // counter's round trip before each item
+  const bool stride = nitems <= 4 * nw;
   for (bool first = true;; first = false) {
     if (!first) {
-      if (lane == 0) it = nw + atomicAdd(counter, 1u);
-      it = __shfl_sync(0xFFFFFFFFu, it, 0);
+      if (stride) {
+        it += nw;
+      } else {
+        if (lane == 0) it = nw + atomicAdd(counter, 1u);
+        it = __shfl_sync(0xFFFFFFFFu, it, 0);
+      }
     }
     if (it >= nitems) break;
     // the query of item `it`: the last i with prefix[i] <= it, found by the
@@ -948,14 +968,14 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
     while (hi - lo > 1) {
       const uint32_t step = (hi - lo + 31) >> 5;
       const uint32_t pos = lo + lane * step;
-      const bool le = pos < hi && __ldg(prefix + pos) <= it;
+      const bool le = pos < hi && (lists_shared ? s_pf[pos] : __ldg(prefix + pos)) <= it;
       const uint32_t b = __ballot_sync(0xFFFFFFFFu, le);  // lane 0 always: prefix[lo] <= it
       const uint32_t j = 31 - __clz(b);
       lo += j * step;
       hi = min(hi, lo + step);
     }
-    const BQ &q = qs[__ldg(qidx + lo)];
-    const uint32_t r0 = (it - __ldg(prefix + lo)) * tile;
+    const BQ &q = qs[lists_shared ? s_qi[lo] : __ldg(qidx + lo)];
+    const uint32_t r0 = (it - (lists_shared ? s_pf[lo] : __ldg(prefix + lo))) * tile;
     const uint32_t r1 = min(q.n, r0 + tile);
     if (CLS == kClsF) tile_filter32<STAGE>(q, r0, r1, lane);
     if (CLS == kClsFS) tile_fs_async<true>(q, r0, r1, lane, ring);
