@@ -947,10 +947,11 @@ __global__ void __launch_bounds__(kBT, (CLS == kClsFS || CLS == kClsS) ? 3 : 0)
   asm volatile("griddepcontrol.launch_dependents;");
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   uint32_t it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  // a launch with a few items per warp (a serving batch split for latency)
-  // strides them statically: warp w takes w, w + nw, ... without the work
-  // counter's round trip before each item
-  const bool stride = nitems <= 4 * nw;
+  // a launch with a few items per warp (a serving batch is split into about
+  // eight per launched warp, for latency) strides them statically: warp w
+  // takes w, w + nw, ... without the work counter's round trip before each
+  // item
+  const bool stride = nitems <= 8 * nw;
   for (bool first = true;; first = false) {
     if (!first) {
       if (stride) {
