@@ -150,6 +150,34 @@ def test_major_dense_outlier_runs(oracle, gpu):
     _check_queries(oracle, col, ref, scale, RAW, x)
 
 
+@pytest.mark.parametrize("vmax,scale", [(5, 10), (10, 10), (3, 100), (5, 100), (10, 100),
+                                        (3, 1000), (5, 1000), (10, 1000)])
+def test_major_sparse_byte_only(oracle, gpu, vmax, scale):
+    """Columns whose code is one sparse byte and 0-7 tail bits (fixed_len
+    8-15, no dense slice): 90 % of the rows hold one value, the rest are
+    uniform.  Every query against the oracle."""
+    from buff_gb300.compress import FLAG_RAW_BITMAPS, MajorColumn
+
+    rng = np.random.default_rng(vmax * 7 + scale)
+    n = 50_003
+    dec = {10: 1, 100: 2, 1000: 3}[scale]
+    x = np.where(rng.uniform(size=n) < 0.9, vmax * 0.7,
+                 np.round(rng.uniform(0, vmax, n), dec))
+    ref = oracle.encode_majority(x, scale, RAW)
+    fl = oracle.header(ref).fixed_len
+    assert 8 <= fl < 16 and oracle.majority_layout(ref, RAW)[0] == 1
+    col = MajorColumn.encode(x, scale, FLAG_RAW_BITMAPS)
+    assert col.serialize() == ref
+    _check_queries(oracle, col, ref, scale, RAW, x)
+    for p in (vmax * 0.7, vmax * 0.7 + 10.0 ** -dec, vmax * 0.35, 0.0):
+        w, c, _ = oracle.range_filter_majority(ref, scale, p, RAW)
+        r = col.range_filter(p)
+        assert np.array_equal(r.words, w) and r.count == c, ("range", p)
+        w, c, _ = oracle.equal_filter_majority(ref, scale, p, RAW)
+        r = col.equal_filter(p)
+        assert np.array_equal(r.words, w) and r.count == c, ("equal", p)
+
+
 def test_major_f32_and_device_input(oracle, gpu):
     import torch
 
