@@ -2204,16 +2204,29 @@ int rapg_sum_impl(const buff_col *c, int precision, double *sum, cudaStream_t s)
   const uint32_t ks_dense = p.ks < kd ? p.ks : kd;
   unsigned long long *d = nullptr;
   uint64_t h[40] = {0};
+  // a plan that reads every dense slice and the whole tail fields is the
+  // buff-major sum's one launch (outlier bytes, slices and tail together:
+  // raw[col], raw[8 + j], raw[8 + kd]); other plans sum their parts one by one
+  const bool one = p.ks == kd && p.tbit0 == 0 && p.ts == c->r && n;
   CK(scratch(&d, 40, s));
-  CK(buffk::zero_u64(d, 40, s));
-  for (uint32_t col = 0; col < m; ++col)
-    if (c->nout[col]) CK(buffk::major_bytesum(c->obytes + c->oofs[col], c->nout[col], d + col, s));
-  if (n && ks_dense) CK(buffk::launch_sum(c, ks_dense, 0, d + 8, s));
-  for (uint32_t j = kd; j < p.ks && n; ++j)
-    CK(buffk::major_bytesum(c->tail + c->rg_skip + (size_t)(j - kd) * n, n, d + 8 + j, s));
-  if (p.ts) CK(buffk::field_sum(c->tail, p.tbit0, p.ts, n, d + 32, s));
+  if (one) {
+    CK(buffk::major_sums(c, major_sum_args(c), d, nullptr, nullptr, s));
+  } else {
+    CK(buffk::zero_u64(d, 40, s));
+    for (uint32_t col = 0; col < m; ++col)
+      if (c->nout[col])
+        CK(buffk::major_bytesum(c->obytes + c->oofs[col], c->nout[col], d + col, s));
+    if (n && ks_dense) CK(buffk::launch_sum(c, ks_dense, 0, d + 8, s));
+    for (uint32_t j = kd; j < p.ks && n; ++j)
+      CK(buffk::major_bytesum(c->tail + c->rg_skip + (size_t)(j - kd) * n, n, d + 8 + j, s));
+    if (p.ts) CK(buffk::field_sum(c->tail, p.tbit0, p.ts, n, d + 32, s));
+  }
   CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  if (one) {
+    h[32] = p.ts ? h[8 + kd] : 0;
+    h[8 + kd] = 0;
+  }
   {
     // the f64 steps of byte_residue_sum (:2229-2404): each partial over
     // 2^(processed - ilen), the base term n * base / 2^dlen last
