@@ -737,32 +737,6 @@ __device__ __forceinline__ int dp4a_sum8(const uint4 &a, const uint4 &b, int acc
 }
 
 // Bits 0, R, 2R, ... of a word.
-constexpr uint32_t every_bit(int R) {
-  uint32_t p = 0;
-  for (int b = 0; b < 32; b += R) p |= 1u << b;
-  return p;
-}
-
-// Tail sum of a lane's 32 rows whose R-bit fields fill the R words at tp
-// (the rows all below n): bit b of word i sits at stream position 32i + b,
-// which weighs 2^((32i + b) mod R) -- wpopc with the phase of every word and
-// the class masks resolved at compile time (3 R^2 operations instead of
-// about 7 R^2 with a run-time width).
-template <int R>
-__device__ __forceinline__ uint32_t tail_sum32(const uint32_t *tp) {
-  uint32_t acc = 0;
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const uint32_t w = tp[i];
-#pragma unroll
-    for (int c = 0; c < R; ++c) {
-      const int sh = ((c - 32 * i) % R + R) % R;  // bits of class c in word i
-      acc += (uint32_t)__popc(w & (every_bit(R) << sh)) << c;
-    }
-  }
-  return acc;
-}
-
 template <bool DO_F>
 __device__ __forceinline__ void tile_fs_async(const BQ &qd, uint32_t r0, uint32_t r1,
                                               uint32_t lane, uint8_t *ring) {

@@ -277,6 +277,63 @@ __device__ __forceinline__ uint32_t wpopc(uint32_t w, uint32_t phase, uint32_t t
   return acc;
 }
 
+constexpr uint32_t every_bit(int R) {
+  uint32_t p = 0;
+  for (int b = 0; b < 32; b += R) p |= 1u << b;
+  return p;
+}
+
+// Tail sum of a lane's 32 rows whose R-bit fields fill the R words at tp
+// (the rows all below n): bit b of word i sits at stream position 32i + b,
+// which weighs 2^((32i + b) mod R) -- wpopc with the phase of every word and
+// the class masks resolved at compile time (3 R^2 operations instead of
+// about 7 R^2 with a run-time width).
+template <int R>
+__device__ __forceinline__ uint32_t tail_sum32(const uint32_t *tp) {
+  uint32_t acc = 0;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const uint32_t w = tp[i];
+#pragma unroll
+    for (int c = 0; c < R; ++c) {
+      const int sh = ((c - 32 * i) % R + R) % R;  // bits of class c in word i
+      acc += (uint32_t)__popc(w & (every_bit(R) << sh)) << c;
+    }
+  }
+  return acc;
+}
+
+// The tail sum of the whole 32-row blocks from block vt on, every nth: a
+// block's 32 R-bit fields fill R words (4R bytes at 4R * block); the words
+// are loaded together and summed with compile-time class masks; bits past
+// tail_bits (the padding rows of the last block) are cleared.
+template <int R>
+__device__ __forceinline__ unsigned long long tail_blocks_sum(const uint8_t *__restrict__ tail,
+                                                              unsigned long long tail_bits,
+                                                              uint32_t vt, uint32_t nth) {
+  const uint32_t nblk = (uint32_t)((tail_bits / R + 31) / 32);
+  unsigned long long acc = 0;
+  for (uint32_t b = vt; b < nblk; b += nth) {
+    const uint32_t *tp = reinterpret_cast<const uint32_t *>(tail) + (size_t)b * R;
+    uint32_t w[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) w[i] = __ldg(tp + i);
+    const unsigned long long bit0 = (unsigned long long)b * 32 * R;
+    if (bit0 + 32 * R > tail_bits) {
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const unsigned long long wb = bit0 + 32 * i;
+        if (wb >= tail_bits)
+          w[i] = 0;
+        else if (wb + 32 > tail_bits)
+          w[i] &= (1u << (uint32_t)(tail_bits - wb)) - 1u;
+      }
+    }
+    acc += tail_sum32<R>(w);
+  }
+  return acc;
+}
+
 // The slice sums (first ks slices, each a flat array of `stride` bytes whose
 // padding rows hold the flipped zero 0x80) and the packed tail sum (n * ts
 // bits, fields weighed by wpopc) of thread tid of nth, added into the
@@ -317,35 +374,17 @@ __device__ __forceinline__ void sum_slices_tail(const uint8_t *__restrict__ slic
     if (lane == 0 && w) atomicAdd(&s_acc[s], w);
   }
   if (ts) {
-    const unsigned long long nbytes = (tail_bits + 7) / 8;
-    const uint32_t ntv = (uint32_t)((nbytes + 15) / 16);
-    unsigned long long acc = 0;
     uint32_t vt = tid + ks * rot;
     if (vt >= nth) vt -= nth;
-    // A word starting at stream bit b0 has phase b0 mod ts (wpopc); the
-    // phases are advanced by conditional subtraction, without a division in
-    // the loop.
-    const uint32_t c32 = 32 % ts;                                            // phase step per word
-    const uint32_t cstep = (uint32_t)(((unsigned long long)nth * 128) % ts);  // per grid step
-    uint32_t pv = (uint32_t)(((unsigned long long)vt * 128) % ts);
-    for (uint32_t v = vt; v < ntv; v += nth) {
-      uint4 d = *reinterpret_cast<const uint4 *>(tail + (size_t)v * 16);
-      const uint32_t *w = reinterpret_cast<const uint32_t *>(&d);
-      uint32_t ph = pv;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const unsigned long long b0 = (unsigned long long)v * 128 + 32 * q;
-        uint32_t word = w[q];
-        if (b0 >= tail_bits)
-          word = 0;
-        else if (b0 + 32 > tail_bits)
-          word &= (1u << (uint32_t)(tail_bits - b0)) - 1u;
-        acc += wpopc(word, ph, ts);
-        ph += c32;
-        if (ph >= ts) ph -= ts;
-      }
-      pv += cstep;
-      if (pv >= ts) pv -= ts;
+    unsigned long long acc = 0;
+    switch (ts) {
+      case 1: acc = tail_blocks_sum<1>(tail, tail_bits, vt, nth); break;
+      case 2: acc = tail_blocks_sum<2>(tail, tail_bits, vt, nth); break;
+      case 3: acc = tail_blocks_sum<3>(tail, tail_bits, vt, nth); break;
+      case 4: acc = tail_blocks_sum<4>(tail, tail_bits, vt, nth); break;
+      case 5: acc = tail_blocks_sum<5>(tail, tail_bits, vt, nth); break;
+      case 6: acc = tail_blocks_sum<6>(tail, tail_bits, vt, nth); break;
+      default: acc = tail_blocks_sum<7>(tail, tail_bits, vt, nth); break;
     }
     acc = warp_sum_ull(acc);
     if (lane == 0 && acc) atomicAdd(&s_acc[8], acc);
