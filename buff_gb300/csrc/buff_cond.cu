@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(kThreads) k_max_range_refine(WinArgs a,
   }
 }
 
-// Window maxima as values.  `shift` drops the right padding of a buff-slice// Window maxima as values.  `shift` drops the right padding of a buff-slice
+// Window maxima as values.  `shift` drops the right padding of a buff-slice
 // code; `empty` marks windows that read no row (f64::min_value()).
 __global__ void k_codes_to_values(const unsigned long long *codes, uint32_t n, long long base,
                                   int dlen, uint32_t shift, uint32_t empty_from, double *out) {
