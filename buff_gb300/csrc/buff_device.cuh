@@ -449,10 +449,13 @@ __device__ __forceinline__ double u53w_to_f64_scaled(uint32_t hi, uint32_t lo, i
 __device__ __forceinline__ double s53_to_f64_scaled(unsigned long long v, int dlen) {
   const unsigned long long sg = (unsigned long long)((long long)v >> 63);
   const unsigned long long m = (v ^ sg) - sg;
+  const uint32_t hi = (uint32_t)(m >> 32), lo = (uint32_t)m;
   uint32_t oh, ol;
-  u53w_bits((uint32_t)(m >> 32), (uint32_t)m, dlen, oh, ol);
-  oh |= (uint32_t)sg & 0x80000000u;
-  return m ? __hiloint2double((int)oh, (int)ol) : 0.0;
+  u53w_bits(hi, lo, dlen, oh, ol);
+  // m = 0 leaves the significand words 0 (the leading-one word is 0): only
+  // the exponent put into oh is cleared
+  oh = (hi | lo) ? (oh | ((uint32_t)sg & 0x80000000u)) : 0u;
+  return __hiloint2double((int)oh, (int)ol);
 }
 
 // The same for a value that fits in 32 bits: exact (|v| < 2^32 <= 2^53), so
